@@ -1,0 +1,188 @@
+/*
+ * piclas_gpu.h -- C-ABI of the GB300 (sm_103a) PIC particle loop.
+ *
+ * The entry points replace the argument-less Fortran routines of PICLas's
+ * Boris-Leapfrog particle loop.  A Fortran host binds them with ISO_C_BINDING
+ * (see INTEGRATION.md); every pointer is a plain host pointer to a contiguous
+ * array laid out exactly like the reference's Fortran array (column-major,
+ * first index fastest).  Index arrays are 1-based, as in the reference.
+ *
+ * Reference routines replaced (paths relative to the PICLas source tree):
+ *   pic_create             InitParticleMesh / InitializeDeposition / InitializeParticleInterpolation
+ *                          (src/particles/particle_mesh/particle_mesh.f90:141,
+ *                           src/particles/pic/deposition/pic_depo.f90:83,
+ *                           src/particles/pic/interpolation/pic_interpolation.f90:105)
+ *   pic_set_field          hand-over of U_N(e)%E(1:3,0:N,0:N,0:N) after HDG()
+ *                          (src/timedisc/timedisc_TimeStepPoissonByBorisLeapfrog.f90:99)
+ *   pic_upload_particles / pic_download_particles
+ *                          PartState(1:6,:), PEM%GlobalElemID, PartSpecies, PDM%ParticleInside,
+ *                          PDM%IsNewPart, PartPosRef (src/particles/particle_vars.f90:50-167)
+ *   pic_interpolate        InterpolateFieldToParticle (pic_interpolation.f90:248)
+ *   pic_push               LastPartPos/LastElem save + Boris push loop
+ *                          (timedisc_TimeStepPoissonByBorisLeapfrog.f90:109-198)
+ *   pic_track              PerformTracking (src/particles/tracking/particle_tracking.f90:32)
+ *   pic_deposit            Deposition (src/particles/pic/deposition/pic_depo.f90:944)
+ *   pic_step               TimeStepPoissonByBorisLeapfrog with the field frozen
+ *                          (timedisc_TimeStepPoissonByBorisLeapfrog.f90:32-286 minus HDG)
+ *   pic_get_status         NbrOfLostParticles and the abort conditions of the loop
+ *                          (particle_triatracking.f90:293-308, eval_xyz.f90:424-441)
+ *   pic_adjoint_run        no reference counterpart (differentiable loop, see its comment)
+ *
+ * Error convention: every int-returning call returns PIC_OK (0) or a positive
+ * pic_error_t.  The library never aborts the host process: where the reference
+ * calls abort(), the library records an error bit in the status word instead.
+ */
+#ifndef PICLAS_GPU_H
+#define PICLAS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes (return values) --------------------------------------- */
+typedef enum pic_error_t {
+  PIC_OK = 0,
+  PIC_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad size, unsupported option          */
+  PIC_ERR_CUDA = 2,              /* a CUDA runtime call failed (message in pic_last_error) */
+  PIC_ERR_OUT_OF_MEMORY = 3,     /* device allocation failed                             */
+  PIC_ERR_NO_DEVICE = 4,         /* no CUDA device visible                               */
+  PIC_ERR_STATE = 5,             /* call out of order (e.g. deposit before upload)       */
+  PIC_ERR_CAPACITY = 6           /* more particles than pic_config_t.max_particles       */
+} pic_error_t;
+
+/* ---- status bits (pic_status_t.error_word), set by device code ------------- */
+#define PIC_STATUS_LOST_PARTICLE   0x01u  /* TriaTracking found no side: particle removed  */
+#define PIC_STATUS_NEWTON_FAILED   0x02u  /* Newton left |xi|>1.5 (isSuccessful=.FALSE.)    */
+#define PIC_STATUS_HOP_LIMIT       0x04u  /* tracking walk exceeded its iteration cap      */
+#define PIC_STATUS_REF_TOLERANCE   0x08u  /* RefTracking: |xi| > epsOneCell (reference aborts) */
+#define PIC_STATUS_BAD_ELEMENT     0x10u  /* element index out of range in particle data   */
+#define PIC_STATUS_NOT_FINITE      0x20u  /* NaN/Inf position or velocity                  */
+
+/* ---- option enums ------------------------------------------------------- */
+enum { PIC_TRACK_TRIA = 1, PIC_TRACK_REFMAPPING = 2 };     /* TrackingMethod           */
+enum { PIC_DEPO_CVWM = 1, PIC_DEPO_SHAPE_FUNCTION = 2 };   /* PIC-Deposition-Type      */
+enum { PIC_PREC_FP64 = 0, PIC_PREC_MIXED = 1 };            /* arithmetic variant       */
+
+#define PIC_MAX_SPECIES 8
+
+/* Run-time options (the ini parameters the path reads). */
+typedef struct pic_config_t {
+  int32_t n_dg;                 /* N: DG polynomial degree (1..5)                       */
+  int32_t tracking;             /* PIC_TRACK_*                                          */
+  int32_t deposition;           /* PIC_DEPO_*                                           */
+  int32_t precision;            /* PIC_PREC_*                                           */
+  int32_t max_particles;        /* capacity of the device particle arrays               */
+  int32_t n_species;            /* 1..PIC_MAX_SPECIES                                   */
+  double  charge[PIC_MAX_SPECIES];   /* Species(s)%ChargeIC                            */
+  double  mass[PIC_MAX_SPECIES];     /* Species(s)%MassIC                              */
+  double  mpf[PIC_MAX_SPECIES];      /* Species(s)%MacroParticleFactor                 */
+  double  external_field[6];    /* PIC-externalField (Ex,Ey,Ez,Bx,By,Bz)                */
+  double  refmapping_eps;       /* RefMappingEps (default 1e-4)                         */
+  double  sf_radius;            /* PIC-shapefunction-radius                             */
+  int32_t sf_alpha;             /* PIC-shapefunction-alpha (>=2)                        */
+  int32_t sort_interval;        /* re-sort particles by element every k steps (0: never) */
+} pic_config_t;
+
+/* Mesh arrays as the reference holds them after init (NGeo = 1 hexahedra).
+ * Shapes are given in the reference's Fortran notation; memory is column-major. */
+typedef struct pic_mesh_t {
+  int32_t n_elems;              /* nElems                                               */
+  int32_t n_geo;                /* NGeo (must be 1)                                     */
+  int32_t n_nodes;              /* nUniqueGlobalNodes (periodic copies are distinct)    */
+  int32_t n_periodic_vectors;   /* GEO%nPeriodicVectors (0..3)                          */
+  double  periodic_vectors[9];  /* GEO%PeriodicVectors(1:3,1:3)                         */
+  double  xmin_glob[3], xmax_glob[3];  /* GEO%x/y/zminglob, x/y/zmaxglob                */
+  /* reference-element data */
+  const double* xi_cl_ngeo;     /* XiCL_NGeo(0:NGeo)                                    */
+  const double* wbary_cl_ngeo;  /* wBaryCL_NGeo(0:NGeo)                                 */
+  const double* xgp;            /* N_Inter(N)%xGP(0:N)  Gauss nodes                     */
+  const double* wgp;            /* N_Inter(N)%wGP(0:N)                                  */
+  const double* wbary_gp;       /* N_Inter(N)%wBary(0:N)                                */
+  /* element geometry */
+  const double* xcl_ngeo;       /* XCL_NGeo(1:3,0:NGeo,0:NGeo,0:NGeo,nElems)             */
+  const double* dxcl_ngeo;      /* dXCL_NGeo(1:3,1:3,0:NGeo,0:NGeo,0:NGeo,nElems)        */
+  const double* elem_bary;      /* ElemBaryNGeo(1:3,nElems)                             */
+  const double* xez_basis;      /* XiEtaZetaBasis(1:3,1:6,nElems)                       */
+  const double* slen_basis;     /* slenXiEtaZetaBasis(1:6,nElems)                       */
+  const double* elem_radius;    /* ElemRadiusNGeo(nElems)                               */
+  const double* eps_one_cell;   /* ElemEpsOneCell(nElems)                               */
+  const double* elem_xgp;       /* Elem_xGP_Shared(1:3,(N+1)^3*nElems)                  */
+  const double* elem_sj;        /* ElemsJ((N+1)^3*nElems)                               */
+  /* linear-element connectivity (TriaTracking) */
+  const double* node_coords;    /* NodeCoords_Shared(1:3,8*nElems): corners, tensor order */
+  const int32_t* elem_node;     /* ElemNodeID_Shared(1:8,nElems): CGNS corner order, 1-based into node_coords */
+  const int32_t* elem_side_node;/* ElemSideNodeID_Shared(1:4,1:6,nElems)+1, 1-based into node_coords */
+  const int32_t* side_nb_elem;  /* SideInfo_Shared(SIDE_NBELEMID) per (1:6,nElems), 1-based */
+  const int32_t* side_pvid;     /* BoundaryType(SIDE_BCID,BC_ALPHA) per (1:6,nElems): 0 inner, +-k periodic */
+  const int32_t* concave_side;  /* ConcaveElemSide_Shared(1:6,nElems) as 0/1             */
+  /* cell_volweight_mean */
+  const int32_t* node_info;     /* NodeInfo_Shared(ElemNodeID(1:8,e)) per (1:8,nElems): unique node, 1-based */
+  const double* node_volume;    /* NodeVolume(nUniqueGlobalNodes)                       */
+  const int32_t* periodic_n_nodes;   /* Periodic_nNodes(nUniqueGlobalNodes)            */
+  const int32_t* periodic_offset;    /* Periodic_offsetNode(nUniqueGlobalNodes)        */
+  const int32_t* periodic_nodes;     /* Periodic_Nodes(nTotalPeriodicNodes), 1-based    */
+  int32_t n_total_periodic_nodes;
+  /* Fast-Init background mesh (RefTracking candidates, shape-function search) */
+  int32_t fibgm_imax[3];        /* FIBGMimax/jmax/kmax (imin=jmin=kmin=1)               */
+  double  fibgm_deltas[3];      /* GEO%FIBGMdeltas                                      */
+  const int32_t* fibgm_n_elems; /* FIBGM_nElems(i,j,k)                                  */
+  const int32_t* fibgm_offset;  /* FIBGM_offsetElem(i,j,k)                              */
+  const int32_t* fibgm_element; /* FIBGM_Element(:), 1-based                            */
+  int32_t fibgm_n_total;
+} pic_mesh_t;
+
+typedef struct pic_status_t {
+  uint32_t error_word;          /* OR of PIC_STATUS_* seen since the last reset         */
+  int32_t  n_lost;              /* NbrOfLostParticles                                   */
+  int32_t  n_inside;            /* particles with PDM%ParticleInside                    */
+  int32_t  n_newton_failed;     /* Newton calls that returned isSuccessful=.FALSE.      */
+  int64_t  n_steps;             /* steps taken by pic_step/pic_push since create        */
+} pic_status_t;
+
+typedef struct pic_ctx pic_ctx_t;
+
+/* Library / device ---------------------------------------------------------- */
+const char* pic_version(void);
+const char* pic_last_error(void);          /* message of the last failed call (thread-local) */
+
+/* Context ------------------------------------------------------------------- */
+int  pic_create(const pic_config_t* cfg, const pic_mesh_t* mesh, pic_ctx_t** ctx_out);
+void pic_destroy(pic_ctx_t* ctx);
+
+/* Field: U_N(e)%E(1:3,0:N,0:N,0:N) for e=1..nElems, contiguous (3*(N+1)^3*nElems doubles). */
+int pic_set_field(pic_ctx_t* ctx, const double* e_dof, int32_t n_elems);
+
+/* Particles: part_state is PartState(1:6,1:n); elem is PEM%GlobalElemID (1-based);
+ * species is PartSpecies (1-based); inside / is_new are PDM%ParticleInside / PDM%IsNewPart. */
+int pic_upload_particles(pic_ctx_t* ctx, const double* part_state, const int32_t* elem,
+                         const int32_t* species, const uint8_t* inside, const uint8_t* is_new,
+                         int32_t n);
+/* Same arrays back in the caller's particle order.  part_pos_ref (PartPosRef(1:3,n)) may be NULL. */
+int pic_download_particles(pic_ctx_t* ctx, double* part_state, int32_t* elem, uint8_t* inside,
+                           uint8_t* is_new, double* part_pos_ref, int32_t n);
+
+/* Loop pieces in reference order.  pic_push also saves LastPartPos/LastElem. */
+int pic_interpolate(pic_ctx_t* ctx);
+int pic_push(pic_ctx_t* ctx, double dt);
+int pic_track(pic_ctx_t* ctx);
+/* Deposition on the current particle state.  part_source is PS_N(e)%PartSource(1:4,0:N,0:N,0:N)
+ * for all elements (4*(N+1)^3*nElems doubles); NULL keeps the result on the device. */
+int pic_deposit(pic_ctx_t* ctx, double* part_source);
+/* FieldAtParticle(1:6,1:n) of the last pic_interpolate / pic_step, caller's particle order. */
+int pic_get_field_at_particles(pic_ctx_t* ctx, double* field, int32_t n);
+
+/* nsteps x {Deposition, InterpolateFieldToParticle, push, PerformTracking} with the field frozen.
+ * part_source (may be NULL) receives the deposition of the last step. */
+int pic_step(pic_ctx_t* ctx, double dt, int32_t nsteps, double* part_source);
+
+int pic_get_status(pic_ctx_t* ctx, pic_status_t* status);
+int pic_reset_status(pic_ctx_t* ctx);
+/* Block the host until all work queued on the context's stream has finished. */
+int pic_synchronize(pic_ctx_t* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PICLAS_GPU_H */

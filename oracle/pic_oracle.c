@@ -1,0 +1,928 @@
+/*
+ * pic_oracle.c -- CPU restatement of PICLas's Boris-Leapfrog PIC particle loop.
+ *
+ * TEST INFRASTRUCTURE ONLY: the oracle that tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py check the GPU library against.  The product never calls it.
+ *
+ * Each routine follows the cited reference Fortran (paths relative to the PICLas source
+ * tree) statement by statement, in the same floating-point evaluation order.  It is built
+ * with -ffp-contract=off so that no multiply-add is fused.  1-based indices as in Fortran.
+ *
+ * Scope restated: NGeo = 1 hexahedra, conforming (no mortar) fully periodic meshes,
+ * PP_nVar = 1 (Poisson/HDG) with Boris-Leapfrog (PP_TimeDiscMethod = 508), non-relativistic
+ * PartRHS, external field = constant PIC-externalField, CVWM and 3D shape_function
+ * deposition, TriaTracking, and RefTracking with CartesianPeriodic = FastPeriodic = T.
+ */
+#include "pic_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static const double EPS_MACH = 2.220446049250313080847e-16;  /* EPSILON(0.0d0) */
+static const double C_LIGHT = 299792458.0;                   /* globals_vars.f90:85 */
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Lagrange basis (basis.f90)
+ * ------------------------------------------------------------------------------------- */
+/* ALMOSTEQUAL_UNITY, basis.f90:1011-1035 */
+static int almost_equal_unity(double x, double y) {
+  if (x == 0.0 || y == 0.0) return fabs(x - y) <= 2.0 * EPS_MACH;
+  return (fabs(x - y) <= EPS_MACH * fabs(x)) && (fabs(x - y) <= EPS_MACH * fabs(y));
+}
+
+/* LagrangeInterpolationPolys, basis.f90:1223-1264 */
+void orc_lagrange_polys(double x, int n, const double* xgp, const double* wbary, double* L) {
+  int hit = 0;
+  for (int i = 0; i <= n; ++i) {
+    L[i] = 0.0;
+    if (almost_equal_unity(x, xgp[i])) { L[i] = 1.0; hit = 1; }
+  }
+  if (hit) return;
+  double s = 0.0;
+  for (int i = 0; i <= n; ++i) { L[i] = wbary[i] / (x - xgp[i]); s = s + L[i]; }
+  for (int i = 0; i <= n; ++i) L[i] = L[i] / s;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * mesh accessors (reference layouts, 1-based element ids)
+ * ------------------------------------------------------------------------------------- */
+#define XCL(m, c, i, j, k, e)      ((m)->xcl_ngeo[((((size_t)((e) - 1) * 2 + (k)) * 2 + (j)) * 2 + (i)) * 3 + (c)])
+#define DXCL(m, dd, nn, i, j, k, e) \
+  ((m)->dxcl_ngeo[(((((size_t)((e) - 1) * 2 + (k)) * 2 + (j)) * 2 + (i)) * 3 + (nn)) * 3 + (dd)])
+#define NODE(m, c, n)              ((m)->node_coords[((size_t)(n) - 1) * 3 + (c)])
+#define SIDENODE(m, q, s, e)       ((m)->elem_side_node[((size_t)((e) - 1) * 6 + (s)) * 4 + (q)])
+
+/* ---------------------------------------------------------------------------------------
+ * Reference mapping x -> xi (eval_xyz.f90)
+ * ------------------------------------------------------------------------------------- */
+/* GetRefNewtonStartValue, RefMappingGuess = 1, eval_xyz.f90:549-562 */
+static void ref_newton_start(const pic_config_t* cfg, const pic_mesh_t* m, const double x[3], double xi[3], int e) {
+  const double epsOne = 1.0 + cfg->refmapping_eps;
+  double Ptild[3], xil[6];
+  for (int c = 0; c < 3; ++c) Ptild[c] = x[c] - m->elem_bary[(size_t)(e - 1) * 3 + c];
+  for (int d = 0; d < 6; ++d) {
+    const double* b = &m->xez_basis[((size_t)(e - 1) * 6 + d) * 3];
+    double dp = Ptild[0] * b[0] + Ptild[1] * b[1] + Ptild[2] * b[2];
+    xil[d] = dp * m->slen_basis[(size_t)(e - 1) * 6 + d];
+  }
+  for (int d = 0; d < 3; ++d) xi[d] = 0.5 * (xil[d] - xil[d + 3]);
+  double mx = fmax(fabs(xi[0]), fmax(fabs(xi[1]), fabs(xi[2])));
+  if (mx > epsOne)
+    for (int d = 0; d < 3; ++d) xi[d] = fmax(fmin(1.0, xi[d]), -1.0);
+}
+
+/* F(xi) = x(xi) - x_in with F = F + XCL*Lag(1,i)*buff (eval_xyz.f90:342-350) */
+static void newton_residual_first(const pic_mesh_t* m, int e, const double Lag[3][2], const double x[3], double F[3]) {
+  for (int c = 0; c < 3; ++c) F[c] = -x[c];
+  for (int k = 0; k <= 1; ++k)
+    for (int j = 0; j <= 1; ++j) {
+      double buff = Lag[1][j] * Lag[2][k];
+      for (int i = 0; i <= 1; ++i)
+        for (int c = 0; c < 3; ++c) F[c] = F[c] + XCL(m, c, i, j, k, e) * Lag[0][i] * buff;
+    }
+}
+
+/* RefElemNewton, eval_xyz.f90:298-445 (N_In = NGeo = 1). Returns isSuccessful. */
+static int ref_elem_newton(const pic_config_t* cfg, const pic_mesh_t* m, double xi[3], const double x[3], int e) {
+  const double* xcl = m->xi_cl_ngeo;
+  const double* wb = m->wbary_cl_ngeo;
+  double Lag[3][2], F[3], xiOld[3], dxi[3], Jac[3][3], sJac[3][3];
+  int success = 1;
+  for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], 1, xcl, wb, Lag[d]);
+  newton_residual_first(m, e, (const double(*)[2])Lag, x, F);
+  double deltaXi2 = (fabs(F[0]) < EPS_MACH && fabs(F[1]) < EPS_MACH && fabs(F[2]) < EPS_MACH) ? 0.0 : 1.0;
+  double normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+  double normFold;
+  int iter = 0;
+  while (deltaXi2 > cfg->refmapping_eps && iter < 100) {
+    iter = iter + 1;
+    for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) Jac[a][b] = 0.0;
+    for (int k = 0; k <= 1; ++k)
+      for (int j = 0; j <= 1; ++j) {
+        double buff = Lag[1][j] * Lag[2][k];
+        for (int i = 0; i <= 1; ++i) {
+          double buff2 = Lag[0][i] * buff;
+          for (int nn = 0; nn < 3; ++nn)
+            for (int dd = 0; dd < 3; ++dd) Jac[nn][dd] = Jac[nn][dd] + DXCL(m, dd, nn, i, j, k, e) * buff2;
+        }
+      }
+    /* getDet, eval_xyz.f90:464-466 */
+    double sdet = (Jac[0][0] * Jac[1][1] - Jac[0][1] * Jac[1][0]) * Jac[2][2]
+                + (Jac[0][1] * Jac[1][2] - Jac[0][2] * Jac[1][1]) * Jac[2][0]
+                + (Jac[0][2] * Jac[1][0] - Jac[0][0] * Jac[1][2]) * Jac[2][1];
+    if (sdet > 0.0) sdet = 1.0 / sdet;
+    /* getInv, eval_xyz.f90:486-494 */
+    sJac[0][0] = (Jac[1][1] * Jac[2][2] - Jac[1][2] * Jac[2][1]) * sdet;
+    sJac[0][1] = (Jac[0][2] * Jac[2][1] - Jac[0][1] * Jac[2][2]) * sdet;
+    sJac[0][2] = (Jac[0][1] * Jac[1][2] - Jac[0][2] * Jac[1][1]) * sdet;
+    sJac[1][0] = (Jac[1][2] * Jac[2][0] - Jac[1][0] * Jac[2][2]) * sdet;
+    sJac[1][1] = (Jac[0][0] * Jac[2][2] - Jac[0][2] * Jac[2][0]) * sdet;
+    sJac[1][2] = (Jac[0][2] * Jac[1][0] - Jac[0][0] * Jac[1][2]) * sdet;
+    sJac[2][0] = (Jac[1][0] * Jac[2][1] - Jac[1][1] * Jac[2][0]) * sdet;
+    sJac[2][1] = (Jac[0][1] * Jac[2][0] - Jac[0][0] * Jac[2][1]) * sdet;
+    sJac[2][2] = (Jac[0][0] * Jac[1][1] - Jac[0][1] * Jac[1][0]) * sdet;
+    for (int r = 0; r < 3; ++r) dxi[r] = ((0.0 + sJac[r][0] * F[0]) + sJac[r][1] * F[1]) + sJac[r][2] * F[2];
+    deltaXi2 = dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2];
+    for (int d = 0; d < 3; ++d) xiOld[d] = xi[d];
+    normFold = normF;
+    normF = normF * 2.0;
+    double lambda = 1.0;
+    int iArmijo = 1;
+    while (normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8) {
+      for (int d = 0; d < 3; ++d) xi[d] = xiOld[d] - lambda * dxi[d];
+      for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], 1, xcl, wb, Lag[d]);
+      for (int c = 0; c < 3; ++c) F[c] = -x[c];
+      for (int k = 0; k <= 1; ++k)
+        for (int j = 0; j <= 1; ++j) {
+          double buff = Lag[1][j] * Lag[2][k];
+          for (int i = 0; i <= 1; ++i) {
+            double buff2 = Lag[0][i] * buff;
+            for (int c = 0; c < 3; ++c) F[c] = F[c] + XCL(m, c, i, j, k, e) * buff2;
+          }
+        }
+      lambda = 0.2 * lambda;
+      iArmijo = iArmijo + 1;
+      normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+    }
+    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = 0; break; }
+  }
+  return success;
+}
+
+/* GetPositionInRefElem, eval_xyz.f90:35-123 (NGeo = 1 branch).  Without isSuccessful the
+ * reference exits the Newton loop silently in Mode 2 (the only mode used on this path without
+ * isSuccessful); the success flag is still returned here for bookkeeping. */
+int orc_get_position_in_ref_elem(const pic_config_t* cfg, const pic_mesh_t* m, const double x[3], double xi[3],
+                                 int elem, int want_success) {
+  (void)want_success;
+  ref_newton_start(cfg, m, x, xi, elem);
+  return ref_elem_newton(cfg, m, xi, x, elem);
+}
+
+/* EvaluateFieldAtRefPos, eval_xyz.f90:167-215 with NVar_IN = 3 */
+void orc_evaluate_field_at_ref_pos(const double xi[3], int N, const double* xgp, const double* wbary, const double* U,
+                                   double out[3]) {
+  double L[3][8];
+  for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], N, xgp, wbary, L[d]);
+  out[0] = out[1] = out[2] = 0.0;
+  const int n1 = N + 1;
+  for (int k = 0; k <= N; ++k)
+    for (int j = 0; j <= N; ++j) {
+      double Lez = L[1][j] * L[2][k];
+      for (int i = 0; i <= N; ++i) {
+        const double* u = &U[((size_t)(k * n1 + j) * n1 + i) * 3];
+        for (int c = 0; c < 3; ++c) out[c] = out[c] + u[c] * L[0][i] * Lez;
+      }
+    }
+}
+
+/* GetEMFieldDW, pic_interpolation_tools.f90:458-527 (components 1:3) */
+static void get_em_field_dw(const pic_mesh_t* m, int N, int e, const double* Ue, const double x[3], double out[3]) {
+  const int n1 = N + 1, ndof = n1 * n1 * n1;
+  double dist[512];
+  for (int r = 0; r < ndof; ++r) dist[r] = 0.0;
+  double DistSum = 0.0;
+  /* DO k; DO l; DO m with Elem_xGP(1:3,k,l,m): k is the first (fastest) array index */
+  for (int k = 0; k <= N; ++k)
+    for (int l = 0; l <= N; ++l)
+      for (int mm = 0; mm <= N; ++mm) {
+        int r = k + n1 * (l + n1 * mm);
+        const double* xg = &m->elem_xgp[((size_t)(e - 1) * ndof + r) * 3];
+        double v0 = xg[0] - x[0], v1 = xg[1] - x[1], v2 = xg[2] - x[2];
+        double norm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+        if (norm > 0.0) {
+          dist[r] = 1.0 / norm;
+        } else {
+          for (int q = 0; q < ndof; ++q) dist[q] = 0.0;
+          dist[r] = 1.0;
+          DistSum = 1.0;
+          break; /* EXIT leaves the innermost (m) loop only */
+        }
+        DistSum = DistSum + dist[r];
+      }
+  out[0] = out[1] = out[2] = 0.0;
+  for (int k = 0; k <= N; ++k)
+    for (int l = 0; l <= N; ++l)
+      for (int mm = 0; mm <= N; ++mm) {
+        int r = k + n1 * (l + n1 * mm);
+        for (int c = 0; c < 3; ++c) out[c] = out[c] + dist[r] / DistSum * Ue[(size_t)r * 3 + c];
+      }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * InterpolateFieldToParticle, pic_interpolation.f90:248-369 + tools:54-115,198-254,399-455
+ * ------------------------------------------------------------------------------------- */
+static void interpolate_single(const pic_config_t* cfg, const pic_mesh_t* m, const double* e_dof, orc_particles_t* p,
+                               int ip, int64_t* nfail) {
+  const int N = cfg->n_dg, ndof = (N + 1) * (N + 1) * (N + 1);
+  double* F = &p->field[(size_t)ip * 6];
+  const double* x = &p->part_state[(size_t)ip * 6];
+  const int e = p->elem[ip];
+  for (int c = 0; c < 6; ++c) F[c] = cfg->external_field[c];     /* GetExternalFieldAtParticle */
+  double xi[3];
+  int suc = 1;
+  if (cfg->tracking != PIC_TRACK_REFMAPPING) {
+    suc = orc_get_position_in_ref_elem(cfg, m, x, xi, e, 1);
+    if (!suc) (*nfail)++;
+  } else {
+    for (int d = 0; d < 3; ++d) xi[d] = p->part_pos_ref[(size_t)ip * 3 + d];
+  }
+  double Eo[3];
+  const double* Ue = &e_dof[(size_t)(e - 1) * ndof * 3];
+  if (!suc && cfg->deposition == PIC_DEPO_CVWM)
+    get_em_field_dw(m, N, e, Ue, x, Eo);
+  else
+    orc_evaluate_field_at_ref_pos(xi, N, m->xgp, m->wbary_gp, Ue, Eo);
+  for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
+  /* components 4:6 of GetEMField are zero for PP_nVar = 1 */
+  for (int c = 3; c < 6; ++c) F[c] = F[c] + 0.0;
+}
+
+int orc_interpolate(const pic_config_t* cfg, const pic_mesh_t* m, const double* e_dof, orc_particles_t* p,
+                    orc_counters_t* c, int nthreads) {
+  int64_t nfail = 0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) reduction(+ : nfail) schedule(static)
+#endif
+  for (int ip = 0; ip < p->n; ++ip) {
+    if (!p->inside[ip]) continue;
+    if (cfg->charge[p->species[ip] - 1] == 0.0) continue;   /* isInterpolateParticle */
+    interpolate_single(cfg, m, e_dof, p, ip, &nfail);
+  }
+  (void)nthreads;
+  if (c) c->n_newton_failed += nfail;
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Boris-Leapfrog push, timedisc_TimeStepPoissonByBorisLeapfrog.f90:109-198
+ * ------------------------------------------------------------------------------------- */
+static void push_single(const pic_config_t* cfg, orc_particles_t* p, int ip, double dt, double c2_inv) {
+  double* s = &p->part_state[(size_t)ip * 6];
+  const double* F = &p->field[(size_t)ip * 6];
+  const int sp = p->species[ip] - 1;
+  const double q = cfg->charge[sp], mass = cfg->mass[sp];
+  const double dtVar = dt, dtFrac = dtVar;
+  const int push = fabs(q) > 0.0;               /* isPushParticle */
+  if (p->is_new[ip]) {
+    if (push) {
+      /* CalcPartRHSSingleParticle -> PartRHS_NR, particle_rhs.f90:232-247 */
+      double qmt = q / mass;
+      double Pt[3] = {F[0] * qmt, F[1] * qmt, F[2] * qmt};
+      for (int c = 0; c < 3; ++c) s[3 + c] = s[3 + c] - Pt[c] * dtVar * 0.5;
+    }
+    p->is_new[ip] = 0;
+  }
+  if (push) {
+    double c1 = (q * dtFrac) / (mass * 2.0);
+    double vv = s[3] * s[3] + s[4] * s[4] + s[5] * s[5];
+    double gamma = 1.0 / sqrt(1.0 - (vv * c2_inv));
+    double vmo[3], vm[3], t[3], vp[3], vpl[3], vn1[3];
+    for (int c = 0; c < 3; ++c) vmo[c] = s[3 + c] * gamma;
+    for (int c = 0; c < 3; ++c) vm[c] = vmo[c] + c1 * F[c];
+    double gm = sqrt(1.0 + (vm[0] * vm[0] + vm[1] * vm[1] + vm[2] * vm[2]) * c2_inv);
+    const double* B = &F[3];
+    double Bn = sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+    double tn = tan(c1 / gm * Bn);
+    double u[3] = {0.0, 0.0, 0.0};                                 /* UNITVECTOR, globals.f90:916-940 */
+    if (fabs(Bn) > 0.0) { double invL = 1.0 / Bn; for (int c = 0; c < 3; ++c) u[c] = B[c] * invL; }
+    for (int c = 0; c < 3; ++c) t[c] = tn * u[c];
+    double cr[3] = {vm[1] * t[2] - vm[2] * t[1], vm[2] * t[0] - vm[0] * t[2], vm[0] * t[1] - vm[1] * t[0]};
+    for (int c = 0; c < 3; ++c) vp[c] = vm[c] + cr[c];
+    double fac = 2.0 / (1.0 + (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
+    double cr2[3] = {vp[1] * t[2] - vp[2] * t[1], vp[2] * t[0] - vp[0] * t[2], vp[0] * t[1] - vp[1] * t[0]};
+    for (int c = 0; c < 3; ++c) vpl[c] = vm[c] + fac * cr2[c];
+    for (int c = 0; c < 3; ++c) vn1[c] = vpl[c] + c1 * F[c];
+    double den = sqrt(1.0 + (vn1[0] * vn1[0] + vn1[1] * vn1[1] + vn1[2] * vn1[2]) * c2_inv);
+    for (int c = 0; c < 3; ++c) s[3 + c] = vn1[c] / den;
+  }
+  for (int c = 0; c < 3; ++c) s[c] = s[c] + s[3 + c] * dtFrac;
+}
+
+void orc_push(const pic_config_t* cfg, orc_particles_t* p, double dt, int nthreads) {
+  const double c2 = C_LIGHT * C_LIGHT;
+  const double c2_inv = 1.0 / c2;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
+#endif
+  for (int ip = 0; ip < p->n; ++ip) {
+    if (!p->inside[ip]) continue;
+    push_single(cfg, p, ip, dt, c2_inv);
+  }
+  (void)nthreads;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * TriaTracking (particle_triatracking.f90:137-484 and helpers)
+ * ------------------------------------------------------------------------------------- */
+/* ParticleInsideQuad3D, particle_mesh_tools.f90:78-222 (regular sides) */
+static int inside_quad3d(const pic_mesh_t* m, const double x[3], int e, double det[6][2]) {
+  int inElem = 1;
+  for (int s = 0; s < 6; ++s) {
+    double A[3][4];
+    for (int q = 0; q < 4; ++q) {
+      int nid = SIDENODE(m, q, s, e);
+      for (int c = 0; c < 3; ++c) A[c][q] = NODE(m, c, nid) - x[c];
+    }
+    double cp0 = A[1][0] * A[2][2] - A[2][0] * A[1][2];
+    double cp1 = A[2][0] * A[0][2] - A[0][0] * A[2][2];
+    double cp2 = A[0][0] * A[1][2] - A[1][0] * A[0][2];
+    double d1 = cp0 * A[0][1] + cp1 * A[1][1] + cp2 * A[2][1];
+    d1 = -d1;
+    double d2 = cp0 * A[0][3] + cp1 * A[1][3] + cp2 * A[2][3];
+    det[s][0] = d1;
+    det[s][1] = d2;
+    int neg = 0, pos = 0;
+    if (d1 < 0.0) neg = 1; else pos = 1;
+    if (d2 < 0.0) neg = 1; else pos = 1;
+    if (m->concave_side[(size_t)(e - 1) * 6 + s]) { if (!pos) inElem = 0; }
+    else { if (neg) inElem = 0; }
+  }
+  return inElem;
+}
+
+/* ParticleThroughSideCheck3DFast, particle_intersection.f90:167-280 (regular side) */
+static int through_side_check(const pic_mesh_t* m, const double P[3], const double V[3], int s, int e, int triNum) {
+  double Ax[3], Ay[3], Az[3];
+  int nid = SIDENODE(m, 0, s, e);
+  Ax[0] = NODE(m, 0, nid) - P[0]; Ay[0] = NODE(m, 1, nid) - P[1]; Az[0] = NODE(m, 2, nid) - P[2];
+  for (int n = 1; n <= 2; ++n) {
+    int q = n + triNum - 1;       /* NodeID = n + TriNum - 1 with n = 2,3 (1-based) */
+    nid = SIDENODE(m, q, s, e);
+    Ax[n] = NODE(m, 0, nid) - P[0]; Ay[n] = NODE(m, 1, nid) - P[1]; Az[n] = NODE(m, 2, nid) - P[2];
+  }
+  const double Vx = V[0], Vy = V[1], Vz = V[2];
+  double dc[3][3];
+  dc[0][0] = (Ay[0] * Vz - Az[0] * Vy) * Ax[2]; dc[0][1] = (Az[0] * Vx - Ax[0] * Vz) * Ay[2]; dc[0][2] = (Ax[0] * Vy - Ay[0] * Vx) * Az[2];
+  dc[1][0] = (Ay[1] * Vz - Az[1] * Vy) * Ax[0]; dc[1][1] = (Az[1] * Vx - Ax[1] * Vz) * Ay[0]; dc[1][2] = (Ax[1] * Vy - Ay[1] * Vx) * Az[0];
+  dc[2][0] = (Ay[2] * Vz - Az[2] * Vy) * Ax[1]; dc[2][1] = (Az[2] * Vx - Ax[2] * Vz) * Ay[1]; dc[2][2] = (Ax[2] * Vy - Ay[2] * Vx) * Az[1];
+  for (int r = 0; r < 3; ++r) {
+    double det = (dc[r][0] + dc[r][1]) + dc[r][2];
+    double mn = DBL_MAX;                                  /* MINVAL over an empty mask = HUGE */
+    for (int q = 0; q < 3; ++q) if (fabs(dc[r][q]) > 0.0 && fabs(dc[r][q]) < mn) mn = fabs(dc[r][q]);
+    double minComp = -EPS_MACH * mn;
+    if (!(det >= minComp)) return 0;
+  }
+  return 1;
+}
+
+/* ParticleThroughSideLastPosCheck, particle_intersection.f90:430-512 (regular side) */
+static int last_pos_check(const pic_mesh_t* m, const double Pl[3], int s, int e, int triNum, double* detOut) {
+  double NC[3][3], Ax[3], Ay[3], Az[3];
+  int nid = SIDENODE(m, 0, s, e);
+  for (int c = 0; c < 3; ++c) NC[c][0] = NODE(m, c, nid);
+  for (int iN = 1; iN <= 2; ++iN) {
+    nid = SIDENODE(m, iN + triNum - 1, s, e);
+    for (int c = 0; c < 3; ++c) NC[c][iN] = NODE(m, c, nid);
+  }
+  for (int q = 0; q < 3; ++q) { Ax[q] = NC[0][q] - Pl[0]; Ay[q] = NC[1][q] - Pl[1]; Az[q] = NC[2][q] - Pl[2]; }
+  double det = ((Ay[0] * Az[1] - Az[0] * Ay[1]) * Ax[2] + (Az[0] * Ax[1] - Ax[0] * Az[1]) * Ay[2] +
+                (Ax[0] * Ay[1] - Ay[0] * Ax[1]) * Az[2]);
+  *detOut = det;
+  return !((det < 0.0) || (det != det));
+}
+
+/* IntersectionWithWall, particle_intersection.f90:79-164 -> TrackInfo%alpha */
+static double intersection_with_wall(const pic_mesh_t* m, const double Pold[3], const double traj[3], int s, int e,
+                                     int triNum) {
+  int n0 = SIDENODE(m, 0, s, e);
+  double xN = NODE(m, 0, n0), yN = NODE(m, 1, n0), zN = NODE(m, 2, n0);
+  int n1 = SIDENODE(m, triNum, s, e), n2 = SIDENODE(m, triNum + 1, s, e);   /* Node1 = TriNum+1, Node2 = TriNum+2 */
+  double V1[3] = {NODE(m, 0, n1) - xN, NODE(m, 1, n1) - yN, NODE(m, 2, n1) - zN};
+  double V2[3] = {NODE(m, 0, n2) - xN, NODE(m, 1, n2) - yN, NODE(m, 2, n2) - zN};
+  double nx = V1[1] * V2[2] - V1[2] * V2[1];
+  double ny = V1[2] * V2[0] - V1[0] * V2[2];
+  double nz = V1[0] * V2[1] - V1[1] * V2[0];
+  double nVal = sqrt(nx * nx + ny * ny + nz * nz);
+  nx = nx / nVal; ny = ny / nVal; nz = nz / nVal;
+  double bx = Pold[0] - xN, by = Pold[1] - yN, bz = Pold[2] - zN;
+  double ax = bx - nx * (bx * nx + by * ny + bz * nz);
+  double ay = by - ny * (bx * nx + by * ny + bz * nz);
+  double az = bz - nz * (bx * nx + by * ny + bz * nz);
+  double dist = sqrt(((ay * bz - az * by) * (ay * bz - az * by) + (az * bx - ax * bz) * (az * bx - ax * bz) +
+                      (ax * by - ay * bx) * (ax * by - ay * bx)) / (ax * ax + ay * ay + az * az));
+  if (dist != dist) dist = sqrt(bx * bx + by * by + bz * bz);
+  double alpha = traj[0] * nx + traj[1] * ny + traj[2] * nz;
+  if (fabs(alpha) > 0.0) alpha = dist / alpha;
+  return alpha;
+}
+
+#define ORC_MAX_TRACK_LOOPS 10000
+
+/* SingleParticleTriaTracking3D, particle_triatracking.f90:137-484 */
+static void tria_track_single(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, int ip,
+                              int64_t* nlost, int64_t* nhop) {
+  (void)cfg;
+  double* x = &p->part_state[(size_t)ip * 6];
+  double* xl = &p->last_part_pos[(size_t)ip * 3];
+  int elem = p->last_elem[ip];
+  int doneLast[6][4];
+  memset(doneLast, 0, sizeof(doneLast));
+  for (int loop = 0;; ++loop) {
+    if (loop >= ORC_MAX_TRACK_LOOPS) { (*nhop)++; p->inside[ip] = 0; return; }
+    double det[6][2];
+    if (inside_quad3d(m, x, elem, det)) { p->elem[ip] = elem; return; }
+    int nThrough = 0, locS[6] = {0}, triT[6] = {0}, globS[6] = {0};
+    int sideID = 0, localSide = 0;
+    double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
+    double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+    if (fabs(len) > 0.0) for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+    for (int s = 0; s < 6; ++s) {
+      int gside = (elem - 1) * 6 + s + 1;   /* global (non-unique) side id */
+      for (int tri = 1; tri <= 2; ++tri) {
+        if (det[s][tri - 1] <= -0.0) {
+          if (through_side_check(m, xl, traj, s, elem, tri)) {
+            if (nThrough < 6) { locS[nThrough] = s; triT[nThrough] = tri; globS[nThrough] = gside; }
+            nThrough++;
+            sideID = gside; localSide = s;
+          }
+        }
+      }
+    }
+    int triNum = triT[0];
+    if (nThrough != 1) {
+      if (nThrough == 0) { (*nlost)++; p->inside[ip] = 0; return; }
+      int second = 0;
+      double minRatio = 0.0;
+      for (int ind2 = 0; ind2 < nThrough && ind2 < 6; ++ind2) {
+        int doCheck = 1;
+        for (int is = 1; is < 6; ++is)
+          if (doneLast[is][0] == elem && doneLast[is][3] == globS[ind2] && doneLast[is][2] == triT[ind2]) doCheck = 0;
+        if (!doCheck) continue;
+        double detM;
+        if (last_pos_check(m, xl, locS[ind2], elem, triT[ind2], &detM)) {
+          double dPP = det[locS[ind2]][triT[ind2] - 1];
+          if (detM == 0.0 && dPP == 0.0) continue;
+          if (detM == 0.0 && minRatio == 0.0) {
+            second++; sideID = globS[ind2]; localSide = locS[ind2]; triNum = triT[ind2];
+          } else {
+            if (detM == 0.0) continue;
+            double ratio = dPP / detM;
+            if (ratio < minRatio) {
+              minRatio = ratio; second++; sideID = globS[ind2]; localSide = locS[ind2]; triNum = triT[ind2];
+            }
+          }
+        }
+      }
+      if (second == 0) { (*nlost)++; p->inside[ip] = 0; return; }
+    }
+    const int pvid = m->side_pvid[(size_t)(elem - 1) * 6 + localSide];
+    const int nb = m->side_nb_elem[(size_t)(elem - 1) * 6 + localSide];
+    for (int q = 5; q >= 1; --q) for (int c = 0; c < 4; ++c) doneLast[q][c] = doneLast[q - 1][c];
+    doneLast[0][0] = elem; doneLast[0][1] = localSide; doneLast[0][2] = triNum; doneLast[0][3] = sideID;
+    if (pvid != 0) {
+      /* IntersectionWithWall + GetBoundaryInteraction -> PeriodicBoundary
+       * (particle_boundary_condition.f90:224-284) */
+      double alpha = intersection_with_wall(m, xl, traj, localSide, elem, triNum);
+      int k = abs(pvid) - 1;
+      double sgn = pvid > 0 ? 1.0 : -1.0;
+      for (int c = 0; c < 3; ++c) xl[c] = xl[c] + traj[c] * alpha;
+      for (int c = 0; c < 3; ++c) xl[c] = xl[c] + copysign(m->periodic_vectors[k * 3 + c], sgn);
+      for (int c = 0; c < 3; ++c) x[c] = xl[c] + (len - alpha) * traj[c];
+    }
+    elem = nb;
+  }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * RefTracking with CartesianPeriodic = FastPeriodic = T (particle_reftracking.f90:30-414, 697-985)
+ * ------------------------------------------------------------------------------------- */
+static void periodic_movement_fast(const pic_mesh_t* m, double x[3], double xl[3]) {
+  const double* mn = m->xmin_glob;
+  const double* mx = m->xmax_glob;
+  for (int d = 0; d < 3; ++d) {
+    int iPV = -1;
+    for (int k = 0; k < m->n_periodic_vectors; ++k) if (m->periodic_vectors[k * 3 + d] != 0.0) { iPV = k; break; }
+    if (iPV < 0) continue;   /* GEO%directions(d) = .FALSE. */
+    const double* pv = &m->periodic_vectors[iPV * 3];
+    if (x[d] > mx[d]) {
+      double n = ceil(fabs(x[d] - mx[d]) / fabs(pv[d]));
+      double mv[3] = {n * pv[0], n * pv[1], n * pv[2]};
+      if (pv[d] > 0.0) { for (int c = 0; c < 3; ++c) { x[c] = x[c] - mv[c]; xl[c] = xl[c] - mv[c]; } }
+      else { for (int c = 0; c < 3; ++c) { x[c] = x[c] + mv[c]; xl[c] = xl[c] + mv[c]; } }
+    }
+    if (x[d] < mn[d]) {
+      double n = ceil(fabs(x[d] - mn[d]) / fabs(pv[d]));
+      double mv[3] = {n * pv[0], n * pv[1], n * pv[2]};
+      if (pv[d] > 0.0) { for (int c = 0; c < 3; ++c) { x[c] = x[c] + mv[c]; xl[c] = xl[c] + mv[c]; } }
+      else { for (int c = 0; c < 3; ++c) { x[c] = x[c] - mv[c]; xl[c] = xl[c] - mv[c]; } }
+    }
+  }
+}
+
+static double maxabs3(const double v[3]) { return fmax(fabs(v[0]), fmax(fabs(v[1]), fabs(v[2]))); }
+
+static int almost_equal(double x, double y) { return fabs(x - y) <= fmax(fabs(x), fabs(y)) * 4.441e-16; }
+
+static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, int ip,
+                             int64_t* ntol) {
+  double* x = &p->part_state[(size_t)ip * 6];
+  double* xl = &p->last_part_pos[(size_t)ip * 3];
+  double* xi = &p->part_pos_ref[(size_t)ip * 3];
+  int elem = p->last_elem[ip];
+  /* no BC elements on a CartesianPeriodic box: PeriodicMovement until the position is stable */
+  if (m->n_periodic_vectors > 0) {
+    double lp[3] = {x[0], x[1], x[2]};
+    periodic_movement_fast(m, x, xl);
+    int guard = 0;
+    while ((!almost_equal(lp[0], x[0]) || !almost_equal(lp[1], x[1]) || !almost_equal(lp[2], x[2])) && guard < 16) {
+      lp[0] = x[0]; lp[1] = x[1]; lp[2] = x[2];
+      periodic_movement_fast(m, x, xl);
+      guard++;
+    }
+  }
+  orc_get_position_in_ref_elem(cfg, m, x, xi, elem, 0);
+  if (maxabs3(xi) < 1.0) { p->elem[ip] = elem; return; }
+  int oldElem = p->last_elem[ip];
+  int cell[3];
+  for (int d = 0; d < 3; ++d) {
+    int cc = (int)floor((x[d] - m->xmin_glob[d]) / m->fibgm_deltas[d]);
+    cc = (cc > 0 ? cc : 0) + 1;
+    cell[d] = cc < m->fibgm_imax[d] ? cc : m->fibgm_imax[d];
+  }
+  size_t cidx = (size_t)(cell[0] - 1) + (size_t)m->fibgm_imax[0] * ((cell[1] - 1) + (size_t)m->fibgm_imax[1] * (cell[2] - 1));
+  int nBGM = m->fibgm_n_elems[cidx];
+  int off = m->fibgm_offset[cidx];
+  double distv[256];
+  int list[256];
+  if (nBGM > 256) nBGM = 256;
+  if (nBGM > 1) {
+    for (int i = 0; i < nBGM; ++i) {
+      int e = m->fibgm_element[off + i];
+      list[i] = e;
+      if (e == oldElem) distv[i] = -DBL_MAX;
+      else {
+        const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
+        double d0 = x[0] - b[0], d1 = x[1] - b[1], d2 = x[2] - b[2];
+        distv[i] = (d0 * d0 + d1 * d1) + d2 * d2;
+        double r = m->elem_radius[e - 1];
+        if (distv[i] > r * r) distv[i] = -DBL_MAX;
+      }
+    }
+    /* InsertionSort, utils.f90:52-101 */
+    for (int i = 1; i < nBGM; ++i) {
+      int j = i - 1;
+      double tr = distv[i];
+      int ti = list[i];
+      while (j >= 0) {
+        if (distv[j] <= tr) break;
+        distv[j + 1] = distv[j]; list[j + 1] = list[j];
+        j--;
+      }
+      distv[j + 1] = tr; list[j + 1] = ti;
+    }
+  } else if (nBGM == 1) {
+    distv[0] = 0.0;
+    list[0] = m->fibgm_element[off];
+  }
+  double oldXi[3] = {xi[0], xi[1], xi[2]};
+  double newXi[3] = {DBL_MAX, DBL_MAX, DBL_MAX};
+  int newElem = -1;
+  for (int i = 0; i < nBGM; ++i) {
+    if (distv[i] == -DBL_MAX) continue;
+    int e = list[i];
+    orc_get_position_in_ref_elem(cfg, m, x, xi, e, 0);
+    if (maxabs3(xi) < 1.0) { p->elem[ip] = e; return; }
+    if (maxabs3(xi) < maxabs3(newXi)) { newXi[0] = xi[0]; newXi[1] = xi[1]; newXi[2] = xi[2]; newElem = e; }
+  }
+  if (maxabs3(oldXi) < maxabs3(newXi)) {
+    xi[0] = oldXi[0]; xi[1] = oldXi[1]; xi[2] = oldXi[2];
+    p->elem[ip] = oldElem;
+  } else {
+    xi[0] = newXi[0]; xi[1] = newXi[1]; xi[2] = newXi[2];
+    p->elem[ip] = newElem;
+  }
+  int te = p->elem[ip];
+  double epsElement = (te >= 1) ? m->eps_one_cell[te - 1] : 1.0;
+  if (te < 1 || maxabs3(xi) > epsElement) (*ntol)++;   /* the reference aborts here (internal element) */
+}
+
+void orc_track(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, orc_counters_t* c, int nthreads) {
+  int64_t nlost = 0, nhop = 0, ntol = 0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) reduction(+ : nlost, nhop, ntol) schedule(static)
+#endif
+  for (int ip = 0; ip < p->n; ++ip) {
+    if (!p->inside[ip]) continue;
+    if (cfg->tracking == PIC_TRACK_TRIA) {
+      if (p->last_elem[ip] == 0) continue;    /* particle_triatracking.f90:101 */
+      tria_track_single(cfg, m, p, ip, &nlost, &nhop);
+    } else {
+      ref_track_single(cfg, m, p, ip, &ntol);
+    }
+  }
+  (void)nthreads;
+  if (c) { c->n_lost += nlost; c->n_hop_limit += nhop; c->n_ref_tolerance += ntol; }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Deposition (pic_depo.f90:944-1025)
+ * ------------------------------------------------------------------------------------- */
+/* one particle's CVWM node scatter, pic_depo_method.f90:471-544 */
+static void cvwm_particle(const pic_config_t* cfg, const pic_mesh_t* m, const orc_particles_t* p, int ip,
+                          double* NS, int64_t* nfail) {
+  const double* s = &p->part_state[(size_t)ip * 6];
+  const int sp = p->species[ip] - 1, e = p->elem[ip];
+  double charge = cfg->charge[sp] * cfg->mpf[sp];
+  double xi[3];
+  int suc = orc_get_position_in_ref_elem(cfg, m, s, xi, e, 1);
+  if (!suc) (*nfail)++;
+  double TS[4] = {s[3] * charge, s[4] * charge, s[5] * charge, charge};
+  double w[8];
+  const int32_t* ni = &m->node_info[(size_t)(e - 1) * 8];
+  if (suc) {
+    double a1 = 0.5 * (xi[0] + 1.0), a2 = 0.5 * (xi[1] + 1.0), a3 = 0.5 * (xi[2] + 1.0);
+    w[0] = (1 - a1) * (1 - a2) * (1 - a3);
+    w[1] = (a1) * (1 - a2) * (1 - a3);
+    w[2] = (a1) * (a2) * (1 - a3);
+    w[3] = (1 - a1) * (a2) * (1 - a3);
+    w[4] = (1 - a1) * (1 - a2) * (a3);
+    w[5] = (a1) * (1 - a2) * (a3);
+    w[6] = (a1) * (a2) * (a3);
+    w[7] = (1 - a1) * (a2) * (a3);
+    for (int iN = 0; iN < 8; ++iN) {
+      int node = ni[iN];
+      for (int v = 0; v < 4; ++v) NS[(size_t)(node - 1) * 4 + v] = NS[(size_t)(node - 1) * 4 + v] + (TS[v] * w[iN]);
+      if (m->n_periodic_vectors > 0 && m->periodic_n_nodes[node - 1] > 0) {
+        int o = m->periodic_offset[node - 1];
+        for (int j = 0; j < m->periodic_n_nodes[node - 1]; ++j) {
+          int tw = m->periodic_nodes[o + j];
+          for (int v = 0; v < 4; ++v) NS[(size_t)(tw - 1) * 4 + v] = NS[(size_t)(tw - 1) * 4 + v] + (TS[v] * w[iN]);
+        }
+      }
+    }
+  } else {
+    const int32_t* en = &m->elem_node[(size_t)(e - 1) * 8];
+    for (int iN = 0; iN < 8; ++iN) {
+      double v0 = NODE(m, 0, en[iN]) - s[0], v1 = NODE(m, 1, en[iN]) - s[1], v2 = NODE(m, 2, en[iN]) - s[2];
+      double norm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+      if (norm > 0.0) w[iN] = 1.0 / norm;
+      else { for (int q = 0; q < 8; ++q) w[q] = 0.0; w[iN] = 1.0; break; }
+    }
+    double DistSum = 0.0;
+    for (int iN = 0; iN < 8; ++iN) DistSum = DistSum + w[iN];
+    for (int iN = 0; iN < 8; ++iN) {
+      int node = ni[iN];
+      for (int v = 0; v < 4; ++v) NS[(size_t)(node - 1) * 4 + v] = NS[(size_t)(node - 1) * 4 + v] + w[iN] / DistSum * TS[v];
+      if (m->n_periodic_vectors > 0 && m->periodic_n_nodes[node - 1] > 0) {
+        int o = m->periodic_offset[node - 1];
+        for (int j = 0; j < m->periodic_n_nodes[node - 1]; ++j) {
+          int tw = m->periodic_nodes[o + j];
+          for (int v = 0; v < 4; ++v) NS[(size_t)(tw - 1) * 4 + v] = NS[(size_t)(tw - 1) * 4 + v] + w[iN] / DistSum * TS[v];
+        }
+      }
+    }
+  }
+}
+
+/* DepositionMethod_CVWM, pic_depo_method.f90:373-744 */
+static int deposit_cvwm(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* PS, orc_counters_t* c,
+                        int nthreads) {
+  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const size_t nn = (size_t)m->n_nodes * 4;
+  int nt = nthreads > 0 ? nthreads : 1;
+  double* NS = (double*)calloc(nn * (size_t)nt, sizeof(double));
+  if (!NS) return 1;
+  int64_t nfail = 0;
+  if (nt == 1) {
+    for (int ip = 0; ip < p->n; ++ip) {
+      if (!p->inside[ip]) continue;
+      if (cfg->charge[p->species[ip] - 1] == 0.0) continue;    /* isDepositParticle */
+      cvwm_particle(cfg, m, p, ip, NS, &nfail);
+    }
+  } else {
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt) reduction(+ : nfail)
+    {
+      double* my = NS + nn * (size_t)omp_get_thread_num();
+#pragma omp for schedule(static)
+      for (int ip = 0; ip < p->n; ++ip) {
+        if (!p->inside[ip]) continue;
+        if (cfg->charge[p->species[ip] - 1] == 0.0) continue;
+        cvwm_particle(cfg, m, p, ip, my, &nfail);
+      }
+    }
+    for (int t = 1; t < nt; ++t)
+      for (size_t q = 0; q < nn; ++q) NS[q] = NS[q] + NS[nn * (size_t)t + q];
+#endif
+  }
+  for (int node = 0; node < m->n_nodes; ++node) {                    /* :692-695 */
+    double V = m->node_volume[node];
+    if (V > 0.0) for (int v = 0; v < 4; ++v) NS[(size_t)node * 4 + v] = NS[(size_t)node * 4 + v] / V;
+  }
+  double Fac[8];
+  for (int i = 0; i <= N; ++i) Fac[i] = (m->xgp[i] + 1.0) / 2.0;     /* pic_depo.f90:274-275 */
+  for (int e = 1; e <= m->n_elems; ++e) {                            /* :710-733 */
+    const int32_t* ni = &m->node_info[(size_t)(e - 1) * 8];
+    double* ps = &PS[(size_t)(e - 1) * ndof * 4];
+    for (int kk = 0; kk <= N; ++kk)
+      for (int ll = 0; ll <= N; ++ll)
+        for (int mm = 0; mm <= N; ++mm) {
+          double a1 = Fac[kk], a2 = Fac[ll], a3 = Fac[mm];
+          int r = kk + n1 * (ll + n1 * mm);
+          for (int v = 0; v < 4; ++v) {
+            const double* S = NS + v;
+            ps[(size_t)r * 4 + v] =
+                S[(size_t)(ni[0] - 1) * 4] * (1 - a1) * (1 - a2) * (1 - a3) +
+                S[(size_t)(ni[1] - 1) * 4] * (a1) * (1 - a2) * (1 - a3) +
+                S[(size_t)(ni[2] - 1) * 4] * (a1) * (a2) * (1 - a3) +
+                S[(size_t)(ni[3] - 1) * 4] * (1 - a1) * (a2) * (1 - a3) +
+                S[(size_t)(ni[4] - 1) * 4] * (1 - a1) * (1 - a2) * (a3) +
+                S[(size_t)(ni[5] - 1) * 4] * (a1) * (1 - a2) * (a3) +
+                S[(size_t)(ni[6] - 1) * 4] * (a1) * (a2) * (a3) +
+                S[(size_t)(ni[7] - 1) * 4] * (1 - a1) * (a2) * (a3);
+          }
+        }
+  }
+  free(NS);
+  if (c) c->n_newton_failed += nfail;
+  return 0;
+}
+
+/* w_sf for the 3D shape function, pic_depo_shapefunction_tools.f90:1243-1246 with beta()
+ * from pic_depo_tools.f90:491-511 */
+static double sf_w(double r_sf, int alpha) {
+  const double PI = acos(-1.0);
+  double BetaFac = tgamma(1.5) * tgamma((double)alpha + 1.0) / tgamma(1.5 + ((double)alpha + 1.0));
+  return 1.0 / (2.0 * BetaFac * (double)alpha + 2.0 * BetaFac) * ((double)alpha + 1.0) / (PI * (r_sf * r_sf * r_sf));
+}
+
+/* depoChargeOnDOFsSF, pic_depo_shapefunction_tools.f90:292-422 (dim_sf = 3) */
+static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], const double Fac[4],
+                                   double r_sf, double r2_sf, double r2_sf_inv, double* PS, uint8_t* done) {
+  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  memset(done, 0, (size_t)m->n_elems);
+  int kmax = (int)ceil((P[0] + r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0]);
+  int kmin = (int)floor((P[0] - r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0] + 1);
+  int lmax = (int)ceil((P[1] + r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1]);
+  int lmin = (int)floor((P[1] - r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1] + 1);
+  int mmax = (int)ceil((P[2] + r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2]);
+  int mmin = (int)floor((P[2] - r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2] + 1);
+  if (kmax > m->fibgm_imax[0]) kmax = m->fibgm_imax[0];
+  if (kmin < 1) kmin = 1;
+  if (lmax > m->fibgm_imax[1]) lmax = m->fibgm_imax[1];
+  if (lmin < 1) lmin = 1;
+  if (mmax > m->fibgm_imax[2]) mmax = m->fibgm_imax[2];
+  if (mmin < 1) mmin = 1;
+  for (int kk = kmin; kk <= kmax; ++kk)
+    for (int ll = lmin; ll <= lmax; ++ll)
+      for (int mm = mmin; mm <= mmax; ++mm) {
+        size_t cidx = (size_t)(kk - 1) + (size_t)m->fibgm_imax[0] * ((ll - 1) + (size_t)m->fibgm_imax[1] * (mm - 1));
+        int nE = m->fibgm_n_elems[cidx], off = m->fibgm_offset[cidx];
+        for (int q = 0; q < nE; ++q) {
+          int e = m->fibgm_element[off + q];
+          if (done[e - 1]) continue;
+          const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
+          double v0 = P[0] - b[0], v1 = P[1] - b[1], v2 = P[2] - b[2];
+          if (sqrt(v0 * v0 + v1 * v1 + v2 * v2) > (r_sf + m->elem_radius[e - 1])) continue;
+          const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
+          double* ps = &PS[(size_t)(e - 1) * ndof * 4];
+          for (int mz = 0; mz <= N; ++mz)
+            for (int l = 0; l <= N; ++l)
+              for (int k = 0; k <= N; ++k) {
+                int r = mz * n1 * n1 + l * n1 + k;
+                double d0 = P[0] - xg[(size_t)r * 3], d1 = P[1] - xg[(size_t)r * 3 + 1], d2 = P[2] - xg[(size_t)r * 3 + 2];
+                double radius2 = (d0 * d0 + d1 * d1) + d2 * d2;
+                if (radius2 <= r2_sf) {
+                  double S = 1.0 - r2_sf_inv * radius2;
+                  double S1 = S * S;
+                  for (int ex = 3; ex <= cfg->sf_alpha; ++ex) S1 = S * S1;
+                  for (int v = 0; v < 4; ++v) ps[(size_t)r * 4 + v] = ps[(size_t)r * 4 + v] + S1 * Fac[v];
+                }
+              }
+          done[e - 1] = 1;
+        }
+      }
+}
+
+/* DepositionMethod_SF, pic_depo_method.f90:851-1003 + calcSfSource (shapefunction_tools:30-164) */
+static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* PS, int nthreads) {
+  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const size_t nps = (size_t)m->n_elems * ndof * 4;
+  const double r_sf = cfg->sf_radius, r2_sf = r_sf * r_sf, r2_sf_inv = 1.0 / r2_sf;
+  const double w_sf = sf_w(r_sf, cfg->sf_alpha);
+  int nt = nthreads > 0 ? nthreads : 1;
+  int nCases = (m->n_periodic_vectors > 0) ? 27 : 0;
+  double* acc = PS;
+  if (nt > 1) { acc = (double*)calloc(nps * (size_t)nt, sizeof(double)); if (!acc) return 1; }
+  uint8_t* doneAll = (uint8_t*)malloc((size_t)m->n_elems * (size_t)nt);
+  if (!doneAll) { if (acc != PS) free(acc); return 1; }
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double* my = (nt > 1) ? acc + nps * (size_t)tid : PS;
+    uint8_t* done = doneAll + (size_t)m->n_elems * tid;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int ip = 0; ip < p->n; ++ip) {
+      if (!p->inside[ip]) continue;
+      const int sp = p->species[ip] - 1;
+      if (cfg->charge[sp] == 0.0) continue;
+      const double* s = &p->part_state[(size_t)ip * 6];
+      double cm = cfg->charge[sp] * cfg->mpf[sp];
+      double Fac[4] = {s[3] * cm, s[4] * cm, s[5] * cm, cm};
+      if (nCases > 1) {
+        for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * w_sf;
+        for (int ic = 0; ic < 27; ++ic) {
+          /* PeriodicSFCaseMatrix, pic_depo.f90:869-879: case = 9a + 3b + c -> (1-a, 1-b, 1-c) */
+          double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);
+          double Ps[3];
+          for (int d = 0; d < 3; ++d)
+            Ps[d] = s[d] + c1 * m->periodic_vectors[0 * 3 + d] + c2 * m->periodic_vectors[1 * 3 + d] +
+                    c3 * m->periodic_vectors[2 * 3 + d];
+          depo_charge_on_dofs_sf(cfg, m, Ps, Fac, r_sf, r2_sf, r2_sf_inv, my, done);
+        }
+      } else {
+        double Fw[4];
+        for (int v = 0; v < 4; ++v) Fw[v] = Fac[v] * w_sf;
+        depo_charge_on_dofs_sf(cfg, m, s, Fw, r_sf, r2_sf, r2_sf_inv, my, done);
+      }
+    }
+  }
+  if (nt > 1) {
+    for (size_t q = 0; q < nps; ++q) {
+      double v = 0.0;
+      for (int t = 0; t < nt; ++t) v = v + acc[nps * (size_t)t + q];
+      PS[q] = v;
+    }
+    free(acc);
+  }
+  free(doneAll);
+  return 0;
+}
+
+int orc_deposit(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* part_source,
+                orc_counters_t* c, int nthreads) {
+  const int n1 = cfg->n_dg + 1;
+  memset(part_source, 0, sizeof(double) * (size_t)m->n_elems * n1 * n1 * n1 * 4);   /* pic_depo.f90:1004-1007 */
+  if (cfg->deposition == PIC_DEPO_CVWM) return deposit_cvwm(cfg, m, p, part_source, c, nthreads);
+  return deposit_sf(cfg, m, p, part_source, nthreads);
+}
+
+/* One TimeStepPoissonByBorisLeapfrog without HDG (the field stays frozen). */
+int orc_step(const pic_config_t* cfg, const pic_mesh_t* m, const double* e_dof, orc_particles_t* p, double dt,
+             int nsteps, double* part_source, orc_counters_t* c, int nthreads) {
+  for (int it = 0; it < nsteps; ++it) {
+    if (part_source) {
+      int rc = orc_deposit(cfg, m, p, part_source, c, nthreads);                   /* :93 */
+      if (rc) return rc;
+    }
+    for (int ip = 0; ip < p->n; ++ip) {                                            /* :109-110 */
+      for (int d = 0; d < 3; ++d) p->last_part_pos[(size_t)ip * 3 + d] = p->part_state[(size_t)ip * 6 + d];
+      p->last_elem[ip] = p->elem[ip];
+    }
+    orc_interpolate(cfg, m, e_dof, p, c, nthreads);                                /* :122 */
+    orc_push(cfg, p, dt, nthreads);                                                /* :128-198 */
+    orc_track(cfg, m, p, c, nthreads);                                             /* :211 */
+  }
+  return 0;
+}
+
+/* VerifyDepositedCharge, pic_analyze.f90:72-91 with NAnalyze = N (identity change of basis) */
+double orc_integrate_charge(const pic_mesh_t* m, int N, const double* PS) {
+  const int n1 = N + 1, ndof = n1 * n1 * n1;
+  double total = 0.0;
+  for (int e = 0; e < m->n_elems; ++e) {
+    double loc = 0.0;
+    for (int mm = 0; mm <= N; ++mm)
+      for (int l = 0; l <= N; ++l)
+        for (int k = 0; k <= N; ++k) {
+          int r = k + n1 * (l + n1 * mm);
+          double J = 1.0 / m->elem_sj[(size_t)e * ndof + r];
+          double w = m->wgp[k] * m->wgp[l] * m->wgp[mm] * J;
+          loc = loc + w * PS[((size_t)e * ndof + r) * 4 + 3];
+        }
+    total = total + loc;
+  }
+  return total;
+}
+
+void orc_map_particles(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, int nthreads) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
+#endif
+  for (int ip = 0; ip < p->n; ++ip) {
+    if (!p->inside[ip]) continue;
+    orc_get_position_in_ref_elem(cfg, m, &p->part_state[(size_t)ip * 6], &p->part_pos_ref[(size_t)ip * 3], p->elem[ip], 0);
+  }
+  (void)nthreads;
+}

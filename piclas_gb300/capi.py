@@ -1,0 +1,180 @@
+"""ctypes mirror of include/piclas_gpu.h.
+
+The structures here are byte-for-byte the C-ABI structs; ``make_mesh_struct`` fills a
+``PicMesh`` from a :class:`piclas_gb300.mesh.BoxMesh` (the arrays are already in the
+reference's Fortran memory order) and keeps the numpy buffers alive alongside it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PIC_MAX_SPECIES = 8
+
+PIC_TRACK_TRIA = 1
+PIC_TRACK_REFMAPPING = 2
+PIC_DEPO_CVWM = 1
+PIC_DEPO_SHAPE_FUNCTION = 2
+PIC_PREC_FP64 = 0
+PIC_PREC_MIXED = 1
+
+PIC_STATUS_LOST_PARTICLE = 0x01
+PIC_STATUS_NEWTON_FAILED = 0x02
+PIC_STATUS_HOP_LIMIT = 0x04
+PIC_STATUS_REF_TOLERANCE = 0x08
+PIC_STATUS_BAD_ELEMENT = 0x10
+PIC_STATUS_NOT_FINITE = 0x20
+
+ERROR_NAMES = {0: "PIC_OK", 1: "PIC_ERR_INVALID_ARGUMENT", 2: "PIC_ERR_CUDA", 3: "PIC_ERR_OUT_OF_MEMORY",
+               4: "PIC_ERR_NO_DEVICE", 5: "PIC_ERR_STATE", 6: "PIC_ERR_CAPACITY"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class PicConfig(C.Structure):
+    _fields_ = [
+        ("n_dg", C.c_int32), ("tracking", C.c_int32), ("deposition", C.c_int32), ("precision", C.c_int32),
+        ("max_particles", C.c_int32), ("n_species", C.c_int32),
+        ("charge", C.c_double * PIC_MAX_SPECIES), ("mass", C.c_double * PIC_MAX_SPECIES),
+        ("mpf", C.c_double * PIC_MAX_SPECIES), ("external_field", C.c_double * 6),
+        ("refmapping_eps", C.c_double), ("sf_radius", C.c_double), ("sf_alpha", C.c_int32),
+        ("sort_interval", C.c_int32),
+    ]
+
+
+class PicMesh(C.Structure):
+    _fields_ = [
+        ("n_elems", C.c_int32), ("n_geo", C.c_int32), ("n_nodes", C.c_int32), ("n_periodic_vectors", C.c_int32),
+        ("periodic_vectors", C.c_double * 9), ("xmin_glob", C.c_double * 3), ("xmax_glob", C.c_double * 3),
+        ("xi_cl_ngeo", _dp), ("wbary_cl_ngeo", _dp), ("xgp", _dp), ("wgp", _dp), ("wbary_gp", _dp),
+        ("xcl_ngeo", _dp), ("dxcl_ngeo", _dp), ("elem_bary", _dp), ("xez_basis", _dp), ("slen_basis", _dp),
+        ("elem_radius", _dp), ("eps_one_cell", _dp), ("elem_xgp", _dp), ("elem_sj", _dp),
+        ("node_coords", _dp), ("elem_node", _ip), ("elem_side_node", _ip), ("side_nb_elem", _ip),
+        ("side_pvid", _ip), ("concave_side", _ip),
+        ("node_info", _ip), ("node_volume", _dp), ("periodic_n_nodes", _ip), ("periodic_offset", _ip),
+        ("periodic_nodes", _ip), ("n_total_periodic_nodes", C.c_int32),
+        ("fibgm_imax", C.c_int32 * 3), ("fibgm_deltas", C.c_double * 3), ("fibgm_n_elems", _ip),
+        ("fibgm_offset", _ip), ("fibgm_element", _ip), ("fibgm_n_total", C.c_int32),
+    ]
+
+
+class PicStatus(C.Structure):
+    _fields_ = [("error_word", C.c_uint32), ("n_lost", C.c_int32), ("n_inside", C.c_int32),
+                ("n_newton_failed", C.c_int32), ("n_steps", C.c_int64)]
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(_ip)
+
+
+def u8ptr(a: np.ndarray):
+    assert a.dtype == np.uint8 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(_u8p)
+
+
+def make_config(n_dg: int, tracking: int, deposition: int, precision: int, species, max_particles: int,
+                external_field=(0.0,) * 6, refmapping_eps: float = 1e-4, sf_radius: float = 0.0,
+                sf_alpha: int = 2, sort_interval: int = 0) -> PicConfig:
+    """species: list of (charge, mass, mpf)."""
+    cfg = PicConfig()
+    cfg.n_dg = n_dg
+    cfg.tracking = tracking
+    cfg.deposition = deposition
+    cfg.precision = precision
+    cfg.max_particles = max_particles
+    cfg.n_species = len(species)
+    for s, (q, m, w) in enumerate(species):
+        cfg.charge[s] = q
+        cfg.mass[s] = m
+        cfg.mpf[s] = w
+    for i in range(6):
+        cfg.external_field[i] = float(external_field[i])
+    cfg.refmapping_eps = refmapping_eps
+    cfg.sf_radius = sf_radius
+    cfg.sf_alpha = sf_alpha
+    cfg.sort_interval = sort_interval
+    return cfg
+
+
+class MeshStruct:
+    """A filled PicMesh plus the numpy arrays it points into."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        keep = {}
+
+        def d(name, arr):
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            keep[name] = a
+            return dptr(a)
+
+        def i(name, arr):
+            a = np.ascontiguousarray(arr, dtype=np.int32)
+            keep[name] = a
+            return iptr(a)
+
+        s = PicMesh()
+        s.n_elems = mesh.n_elems
+        s.n_geo = mesh.n_geo
+        s.n_nodes = mesh.n_nodes
+        s.n_periodic_vectors = 3
+        pv = mesh.periodic_vectors  # column k = vector k
+        for k in range(3):
+            for c in range(3):
+                s.periodic_vectors[k * 3 + c] = float(pv[c, k])
+        for c in range(3):
+            s.xmin_glob[c] = float(mesh.lo[c])
+            s.xmax_glob[c] = float(mesh.hi[c])
+        s.xi_cl_ngeo = d("xi_cl", mesh.xi_cl_ngeo)
+        s.wbary_cl_ngeo = d("wb_cl", mesh.wbary_cl_ngeo)
+        s.xgp = d("xgp", mesh.xgp)
+        s.wgp = d("wgp", mesh.wgp)
+        s.wbary_gp = d("wbgp", mesh.wbary_gp)
+        s.xcl_ngeo = d("xcl", mesh.xcl_ngeo)
+        s.dxcl_ngeo = d("dxcl", mesh.dxcl_ngeo)
+        s.elem_bary = d("bary", mesh.elem_bary)
+        s.xez_basis = d("xez", mesh.xez_basis)
+        s.slen_basis = d("slen", mesh.slen_basis)
+        s.elem_radius = d("rad", mesh.elem_radius)
+        s.eps_one_cell = d("eps1", mesh.eps_one_cell)
+        s.elem_xgp = d("exgp", mesh.elem_xgp)
+        s.elem_sj = d("esj", mesh.elem_sj)
+        s.node_coords = d("nc", mesh.node_coords)
+        s.elem_node = i("en", mesh.elem_node)
+        s.elem_side_node = i("esn", mesh.elem_side_node)
+        s.side_nb_elem = i("snb", mesh.side_nb_elem)
+        s.side_pvid = i("spv", mesh.side_pvid)
+        s.concave_side = i("cc", mesh.concave_side)
+        s.node_info = i("ni", mesh.node_info)
+        s.node_volume = d("nv", mesh.node_volume)
+        s.periodic_n_nodes = i("pn", mesh.periodic_n_nodes)
+        s.periodic_offset = i("po", mesh.periodic_offset)
+        s.periodic_nodes = i("pnodes", mesh.periodic_nodes)
+        s.n_total_periodic_nodes = int(mesh.periodic_n_nodes.sum())
+        for c in range(3):
+            s.fibgm_imax[c] = int(mesh.fibgm_imax[c])
+            s.fibgm_deltas[c] = float(mesh.fibgm_deltas[c])
+        s.fibgm_n_elems = i("fn", mesh.fibgm_n_elems)
+        s.fibgm_offset = i("fo", mesh.fibgm_offset)
+        s.fibgm_element = i("fe", mesh.fibgm_element)
+        s.fibgm_n_total = int(len(mesh.fibgm_element))
+        self.struct = s
+        self._keep = keep
+
+    @property
+    def ptr(self):
+        return C.byref(self.struct)
+
+
+def repo_root() -> str:
+    return os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -1,0 +1,490 @@
+"""Structured hexahedral box meshes in the layout the PICLas particle loop consumes.
+
+The reference reads HOPR ``.h5`` meshes and derives, at init, the arrays the particle
+loop reads (``XCL_NGeo``, ``dXCL_NGeo``, side/node maps, ``NodeVolume``, periodic node
+twins, the FIBGM background mesh ...).  This module generates the same arrays directly
+for a periodic box of ``nx*ny*nz`` linear (NGeo=1) hexahedra, optionally with the interior
+nodes displaced (curved-box test mesh).  Every array is returned in the reference's
+Fortran memory order (first index fastest), so it can be handed to ``pic_create`` as is.
+
+Reference routines restated (paths relative to the PICLas source tree):
+  * Gauss / Chebyshev-Lobatto nodes, barycentric weights, Lagrange polynomials:
+    src/interpolation/basis.f90:643-688, 719-754, 758-833, 952-976, 1011-1035, 1223-1264
+  * dXCL_NGeo: src/mesh/metrics.f90:309-318;  sJ at Gauss points: metrics.f90 (1/detJac)
+  * ElemBaryNGeo: src/particles/particle_mesh/particle_mesh_build.f90:1446-1466
+  * XiEtaZetaBasis / slenXiEtaZetaBasis / ElemRadiusNGeo: particle_mesh_build.f90:1625-1678
+  * ElemEpsOneCell: particle_mesh_build.f90:607-617
+  * ElemSideNodeID / ConcaveElemSide: src/particles/particle_mesh/particle_mesh_tools.f90:1877-1930
+  * CGNS corner map: src/mesh/mesh_tools.f90:728-769;  ElemNodeID: mesh_tools.f90:634-696
+  * NodeVolume: src/particles/pic/deposition/pic_depo_tools.f90:224-355
+  * Periodic node twins: src/particles/pic/deposition/pic_depo.f90:1218-2089
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+EPS_MACH = float(np.finfo(np.float64).eps)   # PP_RealTolerance = EPSILON(1.0D0)
+
+# CGNS corner c (1..8) -> tensor-product corner index a + 2b + 4c (0-based), NGeo = 1.
+# CNS(1:8) = 1, 2, 4, 3, 5, 6, 8, 7 (mesh_tools.f90:748-755) minus one.
+CGNS_TO_TENSOR = (0, 1, 3, 2, 4, 5, 7, 6)
+# NodeMapCGNS(1:4, side) in CGNS corner numbers (mesh_tools.f90:760-765)
+SIDE_CGNS = ((1, 4, 3, 2), (1, 2, 6, 5), (2, 3, 7, 6), (3, 4, 8, 7), (1, 5, 8, 4), (5, 6, 7, 8))
+# neighbour offset (di, dj, dk) of local sides 1..6 (zeta-, eta-, xi+, eta+, xi-, zeta+)
+SIDE_OFFSET = ((0, 0, -1), (0, -1, 0), (1, 0, 0), (0, 1, 0), (-1, 0, 0), (0, 0, 1))
+SIDE_DIR = (2, 1, 0, 1, 0, 2)          # axis normal to each local side
+SIDE_IS_PLUS = (False, False, True, True, False, True)
+
+
+# --------------------------------------------------------------------------------------
+# 1D basis (basis.f90)
+# --------------------------------------------------------------------------------------
+def almost_equal_unity(x: float, y: float) -> bool:
+    """ALMOSTEQUAL_UNITY, basis.f90:1011-1035."""
+    if x == 0.0 or y == 0.0:
+        return abs(x - y) <= 2.0 * EPS_MACH
+    return abs(x - y) <= EPS_MACH * abs(x) and abs(x - y) <= EPS_MACH * abs(y)
+
+
+def lagrange_polys(x: float, xgp, wbary):
+    """LagrangeInterpolationPolys, basis.f90:1223-1264 (barycentric form, node-hit branch)."""
+    n = len(xgp)
+    L = [0.0] * n
+    hit = False
+    for i in range(n):
+        if almost_equal_unity(x, float(xgp[i])):
+            L[i] = 1.0
+            hit = True
+    if hit:
+        return L
+    s = 0.0
+    for i in range(n):
+        L[i] = float(wbary[i]) / (x - float(xgp[i]))
+        s = s + L[i]
+    return [L[i] / s for i in range(n)]
+
+
+def barycentric_weights(xgp):
+    """BarycentricWeights, basis.f90:952-976."""
+    n = len(xgp)
+    w = [1.0] * n
+    for i in range(1, n):
+        for j in range(i):
+            w[j] = w[j] * (xgp[j] - xgp[i])
+            w[i] = w[i] * (xgp[i] - xgp[j])
+    return [1.0 / v for v in w]
+
+
+def _legendre_and_derivative(n: int, x: float):
+    """LegendrePolynomialAndDerivative, basis.f90:643-688 (normalised)."""
+    if n == 0:
+        L, Ld = 1.0, 0.0
+    elif n == 1:
+        L, Ld = x, 1.0
+    else:
+        Lm2, Lm1, Ldm2, Ldm1 = 1.0, x, 0.0, 1.0
+        L = Ld = 0.0
+        for i in range(2, n + 1):
+            L = (float(2 * i - 1) * x * Lm1 - float(i - 1) * Lm2) / float(i)
+            Ld = Ldm2 + float(2 * i - 1) * Lm1
+            Lm2, Lm1 = Lm1, L
+            Ldm2, Ldm1 = Ldm1, Ld
+    s = math.sqrt(float(n) + 0.5)
+    return L * s, Ld * s
+
+
+def legendre_gauss_nodes(n: int):
+    """LegendreGaussNodesAndWeights, basis.f90:758-833 (Newton from Chebyshev guesses)."""
+    x = [0.0] * (n + 1)
+    w = [0.0] * (n + 1)
+    if n == 0:
+        return [0.0], [2.0]
+    if n == 1:
+        x[0] = -math.sqrt(1.0 / 3.0)
+        x[1] = -x[0]
+        return x, [1.0, 1.0]
+    tol = 1.0e-15
+    cheb = 2.0 * math.atan(1.0) / float(n + 1)
+    for i in range((n + 1) // 2):
+        x[i] = -math.cos(cheb * float(2 * i + 1))
+        for _ in range(11):
+            L, Ld = _legendre_and_derivative(n + 1, x[i])
+            dx = -L / Ld
+            x[i] = x[i] + dx
+            if abs(dx) < tol * abs(x[i]):
+                break
+        L, Ld = _legendre_and_derivative(n + 1, x[i])
+        x[n - i] = -x[i]
+        w[i] = (2.0 * n + 3) / ((1.0 - x[i] * x[i]) * Ld * Ld)
+        w[n - i] = w[i]
+    if n % 2 == 0:
+        x[n // 2] = 0.0
+        L, Ld = _legendre_and_derivative(n + 1, 0.0)
+        w[n // 2] = (2.0 * n + 3) / (Ld * Ld)
+    return x, w
+
+
+def cheby_gauss_lobatto_nodes(n: int):
+    """ChebyGaussLobNodesAndWeights, basis.f90:719-754 (nodes only)."""
+    if n == 0:
+        return [0.0]
+    return [-math.cos(float(i) / float(n) * math.acos(-1.0)) for i in range(n + 1)]
+
+
+# --------------------------------------------------------------------------------------
+# mesh container
+# --------------------------------------------------------------------------------------
+@dataclass
+class BoxMesh:
+    """Arrays of a periodic hex box in reference (Fortran) memory order.
+
+    Index arrays are 1-based like the reference.  ``shape`` comments use Fortran notation.
+    """
+    nx: int
+    ny: int
+    nz: int
+    N: int
+    lo: np.ndarray
+    hi: np.ndarray
+    n_elems: int
+    n_nodes: int
+    n_geo: int
+    periodic_vectors: np.ndarray          # (3,3): column k = PeriodicVectors(:,k)
+    xi_cl_ngeo: np.ndarray
+    wbary_cl_ngeo: np.ndarray
+    xgp: np.ndarray
+    wgp: np.ndarray
+    wbary_gp: np.ndarray
+    xcl_ngeo: np.ndarray                  # (3,0:1,0:1,0:1,nElems) -> C [e][c][b][a][3]
+    dxcl_ngeo: np.ndarray                 # (3,3,0:1,0:1,0:1,nElems) -> C [e][c][b][a][nn][dd]
+    elem_bary: np.ndarray                 # (3,nElems)
+    xez_basis: np.ndarray                 # (3,6,nElems)
+    slen_basis: np.ndarray                # (6,nElems)
+    elem_radius: np.ndarray               # (nElems)
+    eps_one_cell: np.ndarray              # (nElems)
+    elem_xgp: np.ndarray                  # (3,0:N,0:N,0:N,nElems) -> C [e][k][j][i][3]
+    elem_sj: np.ndarray                   # (0:N,0:N,0:N,nElems)
+    node_coords: np.ndarray               # (3,8*nElems): tensor-ordered element corners
+    elem_node: np.ndarray                 # (8,nElems) CGNS order, 1-based into node_coords
+    elem_side_node: np.ndarray            # (4,6,nElems) 1-based into node_coords
+    side_nb_elem: np.ndarray              # (6,nElems) 1-based
+    side_pvid: np.ndarray                 # (6,nElems)
+    side_flip: np.ndarray                 # (6,nElems) SIDE_FLIP (0 for master sides)
+    concave_side: np.ndarray              # (6,nElems)
+    node_info: np.ndarray                 # (8,nElems) unique node ids, 1-based
+    unique_node_coords: np.ndarray        # (3,nUniqueNodes)
+    node_volume: np.ndarray               # (nUniqueNodes)
+    periodic_n_nodes: np.ndarray
+    periodic_offset: np.ndarray
+    periodic_nodes: np.ndarray            # 1-based
+    fibgm_imax: tuple
+    fibgm_deltas: np.ndarray
+    fibgm_n_elems: np.ndarray             # (imax,jmax,kmax) -> C [k][j][i]
+    fibgm_offset: np.ndarray
+    fibgm_element: np.ndarray             # 1-based
+    canonical_node: np.ndarray = field(default=None)  # 0-based periodic-unique id per unique node
+
+    @property
+    def n_dof(self) -> int:
+        return (self.N + 1) ** 3
+
+    @property
+    def h(self) -> np.ndarray:
+        return (self.hi - self.lo) / np.array([self.nx, self.ny, self.nz], dtype=np.float64)
+
+    def elem_index(self, i, j, k):
+        return i + self.nx * (j + self.ny * k)
+
+
+def _wrap(v, n):
+    return v % n
+
+
+def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
+                   perturb: float = 0.0, refmapping_eps: float = 1.0e-4) -> BoxMesh:
+    """Build a fully periodic box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
+
+    ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
+    along each axis (h per axis); boundary nodes stay put so the periodic faces match.
+    """
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    L = hi - lo
+    hvec = L / np.array([nx, ny, nz], dtype=np.float64)
+    ne = nx * ny * nz
+
+    # ---- unique (periodic copies distinct) grid nodes --------------------------------
+    gi = np.arange(nx + 1, dtype=np.float64)
+    gj = np.arange(ny + 1, dtype=np.float64)
+    gk = np.arange(nz + 1, dtype=np.float64)
+    X = np.empty((nz + 1, ny + 1, nx + 1, 3), dtype=np.float64)
+    X[..., 0] = lo[0] + gi[None, None, :] * hvec[0]
+    X[..., 1] = lo[1] + gj[None, :, None] * hvec[1]
+    X[..., 2] = lo[2] + gk[:, None, None] * hvec[2]
+    X[:, :, nx, 0] = hi[0]
+    X[:, ny, :, 1] = hi[1]
+    X[nz, :, :, 2] = hi[2]
+    if perturb != 0.0:
+        interior = np.zeros((nz + 1, ny + 1, nx + 1), dtype=bool)
+        interior[1:nz, 1:ny, 1:nx] = True
+        s = (np.sin(2.0 * np.pi * (X[..., 0] - lo[0]) / L[0]) * np.sin(2.0 * np.pi * (X[..., 1] - lo[1]) / L[1])
+             * np.sin(2.0 * np.pi * (X[..., 2] - lo[2]) / L[2]))
+        for d in range(3):
+            X[..., d] = np.where(interior, X[..., d] + perturb * hvec[d] * s, X[..., d])
+    n_unique = (nx + 1) * (ny + 1) * (nz + 1)
+
+    def uid(i, j, k):  # 0-based unique node id of grid node (i,j,k)
+        return i + (nx + 1) * (j + (ny + 1) * k)
+
+    unique_coords = np.ascontiguousarray(X.reshape(-1, 3))
+
+    # ---- element corners (tensor order a + 2b + 4c) ---------------------------------
+    ei, ej, ek = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ei = ei.transpose(2, 1, 0).reshape(-1)   # element e = i + nx*(j + ny*k)
+    ej = ej.transpose(2, 1, 0).reshape(-1)
+    ek = ek.transpose(2, 1, 0).reshape(-1)
+    corner_uid = np.empty((ne, 8), dtype=np.int64)
+    xcl = np.empty((ne, 2, 2, 2, 3), dtype=np.float64)    # [e][c][b][a][3]
+    for c in range(2):
+        for b in range(2):
+            for a in range(2):
+                t = a + 2 * b + 4 * c
+                corner_uid[:, t] = uid(ei + a, ej + b, ek + c)
+                xcl[:, c, b, a, :] = unique_coords[corner_uid[:, t]]
+    node_coords = np.ascontiguousarray(xcl.reshape(ne, 8, 3))   # NodeCoords_Shared(1:3, 8e+t+1)
+
+    # ---- reference-element data ------------------------------------------------------
+    xi_cl = cheby_gauss_lobatto_nodes(1)
+    wb_cl = barycentric_weights(xi_cl)
+    xgp, wgp = legendre_gauss_nodes(N)
+    wb_gp = barycentric_weights(xgp)
+
+    # dXCL_NGeo(dd,nn,i,j,k) = sum_l D(i,l) X(nn,l,j,k) ... (metrics.f90:309-318), D = +-0.5
+    D = np.array([[-0.5, 0.5], [-0.5, 0.5]])
+    dxcl = np.zeros((ne, 2, 2, 2, 3, 3), dtype=np.float64)  # [e][c][b][a][nn][dd]
+    for c in range(2):
+        for b in range(2):
+            for a in range(2):
+                acc = np.zeros((ne, 3, 3))
+                for l in range(2):
+                    acc[:, :, 0] = acc[:, :, 0] + D[a, l] * xcl[:, c, b, l, :]
+                    acc[:, :, 1] = acc[:, :, 1] + D[b, l] * xcl[:, c, l, a, :]
+                    acc[:, :, 2] = acc[:, :, 2] + D[c, l] * xcl[:, l, b, a, :]
+                dxcl[:, c, b, a, :, :] = acc
+
+    # ElemBaryNGeo: evaluate at xi = 0 (particle_mesh_build.f90:1446-1466)
+    L0 = lagrange_polys(0.0, xi_cl, wb_cl)
+    bary = np.zeros((ne, 3))
+    for c in range(2):
+        for b in range(2):
+            buf = L0[b] * L0[c]
+            for a in range(2):
+                bary = bary + xcl[:, c, b, a, :] * L0[a] * buf
+
+    # XiEtaZetaBasis, slenXiEtaZetaBasis, ElemRadiusNGeo (particle_mesh_build.f90:1625-1678)
+    dirs = ((1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0), (-1.0, 0.0, 0.0), (0.0, -1.0, 0.0), (0.0, 0.0, -1.0))
+    xez = np.zeros((ne, 6, 3))
+    slen = np.zeros((ne, 6))
+    for d, xi in enumerate(dirs):
+        La = lagrange_polys(xi[0], xi_cl, wb_cl)
+        Lb = lagrange_polys(xi[1], xi_cl, wb_cl)
+        Lc = lagrange_polys(xi[2], xi_cl, wb_cl)
+        xp = np.zeros((ne, 3))
+        for c in range(2):
+            for b in range(2):
+                for a in range(2):
+                    xp = xp + xcl[:, c, b, a, :] * La[a] * Lb[b] * Lc[c]
+        v = xp - bary
+        xez[:, d, :] = v
+        slen[:, d] = 1.0 / np.einsum("ij,ij->i", v, v)
+    radius = np.sqrt(np.max(np.sum((node_coords - bary[:, None, :]) ** 2, axis=2), axis=1))
+
+    # ---- Gauss points, Jacobian (trilinear map) -------------------------------------
+    lg = [lagrange_polys(float(x), xi_cl, wb_cl) for x in xgp]   # lg[p][a]
+    nd = N + 1
+    elem_xgp = np.zeros((ne, nd, nd, nd, 3))    # [e][k][j][i][3]
+    jac = np.zeros((ne, nd, nd, nd, 3, 3))      # J[a][b] = d x_a / d xi_b
+    for k in range(nd):
+        for j in range(nd):
+            for i in range(nd):
+                xp = np.zeros((ne, 3))
+                J = np.zeros((ne, 3, 3))
+                for c in range(2):
+                    for b in range(2):
+                        for a in range(2):
+                            w = lg[i][a] * lg[j][b] * lg[k][c]
+                            xp = xp + xcl[:, c, b, a, :] * w
+                            J = J + dxcl[:, c, b, a, :, :] * w      # [nn][dd]
+                elem_xgp[:, k, j, i, :] = xp
+                jac[:, k, j, i] = J
+    Jm = jac
+    detJ = (Jm[..., 0, 0] * (Jm[..., 1, 1] * Jm[..., 2, 2] - Jm[..., 2, 1] * Jm[..., 1, 2])
+            + Jm[..., 0, 1] * (Jm[..., 1, 2] * Jm[..., 2, 0] - Jm[..., 1, 0] * Jm[..., 2, 2])
+            + Jm[..., 0, 2] * (Jm[..., 1, 0] * Jm[..., 2, 1] - Jm[..., 1, 1] * Jm[..., 2, 0]))
+    sJ = 1.0 / detJ                               # [e][k][j][i]
+    scaleJ = sJ.reshape(ne, -1).max(axis=1) / sJ.reshape(ne, -1).min(axis=1)
+    eps_one_cell = 1.0 + np.sqrt(3.0 * scaleJ * refmapping_eps)
+
+    # ---- sides: neighbours, periodic vectors, node maps, concavity -----------------
+    side_nb = np.zeros((ne, 6), dtype=np.int32)
+    side_pvid = np.zeros((ne, 6), dtype=np.int32)
+    side_flip = np.zeros((ne, 6), dtype=np.int32)
+    side_node = np.zeros((ne, 6, 4), dtype=np.int32)
+    concave = np.zeros((ne, 6), dtype=np.int32)
+    dims = (nx, ny, nz)
+    ijk = np.stack([ei, ej, ek], axis=1)
+
+    def grid_of(e, t):
+        a, b, c = t & 1, (t >> 1) & 1, (t >> 2) & 1
+        return ((int(ijk[e, 0]) + a) % nx, (int(ijk[e, 1]) + b) % ny, (int(ijk[e, 2]) + c) % nz)
+
+    for e in range(ne):
+        for s in range(6):
+            off = SIDE_OFFSET[s]
+            n3 = [int(ijk[e, d]) + off[d] for d in range(3)]
+            pv = 0
+            for d in range(3):
+                if n3[d] < 0 or n3[d] >= dims[d]:
+                    # crossing the +face moves the particle by -PeriodicVector(d), the -face by +
+                    pv = -(d + 1) if n3[d] >= dims[d] else (d + 1)
+                n3[d] = _wrap(n3[d], dims[d])
+            en = n3[0] + nx * (n3[1] + ny * n3[2])
+            side_nb[e, s] = en + 1
+            side_pvid[e, s] = pv
+            cg = SIDE_CGNS[s]
+            if SIDE_IS_PLUS[s]:
+                nstart = 0
+                side_flip[e, s] = 0
+            else:
+                # slave side: rotate so that node 1 coincides with the master's node 1
+                sm = s_master = {0: 5, 1: 3, 4: 2}[s]
+                master_first = grid_of(en, CGNS_TO_TENSOR[SIDE_CGNS[sm][0] - 1])
+                nstart = -1
+                for r in range(4):
+                    if grid_of(e, CGNS_TO_TENSOR[cg[r] - 1]) == master_first:
+                        nstart = r
+                        break
+                assert nstart >= 0
+                side_flip[e, s] = nstart + 1
+            for q in range(4):
+                t = CGNS_TO_TENSOR[cg[(nstart + q) % 4] - 1]
+                side_node[e, s, q] = 8 * e + t + 1
+    # ConcaveElemSide (particle_mesh_tools.f90:1909-1930); tie-break on planar sides by side IDs
+    nc = node_coords.reshape(-1, 3)
+    for e in range(ne):
+        for s in range(6):
+            p = [nc[side_node[e, s, q] - 1] for q in range(4)]
+            A = [p[q] - p[3] for q in range(3)]   # A(:,NodeNum)
+            detcon = ((A[0][1] * A[1][2] - A[0][2] * A[1][1]) * A[2][0]
+                      + (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * A[2][1]
+                      + (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * A[2][2])
+            if detcon < 0.0:
+                concave[e, s] = 1
+            elif detcon == 0.0:
+                en = side_nb[e, s] - 1
+                # neighbour's local side facing back
+                s_back = {0: 5, 5: 0, 1: 3, 3: 1, 2: 4, 4: 2}[s]
+                side_id = 6 * e + s + 1
+                nb_side_id = 6 * en + s_back + 1
+                if side_id < nb_side_id:
+                    concave[e, s] = 1
+
+    # ---- element nodes (CGNS order) ---------------------------------------------------
+    elem_node = np.zeros((ne, 8), dtype=np.int32)
+    node_info = np.zeros((ne, 8), dtype=np.int32)
+    for c in range(8):
+        t = CGNS_TO_TENSOR[c]
+        elem_node[:, c] = 8 * np.arange(ne) + t + 1
+        node_info[:, c] = corner_uid[:, t] + 1
+
+    # ---- NodeVolume (pic_depo_tools.f90:282-303) ---------------------------------------
+    xg = np.asarray(xgp)
+    wg = np.asarray(wgp)
+    NV = np.zeros(n_unique)
+    signs = ((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1))
+    for i in range(nd):
+        for j in range(nd):
+            for k in range(nd):
+                sjv = sJ[:, k, j, i]
+                for c in range(8):
+                    sx, sy, sz = signs[c]
+                    w = (1.0 + sx * xg[i]) * (1.0 + sy * xg[j]) * (1.0 + sz * xg[k]) * wg[i] * wg[j] * wg[k] / 8.0
+                    np.add.at(NV, node_info[:, c] - 1, 1.0 / sjv * w)
+
+    # ---- periodic twins (pic_depo.f90:1218-2089) --------------------------------------
+    canon = np.empty(n_unique, dtype=np.int64)
+    gk_, gj_, gi_ = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    canon[:] = ((gi_ % nx) + nx * ((gj_ % ny) + ny * (gk_ % nz))).reshape(-1)
+    order = np.argsort(canon, kind="stable")
+    groups = {}
+    for u in order:
+        groups.setdefault(int(canon[u]), []).append(int(u))
+    per_n = np.zeros(n_unique, dtype=np.int32)
+    per_off = np.zeros(n_unique, dtype=np.int32)
+    per_nodes = []
+    for u in range(n_unique):
+        twins = [v for v in groups[int(canon[u])] if v != u]
+        per_off[u] = len(per_nodes)
+        per_n[u] = len(twins)
+        per_nodes.extend(v + 1 for v in twins)
+    per_nodes = np.asarray(per_nodes if per_nodes else [0], dtype=np.int32)
+    NVper = np.zeros(n_unique)
+    for u in range(n_unique):
+        for q in range(per_n[u]):
+            NVper[u] = NVper[u] + NV[per_nodes[per_off[u] + q] - 1]
+    NV = NV + NVper
+
+    # ---- FIBGM: one background cell per unperturbed element cell ----------------------
+    fib_imax = (nx, ny, nz)
+    fib_d = hvec.copy()
+    bmin = node_coords.min(axis=1)
+    bmax = node_coords.max(axis=1)
+    cells = [[] for _ in range(nx * ny * nz)]
+    for e in range(ne):
+        imn = [max(int(math.floor((bmin[e, d] - lo[d]) / fib_d[d])) + 1, 1) for d in range(3)]
+        imx = [min(int(math.ceil((bmax[e, d] - lo[d]) / fib_d[d])), fib_imax[d]) for d in range(3)]
+        for kk in range(imn[2], imx[2] + 1):
+            for jj in range(imn[1], imx[1] + 1):
+                for ii in range(imn[0], imx[0] + 1):
+                    cells[(ii - 1) + nx * ((jj - 1) + ny * (kk - 1))].append(e + 1)
+    fib_n = np.array([len(c) for c in cells], dtype=np.int32)
+    fib_off = np.zeros(len(cells), dtype=np.int32)
+    fib_off[1:] = np.cumsum(fib_n)[:-1]
+    fib_el = np.array([x for c in cells for x in c], dtype=np.int32)
+
+    pv = np.zeros((3, 3))
+    pv[0, 0], pv[1, 1], pv[2, 2] = L[0], L[1], L[2]   # column k = PeriodicVectors(:,k)
+
+    return BoxMesh(
+        nx=nx, ny=ny, nz=nz, N=N, lo=lo, hi=hi, n_elems=ne, n_nodes=n_unique, n_geo=1,
+        periodic_vectors=pv,
+        xi_cl_ngeo=np.asarray(xi_cl), wbary_cl_ngeo=np.asarray(wb_cl),
+        xgp=np.asarray(xgp), wgp=np.asarray(wgp), wbary_gp=np.asarray(wb_gp),
+        xcl_ngeo=np.ascontiguousarray(xcl), dxcl_ngeo=np.ascontiguousarray(dxcl),
+        elem_bary=np.ascontiguousarray(bary), xez_basis=np.ascontiguousarray(xez),
+        slen_basis=np.ascontiguousarray(slen), elem_radius=np.ascontiguousarray(radius),
+        eps_one_cell=np.ascontiguousarray(eps_one_cell),
+        elem_xgp=np.ascontiguousarray(elem_xgp), elem_sj=np.ascontiguousarray(sJ),
+        node_coords=node_coords, elem_node=elem_node, elem_side_node=np.ascontiguousarray(side_node),
+        side_nb_elem=side_nb, side_pvid=side_pvid, side_flip=side_flip, concave_side=concave,
+        node_info=node_info, unique_node_coords=unique_coords, node_volume=NV,
+        periodic_n_nodes=per_n, periodic_offset=per_off, periodic_nodes=per_nodes,
+        fibgm_imax=fib_imax, fibgm_deltas=fib_d, fibgm_n_elems=fib_n, fibgm_offset=fib_off,
+        fibgm_element=fib_el, canonical_node=canon,
+    )
+
+
+def elem_map(mesh: BoxMesh, e: int, xi) -> np.ndarray:
+    """x(xi) of element e (0-based) through the trilinear CL interpolation."""
+    La = lagrange_polys(float(xi[0]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
+    Lb = lagrange_polys(float(xi[1]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
+    Lc = lagrange_polys(float(xi[2]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
+    x = np.zeros(3)
+    for c in range(2):
+        for b in range(2):
+            for a in range(2):
+                x = x + mesh.xcl_ngeo[e, c, b, a] * La[a] * Lb[b] * Lc[c]
+    return x
