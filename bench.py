@@ -1,0 +1,438 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 PIC particle loop (one JSON line on stdout).
+
+Workload (default ``curved``): PICLas's "plain FP64 at scale" case -- 32^3 curved hexahedra
+(interior nodes displaced by 0.05 h sin sin sin), N=3, 8M electrons (2 eV) + 8M ions (mass
+ratio 1836, 0.1 eV), external B_z = 0.1 T, RefTracking, shape_function deposition with radius
+1.5 h (alpha 2), dt = 5e-12 s.  One step = Deposition + InterpolateFieldToParticle +
+Boris push + RefTracking over all particles, the field frozen (the HDG solve is not timed).
+Inputs are seeded synthetic particles; the particle arrays (~1.3 GB) exceed the 129 MB L2,
+so no flush is needed between timed steps.
+
+``--impl reference`` times the reference algorithm on the host cores instead: the C
+restatement of the Fortran loop (oracle/), OpenMP over particles, on a bounded sample of the
+same workload (the PICLas binary itself cannot be built: no Fortran compiler, MPI or HDF5).
+
+Multi-GPU: the loop does not shard across GPUs here (replicas only): each rank runs its own
+instance with seed = rank; ``value`` sums the ranks' particle-steps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s, mixed vs FP64 on 1 GB300 at <=1e-6 rel rho error; HBM GB/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------------------------
+def make_workload(name: str, seed: int, n_override: int | None = None):
+    from piclas_gb300 import workloads
+    if name == "curved":
+        kw = {} if n_override is None else {"n_per_species": n_override // 2}
+        return workloads.curved_two_species(seed=seed, **kw)
+    if name == "plasma_wave":
+        kw = {} if n_override is None else {"n_particles": n_override}
+        return workloads.plasma_wave(seed=seed, **kw)
+    raise ValueError(name)
+
+
+def workload_config(w, name):
+    m = w.mesh
+    if name == "curved":
+        return {"workload": "plain FP64 at scale: 32^3 curved hex, N=3, 8M e- + 8M ions, B_z=0.1 T, "
+                            "RefTracking, shape_function r=1.5h, dt=5e-12",
+                "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "shape_function",
+                "tracking": "RefTracking (CartesianPeriodic/FastPeriodic)", "l2": "inputs larger than L2 (no flush)"}
+    return {"workload": "plasma wave: 8^3 hex, N=3, 200k e-, CVWM, TriaTracking, dt=1e-11",
+            "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "cell_volweight_mean",
+            "tracking": "TriaTracking", "l2": "L2 flushed between timed steps"}
+
+
+def algorithmic_bytes_per_step(w, mixed: bool) -> float:
+    """B_step of the loop: Np(2 S_state + 2*4 + 1) + Ne nDOF (3*8 + 8) [+ nodes 2*4*8 for CVWM]."""
+    from piclas_gb300 import capi
+    s_state = (24 + 12) if mixed else 48
+    if w.tracking == capi.PIC_TRACK_REFMAPPING:
+        s_state += 24                                   # PartPosRef
+    b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_elems * w.mesh.n_dof * (3 * 8 + 8)
+    if w.deposition == capi.PIC_DEPO_CVWM:
+        b += w.mesh.n_nodes * (2 * 4 * 8)
+    return float(b)
+
+
+def dominant_kernel_bytes(w, mixed: bool) -> tuple[str, float]:
+    """Algorithmic bytes of one launch of the dominant kernel."""
+    from piclas_gb300 import capi
+    if w.deposition == capi.PIC_DEPO_SHAPE_FUNCTION:
+        # gather: each packed particle record read once, PartSource written once
+        rec = 32 if mixed else 16 + 24 + 32
+        return "k_sf_gather", float(w.n * rec + w.mesh.n_elems * w.mesh.n_dof * 4 * 8)
+    s_state = (24 + 12) if mixed else 48
+    b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_elems * w.mesh.n_dof * 3 * (4 if mixed else 8)
+    b += w.mesh.n_nodes * 4 * 8
+    return "k_step_cvwm_tria", float(b)
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic(kernel: str):
+    """dram bytes per launch from the committed ncu summary (profiles/ncu_traffic.md), if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.md")
+    try:
+        for line in open(p):
+            if line.startswith("|") and kernel in line:
+                cells = [c.strip() for c in line.strip("|\n").split("|")]
+                return float(cells[-1])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------------
+def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0, nthreads: int | None = None):
+    """Time the reference algorithm (oracle, OpenMP) on a bounded sample of the workload."""
+    import oracle
+    from piclas_gb300 import capi
+    oracle.build()
+    nthreads = nthreads or max(1, os.cpu_count() or 1)
+    # calibrate: particles per second per step on a small sample
+    probe_n = 4000 if name == "curved" else 20000
+    w = make_workload(name, seed=0, n_override=probe_n)
+    ms = capi.MeshStruct(w.mesh)
+    cfg = w.config()
+
+    def run(wk, nsteps):
+        st = oracle.OracleState(wk.part_state, wk.elem, wk.part_species)
+        if wk.tracking == capi.PIC_TRACK_REFMAPPING:
+            oracle.map_particles(cfg, ms, st, nthreads)
+        PS = np.zeros((wk.mesh.n_elems, wk.mesh.n_dof, 4))
+        t0 = time.perf_counter()
+        oracle.step(cfg, ms, wk.e_dof, st, wk.dt, nsteps, PS, nthreads)
+        return time.perf_counter() - t0
+
+    t_probe = run(w, 1)
+    rate = probe_n / max(t_probe, 1e-6)
+    per_step = max(1.0, target_s / max(steps, 1))
+    n_sample = int(min(max(rate * per_step, probe_n), w.n if name == "plasma_wave" else 16_000_000))
+    from piclas_gb300 import workloads
+    if name == "curved":
+        ws = workloads.curved_two_species(n_per_species=max(n_sample // 2, 1), seed=0, mesh=w.mesh)
+    else:
+        ws = workloads.plasma_wave(n_particles=n_sample, seed=0, mesh=w.mesh)
+    if warmup > 0:
+        run(ws, 1)
+    t = run(ws, steps)
+    value = ws.n * steps / t
+    return {"value": value, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{ws.n} particles x {steps} steps on the full {w.mesh.nx}^3 mesh "
+                      f"(C restatement of the reference loop, OpenMP {nthreads} threads, {t:.1f} s)"}
+
+
+# ----------------------------------------------------------------------------------------------
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from piclas_gb300 import ParticleLoop, capi, load_library
+    torch.cuda.set_device(local_rank)
+    load_library(build_if_missing=True)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    mixed = args.precision == "mixed"
+    prec = capi.PIC_PREC_MIXED if mixed else capi.PIC_PREC_FP64
+    t0 = time.time()
+    w = make_workload(args.workload, seed=rank)
+    log(f"[rank {rank}] workload {w.name} built in {time.time() - t0:.1f}s")
+    cfg = w.config(precision=prec, sort_interval=args.sort_interval)
+    loop = ParticleLoop(cfg, w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    stream = torch.cuda.ExternalStream(loop.stream_ptr)
+    flush = None
+    l2_flush = args.workload == "plasma_wave"
+    if l2_flush:
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # warm-up
+    loop.time_step(w.dt, args.warmup)
+    loop.synchronize()
+
+    def timed(nsteps):
+        evs = []
+        launches0 = loop.launch_count
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        loop.synchronize()
+        if not l2_flush:
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            loop.time_step(w.dt, nsteps)
+            b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b)
+        else:
+            ms = 0.0
+            for _ in range(nsteps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                loop.time_step(w.dt, 1)
+                b.record(stream)
+                b.synchronize()
+                ms += a.elapsed_time(b)
+        loop.synchronize()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return ms, loop.launch_count - launches0
+
+    with ClockSampler(local_rank) as clk:
+        ms, launches = timed(args.steps)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = w.n * world * args.steps / (ms / 1e3)
+    st = loop.status()
+
+    # dominant kernel, timed live with CUDA events on the library's stream
+    loop.profile(True)
+    loop.time_step(w.dt, args.steps)
+    prof = loop.profile_read()
+    loop.profile(False)
+    kname, kbytes = dominant_kernel_bytes(w, mixed)
+    dom = prof["deposit_main"]
+    avg_ms = dom["ms"] / max(dom["launches"], 1)
+    peak, peak_kind = hbm_peak()
+    achieved = kbytes / (avg_ms / 1e3) / 1e9
+    traffic = read_traffic(kname)
+
+    # end-to-end through the C-ABI with host buffers: per step the HDG hand-over (E in, PartSource out)
+    E_host = torch.from_numpy(np.ascontiguousarray(w.e_dof)).pin_memory()
+    PS_host = torch.zeros((w.mesh.n_elems, w.mesh.n_dof, 4), dtype=torch.float64).pin_memory()
+    loop.synchronize()
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        loop.set_field_ptr(E_host.data_ptr())
+        loop.time_step_ptr(w.dt, 1, PS_host.data_ptr())
+    te = time.perf_counter() - te0
+    e2e = {"value": w.n * world * args.steps / te if world == 1 else None, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": int(E_host.numel() * 8), "d2h_bytes_per_step": int(PS_host.numel() * 8)}
+    if dist:
+        t = torch.tensor([te], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e["value"] = w.n * world * args.steps / float(t.item())
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64",
+        "data": "synthetic (seeded), frozen field",
+        "config": dict(workload_config(w, args.workload), precision=args.precision, parallelism=f"replicas x{world}"),
+        "gpu_launches": int(launches),
+        "loop_hbm": {"bytes_per_step": algorithmic_bytes_per_step(w, mixed),
+                     "achieved_gbs": algorithmic_bytes_per_step(w, mixed) * args.steps / (ms / 1e3) / 1e9},
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "avg_launch_ms": avg_ms, "share": dom["ms"] / max(sum(v["ms"] for v in prof.values()), 1e-9)},
+        "phases_ms": {k: round(v["ms"] / args.steps, 4) for k, v in prof.items() if v["launches"]},
+        "e2e": e2e,
+        "status": st,
+    }
+    clocks = clk.summary()
+    out["clocks"] = clocks
+    loop.close()
+    del E_host, PS_host
+
+    if rank == 0 and world == 1 and not args.no_extras:
+        try:
+            out["extras"] = extras(args, w)
+        except Exception as ex:  # extras are informative only
+            out["extras"] = {"error": repr(ex)}
+    if rank == 0 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_reference_run(args.workload, steps=1, warmup=0, target_s=args.cpu_seconds)
+        except Exception as ex:
+            out["cpu_baseline"] = {"error": repr(ex)}
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def extras(args, w_main):
+    """Mixed vs FP64 on the same workload, and the plasma-wave pair (FP64 / mixed)."""
+    import torch
+    from piclas_gb300 import ParticleLoop, capi, workloads
+    res = {}
+
+    def rate(w, prec, steps, flush_l2):
+        loop = ParticleLoop(w.config(precision=prec, sort_interval=args.sort_interval), w.mesh)
+        loop.set_field(w.e_dof)
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+        s = torch.cuda.ExternalStream(loop.stream_ptr)
+        loop.time_step(w.dt, 3)
+        loop.synchronize()
+        buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda") if flush_l2 else None
+        tot = 0.0
+        for _ in range(steps):
+            if buf is not None:
+                with torch.cuda.stream(s):
+                    buf.fill_(2.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            loop.time_step(w.dt, 1)
+            b.record(s)
+            b.synchronize()
+            tot += a.elapsed_time(b)
+        loop.close()
+        return w.n * steps / (tot / 1e3), tot / steps
+
+    def rho_after_one_step(w, prec):
+        loop = ParticleLoop(w.config(precision=prec), w.mesh)
+        loop.set_field(w.e_dof)
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+        PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+        loop.time_step(w.dt, 2, PS)
+        g = loop.download_particles()
+        loop.close()
+        return PS, g
+
+    # mixed on the main workload
+    v_mixed, ms_mixed = rate(w_main, capi.PIC_PREC_MIXED, args.steps, False)
+    ps64, g64 = rho_after_one_step(w_main, capi.PIC_PREC_FP64)
+    ps32, g32 = rho_after_one_step(w_main, capi.PIC_PREC_MIXED)
+    err = float(np.max(np.abs(ps32[..., 3] - ps64[..., 3])) / np.max(np.abs(ps64[..., 3])))
+    res["main_mixed"] = {"value": v_mixed, "ms_per_step": ms_mixed, "rho_rel_err_vs_fp64": err,
+                         "elem_mismatch": int((g32["elem"] != g64["elem"]).sum())}
+    # plasma wave (the reference's CPU-runnable case) in FP64 and mixed, L2 flushed between steps
+    pw = workloads.plasma_wave()
+    v64, ms64 = rate(pw, capi.PIC_PREC_FP64, 20, True)
+    v32, ms32 = rate(pw, capi.PIC_PREC_MIXED, 20, True)
+    ps64, g64 = rho_after_one_step(pw, capi.PIC_PREC_FP64)
+    ps32, g32 = rho_after_one_step(pw, capi.PIC_PREC_MIXED)
+    res["plasma_wave"] = {"fp64": {"value": v64, "ms_per_step": ms64}, "mixed": {"value": v32, "ms_per_step": ms32},
+                          "mixed_over_fp64": v32 / v64,
+                          "rho_rel_err_vs_fp64": float(np.max(np.abs(ps32[..., 3] - ps64[..., 3])) /
+                                                       np.max(np.abs(ps64[..., 3]))),
+                          "elem_mismatch": int((g32["elem"] != g64["elem"]).sum())}
+    return res
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    base = cpu_reference_run(args.workload, steps=max(args.steps, 1), warmup=args.warmup, target_s=args.cpu_seconds)
+    out = {"metric": METRIC, "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded), frozen field",
+           "impl": "reference", "config": {"workload": args.workload, "precision": "fp64"},
+           "cpu_baseline": base,
+           "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="curved", choices=["curved", "plasma_wave"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--sort-interval", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        log("warm-up raised to 3 steps")
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

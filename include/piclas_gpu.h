@@ -181,6 +181,21 @@ int pic_get_status(pic_ctx_t* ctx, pic_status_t* status);
 int pic_reset_status(pic_ctx_t* ctx);
 /* Block the host until all work queued on the context's stream has finished. */
 int pic_synchronize(pic_ctx_t* ctx);
+/* Per-phase CUDA-event timing on the context's stream (no reference counterpart: the GPU analogue
+ * of the reference's LBStartTime/LBSplitTime timers, loadbalance_timers.f90:70-172).
+ * pic_profile(ctx,1) clears and starts collection, pic_profile(ctx,0) stops it.  pic_profile_read
+ * returns accumulated milliseconds and kernel launches per phase:
+ *   0 dominant deposition kernel (shape-function gather, or the fused CVWM+push+tracking kernel)
+ *   1 sort-by-element + pack   2 interpolation+push+tracking   3 node -> DOF
+ *   4 particle reorder         5 stand-alone CVWM deposition */
+#define PIC_N_PHASES 6
+int pic_profile(pic_ctx_t* ctx, int32_t enable);
+int pic_profile_read(pic_ctx_t* ctx, double* ms, int64_t* launches, int32_t nphase);
+/* Kernels launched through this context so far (no reference counterpart: instrumentation). */
+int64_t pic_launch_count(pic_ctx_t* ctx);
+/* The cudaStream_t the context enqueues on, as void* (no reference counterpart: lets a caller
+ * time or order its own work against the loop). */
+void* pic_stream(pic_ctx_t* ctx);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,235 @@
+"""piclas_gb300 -- GB300-native (sm_103a) PIC particle loop of PICLas behind a C-ABI.
+
+Host-side mirror of the reference's Boris-Leapfrog particle loop
+(src/timedisc/timedisc_TimeStepPoissonByBorisLeapfrog.f90).  The method names follow the
+reference routines the C-ABI replaces:
+
+    ParticleLoop.interpolate_field_to_particle()   InterpolateFieldToParticle
+    ParticleLoop.push(dt)                          Boris push loop (+ LastPartPos save)
+    ParticleLoop.perform_tracking()                PerformTracking
+    ParticleLoop.deposition()                      Deposition
+    ParticleLoop.time_step(dt, n)                  TimeStepPoissonByBorisLeapfrog, field frozen
+
+Every call goes through ``libpiclas_gpu.so``; there is no CPU fallback.  A non-zero return
+code raises :class:`PicError` carrying the library's message (where the reference would
+``abort``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import capi
+from .capi import (PIC_DEPO_CVWM, PIC_DEPO_SHAPE_FUNCTION, PIC_PREC_FP64, PIC_PREC_MIXED, PIC_TRACK_REFMAPPING,
+                   PIC_TRACK_TRIA, MeshStruct, PicConfig, PicMesh, PicStatus, make_config)
+
+__all__ = ["ParticleLoop", "PicError", "load_library", "library_path", "MeshStruct", "make_config",
+           "PIC_TRACK_TRIA", "PIC_TRACK_REFMAPPING", "PIC_DEPO_CVWM", "PIC_DEPO_SHAPE_FUNCTION",
+           "PIC_PREC_FP64", "PIC_PREC_MIXED", "EXPORTED_SYMBOLS"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy", "pic_set_field",
+                    "pic_upload_particles", "pic_download_particles", "pic_interpolate", "pic_push", "pic_track",
+                    "pic_deposit", "pic_get_field_at_particles", "pic_step", "pic_get_status", "pic_reset_status",
+                    "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read"]
+
+
+class PicError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str):
+        super().__init__(f"{where}: {capi.ERROR_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "_lib", "libpiclas_gpu.so")
+
+
+def load_library(build_if_missing: bool = False):
+    """Load libpiclas_gpu.so (built by ``piclas_gb300.build``)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            from .build import build
+            build()
+        else:
+            raise RuntimeError(f"{path} missing: run `python -m piclas_gb300.build` (no CPU fallback exists)")
+    L = C.CDLL(path)
+    P = C.POINTER
+    dp, ip, u8p = P(C.c_double), P(C.c_int32), P(C.c_uint8)
+    L.pic_version.restype = C.c_char_p
+    L.pic_last_error.restype = C.c_char_p
+    L.pic_create.argtypes = [P(PicConfig), P(PicMesh), P(C.c_void_p)]
+    L.pic_destroy.argtypes = [C.c_void_p]
+    L.pic_destroy.restype = None
+    L.pic_set_field.argtypes = [C.c_void_p, dp, C.c_int32]
+    L.pic_upload_particles.argtypes = [C.c_void_p, dp, ip, ip, u8p, u8p, C.c_int32]
+    L.pic_download_particles.argtypes = [C.c_void_p, dp, ip, u8p, u8p, dp, C.c_int32]
+    L.pic_interpolate.argtypes = [C.c_void_p]
+    L.pic_push.argtypes = [C.c_void_p, C.c_double]
+    L.pic_track.argtypes = [C.c_void_p]
+    L.pic_deposit.argtypes = [C.c_void_p, dp]
+    L.pic_get_field_at_particles.argtypes = [C.c_void_p, dp, C.c_int32]
+    L.pic_step.argtypes = [C.c_void_p, C.c_double, C.c_int32, dp]
+    L.pic_get_status.argtypes = [C.c_void_p, P(PicStatus)]
+    L.pic_reset_status.argtypes = [C.c_void_p]
+    L.pic_synchronize.argtypes = [C.c_void_p]
+    L.pic_launch_count.argtypes = [C.c_void_p]
+    L.pic_launch_count.restype = C.c_int64
+    L.pic_profile.argtypes = [C.c_void_p, C.c_int32]
+    L.pic_profile_read.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), C.c_int32]
+    L.pic_stream.argtypes = [C.c_void_p]
+    L.pic_stream.restype = C.c_void_p
+    _LIB = L
+    return L
+
+
+def _null(t):
+    return C.POINTER(t)()
+
+
+class ParticleLoop:
+    """One GPU context of the particle loop (one mesh, one particle population)."""
+
+    def __init__(self, cfg: PicConfig, mesh, lib=None):
+        self.lib = lib or load_library()
+        self.cfg = cfg
+        self.mesh_struct = mesh if isinstance(mesh, MeshStruct) else MeshStruct(mesh)
+        self.mesh = self.mesh_struct.mesh
+        self.N = cfg.n_dg
+        self.nd = (self.N + 1) ** 3
+        self.n = 0
+        h = C.c_void_p()
+        self._check(self.lib.pic_create(C.byref(cfg), self.mesh_struct.ptr, C.byref(h)), "pic_create")
+        self.handle = h
+
+    def _check(self, rc: int, where: str):
+        if rc != 0:
+            msg = self.lib.pic_last_error().decode(errors="replace")
+            raise PicError(rc, where, msg)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pic_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state hand-over -------------------------------------------------------------------
+    def set_field(self, e_dof: np.ndarray):
+        """U_N(e)%E(1:3,0:N,0:N,0:N) for all elements: array (nElems, (N+1)^3, 3)."""
+        e = np.ascontiguousarray(e_dof, dtype=np.float64)
+        if e.size != self.mesh.n_elems * self.nd * 3:
+            raise ValueError("field has the wrong size")
+        self._check(self.lib.pic_set_field(self.handle, capi.dptr(e), self.mesh.n_elems), "pic_set_field")
+
+    def upload_particles(self, part_state, elem, species, inside=None, is_new=None):
+        ps = np.ascontiguousarray(part_state, dtype=np.float64)
+        n = ps.shape[0]
+        el = np.ascontiguousarray(elem, dtype=np.int32)
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        ins = np.ones(n, np.uint8) if inside is None else np.ascontiguousarray(inside, np.uint8)
+        new = np.ones(n, np.uint8) if is_new is None else np.ascontiguousarray(is_new, np.uint8)
+        self._check(self.lib.pic_upload_particles(self.handle, capi.dptr(ps), capi.iptr(el), capi.iptr(sp),
+                                                  capi.u8ptr(ins), capi.u8ptr(new), n), "pic_upload_particles")
+        self.n = n
+
+    def download_particles(self, with_ref: bool = False):
+        n = self.n
+        ps = np.zeros((n, 6))
+        el = np.zeros(n, np.int32)
+        ins = np.zeros(n, np.uint8)
+        new = np.zeros(n, np.uint8)
+        ref = np.zeros((n, 3)) if with_ref else None
+        self._check(self.lib.pic_download_particles(self.handle, capi.dptr(ps), capi.iptr(el), capi.u8ptr(ins),
+                                                    capi.u8ptr(new), capi.dptr(ref) if with_ref else _null(C.c_double),
+                                                    n), "pic_download_particles")
+        out = dict(part_state=ps, elem=el, inside=ins, is_new=new)
+        if with_ref:
+            out["part_pos_ref"] = ref
+        return out
+
+    # -- loop pieces ------------------------------------------------------------------------
+    def interpolate_field_to_particle(self):
+        self._check(self.lib.pic_interpolate(self.handle), "pic_interpolate")
+
+    def push(self, dt: float):
+        self._check(self.lib.pic_push(self.handle, dt), "pic_push")
+
+    def perform_tracking(self):
+        self._check(self.lib.pic_track(self.handle), "pic_track")
+
+    def deposition(self, out: np.ndarray | None = None, copy: bool = True):
+        """PS_N(e)%PartSource(1:4,...) for all elements as (nElems, (N+1)^3, 4)."""
+        if not copy:
+            self._check(self.lib.pic_deposit(self.handle, _null(C.c_double)), "pic_deposit")
+            return None
+        ps = out if out is not None else np.zeros((self.mesh.n_elems, self.nd, 4))
+        self._check(self.lib.pic_deposit(self.handle, capi.dptr(ps)), "pic_deposit")
+        return ps
+
+    def field_at_particles(self) -> np.ndarray:
+        f = np.zeros((self.n, 6))
+        self._check(self.lib.pic_get_field_at_particles(self.handle, capi.dptr(f), self.n), "pic_get_field_at_particles")
+        return f
+
+    def time_step(self, dt: float, nsteps: int = 1, part_source: np.ndarray | None = None):
+        ptr = capi.dptr(part_source) if part_source is not None else _null(C.c_double)
+        self._check(self.lib.pic_step(self.handle, dt, nsteps, ptr), "pic_step")
+        return part_source
+
+    def status(self) -> dict:
+        s = PicStatus()
+        self._check(self.lib.pic_get_status(self.handle, C.byref(s)), "pic_get_status")
+        return dict(error_word=int(s.error_word), n_lost=int(s.n_lost), n_inside=int(s.n_inside),
+                    n_newton_failed=int(s.n_newton_failed), n_steps=int(s.n_steps))
+
+    def reset_status(self):
+        self._check(self.lib.pic_reset_status(self.handle), "pic_reset_status")
+
+    def synchronize(self):
+        self._check(self.lib.pic_synchronize(self.handle), "pic_synchronize")
+
+    PHASES = ("deposit_main", "sort_pack", "particle_update", "node_to_dof", "reorder", "cvwm_deposit")
+
+    def profile(self, enable: bool):
+        self._check(self.lib.pic_profile(self.handle, 1 if enable else 0), "pic_profile")
+
+    def profile_read(self) -> dict:
+        ms = (C.c_double * 6)()
+        ln = (C.c_int64 * 6)()
+        self._check(self.lib.pic_profile_read(self.handle, ms, ln, 6), "pic_profile_read")
+        return {name: dict(ms=float(ms[i]), launches=int(ln[i])) for i, name in enumerate(self.PHASES)}
+
+    def set_field_ptr(self, ptr: int):
+        """Field from a host pointer (e.g. pinned memory)."""
+        self._check(self.lib.pic_set_field(self.handle, C.cast(ptr, C.POINTER(C.c_double)), self.mesh.n_elems),
+                    "pic_set_field")
+
+    def time_step_ptr(self, dt: float, nsteps: int, part_source_ptr: int):
+        self._check(self.lib.pic_step(self.handle, dt, nsteps, C.cast(part_source_ptr, C.POINTER(C.c_double))),
+                    "pic_step")
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.pic_launch_count(self.handle))
+
+    @property
+    def stream_ptr(self) -> int:
+        return int(self.lib.pic_stream(self.handle) or 0)

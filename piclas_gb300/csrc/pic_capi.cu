@@ -1,0 +1,817 @@
+// pic_capi.cu -- extern "C" boundary of the GB300 particle loop (see include/piclas_gpu.h).
+//
+// The context owns every device array.  Mesh arrays arrive in the reference's layout and are
+// converted once at pic_create:
+//   * periodic node copies (Periodic_Nodes twins) are merged into one periodic-unique node, so
+//     CVWM deposits once per corner instead of once per copy;
+//   * per-element side data is packed into one 32-bit word per side;
+//   * FP32 copies of the mapping data are made for the mixed variant;
+//   * shape-function neighbour lists (source element, periodic image) are built per target
+//     element from the FIBGM, so deposition is a gather without atomics.
+#include "../../include/piclas_gpu.h"
+#include "pic_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace pic;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                            \
+  do {                                                                                            \
+    cudaError_t _e = (expr);                                                                      \
+    if (_e != cudaSuccess) {                                                                      \
+      return fail(_e == cudaErrorMemoryAllocation ? PIC_ERR_OUT_OF_MEMORY : PIC_ERR_CUDA,         \
+                  std::string(#expr) + ": " + cudaGetErrorString(_e));                            \
+    }                                                                                             \
+  } while (0)
+
+template <class T>
+int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(PIC_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return PIC_OK;
+}
+
+}  // namespace
+
+struct pic_ctx {
+  pic_config_t cfg{};
+  int N = 0, nd = 0, ne = 0, n_canon = 0;
+  bool mixed = false, refmap = false, sf = false;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  // mesh
+  DevMesh M{};
+  MeshF MF{};
+  // field
+  double* E = nullptr;
+  float* E32 = nullptr;
+  bool field_set = false;
+  // deposition
+  double* NS = nullptr;
+  double* PS = nullptr;
+  SortBuffers sortb{};
+  SfLists sfl{};
+  SfPack sfk{};
+  // particles
+  DevParticles P{}, Q{};
+  int* perm = nullptr;
+  int* perm_tmp = nullptr;
+  bool have_particles = false;
+  // status
+  DevStatus* st = nullptr;
+  int* d_count = nullptr;
+  int64_t n_steps = 0;
+  int64_t launches = 0;
+  // per-phase CUDA-event timing (pic_profile)
+  bool prof = false;
+  struct Rec { int phase; cudaEvent_t a, b; int launches; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t prof_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
+  template <class T>
+  int alloc(T** p, size_t n) {
+    int rc = dalloc(p, n);
+    if (rc == PIC_OK) allocs.push_back((void*)*p);
+    return rc;
+  }
+  cudaEvent_t take_event() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  // run fn() (which enqueues kernels and returns how many), bracketed by events when profiling
+  template <class F>
+  void phase(int ph, F&& fn) {
+    if (!prof) { launches += fn(); return; }
+    cudaEvent_t a = take_event(), b = take_event();
+    cudaEventRecord(a, stream);
+    const int n = fn();
+    cudaEventRecord(b, stream);
+    launches += n;
+    recs.push_back(Rec{ph, a, b, n});
+  }
+  void collect() {
+    for (auto& r : recs) {
+      float ms = 0.f;
+      cudaEventSynchronize(r.b);
+      cudaEventElapsedTime(&ms, r.a, r.b);
+      prof_ms[r.phase] += ms;
+      prof_launches[r.phase] += r.launches;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    recs.clear();
+  }
+  LaunchArgs args() const {
+    LaunchArgs a;
+    a.M = M; a.MF = MF; a.N = N; a.nd = nd; a.n_canon = n_canon; a.mixed = mixed;
+    a.E = E; a.E32 = E32; a.NS = NS; a.st = st; a.s = stream;
+    return a;
+  }
+};
+
+
+// ---------------------------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+template <class T>
+int upload(pic_ctx* c, T** dst, const std::vector<T>& src) {
+  int rc = c->alloc(dst, src.size());
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return PIC_OK;
+}
+
+// 3D shape function weight, pic_depo_shapefunction_tools.f90:1243-1246 with beta() of
+// pic_depo_tools.f90:491-511
+double sf_weight(double r, int alpha) {
+  const double PI = std::acos(-1.0);
+  const double beta = std::tgamma(1.5) * std::tgamma((double)alpha + 1.0) / std::tgamma(1.5 + ((double)alpha + 1.0));
+  return 1.0 / (2.0 * beta * (double)alpha + 2.0 * beta) * ((double)alpha + 1.0) / (PI * (r * r * r));
+}
+
+int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
+  if (!cfg || !m) return fail(PIC_ERR_INVALID_ARGUMENT, "null config or mesh");
+  if (cfg->n_dg < 1 || cfg->n_dg > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg must be 1..4");
+  if (cfg->tracking != PIC_TRACK_TRIA && cfg->tracking != PIC_TRACK_REFMAPPING)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "unknown tracking method");
+  if (cfg->deposition != PIC_DEPO_CVWM && cfg->deposition != PIC_DEPO_SHAPE_FUNCTION)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "unknown deposition method");
+  if (cfg->precision != PIC_PREC_FP64 && cfg->precision != PIC_PREC_MIXED)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (cfg->n_species < 1 || cfg->n_species > PIC_MAX_SPECIES) return fail(PIC_ERR_INVALID_ARGUMENT, "n_species");
+  if (cfg->max_particles < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "max_particles");
+  for (int s = 0; s < cfg->n_species; ++s)
+    if (!(cfg->mass[s] > 0.0)) return fail(PIC_ERR_INVALID_ARGUMENT, "species mass must be > 0");
+  if (m->n_elems < 1 || m->n_geo != 1) return fail(PIC_ERR_INVALID_ARGUMENT, "only NGeo = 1 meshes are supported");
+  if (m->n_periodic_vectors < 0 || m->n_periodic_vectors > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "n_periodic_vectors");
+  const void* req[] = {m->xi_cl_ngeo, m->wbary_cl_ngeo, m->xgp, m->wgp, m->wbary_gp, m->xcl_ngeo, m->dxcl_ngeo,
+                       m->elem_bary, m->xez_basis, m->slen_basis, m->elem_radius, m->elem_xgp, m->node_coords,
+                       m->elem_side_node, m->side_nb_elem, m->side_pvid, m->concave_side, m->node_info};
+  for (const void* p : req)
+    if (!p) return fail(PIC_ERR_INVALID_ARGUMENT, "missing mesh array");
+  if (cfg->deposition == PIC_DEPO_CVWM && !m->node_volume) return fail(PIC_ERR_INVALID_ARGUMENT, "node_volume");
+  if ((cfg->tracking == PIC_TRACK_REFMAPPING || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION) &&
+      (!m->fibgm_n_elems || !m->fibgm_offset || !m->fibgm_element || !m->eps_one_cell))
+    return fail(PIC_ERR_INVALID_ARGUMENT, "FIBGM arrays required for RefTracking / shape function");
+  if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION && !(cfg->sf_radius > 0.0 && cfg->sf_alpha >= 2))
+    return fail(PIC_ERR_INVALID_ARGUMENT, "shape function radius/alpha");
+  return PIC_OK;
+}
+
+// Shape-function gather lists: for every target element, the (source element, periodic image)
+// pairs whose bounding box lies within R of at least one DOF of the target.  Enumerated from
+// the FIBGM cells covering the target's DOF box grown by R, with cell indices outside the grid
+// wrapped onto their periodic image.
+int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& dofc) {
+  const int ne = m->n_elems, nd = c->nd;
+  const double R = c->cfg.sf_radius, R2 = R * R;
+  std::vector<double> bmin((size_t)ne * 3), bmax((size_t)ne * 3), dmin((size_t)ne * 3), dmax((size_t)ne * 3);
+  for (int e = 0; e < ne; ++e)
+    for (int d = 0; d < 3; ++d) {
+      double lo = 1e300, hi = -1e300, dl = 1e300, dh = -1e300;
+      for (int t = 0; t < 8; ++t) {
+        double v = m->xcl_ngeo[((size_t)e * 8 + t) * 3 + d];
+        lo = std::min(lo, v); hi = std::max(hi, v);
+      }
+      for (int r = 0; r < nd; ++r) {
+        double v = m->elem_xgp[((size_t)e * nd + r) * 3 + d];
+        dl = std::min(dl, v); dh = std::max(dh, v);
+      }
+      bmin[e * 3 + d] = lo; bmax[e * 3 + d] = hi; dmin[e * 3 + d] = dl; dmax[e * 3 + d] = dh;
+    }
+  // periodic vector per axis (axis-aligned boxes only)
+  double Lax[3] = {0, 0, 0};
+  for (int d = 0; d < 3; ++d) {
+    int k = -1;
+    for (int q = 0; q < m->n_periodic_vectors; ++q) {
+      const double* pv = m->periodic_vectors + 3 * q;
+      if (pv[d] != 0.0) {
+        for (int o = 0; o < 3; ++o)
+          if (o != d && pv[o] != 0.0) return fail(PIC_ERR_INVALID_ARGUMENT, "shape function needs axis-aligned periodic vectors");
+        k = q;
+      }
+    }
+    Lax[d] = k >= 0 ? m->periodic_vectors[3 * k + d] : 0.0;
+  }
+  std::vector<int> off(ne + 1, 0), src;
+  std::vector<int8_t> shift;
+  std::vector<int> seen(ne, -1);
+  std::vector<int> seen_shift(ne, 0);
+  const int* imax = m->fibgm_imax;
+  for (int e = 0; e < ne; ++e) {
+    int clo[3], chi[3];
+    for (int d = 0; d < 3; ++d) {
+      clo[d] = (int)std::floor((dmin[e * 3 + d] - R - m->xmin_glob[d]) / m->fibgm_deltas[d]) + 1;
+      chi[d] = (int)std::ceil((dmax[e * 3 + d] + R - m->xmin_glob[d]) / m->fibgm_deltas[d]);
+    }
+    std::vector<std::pair<int, int>> cand;  // (src, packed shift)
+    for (int kk = clo[2]; kk <= chi[2]; ++kk)
+      for (int jj = clo[1]; jj <= chi[1]; ++jj)
+        for (int ii = clo[0]; ii <= chi[0]; ++ii) {
+          int cidx[3] = {ii, jj, kk}, sh[3] = {0, 0, 0};
+          bool ok = true;
+          for (int d = 0; d < 3; ++d) {
+            while (cidx[d] < 1) { if (Lax[d] == 0.0) { ok = false; break; } cidx[d] += imax[d]; sh[d] -= 1; }
+            while (cidx[d] > imax[d]) { if (Lax[d] == 0.0) { ok = false; break; } cidx[d] -= imax[d]; sh[d] += 1; }
+            if (sh[d] < -1 || sh[d] > 1) ok = false;   // the reference visits the 27 images only
+          }
+          if (!ok) continue;
+          size_t ci = (size_t)(cidx[0] - 1) + (size_t)imax[0] * ((cidx[1] - 1) + (size_t)imax[1] * (cidx[2] - 1));
+          int n = m->fibgm_n_elems[ci], o = m->fibgm_offset[ci];
+          // a cell index below 1 wrapped to the top of the grid holds sources near xmax: their
+          // particles are seen from the target at x + sh*L with sh = -1 (and +1 above the grid)
+          for (int q = 0; q < n; ++q) {
+            int s = m->fibgm_element[o + q] - 1;
+            int pk = ((sh[0] + 1) * 9) + ((sh[1] + 1) * 3) + (sh[2] + 1);
+            cand.emplace_back(s, pk);
+          }
+        }
+    std::sort(cand.begin(), cand.end());
+    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+    for (auto& pr : cand) {
+      const int s = pr.first, pk = pr.second;
+      const int sx = pk / 9 - 1, sy = (pk / 3) % 3 - 1, sz = pk % 3 - 1;
+      const double shv[3] = {sx * Lax[0], sy * Lax[1], sz * Lax[2]};
+      // exact-conservative test: min over target DOFs of the distance to the shifted source box
+      bool keep = false;
+      for (int r = 0; r < nd && !keep; ++r) {
+        double d2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+          const double p = m->elem_xgp[((size_t)e * nd + r) * 3 + d];
+          const double lo = bmin[s * 3 + d] + shv[d], hi = bmax[s * 3 + d] + shv[d];
+          const double q = p < lo ? lo - p : (p > hi ? p - hi : 0.0);
+          d2 += q * q;
+        }
+        if (d2 <= R2 * (1.0 + 1e-6)) keep = true;
+      }
+      if (!keep) continue;
+      src.push_back(s);
+      shift.push_back((int8_t)sx); shift.push_back((int8_t)sy); shift.push_back((int8_t)sz);
+    }
+    off[e + 1] = (int)src.size();
+  }
+  int* d_off; int* d_src; int8_t* d_sh; double* d_c;
+  int rc;
+  if ((rc = upload(c, &d_off, off))) return rc;
+  if ((rc = upload(c, &d_src, src))) return rc;
+  if ((rc = upload(c, &d_sh, shift))) return rc;
+  if ((rc = upload(c, &d_c, dofc))) return rc;
+  c->sfl.nb_off = d_off; c->sfl.nb_src = d_src; c->sfl.nb_shift = d_sh; c->sfl.n_pairs = (int)src.size();
+  c->sfl.dof_center = d_c;
+  return PIC_OK;
+}
+
+int alloc_particles(pic_ctx* c, DevParticles& P, int cap, bool with_aux) {
+  int rc;
+  P.cap = cap;
+  P.n = 0;
+  const size_t n = (size_t)std::max(cap, 1);
+  if ((rc = c->alloc(&P.x, n)) || (rc = c->alloc(&P.y, n)) || (rc = c->alloc(&P.z, n))) return rc;
+  if (c->mixed) {
+    if ((rc = c->alloc(&P.vxf, n)) || (rc = c->alloc(&P.vyf, n)) || (rc = c->alloc(&P.vzf, n))) return rc;
+  } else {
+    if ((rc = c->alloc(&P.vx, n)) || (rc = c->alloc(&P.vy, n)) || (rc = c->alloc(&P.vz, n))) return rc;
+  }
+  if ((rc = c->alloc(&P.xi0, n)) || (rc = c->alloc(&P.xi1, n)) || (rc = c->alloc(&P.xi2, n))) return rc;
+  if ((rc = c->alloc(&P.elem, n)) || (rc = c->alloc(&P.last_elem, n))) return rc;
+  if ((rc = c->alloc(&P.species, n)) || (rc = c->alloc(&P.flags, n))) return rc;
+  if (with_aux) {
+    if ((rc = c->alloc(&P.lx, n)) || (rc = c->alloc(&P.ly, n)) || (rc = c->alloc(&P.lz, n))) return rc;
+    if ((rc = c->alloc(&P.field, 6 * n))) return rc;
+  }
+  return PIC_OK;
+}
+
+int device_sync(pic_ctx* c) {
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaGetLastError());
+  return PIC_OK;
+}
+
+}  // namespace
+
+// =============================================================================================
+extern "C" {
+
+const char* pic_version(void) { return "piclas_gb300 0.1 (sm_103a)"; }
+const char* pic_last_error(void) { return g_last_error.c_str(); }
+
+int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
+  if (!out) return fail(PIC_ERR_INVALID_ARGUMENT, "ctx_out is null");
+  *out = nullptr;
+  int rc = validate(cfg, m);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(PIC_ERR_NO_DEVICE, "no CUDA device");
+  pic_ctx* c = new pic_ctx();
+  c->cfg = *cfg;
+  c->N = cfg->n_dg;
+  const int n1 = c->N + 1;
+  c->nd = n1 * n1 * n1;
+  c->ne = m->n_elems;
+  c->mixed = cfg->precision == PIC_PREC_MIXED;
+  c->refmap = cfg->tracking == PIC_TRACK_REFMAPPING;
+  c->sf = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION;
+  const int ne = c->ne, nd = c->nd;
+  auto bail = [&](int code) { pic_destroy(c); return code; };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(PIC_ERR_CUDA, "cudaStreamCreate failed"));
+
+  // ---- element geometry -------------------------------------------------------------------
+  std::vector<double> xcl(m->xcl_ngeo, m->xcl_ngeo + (size_t)ne * 24);
+  std::vector<double> dxcl(m->dxcl_ngeo, m->dxcl_ngeo + (size_t)ne * 72);
+  std::vector<double> bary(m->elem_bary, m->elem_bary + (size_t)ne * 3);
+  std::vector<double> xez(m->xez_basis, m->xez_basis + (size_t)ne * 18);
+  std::vector<double> slen(m->slen_basis, m->slen_basis + (size_t)ne * 6);
+  std::vector<double> rad(m->elem_radius, m->elem_radius + ne);
+  std::vector<double> eps1(ne, 1.0);
+  if (m->eps_one_cell) eps1.assign(m->eps_one_cell, m->eps_one_cell + ne);
+  std::vector<double> exgp(m->elem_xgp, m->elem_xgp + (size_t)ne * nd * 3);
+  std::vector<int> side_nb((size_t)ne * 6);
+  std::vector<uint32_t> side_info((size_t)ne * 6);
+  for (int e = 0; e < ne; ++e) {
+    for (int t = 0; t < 8; ++t)
+      for (int d = 0; d < 3; ++d)
+        if (m->node_coords[((size_t)e * 8 + t) * 3 + d] != xcl[((size_t)e * 8 + t) * 3 + d])
+          return bail(fail(PIC_ERR_INVALID_ARGUMENT, "node_coords must hold each element's 8 corners (tensor order)"));
+    for (int s = 0; s < 6; ++s) {
+      const int nb = m->side_nb_elem[e * 6 + s];
+      if (nb < 1 || nb > ne) return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_nb_elem out of range (open boundaries are not supported)"));
+      side_nb[e * 6 + s] = nb - 1;
+      uint32_t info = 0;
+      for (int q = 0; q < 4; ++q) {
+        const int t = m->elem_side_node[((size_t)e * 6 + s) * 4 + q] - 1 - 8 * e;
+        if (t < 0 || t > 7) return bail(fail(PIC_ERR_INVALID_ARGUMENT, "elem_side_node must point at the element's own corners"));
+        info |= (uint32_t)t << (3 * q);
+      }
+      if (m->concave_side[e * 6 + s]) info |= 1u << 12;
+      const int pv = m->side_pvid[e * 6 + s];
+      if (pv < -m->n_periodic_vectors || pv > m->n_periodic_vectors)
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_pvid out of range"));
+      info |= ((uint32_t)(uint8_t)(int8_t)pv) << 16;
+      side_info[e * 6 + s] = info;
+    }
+  }
+  // ---- periodic-unique nodes (merge Periodic_Nodes twins) ----------------------------------
+  const int nn = m->n_nodes;
+  std::vector<int> rep(nn);
+  for (int u = 0; u < nn; ++u) {
+    int r = u;
+    if (m->periodic_n_nodes && m->periodic_offset && m->periodic_nodes)
+      for (int j = 0; j < m->periodic_n_nodes[u]; ++j) r = std::min(r, m->periodic_nodes[m->periodic_offset[u] + j] - 1);
+    rep[u] = r;
+  }
+  std::vector<int> canon_id(nn, -1);
+  int ncanon = 0;
+  for (int u = 0; u < nn; ++u)
+    if (rep[u] == u) canon_id[u] = ncanon++;
+  for (int u = 0; u < nn; ++u) canon_id[u] = canon_id[rep[u]];
+  std::vector<double> nvol(ncanon, 0.0);
+  for (int u = 0; u < nn; ++u)
+    if (rep[u] == u) nvol[canon_id[u]] = m->node_volume ? m->node_volume[u] : 1.0;
+  std::vector<int> ecan((size_t)ne * 8);
+  for (size_t q = 0; q < (size_t)ne * 8; ++q) {
+    const int u = m->node_info[q] - 1;
+    if (u < 0 || u >= nn) return bail(fail(PIC_ERR_INVALID_ARGUMENT, "node_info out of range"));
+    ecan[q] = canon_id[u];
+  }
+  c->n_canon = ncanon;
+  // ---- FP32 mapping copies (mixed) ----------------------------------------------------------
+  std::vector<float> xclr((size_t)ne * 24), dxclf((size_t)ne * 72), xezf((size_t)ne * 18), slenf((size_t)ne * 6);
+  for (int e = 0; e < ne; ++e) {
+    for (int t = 0; t < 8; ++t)
+      for (int d = 0; d < 3; ++d) xclr[(e * 8 + t) * 3 + d] = (float)(xcl[(e * 8 + t) * 3 + d] - bary[e * 3 + d]);
+    for (int q = 0; q < 72; ++q) dxclf[(size_t)e * 72 + q] = (float)dxcl[(size_t)e * 72 + q];
+    for (int q = 0; q < 18; ++q) xezf[(size_t)e * 18 + q] = (float)xez[(size_t)e * 18 + q];
+    for (int q = 0; q < 6; ++q) slenf[(size_t)e * 6 + q] = (float)slen[(size_t)e * 6 + q];
+  }
+  // ---- FIBGM -------------------------------------------------------------------------------
+  std::vector<int> fn, fo, fe;
+  if (m->fibgm_n_elems) {
+    const size_t ncell = (size_t)m->fibgm_imax[0] * m->fibgm_imax[1] * m->fibgm_imax[2];
+    fn.assign(m->fibgm_n_elems, m->fibgm_n_elems + ncell);
+    fo.assign(m->fibgm_offset, m->fibgm_offset + ncell);
+    fe.resize(m->fibgm_n_total);
+    for (int q = 0; q < m->fibgm_n_total; ++q) fe[q] = m->fibgm_element[q] - 1;
+  } else {
+    fn.assign(1, 0); fo.assign(1, 0); fe.assign(1, 0);
+  }
+  // ---- upload mesh ---------------------------------------------------------------------------
+  double *d_xcl, *d_dxcl, *d_bary, *d_xez, *d_slen, *d_rad, *d_eps1, *d_exgp, *d_nvol;
+  int *d_snb, *d_ecan, *d_fn, *d_fo, *d_fe;
+  uint32_t* d_sinfo;
+  float *d_xclr, *d_dxclf, *d_xezf, *d_slenf;
+  if ((rc = upload(c, &d_xcl, xcl)) || (rc = upload(c, &d_dxcl, dxcl)) || (rc = upload(c, &d_bary, bary)) ||
+      (rc = upload(c, &d_xez, xez)) || (rc = upload(c, &d_slen, slen)) || (rc = upload(c, &d_rad, rad)) ||
+      (rc = upload(c, &d_eps1, eps1)) || (rc = upload(c, &d_exgp, exgp)) || (rc = upload(c, &d_nvol, nvol)) ||
+      (rc = upload(c, &d_snb, side_nb)) || (rc = upload(c, &d_sinfo, side_info)) || (rc = upload(c, &d_ecan, ecan)) ||
+      (rc = upload(c, &d_fn, fn)) || (rc = upload(c, &d_fo, fo)) || (rc = upload(c, &d_fe, fe)) ||
+      (rc = upload(c, &d_xclr, xclr)) || (rc = upload(c, &d_dxclf, dxclf)) || (rc = upload(c, &d_xezf, xezf)) ||
+      (rc = upload(c, &d_slenf, slenf)))
+    return bail(rc);
+  c->M = DevMesh{ne, d_xcl, d_dxcl, d_bary, d_xez, d_slen, d_rad, d_eps1, d_snb, d_sinfo, d_ecan, d_nvol, d_exgp,
+                 d_fn, d_fo, d_fe};
+  c->MF = MeshF{d_xclr, d_dxclf, d_xezf, d_slenf};
+
+  // ---- constants -------------------------------------------------------------------------------
+  Consts k{};
+  k.N = c->N; k.n1 = n1; k.ndof = nd; k.n_species = cfg->n_species;
+  for (int s = 0; s < cfg->n_species; ++s) {
+    k.q[s] = cfg->charge[s]; k.m[s] = cfg->mass[s]; k.mpf[s] = cfg->mpf[s];
+    k.qm[s] = cfg->charge[s] * cfg->mpf[s];
+  }
+  for (int q = 0; q < 6; ++q) k.ext[q] = cfg->external_field[q];
+  k.refmapping_eps = cfg->refmapping_eps > 0.0 ? cfg->refmapping_eps : 1e-4;
+  const double c2 = 299792458.0 * 299792458.0;
+  k.c2_inv = 1.0 / c2;
+  for (int i = 0; i < n1; ++i) {
+    k.xgp[i] = m->xgp[i]; k.wbary_gp[i] = m->wbary_gp[i];
+    k.fac_gp[i] = (m->xgp[i] + 1.0) / 2.0;    // CellVolWeight%Fac, pic_depo.f90:274-275
+    k.xgp_f[i] = (float)m->xgp[i]; k.wbary_gp_f[i] = (float)m->wbary_gp[i];
+  }
+  k.xi_cl[0] = m->xi_cl_ngeo[0]; k.xi_cl[1] = m->xi_cl_ngeo[1];
+  k.wbary_cl[0] = m->wbary_cl_ngeo[0]; k.wbary_cl[1] = m->wbary_cl_ngeo[1];
+  k.n_pv = m->n_periodic_vectors;
+  for (int q = 0; q < 9; ++q) k.pv[q] = m->periodic_vectors[q];
+  for (int d = 0; d < 3; ++d) {
+    k.xmin[d] = m->xmin_glob[d]; k.xmax[d] = m->xmax_glob[d];
+    k.fib_imax[d] = m->fibgm_imax[d] > 0 ? m->fibgm_imax[d] : 1;
+    k.fib_delta[d] = m->fibgm_deltas[d] > 0.0 ? m->fibgm_deltas[d] : 1.0;
+    k.pv_dir[d] = -1;
+    for (int q = 0; q < m->n_periodic_vectors; ++q)
+      if (m->periodic_vectors[3 * q + d] != 0.0) { k.pv_dir[d] = q; break; }   // GEO%DirPeriodicVectors
+  }
+  if (c->sf) {
+    k.sf_r = cfg->sf_radius; k.sf_r2 = cfg->sf_radius * cfg->sf_radius; k.sf_r2_inv = 1.0 / k.sf_r2;
+    k.sf_alpha = cfg->sf_alpha; k.sf_w = sf_weight(cfg->sf_radius, cfg->sf_alpha);
+  }
+  if (upload_consts(k) != cudaSuccess) return bail(fail(PIC_ERR_CUDA, "constant upload"));
+
+  // ---- work arrays -------------------------------------------------------------------------------
+  if ((rc = c->alloc(&c->E, (size_t)ne * nd * 3)) || (rc = c->alloc(&c->E32, (size_t)ne * nd * 3)) ||
+      (rc = c->alloc(&c->NS, (size_t)ncanon * 4)) || (rc = c->alloc(&c->PS, (size_t)ne * nd * 4)) ||
+      (rc = c->alloc(&c->st, 1)) || (rc = c->alloc(&c->d_count, 1)) ||
+      (rc = c->alloc(&c->sortb.count, ne + 1)) || (rc = c->alloc(&c->sortb.offset, ne + 2)) ||
+      (rc = c->alloc(&c->sortb.cursor, ne + 1)))
+    return bail(rc);
+  c->sortb.ne = ne;
+  cudaMemset(c->st, 0, sizeof(DevStatus));
+  cudaMemset(c->PS, 0, sizeof(double) * (size_t)ne * nd * 4);
+  if ((rc = alloc_particles(c, c->P, cfg->max_particles, true)) || (rc = alloc_particles(c, c->Q, cfg->max_particles, false)) ||
+      (rc = c->alloc(&c->perm, std::max(cfg->max_particles, 1))) || (rc = c->alloc(&c->perm_tmp, std::max(cfg->max_particles, 1))))
+    return bail(rc);
+  // the reorder buffer shares the auxiliary arrays (LastPartPos, field) of P
+  c->Q.lx = c->P.lx; c->Q.ly = c->P.ly; c->Q.lz = c->P.lz; c->Q.field = c->P.field;
+  if (c->sf) {
+    std::vector<double> dofc((size_t)ne * 3);
+    for (int e = 0; e < ne; ++e)
+      for (int d = 0; d < 3; ++d) {
+        double lo = 1e300, hi = -1e300;
+        for (int r = 0; r < nd; ++r) { double v = exgp[((size_t)e * nd + r) * 3 + d]; lo = std::min(lo, v); hi = std::max(hi, v); }
+        dofc[(size_t)e * 3 + d] = 0.5 * (lo + hi);
+      }
+    if ((rc = build_sf_lists(c, m, dofc))) return bail(rc);
+    const size_t cap = (size_t)std::max(cfg->max_particles, 1);
+    if ((rc = c->alloc(&c->sfk.posf, cap * 4))) return bail(rc);
+    if (c->mixed) {
+      if ((rc = c->alloc(&c->sfk.facf, cap * 4))) return bail(rc);
+    } else {
+      if ((rc = c->alloc(&c->sfk.pos, cap * 3)) || (rc = c->alloc(&c->sfk.fac, cap * 4))) return bail(rc);
+    }
+  }
+  if ((rc = device_sync(c))) return bail(rc);
+  *out = c;
+  return PIC_OK;
+}
+
+void pic_destroy(pic_ctx_t* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& r : c->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  for (auto e : c->pool) cudaEventDestroy(e);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int pic_set_field(pic_ctx_t* c, const double* e_dof, int32_t n_elems) {
+  if (!c || !e_dof) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  if (n_elems != c->ne) return fail(PIC_ERR_INVALID_ARGUMENT, "n_elems does not match the mesh");
+  const size_t n = (size_t)c->ne * c->nd * 3;
+  CUDA_TRY(cudaMemcpyAsync(c->E, e_dof, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->mixed) k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->E, c->E32, n);
+  CUDA_TRY(cudaGetLastError());
+  c->field_set = true;
+  return PIC_OK;
+}
+
+__global__ void k_iota(int* p, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = i;
+}
+
+int pic_upload_particles(pic_ctx_t* c, const double* ps, const int32_t* elem, const int32_t* species,
+                         const uint8_t* inside, const uint8_t* is_new, int32_t n) {
+  if (!c || (n > 0 && (!ps || !elem || !species))) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  if (n < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "negative particle count");
+  if (n > c->P.cap) return fail(PIC_ERR_CAPACITY, "more particles than max_particles");
+  std::vector<double> x(n), y(n), z(n), vx(n), vy(n), vz(n);
+  std::vector<float> vxf, vyf, vzf;
+  std::vector<int> el(n);
+  std::vector<uint8_t> sp(n), fl(n);
+  for (int i = 0; i < n; ++i) {
+    const double* s = ps + (size_t)i * 6;
+    x[i] = s[0]; y[i] = s[1]; z[i] = s[2]; vx[i] = s[3]; vy[i] = s[4]; vz[i] = s[5];
+    const bool in = inside ? inside[i] != 0 : true;
+    if (in && (elem[i] < 1 || elem[i] > c->ne)) return fail(PIC_ERR_INVALID_ARGUMENT, "element id out of range");
+    if (species[i] < 1 || species[i] > c->cfg.n_species) return fail(PIC_ERR_INVALID_ARGUMENT, "species id out of range");
+    bool finite = std::isfinite(s[0]) && std::isfinite(s[1]) && std::isfinite(s[2]) && std::isfinite(s[3]) &&
+                  std::isfinite(s[4]) && std::isfinite(s[5]);
+    if (in && !finite) return fail(PIC_ERR_INVALID_ARGUMENT, "non-finite particle state");
+    el[i] = in ? elem[i] - 1 : 0;
+    sp[i] = (uint8_t)(species[i] - 1);
+    fl[i] = (uint8_t)((in ? kInside : 0) | ((is_new ? is_new[i] != 0 : false) ? kNew : 0));
+  }
+  cudaStream_t s = c->stream;
+  const size_t bd = sizeof(double) * (size_t)n;
+  CUDA_TRY(cudaMemcpyAsync(c->P.x, x.data(), bd, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(c->P.y, y.data(), bd, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(c->P.z, z.data(), bd, cudaMemcpyHostToDevice, s));
+  if (c->mixed) {
+    vxf.assign(vx.begin(), vx.end()); vyf.assign(vy.begin(), vy.end()); vzf.assign(vz.begin(), vz.end());
+    CUDA_TRY(cudaMemcpyAsync(c->P.vxf, vxf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->P.vyf, vyf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->P.vzf, vzf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+  } else {
+    CUDA_TRY(cudaMemcpyAsync(c->P.vx, vx.data(), bd, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->P.vy, vy.data(), bd, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->P.vz, vz.data(), bd, cudaMemcpyHostToDevice, s));
+  }
+  CUDA_TRY(cudaMemcpyAsync(c->P.elem, el.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(c->P.last_elem, el.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(c->P.species, sp.data(), n, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(c->P.flags, fl.data(), n, cudaMemcpyHostToDevice, s));
+  c->P.n = n;
+  c->Q.n = n;
+  if (n > 0) k_iota<<<(n + 255) / 256, 256, 0, s>>>(c->perm, n);
+  LaunchArgs A = c->args();
+  if (c->refmap) launch_map_particles(A, c->P);       // PartPosRef at insertion
+  // group by element
+  launch_reorder(A, c->P, c->Q, c->perm, c->perm_tmp, c->sortb);
+  std::swap(c->P.x, c->Q.x); std::swap(c->P.y, c->Q.y); std::swap(c->P.z, c->Q.z);
+  std::swap(c->P.vx, c->Q.vx); std::swap(c->P.vy, c->Q.vy); std::swap(c->P.vz, c->Q.vz);
+  std::swap(c->P.vxf, c->Q.vxf); std::swap(c->P.vyf, c->Q.vyf); std::swap(c->P.vzf, c->Q.vzf);
+  std::swap(c->P.xi0, c->Q.xi0); std::swap(c->P.xi1, c->Q.xi1); std::swap(c->P.xi2, c->Q.xi2);
+  std::swap(c->P.elem, c->Q.elem); std::swap(c->P.last_elem, c->Q.last_elem);
+  std::swap(c->P.species, c->Q.species); std::swap(c->P.flags, c->Q.flags);
+  std::swap(c->perm, c->perm_tmp);
+  int rc = device_sync(c);
+  if (rc) return rc;
+  c->have_particles = true;
+  return PIC_OK;
+}
+
+static void swap_sorted(pic_ctx* c) {
+  std::swap(c->P.x, c->Q.x); std::swap(c->P.y, c->Q.y); std::swap(c->P.z, c->Q.z);
+  std::swap(c->P.vx, c->Q.vx); std::swap(c->P.vy, c->Q.vy); std::swap(c->P.vz, c->Q.vz);
+  std::swap(c->P.vxf, c->Q.vxf); std::swap(c->P.vyf, c->Q.vyf); std::swap(c->P.vzf, c->Q.vzf);
+  std::swap(c->P.xi0, c->Q.xi0); std::swap(c->P.xi1, c->Q.xi1); std::swap(c->P.xi2, c->Q.xi2);
+  std::swap(c->P.elem, c->Q.elem); std::swap(c->P.last_elem, c->Q.last_elem);
+  std::swap(c->P.species, c->Q.species); std::swap(c->P.flags, c->Q.flags);
+  std::swap(c->perm, c->perm_tmp);
+}
+
+int pic_download_particles(pic_ctx_t* c, double* ps, int32_t* elem, uint8_t* inside, uint8_t* is_new,
+                           double* part_pos_ref, int32_t n) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  if (n != c->P.n) return fail(PIC_ERR_INVALID_ARGUMENT, "n does not match the uploaded particle count");
+  int rc = device_sync(c);
+  if (rc) return rc;
+  std::vector<double> x(n), y(n), z(n), vx(n), vy(n), vz(n), a(n), b(n), d(n);
+  std::vector<float> vf(n);
+  std::vector<int> el(n), pm(n);
+  std::vector<uint8_t> fl(n);
+  const size_t bd = sizeof(double) * (size_t)n;
+  if (n > 0) {
+    CUDA_TRY(cudaMemcpy(x.data(), c->P.x, bd, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(y.data(), c->P.y, bd, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(z.data(), c->P.z, bd, cudaMemcpyDeviceToHost));
+    if (c->mixed) {
+      CUDA_TRY(cudaMemcpy(vf.data(), c->P.vxf, sizeof(float) * n, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n; ++i) vx[i] = vf[i];
+      CUDA_TRY(cudaMemcpy(vf.data(), c->P.vyf, sizeof(float) * n, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n; ++i) vy[i] = vf[i];
+      CUDA_TRY(cudaMemcpy(vf.data(), c->P.vzf, sizeof(float) * n, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n; ++i) vz[i] = vf[i];
+    } else {
+      CUDA_TRY(cudaMemcpy(vx.data(), c->P.vx, bd, cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(vy.data(), c->P.vy, bd, cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(vz.data(), c->P.vz, bd, cudaMemcpyDeviceToHost));
+    }
+    CUDA_TRY(cudaMemcpy(el.data(), c->P.elem, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(fl.data(), c->P.flags, n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(pm.data(), c->perm, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    if (part_pos_ref) {
+      CUDA_TRY(cudaMemcpy(a.data(), c->P.xi0, bd, cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(b.data(), c->P.xi1, bd, cudaMemcpyDeviceToHost));
+      CUDA_TRY(cudaMemcpy(d.data(), c->P.xi2, bd, cudaMemcpyDeviceToHost));
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    const int i = pm[j];
+    if (i < 0 || i >= n) return fail(PIC_ERR_STATE, "corrupt particle permutation");
+    if (ps) {
+      double* s = ps + (size_t)i * 6;
+      s[0] = x[j]; s[1] = y[j]; s[2] = z[j]; s[3] = vx[j]; s[4] = vy[j]; s[5] = vz[j];
+    }
+    if (elem) elem[i] = el[j] + 1;
+    if (inside) inside[i] = (fl[j] & kInside) ? 1 : 0;
+    if (is_new) is_new[i] = (fl[j] & kNew) ? 1 : 0;
+    if (part_pos_ref) { part_pos_ref[(size_t)i * 3] = a[j]; part_pos_ref[(size_t)i * 3 + 1] = b[j]; part_pos_ref[(size_t)i * 3 + 2] = d[j]; }
+  }
+  return PIC_OK;
+}
+
+int pic_interpolate(pic_ctx_t* c) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  if (!c->field_set || !c->have_particles) return fail(PIC_ERR_STATE, "field and particles must be set first");
+  c->launches += launch_interpolate(c->args(), c->P, c->refmap, !c->sf);
+  CUDA_TRY(cudaGetLastError());
+  return PIC_OK;
+}
+
+int pic_push(pic_ctx_t* c, double dt) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  if (!c->have_particles) return fail(PIC_ERR_STATE, "particles must be uploaded first");
+  c->launches += launch_push(c->args(), c->P, dt);
+  CUDA_TRY(cudaGetLastError());
+  return PIC_OK;
+}
+
+int pic_track(pic_ctx_t* c) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  if (!c->have_particles) return fail(PIC_ERR_STATE, "particles must be uploaded first");
+  c->launches += launch_track(c->args(), c->P, c->refmap);
+  CUDA_TRY(cudaGetLastError());
+  return PIC_OK;
+}
+
+enum { PH_MAIN = 0, PH_PACK = 1, PH_PARTICLE = 2, PH_NODE2DOF = 3, PH_REORDER = 4, PH_OTHER = 5 };
+
+static int deposit_device(pic_ctx* c) {
+  const LaunchArgs A = c->args();
+  if (c->sf) {
+    c->phase(PH_PACK, [&] { return launch_sf_pack(A, c->P, c->sortb, c->sfl, c->sfk); });
+    c->phase(PH_MAIN, [&] { return launch_sf_gather(A, c->sortb, c->sfl, c->sfk, c->PS); });
+  } else {
+    c->phase(PH_OTHER, [&] { return launch_deposit_cvwm(A, c->P, c->PS); });
+  }
+  return PIC_OK;
+}
+
+int pic_deposit(pic_ctx_t* c, double* part_source) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  if (!c->have_particles) return fail(PIC_ERR_STATE, "particles must be uploaded first");
+  deposit_device(c);
+  CUDA_TRY(cudaGetLastError());
+  if (part_source) {
+    CUDA_TRY(cudaMemcpyAsync(part_source, c->PS, sizeof(double) * (size_t)c->ne * c->nd * 4, cudaMemcpyDeviceToHost,
+                             c->stream));
+    return device_sync(c);
+  }
+  return PIC_OK;
+}
+
+int pic_get_field_at_particles(pic_ctx_t* c, double* field, int32_t n) {
+  if (!c || !field) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  if (n != c->P.n) return fail(PIC_ERR_INVALID_ARGUMENT, "n does not match the particle count");
+  int rc = device_sync(c);
+  if (rc) return rc;
+  std::vector<double> f((size_t)6 * c->P.cap);
+  std::vector<int> pm(n);
+  if (n > 0) {
+    CUDA_TRY(cudaMemcpy(f.data(), c->P.field, sizeof(double) * 6 * (size_t)c->P.cap, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(pm.data(), c->perm, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  }
+  for (int j = 0; j < n; ++j)
+    for (int q = 0; q < 6; ++q) field[(size_t)pm[j] * 6 + q] = f[(size_t)q * c->P.cap + j];
+  return PIC_OK;
+}
+
+int pic_step(pic_ctx_t* c, double dt, int32_t nsteps, double* part_source) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  if (nsteps < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "nsteps < 0");
+  if (!c->field_set || !c->have_particles) return fail(PIC_ERR_STATE, "field and particles must be set first");
+  const int sort_every = c->cfg.sort_interval;
+  for (int it = 0; it < nsteps; ++it) {
+    LaunchArgs A = c->args();
+    if (sort_every > 0 && c->n_steps > 0 && (c->n_steps % sort_every) == 0) {
+      c->phase(PH_REORDER, [&] { return launch_reorder(A, c->P, c->Q, c->perm, c->perm_tmp, c->sortb); });
+      swap_sorted(c);
+      A = c->args();
+    }
+    if (!c->sf && !c->refmap) {
+      // Deposition + InterpolateFieldToParticle + push + TriaTracking in one kernel, then node -> DOF
+      c->phase(PH_MAIN, [&] { return launch_cvwm_fused(A, c->P, dt); });
+      c->phase(PH_NODE2DOF, [&] { return launch_node_to_dof(A, c->PS); });
+    } else {
+      deposit_device(c);                                  // Deposition on x_n
+      if (c->refmap) {
+        c->phase(PH_PARTICLE, [&] { return launch_step_ref(A, c->P, dt); });   // interpolation + push + RefTracking
+      } else {
+        c->phase(PH_PARTICLE, [&] {
+          return launch_interpolate(A, c->P, false, !c->sf) + launch_push(A, c->P, dt) + launch_track(A, c->P, false);
+        });
+      }
+    }
+    c->n_steps++;
+  }
+  CUDA_TRY(cudaGetLastError());
+  if (part_source) {
+    CUDA_TRY(cudaMemcpyAsync(part_source, c->PS, sizeof(double) * (size_t)c->ne * c->nd * 4, cudaMemcpyDeviceToHost,
+                             c->stream));
+    return device_sync(c);
+  }
+  return PIC_OK;
+}
+
+int pic_get_status(pic_ctx_t* c, pic_status_t* out) {
+  if (!c || !out) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  launch_count_inside(c->args(), c->P, c->d_count);
+  int rc = device_sync(c);
+  if (rc) return rc;
+  DevStatus s{};
+  int cnt = 0;
+  CUDA_TRY(cudaMemcpy(&s, c->st, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(&cnt, c->d_count, sizeof(int), cudaMemcpyDeviceToHost));
+  out->error_word = s.error_word;
+  out->n_lost = s.n_lost;
+  out->n_inside = cnt;
+  out->n_newton_failed = s.n_newton_failed;
+  out->n_steps = c->n_steps;
+  return PIC_OK;
+}
+
+int pic_reset_status(pic_ctx_t* c) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  CUDA_TRY(cudaMemsetAsync(c->st, 0, sizeof(DevStatus), c->stream));
+  return device_sync(c);
+}
+
+int pic_synchronize(pic_ctx_t* c) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  return device_sync(c);
+}
+
+int pic_profile(pic_ctx_t* c, int32_t enable) {
+  if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
+  int rc = device_sync(c);
+  if (rc) return rc;
+  c->collect();
+  for (int q = 0; q < 8; ++q) { c->prof_ms[q] = 0.0; c->prof_launches[q] = 0; }
+  c->prof = enable != 0;
+  return PIC_OK;
+}
+
+int pic_profile_read(pic_ctx_t* c, double* ms, int64_t* launches, int32_t nphase) {
+  if (!c || !ms || !launches || nphase < 1) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  int rc = device_sync(c);
+  if (rc) return rc;
+  c->collect();
+  for (int q = 0; q < nphase && q < 8; ++q) { ms[q] = c->prof_ms[q]; launches[q] = c->prof_launches[q]; }
+  return PIC_OK;
+}
+
+// number of kernels launched through this context (for the benchmark's launch count)
+int64_t pic_launch_count(pic_ctx_t* c) { return c ? c->launches : 0; }
+
+// the context's CUDA stream (for event timing by a caller that shares the device)
+void* pic_stream(pic_ctx_t* c) { return c ? (void*)c->stream : nullptr; }
+
+}  // extern "C"

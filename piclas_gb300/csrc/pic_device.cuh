@@ -1,0 +1,660 @@
+// pic_device.cuh -- device data layout and per-particle routines of the GB300 particle loop.
+//
+// FP64 routines keep the reference's floating-point evaluation order (the library is compiled
+// with -fmad=false, so no multiply-add is contracted behind our back); element decisions are
+// therefore bit-identical to the reference's CPU arithmetic.  FP32 routines of the mixed
+// variant request fused multiply-adds explicitly with fmaf().
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pic {
+
+constexpr int kMaxN = 5;                 // highest DG degree instantiated
+constexpr int kMaxTrackLoops = 10000;    // hop cap of the tracking walks (status bit on overflow)
+constexpr double kEpsMach = 2.220446049250313080847e-16;
+
+// ---- device status word -------------------------------------------------------------
+struct DevStatus {
+  unsigned int error_word;
+  int n_lost;
+  int n_newton_failed;
+  int n_ref_tolerance;
+};
+
+// ---- run-time constants (constant memory) -------------------------------------------
+struct Consts {
+  int N, n1, ndof, n_species;
+  double q[8], m[8], mpf[8], qm[8];            // charge, mass, MPF, charge*MPF
+  double ext[6];                               // PIC-externalField
+  double refmapping_eps;
+  double c2_inv;
+  double xgp[kMaxN + 1], wbary_gp[kMaxN + 1], fac_gp[kMaxN + 1];
+  float xgp_f[kMaxN + 1], wbary_gp_f[kMaxN + 1];
+  double xi_cl[2], wbary_cl[2];
+  int n_pv;
+  double pv[9];                                // PeriodicVectors(1:3,k) at pv[3k..3k+2]
+  double xmin[3], xmax[3];
+  int fib_imax[3];
+  double fib_delta[3];
+  double sf_r, sf_r2, sf_r2_inv, sf_w;
+  int sf_alpha;
+  int pv_dir[3];                               // periodic vector index per axis (-1: none)
+};
+// one copy per translation unit; only pic_kernels.cu launches kernels that read it
+static __constant__ Consts c_k;
+
+// ---- mesh (device arrays) ---------------------------------------------------------------
+struct DevMesh {
+  int ne;
+  const double* xcl;       // [ne][8][3] corners in tensor order (= NodeCoords of the element)
+  const double* dxcl;      // [ne][8][3 nn][3 dd]
+  const double* bary;      // [ne][3]
+  const double* xez;       // [ne][6][3]
+  const double* slen;      // [ne][6]
+  const double* radius;    // [ne]
+  const double* eps1;      // [ne]
+  const int* side_nb;      // [ne][6] 0-based neighbour
+  const uint32_t* side_info;  // [ne][6]: bits 0-11 corner ids (4x3), bit 12 concave, bits 16-23 pvid (int8)
+  const int* canon_node;   // [ne][8] periodic-unique node (CGNS corner order)
+  const double* node_vol;  // [n_canon]
+  const double* elem_xgp;  // [ne][ndof][3]
+  const int* fib_n;        // FIBGM cells
+  const int* fib_off;
+  const int* fib_elem;     // 0-based
+};
+
+// ---- particles (SoA) ---------------------------------------------------------------------
+struct DevParticles {
+  int n;
+  double *x, *y, *z;           // PartState(1:3)
+  double *vx, *vy, *vz;        // PartState(4:6) in FP64 mode
+  float *vxf, *vyf, *vzf;      // PartState(4:6) in mixed mode
+  double *lx, *ly, *lz;        // LastPartPos
+  double *xi0, *xi1, *xi2;     // PartPosRef
+  int* elem;                   // 0-based GlobalElemID-1
+  int* last_elem;
+  uint8_t* species;            // 0-based
+  uint8_t* flags;              // bit0 inside, bit1 IsNewPart
+  double* field;               // FieldAtParticle [6][cap]
+  int cap;
+};
+
+constexpr uint8_t kInside = 1, kNew = 2;
+
+__device__ __forceinline__ void flag_status(DevStatus* st, unsigned int bit) { atomicOr(&st->error_word, bit); }
+
+// ==========================================================================================
+// Lagrange basis, basis.f90:1011-1035 and 1223-1264
+// ==========================================================================================
+__device__ __forceinline__ bool almost_equal_unity(double x, double y) {
+  if (x == 0.0 || y == 0.0) return fabs(x - y) <= 2.0 * kEpsMach;
+  return (fabs(x - y) <= kEpsMach * fabs(x)) && (fabs(x - y) <= kEpsMach * fabs(y));
+}
+
+template <int NP>
+__device__ __forceinline__ void lagrange(double x, const double* xgp, const double* wb, double* L) {
+  bool hit = false;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    L[i] = 0.0;
+    if (almost_equal_unity(x, xgp[i])) { L[i] = 1.0; hit = true; }
+  }
+  if (hit) return;
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) { L[i] = wb[i] / (x - xgp[i]); s = s + L[i]; }
+#pragma unroll
+  for (int i = 0; i < NP; ++i) L[i] = L[i] / s;
+}
+
+// FP32 variant (mixed precision): same barycentric formula, node hit within FP32 eps
+template <int NP>
+__device__ __forceinline__ void lagrange_f(float x, const float* xgp, const float* wb, float* L) {
+  bool hit = false;
+  const float eps = 1.1920929e-07f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    L[i] = 0.0f;
+    float d = fabsf(x - xgp[i]);
+    if (d <= eps * fabsf(xgp[i]) || (xgp[i] == 0.0f && d <= 2.0f * eps)) { L[i] = 1.0f; hit = true; }
+  }
+  if (hit) return;
+  float s = 0.0f;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) { L[i] = __fdiv_rn(wb[i], x - xgp[i]); s += L[i]; }
+  const float inv = __frcp_rn(s);
+#pragma unroll
+  for (int i = 0; i < NP; ++i) L[i] = L[i] * inv;
+}
+
+// ==========================================================================================
+// x -> xi: GetRefNewtonStartValue (guess 1, eval_xyz.f90:549-562) + RefElemNewton (:298-445)
+// ==========================================================================================
+__device__ __forceinline__ void newton_start(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const double epsOne = 1.0 + c_k.refmapping_eps;
+  const double* b = M.bary + (size_t)e * 3;
+  double P0 = x[0] - __ldg(b + 0), P1 = x[1] - __ldg(b + 1), P2 = x[2] - __ldg(b + 2);
+  double xil[6];
+  const double* B = M.xez + (size_t)e * 18;
+  const double* S = M.slen + (size_t)e * 6;
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    double dp = P0 * __ldg(B + 3 * d) + P1 * __ldg(B + 3 * d + 1) + P2 * __ldg(B + 3 * d + 2);
+    xil[d] = dp * __ldg(S + d);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) xi[d] = 0.5 * (xil[d] - xil[d + 3]);
+  double mx = fmax(fabs(xi[0]), fmax(fabs(xi[1]), fabs(xi[2])));
+  if (mx > epsOne) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xi[d] = fmax(fmin(1.0, xi[d]), -1.0);
+  }
+}
+
+// Returns isSuccessful (false when the iterate left |xi| <= 1.5).
+static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const double* X = M.xcl + (size_t)e * 24;
+  const double* DX = M.dxcl + (size_t)e * 72;
+  double Xl[24];
+#pragma unroll
+  for (int q = 0; q < 24; ++q) Xl[q] = __ldg(X + q);
+  double L[3][2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) lagrange<2>(xi[d], c_k.xi_cl, c_k.wbary_cl, L[d]);
+  double F[3] = {-x[0], -x[1], -x[2]};
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      double buff = L[1][j] * L[2][k];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int t = i + 2 * j + 4 * k;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) F[c] = F[c] + Xl[3 * t + c] * L[0][i] * buff;
+      }
+    }
+  double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
+  double normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+  int iter = 0;
+  bool success = true;
+  while (deltaXi2 > c_k.refmapping_eps && iter < 100) {
+    iter = iter + 1;
+    double J[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) J[a][b] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        double buff = L[1][j] * L[2][k];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          double buff2 = L[0][i] * buff;
+          const int t = i + 2 * j + 4 * k;
+#pragma unroll
+          for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd) J[nn][dd] = J[nn][dd] + __ldg(DX + 9 * t + 3 * nn + dd) * buff2;
+        }
+      }
+    double sdet = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * J[2][2] + (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * J[2][0] +
+                  (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * J[2][1];
+    if (sdet > 0.0) sdet = 1.0 / sdet;
+    double sJ[3][3];
+    sJ[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * sdet;
+    sJ[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * sdet;
+    sJ[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * sdet;
+    sJ[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * sdet;
+    sJ[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * sdet;
+    sJ[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * sdet;
+    sJ[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * sdet;
+    sJ[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * sdet;
+    sJ[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * sdet;
+    double dxi[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) dxi[r] = ((0.0 + sJ[r][0] * F[0]) + sJ[r][1] * F[1]) + sJ[r][2] * F[2];
+    deltaXi2 = dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2];
+    double xo[3] = {xi[0], xi[1], xi[2]};
+    double normFold = normF;
+    normF = normF * 2.0;
+    double lambda = 1.0;
+    int iArmijo = 1;
+    while (normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xi[d] = xo[d] - lambda * dxi[d];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) lagrange<2>(xi[d], c_k.xi_cl, c_k.wbary_cl, L[d]);
+      F[0] = -x[0]; F[1] = -x[1]; F[2] = -x[2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          double buff = L[1][j] * L[2][k];
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            double buff2 = L[0][i] * buff;
+            const int t = i + 2 * j + 4 * k;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) F[c] = F[c] + Xl[3 * t + c] * buff2;
+          }
+        }
+      lambda = 0.2 * lambda;
+      iArmijo = iArmijo + 1;
+      normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+    }
+    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = false; break; }
+  }
+  return success;
+}
+
+__device__ __forceinline__ bool position_in_ref_elem(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  newton_start(M, e, x, xi);
+  return ref_elem_newton(M, e, x, xi);
+}
+
+// ==========================================================================================
+// Field at a reference position: EvaluateFieldAtRefPos, eval_xyz.f90:167-215 (NVar_in = 3)
+// ==========================================================================================
+template <int N>
+__device__ __forceinline__ void eval_field(const double* __restrict__ U, const double xi[3], double out[3]) {
+  constexpr int n1 = N + 1;
+  double L[3][n1];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) lagrange<n1>(xi[d], c_k.xgp, c_k.wbary_gp, L[d]);
+  out[0] = out[1] = out[2] = 0.0;
+#pragma unroll
+  for (int k = 0; k < n1; ++k)
+#pragma unroll
+    for (int j = 0; j < n1; ++j) {
+      double Lez = L[1][j] * L[2][k];
+#pragma unroll
+      for (int i = 0; i < n1; ++i) {
+        const double* u = U + ((k * n1 + j) * n1 + i) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[c] = out[c] + __ldg(u + c) * L[0][i] * Lez;
+      }
+    }
+}
+
+// GetEMFieldDW, pic_interpolation_tools.f90:458-527 (inverse-distance fallback when Newton failed)
+template <int N>
+static __device__ __noinline__ void eval_field_dw(const DevMesh& M, const double* __restrict__ U, int e, const double x[3],
+                                          double out[3]) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  double dist[nd];
+#pragma unroll
+  for (int r = 0; r < nd; ++r) dist[r] = 0.0;
+  double DistSum = 0.0;
+  const double* xg = M.elem_xgp + (size_t)e * nd * 3;
+  for (int k = 0; k < n1; ++k)
+    for (int l = 0; l < n1; ++l)
+      for (int mm = 0; mm < n1; ++mm) {
+        int r = k + n1 * (l + n1 * mm);
+        double v0 = __ldg(xg + 3 * r) - x[0], v1 = __ldg(xg + 3 * r + 1) - x[1], v2 = __ldg(xg + 3 * r + 2) - x[2];
+        double norm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+        if (norm > 0.0) {
+          dist[r] = 1.0 / norm;
+        } else {
+          for (int q = 0; q < nd; ++q) dist[q] = 0.0;
+          dist[r] = 1.0;
+          DistSum = 1.0;
+          break;
+        }
+        DistSum = DistSum + dist[r];
+      }
+  out[0] = out[1] = out[2] = 0.0;
+  for (int k = 0; k < n1; ++k)
+    for (int l = 0; l < n1; ++l)
+      for (int mm = 0; mm < n1; ++mm) {
+        int r = k + n1 * (l + n1 * mm);
+        for (int c = 0; c < 3; ++c) out[c] = out[c] + dist[r] / DistSum * __ldg(U + 3 * r + c);
+      }
+}
+
+// ==========================================================================================
+// Boris-Leapfrog push, timedisc_TimeStepPoissonByBorisLeapfrog.f90:128-197 (FP64)
+// ==========================================================================================
+__device__ __forceinline__ void boris_push(double v[3], const double F[6], int sp, bool& is_new, double dt) {
+  const double q = c_k.q[sp], mass = c_k.m[sp];
+  const bool push = fabs(q) > 0.0;
+  if (is_new) {
+    if (push) {
+      double qmt = q / mass;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[c] = v[c] - (F[c] * qmt) * dt * 0.5;
+    }
+    is_new = false;
+  }
+  if (!push) return;
+  const double c2_inv = c_k.c2_inv;
+  double c1 = (q * dt) / (mass * 2.0);
+  double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  double gamma = 1.0 / sqrt(1.0 - (vv * c2_inv));
+  double vm[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) vm[c] = v[c] * gamma + c1 * F[c];
+  double gm = sqrt(1.0 + (vm[0] * vm[0] + vm[1] * vm[1] + vm[2] * vm[2]) * c2_inv);
+  double Bn = sqrt(F[3] * F[3] + F[4] * F[4] + F[5] * F[5]);
+  double t[3] = {0.0, 0.0, 0.0};
+  if (fabs(Bn) > 0.0) {
+    double tn = tan(c1 / gm * Bn);
+    double invL = 1.0 / Bn;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) t[c] = tn * (F[3 + c] * invL);
+  } else {
+    double tn = tan(c1 / gm * Bn);   // tan(0): keeps the reference's evaluation (t = tan(.)*0)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) t[c] = tn * 0.0;
+  }
+  double vp[3] = {vm[0] + (vm[1] * t[2] - vm[2] * t[1]), vm[1] + (vm[2] * t[0] - vm[0] * t[2]),
+                  vm[2] + (vm[0] * t[1] - vm[1] * t[0])};
+  double fac = 2.0 / (1.0 + (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
+  double vn1[3];
+  vn1[0] = vm[0] + fac * (vp[1] * t[2] - vp[2] * t[1]);
+  vn1[1] = vm[1] + fac * (vp[2] * t[0] - vp[0] * t[2]);
+  vn1[2] = vm[2] + fac * (vp[0] * t[1] - vp[1] * t[0]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) vn1[c] = vn1[c] + c1 * F[c];
+  double den = sqrt(1.0 + (vn1[0] * vn1[0] + vn1[1] * vn1[1] + vn1[2] * vn1[2]) * c2_inv);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) v[c] = vn1[c] / den;
+}
+
+// ==========================================================================================
+// TriaTracking, particle_triatracking.f90:137-484 with the helpers of particle_mesh_tools.f90
+// and particle_intersection.f90 (regular, non-mortar sides)
+// ==========================================================================================
+__device__ __forceinline__ int side_corner(uint32_t info, int q) { return (info >> (3 * q)) & 7; }
+__device__ __forceinline__ bool side_concave(uint32_t info) { return (info >> 12) & 1; }
+__device__ __forceinline__ int side_pvid(uint32_t info) { return (int)(int8_t)((info >> 16) & 0xff); }
+
+// ParticleInsideQuad3D, particle_mesh_tools.f90:78-222
+__device__ __forceinline__ bool inside_quad3d(const double* __restrict__ X, const uint32_t* __restrict__ sinfo,
+                                              const double x[3], double det[6][2]) {
+  bool in = true;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    const uint32_t info = __ldg(sinfo + s);
+    double A[3][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int t = side_corner(info, q);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) A[c][q] = __ldg(X + 3 * t + c) - x[c];
+    }
+    double cp0 = A[1][0] * A[2][2] - A[2][0] * A[1][2];
+    double cp1 = A[2][0] * A[0][2] - A[0][0] * A[2][2];
+    double cp2 = A[0][0] * A[1][2] - A[1][0] * A[0][2];
+    double d1 = cp0 * A[0][1] + cp1 * A[1][1] + cp2 * A[2][1];
+    d1 = -d1;
+    double d2 = cp0 * A[0][3] + cp1 * A[1][3] + cp2 * A[2][3];
+    det[s][0] = d1;
+    det[s][1] = d2;
+    bool neg = (d1 < 0.0) || (d2 < 0.0);
+    bool pos = !(d1 < 0.0) || !(d2 < 0.0);
+    if (side_concave(info)) { if (!pos) in = false; }
+    else { if (neg) in = false; }
+  }
+  return in;
+}
+
+// ParticleThroughSideCheck3DFast, particle_intersection.f90:167-280
+__device__ __forceinline__ bool through_side(const double* __restrict__ X, uint32_t info, const double P[3],
+                                             const double V[3], int tri) {
+  double Ax[3], Ay[3], Az[3];
+  int t = side_corner(info, 0);
+  Ax[0] = __ldg(X + 3 * t) - P[0]; Ay[0] = __ldg(X + 3 * t + 1) - P[1]; Az[0] = __ldg(X + 3 * t + 2) - P[2];
+#pragma unroll
+  for (int n = 1; n <= 2; ++n) {
+    t = side_corner(info, n + tri - 1);
+    Ax[n] = __ldg(X + 3 * t) - P[0]; Ay[n] = __ldg(X + 3 * t + 1) - P[1]; Az[n] = __ldg(X + 3 * t + 2) - P[2];
+  }
+  const double Vx = V[0], Vy = V[1], Vz = V[2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int a = r, b = (r + 2) % 3;   // row r uses node r and node (r+2)%3
+    double c0 = (Ay[a] * Vz - Az[a] * Vy) * Ax[b];
+    double c1 = (Az[a] * Vx - Ax[a] * Vz) * Ay[b];
+    double c2 = (Ax[a] * Vy - Ay[a] * Vx) * Az[b];
+    double det = (c0 + c1) + c2;
+    double mn = 1.7976931348623157e308;
+    if (fabs(c0) > 0.0 && fabs(c0) < mn) mn = fabs(c0);
+    if (fabs(c1) > 0.0 && fabs(c1) < mn) mn = fabs(c1);
+    if (fabs(c2) > 0.0 && fabs(c2) < mn) mn = fabs(c2);
+    if (!(det >= -kEpsMach * mn)) return false;
+  }
+  return true;
+}
+
+// ParticleThroughSideLastPosCheck, particle_intersection.f90:430-512
+__device__ __forceinline__ bool last_pos_check(const double* __restrict__ X, uint32_t info, const double Pl[3], int tri,
+                                               double& detOut) {
+  double Ax[3], Ay[3], Az[3];
+  int t0 = side_corner(info, 0), t1 = side_corner(info, tri), t2 = side_corner(info, tri + 1);
+  const int ts[3] = {t0, t1, t2};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    Ax[q] = __ldg(X + 3 * ts[q]) - Pl[0];
+    Ay[q] = __ldg(X + 3 * ts[q] + 1) - Pl[1];
+    Az[q] = __ldg(X + 3 * ts[q] + 2) - Pl[2];
+  }
+  double det = ((Ay[0] * Az[1] - Az[0] * Ay[1]) * Ax[2] + (Az[0] * Ax[1] - Ax[0] * Az[1]) * Ay[2] +
+                (Ax[0] * Ay[1] - Ay[0] * Ax[1]) * Az[2]);
+  detOut = det;
+  return !((det < 0.0) || (det != det));
+}
+
+// IntersectionWithWall, particle_intersection.f90:79-164 -> alpha
+__device__ __forceinline__ double wall_alpha(const double* __restrict__ X, uint32_t info, const double Pold[3],
+                                             const double traj[3], int tri) {
+  int t0 = side_corner(info, 0), t1 = side_corner(info, tri), t2 = side_corner(info, tri + 1);
+  double xN = __ldg(X + 3 * t0), yN = __ldg(X + 3 * t0 + 1), zN = __ldg(X + 3 * t0 + 2);
+  double V1[3] = {__ldg(X + 3 * t1) - xN, __ldg(X + 3 * t1 + 1) - yN, __ldg(X + 3 * t1 + 2) - zN};
+  double V2[3] = {__ldg(X + 3 * t2) - xN, __ldg(X + 3 * t2 + 1) - yN, __ldg(X + 3 * t2 + 2) - zN};
+  double nx = V1[1] * V2[2] - V1[2] * V2[1];
+  double ny = V1[2] * V2[0] - V1[0] * V2[2];
+  double nz = V1[0] * V2[1] - V1[1] * V2[0];
+  double nVal = sqrt(nx * nx + ny * ny + nz * nz);
+  nx = nx / nVal; ny = ny / nVal; nz = nz / nVal;
+  double bx = Pold[0] - xN, by = Pold[1] - yN, bz = Pold[2] - zN;
+  double pr = bx * nx + by * ny + bz * nz;
+  double ax = bx - nx * pr, ay = by - ny * pr, az = bz - nz * pr;
+  double dist = sqrt(((ay * bz - az * by) * (ay * bz - az * by) + (az * bx - ax * bz) * (az * bx - ax * bz) +
+                      (ax * by - ay * bx) * (ax * by - ay * bx)) / (ax * ax + ay * ay + az * az));
+  if (dist != dist) dist = sqrt(bx * bx + by * by + bz * bz);
+  double alpha = traj[0] * nx + traj[1] * ny + traj[2] * nz;
+  if (fabs(alpha) > 0.0) alpha = dist / alpha;
+  return alpha;
+}
+
+// Walk from `elem` (= LastElem); updates x / xl at periodic crossings.  Returns the new element,
+// -1 if the particle is lost, -2 if the hop cap was hit.
+static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double x[3], double xl[3]) {
+  int doneE[6] = {0, 0, 0, 0, 0, 0}, doneS[6] = {0, 0, 0, 0, 0, 0}, doneT[6] = {0, 0, 0, 0, 0, 0};
+  // doneE/doneS/doneT hold DoneLastElem(1/4/3, 1:6) with 1-based element and side ids (0 = empty)
+  for (int loop = 0; loop < kMaxTrackLoops; ++loop) {
+    const double* X = M.xcl + (size_t)elem * 24;
+    const uint32_t* sinfo = M.side_info + (size_t)elem * 6;
+    double det[6][2];
+    if (inside_quad3d(X, sinfo, x, det)) return elem;
+    int nThrough = 0, locS[6], triT[6];
+    int localSide = 0;
+    double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
+    double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+    if (fabs(len) > 0.0) { traj[0] = traj[0] / len; traj[1] = traj[1] / len; traj[2] = traj[2] / len; }
+    for (int s = 0; s < 6; ++s) {
+      const uint32_t info = __ldg(sinfo + s);
+      for (int tri = 1; tri <= 2; ++tri) {
+        if (det[s][tri - 1] <= -0.0) {
+          if (through_side(X, info, xl, traj, tri)) {
+            if (nThrough < 6) { locS[nThrough] = s; triT[nThrough] = tri; }
+            nThrough++;
+            localSide = s;
+          }
+        }
+      }
+    }
+    int triNum = triT[0];
+    if (nThrough != 1) {
+      if (nThrough == 0) return -1;
+      int second = 0;
+      double minRatio = 0.0;
+      const int gElem = elem + 1;
+      for (int ind2 = 0; ind2 < nThrough && ind2 < 6; ++ind2) {
+        const int gSide = elem * 6 + locS[ind2] + 1;
+        bool doCheck = true;
+        for (int is = 1; is < 6; ++is)
+          if (doneE[is] == gElem && doneS[is] == gSide && doneT[is] == triT[ind2]) doCheck = false;
+        if (!doCheck) continue;
+        double detM;
+        if (last_pos_check(X, __ldg(sinfo + locS[ind2]), xl, triT[ind2], detM)) {
+          double dPP = det[locS[ind2]][triT[ind2] - 1];
+          if (detM == 0.0 && dPP == 0.0) continue;
+          if (detM == 0.0 && minRatio == 0.0) {
+            second++; localSide = locS[ind2]; triNum = triT[ind2];
+          } else {
+            if (detM == 0.0) continue;
+            double ratio = dPP / detM;
+            if (ratio < minRatio) { minRatio = ratio; second++; localSide = locS[ind2]; triNum = triT[ind2]; }
+          }
+        }
+      }
+      if (second == 0) return -1;
+    }
+    const uint32_t info = __ldg(sinfo + localSide);
+    const int pvid = side_pvid(info);
+    const int nb = __ldg(M.side_nb + (size_t)elem * 6 + localSide);
+#pragma unroll
+    for (int q = 5; q >= 1; --q) { doneE[q] = doneE[q - 1]; doneS[q] = doneS[q - 1]; doneT[q] = doneT[q - 1]; }
+    doneE[0] = elem + 1; doneS[0] = elem * 6 + localSide + 1; doneT[0] = triNum;
+    if (pvid != 0) {
+      // IntersectionWithWall + PeriodicBoundary, particle_boundary_condition.f90:224-284
+      double alpha = wall_alpha(X, info, xl, traj, triNum);
+      const int k = abs(pvid) - 1;
+      const double sg = pvid > 0 ? 1.0 : -1.0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) xl[c] = xl[c] + traj[c] * alpha;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) xl[c] = xl[c] + copysign(c_k.pv[3 * k + c], sg);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c] = xl[c] + (len - alpha) * traj[c];
+    }
+    elem = nb;
+  }
+  return -2;
+}
+
+// ==========================================================================================
+// RefTracking with CartesianPeriodic = FastPeriodic = T (particle_reftracking.f90:30-414, 697-985)
+// ==========================================================================================
+__device__ __forceinline__ void periodic_movement_fast(double x[3], double xl[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int k = c_k.pv_dir[d];
+    if (k < 0) continue;
+    const double* pv = c_k.pv + 3 * k;
+    if (x[d] > c_k.xmax[d]) {
+      double n = ceil(fabs(x[d] - c_k.xmax[d]) / fabs(pv[d]));
+      double mv[3] = {n * pv[0], n * pv[1], n * pv[2]};
+      if (pv[d] > 0.0) { for (int c = 0; c < 3; ++c) { x[c] = x[c] - mv[c]; xl[c] = xl[c] - mv[c]; } }
+      else { for (int c = 0; c < 3; ++c) { x[c] = x[c] + mv[c]; xl[c] = xl[c] + mv[c]; } }
+    }
+    if (x[d] < c_k.xmin[d]) {
+      double n = ceil(fabs(x[d] - c_k.xmin[d]) / fabs(pv[d]));
+      double mv[3] = {n * pv[0], n * pv[1], n * pv[2]};
+      if (pv[d] > 0.0) { for (int c = 0; c < 3; ++c) { x[c] = x[c] + mv[c]; xl[c] = xl[c] + mv[c]; } }
+      else { for (int c = 0; c < 3; ++c) { x[c] = x[c] - mv[c]; xl[c] = xl[c] - mv[c]; } }
+    }
+  }
+}
+
+__device__ __forceinline__ double maxabs3(const double v[3]) { return fmax(fabs(v[0]), fmax(fabs(v[1]), fabs(v[2]))); }
+__device__ __forceinline__ bool almost_equal(double a, double b) { return fabs(a - b) <= fmax(fabs(a), fabs(b)) * 4.441e-16; }
+
+constexpr int kMaxBgmCand = 64;
+
+// Returns the new element (0-based); sets tol_fail when the reference would abort.
+static __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[3], double xl[3], double xi[3],
+                                      bool& tol_fail) {
+  tol_fail = false;
+  if (c_k.n_pv > 0) {
+    double lp[3] = {x[0], x[1], x[2]};
+    periodic_movement_fast(x, xl);
+    int guard = 0;
+    while ((!almost_equal(lp[0], x[0]) || !almost_equal(lp[1], x[1]) || !almost_equal(lp[2], x[2])) && guard < 16) {
+      lp[0] = x[0]; lp[1] = x[1]; lp[2] = x[2];
+      periodic_movement_fast(x, xl);
+      guard++;
+    }
+  }
+  position_in_ref_elem(M, last_elem, x, xi);
+  if (maxabs3(xi) < 1.0) return last_elem;
+  const int oldElem = last_elem;
+  int cell[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int cc = (int)floor((x[d] - c_k.xmin[d]) / c_k.fib_delta[d]);
+    cc = (cc > 0 ? cc : 0) + 1;
+    cell[d] = cc < c_k.fib_imax[d] ? cc : c_k.fib_imax[d];
+  }
+  const size_t cidx = (size_t)(cell[0] - 1) + (size_t)c_k.fib_imax[0] * ((cell[1] - 1) + (size_t)c_k.fib_imax[1] * (cell[2] - 1));
+  int nBGM = __ldg(M.fib_n + cidx);
+  const int off = __ldg(M.fib_off + cidx);
+  if (nBGM > kMaxBgmCand) nBGM = kMaxBgmCand;
+  double dist[kMaxBgmCand];
+  int list[kMaxBgmCand];
+  if (nBGM > 1) {
+    for (int i = 0; i < nBGM; ++i) {
+      const int e = __ldg(M.fib_elem + off + i);
+      list[i] = e;
+      if (e == oldElem) {
+        dist[i] = -1.7976931348623157e308;
+      } else {
+        double d0 = x[0] - __ldg(M.bary + 3 * e), d1 = x[1] - __ldg(M.bary + 3 * e + 1), d2 = x[2] - __ldg(M.bary + 3 * e + 2);
+        dist[i] = (d0 * d0 + d1 * d1) + d2 * d2;
+        double r = __ldg(M.radius + e);
+        if (dist[i] > r * r) dist[i] = -1.7976931348623157e308;
+      }
+    }
+    for (int i = 1; i < nBGM; ++i) {   // InsertionSort, utils.f90:52-101
+      int j = i - 1;
+      double tr = dist[i];
+      int ti = list[i];
+      while (j >= 0) {
+        if (dist[j] <= tr) break;
+        dist[j + 1] = dist[j]; list[j + 1] = list[j];
+        j--;
+      }
+      dist[j + 1] = tr; list[j + 1] = ti;
+    }
+  } else if (nBGM == 1) {
+    dist[0] = 0.0;
+    list[0] = __ldg(M.fib_elem + off);
+  }
+  double oldXi[3] = {xi[0], xi[1], xi[2]};
+  double newXi[3] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308};
+  int newElem = -1;
+  for (int i = 0; i < nBGM; ++i) {
+    if (dist[i] == -1.7976931348623157e308) continue;
+    const int e = list[i];
+    position_in_ref_elem(M, e, x, xi);
+    if (maxabs3(xi) < 1.0) return e;
+    if (maxabs3(xi) < maxabs3(newXi)) { newXi[0] = xi[0]; newXi[1] = xi[1]; newXi[2] = xi[2]; newElem = e; }
+  }
+  int te;
+  if (maxabs3(oldXi) < maxabs3(newXi)) {
+    xi[0] = oldXi[0]; xi[1] = oldXi[1]; xi[2] = oldXi[2];
+    te = oldElem;
+  } else {
+    xi[0] = newXi[0]; xi[1] = newXi[1]; xi[2] = newXi[2];
+    te = newElem;
+  }
+  if (te < 0 || maxabs3(xi) > __ldg(M.eps1 + te)) tol_fail = true;
+  return te < 0 ? oldElem : te;
+}
+
+}  // namespace pic

@@ -1,0 +1,1136 @@
+// pic_kernels.cu -- sm_103a kernels of the Boris-Leapfrog PIC particle loop.
+//
+// Layout: particles in SoA (x,y,z / vx,vy,vz / elem / flags), kept grouped by element by a
+// counting sort so that a warp mostly works on one element: its corner nodes, DOFs and field
+// stay in L1, and CVWM charge is reduced across the warp before the global atomics.
+#include "pic_kernels.cuh"
+
+#include <cstdio>
+
+namespace pic {
+
+
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------------------------
+// warp reduce-scatter: lane k ends with the warp sum of v[k] (k = node*4 + component)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double reduce_scatter32(double v[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool upper = (lane & h) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const double a = v[j], b = v[j + h];
+      const double recv = __shfl_xor_sync(kFull, upper ? a : b, h);
+      v[j] = (upper ? b : a) + recv;
+    }
+  }
+  return v[0];
+}
+
+// Knuth TwoSum
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// compensated variant: (hi, lo) pairs, exact partial sums carried in lo
+__device__ __forceinline__ double reduce_scatter32_ts(float hi[32], float lo[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool upper = (lane & h) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const float ah = hi[j], bh = hi[j + h], al = lo[j], bl = lo[j + h];
+      const float rh = __shfl_xor_sync(kFull, upper ? ah : bh, h);
+      const float rl = __shfl_xor_sync(kFull, upper ? al : bl, h);
+      float s, e;
+      two_sum(upper ? bh : ah, rh, s, e);
+      hi[j] = s;
+      lo[j] = __fadd_rn(__fadd_rn(upper ? bl : al, rl), e);
+    }
+  }
+  return (double)hi[0] + (double)lo[0];
+}
+
+// Scatter one particle's 8 corner contributions (contrib[k], k = node*4+comp) to the
+// periodic-unique node sums.  Called by all 32 lanes; lanes with active=false add nothing.
+__device__ __forceinline__ void cvwm_scatter(const DevMesh& M, bool active, int e, double contrib[32], double* NS) {
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(kFull, active);
+  if (act == 0) return;
+  const int leader = __ffs(act) - 1;
+  const int e0 = __shfl_sync(kFull, e, leader);
+  const bool same = __all_sync(kFull, !active || e == e0);
+  if (same) {
+    if (!active) {
+#pragma unroll
+      for (int k = 0; k < 32; ++k) contrib[k] = 0.0;
+    }
+    const double s = reduce_scatter32(contrib);
+    const int node = __ldg(M.canon_node + (size_t)e0 * 8 + (lane >> 2));
+    atomicAdd(NS + (size_t)node * 4 + (lane & 3), s);
+  } else if (active) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) atomicAdd(NS + (size_t)node * 4 + c, contrib[4 * n + c]);
+    }
+  }
+}
+
+__device__ __forceinline__ void cvwm_scatter_ts(const DevMesh& M, bool active, int e, float hi[32], double* NS) {
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(kFull, active);
+  if (act == 0) return;
+  const int leader = __ffs(act) - 1;
+  const int e0 = __shfl_sync(kFull, e, leader);
+  const bool same = __all_sync(kFull, !active || e == e0);
+  if (same) {
+    float lo[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) { lo[k] = 0.0f; if (!active) hi[k] = 0.0f; }
+    const double s = reduce_scatter32_ts(hi, lo);
+    const int node = __ldg(M.canon_node + (size_t)e0 * 8 + (lane >> 2));
+    atomicAdd(NS + (size_t)node * 4 + (lane & 3), s);
+  } else if (active) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) atomicAdd(NS + (size_t)node * 4 + c, (double)hi[4 * n + c]);
+    }
+  }
+}
+
+// CVWM corner weights of one particle (pic_depo_method.f90:479-539) in FP64, as contributions.
+__device__ __forceinline__ void cvwm_contrib(const DevMesh& M, int e, bool suc, const double xi[3], const double x[3],
+                                             const double TS[4], double out[32]) {
+  double w[8];
+  if (suc) {
+    const double a1 = 0.5 * (xi[0] + 1.0), a2 = 0.5 * (xi[1] + 1.0), a3 = 0.5 * (xi[2] + 1.0);
+    w[0] = (1 - a1) * (1 - a2) * (1 - a3);
+    w[1] = (a1) * (1 - a2) * (1 - a3);
+    w[2] = (a1) * (a2) * (1 - a3);
+    w[3] = (1 - a1) * (a2) * (1 - a3);
+    w[4] = (1 - a1) * (1 - a2) * (a3);
+    w[5] = (a1) * (1 - a2) * (a3);
+    w[6] = (a1) * (a2) * (a3);
+    w[7] = (1 - a1) * (a2) * (a3);
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) out[4 * n + c] = TS[c] * w[n];
+  } else {
+    // inverse-distance weights to the corners (CGNS corner order)
+    const double* X = M.xcl + (size_t)e * 24;
+    const int cg2t[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+    for (int n = 0; n < 8; ++n) w[n] = 0.0;
+    for (int n = 0; n < 8; ++n) {
+      const int t = cg2t[n];
+      double v0 = __ldg(X + 3 * t) - x[0], v1 = __ldg(X + 3 * t + 1) - x[1], v2 = __ldg(X + 3 * t + 2) - x[2];
+      double norm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+      if (norm > 0.0) w[n] = 1.0 / norm;
+      else { for (int q = 0; q < 8; ++q) w[q] = 0.0; w[n] = 1.0; break; }
+    }
+    double ds = 0.0;
+    for (int n = 0; n < 8; ++n) ds = ds + w[n];
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) out[4 * n + c] = w[n] / ds * TS[c];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Mixed-precision (FP32) mapping on linear, uncurved elements: Newton in element-local
+// coordinates relative to the barycentre.  Only used with TriaTracking meshes.
+// ---------------------------------------------------------------------------------------------
+
+
+__device__ __forceinline__ bool position_in_ref_elem_f(const MeshF& F, int e, const float p[3], float xi[3]) {
+  const float* B = F.xez + (size_t)e * 18;
+  const float* S = F.slen + (size_t)e * 6;
+  float xil[6];
+#pragma unroll
+  for (int d = 0; d < 6; ++d)
+    xil[d] = fmaf(p[0], __ldg(B + 3 * d), fmaf(p[1], __ldg(B + 3 * d + 1), p[2] * __ldg(B + 3 * d + 2))) * __ldg(S + d);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) xi[d] = 0.5f * (xil[d] - xil[d + 3]);
+  const float epsOne = 1.0f + (float)c_k.refmapping_eps;
+  if (fmaxf(fabsf(xi[0]), fmaxf(fabsf(xi[1]), fabsf(xi[2]))) > epsOne) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xi[d] = fmaxf(fminf(1.0f, xi[d]), -1.0f);
+  }
+  const float* X = F.xclr + (size_t)e * 24;
+  const float* DX = F.dxcl + (size_t)e * 72;
+  bool success = true;
+  float deltaXi2 = 1.0f;
+  for (int iter = 0; iter < 100 && deltaXi2 > (float)c_k.refmapping_eps; ++iter) {
+    float l[3][2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { l[d][0] = 0.5f * (1.0f - xi[d]); l[d][1] = 0.5f * (1.0f + xi[d]); }
+    float Fr[3] = {-p[0], -p[1], -p[2]}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const float w = l[0][t & 1] * l[1][(t >> 1) & 1] * l[2][t >> 2];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Fr[c] = fmaf(__ldg(X + 3 * t + c), w, Fr[c]);
+#pragma unroll
+      for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) J[nn][dd] = fmaf(__ldg(DX + 9 * t + 3 * nn + dd), w, J[nn][dd]);
+    }
+    float det = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * J[2][2] + (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * J[2][0] +
+                (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * J[2][1];
+    const float sd = 1.0f / det;
+    float dxi[3];
+    dxi[0] = ((J[1][1] * J[2][2] - J[1][2] * J[2][1]) * Fr[0] + (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * Fr[1] +
+              (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * Fr[2]) * sd;
+    dxi[1] = ((J[1][2] * J[2][0] - J[1][0] * J[2][2]) * Fr[0] + (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * Fr[1] +
+              (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * Fr[2]) * sd;
+    dxi[2] = ((J[1][0] * J[2][1] - J[1][1] * J[2][0]) * Fr[0] + (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * Fr[1] +
+              (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * Fr[2]) * sd;
+    deltaXi2 = dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xi[d] -= dxi[d];
+    if (fabsf(xi[0]) > 1.5f || fabsf(xi[1]) > 1.5f || fabsf(xi[2]) > 1.5f) { success = false; break; }
+  }
+  return success;
+}
+
+template <int N>
+__device__ __forceinline__ void eval_field_f(const float* __restrict__ U, const float xi[3], float out[3]) {
+  constexpr int n1 = N + 1;
+  float L[3][n1];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) lagrange_f<n1>(xi[d], c_k.xgp_f, c_k.wbary_gp_f, L[d]);
+  out[0] = out[1] = out[2] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < n1; ++k)
+#pragma unroll
+    for (int j = 0; j < n1; ++j) {
+      const float Lez = L[1][j] * L[2][k];
+#pragma unroll
+      for (int i = 0; i < n1; ++i) {
+        const float* u = U + ((k * n1 + j) * n1 + i) * 3;
+        const float w = L[0][i] * Lez;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[c] = fmaf(__ldg(u + c), w, out[c]);
+      }
+    }
+}
+
+// FP32 Boris push (mixed variant)
+__device__ __forceinline__ void boris_push_f(float v[3], const float F[6], int sp, bool& is_new, float dt) {
+  const float q = (float)c_k.q[sp], qmt = (float)(c_k.q[sp] / c_k.m[sp]);
+  const bool push = fabsf(q) > 0.0f;
+  if (is_new) {
+    if (push) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[c] = fmaf(-F[c] * qmt, dt * 0.5f, v[c]);
+    }
+    is_new = false;
+  }
+  if (!push) return;
+  const float c2i = (float)c_k.c2_inv;
+  const float c1 = 0.5f * qmt * dt;
+  const float vv = fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2]));
+  const float gamma = rsqrtf(1.0f - vv * c2i);
+  float vm[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) vm[c] = fmaf(v[c], gamma, c1 * F[c]);
+  const float gm = sqrtf(fmaf(fmaf(vm[0], vm[0], fmaf(vm[1], vm[1], vm[2] * vm[2])), c2i, 1.0f));
+  const float Bn = sqrtf(fmaf(F[3], F[3], fmaf(F[4], F[4], F[5] * F[5])));
+  float t[3] = {0.0f, 0.0f, 0.0f};
+  if (Bn > 0.0f) {
+    const float s = tanf(c1 / gm * Bn) / Bn;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) t[c] = s * F[3 + c];
+  }
+  const float vp[3] = {vm[0] + (vm[1] * t[2] - vm[2] * t[1]), vm[1] + (vm[2] * t[0] - vm[0] * t[2]),
+                       vm[2] + (vm[0] * t[1] - vm[1] * t[0])};
+  const float fac = 2.0f / (1.0f + fmaf(t[0], t[0], fmaf(t[1], t[1], t[2] * t[2])));
+  float vn[3];
+  vn[0] = fmaf(fac, vp[1] * t[2] - vp[2] * t[1], vm[0]) + c1 * F[0];
+  vn[1] = fmaf(fac, vp[2] * t[0] - vp[0] * t[2], vm[1]) + c1 * F[1];
+  vn[2] = fmaf(fac, vp[0] * t[1] - vp[1] * t[0], vm[2]) + c1 * F[2];
+  const float inv = rsqrtf(fmaf(fmaf(vn[0], vn[0], fmaf(vn[1], vn[1], vn[2] * vn[2])), c2i, 1.0f));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) v[c] = vn[c] * inv;
+}
+
+// =============================================================================================
+// Fused step for cell_volweight_mean + TriaTracking
+// =============================================================================================
+template <int N, bool MIXED>
+__global__ void __launch_bounds__(256) k_step_cvwm_tria(DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
+                                                        const float* __restrict__ E32, double* __restrict__ NS,
+                                                        double dt, DevStatus* st) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in_range = i < P.n;
+  const uint8_t fl = in_range ? P.flags[i] : 0;
+  const bool inside = (fl & kInside) != 0;
+  const int sp = inside ? P.species[i] : 0;
+  const bool charged = inside && (c_k.q[sp] != 0.0);
+  int e = inside ? P.elem[i] : 0;
+  double x[3] = {0.0, 0.0, 0.0};
+  if (inside) { x[0] = P.x[i]; x[1] = P.y[i]; x[2] = P.z[i]; }
+
+  // ---- Deposition (CVWM) and interpolation share one x -> xi mapping ------------------------
+  double Fd[6];
+  float Ff[6];
+  if constexpr (!MIXED) {
+    double v[3] = {0.0, 0.0, 0.0};
+    if (inside) { v[0] = P.vx[i]; v[1] = P.vy[i]; v[2] = P.vz[i]; }
+    double xi[3] = {0.0, 0.0, 0.0};
+    bool suc = true;
+    if (charged) {
+      suc = position_in_ref_elem(M, e, x, xi);
+      if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
+    }
+    {
+      double contrib[32];
+      if (charged) {
+        const double ch = c_k.qm[sp];
+        const double TS[4] = {v[0] * ch, v[1] * ch, v[2] * ch, ch};
+        cvwm_contrib(M, e, suc, xi, x, TS, contrib);
+      }
+      cvwm_scatter(M, charged, e, contrib, NS);
+    }
+    if (!inside) return;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) Fd[c] = c_k.ext[c];
+    if (charged) {
+      double Eo[3];
+      const double* U = E + (size_t)e * nd * 3;
+      if (suc) eval_field<N>(U, xi, Eo);
+      else eval_field_dw<N>(M, U, e, x, Eo);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Fd[c] = Fd[c] + Eo[c];
+#pragma unroll
+      for (int c = 3; c < 6; ++c) Fd[c] = Fd[c] + 0.0;
+    }
+    bool isnew = (fl & kNew) != 0;
+    boris_push(v, Fd, sp, isnew, dt);
+    double xl[3] = {x[0], x[1], x[2]};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
+    int ne = tria_track(M, e, x, xl);
+    uint8_t nf = isnew ? (fl | kNew) : (fl & ~kNew);
+    if (ne < 0) {
+      nf &= ~kInside;
+      if (ne == -1) { atomicAdd(&st->n_lost, 1); flag_status(st, 0x01u); }
+      else flag_status(st, 0x04u);
+      ne = e;
+    }
+    P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+    P.elem[i] = ne;
+    P.flags[i] = nf;
+  } else {
+    float v[3] = {0.0f, 0.0f, 0.0f};
+    if (inside) { v[0] = P.vxf[i]; v[1] = P.vyf[i]; v[2] = P.vzf[i]; }
+    float xi[3] = {0.0f, 0.0f, 0.0f};
+    bool suc = true;
+    if (charged) {
+      const double* b = M.bary + (size_t)e * 3;
+      const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
+      suc = position_in_ref_elem_f(MF, e, p, xi);
+      if (!suc) {
+        // fall back to the FP64 mapping so that the inverse-distance branch matches the reference's
+        double xd[3];
+        suc = position_in_ref_elem(M, e, x, xd);
+        xi[0] = (float)xd[0]; xi[1] = (float)xd[1]; xi[2] = (float)xd[2];
+        if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
+      }
+    }
+    {
+      float hi[32];
+      if (charged) {
+        const float ch = (float)c_k.qm[sp];
+        const float TS[4] = {v[0] * ch, v[1] * ch, v[2] * ch, ch};
+        if (suc) {
+          const float a1 = 0.5f * (xi[0] + 1.0f), a2 = 0.5f * (xi[1] + 1.0f), a3 = 0.5f * (xi[2] + 1.0f);
+          const float b1 = 1.0f - a1, b2 = 1.0f - a2, b3 = 1.0f - a3;
+          const float w[8] = {b1 * b2 * b3, a1 * b2 * b3, a1 * a2 * b3, b1 * a2 * b3,
+                              b1 * b2 * a3, a1 * b2 * a3, a1 * a2 * a3, b1 * a2 * a3};
+#pragma unroll
+          for (int n = 0; n < 8; ++n)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) hi[4 * n + c] = TS[c] * w[n];
+        } else {
+          double TSd[4] = {(double)TS[0], (double)TS[1], (double)TS[2], (double)TS[3]};
+          double xd[3] = {0, 0, 0}, cd[32];
+          cvwm_contrib(M, e, false, xd, x, TSd, cd);
+#pragma unroll
+          for (int k = 0; k < 32; ++k) hi[k] = (float)cd[k];
+        }
+      }
+      cvwm_scatter_ts(M, charged, e, hi, NS);
+    }
+    if (!inside) return;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) Ff[c] = (float)c_k.ext[c];
+    if (charged) {
+      float Eo[3];
+      if (suc) {
+        eval_field_f<N>(E32 + (size_t)e * nd * 3, xi, Eo);
+      } else {
+        double Ed[3];
+        eval_field_dw<N>(M, E + (size_t)e * nd * 3, e, x, Ed);
+        Eo[0] = (float)Ed[0]; Eo[1] = (float)Ed[1]; Eo[2] = (float)Ed[2];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Ff[c] += Eo[c];
+    }
+    bool isnew = (fl & kNew) != 0;
+    boris_push_f(v, Ff, sp, isnew, (float)dt);
+    double xl[3] = {x[0], x[1], x[2]};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
+    int ne = tria_track(M, e, x, xl);
+    uint8_t nf = isnew ? (fl | kNew) : (fl & ~kNew);
+    if (ne < 0) {
+      nf &= ~kInside;
+      if (ne == -1) { atomicAdd(&st->n_lost, 1); flag_status(st, 0x01u); }
+      else flag_status(st, 0x04u);
+      ne = e;
+    }
+    P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+    P.elem[i] = ne;
+    P.flags[i] = nf;
+  }
+}
+
+// Node sums -> DOFs (pic_depo_method.f90:692-733): PartSource(1:4,k,l,m) of every element.
+template <int N>
+__global__ void k_node_to_dof(DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M.ne * nd) return;
+  const int e = t / nd, r = t - e * nd;
+  const int kk = r % n1, ll = (r / n1) % n1, mm = r / (n1 * n1);
+  const double a1 = c_k.fac_gp[kk], a2 = c_k.fac_gp[ll], a3 = c_k.fac_gp[mm];
+  double S[8][4];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
+    const double V = __ldg(M.node_vol + node);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double s = __ldg(NS + (size_t)node * 4 + c);
+      S[n][c] = V > 0.0 ? s / V : s;
+    }
+  }
+  double out[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    out[c] = S[0][c] * (1 - a1) * (1 - a2) * (1 - a3) + S[1][c] * (a1) * (1 - a2) * (1 - a3) +
+             S[2][c] * (a1) * (a2) * (1 - a3) + S[3][c] * (1 - a1) * (a2) * (1 - a3) +
+             S[4][c] * (1 - a1) * (1 - a2) * (a3) + S[5][c] * (a1) * (1 - a2) * (a3) +
+             S[6][c] * (a1) * (a2) * (a3) + S[7][c] * (1 - a1) * (a2) * (a3);
+  double2* o = reinterpret_cast<double2*>(PS + (size_t)t * 4);
+  o[0] = make_double2(out[0], out[1]);
+  o[1] = make_double2(out[2], out[3]);
+}
+
+// =============================================================================================
+// Separate loop pieces (the reference's individual routines)
+// =============================================================================================
+template <int N, bool MIXED>
+__global__ void __launch_bounds__(256) k_interpolate(DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
+                                                     const float* __restrict__ E32, DevStatus* st, bool refmap,
+                                                     bool cvwm) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  if (!(fl & kInside)) return;
+  const int sp = P.species[i];
+  if (c_k.q[sp] == 0.0) return;   // isInterpolateParticle
+  const int e = P.elem[i];
+  const double x[3] = {P.x[i], P.y[i], P.z[i]};
+  double F[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) F[c] = c_k.ext[c];
+  double Eo[3];
+  if constexpr (!MIXED) {
+    double xi[3];
+    bool suc = true;
+    if (!refmap) {
+      suc = position_in_ref_elem(M, e, x, xi);
+      if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
+    } else {
+      xi[0] = P.xi0[i]; xi[1] = P.xi1[i]; xi[2] = P.xi2[i];
+    }
+    const double* U = E + (size_t)e * nd * 3;
+    if (!suc && cvwm) eval_field_dw<N>(M, U, e, x, Eo);
+    else eval_field<N>(U, xi, Eo);
+  } else {
+    float xi[3];
+    bool suc = true;
+    if (!refmap) {
+      const double* b = M.bary + (size_t)e * 3;
+      const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
+      suc = position_in_ref_elem_f(MF, e, p, xi);
+      if (!suc) {
+        double xd[3];
+        suc = position_in_ref_elem(M, e, x, xd);
+        xi[0] = (float)xd[0]; xi[1] = (float)xd[1]; xi[2] = (float)xd[2];
+        if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
+      }
+    } else {
+      xi[0] = (float)P.xi0[i]; xi[1] = (float)P.xi1[i]; xi[2] = (float)P.xi2[i];
+    }
+    if (!suc && cvwm) {
+      eval_field_dw<N>(M, E + (size_t)e * nd * 3, e, x, Eo);
+    } else {
+      float Ef[3];
+      eval_field_f<N>(E32 + (size_t)e * nd * 3, xi, Ef);
+      Eo[0] = Ef[0]; Eo[1] = Ef[1]; Eo[2] = Ef[2];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) P.field[(size_t)c * P.cap + i] = F[c];
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_push(DevParticles P, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  if (!(fl & kInside)) return;
+  const int sp = P.species[i];
+  double x[3] = {P.x[i], P.y[i], P.z[i]};
+  P.lx[i] = x[0]; P.ly[i] = x[1]; P.lz[i] = x[2];      // LastPartPos (timedisc...:109-110)
+  P.last_elem[i] = P.elem[i];
+  bool isnew = (fl & kNew) != 0;
+  if constexpr (!MIXED) {
+    double F[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) F[c] = P.field[(size_t)c * P.cap + i];
+    double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+    boris_push(v, F, sp, isnew, dt);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
+  } else {
+    float F[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) F[c] = (float)P.field[(size_t)c * P.cap + i];
+    float v[3] = {P.vxf[i], P.vyf[i], P.vzf[i]};
+    boris_push_f(v, F, sp, isnew, (float)dt);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
+  }
+  P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+  P.flags[i] = isnew ? (fl | kNew) : (fl & ~kNew);
+}
+
+__global__ void __launch_bounds__(256) k_track_tria(DevMesh M, DevParticles P, DevStatus* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  if (!(fl & kInside)) return;
+  const int le = P.last_elem[i];
+  if (le < 0) return;
+  double x[3] = {P.x[i], P.y[i], P.z[i]};
+  double xl[3] = {P.lx[i], P.ly[i], P.lz[i]};
+  int ne = tria_track(M, le, x, xl);
+  if (ne < 0) {
+    P.flags[i] = fl & ~kInside;
+    if (ne == -1) { atomicAdd(&st->n_lost, 1); flag_status(st, 0x01u); }
+    else flag_status(st, 0x04u);
+    ne = le;
+  }
+  P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+  P.lx[i] = xl[0]; P.ly[i] = xl[1]; P.lz[i] = xl[2];
+  P.elem[i] = ne;
+}
+
+__global__ void __launch_bounds__(256) k_track_ref(DevMesh M, DevParticles P, DevStatus* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  if (!(fl & kInside)) return;
+  double x[3] = {P.x[i], P.y[i], P.z[i]};
+  double xl[3] = {P.lx[i], P.ly[i], P.lz[i]};
+  double xi[3];
+  bool tol = false;
+  const int ne = ref_track(M, P.last_elem[i], x, xl, xi, tol);
+  if (tol) { atomicAdd(&st->n_ref_tolerance, 1); flag_status(st, 0x08u); }
+  P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+  P.lx[i] = xl[0]; P.ly[i] = xl[1]; P.lz[i] = xl[2];
+  P.xi0[i] = xi[0]; P.xi1[i] = xi[1]; P.xi2[i] = xi[2];
+  P.elem[i] = ne;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_deposit_cvwm(DevMesh M, MeshF MF, DevParticles P, double* __restrict__ NS,
+                                                      DevStatus* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in_range = i < P.n;
+  const uint8_t fl = in_range ? P.flags[i] : 0;
+  const bool inside = (fl & kInside) != 0;
+  const int sp = inside ? P.species[i] : 0;
+  const bool charged = inside && (c_k.q[sp] != 0.0);
+  const int e = inside ? P.elem[i] : 0;
+  double x[3] = {0.0, 0.0, 0.0};
+  if (inside) { x[0] = P.x[i]; x[1] = P.y[i]; x[2] = P.z[i]; }
+  if constexpr (!MIXED) {
+    double contrib[32];
+    if (charged) {
+      double xi[3];
+      const bool suc = position_in_ref_elem(M, e, x, xi);
+      if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
+      const double ch = c_k.qm[sp];
+      const double TS[4] = {P.vx[i] * ch, P.vy[i] * ch, P.vz[i] * ch, ch};
+      cvwm_contrib(M, e, suc, xi, x, TS, contrib);
+    }
+    cvwm_scatter(M, charged, e, contrib, NS);
+  } else {
+    float hi[32];
+    if (charged) {
+      const double* b = M.bary + (size_t)e * 3;
+      const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
+      float xi[3];
+      bool suc = position_in_ref_elem_f(MF, e, p, xi);
+      const float ch = (float)c_k.qm[sp];
+      const float TS[4] = {P.vxf[i] * ch, P.vyf[i] * ch, P.vzf[i] * ch, ch};
+      if (!suc) {
+        double xd[3];
+        suc = position_in_ref_elem(M, e, x, xd);
+        if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
+        double TSd[4] = {TS[0], TS[1], TS[2], TS[3]}, cd[32];
+        cvwm_contrib(M, e, suc, xd, x, TSd, cd);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) hi[k] = (float)cd[k];
+      } else {
+        const float a1 = 0.5f * (xi[0] + 1.0f), a2 = 0.5f * (xi[1] + 1.0f), a3 = 0.5f * (xi[2] + 1.0f);
+        const float b1 = 1.0f - a1, b2 = 1.0f - a2, b3 = 1.0f - a3;
+        const float w[8] = {b1 * b2 * b3, a1 * b2 * b3, a1 * a2 * b3, b1 * a2 * b3,
+                            b1 * b2 * a3, a1 * b2 * a3, a1 * a2 * a3, b1 * a2 * a3};
+#pragma unroll
+        for (int n = 0; n < 8; ++n)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) hi[4 * n + c] = TS[c] * w[n];
+      }
+    }
+    cvwm_scatter_ts(M, charged, e, hi, NS);
+  }
+}
+
+// =============================================================================================
+// Counting sort by element (integer keys: element ids are exact)
+// =============================================================================================
+__global__ void k_hist(DevParticles P, int* __restrict__ count, int ne) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const int key = (P.flags[i] & kInside) ? P.elem[i] : ne;
+  atomicAdd(count + key, 1);
+}
+
+// single-CTA exclusive scan of count[0..n) into offset[0..n] (offset[n] = total)
+__global__ void __launch_bounds__(1024) k_scan(const int* __restrict__ count, int* __restrict__ offset,
+                                               int* __restrict__ cursor, int n) {
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int base = 0; base < n; base += 1024) {
+    const int idx = base + threadIdx.x;
+    const int v = idx < n ? count[idx] : 0;
+    int s = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(kFull, s, o);
+      if (lane >= o) s += t;
+    }
+    if (lane == 31) warp_tot[wid] = s;
+    __syncthreads();
+    if (wid == 0) {
+      int w = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, w, o);
+        if (lane >= o) w += t;
+      }
+      warp_tot[lane] = w;
+    }
+    __syncthreads();
+    const int excl = carry + (wid > 0 ? warp_tot[wid - 1] : 0) + s - v;
+    if (idx < n) { offset[idx] = excl; cursor[idx] = excl; }
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) offset[n] = carry;
+}
+
+// =============================================================================================
+// Shape-function deposition: pack particles by element, then gather per target element
+// =============================================================================================
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_sf_pack(DevParticles P, int* __restrict__ cursor, const double* __restrict__ dofc,
+                                                 SfPack K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  if (!(fl & kInside)) return;
+  const int sp = P.species[i];
+  const int e = P.elem[i];
+  const double qm = c_k.qm[sp];
+  const double x = P.x[i], y = P.y[i], z = P.z[i];
+  const int slot = atomicAdd(cursor + e, 1);
+  const double* c = dofc + (size_t)e * 3;
+  const float4 rel = make_float4((float)(x - __ldg(c)), (float)(y - __ldg(c + 1)), (float)(z - __ldg(c + 2)), 0.0f);
+  reinterpret_cast<float4*>(K.posf)[slot] = rel;
+  if constexpr (!MIXED) {
+    const double w = c_k.sf_w;
+    // Fac(1:3) = PartVelo*ChargeMPF, Fac(4) = ChargeMPF, Fac = Fac*w_sf (shapefunction_tools:78-100)
+    const double f0 = (P.vx[i] * qm) * w, f1 = (P.vy[i] * qm) * w, f2 = (P.vz[i] * qm) * w, f3 = qm * w;
+    K.pos[(size_t)slot * 3] = x; K.pos[(size_t)slot * 3 + 1] = y; K.pos[(size_t)slot * 3 + 2] = z;
+    double2* fp = reinterpret_cast<double2*>(K.fac + (size_t)slot * 4);
+    fp[0] = make_double2(f0, f1);
+    fp[1] = make_double2(f2, f3);
+  } else {
+    const float w = (float)(c_k.sf_w * qm);
+    reinterpret_cast<float4*>(K.facf)[slot] = make_float4(P.vxf[i] * w, P.vyf[i] * w, P.vzf[i] * w, w);
+  }
+}
+
+constexpr int kSfChunk = 256;
+
+template <int N>
+struct SfShape {
+  static constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  static constexpr int split = nd >= 128 ? 1 : 128 / nd;
+  static constexpr int threads = ((nd * split + 31) / 32) * 32;
+};
+
+// FP64 gather.  An FP32 pre-test on coordinates relative to the target element's DOF centre
+// discards pairs outside (1+1e-4) R; the rest is evaluated exactly as the reference does in FP64.
+template <int N>
+__global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh M, SfLists L, const int* __restrict__ off,
+                                                                        SfPack K, double* __restrict__ PS) {
+  using S = SfShape<N>;
+  constexpr int nd = S::nd, split = S::split;
+  __shared__ double s_pos[kSfChunk][3];
+  __shared__ double s_fac[kSfChunk][4];
+  __shared__ float4 s_rel[kSfChunk];
+  __shared__ double s_red[split > 1 ? S::threads : 1][4];
+  const int e = blockIdx.x;
+  const int t = threadIdx.x;
+  const int dof = t % nd, part = t / nd;
+  const bool active = t < nd * split;
+  const double* ce = L.dof_center + (size_t)e * 3;
+  const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
+  double xg[3] = {0, 0, 0};
+  float xgf[3] = {0, 0, 0};
+  if (active) {
+    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
+    xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
+    xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
+  }
+  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  const float R2f = (float)(R2 * (1.0 + 1.0e-4));
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const int p0 = __ldg(L.nb_off + e), p1 = __ldg(L.nb_off + e + 1);
+  for (int p = p0; p < p1; ++p) {
+    const int s = __ldg(L.nb_src + p);
+    double sh[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int k = c_k.pv_dir[d];
+      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+    }
+    const double* cs = L.dof_center + (size_t)s * 3;
+    const float ox = (float)((__ldg(cs) + sh[0]) - cex), oy = (float)((__ldg(cs + 1) + sh[1]) - cey),
+                oz = (float)((__ldg(cs + 2) + sh[2]) - cez);
+    const int b0 = __ldg(off + s), cnt = __ldg(off + s + 1) - b0;
+    for (int base = 0; base < cnt; base += kSfChunk) {
+      const int nl = min(kSfChunk, cnt - base);
+      __syncthreads();
+      for (int q = t; q < nl; q += S::threads) {
+        const size_t j = (size_t)b0 + base + q;
+        const float4 r = reinterpret_cast<const float4*>(K.posf)[j];
+        s_rel[q] = make_float4(r.x + ox, r.y + oy, r.z + oz, 0.0f);
+        s_pos[q][0] = K.pos[3 * j] + sh[0];
+        s_pos[q][1] = K.pos[3 * j + 1] + sh[1];
+        s_pos[q][2] = K.pos[3 * j + 2] + sh[2];
+        const double2* fp = reinterpret_cast<const double2*>(K.fac + 4 * j);
+        const double2 f01 = fp[0], f23 = fp[1];
+        s_fac[q][0] = f01.x; s_fac[q][1] = f01.y; s_fac[q][2] = f23.x; s_fac[q][3] = f23.y;
+      }
+      __syncthreads();
+      if (active) {
+        for (int q = part; q < nl; q += split) {
+          const float4 r = s_rel[q];
+          const float dx = r.x - xgf[0], dy = r.y - xgf[1], dz = r.z - xgf[2];
+          const float r2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (r2f <= R2f) {
+            const double d0 = s_pos[q][0] - xg[0], d1 = s_pos[q][1] - xg[1], d2 = s_pos[q][2] - xg[2];
+            const double r2 = (d0 * d0 + d1 * d1) + d2 * d2;
+            if (r2 <= R2) {
+              const double Sv = 1.0 - R2inv * r2;
+              double S1 = Sv * Sv;
+              for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+#pragma unroll
+              for (int c = 0; c < 4; ++c) acc[c] = acc[c] + S1 * s_fac[q][c];
+            }
+          }
+        }
+      }
+    }
+  }
+  if constexpr (split > 1) {
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s_red[t][c] = acc[c];
+    __syncthreads();
+    if (t < nd) {
+      for (int k = 1; k < split; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] = acc[c] + s_red[t + k * nd][c];
+    }
+  }
+  if (t < nd) {
+    double2* o = reinterpret_cast<double2*>(PS + ((size_t)e * nd + dof) * 4);
+    o[0] = make_double2(acc[0], acc[1]);
+    o[1] = make_double2(acc[2], acc[3]);
+  }
+}
+
+// Mixed gather: FP32 distances and weights, per-DOF TwoSum-compensated FP32 sums, FP64 result.
+template <int N>
+__global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh M, SfLists L, const int* __restrict__ off,
+                                                                         SfPack K, double* __restrict__ PS) {
+  using S = SfShape<N>;
+  constexpr int nd = S::nd, split = S::split;
+  __shared__ float4 s_rel[kSfChunk];
+  __shared__ float4 s_fac[kSfChunk];
+  __shared__ float s_red[split > 1 ? S::threads : 1][8];
+  const int e = blockIdx.x;
+  const int t = threadIdx.x;
+  const int dof = t % nd, part = t / nd;
+  const bool active = t < nd * split;
+  const double* ce = L.dof_center + (size_t)e * 3;
+  const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
+  float xgf[3] = {0, 0, 0};
+  if (active) {
+    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
+    xgf[0] = (float)(__ldg(g) - cex); xgf[1] = (float)(__ldg(g + 1) - cey); xgf[2] = (float)(__ldg(g + 2) - cez);
+  }
+  const float R2 = (float)c_k.sf_r2, R2inv = (float)c_k.sf_r2_inv;
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  const int p0 = __ldg(L.nb_off + e), p1 = __ldg(L.nb_off + e + 1);
+  for (int p = p0; p < p1; ++p) {
+    const int s = __ldg(L.nb_src + p);
+    double sh[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int k = c_k.pv_dir[d];
+      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+    }
+    const double* cs = L.dof_center + (size_t)s * 3;
+    const float ox = (float)((__ldg(cs) + sh[0]) - cex), oy = (float)((__ldg(cs + 1) + sh[1]) - cey),
+                oz = (float)((__ldg(cs + 2) + sh[2]) - cez);
+    const int b0 = __ldg(off + s), cnt = __ldg(off + s + 1) - b0;
+    for (int base = 0; base < cnt; base += kSfChunk) {
+      const int nl = min(kSfChunk, cnt - base);
+      __syncthreads();
+      for (int q = t; q < nl; q += S::threads) {
+        const size_t j = (size_t)b0 + base + q;
+        const float4 r = reinterpret_cast<const float4*>(K.posf)[j];
+        s_rel[q] = make_float4(r.x + ox, r.y + oy, r.z + oz, 0.0f);
+        s_fac[q] = reinterpret_cast<const float4*>(K.facf)[j];
+      }
+      __syncthreads();
+      if (active) {
+        for (int q = part; q < nl; q += split) {
+          const float4 r = s_rel[q];
+          const float dx = r.x - xgf[0], dy = r.y - xgf[1], dz = r.z - xgf[2];
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (r2 <= R2) {
+            const float Sv = fmaf(-R2inv, r2, 1.0f);
+            float S1 = Sv * Sv;
+            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            const float4 f = s_fac[q];
+            const float fc[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              float sm, er;
+              two_sum(hi[c], S1 * fc[c], sm, er);
+              hi[c] = sm;
+              lo[c] += er;
+            }
+          }
+        }
+      }
+    }
+  }
+  double acc[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) acc[c] = (double)hi[c] + (double)lo[c];
+  if constexpr (split > 1) {
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { s_red[t][c] = hi[c]; s_red[t][4 + c] = lo[c]; }
+    __syncthreads();
+    if (t < nd) {
+      for (int k = 1; k < split; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] = acc[c] + ((double)s_red[t + k * nd][c] + (double)s_red[t + k * nd][4 + c]);
+    }
+  }
+  if (t < nd) {
+    double2* o = reinterpret_cast<double2*>(PS + ((size_t)e * nd + dof) * 4);
+    o[0] = make_double2(acc[0], acc[1]);
+    o[1] = make_double2(acc[2], acc[3]);
+  }
+}
+
+// =============================================================================================
+// Fused remainder for RefTracking: interpolation at PartPosRef + push + RefTracking
+// =============================================================================================
+template <int N, bool MIXED>
+__global__ void __launch_bounds__(256) k_step_ref(DevMesh M, DevParticles P, const double* __restrict__ E,
+                                                  const float* __restrict__ E32, double dt, DevStatus* st) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  if (!(fl & kInside)) return;
+  const int sp = P.species[i];
+  const bool charged = c_k.q[sp] != 0.0;
+  const int e = P.elem[i];
+  double x[3] = {P.x[i], P.y[i], P.z[i]};
+  double xi[3] = {P.xi0[i], P.xi1[i], P.xi2[i]};
+  bool isnew = (fl & kNew) != 0;
+  if constexpr (!MIXED) {
+    double F[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) F[c] = c_k.ext[c];
+    if (charged) {
+      double Eo[3];
+      eval_field<N>(E + (size_t)e * nd * 3, xi, Eo);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
+    }
+    double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
+    boris_push(v, F, sp, isnew, dt);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
+  } else {
+    float F[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) F[c] = (float)c_k.ext[c];
+    if (charged) {
+      float Eo[3];
+      const float xf[3] = {(float)xi[0], (float)xi[1], (float)xi[2]};
+      eval_field_f<N>(E32 + (size_t)e * nd * 3, xf, Eo);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) F[c] += Eo[c];
+    }
+    float v[3] = {P.vxf[i], P.vyf[i], P.vzf[i]};
+    boris_push_f(v, F, sp, isnew, (float)dt);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
+  }
+  double xl[3] = {P.x[i], P.y[i], P.z[i]};
+  bool tol = false;
+  const int ne = ref_track(M, e, x, xl, xi, tol);
+  if (tol) { atomicAdd(&st->n_ref_tolerance, 1); flag_status(st, 0x08u); }
+  P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+  P.xi0[i] = xi[0]; P.xi1[i] = xi[1]; P.xi2[i] = xi[2];
+  P.elem[i] = ne;
+  P.flags[i] = isnew ? (fl | kNew) : (fl & ~kNew);
+}
+
+// =============================================================================================
+// Reorder the particle arrays by element (counting-sort scatter)
+// =============================================================================================
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_reorder(DevParticles P, DevParticles Q, const int* __restrict__ perm_in,
+                                                 int* __restrict__ perm_out, int* __restrict__ cursor, int ne) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const uint8_t fl = P.flags[i];
+  const int key = (fl & kInside) ? P.elem[i] : ne;
+  const int j = atomicAdd(cursor + key, 1);
+  Q.x[j] = P.x[i]; Q.y[j] = P.y[i]; Q.z[j] = P.z[i];
+  if constexpr (!MIXED) { Q.vx[j] = P.vx[i]; Q.vy[j] = P.vy[i]; Q.vz[j] = P.vz[i]; }
+  else { Q.vxf[j] = P.vxf[i]; Q.vyf[j] = P.vyf[i]; Q.vzf[j] = P.vzf[i]; }
+  Q.xi0[j] = P.xi0[i]; Q.xi1[j] = P.xi1[i]; Q.xi2[j] = P.xi2[i];
+  Q.elem[j] = P.elem[i];
+  Q.last_elem[j] = P.last_elem[i];
+  Q.species[j] = P.species[i];
+  Q.flags[j] = fl;
+  perm_out[j] = perm_in[i];
+}
+
+__global__ void __launch_bounds__(256) k_map_particles(DevMesh M, DevParticles P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  if (!(P.flags[i] & kInside)) return;
+  const double x[3] = {P.x[i], P.y[i], P.z[i]};
+  double xi[3];
+  position_in_ref_elem(M, P.elem[i], x, xi);
+  P.xi0[i] = xi[0]; P.xi1[i] = xi[1]; P.xi2[i] = xi[2];
+}
+
+__global__ void k_count_inside(DevParticles P, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int v = (i < P.n && (P.flags[i] & kInside)) ? 1 : 0;
+  v = __reduce_add_sync(kFull, v);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
+}
+
+// =============================================================================================
+// launch wrappers
+// =============================================================================================
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+#define PIC_DISPATCH_N(Nv, ...)                               \
+  switch (Nv) {                                               \
+    case 1: { constexpr int NN = 1; __VA_ARGS__; } break;     \
+    case 2: { constexpr int NN = 2; __VA_ARGS__; } break;     \
+    case 3: { constexpr int NN = 3; __VA_ARGS__; } break;     \
+    case 4: { constexpr int NN = 4; __VA_ARGS__; } break;     \
+    default: break;                                           \
+  }
+
+int launch_node_to_dof(const LaunchArgs& A, double* PS) {
+  PIC_DISPATCH_N(A.N, { k_node_to_dof<NN><<<nblk(A.M.ne * A.nd, 256), 256, 0, A.s>>>(A.M, A.NS, PS); });
+  return 1;
+}
+
+int launch_cvwm_fused(const LaunchArgs& A, const DevParticles& P, double dt) {
+  cudaMemsetAsync(A.NS, 0, sizeof(double) * 4 * (size_t)A.n_canon, A.s);
+  if (P.n <= 0) return 0;
+  PIC_DISPATCH_N(A.N, {
+    if (A.mixed) k_step_cvwm_tria<NN, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.NS, dt, A.st);
+    else k_step_cvwm_tria<NN, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.NS, dt, A.st);
+  });
+  return 1;
+}
+
+int launch_step_cvwm_tria(const LaunchArgs& A, const DevParticles& P, double* PS, double dt) {
+  int launches = launch_cvwm_fused(A, P, dt);
+  if (PS) launches += launch_node_to_dof(A, PS);
+  return launches;
+}
+
+int launch_interpolate(const LaunchArgs& A, const DevParticles& P, bool refmap, bool cvwm) {
+  if (P.n <= 0) return 0;
+  PIC_DISPATCH_N(A.N, {
+    if (A.mixed) k_interpolate<NN, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.st, refmap, cvwm);
+    else k_interpolate<NN, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.st, refmap, cvwm);
+  });
+  return 1;
+}
+
+int launch_push(const LaunchArgs& A, const DevParticles& P, double dt) {
+  if (P.n <= 0) return 0;
+  if (A.mixed) k_push<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt);
+  else k_push<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt);
+  return 1;
+}
+
+int launch_track(const LaunchArgs& A, const DevParticles& P, bool refmap) {
+  if (P.n <= 0) return 0;
+  if (refmap) k_track_ref<<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
+  else k_track_tria<<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
+  return 1;
+}
+
+int launch_deposit_cvwm(const LaunchArgs& A, const DevParticles& P, double* PS) {
+  int launches = 0;
+  cudaMemsetAsync(A.NS, 0, sizeof(double) * 4 * (size_t)A.n_canon, A.s);
+  if (P.n > 0) {
+    if (A.mixed) k_deposit_cvwm<true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.NS, A.st);
+    else k_deposit_cvwm<false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.NS, A.st);
+    launches++;
+  }
+  return launches + launch_node_to_dof(A, PS);
+}
+
+int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B) {
+  cudaMemsetAsync(B.count, 0, sizeof(int) * (B.ne + 1), A.s);
+  if (P.n > 0) k_hist<<<nblk(P.n, 256), 256, 0, A.s>>>(P, B.count, B.ne);
+  k_scan<<<1, 1024, 0, A.s>>>(B.count, B.offset, B.cursor, B.ne + 1);
+  return P.n > 0 ? 2 : 1;
+}
+
+int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K) {
+  int launches = launch_sort_offsets(A, P, B);
+  if (P.n > 0) {
+    if (A.mixed) k_sf_pack<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, B.cursor, L.dof_center, K);
+    else k_sf_pack<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, B.cursor, L.dof_center, K);
+    launches++;
+  }
+  return launches;
+}
+
+int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
+  PIC_DISPATCH_N(A.N, {
+    if (A.mixed) k_sf_gather_mixed<NN><<<A.M.ne, SfShape<NN>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+    else k_sf_gather_fp64<NN><<<A.M.ne, SfShape<NN>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  });
+  return 1;
+}
+
+int launch_deposit_sf(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L,
+                      const SfPack& K, double* PS) {
+  return launch_sf_pack(A, P, B, L, K) + launch_sf_gather(A, B, L, K, PS);
+}
+
+int launch_step_ref(const LaunchArgs& A, const DevParticles& P, double dt) {
+  if (P.n <= 0) return 0;
+  PIC_DISPATCH_N(A.N, {
+    if (A.mixed) k_step_ref<NN, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.E, A.E32, dt, A.st);
+    else k_step_ref<NN, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.E, A.E32, dt, A.st);
+  });
+  return 1;
+}
+
+int launch_reorder(const LaunchArgs& A, DevParticles& P, DevParticles& Q, int* perm, int* perm_tmp,
+                   const SortBuffers& B) {
+  if (P.n <= 0) return 0;
+  int launches = launch_sort_offsets(A, P, B);
+  if (A.mixed) k_reorder<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, Q, perm, perm_tmp, B.cursor, B.ne);
+  else k_reorder<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, Q, perm, perm_tmp, B.cursor, B.ne);
+  return launches + 1;
+}
+
+int launch_map_particles(const LaunchArgs& A, const DevParticles& P) {
+  if (P.n <= 0) return 0;
+  k_map_particles<<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P);
+  return 1;
+}
+
+cudaError_t upload_consts(const Consts& k) { return cudaMemcpyToSymbol(c_k, &k, sizeof(Consts)); }
+
+int launch_count_inside(const LaunchArgs& A, const DevParticles& P, int* out) {
+  cudaMemsetAsync(out, 0, sizeof(int), A.s);
+  if (P.n <= 0) return 0;
+  k_count_inside<<<nblk(P.n, 256), 256, 0, A.s>>>(P, out);
+  return 1;
+}
+
+}  // namespace pic

@@ -1,0 +1,73 @@
+// pic_kernels.cuh -- kernel declarations shared by the C-ABI layer and the kernel units.
+#pragma once
+#include "pic_device.cuh"
+
+namespace pic {
+
+// FP32 copies of the mapping data (mixed variant, linear uncurved elements)
+struct MeshF {
+  const float* xclr;   // [ne][8][3] corners minus barycentre
+  const float* dxcl;   // [ne][8][9]
+  const float* xez;    // [ne][6][3]
+  const float* slen;   // [ne][6]
+};
+
+// everything a launch needs besides the particle arrays
+struct LaunchArgs {
+  DevMesh M;
+  MeshF MF;
+  int N, nd, n_canon;
+  bool mixed;
+  const double* E;       // [ne][nd][3]
+  const float* E32;      // [ne][nd][3] (mixed)
+  double* NS;            // [n_canon][4] CVWM node sums
+  DevStatus* st;
+  cudaStream_t s;
+};
+
+// counting sort by element
+struct SortBuffers {
+  int* count;        // [ne+1]
+  int* offset;       // [ne+2]
+  int* cursor;       // [ne+1]
+  int ne;
+};
+
+// shape-function deposition (gather over element neighbour lists)
+struct SfLists {
+  const int* nb_off;      // [ne+1]
+  const int* nb_src;      // [n_pairs] source element (0-based)
+  const int8_t* nb_shift; // [n_pairs][3] periodic image in units of the periodic vectors
+  int n_pairs;
+  const double* dof_center;   // [ne][3] centre of the element's DOF bounding box
+};
+struct SfPack {
+  double* pos;     // [cap][3] FP64 position (FP64 variant)
+  double* fac;     // [cap][4] w_sf*q*MPF*(v,1) (FP64 variant)
+  float* posf;     // [cap][4] position relative to the source element's DOF centre (FP32), 4th = pad
+  float* facf;     // [cap][4] (mixed variant)
+};
+
+// Launch wrappers; each returns the number of kernels it launched.
+int launch_interpolate(const LaunchArgs& A, const DevParticles& P, bool refmap, bool cvwm);
+int launch_push(const LaunchArgs& A, const DevParticles& P, double dt);
+int launch_track(const LaunchArgs& A, const DevParticles& P, bool refmap);
+int launch_deposit_cvwm(const LaunchArgs& A, const DevParticles& P, double* part_source);
+// fused: Deposition (CVWM) + InterpolateFieldToParticle + push + TriaTracking
+int launch_step_cvwm_tria(const LaunchArgs& A, const DevParticles& P, double* part_source, double dt);
+int launch_cvwm_fused(const LaunchArgs& A, const DevParticles& P, double dt);
+int launch_node_to_dof(const LaunchArgs& A, double* part_source);
+int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B);
+int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K);
+int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* part_source);
+int launch_deposit_sf(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L,
+                      const SfPack& K, double* part_source);
+// fused remainder for RefTracking: interpolation at PartPosRef + push + RefTracking
+int launch_step_ref(const LaunchArgs& A, const DevParticles& P, double dt);
+int launch_reorder(const LaunchArgs& A, DevParticles& P, DevParticles& Q, int* perm, int* perm_tmp,
+                   const SortBuffers& B);
+int launch_map_particles(const LaunchArgs& A, const DevParticles& P);
+int launch_count_inside(const LaunchArgs& A, const DevParticles& P, int* out);
+cudaError_t upload_consts(const Consts& k);
+
+}  // namespace pic

@@ -1,0 +1,73 @@
+"""CPU tests of the drop-in boundary: the C-ABI library loads and exports every declared symbol,
+and the host-side checks reject bad input before any device work."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from piclas_gb300 import EXPORTED_SYMBOLS, build, capi, library_path, load_library
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "piclas_gpu.h")
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pic_[a-z_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return load_library()
+
+
+def test_header_matches_python_binding():
+    assert header_functions() == sorted(EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", library_path()], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (pic_[a-z_]+)\b", out))
+    missing = [s for s in header_functions() if s not in exported]
+    assert not missing, missing
+    for s in header_functions():
+        assert hasattr(lib, s)
+
+
+def test_version_and_error_string(lib):
+    assert b"sm_103a" in lib.pic_version()
+    assert isinstance(lib.pic_last_error(), bytes)
+
+
+def test_null_arguments_rejected_without_device_work(lib):
+    h = C.c_void_p()
+    assert lib.pic_create(None, None, C.byref(h)) == 1          # PIC_ERR_INVALID_ARGUMENT
+    assert lib.pic_step(None, 1e-12, 1, None) == 1
+    assert lib.pic_deposit(None, None) == 1
+    assert lib.pic_get_status(None, None) == 1
+    lib.pic_destroy(None)                                       # no-op
+
+
+def test_bad_options_rejected(lib):
+    from piclas_gb300.mesh import build_box_mesh
+    mesh = build_box_mesh(2, 2, 2, 1)
+    ms = capi.MeshStruct(mesh)
+    h = C.c_void_p()
+    cfg = capi.make_config(9, 1, 1, 0, [(-1.0, 1.0, 1.0)], 10)     # N = 9 unsupported
+    assert lib.pic_create(C.byref(cfg), ms.ptr, C.byref(h)) == 1
+    cfg = capi.make_config(1, 7, 1, 0, [(-1.0, 1.0, 1.0)], 10)     # unknown tracking
+    assert lib.pic_create(C.byref(cfg), ms.ptr, C.byref(h)) == 1
+    cfg = capi.make_config(1, 1, 2, 0, [(-1.0, 1.0, 1.0)], 10, sf_radius=0.0)   # SF without radius
+    assert lib.pic_create(C.byref(cfg), ms.ptr, C.byref(h)) == 1
+    assert b"radius" in lib.pic_last_error()
+
+
+def test_struct_sizes_match_c():
+    # pic_config_t: 6 ints + 3*8 + 6 doubles + 2 doubles + 2 ints
+    assert C.sizeof(capi.PicConfig) == 6 * 4 + 3 * 8 * 8 + 6 * 8 + 2 * 8 + 2 * 4
+    assert C.sizeof(capi.PicStatus) == 24

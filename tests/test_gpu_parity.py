@@ -1,0 +1,224 @@
+"""GPU parity: libpiclas_gpu.so (through the C-ABI) against the CPU oracle on seeded inputs.
+
+Tolerances (FP64 variant): element ids bit-exact; positions and velocities bit-exact on the
+CVWM/TriaTracking path (same evaluation order, no FMA contraction on either side) and within
+1e-13 relative on the B-field path (CUDA's tan may differ from libm's in the last bit);
+PartSource within 1e-12 of its maximum (atomic summation order).
+Mixed variant: relative charge-density error <= 1e-6 against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from piclas_gb300 import ParticleLoop, PicError, capi, workloads
+from piclas_gb300.mesh import build_box_mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_gpu(w, nsteps, precision=capi.PIC_PREC_FP64, dt=None, sort_interval=0):
+    cfg = w.config(precision=precision, sort_interval=sort_interval)
+    loop = ParticleLoop(cfg, w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    loop.time_step(dt or w.dt, nsteps, PS)
+    out = loop.download_particles(with_ref=True)
+    out["PS"] = PS
+    out["status"] = loop.status()
+    loop.close()
+    return out
+
+
+def _run_oracle(oracle, w, nsteps, dt=None):
+    cfg = w.config()
+    ms = capi.MeshStruct(w.mesh)
+    st = oracle.OracleState(w.part_state, w.elem, w.part_species)
+    if w.tracking == capi.PIC_TRACK_REFMAPPING:
+        oracle.map_particles(cfg, ms, st)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle.step(cfg, ms, w.e_dof, st, dt or w.dt, nsteps, PS)
+    return st, PS
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_plasma_wave_fp64_bitexact(gpu_lib, oracle_lib):
+    w = workloads.plasma_wave(n_cells=8, N=3, n_particles=20000, nsteps=10, seed=0, T_eV=200.0)
+    g = _run_gpu(w, 10)
+    st, PS = _run_oracle(oracle_lib, w, 10)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["n_lost"] == 0 and g["status"]["error_word"] == 0
+    assert (st.elem != w.elem).sum() > 50          # the walk crossed faces, incl. periodic ones
+
+
+def test_plasma_wave_with_resort(gpu_lib, oracle_lib):
+    w = workloads.plasma_wave(n_cells=4, N=2, n_particles=5000, nsteps=6, seed=4, T_eV=500.0)
+    g = _run_gpu(w, 6, sort_interval=2)
+    st, PS = _run_oracle(oracle_lib, w, 6)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+
+
+def test_pieces_match_oracle(gpu_lib, oracle_lib):
+    """interpolate / push / track / deposit called one by one, as the Fortran host would."""
+    w = workloads.plasma_wave(n_cells=4, N=3, n_particles=3000, seed=7, T_eV=100.0)
+    cfg = w.config()
+    ms = capi.MeshStruct(w.mesh)
+    loop = ParticleLoop(cfg, w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PSo = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PSo)
+    PSg = loop.deposition()
+    assert _rel(PSg, PSo) <= 1e-12
+    oracle_lib.save_last(st)
+    oracle_lib.interpolate(cfg, ms, w.e_dof, st)
+    loop.interpolate_field_to_particle()
+    assert np.array_equal(loop.field_at_particles(), st.field)
+    oracle_lib.push(cfg, st, w.dt)
+    loop.push(w.dt)
+    oracle_lib.track(cfg, ms, st)
+    loop.perform_tracking()
+    g = loop.download_particles()
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert np.array_equal(g["elem"], st.elem)
+    loop.close()
+
+
+def test_curved_sf_reftracking_fp64(gpu_lib, oracle_lib):
+    w = workloads.curved_two_species(n_cells=6, n_per_species=2000, seed=3, Te_eV=1000.0, nsteps=4)
+    g = _run_gpu(w, 4, dt=2e-11)
+    st, PS = _run_oracle(oracle_lib, w, 4, dt=2e-11)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
+    assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
+    assert _rel(g["part_pos_ref"], st.part_pos_ref) <= 1e-10
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0
+
+
+def test_cvwm_kat_on_gpu(gpu_lib):
+    """Plasma_Ball_cell_volweight_mean: integral of the deposited charge = 10.68010874898 C."""
+    import json, os
+    import oracle
+    k = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")))["cvwm_plasma_ball"]
+    from test_oracle import _plasma_ball
+    mesh, cfg, ps, elem = _plasma_ball({"cvwm_plasma_ball": k})
+    loop = ParticleLoop(cfg, mesh)
+    loop.upload_particles(ps, elem, np.ones(len(elem), np.int32))
+    PS = loop.deposition()
+    q = oracle.integrate_charge(capi.MeshStruct(mesh), mesh.N, PS)
+    assert abs(q - k["total_charge"]) <= k["tolerance_abs"]
+    loop.close()
+
+
+def test_mixed_precision_rho_error(gpu_lib, oracle_lib):
+    w = workloads.plasma_wave(n_cells=8, N=3, n_particles=50000, nsteps=5, seed=1)
+    g = _run_gpu(w, 5, precision=capi.PIC_PREC_MIXED)
+    st, PS = _run_oracle(oracle_lib, w, 5)
+    rho_err = _rel(g["PS"][..., 3], PS[..., 3])
+    assert rho_err <= 1e-6, rho_err
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-9
+    assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-5
+
+
+def test_mixed_sf_rho_error(gpu_lib, oracle_lib):
+    w = workloads.curved_two_species(n_cells=6, n_per_species=3000, seed=5, nsteps=2)
+    g = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
+    st, PS = _run_oracle(oracle_lib, w, 2)
+    # electrons and ions cancel; compare each output against the species-summed magnitude
+    assert _rel(g["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert np.array_equal(g["elem"], st.elem)
+
+
+# ---- edge cases ------------------------------------------------------------------------------
+def test_empty_particle_set(gpu_lib):
+    w = workloads.plasma_wave(n_cells=2, N=1, n_particles=10)
+    loop = ParticleLoop(w.config(max_particles=10), w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(np.zeros((0, 6)), np.zeros(0, np.int32), np.zeros(0, np.int32))
+    PS = loop.deposition()
+    assert np.all(PS == 0.0)
+    loop.time_step(1e-11, 3)
+    assert loop.status()["n_inside"] == 0
+    loop.close()
+
+
+def test_capacity_and_bad_ids_rejected(gpu_lib):
+    w = workloads.plasma_wave(n_cells=2, N=1, n_particles=10)
+    loop = ParticleLoop(w.config(max_particles=5), w.mesh)
+    with pytest.raises(PicError) as e:
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+    assert e.value.code == 6
+    bad = w.elem[:5].copy()
+    bad[2] = 99
+    with pytest.raises(PicError) as e:
+        loop.upload_particles(w.part_state[:5], bad, w.part_species[:5])
+    assert e.value.code == 1
+    nan = w.part_state[:5].copy()
+    nan[1, 0] = np.nan
+    with pytest.raises(PicError):
+        loop.upload_particles(nan, w.elem[:5], w.part_species[:5])
+    with pytest.raises(PicError) as e:
+        loop.time_step(1e-11, 1)                  # no field, no particles yet
+    assert e.value.code == 5
+    loop.close()
+
+
+def test_particles_on_faces_nodes_and_holes(gpu_lib, oracle_lib):
+    """Particles exactly on element faces, edges and corners (incl. periodic ones), plus holes."""
+    mesh = build_box_mesh(4, 4, 4, 2)
+    pts = []
+    for x in (0.0, 0.25, 0.5, 0.999999999, 1.0):
+        for y in (0.0, 0.25, 0.75):
+            pts.append((x, y, 0.5))
+            pts.append((x, y, 0.0))
+    x = np.array(pts)
+    n = len(x)
+    rng = np.random.default_rng(0)
+    v = rng.normal(0, 4e5, size=(n, 3))
+    ps = np.ascontiguousarray(np.concatenate([x, v], axis=1))
+    elem = workloads._elem_of_uniform(mesh, np.minimum(x, np.nextafter(1.0, 0)))
+    inside = np.ones(n, np.uint8)
+    inside[::7] = 0                              # holes in the particle vector
+    cfg = capi.make_config(2, capi.PIC_TRACK_TRIA, capi.PIC_DEPO_CVWM, capi.PIC_PREC_FP64,
+                           [(workloads.Q_ELECTRON, workloads.M_ELECTRON, 1e5)], n)
+    e_dof = np.zeros((mesh.n_elems, mesh.n_dof, 3))
+    loop = ParticleLoop(cfg, mesh)
+    loop.set_field(e_dof)
+    loop.upload_particles(ps, elem, np.ones(n, np.int32), inside=inside)
+    PSg = np.zeros((mesh.n_elems, mesh.n_dof, 4))
+    loop.time_step(5e-11, 3, PSg)
+    g = loop.download_particles()
+    ms = capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(ps, elem, np.ones(n, np.int32), inside=inside)
+    PSo = np.zeros_like(PSg)
+    oracle_lib.step(cfg, ms, e_dof, st, 5e-11, 3, PSo)
+    assert np.array_equal(g["elem"][inside == 1], st.elem[inside == 1])
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["part_state"][inside == 1], st.part_state[inside == 1])
+    assert _rel(PSg, PSo) <= 1e-12
+    loop.close()
+
+
+def test_full_size_plasma_wave_properties(gpu_lib):
+    """200k electrons, 8^3, N=3, 100 steps: charge conservation each run, elements consistent
+    with the geometry (uniform cubes), nothing lost."""
+    import oracle
+    w = workloads.plasma_wave()
+    for prec in (capi.PIC_PREC_FP64, capi.PIC_PREC_MIXED):
+        g = _run_gpu(w, w.nsteps, precision=prec, sort_interval=10)
+        assert g["status"]["n_lost"] == 0 and g["status"]["error_word"] == 0
+        x = g["part_state"][:, :3]
+        assert np.array_equal(workloads._elem_of_uniform(w.mesh, x), g["elem"])
+        q = oracle.integrate_charge(capi.MeshStruct(w.mesh), w.mesh.N, g["PS"])
+        total = w.n * w.species[0][0] * w.species[0][2]
+        assert abs(q - total) <= 1e-10 * abs(total)

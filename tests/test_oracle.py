@@ -1,0 +1,165 @@
+"""CPU tests: the oracle against the reference's known answers and analytic solutions."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from piclas_gb300 import capi, workloads
+from piclas_gb300.mesh import (barycentric_weights, build_box_mesh, cheby_gauss_lobatto_nodes, elem_map,
+                               lagrange_polys, legendre_gauss_nodes)
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")
+
+
+@pytest.fixture(scope="module")
+def kat():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+# ---- basis (basis.f90) -----------------------------------------------------------------------
+def test_gauss_nodes_are_legendre_roots():
+    for N in (1, 2, 3, 4):
+        x, w = legendre_gauss_nodes(N)
+        ref, wref = np.polynomial.legendre.leggauss(N + 1)
+        assert np.allclose(x, ref, atol=1e-15, rtol=0)
+        assert np.allclose(w, wref, atol=2e-15, rtol=0)
+
+
+def test_lagrange_kronecker_and_partition(oracle_lib):
+    x, _ = legendre_gauss_nodes(3)
+    wb = barycentric_weights(x)
+    for i, xi in enumerate(x):
+        L = oracle_lib.lagrange_polys(xi, x, wb)
+        assert np.array_equal(L, np.eye(4)[i])          # ALMOSTEQUAL_UNITY branch
+    for t in np.linspace(-0.99, 0.99, 17):
+        L = oracle_lib.lagrange_polys(t, x, wb)
+        assert abs(L.sum() - 1.0) < 1e-15
+        assert np.allclose(L, lagrange_polys(t, x, wb), rtol=0, atol=0)   # C and Python restatements agree
+
+
+def test_cl_nodes_ngeo1():
+    assert cheby_gauss_lobatto_nodes(1) == [-1.0, 1.0]
+    assert barycentric_weights([-1.0, 1.0]) == [-0.5, 0.5]
+
+
+# ---- cell_volweight_mean charge conservation (Plasma_Ball_cell_volweight_mean) ---------------
+def _plasma_ball(kat, seed=0):
+    k = kat["cvwm_plasma_ball"]
+    mesh = build_box_mesh(10, 10, 10, k["N"], lo=(-1, -1, -1), hi=(1, 1, 1))
+    rng = np.random.default_rng(seed)
+    n = k["n_particles"]
+    # uniform in a sphere of RadiusIC around the origin
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    r = k["sphere_radius"] * rng.random(n) ** (1.0 / 3.0)
+    x = d * r[:, None]
+    ps = np.concatenate([x, np.zeros((n, 3))], axis=1)
+    elem = workloads._elem_of_uniform(mesh, x)
+    cfg = capi.make_config(k["N"], capi.PIC_TRACK_TRIA, capi.PIC_DEPO_CVWM, capi.PIC_PREC_FP64,
+                           [(k["charge_ic"], 1.0, k["mpf"])], n)
+    return mesh, cfg, ps, elem
+
+
+def test_cvwm_total_charge_kat(oracle_lib, kat):
+    k = kat["cvwm_plasma_ball"]
+    mesh, cfg, ps, elem = _plasma_ball(kat)
+    ms = capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(ps, elem, np.ones(len(elem), np.int32))
+    PS = np.zeros((mesh.n_elems, mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS)
+    q = oracle_lib.integrate_charge(ms, mesh.N, PS)
+    assert abs(q - k["total_charge"]) <= k["tolerance_abs"], (q, k["total_charge"])
+
+
+def test_cvwm_charge_conservation_periodic_twins(oracle_lib):
+    """Particles everywhere (incl. periodic corners): the integral still equals the charge."""
+    w = workloads.plasma_wave(n_cells=4, N=2, n_particles=3000, seed=3)
+    ms = capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(w.config(), ms, st, PS)
+    total = w.n * w.species[0][0] * w.species[0][2]
+    assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - total) <= 1e-13 * abs(total)
+
+
+# ---- Boris push convergence (NIG_convtest_t_poisson constant B_z, orders 2) -------------------
+def _gyration_error(oracle_lib, case, dt, use_gamma):
+    q, m = case["charge"], case["mass"]
+    if use_gamma:
+        g = case["gamma"]
+        vperp = workloads.C_LIGHT * math.sqrt(1.0 - 1.0 / g ** 2)
+        B = g * vperp
+        omega = abs(q) * B / (g * m)
+    else:
+        vperp, B = 1.0, 1.0
+        omega = abs(q) * B / m
+    rc = vperp / omega
+    phi = math.atan2(case["base_point"][1], case["base_point"][0])
+    # InitAnalyticalParticleState (pic_interpolation.f90:572-584): x(0) and v(-dt/2) from the
+    # analytic solution, IsNewPart = .FALSE.
+    x0 = np.array([math.cos(phi) * rc, math.sin(phi) * rc, 0.0])
+    th = omega * (-0.5 * dt) + phi
+    v0 = np.array([-math.sin(th) * vperp, math.cos(th) * vperp, 0.0])
+    cfg = capi.make_config(1, capi.PIC_TRACK_TRIA, capi.PIC_DEPO_CVWM, capi.PIC_PREC_FP64, [(q, m, 1.0)], 1)
+    st = oracle_lib.OracleState(np.concatenate([x0, v0])[None, :], np.array([1]), np.array([1]),
+                                is_new=np.zeros(1, np.uint8))
+    st.field[0, 5] = B
+    nsteps = int(round(case["tend"] / dt))
+    for _ in range(nsteps):
+        oracle_lib.push(cfg, st, dt)
+    t = nsteps * dt
+    ex = np.array([math.cos(omega * t + phi) * rc, math.sin(omega * t + phi) * rc, 0.0])
+    return np.linalg.norm(st.part_state[0, :3] - ex) / rc
+
+
+@pytest.mark.parametrize("which", ["nonrel", "rel"])
+def test_boris_second_order(oracle_lib, kat, which):
+    case = kat["boris_gyration_" + which]
+    dts = case["dt"][1:4] if which == "nonrel" else case["dt"][:3]
+    errs = [_gyration_error(oracle_lib, case, dt, which == "rel") for dt in dts]
+    orders = [math.log(errs[i] / errs[i + 1]) / math.log(dts[i] / dts[i + 1]) for i in range(len(dts) - 1)]
+    for o in orders:
+        assert abs(o - case["order"]) <= case["order_tolerance"] * case["order"], (errs, orders)
+
+
+# ---- tracking consistency ---------------------------------------------------------------------
+def test_tria_tracking_matches_geometry(oracle_lib):
+    w = workloads.plasma_wave(n_cells=6, N=2, n_particles=4000, seed=5, T_eV=2000.0)  # fast: many crossings
+    ms = capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.step(w.config(), ms, w.e_dof, st, 2e-10, 5)
+    assert st.counters.n_lost == 0
+    assert (st.elem != w.elem).sum() > 100
+    x = st.part_state[:, :3]
+    assert np.all((x >= 0) & (x <= 1))
+    assert np.array_equal(workloads._elem_of_uniform(w.mesh, x), st.elem)
+
+
+def test_ref_tracking_curved_mesh(oracle_lib):
+    w = workloads.curved_two_species(n_cells=6, n_per_species=1500, seed=2, Te_eV=5000.0)
+    ms = capi.MeshStruct(w.mesh)
+    cfg = w.config()
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.map_particles(cfg, ms, st)
+    oracle_lib.step(cfg, ms, w.e_dof, st, 2e-11, 4)
+    assert st.counters.n_ref_tolerance == 0
+    assert (st.elem != w.elem).sum() > 50
+    assert np.abs(st.part_pos_ref).max() < 1.0
+    # x(xi) in the found element reproduces the particle position
+    for i in range(0, st.n, 97):
+        xe = elem_map(w.mesh, st.elem[i] - 1, st.part_pos_ref[i])
+        assert np.linalg.norm(xe - st.part_state[i, :3]) < 1e-3 * w.mesh.h[0]
+
+
+def test_shape_function_charge(oracle_lib):
+    w = workloads.curved_two_species(n_cells=6, n_per_species=800, seed=1)
+    ms = capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state[:800], w.elem[:800], w.part_species[:800])
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(w.config(), ms, st, PS)
+    total = 800 * w.species[0][0] * w.species[0][2]
+    q = oracle_lib.integrate_charge(ms, w.mesh.N, PS)
+    assert abs(q - total) <= 2e-3 * abs(total)      # quadrature of the kernel on the DG grid
