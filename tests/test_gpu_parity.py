@@ -221,4 +221,6 @@ def test_full_size_plasma_wave_properties(gpu_lib):
         assert np.array_equal(workloads._elem_of_uniform(w.mesh, x), g["elem"])
         q = oracle.integrate_charge(capi.MeshStruct(w.mesh), w.mesh.N, g["PS"])
         total = w.n * w.species[0][0] * w.species[0][2]
-        assert abs(q - total) <= 1e-10 * abs(total)
+        # FP64: summation order only; mixed: FP32 corner weights sum to 1 within a few FP32 ulps
+        tol = 1e-12 if prec == capi.PIC_PREC_FP64 else 1e-6
+        assert abs(q - total) <= tol * abs(total), (prec, q, total)
