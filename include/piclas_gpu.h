@@ -191,6 +191,18 @@ int pic_synchronize(pic_ctx_t* ctx);
 #define PIC_N_PHASES 6
 int pic_profile(pic_ctx_t* ctx, int32_t enable);
 int pic_profile_read(pic_ctx_t* ctx, double* ms, int64_t* launches, int32_t nphase);
+/* cell_volweight_mean deposition that makes no device allocation (no reference counterpart).
+ * For callers that cannot call cudaMalloc while their time loop runs (e.g. a host whose device
+ * memory belongs to another runtime or to a fixed pool): the particles and the result stay in the
+ * caller's device arrays -- d_part_state is PartState(1:6,n), d_elem / d_species are 1-based
+ * PEM%GlobalElemID / PartSpecies, d_part_source receives PartSource(1:4,0:N,0:N,0:N,nElems) -- and
+ * the node-sum scratch is a fixed file-scope device array for at most 131072 periodic-unique mesh
+ * nodes (4 MiB per GPU, held until the process exits; larger meshes return PIC_ERR_CAPACITY).
+ * The work is queued on `stream` (a cudaStream_t, NULL = default stream) and not waited for.
+ * Calls share the array: calls that overlap on the GPU race, so order them on one stream.  The
+ * first call on a device looks up the array's address; make it before any stream capture. */
+int pic_deposit_cvwm_noalloc(pic_ctx_t* ctx, const double* d_part_state, const int32_t* d_elem,
+                             const int32_t* d_species, int32_t n, double* d_part_source, void* stream);
 /* Kernels launched through this context so far (no reference counterpart: instrumentation). */
 int64_t pic_launch_count(pic_ctx_t* ctx);
 /* The cudaStream_t the context enqueues on, as void* (no reference counterpart: lets a caller

@@ -35,7 +35,8 @@ _LIB = None
 EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy", "pic_set_field",
                     "pic_upload_particles", "pic_download_particles", "pic_interpolate", "pic_push", "pic_track",
                     "pic_deposit", "pic_get_field_at_particles", "pic_step", "pic_get_status", "pic_reset_status",
-                    "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read"]
+                    "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
+                    "pic_deposit_cvwm_noalloc"]
 
 
 class PicError(RuntimeError):
@@ -84,6 +85,8 @@ def load_library(build_if_missing: bool = False):
     L.pic_launch_count.restype = C.c_int64
     L.pic_profile.argtypes = [C.c_void_p, C.c_int32]
     L.pic_profile_read.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), C.c_int32]
+    L.pic_deposit_cvwm_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                           C.c_void_p]
     L.pic_stream.argtypes = [C.c_void_p]
     L.pic_stream.restype = C.c_void_p
     _LIB = L

@@ -10,6 +10,7 @@
 //     element from the FIBGM, so deposition is a gather without atomics.
 #include "../../include/piclas_gpu.h"
 #include "pic_kernels.cuh"
+#include "pic_ctx.h"
 
 #include <algorithm>
 #include <cmath>
@@ -48,85 +49,15 @@ int dalloc(T** p, size_t n) {
 
 }  // namespace
 
-struct pic_ctx {
-  pic_config_t cfg{};
-  int N = 0, nd = 0, ne = 0, n_canon = 0;
-  bool mixed = false, refmap = false, sf = false;
-  cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
-  // mesh
-  DevMesh M{};
-  MeshF MF{};
-  // field
-  double* E = nullptr;
-  float* E32 = nullptr;
-  bool field_set = false;
-  // deposition
-  double* NS = nullptr;
-  double* PS = nullptr;
-  SortBuffers sortb{};
-  SfLists sfl{};
-  SfPack sfk{};
-  // particles
-  DevParticles P{}, Q{};
-  int* perm = nullptr;
-  int* perm_tmp = nullptr;
-  bool have_particles = false;
-  // status
-  DevStatus* st = nullptr;
-  int* d_count = nullptr;
-  int64_t n_steps = 0;
-  int64_t launches = 0;
-  // per-phase CUDA-event timing (pic_profile)
-  bool prof = false;
-  struct Rec { int phase; cudaEvent_t a, b; int launches; };
-  std::vector<Rec> recs;
-  std::vector<cudaEvent_t> pool;
-  double prof_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  int64_t prof_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+namespace pic_internal {
+int dalloc_bytes(void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return fail(PIC_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return PIC_OK;
+}
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace pic_internal
 
-  template <class T>
-  int alloc(T** p, size_t n) {
-    int rc = dalloc(p, n);
-    if (rc == PIC_OK) allocs.push_back((void*)*p);
-    return rc;
-  }
-  cudaEvent_t take_event() {
-    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
-    cudaEvent_t e;
-    cudaEventCreate(&e);
-    return e;
-  }
-  // run fn() (which enqueues kernels and returns how many), bracketed by events when profiling
-  template <class F>
-  void phase(int ph, F&& fn) {
-    if (!prof) { launches += fn(); return; }
-    cudaEvent_t a = take_event(), b = take_event();
-    cudaEventRecord(a, stream);
-    const int n = fn();
-    cudaEventRecord(b, stream);
-    launches += n;
-    recs.push_back(Rec{ph, a, b, n});
-  }
-  void collect() {
-    for (auto& r : recs) {
-      float ms = 0.f;
-      cudaEventSynchronize(r.b);
-      cudaEventElapsedTime(&ms, r.a, r.b);
-      prof_ms[r.phase] += ms;
-      prof_launches[r.phase] += r.launches;
-      pool.push_back(r.a);
-      pool.push_back(r.b);
-    }
-    recs.clear();
-  }
-  LaunchArgs args() const {
-    LaunchArgs a;
-    a.M = M; a.MF = MF; a.N = N; a.nd = nd; a.n_canon = n_canon; a.mixed = mixed;
-    a.E = E; a.E32 = E32; a.NS = NS; a.st = st; a.s = stream;
-    return a;
-  }
-};
 
 
 // ---------------------------------------------------------------------------------------------
@@ -472,6 +403,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     k.sf_alpha = cfg->sf_alpha; k.sf_w = sf_weight(cfg->sf_radius, cfg->sf_alpha);
   }
   if (upload_consts(k) != cudaSuccess) return bail(fail(PIC_ERR_CUDA, "constant upload"));
+  c->k = k;
 
   // ---- work arrays -------------------------------------------------------------------------------
   if ((rc = c->alloc(&c->E, (size_t)ne * nd * 3)) || (rc = c->alloc(&c->E32, (size_t)ne * nd * 3)) ||

@@ -657,4 +657,174 @@ static __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, do
   return te < 0 ? oldElem : te;
 }
 
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------------------------
+// warp reduce-scatter: lane k ends with the warp sum of v[k] (k = node*4 + component)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double reduce_scatter32(double v[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool upper = (lane & h) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const double a = v[j], b = v[j + h];
+      const double recv = __shfl_xor_sync(kFull, upper ? a : b, h);
+      v[j] = (upper ? b : a) + recv;
+    }
+  }
+  return v[0];
+}
+
+// Knuth TwoSum
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// compensated variant: (hi, lo) pairs, exact partial sums carried in lo
+__device__ __forceinline__ double reduce_scatter32_ts(float hi[32], float lo[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool upper = (lane & h) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const float ah = hi[j], bh = hi[j + h], al = lo[j], bl = lo[j + h];
+      const float rh = __shfl_xor_sync(kFull, upper ? ah : bh, h);
+      const float rl = __shfl_xor_sync(kFull, upper ? al : bl, h);
+      float s, e;
+      two_sum(upper ? bh : ah, rh, s, e);
+      hi[j] = s;
+      lo[j] = __fadd_rn(__fadd_rn(upper ? bl : al, rl), e);
+    }
+  }
+  return (double)hi[0] + (double)lo[0];
+}
+
+// Scatter one particle's 8 corner contributions (contrib[k], k = node*4+comp) to the
+// periodic-unique node sums.  Called by all 32 lanes; lanes with active=false add nothing.
+__device__ __forceinline__ void cvwm_scatter(const DevMesh& M, bool active, int e, double contrib[32], double* NS) {
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(kFull, active);
+  if (act == 0) return;
+  const int leader = __ffs(act) - 1;
+  const int e0 = __shfl_sync(kFull, e, leader);
+  const bool same = __all_sync(kFull, !active || e == e0);
+  if (same) {
+    if (!active) {
+#pragma unroll
+      for (int k = 0; k < 32; ++k) contrib[k] = 0.0;
+    }
+    const double s = reduce_scatter32(contrib);
+    const int node = __ldg(M.canon_node + (size_t)e0 * 8 + (lane >> 2));
+    atomicAdd(NS + (size_t)node * 4 + (lane & 3), s);
+  } else if (active) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) atomicAdd(NS + (size_t)node * 4 + c, contrib[4 * n + c]);
+    }
+  }
+}
+
+__device__ __forceinline__ void cvwm_scatter_ts(const DevMesh& M, bool active, int e, float hi[32], double* NS) {
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(kFull, active);
+  if (act == 0) return;
+  const int leader = __ffs(act) - 1;
+  const int e0 = __shfl_sync(kFull, e, leader);
+  const bool same = __all_sync(kFull, !active || e == e0);
+  if (same) {
+    float lo[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) { lo[k] = 0.0f; if (!active) hi[k] = 0.0f; }
+    const double s = reduce_scatter32_ts(hi, lo);
+    const int node = __ldg(M.canon_node + (size_t)e0 * 8 + (lane >> 2));
+    atomicAdd(NS + (size_t)node * 4 + (lane & 3), s);
+  } else if (active) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) atomicAdd(NS + (size_t)node * 4 + c, (double)hi[4 * n + c]);
+    }
+  }
+}
+
+// CVWM corner weights of one particle (pic_depo_method.f90:479-539) in FP64, as contributions.
+__device__ __forceinline__ void cvwm_contrib(const DevMesh& M, int e, bool suc, const double xi[3], const double x[3],
+                                             const double TS[4], double out[32]) {
+  double w[8];
+  if (suc) {
+    const double a1 = 0.5 * (xi[0] + 1.0), a2 = 0.5 * (xi[1] + 1.0), a3 = 0.5 * (xi[2] + 1.0);
+    w[0] = (1 - a1) * (1 - a2) * (1 - a3);
+    w[1] = (a1) * (1 - a2) * (1 - a3);
+    w[2] = (a1) * (a2) * (1 - a3);
+    w[3] = (1 - a1) * (a2) * (1 - a3);
+    w[4] = (1 - a1) * (1 - a2) * (a3);
+    w[5] = (a1) * (1 - a2) * (a3);
+    w[6] = (a1) * (a2) * (a3);
+    w[7] = (1 - a1) * (a2) * (a3);
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) out[4 * n + c] = TS[c] * w[n];
+  } else {
+    // inverse-distance weights to the corners (CGNS corner order)
+    const double* X = M.xcl + (size_t)e * 24;
+    const int cg2t[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+    for (int n = 0; n < 8; ++n) w[n] = 0.0;
+    for (int n = 0; n < 8; ++n) {
+      const int t = cg2t[n];
+      double v0 = __ldg(X + 3 * t) - x[0], v1 = __ldg(X + 3 * t + 1) - x[1], v2 = __ldg(X + 3 * t + 2) - x[2];
+      double norm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+      if (norm > 0.0) w[n] = 1.0 / norm;
+      else { for (int q = 0; q < 8; ++q) w[q] = 0.0; w[n] = 1.0; break; }
+    }
+    double ds = 0.0;
+    for (int n = 0; n < 8; ++n) ds = ds + w[n];
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) out[4 * n + c] = w[n] / ds * TS[c];
+  }
+}
+
+
+// Node sums -> DOFs (pic_depo_method.f90:692-733): PartSource(1:4,k,l,m) of every element.
+template <int N>
+__global__ void k_node_to_dof(DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M.ne * nd) return;
+  const int e = t / nd, r = t - e * nd;
+  const int kk = r % n1, ll = (r / n1) % n1, mm = r / (n1 * n1);
+  const double a1 = c_k.fac_gp[kk], a2 = c_k.fac_gp[ll], a3 = c_k.fac_gp[mm];
+  double S[8][4];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
+    const double V = __ldg(M.node_vol + node);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double s = __ldg(NS + (size_t)node * 4 + c);
+      S[n][c] = V > 0.0 ? s / V : s;
+    }
+  }
+  double out[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    out[c] = S[0][c] * (1 - a1) * (1 - a2) * (1 - a3) + S[1][c] * (a1) * (1 - a2) * (1 - a3) +
+             S[2][c] * (a1) * (a2) * (1 - a3) + S[3][c] * (1 - a1) * (a2) * (1 - a3) +
+             S[4][c] * (1 - a1) * (1 - a2) * (a3) + S[5][c] * (a1) * (1 - a2) * (a3) +
+             S[6][c] * (a1) * (a2) * (a3) + S[7][c] * (1 - a1) * (a2) * (a3);
+  double2* o = reinterpret_cast<double2*>(PS + (size_t)t * 4);
+  o[0] = make_double2(out[0], out[1]);
+  o[1] = make_double2(out[2], out[3]);
+}
+
 }  // namespace pic
