@@ -178,6 +178,28 @@ int pic_get_field_at_particles(pic_ctx_t* ctx, double* field, int32_t n);
 int pic_step(pic_ctx_t* ctx, double dt, int32_t nsteps, double* part_source);
 
 int pic_get_status(pic_ctx_t* ctx, pic_status_t* status);
+
+/* Differentiable loop (no reference counterpart; the reference has no adjoint).  Starting from the
+ * uploaded particles (taken as x_0 and v_{-1/2}; IsNewPart is not applied), runs nsteps of
+ * {interpolation, Boris push, TriaTracking} with the field frozen and B = b_scale * B_ext, deposits
+ * the charge with cell_volweight_mean and returns
+ *     loss = sum over all DOFs of (rho/rho_scale - rho_target)^2 ,
+ * rho_target given as (nDOF, nElems).  If dL_dv0 (3,n) or dL_dB is non-NULL, a hand-written
+ * reverse pass returns dL/dv_{-1/2} per particle (caller order) and dL/d|B|.  Element ids of the
+ * forward pass are replayed in the reverse pass; (x, v, elem) are checkpointed every
+ * checkpoint_every steps and each segment is recomputed.  precision PIC_PREC_FP64 gives the FP64
+ * gradient, PIC_PREC_MIXED the FP32 adjoint (positions stay FP64).  The context's own particle
+ * state is not modified.  Requires cell_volweight_mean + TriaTracking and N <= 3. */
+typedef struct pic_adjoint_cfg_t {
+  int32_t nsteps;
+  int32_t checkpoint_every;
+  int32_t precision;
+  double  dt;
+  double  rho_scale;
+  double  b_scale;
+} pic_adjoint_cfg_t;
+int pic_adjoint_run(pic_ctx_t* ctx, const pic_adjoint_cfg_t* cfg, const double* rho_target, double* loss,
+                    double* dL_dv0, double* dL_dB);
 int pic_reset_status(pic_ctx_t* ctx);
 /* Block the host until all work queued on the context's stream has finished. */
 int pic_synchronize(pic_ctx_t* ctx);

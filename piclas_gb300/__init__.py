@@ -36,7 +36,7 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_upload_particles", "pic_download_particles", "pic_interpolate", "pic_push", "pic_track",
                     "pic_deposit", "pic_get_field_at_particles", "pic_step", "pic_get_status", "pic_reset_status",
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
-                    "pic_deposit_cvwm_noalloc"]
+                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run"]
 
 
 class PicError(RuntimeError):
@@ -87,6 +87,7 @@ def load_library(build_if_missing: bool = False):
     L.pic_profile_read.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), C.c_int32]
     L.pic_deposit_cvwm_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
                                            C.c_void_p]
+    L.pic_adjoint_run.argtypes = [C.c_void_p, P(capi.PicAdjointConfig), dp, dp, dp, dp]
     L.pic_stream.argtypes = [C.c_void_p]
     L.pic_stream.restype = C.c_void_p
     _LIB = L
@@ -208,6 +209,21 @@ class ParticleLoop:
 
     def synchronize(self):
         self._check(self.lib.pic_synchronize(self.handle), "pic_synchronize")
+
+    def adjoint(self, nsteps: int, dt: float, rho_target: np.ndarray, rho_scale: float, b_scale: float = 1.0,
+                checkpoint_every: int = 10, precision: int = PIC_PREC_FP64, gradients: bool = True):
+        """Loss of the differentiable loop and (optionally) dL/dv0 (n,3) and dL/d|B|."""
+        a = capi.PicAdjointConfig(nsteps, checkpoint_every, precision, dt, rho_scale, b_scale)
+        tgt = np.ascontiguousarray(rho_target, dtype=np.float64)
+        if tgt.size != self.mesh.n_elems * self.nd:
+            raise ValueError("rho_target has the wrong size")
+        loss = C.c_double(0.0)
+        gv = np.zeros((self.n, 3)) if gradients else None
+        gb = C.c_double(0.0)
+        self._check(self.lib.pic_adjoint_run(self.handle, C.byref(a), capi.dptr(tgt), C.byref(loss),
+                                             capi.dptr(gv) if gradients else _null(C.c_double),
+                                             C.byref(gb) if gradients else _null(C.c_double)), "pic_adjoint_run")
+        return (loss.value, gv, gb.value) if gradients else loss.value
 
     PHASES = ("deposit_main", "sort_pack", "particle_update", "node_to_dof", "reorder", "cvwm_deposit")
 

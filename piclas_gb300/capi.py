@@ -62,6 +62,11 @@ class PicMesh(C.Structure):
     ]
 
 
+class PicAdjointConfig(C.Structure):
+    _fields_ = [("nsteps", C.c_int32), ("checkpoint_every", C.c_int32), ("precision", C.c_int32),
+                ("dt", C.c_double), ("rho_scale", C.c_double), ("b_scale", C.c_double)]
+
+
 class PicStatus(C.Structure):
     _fields_ = [("error_word", C.c_uint32), ("n_lost", C.c_int32), ("n_inside", C.c_int32),
                 ("n_newton_failed", C.c_int32), ("n_steps", C.c_int64)]

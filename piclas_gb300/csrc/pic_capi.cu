@@ -207,14 +207,41 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
     }
     off[e + 1] = (int)src.size();
   }
-  int* d_off; int* d_src; int8_t* d_sh; double* d_c;
+  // DOF-box radius per element (staging cull) and a Morton order of the targets
+  std::vector<float> drad(ne);
+  std::vector<std::pair<uint64_t, int>> mort(ne);
+  for (int e = 0; e < ne; ++e) {
+    double r2 = 0.0;
+    for (int r = 0; r < nd; ++r) {
+      double q = 0.0;
+      for (int d = 0; d < 3; ++d) { double v = m->elem_xgp[((size_t)e * nd + r) * 3 + d] - dofc[(size_t)e * 3 + d]; q += v * v; }
+      r2 = std::max(r2, q);
+    }
+    drad[e] = (float)(std::sqrt(r2) * (1.0 + 1e-6));
+    uint64_t code = 0;
+    uint32_t ic[3];
+    for (int d = 0; d < 3; ++d) {
+      double u = (dofc[(size_t)e * 3 + d] - m->xmin_glob[d]) / std::max(m->xmax_glob[d] - m->xmin_glob[d], 1e-300);
+      u = std::min(std::max(u, 0.0), 1.0);
+      ic[d] = (uint32_t)(u * 1048575.0);
+    }
+    for (int b = 19; b >= 0; --b)
+      for (int d = 2; d >= 0; --d) code = (code << 1) | ((ic[d] >> b) & 1u);
+    mort[e] = {code, e};
+  }
+  std::sort(mort.begin(), mort.end());
+  std::vector<int> order(ne);
+  for (int e = 0; e < ne; ++e) order[e] = mort[e].second;
+  int* d_off; int* d_src; int8_t* d_sh; double* d_c; float* d_r; int* d_o;
   int rc;
   if ((rc = upload(c, &d_off, off))) return rc;
   if ((rc = upload(c, &d_src, src))) return rc;
   if ((rc = upload(c, &d_sh, shift))) return rc;
   if ((rc = upload(c, &d_c, dofc))) return rc;
+  if ((rc = upload(c, &d_r, drad))) return rc;
+  if ((rc = upload(c, &d_o, order))) return rc;
   c->sfl.nb_off = d_off; c->sfl.nb_src = d_src; c->sfl.nb_shift = d_sh; c->sfl.n_pairs = (int)src.size();
-  c->sfl.dof_center = d_c;
+  c->sfl.dof_center = d_c; c->sfl.dof_radius = d_r; c->sfl.order = d_o;
   return PIC_OK;
 }
 
@@ -367,7 +394,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       (rc = upload(c, &d_slenf, slenf)))
     return bail(rc);
   c->M = DevMesh{ne, d_xcl, d_dxcl, d_bary, d_xez, d_slen, d_rad, d_eps1, d_snb, d_sinfo, d_ecan, d_nvol, d_exgp,
-                 d_fn, d_fo, d_fe};
+                 d_fn, d_fo, d_fe, d_xclr};
   c->MF = MeshF{d_xclr, d_dxclf, d_xezf, d_slenf};
 
   // ---- constants -------------------------------------------------------------------------------

@@ -62,6 +62,7 @@ struct DevMesh {
   const int* fib_n;        // FIBGM cells
   const int* fib_off;
   const int* fib_elem;     // 0-based
+  const float* xclr;       // [ne][8][3] FP32 corners minus the barycentre (inside-test pre-filter)
 };
 
 // ---- particles (SoA) ---------------------------------------------------------------------
@@ -251,9 +252,85 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
   return success;
 }
 
+// FP64 Newton of the mixed variant: same start value, stopping rule (||dxi||^2 <= RefMappingEps,
+// 100 iterations), Armijo damping and plausibility bound as RefElemNewton, but with the NGeo = 1
+// shape functions written as (1 -+ xi)/2 (no barycentric divisions), fused multiply-adds and one
+// reciprocal of det(J) per iteration.  Converges to the same xi up to rounding.
+static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const double* X = M.xcl + (size_t)e * 24;
+  const double* DX = M.dxcl + (size_t)e * 72;
+  double Xl[24];
+#pragma unroll
+  for (int q = 0; q < 24; ++q) Xl[q] = __ldg(X + q);
+  auto residual = [&](const double z[3], double F[3]) {
+    const double l[3][2] = {{0.5 * (1.0 - z[0]), 0.5 * (1.0 + z[0])}, {0.5 * (1.0 - z[1]), 0.5 * (1.0 + z[1])},
+                            {0.5 * (1.0 - z[2]), 0.5 * (1.0 + z[2])}};
+    F[0] = -x[0]; F[1] = -x[1]; F[2] = -x[2];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const double w = l[0][t & 1] * l[1][(t >> 1) & 1] * l[2][t >> 2];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) F[c] = fma(Xl[3 * t + c], w, F[c]);
+    }
+  };
+  double F[3];
+  residual(xi, F);
+  double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
+  double normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
+  bool success = true;
+  for (int iter = 0; iter < 100 && deltaXi2 > c_k.refmapping_eps; ++iter) {
+    const double l[3][2] = {{0.5 * (1.0 - xi[0]), 0.5 * (1.0 + xi[0])}, {0.5 * (1.0 - xi[1]), 0.5 * (1.0 + xi[1])},
+                            {0.5 * (1.0 - xi[2]), 0.5 * (1.0 + xi[2])}};
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const double w = l[0][t & 1] * l[1][(t >> 1) & 1] * l[2][t >> 2];
+#pragma unroll
+      for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) J[nn][dd] = fma(__ldg(DX + 9 * t + 3 * nn + dd), w, J[nn][dd]);
+    }
+    const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
+    const double c01 = fma(J[0][2], J[2][1], -J[0][1] * J[2][2]);
+    const double c02 = fma(J[0][1], J[1][2], -J[0][2] * J[1][1]);
+    const double c10 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
+    const double c11 = fma(J[0][0], J[2][2], -J[0][2] * J[2][0]);
+    const double c12 = fma(J[0][2], J[1][0], -J[0][0] * J[1][2]);
+    const double c20 = fma(J[1][0], J[2][1], -J[1][1] * J[2][0]);
+    const double c21 = fma(J[0][1], J[2][0], -J[0][0] * J[2][1]);
+    const double c22 = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
+    double det = fma(J[0][0], c00, fma(J[0][1], c10, J[0][2] * c20));
+    const double sd = det > 0.0 ? 1.0 / det : det;
+    double dxi[3];
+    dxi[0] = fma(c00, F[0], fma(c01, F[1], c02 * F[2])) * sd;
+    dxi[1] = fma(c10, F[0], fma(c11, F[1], c12 * F[2])) * sd;
+    dxi[2] = fma(c20, F[0], fma(c21, F[1], c22 * F[2])) * sd;
+    deltaXi2 = fma(dxi[0], dxi[0], fma(dxi[1], dxi[1], dxi[2] * dxi[2]));
+    const double xo[3] = {xi[0], xi[1], xi[2]};
+    const double normFold = normF;
+    normF = normF * 2.0;
+    double lambda = 1.0;
+    for (int iArmijo = 1; normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) xi[dd] = fma(-lambda, dxi[dd], xo[dd]);
+      residual(xi, F);
+      lambda = 0.2 * lambda;
+      normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
+    }
+    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = false; break; }
+  }
+  return success;
+}
+
 __device__ __forceinline__ bool position_in_ref_elem(const DevMesh& M, int e, const double x[3], double xi[3]) {
   newton_start(M, e, x, xi);
   return ref_elem_newton(M, e, x, xi);
+}
+
+template <bool FAST>
+__device__ __forceinline__ bool position_in_ref_elem_t(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  newton_start(M, e, x, xi);
+  return FAST ? ref_elem_newton_fast(M, e, x, xi) : ref_elem_newton(M, e, x, xi);
 }
 
 // ==========================================================================================
@@ -471,9 +548,49 @@ __device__ __forceinline__ double wall_alpha(const double* __restrict__ X, uint3
   return alpha;
 }
 
+// FP32 pre-filter of ParticleInsideQuad3D: true only if all 12 signed volumes are positive with a
+// margin far above the FP32 error, so that the FP64 volumes have the same (positive) signs and the
+// particle is inside for convex and concave sides alike; otherwise the caller runs the FP64 test.
+// Error bound (L1 norms n_q of the edge vectors A_q, S = |p|_1 + sqrt(3) * element radius >= every
+// |corner|_1, |p|_1, |A_q|_1): inputs are off by <= 1.8e-7 S per vector and the FP32 evaluation adds
+// <= 3e-7 n_a n_b n_c, so |det32 - det| <= 1.8e-7 S (n_a n_b + n_a n_c + n_b n_c) + 3e-7 n_a n_b n_c.
+// The thresholds below are 1e-5 times the same terms (>= 33x margin).
+__device__ __forceinline__ bool certainly_inside_f32(const DevMesh& M, int e, const double x[3]) {
+  if (!M.xclr) return false;
+  const double* b = M.bary + (size_t)e * 3;
+  const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
+  const float S = fabsf(p[0]) + fabsf(p[1]) + fabsf(p[2]) + 1.7320509f * (float)__ldg(M.radius + e) * 1.0001f;
+  const float* X = M.xclr + (size_t)e * 24;
+  const uint32_t* sinfo = M.side_info + (size_t)e * 6;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    const uint32_t info = __ldg(sinfo + s);
+    float A[4][3], n[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int t = side_corner(info, q);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) A[q][c] = __ldg(X + 3 * t + c) - p[c];
+      n[q] = fabsf(A[q][0]) + fabsf(A[q][1]) + fabsf(A[q][2]);
+    }
+    // crossP = A1 x A3 ; det1 = -(crossP . A2) ; det2 = crossP . A4  (same vectors as the FP64 test)
+    const float cp0 = A[0][1] * A[2][2] - A[0][2] * A[2][1];
+    const float cp1 = A[0][2] * A[2][0] - A[0][0] * A[2][2];
+    const float cp2 = A[0][0] * A[2][1] - A[0][1] * A[2][0];
+    const float d1 = -(cp0 * A[1][0] + cp1 * A[1][1] + cp2 * A[1][2]);
+    const float d2 = cp0 * A[3][0] + cp1 * A[3][1] + cp2 * A[3][2];
+    const float n02 = n[0] * n[2];
+    const float T1 = 1e-5f * (S * (n02 + n[0] * n[1] + n[2] * n[1]) + n02 * n[1]);
+    const float T2 = 1e-5f * (S * (n02 + n[0] * n[3] + n[2] * n[3]) + n02 * n[3]);
+    if (!(d1 > T1) || !(d2 > T2)) return false;
+  }
+  return true;
+}
+
 // Walk from `elem` (= LastElem); updates x / xl at periodic crossings.  Returns the new element,
 // -1 if the particle is lost, -2 if the hop cap was hit.
 static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double x[3], double xl[3]) {
+  if (certainly_inside_f32(M, elem, x)) return elem;     // same decision as the FP64 test below
   int doneE[6] = {0, 0, 0, 0, 0, 0}, doneS[6] = {0, 0, 0, 0, 0, 0}, doneT[6] = {0, 0, 0, 0, 0, 0};
   // doneE/doneS/doneT hold DoneLastElem(1/4/3, 1:6) with 1-based element and side ids (0 = empty)
   for (int loop = 0; loop < kMaxTrackLoops; ++loop) {
@@ -577,8 +694,10 @@ __device__ __forceinline__ bool almost_equal(double a, double b) { return fabs(a
 
 constexpr int kMaxBgmCand = 64;
 
-// Returns the new element (0-based); sets tol_fail when the reference would abort.
-static __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[3], double xl[3], double xi[3],
+// Returns the new element (0-based); sets tol_fail when the reference would abort.  FAST selects
+// the mixed variant's Newton (ref_elem_newton_fast).
+template <bool FAST>
+__device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[3], double xl[3], double xi[3],
                                       bool& tol_fail) {
   tol_fail = false;
   if (c_k.n_pv > 0) {
@@ -591,7 +710,7 @@ static __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, do
       guard++;
     }
   }
-  position_in_ref_elem(M, last_elem, x, xi);
+  position_in_ref_elem_t<FAST>(M, last_elem, x, xi);
   if (maxabs3(xi) < 1.0) return last_elem;
   const int oldElem = last_elem;
   int cell[3];
@@ -641,7 +760,7 @@ static __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, do
   for (int i = 0; i < nBGM; ++i) {
     if (dist[i] == -1.7976931348623157e308) continue;
     const int e = list[i];
-    position_in_ref_elem(M, e, x, xi);
+    position_in_ref_elem_t<FAST>(M, e, x, xi);
     if (maxabs3(xi) < 1.0) return e;
     if (maxabs3(xi) < maxabs3(newXi)) { newXi[0] = xi[0]; newXi[1] = xi[1]; newXi[2] = xi[2]; newElem = e; }
   }
@@ -795,8 +914,18 @@ __device__ __forceinline__ void cvwm_contrib(const DevMesh& M, int e, bool suc, 
 }
 
 
+// NodeSource / NodeVolume once per node (pic_depo_method.f90:684-690), in place, so that the DOF
+// kernel below reads normalised sums instead of dividing 32 times per DOF (FP64 division is slow).
+static __global__ void k_node_normalize(const double* __restrict__ node_vol, double* __restrict__ NS, int n_nodes) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_nodes * 4) return;
+  const double V = __ldg(node_vol + t / 4);
+  if (V > 0.0) NS[t] = NS[t] / V;
+}
+
 // Node sums -> DOFs (pic_depo_method.f90:692-733): PartSource(1:4,k,l,m) of every element.
-template <int N>
+// NORMALIZED: NS already holds NodeSource / NodeVolume (k_node_normalize ran first).
+template <int N, bool NORMALIZED = false>
 __global__ void k_node_to_dof(DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -808,11 +937,16 @@ __global__ void k_node_to_dof(DevMesh M, const double* __restrict__ NS, double* 
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
     const int node = __ldg(M.canon_node + (size_t)e * 8 + n);
-    const double V = __ldg(M.node_vol + node);
+    if constexpr (NORMALIZED) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const double s = __ldg(NS + (size_t)node * 4 + c);
-      S[n][c] = V > 0.0 ? s / V : s;
+      for (int c = 0; c < 4; ++c) S[n][c] = __ldg(NS + (size_t)node * 4 + c);
+    } else {
+      const double V = __ldg(M.node_vol + node);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const double s = __ldg(NS + (size_t)node * 4 + c);
+        S[n][c] = V > 0.0 ? s / V : s;
+      }
     }
   }
   double out[4];

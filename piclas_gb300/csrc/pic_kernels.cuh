@@ -40,6 +40,8 @@ struct SfLists {
   const int8_t* nb_shift; // [n_pairs][3] periodic image in units of the periodic vectors
   int n_pairs;
   const double* dof_center;   // [ne][3] centre of the element's DOF bounding box
+  const float* dof_radius;    // [ne] largest distance of a DOF from dof_center
+  const int* order;           // [ne] target elements in Morton order of their DOF centres (L2 reuse)
 };
 struct SfPack {
   double* pos;     // [cap][3] FP64 position (FP64 variant)

@@ -208,3 +208,32 @@ def batch_instances(count: int = 32, seed: int = 0):
         amp = float(rng.uniform(0.005, 0.05))
         out.append(dict(n_cells=nc, n_particles=npart, amp=amp, seed=i, nsteps=100))
     return out
+
+
+def differentiable_loop(n_cells: int = 16, N: int = 2, n_particles: int = 1_000_000, T_eV: float = 1.0,
+                        Bz: float = 0.05, E0: float = 1.0e3, n0: float = 1.0e11, dt: float = 1.0e-11,
+                        nsteps: int = 50, seed: int = 0, mesh: BoxMesh | None = None) -> Workload:
+    """Differentiable loop: 16^3 linear hex, N=2, 1M electrons uniform in space, Maxwellian 1 eV,
+    B_z = 0.05 T, frozen field E_y = E0 sin(2 pi y), 50 push steps; the loss target at the DOFs is
+    rho_target = 1 + 0.05 cos(2 pi y) in units of the mean charge density (``info['rho_scale']``)."""
+    rng = np.random.default_rng(seed)
+    if mesh is None:
+        mesh = build_box_mesh(n_cells, n_cells, n_cells, N)
+    n = n_particles
+    x = mesh.lo + rng.random((n, 3)) * (mesh.hi - mesh.lo)
+    v = rng.normal(0.0, maxwell_sigma(T_eV, M_ELECTRON), size=(n, 3))
+    ps = np.ascontiguousarray(np.concatenate([x, v], axis=1))
+    elem = _elem_of_uniform(mesh, x)
+    vol = float(np.prod(mesh.hi - mesh.lo))
+    mpf = n0 * vol / n
+    xg = mesh.elem_xgp.reshape(mesh.n_elems, -1, 3)
+    Ly = mesh.hi[1] - mesh.lo[1]
+    e_dof = np.zeros_like(xg)
+    e_dof[..., 1] = E0 * np.sin(2.0 * math.pi * (xg[..., 1] - mesh.lo[1]) / Ly)
+    target = 1.0 + 0.05 * np.cos(2.0 * math.pi * (xg[..., 1] - mesh.lo[1]) / Ly)
+    rho_scale = Q_ELECTRON * mpf * n / vol
+    return Workload(name=f"adjoint_{mesh.nx}^3_N{mesh.N}_{n}", mesh=mesh, species=[(Q_ELECTRON, M_ELECTRON, mpf)],
+                    tracking=capi.PIC_TRACK_TRIA, deposition=capi.PIC_DEPO_CVWM, part_state=ps, elem=elem,
+                    part_species=np.ones(n, np.int32), e_dof=np.ascontiguousarray(e_dof), dt=dt, nsteps=nsteps,
+                    external_field=(0.0, 0.0, 0.0, 0.0, 0.0, Bz),
+                    info=dict(rho_target=np.ascontiguousarray(target), rho_scale=rho_scale, Bz=Bz, E0=E0, seed=seed))

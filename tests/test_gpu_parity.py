@@ -224,3 +224,59 @@ def test_full_size_plasma_wave_properties(gpu_lib):
         # FP64: summation order only; mixed: FP32 corner weights sum to 1 within a few FP32 ulps
         tol = 1e-12 if prec == capi.PIC_PREC_FP64 else 1e-6
         assert abs(q - total) <= tol * abs(total), (prec, q, total)
+
+
+def test_near_face_particles_element_ids_exact(gpu_lib, oracle_lib):
+    """Particles at 1e-13..1e-3 cell widths on either side of faces, edges and corners: the FP32
+    pre-filter of the inside test must hand all of them to the FP64 test, so element ids stay
+    identical to the oracle's."""
+    mesh = build_box_mesh(4, 4, 4, 2)
+    h = 0.25
+    rng = np.random.default_rng(3)
+    pts = []
+    for off in (1e-13, 1e-11, 1e-9, 1e-7, 1e-5, 1e-3):
+        for sgn in (-1.0, 1.0):
+            for k in range(40):
+                base = rng.integers(1, 4, size=3) * h          # an interior grid node
+                axes = rng.random(3) < 0.5                    # face / edge / corner neighbourhoods
+                axes[rng.integers(0, 3)] = True
+                jitter = np.where(axes, sgn * off * h, rng.random(3) * h * 0.9 + 0.05 * h)
+                pts.append(base + jitter - np.where(axes, 0.0, 0.5 * h))
+    x = np.array(pts)
+    n = len(x)
+    v = rng.normal(0, 4e5, size=(n, 3))
+    ps = np.ascontiguousarray(np.concatenate([x, v], axis=1))
+    # start each particle in the element the oracle's own tracking puts it in (walk from floor())
+    elem0 = workloads._elem_of_uniform(mesh, x)
+    cfg = capi.make_config(2, capi.PIC_TRACK_TRIA, capi.PIC_DEPO_CVWM, capi.PIC_PREC_FP64,
+                           [(workloads.Q_ELECTRON, workloads.M_ELECTRON, 1e5)], n)
+    e_dof = np.zeros((mesh.n_elems, mesh.n_dof, 3))
+    ms = capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(ps, elem0, np.ones(n, np.int32), is_new=np.zeros(n, np.uint8))
+    PSo = np.zeros((mesh.n_elems, mesh.n_dof, 4))
+    oracle_lib.step(cfg, ms, e_dof, st, 1e-13, 2, PSo)       # tiny steps: particles stay near the faces
+    loop = ParticleLoop(cfg, mesh)
+    loop.set_field(e_dof)
+    loop.upload_particles(ps, elem0, np.ones(n, np.int32), is_new=np.zeros(n, np.uint8))
+    PSg = np.zeros_like(PSo)
+    loop.time_step(1e-13, 2, PSg)
+    g = loop.download_particles()
+    loop.close()
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+
+
+def test_mixed_error_per_step_plasma_wave(gpu_lib):
+    """Mixed vs FP64 on the plasma wave, every step: rho, E at particles, x and v stay within the
+    mixed variant's budget and element ids never differ."""
+    from piclas_gb300 import precision_report
+    w = workloads.plasma_wave(n_cells=8, N=3, n_particles=20000, nsteps=10, seed=3)
+    rows = precision_report.mixed_vs_fp64_per_step(w, 10)
+    assert len(rows) == 10
+    for r in rows:
+        assert r["rho"] <= 1e-6, r
+        assert r["E"] <= 1e-5, r
+        assert r["v"] <= 1e-5, r
+        assert r["x_m"] <= 1e-9, r
+        assert r["elem_mismatch"] == 0, r
