@@ -79,16 +79,47 @@ def algorithmic_bytes_per_step(w, mixed: bool) -> float:
 
 
 def dominant_kernel_bytes(w, mixed: bool) -> tuple[str, float]:
-    """Algorithmic bytes of one launch of the dominant kernel."""
+    """Name and algorithmic bytes of one launch of the dominant kernel."""
     from piclas_gb300 import capi
     if w.deposition == capi.PIC_DEPO_SHAPE_FUNCTION:
         # gather: each packed particle record read once, PartSource written once
         rec = 32 if mixed else 16 + 24 + 32
-        return "k_sf_gather", float(w.n * rec + w.mesh.n_elems * w.mesh.n_dof * 4 * 8)
+        name = f"k_sf_gather{5 if sf_gather_variant() == 5 else 2}<{w.mesh.N},{int(mixed)}>"
+        return name, float(w.n * rec + w.mesh.n_elems * w.mesh.n_dof * 4 * 8)
     s_state = (24 + 12) if mixed else 48
     b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_elems * w.mesh.n_dof * 3 * (4 if mixed else 8)
     b += w.mesh.n_nodes * 4 * 8
-    return "k_step_cvwm_tria", float(b)
+    return f"k_step_cvwm_tria<{w.mesh.N},{int(mixed)}>", float(b)
+
+
+def sf_gather_variant() -> int:
+    """Compile-time shape-function gather variant of the loaded library (from pic_version)."""
+    from piclas_gb300 import load_library
+    v = load_library().pic_version().decode()
+    try:
+        return int(v.split("sf gather")[1].strip(" )"))
+    except Exception:
+        return 5
+
+
+def sf_hits_per_launch(w) -> float:
+    """Expected (particle, DOF) pairs with r <= R: particles x DOF density x sphere volume."""
+    vol = float(np.prod(np.asarray(w.mesh.hi) - np.asarray(w.mesh.lo)))
+    dof_density = w.mesh.n_elems * w.mesh.n_dof / vol
+    return w.n * dof_density * 4.0 / 3.0 * math.pi * w.sf_radius ** 3
+
+
+def compute_roofline(w, mixed: bool, avg_ms: float):
+    """The FP64 gather is bound by GB300's FP64 pipe, not by HBM: FLOP/s of its hits against the
+    nominal FP64 rate (no measured FP64 peak exists for this GPU; 1.25 TFLOP/s nominal)."""
+    from piclas_gb300 import capi
+    if w.deposition != capi.PIC_DEPO_SHAPE_FUNCTION or mixed:
+        return None
+    hits = sf_hits_per_launch(w)
+    flops = 19.0 * hits     # per hit: r^2 (3 sub, 3 mul, 2 add), 1 - r^2/R^2 (2), ^2 (1), 4 x (mul, add)
+    achieved = flops / (avg_ms / 1e3) / 1e9
+    return {"bound": "fp64", "achieved": achieved, "peak": 1250.0, "unit": "GFLOP/s", "frac": achieved / 1250.0,
+            "peak_kind": "nominal", "hits_per_launch": hits, "flops_per_hit": 19}
 
 
 def hbm_peak():
@@ -100,14 +131,16 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def read_traffic(kernel: str):
-    """dram bytes per launch from the committed ncu summary (profiles/ncu_traffic.md), if any."""
+def read_traffic(key: str):
+    """DRAM bytes per launch from the committed ncu summary (profiles/ncu_traffic.md): the row whose
+    first cell is ``key`` ("kernel @ workload"), last cell = bytes per full-size launch."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.md")
     try:
         for line in open(p):
-            if line.startswith("|") and kernel in line:
-                cells = [c.strip() for c in line.strip("|\n").split("|")]
-                return float(cells[-1])
+            if line.startswith("|"):
+                cells = [c.strip() for c in line.strip().strip("|").split("|")]
+                if cells and cells[0] == key:
+                    return float(cells[-1])
     except Exception:
         pass
     return None
@@ -163,16 +196,23 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------------------------
 def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0, nthreads: int | None = None):
-    """Time the reference algorithm (oracle, OpenMP) on a bounded sample of the workload."""
+    """Time the reference algorithm (oracle, OpenMP) on a bounded sample of the workload: the full mesh
+    with as many particles as fit ~target_s seconds per step (at most the full particle count).  The
+    per-step cost is a fixed part (zeroing PartSource, per-thread accumulators and their reduction) plus
+    a per-particle part; two probe sizes fit both, so that the sample is sized for the target time."""
     import oracle
-    from piclas_gb300 import capi
+    from piclas_gb300 import capi, workloads
     oracle.build()
     nthreads = nthreads or max(1, os.cpu_count() or 1)
-    # calibrate: particles per second per step on a small sample
-    probe_n = 20000
-    w = make_workload(name, seed=0, n_override=probe_n)
+    w = make_workload(name, seed=0, n_override=20000)
     ms = capi.MeshStruct(w.mesh)
     cfg = w.config()
+    n_full = 16_000_000 if name == "curved" else 200_000
+
+    def sample(n):
+        if name == "curved":
+            return workloads.curved_two_species(n_per_species=max(n // 2, 1), seed=0, mesh=w.mesh)
+        return workloads.plasma_wave(n_particles=n, seed=0, mesh=w.mesh)
 
     def run(wk, nsteps):
         st = oracle.OracleState(wk.part_state, wk.elem, wk.part_species)
@@ -183,23 +223,22 @@ def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0
         oracle.step(cfg, ms, wk.e_dof, st, wk.dt, nsteps, PS, nthreads)
         return time.perf_counter() - t0
 
+    n1, n2 = 20000, min(100000, n_full)
     run(w, 1)                      # first run pays thread start-up and page faults
-    t_probe = run(w, 1)
-    rate = probe_n / max(t_probe, 1e-6)
-    per_step = max(1.0, target_s / max(steps, 1))
-    n_sample = int(min(max(rate * per_step, probe_n), w.n if name == "plasma_wave" else 16_000_000))
-    from piclas_gb300 import workloads
-    if name == "curved":
-        ws = workloads.curved_two_species(n_per_species=max(n_sample // 2, 1), seed=0, mesh=w.mesh)
-    else:
-        ws = workloads.plasma_wave(n_particles=n_sample, seed=0, mesh=w.mesh)
+    t1 = run(w, 1)
+    t2 = run(sample(n2), 1) if n2 > n1 else t1
+    per = max((t2 - t1) / max(n2 - n1, 1), 1e-9)
+    fixed = max(t1 - per * n1, 0.0)
+    n_sample = int(min(max((target_s - fixed) / per, n1), n_full))
+    ws = sample(n_sample)
     if warmup > 0:
         run(ws, 1)
     t = run(ws, steps)
     value = ws.n * steps / t
     return {"value": value, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
-            "sample": f"{ws.n} particles x {steps} steps on the full {w.mesh.nx}^3 mesh "
-                      f"(C restatement of the reference loop, OpenMP {nthreads} threads, {t:.1f} s)"}
+            "sample": f"{ws.n} of {n_full} particles x {steps} steps on the full {w.mesh.nx}^3 mesh "
+                      f"(C restatement of the reference loop, OpenMP {nthreads} threads, {t:.1f} s; "
+                      f"fitted per step {fixed:.2f} s + {per * 1e6:.2f} us/particle)"}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -288,7 +327,7 @@ def run_gpu(args, rank, world, local_rank):
     avg_ms = dom["ms"] / max(dom["launches"], 1)
     peak, peak_kind = hbm_peak()
     achieved = kbytes / (avg_ms / 1e3) / 1e9
-    traffic = read_traffic(kname)
+    traffic = read_traffic(f"{kname} @ {args.workload}" + ("" if args.cells is None and args.particles is None else " (custom size)"))
 
     # end-to-end through the C-ABI with host buffers: per step the HDG hand-over (E in, PartSource out)
     E_host = torch.from_numpy(np.ascontiguousarray(w.e_dof)).pin_memory()
@@ -317,8 +356,11 @@ def run_gpu(args, rank, world, local_rank):
                      "achieved_gbs": algorithmic_bytes_per_step(w, mixed) * args.steps / (ms / 1e3) / 1e9},
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "avg_launch_ms": avg_ms, "share": dom["ms"] / max(sum(v["ms"] for v in prof.values()), 1e-9)},
+                     "avg_launch_ms": avg_ms, "share": dom["ms"] / max(sum(v["ms"] for v in prof.values()), 1e-9),
+                     "note": ("bound by the FP64 pipe, not HBM (see compute_roofline)"
+                              if kname.startswith("k_sf_gather") and not mixed else None)},
         "phases_ms": {k: round(v["ms"] / args.steps, 4) for k, v in prof.items() if v["launches"]},
+        "compute_roofline": compute_roofline(w, mixed, avg_ms),
         "e2e": e2e,
         "status": st,
     }
@@ -459,7 +501,10 @@ def run_batch(args):
 def run_reference(args, rank):
     if rank != 0:
         return
-    base = cpu_reference_run(args.workload, steps=max(args.steps, 1), warmup=args.warmup, target_s=args.cpu_seconds)
+    nsteps = max(args.steps, 1)
+    # each step a bounded sample; the whole run (probes, warm-up, steps) stays within about three minutes
+    per_step = min(args.cpu_seconds, 150.0 / (nsteps + (1 if args.warmup > 0 else 0)))
+    base = cpu_reference_run(args.workload, steps=nsteps, warmup=args.warmup, target_s=per_step)
     out = {"metric": METRIC, "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded), frozen field",

@@ -277,7 +277,10 @@ int device_sync(pic_ctx* c) {
 // =============================================================================================
 extern "C" {
 
-const char* pic_version(void) { return "piclas_gb300 0.1 (sm_103a)"; }
+const char* pic_version(void) {
+  static const std::string v = "piclas_gb300 0.1 (sm_103a; sf gather " + std::to_string(pic::sf_gather_variant()) + ")";
+  return v.c_str();
+}
 const char* pic_last_error(void) { return g_last_error.c_str(); }
 
 int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {

@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh
 //            FP64 (decision r^2 <= R^2 in FP64 as the reference), or in FP32 with TwoSum-compensated
 //            per-DOF sums (mixed).  Lanes are busy in proportion to their hit counts instead of
 //            executing the evaluation for every particle any lane of the warp hits.
-constexpr int kSf2Chunk = 256;
+[[maybe_unused]] constexpr int kSf2Chunk = 256;   // used by the PIC_SF_GATHER=2 build
 constexpr int kSf2Threads = 128;   // 4 warps: (DOF half) x (particle parity)
 
 template <int N, bool MIXED>
@@ -880,129 +880,129 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L
   }
 }
 
-// Group-balanced two-phase gather for N = 3 (64 DOFs).  Work per lane in the evaluation phase is
-// proportional to the lane's hit count; with one DOF per lane a source element on one side of the
-// target gives the near DOFs many hits and the far ones none.  Here every lane owns the four DOFs
-// (i,j,k), (3-i,3-j,3-k), (3-i,j,k), (i,3-j,3-k) -- the orbit of (i,j,k) under the point reflection
-// and the reflection in xi -- whose hit counts add up to nearly the same total for every lane.
-// Lanes l and l^16 own the same group and take alternate particles; four warps split the staged
-// particles further (8 particle classes q % 8).  Phase A (FP32 test) writes one list per owned DOF;
-// phase B walks the four lists back to back, rotating the per-DOF registers at each list end so
-// that the arithmetic always uses slot 0 (register moves only, no extra FP64 instruction).
-//
-// FP64 evaluation: with p, g the particle and DOF positions relative to the target's DOF centre,
+// Round-robin gather, one DOF per lane (N <= 3).  Candidates of all (source, image) pairs of the target
+// are taken row by row (particle r of every pair, then r+1, ...) and the staging set is filled to at
+// least kSf5Chunk - kSf5Threads entries, so every set surrounds the target evenly and each DOF's
+// hit count is close to the mean: per-lane hit lists then keep the lanes of a warp about equally busy
+// (simulated 86 % of lane slots carry a hit, 46 % with sets from one source element at a time).
+// Warps: (DOF half) x (particle parity) for nd > 32, four parities for nd <= 32.
+// FP64: with p, g the particle and DOF positions relative to the target's DOF centre,
 // 1 - |p-g|^2/R^2 = A_p + B_g + p'.g with A_p = -|p|^2/R^2, p' = 2p/R^2 (per staged particle) and
-// B_g = 1 - |g|^2/R^2 (per DOF): one add and three fused multiply-adds per hit.  It differs from
-// the reference's (1 - r^2/R^2) by rounding only (|terms| <= 8, so ~1e-15 absolute); the reference
-// keeps r^2 <= R^2, here 1 - r^2/R^2 >= 0.
-constexpr int kSf3Chunk = 256;
-constexpr int kSf3Threads = 128;
-constexpr int kSf3Slot = kSf3Chunk / 8;   // entries per owned DOF and lane (one particle class)
+// B_g = 1 - |g|^2/R^2 (per DOF): one add and three fused multiply-adds per hit, 9 FP64 instructions
+// per hit in all.  It differs from the reference's (1 - r^2/R^2) by rounding only (|terms| <= 8, so
+// ~1e-15 absolute); the reference keeps r^2 <= R^2, here 1 - r^2/R^2 >= 0 (read from the sign bit).
+// Mixed: FP32 distances and weights with TwoSum-compensated per-DOF sums.
+constexpr int kSf5Chunk = 256;
+constexpr int kSf5Threads = 128;
+constexpr int kSf5Pairs = 160;
 
-template <int S>
-__device__ __forceinline__ void rot4(double (&a)[4][S]) {
-#pragma unroll
-  for (int c = 0; c < S; ++c) {
-    const double t = a[0][c];
-    a[0][c] = a[1][c]; a[1][c] = a[2][c]; a[2][c] = a[3][c]; a[3][c] = t;
-  }
-}
-template <int S>
-__device__ __forceinline__ void rot4(float (&a)[4][S]) {
-#pragma unroll
-  for (int c = 0; c < S; ++c) {
-    const float t = a[0][c];
-    a[0][c] = a[1][c]; a[1][c] = a[2][c]; a[2][c] = a[3][c]; a[3][c] = t;
-  }
-}
-__device__ __forceinline__ void rot4(int (&a)[4]) {
-  const int t = a[0];
-  a[0] = a[1]; a[1] = a[2]; a[2] = a[3]; a[3] = t;
-}
-
-template <bool MIXED>
-__global__ void __launch_bounds__(kSf3Threads, 4) k_sf_gather3(DevMesh M, SfLists L, const int* __restrict__ off,
+template <int N, bool MIXED>
+__global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L, const int* __restrict__ off,
                                                             SfPack K, double* __restrict__ PS) {
-  constexpr int nd = 64;
-  __shared__ float4 s_rel[kSf3Chunk];
-  __shared__ float4 s_facf[MIXED ? kSf3Chunk : 1];
-  __shared__ double2 s_pq[MIXED ? 1 : 2 * kSf3Chunk];    // (p'x, p'y), (p'z, A_p)
-  __shared__ double2 s_fac[MIXED ? 1 : 2 * kSf3Chunk];
-  __shared__ uint8_t s_list[kSf3Threads / 32][4 * kSf3Slot][32];
-  __shared__ double s_red[kSf3Threads / 32][nd][4];
-  __shared__ int s_idx[kSf3Chunk];
-  __shared__ int s_cnt;
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  static_assert(nd <= 64, "one DOF per lane, at most two DOF halves");
+  constexpr int halves = nd > 32 ? 2 : 1, npar = 4 / halves;
+  constexpr int cap = kSf5Chunk / npar;                  // hit-list entries per lane
+  __shared__ float4 s_rel[kSf5Chunk];
+  __shared__ float4 s_facf[MIXED ? kSf5Chunk : 1];
+  __shared__ __align__(16) double2 s_pq[2 * kSf5Chunk];  // FP64: (p'x, p'y), (p'z, A_p); per-DOF sums at the end
+  __shared__ double2 s_fac[MIXED ? 1 : 2 * kSf5Chunk];
+  __shared__ uint8_t s_list[kSf5Threads / 32][cap][32];
+  __shared__ int s_j[kSf5Chunk];
+  __shared__ uint8_t s_pr[kSf5Chunk];
+  __shared__ int s_b0[kSf5Pairs], s_n[kSf5Pairs];
+  __shared__ float s_o[kSf5Pairs][3];
+  __shared__ double s_off[MIXED ? 1 : kSf5Pairs][3];
+  __shared__ int s_cnt, s_max;
+  static_assert(sizeof(double) * 4 * npar * (halves * 32) <= sizeof(double2) * 2 * kSf5Chunk, "sums alias s_pq");
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int grp = lane & 15, cls = (w << 1) | (lane >> 4);
+  const int dof = (w % halves) * 32 + lane, parity = w / halves;
+  const bool active = dof < nd;
   const int e = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
   const double* ce = L.dof_center + (size_t)e * 3;
   const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
   const double R2inv = c_k.sf_r2_inv;
   const float R2f = (float)(c_k.sf_r2 * (1.0 + 1.0e-4));
-  const float R2s = (float)c_k.sf_r2, R2invs = (float)R2inv;
   const float cull = (float)c_k.sf_r + __ldg(L.dof_radius + e);
   const float cull2 = cull * cull * 1.0001f;
-  // owned DOFs: group (i, j, k) with i, j in {0, 1}
-  int dofs[4];
-  {
-    const int i = grp & 1, j = (grp >> 1) & 1, k = grp >> 2;
-    dofs[0] = i + 4 * j + 16 * k;
-    dofs[1] = (3 - i) + 4 * (3 - j) + 16 * (3 - k);
-    dofs[2] = (3 - i) + 4 * j + 16 * k;
-    dofs[3] = i + 4 * (3 - j) + 16 * (3 - k);
-  }
-  double gd[4][4];          // (gx, gy, gz, B_g) per owned DOF (FP64 variant)
-  float gf[4][3];           // FP32 DOF position relative to the centre
-  double acc[4][4];
-  float hi[4][4], lo[4][4];
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    const double* g = M.elem_xgp + ((size_t)e * nd + dofs[s]) * 3;
+  double gd[4] = {0.0, 0.0, 0.0, 0.0};
+  float gf[3] = {0.f, 0.f, 0.f};
+  if (active) {
+    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
     const double gx = __ldg(g) - cex, gy = __ldg(g + 1) - cey, gz = __ldg(g + 2) - cez;
-    gd[s][0] = gx; gd[s][1] = gy; gd[s][2] = gz;
-    gd[s][3] = fma(-R2inv, fma(gx, gx, fma(gy, gy, gz * gz)), 1.0);
-    gf[s][0] = (float)gx; gf[s][1] = (float)gy; gf[s][2] = (float)gz;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) { acc[s][c] = 0.0; hi[s][c] = 0.f; lo[s][c] = 0.f; }
+    gd[0] = gx; gd[1] = gy; gd[2] = gz;
+    gd[3] = fma(-R2inv, fma(gx, gx, fma(gy, gy, gz * gz)), 1.0);
+    gf[0] = (float)gx; gf[1] = (float)gy; gf[2] = (float)gz;
   }
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  const double t2 = 2.0 * R2inv;
   const int p0 = __ldg(L.nb_off + e), p1 = __ldg(L.nb_off + e + 1);
-  for (int p = p0; p < p1; ++p) {
-    const int src = __ldg(L.nb_src + p);
-    double sh[3];
+  for (int pw = p0; pw < p1; pw += kSf5Pairs) {
+    const int npw = min(kSf5Pairs, p1 - pw);
+    __syncthreads();                       // the previous window is finished with the pair tables
+    if (t == 0) s_max = 0;
+    __syncthreads();
+    for (int i = t; i < npw; i += kSf5Threads) {
+      const int p = pw + i;
+      const int src = __ldg(L.nb_src + p);
+      double sh[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int k = c_k.pv_dir[d];
-      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+      for (int d = 0; d < 3; ++d) {
+        const int k = c_k.pv_dir[d];
+        sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+      }
+      const double* cs = L.dof_center + (size_t)src * 3;
+      s_o[i][0] = (float)((__ldg(cs) + sh[0]) - cex);
+      s_o[i][1] = (float)((__ldg(cs + 1) + sh[1]) - cey);
+      s_o[i][2] = (float)((__ldg(cs + 2) + sh[2]) - cez);
+      if constexpr (!MIXED) { s_off[i][0] = sh[0] - cex; s_off[i][1] = sh[1] - cey; s_off[i][2] = sh[2] - cez; }
+      const int b0 = __ldg(off + src), n = __ldg(off + src + 1) - b0;
+      s_b0[i] = b0;
+      s_n[i] = n;
+      atomicMax(&s_max, n);
     }
-    const double* cs = L.dof_center + (size_t)src * 3;
-    const float ox = (float)((__ldg(cs) + sh[0]) - cex), oy = (float)((__ldg(cs + 1) + sh[1]) - cey),
-                oz = (float)((__ldg(cs + 2) + sh[2]) - cez);
-    const int b0 = __ldg(off + src), cnt = __ldg(off + src + 1) - b0;
-    for (int base = 0; base < cnt; base += kSf3Chunk) {
-      const int nl = min(kSf3Chunk, cnt - base);
-      __syncthreads();
+    __syncthreads();
+    const long long total = (long long)npw * s_max;    // candidates (row, pair), row-major
+    long long cursor = 0;
+    while (cursor < total) {
+      __syncthreads();                     // the previous set is evaluated
       if (t == 0) s_cnt = 0;
       __syncthreads();
-      for (int q = t; q < nl; q += kSf3Threads) {
-        const size_t j = (size_t)b0 + base + q;
-        const float4 r = reinterpret_cast<const float4*>(K.posf)[j];
-        const float rx = r.x + ox, ry = r.y + oy, rz = r.z + oz;
-        if (fmaf(rx, rx, fmaf(ry, ry, rz * rz)) <= cull2) {
-          const int slot = atomicAdd(&s_cnt, 1);
-          s_rel[slot] = make_float4(rx, ry, rz, 0.0f);
-          s_idx[slot] = (int)(j - b0);
-          if constexpr (MIXED) s_facf[slot] = reinterpret_cast<const float4*>(K.facf)[j];
+      int nst = 0;
+      while (cursor < total && nst <= kSf5Chunk - kSf5Threads) {
+        const long long c = cursor + t;
+        bool app = false;
+        if (c < total) {
+          const long long rowl = c / npw;
+          const int pr = (int)(c - rowl * npw);
+          if (rowl < s_n[pr]) {
+            const int j = s_b0[pr] + (int)rowl;
+            const float4 r = reinterpret_cast<const float4*>(K.posf)[j];
+            const float rx = r.x + s_o[pr][0], ry = r.y + s_o[pr][1], rz = r.z + s_o[pr][2];
+            if (fmaf(rx, rx, fmaf(ry, ry, rz * rz)) <= cull2) {
+              const int slot = atomicAdd(&s_cnt, 1);
+              s_rel[slot] = make_float4(rx, ry, rz, 0.0f);
+              if constexpr (MIXED) {
+                s_facf[slot] = reinterpret_cast<const float4*>(K.facf)[j];
+              } else {
+                s_j[slot] = j;
+                s_pr[slot] = (uint8_t)pr;
+              }
+              app = true;
+            }
+          }
         }
+        nst += __syncthreads_count(app);
+        cursor += kSf5Threads;
       }
-      __syncthreads();
-      const int nst = s_cnt;
       if constexpr (!MIXED) {
-        // FP64 staging over the compacted set (every lane busy)
-        const double t2 = 2.0 * R2inv;
-        for (int slot = t; slot < nst; slot += kSf3Threads) {
-          const size_t j = (size_t)b0 + s_idx[slot];
-          const double px = (K.pos[3 * j] + sh[0]) - cex, py = (K.pos[3 * j + 1] + sh[1]) - cey,
-                       pz = (K.pos[3 * j + 2] + sh[2]) - cez;
+        // FP64 staging over the compacted set
+        for (int slot = t; slot < nst; slot += kSf5Threads) {
+          const size_t j = (size_t)s_j[slot];
+          const int pr = s_pr[slot];
+          const double px = K.pos[3 * j] + s_off[pr][0], py = K.pos[3 * j + 1] + s_off[pr][1],
+                       pz = K.pos[3 * j + 2] + s_off[pr][2];
           s_pq[2 * slot] = make_double2(px * t2, py * t2);
           s_pq[2 * slot + 1] = make_double2(pz * t2, -R2inv * fma(px, px, fma(py, py, pz * pz)));
           const double2* fp = reinterpret_cast<const double2*>(K.fac + 4 * j);
@@ -1011,35 +1011,23 @@ __global__ void __launch_bounds__(kSf3Threads, 4) k_sf_gather3(DevMesh M, SfList
         }
         __syncthreads();
       }
-      // phase A: FP32 test of this lane's particle class against its four DOFs
-      int nh[4] = {0, 0, 0, 0};
-      for (int m = 0; cls + 8 * m < nst; ++m) {
-        const float4 r = s_rel[cls + 8 * m];
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const float dx = r.x - gf[s][0], dy = r.y - gf[s][1], dz = r.z - gf[s][2];
-          if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[w][s * kSf3Slot + nh[s]++][lane] = (uint8_t)m;
-        }
+      if (!active) continue;
+      // phase A: FP32 test of this lane's DOF against its parity's particles
+      int nh = 0;
+      for (int m = 0; parity + npar * m < nst; ++m) {
+        const float4 r = s_rel[parity + npar * m];
+        const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[w][nh++][lane] = (uint8_t)m;
       }
-      // phase B: the four lists back to back; slot 0 always holds the DOF being evaluated
-      const int total = nh[0] + nh[1] + nh[2] + nh[3];
-      int base_s[4] = {0, kSf3Slot, 2 * kSf3Slot, 3 * kSf3Slot};
-      int rot = 0, kk = 0;
-      for (int it = 0; it < total; ++it) {
-        while (kk == nh[0]) {
-          rot4(nh); rot4(base_s); rot4(gf);
-          if constexpr (MIXED) { rot4(hi); rot4(lo); } else { rot4(gd); rot4(acc); }
-          kk = 0;
-          ++rot;
-        }
-        const int q = cls + 8 * (int)s_list[w][base_s[0] + kk][lane];
-        ++kk;
+      // phase B: this lane's hits
+      for (int k = 0; k < nh; ++k) {
+        const int q = parity + npar * (int)s_list[w][k][lane];
         if constexpr (MIXED) {
           const float4 r = s_rel[q];
-          const float dx = r.x - gf[0][0], dy = r.y - gf[0][1], dz = r.z - gf[0][2];
+          const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (r2 <= R2s) {
-            const float Sv = fmaf(-R2invs, r2, 1.0f);
+          if (r2 <= (float)c_k.sf_r2) {
+            const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
             float S1 = Sv * Sv;
             for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
             const float4 f = s_facf[q];
@@ -1047,46 +1035,47 @@ __global__ void __launch_bounds__(kSf3Threads, 4) k_sf_gather3(DevMesh M, SfList
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
               float sm, er;
-              two_sum(hi[0][c], S1 * fc[c], sm, er);
-              hi[0][c] = sm;
-              lo[0][c] += er;
+              two_sum(hi[c], S1 * fc[c], sm, er);
+              hi[c] = sm;
+              lo[c] += er;
             }
           }
         } else {
           const double2 pa = s_pq[2 * q], pb = s_pq[2 * q + 1];
-          const double Sv = fma(pa.x, gd[0][0], fma(pa.y, gd[0][1], fma(pb.x, gd[0][2], pb.y + gd[0][3])));
+          const double Sv = fma(pa.x, gd[0], fma(pa.y, gd[1], fma(pb.x, gd[2], pb.y + gd[3])));
           // Sv >= 0 read from the sign bit (integer pipe); -0.0 is skipped, its contribution is 0
           if (__double_as_longlong(Sv) >= 0) {
             double S1 = Sv * Sv;
             for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
             const double2 f01 = s_fac[2 * q], f23 = s_fac[2 * q + 1];
-            acc[0][0] = fma(S1, f01.x, acc[0][0]);
-            acc[0][1] = fma(S1, f01.y, acc[0][1]);
-            acc[0][2] = fma(S1, f23.x, acc[0][2]);
-            acc[0][3] = fma(S1, f23.y, acc[0][3]);
+            acc[0] = fma(S1, f01.x, acc[0]);
+            acc[1] = fma(S1, f01.y, acc[1]);
+            acc[2] = fma(S1, f23.x, acc[2]);
+            acc[3] = fma(S1, f23.y, acc[3]);
           }
         }
       }
-      for (int r = (4 - (rot & 3)) & 3; r > 0; --r) {
-        rot4(nh); rot4(base_s); rot4(gf);
-        if constexpr (MIXED) { rot4(hi); rot4(lo); } else { rot4(gd); rot4(acc); }
-      }
     }
   }
-  // combine the two particle classes of a warp (lanes l, l^16), then the four warps
+  if constexpr (MIXED) {
 #pragma unroll
-  for (int s = 0; s < 4; ++s)
+    for (int c = 0; c < 4; ++c) acc[c] = (double)hi[c] + (double)lo[c];
+  }
+  // per-DOF sums over the particle parities
+  __syncthreads();
+  double (*s_red)[halves * 32][4] = reinterpret_cast<double (*)[halves * 32][4]>(s_pq);
+  if (active) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      double v = MIXED ? (double)hi[s][c] + (double)lo[s][c] : acc[s][c];
-      v = v + __shfl_xor_sync(0xffffffffu, v, 16);
-      if (lane < 16) s_red[w][dofs[s]][c] = v;
-    }
+    for (int c = 0; c < 4; ++c) s_red[parity][dof][c] = acc[c];
+  }
   __syncthreads();
   if (t < nd) {
     double o[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) o[c] = (s_red[0][t][c] + s_red[1][t][c]) + (s_red[2][t][c] + s_red[3][t][c]);
+    for (int c = 0; c < 4; ++c) {
+      o[c] = s_red[0][t][c];
+      for (int k = 1; k < npar; ++k) o[c] = o[c] + s_red[k][t][c];
+    }
     double2* out = reinterpret_cast<double2*>(PS + ((size_t)e * nd + t) * 4);
     out[0] = make_double2(o[0], o[1]);
     out[1] = make_double2(o[2], o[3]);
@@ -1278,17 +1267,28 @@ int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers
   return launches;
 }
 
+// Shape-function gather variant for N <= 3 (compile-time choice, 5 by default): 5 = round-robin staging,
+// one DOF per lane; 2 = staging one source element at a time, one DOF per lane.
+#ifndef PIC_SF_GATHER
+#define PIC_SF_GATHER 5
+#endif
+
+template <int N, bool MIXED>
+static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
+#if PIC_SF_GATHER == 5
+  k_sf_gather5<N, MIXED><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+#else
+  k_sf_gather2<N, MIXED><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+#endif
+}
+
+int sf_gather_variant() { return PIC_SF_GATHER; }
+
 int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
   switch (A.N) {
-    case 1: if (A.mixed) k_sf_gather2<1, true><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-            else k_sf_gather2<1, false><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-            break;
-    case 2: if (A.mixed) k_sf_gather2<2, true><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-            else k_sf_gather2<2, false><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-            break;
-    case 3: if (A.mixed) k_sf_gather2<3, true><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-            else k_sf_gather3<false><<<A.M.ne, kSf3Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-            break;
+    case 1: if (A.mixed) launch_gather_n<1, true>(A, B, L, K, PS); else launch_gather_n<1, false>(A, B, L, K, PS); break;
+    case 2: if (A.mixed) launch_gather_n<2, true>(A, B, L, K, PS); else launch_gather_n<2, false>(A, B, L, K, PS); break;
+    case 3: if (A.mixed) launch_gather_n<3, true>(A, B, L, K, PS); else launch_gather_n<3, false>(A, B, L, K, PS); break;
     default:   // nd > 64: one thread per DOF, single phase
       if (A.mixed) k_sf_gather_mixed<4><<<A.M.ne, SfShape<4>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
       else k_sf_gather_fp64<4><<<A.M.ne, SfShape<4>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);

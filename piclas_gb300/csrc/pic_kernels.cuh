@@ -61,6 +61,7 @@ int launch_cvwm_fused(const LaunchArgs& A, const DevParticles& P, double dt);
 int launch_node_to_dof(const LaunchArgs& A, double* part_source);
 int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B);
 int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K);
+int sf_gather_variant();   // compile-time shape-function gather variant (PIC_SF_GATHER)
 int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* part_source);
 int launch_deposit_sf(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L,
                       const SfPack& K, double* part_source);
