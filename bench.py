@@ -146,6 +146,19 @@ def read_traffic(key: str):
     return None
 
 
+def replica_rate(n_local: int, steps: int, seconds_local: float, dist=None, device: str = "cpu"):
+    """Whole-job particle-steps/s of independent replicas (one per rank, no data-path collective):
+    particles summed over the ranks, time of the slowest rank.  Returns (rate, slowest seconds)."""
+    if dist is None:
+        return n_local * steps / seconds_local, seconds_local
+    import torch
+    t = torch.tensor([seconds_local], dtype=torch.float64, device=device)
+    n = torch.tensor([float(n_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(n.item()) * steps / float(t.item()), float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples while the timed region runs."""
 
@@ -310,11 +323,8 @@ def run_gpu(args, rank, world, local_rank):
 
     with ClockSampler(local_rank) as clk:
         ms, launches = timed(args.steps)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = w.n * world * args.steps / (ms / 1e3)
+    value, ms = replica_rate(w.n, args.steps, ms / 1e3, dist, "cuda")
+    ms *= 1e3
     st = loop.status()
 
     # dominant kernel, timed live with CUDA events on the library's stream
@@ -338,12 +348,8 @@ def run_gpu(args, rank, world, local_rank):
         loop.set_field_ptr(E_host.data_ptr())
         loop.time_step_ptr(w.dt, 1, PS_host.data_ptr())
     te = time.perf_counter() - te0
-    e2e = {"value": w.n * world * args.steps / te if world == 1 else None, "unit": "particle-steps/s",
+    e2e = {"value": replica_rate(w.n, args.steps, te, dist, "cuda")[0], "unit": "particle-steps/s",
            "h2d_bytes_per_step": int(E_host.numel() * 8), "d2h_bytes_per_step": int(PS_host.numel() * 8)}
-    if dist:
-        t = torch.tensor([te], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e["value"] = w.n * world * args.steps / float(t.item())
 
     out = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,

@@ -114,7 +114,7 @@ typedef struct pic_mesh_t {
   const double* node_coords;    /* NodeCoords_Shared(1:3,8*nElems): corners, tensor order */
   const int32_t* elem_node;     /* ElemNodeID_Shared(1:8,nElems): CGNS corner order, 1-based into node_coords */
   const int32_t* elem_side_node;/* ElemSideNodeID_Shared(1:4,1:6,nElems)+1, 1-based into node_coords */
-  const int32_t* side_nb_elem;  /* SideInfo_Shared(SIDE_NBELEMID) per (1:6,nElems), 1-based */
+  const int32_t* side_nb_elem;  /* SideInfo_Shared(SIDE_NBELEMID) per (1:6,nElems), 1-based; 0 at walls */
   const int32_t* side_pvid;     /* BoundaryType(SIDE_BCID,BC_ALPHA) per (1:6,nElems): 0 inner, +-k periodic */
   const int32_t* concave_side;  /* ConcaveElemSide_Shared(1:6,nElems) as 0/1             */
   /* cell_volweight_mean */
@@ -131,6 +131,11 @@ typedef struct pic_mesh_t {
   const int32_t* fibgm_offset;  /* FIBGM_offsetElem(i,j,k)                              */
   const int32_t* fibgm_element; /* FIBGM_Element(:), 1-based                            */
   int32_t fibgm_n_total;
+  /* particle boundaries of non-periodic sides (TriaTracking + cell_volweight_mean only):
+   * PartBound%TargetBoundCond of the side's BC per (1:6,nElems): 1 open (RemoveParticle),
+   * 2 reflective (PerfectReflection: MomentumACC = 0, no wall velocity), 0 for inner and periodic
+   * sides; a side with side_nb_elem = 0 must be 1 or 2.  NULL: every side is inner or periodic. */
+  const int32_t* side_bc;
 } pic_mesh_t;
 
 typedef struct pic_status_t {

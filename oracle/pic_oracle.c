@@ -420,6 +420,33 @@ static double intersection_with_wall(const pic_mesh_t* m, const double Pold[3], 
   return alpha;
 }
 
+/* CalcNormAndTangTriangle, particle_surfaces.f90:256-319 (TriaTracking): unit normal of triangle TriNum of
+ * a side, (Node(TriNum+1)-Node1) x (Node(TriNum+2)-Node1) normalised (the routine's two sign flips cancel) */
+static void triangle_normal(const pic_mesh_t* m, int s, int e, int triNum, double nrm[3]) {
+  int n0 = SIDENODE(m, 0, s, e), n1 = SIDENODE(m, triNum, s, e), n2 = SIDENODE(m, triNum + 1, s, e);
+  double V1[3] = {NODE(m, 0, n1) - NODE(m, 0, n0), NODE(m, 1, n1) - NODE(m, 1, n0), NODE(m, 2, n1) - NODE(m, 2, n0)};
+  double V2[3] = {NODE(m, 0, n2) - NODE(m, 0, n0), NODE(m, 1, n2) - NODE(m, 1, n0), NODE(m, 2, n2) - NODE(m, 2, n0)};
+  double nx = -V1[1] * V2[2] + V1[2] * V2[1];
+  double ny = -V1[2] * V2[0] + V1[0] * V2[2];
+  double nz = -V1[0] * V2[1] + V1[1] * V2[0];
+  double nVal = sqrt(nx * nx + ny * ny + nz * nz);
+  nrm[0] = -nx / nVal; nrm[1] = -ny / nVal; nrm[2] = -nz / nVal;
+}
+
+/* PerfectReflection, surfacemodel_tools.f90:81-256, without wall velocity or rotating frame: the velocity and
+ * the remaining trajectory are mirrored at the point of intersection, which becomes LastPartPos */
+static void perfect_reflection(double v[3], double x[3], double xl[3], const double traj_in[3], double len,
+                               double alpha, const double nrm[3]) {
+  double poi[3], traj[3] = {traj_in[0], traj_in[1], traj_in[2]};
+  for (int c = 0; c < 3; ++c) poi[c] = xl[c] + traj[c] * alpha;
+  double dv = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2];
+  for (int c = 0; c < 3; ++c) v[c] = v[c] - 2.0 * dv * nrm[c];
+  for (int c = 0; c < 3; ++c) xl[c] = poi[c];
+  double dt = traj[0] * nrm[0] + traj[1] * nrm[1] + traj[2] * nrm[2];
+  for (int c = 0; c < 3; ++c) traj[c] = traj[c] - 2.0 * dt * nrm[c];
+  for (int c = 0; c < 3; ++c) x[c] = xl[c] + traj[c] * (len - alpha);
+}
+
 #define ORC_MAX_TRACK_LOOPS 10000
 
 /* SingleParticleTriaTracking3D, particle_triatracking.f90:137-484 */
@@ -481,6 +508,18 @@ static void tria_track_single(const pic_config_t* cfg, const pic_mesh_t* m, orc_
     }
     const int pvid = m->side_pvid[(size_t)(elem - 1) * 6 + localSide];
     const int nb = m->side_nb_elem[(size_t)(elem - 1) * 6 + localSide];
+    const int bc = m->side_bc ? m->side_bc[(size_t)(elem - 1) * 6 + localSide] : 0;
+    /* particle boundary of a wall side (particle_triatracking.f90:409-433, GetBoundaryInteraction
+     * particle_boundary_condition.f90:35-221) */
+    if (bc == 1) { p->inside[ip] = 0; return; }            /* open: RemoveParticle, not a lost particle */
+    if (bc == 2) {                                          /* reflective: PerfectReflection, same element */
+      double alpha = intersection_with_wall(m, xl, traj, localSide, elem, triNum);
+      double nrm[3];
+      triangle_normal(m, localSide, elem, triNum, nrm);
+      perfect_reflection(&p->part_state[(size_t)ip * 6 + 3], x, xl, traj, len, alpha, nrm);
+      memset(doneLast, 0, sizeof(doneLast));
+      continue;
+    }
     for (int q = 5; q >= 1; --q) for (int c = 0; c < 4; ++c) doneLast[q][c] = doneLast[q - 1][c];
     doneLast[0][0] = elem; doneLast[0][1] = localSide; doneLast[0][2] = triNum; doneLast[0][3] = sideID;
     if (pvid != 0) {

@@ -59,6 +59,7 @@ class PicMesh(C.Structure):
         ("periodic_nodes", _ip), ("n_total_periodic_nodes", C.c_int32),
         ("fibgm_imax", C.c_int32 * 3), ("fibgm_deltas", C.c_double * 3), ("fibgm_n_elems", _ip),
         ("fibgm_offset", _ip), ("fibgm_element", _ip), ("fibgm_n_total", C.c_int32),
+        ("side_bc", _ip),
     ]
 
 
@@ -132,9 +133,9 @@ class MeshStruct:
         s.n_elems = mesh.n_elems
         s.n_geo = mesh.n_geo
         s.n_nodes = mesh.n_nodes
-        s.n_periodic_vectors = 3
         pv = mesh.periodic_vectors  # column k = vector k
-        for k in range(3):
+        s.n_periodic_vectors = int(pv.shape[1])
+        for k in range(pv.shape[1]):
             for c in range(3):
                 s.periodic_vectors[k * 3 + c] = float(pv[c, k])
         for c in range(3):
@@ -173,6 +174,7 @@ class MeshStruct:
         s.fibgm_offset = i("fo", mesh.fibgm_offset)
         s.fibgm_element = i("fe", mesh.fibgm_element)
         s.fibgm_n_total = int(len(mesh.fibgm_element))
+        s.side_bc = i("sbc", mesh.side_bc) if mesh.side_bc is not None else C.POINTER(C.c_int32)()
         self.struct = s
         self._keep = keep
 

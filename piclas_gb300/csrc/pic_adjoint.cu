@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(128) k_adj_fwd(DevMesh M, AdjState S, const T*
   double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
   for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
-  int ne = tria_track(M, e, x, xl);
+  double vw[3] = {0.0, 0.0, 0.0};     // the adjoint runs on meshes without walls: no reflection
+  int ne = tria_track(M, e, x, xl, vw);
   if (ne < 0) { flag_status(st, ne == -1 ? 0x01u : 0x04u); ne = e; }
   S.x[i] = x[0]; S.y[i] = x[1]; S.z[i] = x[2];
   vx[i] = v[0]; vy[i] = v[1]; vz[i] = v[2];
@@ -510,6 +511,8 @@ extern "C" int pic_adjoint_run(pic_ctx_t* c, const pic_adjoint_cfg_t* a, const d
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "adjoint configuration");
   if (a->precision != PIC_PREC_FP64 && a->precision != PIC_PREC_MIXED)
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "adjoint precision");
+  if (c->has_walls)
+    return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs a mesh without open/reflective sides");
   if (!c->field_set || !c->have_particles) return pic_internal::set_error(PIC_ERR_STATE, "field and particles must be set first");
   if (cudaMemcpyToSymbolAsync(c_k, &c->k, sizeof(Consts), 0, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
     return pic_internal::set_error(PIC_ERR_CUDA, "adjoint constants");

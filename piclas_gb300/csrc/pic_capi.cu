@@ -323,8 +323,15 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
           return bail(fail(PIC_ERR_INVALID_ARGUMENT, "node_coords must hold each element's 8 corners (tensor order)"));
     for (int s = 0; s < 6; ++s) {
       const int nb = m->side_nb_elem[e * 6 + s];
-      if (nb < 1 || nb > ne) return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_nb_elem out of range (open boundaries are not supported)"));
-      side_nb[e * 6 + s] = nb - 1;
+      const int bc = m->side_bc ? m->side_bc[e * 6 + s] : 0;
+      if (bc < 0 || bc > 3) return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_bc must be 0..3"));
+      const bool wall = bc == 1 || bc == 2;
+      if (wall ? nb != 0 : (nb < 1 || nb > ne))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_nb_elem must be 1..nElems, or 0 exactly at open/reflective sides"));
+      if (wall && (cfg->tracking != PIC_TRACK_TRIA || cfg->deposition != PIC_DEPO_CVWM))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "open/reflective particle boundaries need TriaTracking + cell_volweight_mean"));
+      c->has_walls = c->has_walls || wall;
+      side_nb[e * 6 + s] = wall ? -1 : nb - 1;
       uint32_t info = 0;
       for (int q = 0; q < 4; ++q) {
         const int t = m->elem_side_node[((size_t)e * 6 + s) * 4 + q] - 1 - 8 * e;
@@ -336,6 +343,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       if (pv < -m->n_periodic_vectors || pv > m->n_periodic_vectors)
         return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_pvid out of range"));
       info |= ((uint32_t)(uint8_t)(int8_t)pv) << 16;
+      if (wall) info |= (uint32_t)bc << 24;     // 1 open, 2 reflective
       side_info[e * 6 + s] = info;
     }
   }

@@ -447,6 +447,8 @@ __device__ __forceinline__ void boris_push(double v[3], const double F[6], int s
 // ==========================================================================================
 __device__ __forceinline__ int side_corner(uint32_t info, int q) { return (info >> (3 * q)) & 7; }
 __device__ __forceinline__ bool side_concave(uint32_t info) { return (info >> 12) & 1; }
+// particle boundary of a wall side: 0 none (inner or periodic), 1 open, 2 reflective
+__device__ __forceinline__ int side_wall(uint32_t info) { return (info >> 24) & 3; }
 __device__ __forceinline__ int side_pvid(uint32_t info) { return (int)(int8_t)((info >> 16) & 0xff); }
 
 // ParticleInsideQuad3D, particle_mesh_tools.f90:78-222
@@ -587,9 +589,47 @@ __device__ __forceinline__ bool certainly_inside_f32(const DevMesh& M, int e, co
   return true;
 }
 
-// Walk from `elem` (= LastElem); updates x / xl at periodic crossings.  Returns the new element,
-// -1 if the particle is lost, -2 if the hop cap was hit.
-static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double x[3], double xl[3]) {
+// CalcNormAndTangTriangle, particle_surfaces.f90:256-319 (TriaTracking): unit normal of triangle `tri`,
+// (P(tri+1)-P1) x (P(tri+2)-P1) normalised (the routine's two sign flips cancel)
+__device__ __forceinline__ void triangle_normal(const double* __restrict__ X, uint32_t info, int tri, double n[3]) {
+  const int t0 = side_corner(info, 0), t1 = side_corner(info, tri), t2 = side_corner(info, tri + 1);
+  double V1[3], V2[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double p0 = __ldg(X + 3 * t0 + c);
+    V1[c] = __ldg(X + 3 * t1 + c) - p0;
+    V2[c] = __ldg(X + 3 * t2 + c) - p0;
+  }
+  const double nx = -V1[1] * V2[2] + V1[2] * V2[1];
+  const double ny = -V1[2] * V2[0] + V1[0] * V2[2];
+  const double nz = -V1[0] * V2[1] + V1[1] * V2[0];
+  const double nVal = sqrt(nx * nx + ny * ny + nz * nz);
+  n[0] = -nx / nVal; n[1] = -ny / nVal; n[2] = -nz / nVal;
+}
+
+// PerfectReflection, surfacemodel_tools.f90:81-256, without wall velocity or rotating frame: velocity and the
+// rest of the trajectory mirrored at the point of intersection, which becomes LastPartPos
+__device__ __forceinline__ void perfect_reflection(double v[3], double x[3], double xl[3], const double traj_in[3],
+                                                   double len, double alpha, const double n[3]) {
+  double poi[3], traj[3] = {traj_in[0], traj_in[1], traj_in[2]};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) poi[c] = xl[c] + traj[c] * alpha;
+  const double dv = v[0] * n[0] + v[1] * n[1] + v[2] * n[2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) v[c] = v[c] - 2.0 * dv * n[c];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) xl[c] = poi[c];
+  const double dt = traj[0] * n[0] + traj[1] * n[1] + traj[2] * n[2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) traj[c] = traj[c] - 2.0 * dt * n[c];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) x[c] = xl[c] + traj[c] * (len - alpha);
+}
+
+// Walk from `elem` (= LastElem); updates x / xl at periodic crossings and x / xl / v at reflective walls.
+// Returns the new element, -1 if the particle is lost, -2 if the hop cap was hit, -3 if it left through an
+// open boundary (RemoveParticle; not a lost particle).
+static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double x[3], double xl[3], double v[3]) {
   if (certainly_inside_f32(M, elem, x)) return elem;     // same decision as the FP64 test below
   int doneE[6] = {0, 0, 0, 0, 0, 0}, doneS[6] = {0, 0, 0, 0, 0, 0}, doneT[6] = {0, 0, 0, 0, 0, 0};
   // doneE/doneS/doneT hold DoneLastElem(1/4/3, 1:6) with 1-based element and side ids (0 = empty)
@@ -645,6 +685,19 @@ static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double
     const uint32_t info = __ldg(sinfo + localSide);
     const int pvid = side_pvid(info);
     const int nb = __ldg(M.side_nb + (size_t)elem * 6 + localSide);
+    // particle boundary of a wall side (particle_triatracking.f90:409-433, GetBoundaryInteraction
+    // particle_boundary_condition.f90:35-221)
+    const int wall = side_wall(info);
+    if (wall == 1) return -3;
+    if (wall == 2) {
+      const double alpha = wall_alpha(X, info, xl, traj, triNum);
+      double n[3];
+      triangle_normal(X, info, triNum, n);
+      perfect_reflection(v, x, xl, traj, len, alpha, n);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) { doneE[q] = 0; doneS[q] = 0; doneT[q] = 0; }
+      continue;
+    }
 #pragma unroll
     for (int q = 5; q >= 1; --q) { doneE[q] = doneE[q - 1]; doneS[q] = doneS[q - 1]; doneT[q] = doneT[q - 1]; }
     doneE[0] = elem + 1; doneS[0] = elem * 6 + localSide + 1; doneT[0] = triNum;

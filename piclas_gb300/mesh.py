@@ -152,7 +152,7 @@ class BoxMesh:
     n_elems: int
     n_nodes: int
     n_geo: int
-    periodic_vectors: np.ndarray          # (3,3): column k = PeriodicVectors(:,k)
+    periodic_vectors: np.ndarray          # (3, nPeriodicVectors): column k = PeriodicVectors(:,k)
     xi_cl_ngeo: np.ndarray
     wbary_cl_ngeo: np.ndarray
     xgp: np.ndarray
@@ -186,6 +186,8 @@ class BoxMesh:
     fibgm_offset: np.ndarray
     fibgm_element: np.ndarray             # 1-based
     canonical_node: np.ndarray = field(default=None)  # 0-based periodic-unique id per unique node
+    side_bc: np.ndarray = field(default=None)         # (6,nElems) 1 open / 2 reflective wall, 0 otherwise; None: no walls
+    bc: tuple = ("periodic", "periodic", "periodic")  # particle boundary per axis
 
     @property
     def n_dof(self) -> int:
@@ -203,13 +205,25 @@ def _wrap(v, n):
     return v % n
 
 
+WALL_BC = {"open": 1, "reflective": 2}      # PartBound%TargetBoundCond
+
+
 def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
-                   perturb: float = 0.0, refmapping_eps: float = 1.0e-4) -> BoxMesh:
-    """Build a fully periodic box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
+                   perturb: float = 0.0, refmapping_eps: float = 1.0e-4,
+                   bc=("periodic", "periodic", "periodic")) -> BoxMesh:
+    """Build a box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
 
     ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
     along each axis (h per axis); boundary nodes stay put so the periodic faces match.
+    ``bc`` gives the particle boundary of both faces of each axis: "periodic" (a periodic vector, node
+    twins for cell_volweight_mean), "open" or "reflective" (wall sides without a neighbour: SIDE_NBELEMID
+    = 0, master orientation, convex).
     """
+    bc = tuple(bc)
+    if len(bc) != 3 or any(b not in ("periodic", "open", "reflective") for b in bc):
+        raise ValueError(f"bc must hold 'periodic', 'open' or 'reflective' per axis, got {bc}")
+    periodic = [b == "periodic" for b in bc]
+    pv_index = {d: q + 1 for q, d in enumerate([d for d in range(3) if periodic[d]])}   # 1-based vector id
     lo = np.asarray(lo, dtype=np.float64)
     hi = np.asarray(hi, dtype=np.float64)
     L = hi - lo
@@ -341,21 +355,27 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         a, b, c = t & 1, (t >> 1) & 1, (t >> 2) & 1
         return ((int(ijk[e, 0]) + a) % nx, (int(ijk[e, 1]) + b) % ny, (int(ijk[e, 2]) + c) % nz)
 
+    side_bc = np.zeros((ne, 6), dtype=np.int32)
     for e in range(ne):
         for s in range(6):
             off = SIDE_OFFSET[s]
             n3 = [int(ijk[e, d]) + off[d] for d in range(3)]
             pv = 0
+            wall = 0
             for d in range(3):
                 if n3[d] < 0 or n3[d] >= dims[d]:
-                    # crossing the +face moves the particle by -PeriodicVector(d), the -face by +
-                    pv = -(d + 1) if n3[d] >= dims[d] else (d + 1)
+                    if periodic[d]:
+                        # crossing the +face moves the particle by -PeriodicVector, the -face by +
+                        pv = -pv_index[d] if n3[d] >= dims[d] else pv_index[d]
+                    else:
+                        wall = WALL_BC[bc[d]]
                 n3[d] = _wrap(n3[d], dims[d])
             en = n3[0] + nx * (n3[1] + ny * n3[2])
-            side_nb[e, s] = en + 1
+            side_nb[e, s] = 0 if wall else en + 1
             side_pvid[e, s] = pv
+            side_bc[e, s] = wall
             cg = SIDE_CGNS[s]
-            if SIDE_IS_PLUS[s]:
+            if SIDE_IS_PLUS[s] or wall:      # walls are master sides (flip 0)
                 nstart = 0
                 side_flip[e, s] = 0
             else:
@@ -383,7 +403,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                       + (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * A[2][2])
             if detcon < 0.0:
                 concave[e, s] = 1
-            elif detcon == 0.0:
+            elif detcon == 0.0 and side_nb[e, s] > 0:      # walls: SIDE_NBSIDEID = 0, never concave
                 en = side_nb[e, s] - 1
                 # neighbour's local side facing back
                 s_back = {0: 5, 5: 0, 1: 3, 3: 1, 2: 4, 4: 2}[s]
@@ -417,7 +437,8 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     # ---- periodic twins (pic_depo.f90:1218-2089) --------------------------------------
     canon = np.empty(n_unique, dtype=np.int64)
     gk_, gj_, gi_ = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
-    canon[:] = ((gi_ % nx) + nx * ((gj_ % ny) + ny * (gk_ % nz))).reshape(-1)
+    px, py, pz = (nx if periodic[0] else nx + 1), (ny if periodic[1] else ny + 1), (nz if periodic[2] else nz + 1)
+    canon[:] = ((gi_ % px) + px * ((gj_ % py) + py * (gk_ % pz))).reshape(-1)
     order = np.argsort(canon, kind="stable")
     groups = {}
     for u in order:
@@ -455,8 +476,9 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     fib_off[1:] = np.cumsum(fib_n)[:-1]
     fib_el = np.array([x for c in cells for x in c], dtype=np.int32)
 
-    pv = np.zeros((3, 3))
-    pv[0, 0], pv[1, 1], pv[2, 2] = L[0], L[1], L[2]   # column k = PeriodicVectors(:,k)
+    pv = np.zeros((3, len(pv_index)))                 # column k = PeriodicVectors(:,k)
+    for d, q in pv_index.items():
+        pv[d, q - 1] = L[d]
 
     return BoxMesh(
         nx=nx, ny=ny, nz=nz, N=N, lo=lo, hi=hi, n_elems=ne, n_nodes=n_unique, n_geo=1,
@@ -474,6 +496,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         periodic_n_nodes=per_n, periodic_offset=per_off, periodic_nodes=per_nodes,
         fibgm_imax=fib_imax, fibgm_deltas=fib_d, fibgm_n_elems=fib_n, fibgm_offset=fib_off,
         fibgm_element=fib_el, canonical_node=canon,
+        side_bc=side_bc if side_bc.any() else None, bc=bc,
     )
 
 

@@ -280,3 +280,73 @@ def test_mixed_error_per_step_plasma_wave(gpu_lib):
         assert r["v"] <= 1e-5, r
         assert r["x_m"] <= 1e-9, r
         assert r["elem_mismatch"] == 0, r
+
+
+@pytest.mark.parametrize("N", [1, 2])
+def test_sf_gather_low_order(gpu_lib, oracle_lib, N):
+    """Shape-function gather for N = 1, 2 (8 and 27 DOFs per element: one DOF half, four particle
+    parities per CTA) in FP64 and mixed against the oracle."""
+    w = workloads.curved_two_species(n_cells=5, N=N, n_per_species=1500, seed=11, nsteps=2)
+    g = _run_gpu(w, 2)
+    st, PS = _run_oracle(oracle_lib, w, 2)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["PS"], PS) <= 1e-12
+    gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
+    assert np.array_equal(gm["elem"], st.elem)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-4
+
+
+# ---- particle boundaries: open and reflective walls --------------------------------------------
+def _wall_workload(seed=21, n=6000):
+    mesh = build_box_mesh(5, 5, 5, 2, bc=("reflective", "open", "periodic"))
+    return workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=2000.0, seed=seed, dt=2e-10)
+
+
+def test_walls_fp64_bitexact(gpu_lib, oracle_lib):
+    """Reflective x walls, open y walls, periodic z: 12 fused steps bit-exact against the oracle
+    (removed particles keep their last state, inside = 0, and are not counted as lost)."""
+    w = _wall_workload()
+    g = _run_gpu(w, 12)
+    st, PS = _run_oracle(oracle_lib, w, 12)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["n_lost"] == 0 and g["status"]["error_word"] == 0
+    assert (st.inside == 0).sum() > 200                                   # the open walls removed particles
+    assert (np.sign(st.part_state[:, 3]) != np.sign(w.part_state[:, 3])).sum() > 200   # reflections
+
+
+def test_walls_separate_routines_and_mixed(gpu_lib, oracle_lib):
+    """The same walls through pic_push + pic_track (FP64, bit-exact) and the mixed fused step."""
+    w = _wall_workload(seed=22, n=3000)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    loop = ParticleLoop(cfg, w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    for _ in range(6):
+        oracle_lib.save_last(st)
+        oracle_lib.interpolate(cfg, ms, w.e_dof, st)
+        loop.interpolate_field_to_particle()
+        oracle_lib.push(cfg, st, w.dt)
+        loop.push(w.dt)
+        oracle_lib.track(cfg, ms, st)
+        loop.perform_tracking()
+    g = loop.download_particles()
+    loop.close()
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    gm = _run_gpu(w, 6, precision=capi.PIC_PREC_MIXED)
+    st6, PS6 = _run_oracle(oracle_lib, w, 6)
+    assert abs(int(gm["inside"].sum()) - int(st6.inside.sum())) <= 2
+    assert _rel(gm["PS"][..., 3], PS6[..., 3]) <= 1e-5
+
+
+def test_walls_rejected_where_unsupported(gpu_lib):
+    w = _wall_workload(n=100)
+    cfg = capi.make_config(w.mesh.N, capi.PIC_TRACK_REFMAPPING, capi.PIC_DEPO_CVWM, capi.PIC_PREC_FP64, w.species, 100)
+    with pytest.raises(PicError) as e:
+        ParticleLoop(cfg, w.mesh)
+    assert e.value.code == 1

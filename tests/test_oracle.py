@@ -163,3 +163,58 @@ def test_shape_function_charge(oracle_lib):
     total = 800 * w.species[0][0] * w.species[0][2]
     q = oracle_lib.integrate_charge(ms, w.mesh.N, PS)
     assert abs(q - total) <= 2e-3 * abs(total)      # quadrature of the kernel on the DG grid
+
+
+# ---- particle boundaries: open and reflective walls (TriaTracking) ----------------------------
+def _wall_case(bc, n=4000, T_eV=2000.0, seed=9, cells=5, N=2, field=False):
+    mesh = build_box_mesh(cells, cells, cells, N, bc=bc)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=T_eV, seed=seed, dt=2e-10)
+    if not field:
+        w.e_dof[:] = 0.0
+    return w
+
+
+def _oracle_steps(oracle_lib, w, nsteps):
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species, is_new=np.zeros(w.n, np.uint8))
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, nsteps)
+    return st
+
+
+def test_wall_mesh_arrays():
+    m = build_box_mesh(3, 3, 3, 1, bc=("reflective", "open", "periodic"))
+    assert m.periodic_vectors.shape == (3, 1) and m.periodic_vectors[2, 0] == 1.0
+    walls = m.side_nb_elem == 0
+    assert np.array_equal(walls, m.side_bc > 0)
+    assert (m.side_bc == 2).sum() == 2 * 9 and (m.side_bc == 1).sum() == 2 * 9
+    assert np.all(np.abs(m.side_pvid[walls]) == 0) and set(np.unique(np.abs(m.side_pvid))) == {0, 1}
+    assert not m.concave_side[walls].any()
+    # node twins only across the periodic z faces; node volumes still add up to the box volume
+    assert m.periodic_n_nodes.max() == 1
+    assert abs(m.node_volume.sum() - (1.0 + m.node_volume[m.periodic_n_nodes > 0].sum() / 2.0)) < 1e-12
+
+
+def test_reflective_walls_keep_particles(oracle_lib):
+    w = _wall_case(("reflective", "reflective", "reflective"))
+    st = _oracle_steps(oracle_lib, w, 30)
+    x, v0, v = st.part_state[:, :3], w.part_state[:, 3:], st.part_state[:, 3:]
+    assert st.inside.all() and st.counters.n_lost == 0
+    assert (x >= 0.0).all() and (x <= 1.0).all()
+    # specular reflection keeps |v| (no field); many particles were reflected at least once
+    assert np.allclose(np.linalg.norm(v, axis=1), np.linalg.norm(v0, axis=1), rtol=1e-13, atol=0.0)
+    assert (np.sign(v) != np.sign(v0)).any(axis=1).sum() > 500
+    assert np.array_equal(st.elem, workloads._elem_of_uniform(w.mesh, x))
+
+
+def test_open_walls_remove_the_leaving_particles(oracle_lib):
+    w = _wall_case(("open", "periodic", "periodic"))
+    K = 30
+    st = _oracle_steps(oracle_lib, w, K)
+    # free streaming: a particle is removed iff its straight path ends outside 0 < x < 1
+    xf = w.part_state[:, 0] + w.part_state[:, 3] * (w.dt * K)
+    clear = (np.abs(xf) > 1e-9) & (np.abs(xf - 1.0) > 1e-9)
+    expect = (xf > 0.0) & (xf < 1.0)
+    assert np.array_equal(st.inside[clear].astype(bool), expect[clear])
+    assert (~expect).sum() > 300 and st.counters.n_lost == 0
+    kept = st.inside.astype(bool)
+    assert np.array_equal(st.elem[kept], workloads._elem_of_uniform(w.mesh, st.part_state[kept, :3]))

@@ -1,0 +1,53 @@
+"""Multi-GPU is replicas only: the one cross-rank step of bench.py is the whole-job rate (particles summed
+over ranks, time of the slowest rank).  Checked here with two gloo ranks on the CPU."""
+import os
+import socket
+import sys
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # rank r ran 100 (r+1) particles for 5 steps in 1 + r seconds
+    rate, slowest = bench.replica_rate(100 * (rank + 1), 5, 1.0 + rank, dist, "cpu")
+    out.put((rank, rate, slowest))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_replica_rate_two_gloo_ranks():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for _, rate, slowest in res:
+        assert slowest == 2.0
+        assert rate == pytest.approx((100 + 200) * 5 / 2.0)
+
+
+def test_replica_rate_single_process():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.replica_rate(1000, 4, 2.0) == (2000.0, 2.0)
