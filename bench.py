@@ -243,6 +243,9 @@ def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0
     per = max((t2 - t1) / max(n2 - n1, 1), 1e-9)
     fixed = max(t1 - per * n1, 0.0)
     n_sample = int(min(max((target_s - fixed) / per, n1), n_full))
+    if n_sample == n_full:
+        # the whole workload fits: time more steps instead (at most 1000) so the sample lasts ~target_s
+        steps = int(min(max(steps, target_s / max(fixed + per * n_full, 1e-6)), 1000))
     ws = sample(n_sample)
     if warmup > 0:
         run(ws, 1)

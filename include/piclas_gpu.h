@@ -62,7 +62,9 @@ typedef enum pic_error_t {
 
 /* ---- option enums ------------------------------------------------------- */
 enum { PIC_TRACK_TRIA = 1, PIC_TRACK_REFMAPPING = 2 };     /* TrackingMethod           */
-enum { PIC_DEPO_CVWM = 1, PIC_DEPO_SHAPE_FUNCTION = 2 };   /* PIC-Deposition-Type      */
+/* PIC-Deposition-Type: cell_volweight_mean, shape_function, shape_function_cc (charge-corrected: each
+ * particle's deposit scaled so that its quadrature integral is exactly q*MPF; periodic meshes) */
+enum { PIC_DEPO_CVWM = 1, PIC_DEPO_SHAPE_FUNCTION = 2, PIC_DEPO_SHAPE_FUNCTION_CC = 3 };
 enum { PIC_PREC_FP64 = 0, PIC_PREC_MIXED = 1 };            /* arithmetic variant       */
 
 #define PIC_MAX_SPECIES 8

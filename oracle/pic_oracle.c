@@ -847,7 +847,59 @@ static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m,
       }
 }
 
-/* DepositionMethod_SF, pic_depo_method.f90:851-1003 + calcSfSource (shapefunction_tools:30-164) */
+/* calcTotalChargePeriodic_cc, pic_depo_shapefunction_tools.f90:425-555 (dim_sf = 3): the quadrature
+ * integral sum wGP(k) wGP(l) wGP(m) Fac S1 / sJ over the DOFs within r_sf of one (shifted) position, added
+ * term by term to the running total (totalChargePeriodicSF is INOUT across the 27 images) */
+static double total_charge_cc(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], double Fac4,
+                              double totalCharge, double r_sf, double r2_sf, double r2_sf_inv, uint8_t* done) {
+  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  memset(done, 0, (size_t)m->n_elems);
+  int kmax = (int)ceil((P[0] + r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0]);
+  int kmin = (int)floor((P[0] - r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0] + 1);
+  int lmax = (int)ceil((P[1] + r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1]);
+  int lmin = (int)floor((P[1] - r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1] + 1);
+  int mmax = (int)ceil((P[2] + r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2]);
+  int mmin = (int)floor((P[2] - r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2] + 1);
+  if (kmax > m->fibgm_imax[0]) kmax = m->fibgm_imax[0];
+  if (kmin < 1) kmin = 1;
+  if (lmax > m->fibgm_imax[1]) lmax = m->fibgm_imax[1];
+  if (lmin < 1) lmin = 1;
+  if (mmax > m->fibgm_imax[2]) mmax = m->fibgm_imax[2];
+  if (mmin < 1) mmin = 1;
+  for (int kk = kmin; kk <= kmax; ++kk)
+    for (int ll = lmin; ll <= lmax; ++ll)
+      for (int mm = mmin; mm <= mmax; ++mm) {
+        size_t cidx = (size_t)(kk - 1) + (size_t)m->fibgm_imax[0] * ((ll - 1) + (size_t)m->fibgm_imax[1] * (mm - 1));
+        int nE = m->fibgm_n_elems[cidx], off = m->fibgm_offset[cidx];
+        for (int q = 0; q < nE; ++q) {
+          int e = m->fibgm_element[off + q];
+          if (done[e - 1]) continue;
+          const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
+          double v0 = P[0] - b[0], v1 = P[1] - b[1], v2 = P[2] - b[2];
+          if (sqrt(v0 * v0 + v1 * v1 + v2 * v2) > (r_sf + m->elem_radius[e - 1])) continue;
+          const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
+          const double* sj = &m->elem_sj[(size_t)(e - 1) * ndof];
+          for (int mz = 0; mz <= N; ++mz)
+            for (int l = 0; l <= N; ++l)
+              for (int k = 0; k <= N; ++k) {
+                int r = mz * n1 * n1 + l * n1 + k;
+                double d0 = P[0] - xg[(size_t)r * 3], d1 = P[1] - xg[(size_t)r * 3 + 1], d2 = P[2] - xg[(size_t)r * 3 + 2];
+                double radius2 = (d0 * d0 + d1 * d1) + d2 * d2;
+                if (radius2 <= r2_sf) {
+                  double S = 1.0 - r2_sf_inv * radius2;
+                  double S1 = S * S;
+                  for (int ex = 3; ex <= cfg->sf_alpha; ++ex) S1 = S * S1;
+                  totalCharge = totalCharge + m->wgp[k] * m->wgp[l] * m->wgp[mz] * Fac4 * S1 / sj[r];
+                }
+              }
+          done[e - 1] = 1;
+        }
+      }
+  return totalCharge;
+}
+
+/* DepositionMethod_SF, pic_depo_method.f90:851-1003 + calcSfSource (shapefunction_tools:30-164);
+ * shape_function_cc with periodic images: calcSfSource:96-120 (totalChargePeriodicSF, Fac*Fac(4)/total) */
 static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* PS, int nthreads) {
   const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
   const size_t nps = (size_t)m->n_elems * ndof * 4;
@@ -880,7 +932,21 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
       double cm = cfg->charge[sp] * cfg->mpf[sp];
       double Fac[4] = {s[3] * cm, s[4] * cm, s[5] * cm, cm};
       if (nCases > 1) {
-        for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * w_sf;
+        if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC) {
+          double totalCharge = 0.0;
+          for (int ic = 0; ic < 27; ++ic) {
+            double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);
+            double Ps[3];
+            for (int d = 0; d < 3; ++d)
+              Ps[d] = s[d] + c1 * m->periodic_vectors[0 * 3 + d] + c2 * m->periodic_vectors[1 * 3 + d] +
+                      c3 * m->periodic_vectors[2 * 3 + d];
+            totalCharge = total_charge_cc(cfg, m, Ps, Fac[3], totalCharge, r_sf, r2_sf, r2_sf_inv, done);
+          }
+          const double f4 = Fac[3];
+          for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * f4 / totalCharge;
+        } else {
+          for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * w_sf;
+        }
         for (int ic = 0; ic < 27; ++ic) {
           /* PeriodicSFCaseMatrix, pic_depo.f90:869-879: case = 9a + 3b + c -> (1-a, 1-b, 1-c) */
           double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);

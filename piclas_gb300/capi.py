@@ -17,6 +17,7 @@ PIC_TRACK_TRIA = 1
 PIC_TRACK_REFMAPPING = 2
 PIC_DEPO_CVWM = 1
 PIC_DEPO_SHAPE_FUNCTION = 2
+PIC_DEPO_SHAPE_FUNCTION_CC = 3
 PIC_PREC_FP64 = 0
 PIC_PREC_MIXED = 1
 

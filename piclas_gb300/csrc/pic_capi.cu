@@ -91,8 +91,11 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   if (cfg->n_dg < 1 || cfg->n_dg > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg must be 1..4");
   if (cfg->tracking != PIC_TRACK_TRIA && cfg->tracking != PIC_TRACK_REFMAPPING)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown tracking method");
-  if (cfg->deposition != PIC_DEPO_CVWM && cfg->deposition != PIC_DEPO_SHAPE_FUNCTION)
+  if (cfg->deposition != PIC_DEPO_CVWM && cfg->deposition != PIC_DEPO_SHAPE_FUNCTION &&
+      cfg->deposition != PIC_DEPO_SHAPE_FUNCTION_CC)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown deposition method");
+  if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC && m->n_periodic_vectors < 1)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_cc is built for periodic meshes (the 27-image branch)");
   if (cfg->precision != PIC_PREC_FP64 && cfg->precision != PIC_PREC_MIXED)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown precision");
   if (cfg->n_species < 1 || cfg->n_species > PIC_MAX_SPECIES) return fail(PIC_ERR_INVALID_ARGUMENT, "n_species");
@@ -234,6 +237,32 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
   for (int e = 0; e < ne; ++e) order[e] = mort[e].second;
   int* d_off; int* d_src; int8_t* d_sh; double* d_c; float* d_r; int* d_o;
   int rc;
+  if (c->cc) {
+    // the pairs transposed to (source -> target, image), and wGP(k) wGP(l) wGP(m) / sJ per DOF
+    const int n1 = c->N + 1;
+    std::vector<int> toff(ne + 1, 0), ttgt(src.size());
+    std::vector<int8_t> tsh(shift.size());
+    for (size_t q = 0; q < src.size(); ++q) toff[src[q] + 1]++;
+    for (int e = 0; e < ne; ++e) toff[e + 1] += toff[e];
+    std::vector<int> cur(toff.begin(), toff.end() - 1);
+    for (int e = 0; e < ne; ++e)
+      for (int q = off[e]; q < off[e + 1]; ++q) {
+        const int t = cur[src[q]]++;
+        ttgt[t] = e;
+        for (int d = 0; d < 3; ++d) tsh[3 * (size_t)t + d] = shift[3 * (size_t)q + d];
+      }
+    std::vector<double> dw((size_t)ne * nd);
+    for (int e = 0; e < ne; ++e)
+      for (int r = 0; r < nd; ++r) {
+        const int k = r % n1, l = (r / n1) % n1, mm = r / (n1 * n1);
+        dw[(size_t)e * nd + r] = m->wgp[k] * m->wgp[l] * m->wgp[mm] / m->elem_sj[(size_t)e * nd + r];
+      }
+    int* d_toff; int* d_ttgt; int8_t* d_tsh; double* d_dw;
+    if ((rc = upload(c, &d_toff, toff)) || (rc = upload(c, &d_ttgt, ttgt)) || (rc = upload(c, &d_tsh, tsh)) ||
+        (rc = upload(c, &d_dw, dw)))
+      return rc;
+    c->sfl.t_off = d_toff; c->sfl.t_tgt = d_ttgt; c->sfl.t_shift = d_tsh; c->sfl.dof_w = d_dw;
+  }
   if ((rc = upload(c, &d_off, off))) return rc;
   if ((rc = upload(c, &d_src, src))) return rc;
   if ((rc = upload(c, &d_sh, shift))) return rc;
@@ -298,7 +327,8 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   c->ne = m->n_elems;
   c->mixed = cfg->precision == PIC_PREC_MIXED;
   c->refmap = cfg->tracking == PIC_TRACK_REFMAPPING;
-  c->sf = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION;
+  c->sf = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC;
+  c->cc = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC;
   const int ne = c->ne, nd = c->nd;
   auto bail = [&](int code) { pic_destroy(c); return code; };
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -438,7 +468,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   }
   if (c->sf) {
     k.sf_r = cfg->sf_radius; k.sf_r2 = cfg->sf_radius * cfg->sf_radius; k.sf_r2_inv = 1.0 / k.sf_r2;
-    k.sf_alpha = cfg->sf_alpha; k.sf_w = sf_weight(cfg->sf_radius, cfg->sf_alpha);
+    k.sf_alpha = cfg->sf_alpha; k.sf_w = c->cc ? 1.0 : sf_weight(cfg->sf_radius, cfg->sf_alpha);   // cc: Fac = q MPF (v,1), normalised later
   }
   if (upload_consts(k) != cudaSuccess) return bail(fail(PIC_ERR_CUDA, "constant upload"));
   c->k = k;
@@ -658,6 +688,7 @@ static int deposit_device(pic_ctx* c) {
   const LaunchArgs A = c->args();
   if (c->sf) {
     c->phase(PH_PACK, [&] { return launch_sf_pack(A, c->P, c->sortb, c->sfl, c->sfk); });
+    if (c->cc) c->phase(PH_MAIN, [&] { return launch_sf_cc_norm(A, c->sortb, c->sfl, c->sfk); });
     c->phase(PH_MAIN, [&] { return launch_sf_gather(A, c->sortb, c->sfl, c->sfk, c->PS); });
   } else {
     c->phase(PH_OTHER, [&] { return launch_deposit_cvwm(A, c->P, c->PS); });

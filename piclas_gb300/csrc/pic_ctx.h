@@ -16,6 +16,7 @@ struct pic_ctx {
   int N = 0, nd = 0, ne = 0, n_canon = 0;
   bool mixed = false, refmap = false, sf = false;
   bool has_walls = false;       // some side is an open or reflective particle boundary
+  bool cc = false;              // shape_function_cc
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
   // mesh

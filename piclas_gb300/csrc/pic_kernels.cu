@@ -1117,6 +1117,113 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
 }
 
 // =============================================================================================
+// shape_function_cc normalisation (calcSfSource:96-120 with calcTotalChargePeriodic_cc:425-555).
+// One CTA per source element, one thread per packed particle of it.  For every (target, image) pair
+// of the source the CTA stages the target's DOFs shifted back by the image (FP64, with the weight
+// wGP^3/sJ) and their FP32 position relative to the source's DOF centre; each thread tests its particle
+// in FP32 against (1+1e-4) R^2 into a hit list, then evaluates the hits exactly (FP64: r^2 <= R^2 and
+// (1 - r^2/R^2)^alpha wGP^3/sJ; mixed: FP32).  The packed Fac (q MPF (v,1)) is multiplied by
+// 1/sum, i.e. Fac * Fac(4) / totalCharge of the reference up to rounding.
+// =============================================================================================
+constexpr int kCcThreads = 128;
+
+template <int N, bool MIXED>
+__global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L, const int* __restrict__ off, SfPack K,
+                                                           DevStatus* st) {
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  __shared__ double s_g[nd][4];                 // DOF position minus the image shift; wGP^3/sJ
+  __shared__ float4 s_gf[nd];                   // FP32, relative to the source's DOF centre
+  __shared__ uint8_t s_list[nd][kCcThreads];
+  const int s = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
+  const int t = threadIdx.x;
+  const int b0 = __ldg(off + s), cnt = __ldg(off + s + 1) - b0;
+  const double* cs = L.dof_center + (size_t)s * 3;
+  const double csx = __ldg(cs), csy = __ldg(cs + 1), csz = __ldg(cs + 2);
+  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  const float R2f = (float)(R2 * (1.0 + 1.0e-4));
+  const int q0 = __ldg(L.t_off + s), q1 = __ldg(L.t_off + s + 1);
+  for (int base = 0; base < cnt; base += kCcThreads) {
+    const int j = b0 + base + t;
+    const bool act = base + t < cnt;
+    double p[3] = {0.0, 0.0, 0.0};
+    float pf[3] = {0.f, 0.f, 0.f};
+    if (act) {
+      const float4 r = reinterpret_cast<const float4*>(K.posf)[j];     // relative to the source DOF centre
+      pf[0] = r.x; pf[1] = r.y; pf[2] = r.z;
+      if constexpr (!MIXED) { p[0] = K.pos[3 * (size_t)j]; p[1] = K.pos[3 * (size_t)j + 1]; p[2] = K.pos[3 * (size_t)j + 2]; }
+    }
+    double acc = 0.0;
+    float accf = 0.f;
+    for (int q = q0; q < q1; ++q) {
+      const int e = __ldg(L.t_tgt + q);
+      double sh[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int k = c_k.pv_dir[d];
+        sh[d] = k >= 0 ? (double)L.t_shift[3 * q + d] * c_k.pv[3 * k + d] : 0.0;
+      }
+      __syncthreads();                          // the previous pair's DOFs are no longer read
+      for (int d = t; d < nd; d += kCcThreads) {
+        const double* g = M.elem_xgp + ((size_t)e * nd + d) * 3;
+        const double gx = __ldg(g) - sh[0], gy = __ldg(g + 1) - sh[1], gz = __ldg(g + 2) - sh[2];
+        s_g[d][0] = gx; s_g[d][1] = gy; s_g[d][2] = gz;
+        s_g[d][3] = __ldg(L.dof_w + (size_t)e * nd + d);
+        s_gf[d] = make_float4((float)(gx - csx), (float)(gy - csy), (float)(gz - csz), 0.0f);
+      }
+      __syncthreads();
+      if (!act) continue;
+      int nh = 0;
+      for (int d = 0; d < nd; ++d) {
+        const float4 g = s_gf[d];
+        const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[nh++][t] = (uint8_t)d;
+      }
+      for (int k = 0; k < nh; ++k) {
+        const int d = s_list[k][t];
+        if constexpr (MIXED) {
+          const float4 g = s_gf[d];
+          const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (r2 <= (float)R2) {
+            const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
+            float S1 = Sv * Sv;
+            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            accf = fmaf((float)s_g[d][3], S1, accf);
+          }
+        } else {
+          const double d0 = p[0] - s_g[d][0], d1 = p[1] - s_g[d][1], d2 = p[2] - s_g[d][2];
+          const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
+          if (r2 <= R2) {
+            const double Sv = fma(-R2inv, r2, 1.0);
+            double S1 = Sv * Sv;
+            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            acc = fma(s_g[d][3], S1, acc);
+          }
+        }
+      }
+    }
+    if (act) {
+      const double tot = MIXED ? (double)accf : acc;
+      const bool ok = tot > 0.0;
+      if (!ok) flag_status(st, 0x20u);          // no DOF within R: the reference would divide by zero
+      const double sc = ok ? 1.0 / tot : 0.0;
+      if constexpr (MIXED) {
+        float4* f = reinterpret_cast<float4*>(K.facf) + j;
+        const float4 v = *f;
+        const float scf = (float)sc;
+        *f = make_float4(v.x * scf, v.y * scf, v.z * scf, v.w * scf);
+      } else {
+        double2* f = reinterpret_cast<double2*>(K.fac + 4 * (size_t)j);
+        const double2 a = f[0], b = f[1];
+        f[0] = make_double2(a.x * sc, a.y * sc);
+        f[1] = make_double2(b.x * sc, b.y * sc);
+      }
+    }
+  }
+}
+
+
+// =============================================================================================
 // Fused remainder for RefTracking: interpolation at PartPosRef + push + RefTracking
 // =============================================================================================
 template <int N, bool MIXED>
@@ -1349,6 +1456,14 @@ static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfL
 #else
   k_sf_gather2<N, MIXED><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #endif
+}
+
+int launch_sf_cc_norm(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K) {
+  PIC_DISPATCH_N(A.N, {
+    if (A.mixed) k_sf_cc_norm<NN, true><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+    else k_sf_cc_norm<NN, false><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+  });
+  return 1;
 }
 
 int sf_gather_variant() { return PIC_SF_GATHER; }

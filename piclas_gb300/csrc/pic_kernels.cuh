@@ -42,6 +42,11 @@ struct SfLists {
   const double* dof_center;   // [ne][3] centre of the element's DOF bounding box
   const float* dof_radius;    // [ne] largest distance of a DOF from dof_center
   const int* order;           // [ne] target elements in Morton order of their DOF centres (L2 reuse)
+  // shape_function_cc: the same pairs seen from the source element, and the quadrature weight per DOF
+  const int* t_off;           // [ne+1] per source element
+  const int* t_tgt;           // [n_pairs] target element (0-based)
+  const int8_t* t_shift;      // [n_pairs][3] periodic image of the source particles
+  const double* dof_w;        // [ne][nd] wGP(k) wGP(l) wGP(m) / sJ
 };
 struct SfPack {
   double* pos;     // [cap][3] FP64 position (FP64 variant)
@@ -62,6 +67,9 @@ int launch_node_to_dof(const LaunchArgs& A, double* part_source);
 int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B);
 int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K);
 int sf_gather_variant();   // compile-time shape-function gather variant (PIC_SF_GATHER)
+// shape_function_cc: scales each packed particle's Fac by q*MPF / (its quadrature charge over all DOFs
+// within R), so that every particle deposits exactly its charge
+int launch_sf_cc_norm(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K);
 int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* part_source);
 int launch_deposit_sf(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L,
                       const SfPack& K, double* part_source);

@@ -350,3 +350,50 @@ def test_walls_rejected_where_unsupported(gpu_lib):
     with pytest.raises(PicError) as e:
         ParticleLoop(cfg, w.mesh)
     assert e.value.code == 1
+
+
+# ---- shape_function_cc -----------------------------------------------------------------------------
+def _cc_workload(n_cells=6, n_per_species=2000, seed=13):
+    w = workloads.curved_two_species(n_cells=n_cells, n_per_species=n_per_species, seed=seed, nsteps=2)
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION_CC
+    return w
+
+
+def test_shape_function_cc_against_oracle(gpu_lib, oracle_lib):
+    w = _cc_workload()
+    g = _run_gpu(w, 2)
+    st, PS = _run_oracle(oracle_lib, w, 2)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["PS"], PS) <= 1e-12
+    gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert g["status"]["error_word"] == 0
+
+
+@pytest.mark.parametrize("prec,tol", [(capi.PIC_PREC_FP64, 1e-12), (capi.PIC_PREC_MIXED, 1e-5)])
+def test_shape_function_cc_conserves_charge(gpu_lib, oracle_lib, prec, tol):
+    """Charge-corrected deposition: the quadrature integral of each species' deposit equals its total
+    charge (the defining property; plain shape_function misses it by the quadrature error)."""
+    w = _cc_workload(n_cells=12, n_per_species=100_000, seed=5)
+    ms = capi.MeshStruct(w.mesh)
+    for sp in (1, 2):
+        sel = w.part_species == sp
+        loop = ParticleLoop(w.config(precision=prec), w.mesh)
+        loop.set_field(w.e_dof)
+        loop.upload_particles(w.part_state[sel], w.elem[sel], w.part_species[sel])
+        PS = loop.deposition()
+        loop.close()
+        q = w.species[sp - 1][0] * w.species[sp - 1][2] * int(sel.sum())
+        Q = oracle_lib.integrate_charge(ms, w.mesh.N, PS)
+        assert abs(Q - q) <= tol * abs(q), (sp, Q, q)
+
+
+def test_walls_with_resort(gpu_lib, oracle_lib):
+    """Removed particles sort behind all elements at every re-sort; results stay bit-exact."""
+    w = _wall_workload(seed=23, n=4000)
+    g = _run_gpu(w, 12, sort_interval=3)
+    st, PS = _run_oracle(oracle_lib, w, 12)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
