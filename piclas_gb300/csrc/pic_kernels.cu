@@ -1118,30 +1118,66 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
 
 // =============================================================================================
 // shape_function_cc normalisation (calcSfSource:96-120 with calcTotalChargePeriodic_cc:425-555).
-// One CTA per source element, one thread per packed particle of it.  For every (target, image) pair
-// of the source the CTA stages the target's DOFs shifted back by the image (FP64, with the weight
-// wGP^3/sJ) and their FP32 position relative to the source's DOF centre; each thread tests its particle
-// in FP32 against (1+1e-4) R^2 into a hit list, then evaluates the hits exactly (FP64: r^2 <= R^2 and
-// (1 - r^2/R^2)^alpha wGP^3/sJ; mixed: FP32).  The packed Fac (q MPF (v,1)) is multiplied by
+// One CTA per source element, one thread per packed particle of it.  Per round the CTA stages the DOFs
+// of four (target, image) pairs of the source, taken at stride npairs/4 so that they lie on different
+// sides (a single target leaves the particles on the far side of the source idle): each DOF shifted back
+// by the image (FP64, with the weight wGP^3/sJ) and its FP32 position relative to the source's DOF
+// centre.  Each thread tests its particle in FP32 against (1+1e-4) R^2 into a hit list, then evaluates
+// the hits exactly (FP64: r^2 <= R^2 and (1 - r^2/R^2)^alpha wGP^3/sJ; mixed: FP32).  The packed Fac (q MPF (v,1)) is multiplied by
 // 1/sum, i.e. Fac * Fac(4) / totalCharge of the reference up to rounding.
 // =============================================================================================
 constexpr int kCcThreads = 128;
+// pairs staged per round (taken at stride npairs/round: targets on all sides); 2 for N = 4 (48 KB smem)
+template <int N>
+__host__ __device__ constexpr int cc_round() { return (N + 1) * (N + 1) * (N + 1) > 64 ? 2 : 4; }
+constexpr int kCcCap = 256;       // hit-list entries per thread: a whole round (ns <= 256), so no lane flushes alone
+
+template <int N, bool MIXED>
+__device__ __forceinline__ void cc_eval(const double (*s_g)[4], const float4* s_gf, const uint8_t (*s_list)[kCcThreads],
+                                        int nh, const double p[3], const float pf[3], double& acc, float& accf) {
+  const int t = threadIdx.x;
+  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  for (int k = 0; k < nh; ++k) {
+    const int d = s_list[k][t];
+    if constexpr (MIXED) {
+      const float4 g = s_gf[d];
+      const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      if (r2 <= (float)R2) {
+        const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
+        float S1 = Sv * Sv;
+        for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+        accf = fmaf(g.w, S1, accf);
+      }
+    } else {
+      const double d0 = p[0] - s_g[d][0], d1 = p[1] - s_g[d][1], d2 = p[2] - s_g[d][2];
+      const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
+      if (r2 <= R2) {
+        const double Sv = fma(-R2inv, r2, 1.0);
+        double S1 = Sv * Sv;
+        for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+        acc = fma(s_g[d][3], S1, acc);
+      }
+    }
+  }
+}
 
 template <int N, bool MIXED>
 __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L, const int* __restrict__ off, SfPack K,
                                                            DevStatus* st) {
-  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
-  __shared__ double s_g[nd][4];                 // DOF position minus the image shift; wGP^3/sJ
-  __shared__ float4 s_gf[nd];                   // FP32, relative to the source's DOF centre
-  __shared__ uint8_t s_list[nd][kCcThreads];
+  constexpr int n1 = N + 1, nd = n1 * n1 * n1, ns = cc_round<N>() * nd;
+  __shared__ double s_g[MIXED ? 1 : ns][4];     // DOF position minus the image shift; wGP^3/sJ
+  __shared__ float4 s_gf[ns];                   // FP32 position relative to the source's DOF centre; w = weight
+  __shared__ uint8_t s_list[kCcCap][kCcThreads];
+  static_assert(ns <= kCcCap, "a round's DOFs must fit one hit list");
   const int s = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
   const int t = threadIdx.x;
   const int b0 = __ldg(off + s), cnt = __ldg(off + s + 1) - b0;
   const double* cs = L.dof_center + (size_t)s * 3;
   const double csx = __ldg(cs), csy = __ldg(cs + 1), csz = __ldg(cs + 2);
-  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
-  const float R2f = (float)(R2 * (1.0 + 1.0e-4));
-  const int q0 = __ldg(L.t_off + s), q1 = __ldg(L.t_off + s + 1);
+  const float R2f = (float)(c_k.sf_r2 * (1.0 + 1.0e-4));
+  const int q0 = __ldg(L.t_off + s), npair = __ldg(L.t_off + s + 1) - q0;
+  const int stride = (npair + cc_round<N>() - 1) / cc_round<N>();
   for (int base = 0; base < cnt; base += kCcThreads) {
     const int j = b0 + base + t;
     const bool act = base + t < cnt;
@@ -1154,53 +1190,34 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
     }
     double acc = 0.0;
     float accf = 0.f;
-    for (int q = q0; q < q1; ++q) {
-      const int e = __ldg(L.t_tgt + q);
-      double sh[3];
+    for (int r = 0; r < stride; ++r) {
+      __syncthreads();                          // the previous round's DOFs are no longer read
+      for (int i = t; i < ns; i += kCcThreads) {
+        const int kq = i / nd, d = i - kq * nd, pi = r + kq * stride;
+        if (pi >= npair) { s_gf[i] = make_float4(1e30f, 1e30f, 1e30f, 0.0f); continue; }   // never a hit
+        const int q = q0 + pi;
+        const int e = __ldg(L.t_tgt + q);
+        double sh[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const int k = c_k.pv_dir[d];
-        sh[d] = k >= 0 ? (double)L.t_shift[3 * q + d] * c_k.pv[3 * k + d] : 0.0;
-      }
-      __syncthreads();                          // the previous pair's DOFs are no longer read
-      for (int d = t; d < nd; d += kCcThreads) {
+        for (int dd = 0; dd < 3; ++dd) {
+          const int k = c_k.pv_dir[dd];
+          sh[dd] = k >= 0 ? (double)L.t_shift[3 * q + dd] * c_k.pv[3 * k + dd] : 0.0;
+        }
         const double* g = M.elem_xgp + ((size_t)e * nd + d) * 3;
         const double gx = __ldg(g) - sh[0], gy = __ldg(g + 1) - sh[1], gz = __ldg(g + 2) - sh[2];
-        s_g[d][0] = gx; s_g[d][1] = gy; s_g[d][2] = gz;
-        s_g[d][3] = __ldg(L.dof_w + (size_t)e * nd + d);
-        s_gf[d] = make_float4((float)(gx - csx), (float)(gy - csy), (float)(gz - csz), 0.0f);
+        const double wgt = __ldg(L.dof_w + (size_t)e * nd + d);
+        if constexpr (!MIXED) { s_g[i][0] = gx; s_g[i][1] = gy; s_g[i][2] = gz; s_g[i][3] = wgt; }
+        s_gf[i] = make_float4((float)(gx - csx), (float)(gy - csy), (float)(gz - csz), (float)wgt);
       }
       __syncthreads();
       if (!act) continue;
       int nh = 0;
-      for (int d = 0; d < nd; ++d) {
-        const float4 g = s_gf[d];
+      for (int i = 0; i < ns; ++i) {
+        const float4 g = s_gf[i];
         const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[nh++][t] = (uint8_t)d;
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[nh++][t] = (uint8_t)i;
       }
-      for (int k = 0; k < nh; ++k) {
-        const int d = s_list[k][t];
-        if constexpr (MIXED) {
-          const float4 g = s_gf[d];
-          const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (r2 <= (float)R2) {
-            const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
-            float S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
-            accf = fmaf((float)s_g[d][3], S1, accf);
-          }
-        } else {
-          const double d0 = p[0] - s_g[d][0], d1 = p[1] - s_g[d][1], d2 = p[2] - s_g[d][2];
-          const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
-          if (r2 <= R2) {
-            const double Sv = fma(-R2inv, r2, 1.0);
-            double S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
-            acc = fma(s_g[d][3], S1, acc);
-          }
-        }
-      }
+      cc_eval<N, MIXED>(s_g, s_gf, s_list, nh, p, pf, acc, accf);
     }
     if (act) {
       const double tot = MIXED ? (double)accf : acc;
@@ -1222,12 +1239,20 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
   }
 }
 
-
 // =============================================================================================
 // Fused remainder for RefTracking: interpolation at PartPosRef + push + RefTracking
 // =============================================================================================
+// resident CTAs per SM the RefTracking step is compiled for (FP64 / mixed): 2 x 256 threads caps it at 128
+// registers (no spills); against 1 CTA/SM (170 registers) 62.4 vs 64.1 ms (FP64) and 14.0 vs 16.0 ms (mixed)
+// per step at 32^3 / 16M particles
+#ifndef PIC_REF_MINB
+#define PIC_REF_MINB 2
+#endif
+#ifndef PIC_REF_MIXED_MINB
+#define PIC_REF_MIXED_MINB 2
+#endif
 template <int N, bool MIXED>
-__global__ void __launch_bounds__(256) k_step_ref(DevMesh M, DevParticles P, const double* __restrict__ E,
+__global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB) k_step_ref(DevMesh M, DevParticles P, const double* __restrict__ E,
                                                   const float* __restrict__ E32, double dt, DevStatus* st) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
