@@ -186,6 +186,18 @@ int pic_step(pic_ctx_t* ctx, double dt, int32_t nsteps, double* part_source);
 
 int pic_get_status(pic_ctx_t* ctx, pic_status_t* status);
 
+/* Particle state in the reference's checkpoint layout (FillParticleData, src/io_hdf5/hdf5_output_particle.f90:1531):
+ * the particles inside the domain grouped by element, in ascending caller index within an element
+ * (UpdateNextFreePosition order); part_data(1:7, n_out) = PartState(1:6), Species; part_int(1:2, nElems) =
+ * (FirstPartID, LastPartID) = offset_npart + the element's range, LastPartID - FirstPartID particles.
+ * part_data may be NULL to query n_out first; capacity is the number of particles part_data holds. */
+int pic_get_part_data(pic_ctx_t* ctx, double* part_data, int64_t* part_int, int64_t offset_npart, int32_t capacity,
+                      int32_t* n_out);
+/* Restart from that layout (particle_readin.f90): particle k of part_data lies in the element whose
+ * part_int range holds offset_npart + k; uploaded with ParticleInside = T, IsNewPart = F. */
+int pic_set_part_data(pic_ctx_t* ctx, const double* part_data, const int64_t* part_int, int64_t offset_npart,
+                      int32_t n_part);
+
 /* Differentiable loop (no reference counterpart; the reference has no adjoint).  Starting from the
  * uploaded particles (taken as x_0 and v_{-1/2}; IsNewPart is not applied), runs nsteps of
  * {interpolation, Boris push, TriaTracking} with the field frozen and B = b_scale * B_ext, deposits

@@ -36,7 +36,7 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_upload_particles", "pic_download_particles", "pic_interpolate", "pic_push", "pic_track",
                     "pic_deposit", "pic_get_field_at_particles", "pic_step", "pic_get_status", "pic_reset_status",
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
-                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run"]
+                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data"]
 
 
 class PicError(RuntimeError):
@@ -77,6 +77,9 @@ def load_library(build_if_missing: bool = False):
     L.pic_track.argtypes = [C.c_void_p]
     L.pic_deposit.argtypes = [C.c_void_p, dp]
     L.pic_get_field_at_particles.argtypes = [C.c_void_p, dp, C.c_int32]
+    i64p = P(C.c_int64)
+    L.pic_get_part_data.argtypes = [C.c_void_p, dp, i64p, C.c_int64, C.c_int32, P(C.c_int32)]
+    L.pic_set_part_data.argtypes = [C.c_void_p, dp, i64p, C.c_int64, C.c_int32]
     L.pic_step.argtypes = [C.c_void_p, C.c_double, C.c_int32, dp]
     L.pic_get_status.argtypes = [C.c_void_p, P(PicStatus)]
     L.pic_reset_status.argtypes = [C.c_void_p]
@@ -187,6 +190,28 @@ class ParticleLoop:
         ps = out if out is not None else np.zeros((self.mesh.n_elems, self.nd, 4))
         self._check(self.lib.pic_deposit(self.handle, capi.dptr(ps)), "pic_deposit")
         return ps
+
+    def get_part_data(self, offset_npart: int = 0):
+        """Checkpoint layout of the reference (FillParticleData): PartData (n, 7) = x, y, z, vx, vy, vz, species
+        of the particles inside, grouped by element; PartInt (nElems, 2) = (FirstPartID, LastPartID)."""
+        ne = self.mesh.n_elems
+        part_int = np.zeros((ne, 2), np.int64)
+        n = C.c_int32(0)
+        i64 = part_int.ctypes.data_as(C.POINTER(C.c_int64))
+        self._check(self.lib.pic_get_part_data(self.handle, _null(C.c_double), i64, offset_npart, 0, C.byref(n)),
+                    "pic_get_part_data")
+        part_data = np.zeros((n.value, 7))
+        self._check(self.lib.pic_get_part_data(self.handle, capi.dptr(part_data), i64, offset_npart, n.value,
+                                               C.byref(n)), "pic_get_part_data")
+        return part_data, part_int
+
+    def set_part_data(self, part_data: np.ndarray, part_int: np.ndarray, offset_npart: int = 0):
+        """Restart from the checkpoint layout: IsNewPart = F; the caller order becomes the PartData order."""
+        pd = np.ascontiguousarray(part_data, dtype=np.float64)
+        pi = np.ascontiguousarray(part_int, dtype=np.int64)
+        self._check(self.lib.pic_set_part_data(self.handle, capi.dptr(pd), pi.ctypes.data_as(C.POINTER(C.c_int64)),
+                                               offset_npart, pd.shape[0]), "pic_set_part_data")
+        self.n = pd.shape[0]
 
     def field_at_particles(self) -> np.ndarray:
         f = np.zeros((self.n, 6))

@@ -709,6 +709,70 @@ int pic_deposit(pic_ctx_t* c, double* part_source) {
   return PIC_OK;
 }
 
+int pic_get_part_data(pic_ctx_t* c, double* part_data, int64_t* part_int, int64_t offset_npart, int32_t capacity,
+                      int32_t* n_out) {
+  if (!c || !part_int || !n_out) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  const int n = c->P.n, ne = c->ne;
+  std::vector<double> ps((size_t)n * 6);
+  std::vector<int32_t> el(n);
+  std::vector<uint8_t> ins(n), sp(n);
+  std::vector<int> pm(n);
+  int rc = pic_download_particles(c, ps.data(), el.data(), ins.data(), nullptr, nullptr, n);
+  if (rc) return rc;
+  if (n > 0) {
+    CUDA_TRY(cudaMemcpy(sp.data(), c->P.species, n, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(pm.data(), c->perm, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  }
+  std::vector<int> spc(n, 0);
+  for (int j = 0; j < n; ++j) spc[pm[j]] = sp[j] + 1;
+  // stable counting sort by element: ascending caller index within an element
+  std::vector<int64_t> first(ne + 1, 0);
+  for (int i = 0; i < n; ++i)
+    if (ins[i]) first[el[i]]++;                       // el is 1-based: counts land in first[1..ne]
+  for (int e = 0; e < ne; ++e) first[e + 1] += first[e];
+  const int64_t total = first[ne];
+  *n_out = (int32_t)total;
+  for (int e = 0; e < ne; ++e) {
+    part_int[2 * (size_t)e] = offset_npart + first[e];
+    part_int[2 * (size_t)e + 1] = offset_npart + first[e + 1];
+  }
+  if (!part_data) return PIC_OK;
+  if (total > capacity) return fail(PIC_ERR_CAPACITY, "part_data holds fewer particles than are inside");
+  std::vector<int64_t> cur(first.begin(), first.end() - 1);
+  for (int i = 0; i < n; ++i) {
+    if (!ins[i]) continue;
+    double* d = part_data + 7 * (size_t)cur[el[i] - 1]++;
+    for (int q = 0; q < 6; ++q) d[q] = ps[(size_t)i * 6 + q];
+    d[6] = (double)spc[i];
+  }
+  return PIC_OK;
+}
+
+int pic_set_part_data(pic_ctx_t* c, const double* part_data, const int64_t* part_int, int64_t offset_npart,
+                      int32_t n_part) {
+  if (!c || !part_int || (n_part > 0 && !part_data)) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  if (n_part < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "negative particle count");
+  std::vector<double> ps((size_t)n_part * 6);
+  std::vector<int32_t> el(n_part, 0), spc(n_part, 0);
+  for (int e = 0; e < c->ne; ++e) {
+    const int64_t a = part_int[2 * (size_t)e] - offset_npart, b = part_int[2 * (size_t)e + 1] - offset_npart;
+    if (a < 0 || b < a || b > n_part) return fail(PIC_ERR_INVALID_ARGUMENT, "part_int range outside part_data");
+    for (int64_t k = a; k < b; ++k) {
+      if (el[k] != 0) return fail(PIC_ERR_INVALID_ARGUMENT, "part_int ranges overlap");
+      el[k] = e + 1;
+    }
+  }
+  for (int k = 0; k < n_part; ++k) {
+    if (el[k] == 0) return fail(PIC_ERR_INVALID_ARGUMENT, "particle outside every part_int range");
+    const double* d = part_data + 7 * (size_t)k;
+    for (int q = 0; q < 6; ++q) ps[(size_t)k * 6 + q] = d[q];
+    spc[k] = (int32_t)d[6];
+    if ((double)spc[k] != d[6]) return fail(PIC_ERR_INVALID_ARGUMENT, "species column is not an integer");
+  }
+  std::vector<uint8_t> inside(n_part, 1), is_new(n_part, 0);
+  return pic_upload_particles(c, ps.data(), el.data(), spc.data(), inside.data(), is_new.data(), n_part);
+}
+
 int pic_get_field_at_particles(pic_ctx_t* c, double* field, int32_t n) {
   if (!c || !field) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
   if (n != c->P.n) return fail(PIC_ERR_INVALID_ARGUMENT, "n does not match the particle count");

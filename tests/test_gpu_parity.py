@@ -397,3 +397,40 @@ def test_walls_with_resort(gpu_lib, oracle_lib):
     assert np.array_equal(g["elem"], st.elem)
     assert np.array_equal(g["part_state"], st.part_state)
     assert _rel(g["PS"], PS) <= 1e-12
+
+
+# ---- checkpoint layout and restart (FillParticleData / particle read-in) -------------------------
+def _fill_particle_data(state, elem, inside, species, ne, offset=0):
+    """FillParticleData restated in numpy: inside particles grouped by element, ascending index within."""
+    idx = np.flatnonzero(inside)
+    idx = idx[np.argsort(elem[idx], kind="stable")]
+    pd = np.concatenate([state[idx], species[idx, None].astype(np.float64)], axis=1)
+    counts = np.bincount(elem[idx] - 1, minlength=ne)
+    first = offset + np.concatenate([[0], np.cumsum(counts)[:-1]])
+    return pd, np.stack([first, first + counts], axis=1), idx
+
+
+def test_part_data_layout_and_restart(gpu_lib):
+    w = _wall_workload(seed=31, n=5000)            # open walls remove particles: holes in the caller order
+    loop = ParticleLoop(w.config(), w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    loop.time_step(w.dt, 6)
+    g = loop.download_particles()
+    pd, pi = loop.get_part_data(offset_npart=1000)
+    ref_pd, ref_pi, order = _fill_particle_data(g["part_state"], g["elem"], g["inside"], w.part_species,
+                                                w.mesh.n_elems, offset=1000)
+    assert np.array_equal(pi, ref_pi) and np.array_equal(pd, ref_pd)
+    assert pd.shape[0] == int(g["inside"].sum()) < w.n
+    # restart a second context from the checkpoint; both continue identically
+    loop2 = ParticleLoop(w.config(), w.mesh)
+    loop2.set_field(w.e_dof)
+    loop2.set_part_data(pd, pi, offset_npart=1000)
+    loop.time_step(w.dt, 5)
+    loop2.time_step(w.dt, 5)
+    a, b = loop.download_particles(), loop2.download_particles()
+    assert np.array_equal(a["part_state"][order], b["part_state"])
+    assert np.array_equal(a["elem"][order], b["elem"])
+    assert np.array_equal(a["inside"][order], b["inside"])
+    loop.close()
+    loop2.close()
