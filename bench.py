@@ -456,7 +456,29 @@ def extras(args, w_main):
     from piclas_gb300 import precision_report
     res["plasma_wave_mixed_per_step"] = precision_report.summarize(
         precision_report.mixed_vs_fp64_per_step(pw, pw.nsteps))
+    res["adjoint"] = adjoint_timing()
     return res
+
+
+def adjoint_timing():
+    """The differentiable loop (16^3, N=2, 1M electrons, B_z = 0.05 T, 50 steps, checkpoint every 10): wall
+    time of one pic_adjoint_run (forward, recomputed segments and reverse pass) in FP64 and FP32."""
+    import torch
+    from piclas_gb300 import ParticleLoop, capi, workloads
+    w = workloads.differentiable_loop()
+    loop = ParticleLoop(w.config(), w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species, is_new=np.zeros(w.n, np.uint8))
+    out = {"workload": "16^3 linear hex, N=2, 1M e-, 50 push+deposit steps, checkpoint 10", "particles": w.n}
+    for name, prec in (("fp64", capi.PIC_PREC_FP64), ("fp32", capi.PIC_PREC_MIXED)):
+        loop.adjoint(w.nsteps, w.dt, w.info["rho_target"], w.info["rho_scale"], precision=prec)   # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L, gv, gb = loop.adjoint(w.nsteps, w.dt, w.info["rho_target"], w.info["rho_scale"], precision=prec)
+        t = time.perf_counter() - t0
+        out[name] = {"seconds": t, "particle_steps_per_s": w.n * w.nsteps / t, "loss": L, "dL_dB": gb}
+    loop.close()
+    return out
 
 
 def run_batch(args):

@@ -63,8 +63,10 @@ typedef enum pic_error_t {
 /* ---- option enums ------------------------------------------------------- */
 enum { PIC_TRACK_TRIA = 1, PIC_TRACK_REFMAPPING = 2 };     /* TrackingMethod           */
 /* PIC-Deposition-Type: cell_volweight_mean, shape_function, shape_function_cc (charge-corrected: each
- * particle's deposit scaled so that its quadrature integral is exactly q*MPF; periodic meshes) */
-enum { PIC_DEPO_CVWM = 1, PIC_DEPO_SHAPE_FUNCTION = 2, PIC_DEPO_SHAPE_FUNCTION_CC = 3 };
+ * particle's deposit scaled so that its quadrature integral is exactly q*MPF; periodic meshes),
+ * shape_function_adaptive (as _cc with the radius of the particle's element, pic_mesh_t.sf_elem_radius) */
+enum { PIC_DEPO_CVWM = 1, PIC_DEPO_SHAPE_FUNCTION = 2, PIC_DEPO_SHAPE_FUNCTION_CC = 3,
+       PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE = 4 };
 enum { PIC_PREC_FP64 = 0, PIC_PREC_MIXED = 1 };            /* arithmetic variant       */
 
 #define PIC_MAX_SPECIES 8
@@ -138,6 +140,9 @@ typedef struct pic_mesh_t {
    * 2 reflective (PerfectReflection: MomentumACC = 0, no wall velocity), 0 for inner and periodic
    * sides; a side with side_nb_elem = 0 must be 1 or 2.  NULL: every side is inner or periodic. */
   const int32_t* side_bc;
+  /* shape_function_adaptive: SFElemr2_Shared(1,nElems), the shape-function radius of each element
+   * (InitShapeFunctionAdaptive, pic_depo.f90:727-815); NULL otherwise */
+  const double* sf_elem_radius;
 } pic_mesh_t;
 
 typedef struct pic_status_t {

@@ -921,6 +921,7 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
 #endif
     double* my = (nt > 1) ? acc + nps * (size_t)tid : PS;
     uint8_t* done = doneAll + (size_t)m->n_elems * tid;
+    const int adaptive = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE;
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
@@ -931,8 +932,15 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
       const double* s = &p->part_state[(size_t)ip * 6];
       double cm = cfg->charge[sp] * cfg->mpf[sp];
       double Fac[4] = {s[3] * cm, s[4] * cm, s[5] * cm, cm};
+      /* shape_function_adaptive: the radius of the particle's element (calcSfSource:83-92) */
+      double r_sf_p = r_sf, r2_sf_p = r2_sf, r2_sf_inv_p = r2_sf_inv;
+      if (adaptive) {
+        r_sf_p = m->sf_elem_radius[p->elem[ip] - 1];
+        r2_sf_p = r_sf_p * r_sf_p;
+        r2_sf_inv_p = 1.0 / r2_sf_p;
+      }
       if (nCases > 1) {
-        if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC) {
+        if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC || adaptive) {
           double totalCharge = 0.0;
           for (int ic = 0; ic < 27; ++ic) {
             double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);
@@ -940,7 +948,7 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
             for (int d = 0; d < 3; ++d)
               Ps[d] = s[d] + c1 * m->periodic_vectors[0 * 3 + d] + c2 * m->periodic_vectors[1 * 3 + d] +
                       c3 * m->periodic_vectors[2 * 3 + d];
-            totalCharge = total_charge_cc(cfg, m, Ps, Fac[3], totalCharge, r_sf, r2_sf, r2_sf_inv, done);
+            totalCharge = total_charge_cc(cfg, m, Ps, Fac[3], totalCharge, r_sf_p, r2_sf_p, r2_sf_inv_p, done);
           }
           const double f4 = Fac[3];
           for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * f4 / totalCharge;
@@ -954,7 +962,7 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
           for (int d = 0; d < 3; ++d)
             Ps[d] = s[d] + c1 * m->periodic_vectors[0 * 3 + d] + c2 * m->periodic_vectors[1 * 3 + d] +
                     c3 * m->periodic_vectors[2 * 3 + d];
-          depo_charge_on_dofs_sf(cfg, m, Ps, Fac, r_sf, r2_sf, r2_sf_inv, my, done);
+          depo_charge_on_dofs_sf(cfg, m, Ps, Fac, r_sf_p, r2_sf_p, r2_sf_inv_p, my, done);
         }
       } else {
         double Fw[4];

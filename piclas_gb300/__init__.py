@@ -22,11 +22,11 @@ import os
 import numpy as np
 
 from . import capi
-from .capi import (PIC_DEPO_CVWM, PIC_DEPO_SHAPE_FUNCTION, PIC_DEPO_SHAPE_FUNCTION_CC, PIC_PREC_FP64, PIC_PREC_MIXED, PIC_TRACK_REFMAPPING,
+from .capi import (PIC_DEPO_CVWM, PIC_DEPO_SHAPE_FUNCTION, PIC_DEPO_SHAPE_FUNCTION_CC, PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE, PIC_PREC_FP64, PIC_PREC_MIXED, PIC_TRACK_REFMAPPING,
                    PIC_TRACK_TRIA, MeshStruct, PicConfig, PicMesh, PicStatus, make_config)
 
 __all__ = ["ParticleLoop", "PicError", "load_library", "library_path", "MeshStruct", "make_config",
-           "PIC_TRACK_TRIA", "PIC_TRACK_REFMAPPING", "PIC_DEPO_CVWM", "PIC_DEPO_SHAPE_FUNCTION", "PIC_DEPO_SHAPE_FUNCTION_CC",
+           "PIC_TRACK_TRIA", "PIC_TRACK_REFMAPPING", "PIC_DEPO_CVWM", "PIC_DEPO_SHAPE_FUNCTION", "PIC_DEPO_SHAPE_FUNCTION_CC", "PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE",
            "PIC_PREC_FP64", "PIC_PREC_MIXED", "EXPORTED_SYMBOLS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))

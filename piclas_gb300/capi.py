@@ -18,6 +18,7 @@ PIC_TRACK_REFMAPPING = 2
 PIC_DEPO_CVWM = 1
 PIC_DEPO_SHAPE_FUNCTION = 2
 PIC_DEPO_SHAPE_FUNCTION_CC = 3
+PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE = 4
 PIC_PREC_FP64 = 0
 PIC_PREC_MIXED = 1
 
@@ -60,7 +61,7 @@ class PicMesh(C.Structure):
         ("periodic_nodes", _ip), ("n_total_periodic_nodes", C.c_int32),
         ("fibgm_imax", C.c_int32 * 3), ("fibgm_deltas", C.c_double * 3), ("fibgm_n_elems", _ip),
         ("fibgm_offset", _ip), ("fibgm_element", _ip), ("fibgm_n_total", C.c_int32),
-        ("side_bc", _ip),
+        ("side_bc", _ip), ("sf_elem_radius", _dp),
     ]
 
 
@@ -176,6 +177,8 @@ class MeshStruct:
         s.fibgm_element = i("fe", mesh.fibgm_element)
         s.fibgm_n_total = int(len(mesh.fibgm_element))
         s.side_bc = i("sbc", mesh.side_bc) if mesh.side_bc is not None else C.POINTER(C.c_int32)()
+        sfr = getattr(mesh, "sf_elem_radius", None)
+        s.sf_elem_radius = d("sfr", sfr) if sfr is not None else C.POINTER(C.c_double)()
         self.struct = s
         self._keep = keep
 

@@ -91,11 +91,11 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   if (cfg->n_dg < 1 || cfg->n_dg > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg must be 1..4");
   if (cfg->tracking != PIC_TRACK_TRIA && cfg->tracking != PIC_TRACK_REFMAPPING)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown tracking method");
-  if (cfg->deposition != PIC_DEPO_CVWM && cfg->deposition != PIC_DEPO_SHAPE_FUNCTION &&
-      cfg->deposition != PIC_DEPO_SHAPE_FUNCTION_CC)
+  if (cfg->deposition < PIC_DEPO_CVWM || cfg->deposition > PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown deposition method");
-  if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC && m->n_periodic_vectors < 1)
-    return fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_cc is built for periodic meshes (the 27-image branch)");
+  if ((cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE) &&
+      m->n_periodic_vectors < 1)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_cc/_adaptive are built for periodic meshes (the 27-image branch)");
   if (cfg->precision != PIC_PREC_FP64 && cfg->precision != PIC_PREC_MIXED)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown precision");
   if (cfg->n_species < 1 || cfg->n_species > PIC_MAX_SPECIES) return fail(PIC_ERR_INVALID_ARGUMENT, "n_species");
@@ -110,11 +110,20 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   for (const void* p : req)
     if (!p) return fail(PIC_ERR_INVALID_ARGUMENT, "missing mesh array");
   if (cfg->deposition == PIC_DEPO_CVWM && !m->node_volume) return fail(PIC_ERR_INVALID_ARGUMENT, "node_volume");
-  if ((cfg->tracking == PIC_TRACK_REFMAPPING || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION) &&
+  const bool sf = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC ||
+                  cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE;
+  if ((cfg->tracking == PIC_TRACK_REFMAPPING || sf) &&
       (!m->fibgm_n_elems || !m->fibgm_offset || !m->fibgm_element || !m->eps_one_cell))
     return fail(PIC_ERR_INVALID_ARGUMENT, "FIBGM arrays required for RefTracking / shape function");
-  if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION && !(cfg->sf_radius > 0.0 && cfg->sf_alpha >= 2))
-    return fail(PIC_ERR_INVALID_ARGUMENT, "shape function radius/alpha");
+  if (sf && cfg->sf_alpha < 2) return fail(PIC_ERR_INVALID_ARGUMENT, "shape function alpha must be >= 2");
+  if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE) {
+    if (!m->sf_elem_radius) return fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_adaptive needs sf_elem_radius");
+    for (int e = 0; e < m->n_elems; ++e)
+      if (!(m->sf_elem_radius[e] > 0.0) || !std::isfinite(m->sf_elem_radius[e]))
+        return fail(PIC_ERR_INVALID_ARGUMENT, "sf_elem_radius must be positive and finite");
+  } else if (sf && !(cfg->sf_radius > 0.0)) {
+    return fail(PIC_ERR_INVALID_ARGUMENT, "shape function radius");
+  }
   return PIC_OK;
 }
 
@@ -124,7 +133,8 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
 // wrapped onto their periodic image.
 int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& dofc) {
   const int ne = m->n_elems, nd = c->nd;
-  const double R = c->cfg.sf_radius, R2 = R * R;
+  const double R = c->sf_rmax;
+  auto R2src = [&](int s) { const double r = c->adaptive ? m->sf_elem_radius[s] : c->cfg.sf_radius; return r * r; };
   std::vector<double> bmin((size_t)ne * 3), bmax((size_t)ne * 3), dmin((size_t)ne * 3), dmax((size_t)ne * 3);
   for (int e = 0; e < ne; ++e)
     for (int d = 0; d < 3; ++d) {
@@ -202,7 +212,7 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
           const double q = p < lo ? lo - p : (p > hi ? p - hi : 0.0);
           d2 += q * q;
         }
-        if (d2 <= R2 * (1.0 + 1e-6)) keep = true;
+        if (d2 <= R2src(s) * (1.0 + 1e-6)) keep = true;
       }
       if (!keep) continue;
       src.push_back(s);
@@ -262,6 +272,12 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
         (rc = upload(c, &d_dw, dw)))
       return rc;
     c->sfl.t_off = d_toff; c->sfl.t_tgt = d_ttgt; c->sfl.t_shift = d_tsh; c->sfl.dof_w = d_dw;
+  }
+  if (c->adaptive) {
+    std::vector<double> er(m->sf_elem_radius, m->sf_elem_radius + ne);
+    double* d_er;
+    if ((rc = upload(c, &d_er, er))) return rc;
+    c->sfl.elem_r = d_er;
   }
   if ((rc = upload(c, &d_off, off))) return rc;
   if ((rc = upload(c, &d_src, src))) return rc;
@@ -327,10 +343,18 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   c->ne = m->n_elems;
   c->mixed = cfg->precision == PIC_PREC_MIXED;
   c->refmap = cfg->tracking == PIC_TRACK_REFMAPPING;
-  c->sf = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC;
-  c->cc = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC;
+  c->sf = cfg->deposition != PIC_DEPO_CVWM;
+  c->adaptive = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE;
+  c->cc = cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC || c->adaptive;     // both normalise per particle
+  c->sf_rmax = cfg->sf_radius;
   const int ne = c->ne, nd = c->nd;
   auto bail = [&](int code) { pic_destroy(c); return code; };
+  if (c->adaptive && (cfg->n_dg > 3 || pic::sf_gather_variant() != 5))
+    return bail(fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_adaptive needs N <= 3 and the round-robin gather"));
+  if (c->adaptive) {
+    c->sf_rmax = 0.0;
+    for (int e = 0; e < m->n_elems; ++e) c->sf_rmax = std::max(c->sf_rmax, m->sf_elem_radius[e]);
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(PIC_ERR_CUDA, "cudaStreamCreate failed"));
 
@@ -467,7 +491,8 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       if (m->periodic_vectors[3 * q + d] != 0.0) { k.pv_dir[d] = q; break; }   // GEO%DirPeriodicVectors
   }
   if (c->sf) {
-    k.sf_r = cfg->sf_radius; k.sf_r2 = cfg->sf_radius * cfg->sf_radius; k.sf_r2_inv = 1.0 / k.sf_r2;
+    // the largest radius (adaptive: the per-element radii bound the searches; exact per-particle radii in the kernels)
+    k.sf_r = c->sf_rmax; k.sf_r2 = c->sf_rmax * c->sf_rmax; k.sf_r2_inv = 1.0 / k.sf_r2;
     k.sf_alpha = cfg->sf_alpha; k.sf_w = c->cc ? 1.0 : sf_weight(cfg->sf_radius, cfg->sf_alpha);   // cc: Fac = q MPF (v,1), normalised later
   }
   if (upload_consts(k) != cudaSuccess) return bail(fail(PIC_ERR_CUDA, "constant upload"));

@@ -16,7 +16,9 @@ struct pic_ctx {
   int N = 0, nd = 0, ne = 0, n_canon = 0;
   bool mixed = false, refmap = false, sf = false;
   bool has_walls = false;       // some side is an open or reflective particle boundary
-  bool cc = false;              // shape_function_cc
+  bool cc = false;              // shape_function_cc or _adaptive: per-particle charge normalisation
+  bool adaptive = false;        // shape_function_adaptive: radius per source element (SfLists::elem_r)
+  double sf_rmax = 0.0;         // largest shape-function radius
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
   // mesh

@@ -923,7 +923,7 @@ constexpr int kSf5Chunk = 256;
 constexpr int kSf5Threads = 128;
 constexpr int kSf5Pairs = 160;
 
-template <int N, bool MIXED>
+template <int N, bool MIXED, bool ADAPT>
 __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L, const int* __restrict__ off,
                                                             SfPack K, double* __restrict__ PS) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
@@ -940,6 +940,11 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
   __shared__ int s_b0[kSf5Pairs], s_n[kSf5Pairs];
   __shared__ float s_o[kSf5Pairs][3];
   __shared__ double s_off[MIXED ? 1 : kSf5Pairs][3];
+  // shape_function_adaptive: radius of each pair's source element
+  __shared__ float s_r2f[ADAPT ? kSf5Pairs : 1];                  // (1+1e-4) R_s^2, FP32 pre-test
+  __shared__ double s_rinv[ADAPT && !MIXED ? kSf5Pairs : 1];      // 1/R_s^2
+  __shared__ float2 s_rpf[ADAPT && MIXED ? kSf5Pairs : 1];        // (R_s^2, 1/R_s^2)
+  __shared__ float2 s_rp[ADAPT && MIXED ? kSf5Chunk : 1];         // the same per staged particle
   __shared__ int s_cnt, s_max;
   static_assert(sizeof(double) * 4 * npar * (halves * 32) <= sizeof(double2) * 2 * kSf5Chunk, "sums alias s_pq");
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -958,7 +963,8 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
     const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
     const double gx = __ldg(g) - cex, gy = __ldg(g + 1) - cey, gz = __ldg(g + 2) - cez;
     gd[0] = gx; gd[1] = gy; gd[2] = gz;
-    gd[3] = fma(-R2inv, fma(gx, gx, fma(gy, gy, gz * gz)), 1.0);
+    // B_g = 1 - |g|^2/R^2; adaptive: |g|^2 (the particle's own radius enters at each hit)
+    gd[3] = ADAPT ? fma(gx, gx, fma(gy, gy, gz * gz)) : fma(-R2inv, fma(gx, gx, fma(gy, gy, gz * gz)), 1.0);
     gf[0] = (float)gx; gf[1] = (float)gy; gf[2] = (float)gz;
   }
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -984,6 +990,12 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
       s_o[i][1] = (float)((__ldg(cs + 1) + sh[1]) - cey);
       s_o[i][2] = (float)((__ldg(cs + 2) + sh[2]) - cez);
       if constexpr (!MIXED) { s_off[i][0] = sh[0] - cex; s_off[i][1] = sh[1] - cey; s_off[i][2] = sh[2] - cez; }
+      if constexpr (ADAPT) {
+        const double r = __ldg(L.elem_r + src), r2 = r * r;
+        s_r2f[i] = (float)(r2 * (1.0 + 1.0e-4));
+        if constexpr (MIXED) s_rpf[i] = make_float2((float)r2, (float)(1.0 / r2));
+        else s_rinv[i] = 1.0 / r2;
+      }
       const int b0 = __ldg(off + src), n = __ldg(off + src + 1) - b0;
       s_b0[i] = b0;
       s_n[i] = n;
@@ -1009,9 +1021,10 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
             const float rx = r.x + s_o[pr][0], ry = r.y + s_o[pr][1], rz = r.z + s_o[pr][2];
             if (fmaf(rx, rx, fmaf(ry, ry, rz * rz)) <= cull2) {
               const int slot = atomicAdd(&s_cnt, 1);
-              s_rel[slot] = make_float4(rx, ry, rz, 0.0f);
+              s_rel[slot] = make_float4(rx, ry, rz, ADAPT ? s_r2f[pr] : 0.0f);
               if constexpr (MIXED) {
                 s_facf[slot] = reinterpret_cast<const float4*>(K.facf)[j];
+                if constexpr (ADAPT) s_rp[slot] = s_rpf[pr];
               } else {
                 s_j[slot] = j;
                 s_pr[slot] = (uint8_t)pr;
@@ -1030,8 +1043,15 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
           const int pr = s_pr[slot];
           const double px = K.pos[3 * j] + s_off[pr][0], py = K.pos[3 * j + 1] + s_off[pr][1],
                        pz = K.pos[3 * j + 2] + s_off[pr][2];
-          s_pq[2 * slot] = make_double2(px * t2, py * t2);
-          s_pq[2 * slot + 1] = make_double2(pz * t2, -R2inv * fma(px, px, fma(py, py, pz * pz)));
+          if constexpr (ADAPT) {
+            // 1 - |p-g|^2/R^2 = (1 - |p|^2/R^2) + (2p/R^2).g - |g|^2/R^2 with the source's R
+            const double ri = s_rinv[pr], tt = 2.0 * ri;
+            s_pq[2 * slot] = make_double2(px * tt, py * tt);
+            s_pq[2 * slot + 1] = make_double2(pz * tt, fma(-ri, fma(px, px, fma(py, py, pz * pz)), 1.0));
+          } else {
+            s_pq[2 * slot] = make_double2(px * t2, py * t2);
+            s_pq[2 * slot + 1] = make_double2(pz * t2, -R2inv * fma(px, px, fma(py, py, pz * pz)));
+          }
           const double2* fp = reinterpret_cast<const double2*>(K.fac + 4 * j);
           s_fac[2 * slot] = fp[0];
           s_fac[2 * slot + 1] = fp[1];
@@ -1044,7 +1064,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
       for (int m = 0; parity + npar * m < nst; ++m) {
         const float4 r = s_rel[parity + npar * m];
         const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[w][nh++][lane] = (uint8_t)m;
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f)) s_list[w][nh++][lane] = (uint8_t)m;
       }
       // phase B: this lane's hits
       float part[4] = {0.f, 0.f, 0.f, 0.f};      // mixed: this staged set's FP32 partial sums
@@ -1054,8 +1074,9 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
           const float4 r = s_rel[q];
           const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (r2 <= (float)c_k.sf_r2) {
-            const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
+          const float2 rp = ADAPT ? s_rp[q] : make_float2((float)c_k.sf_r2, (float)R2inv);
+          if (r2 <= rp.x) {
+            const float Sv = fmaf(-rp.y, r2, 1.0f);
             float S1 = Sv * Sv;
             for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
             const float4 f = s_facf[q];
@@ -1066,7 +1087,8 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
           }
         } else {
           const double2 pa = s_pq[2 * q], pb = s_pq[2 * q + 1];
-          const double Sv = fma(pa.x, gd[0], fma(pa.y, gd[1], fma(pb.x, gd[2], pb.y + gd[3])));
+          const double Sv = ADAPT ? fma(pa.x, gd[0], fma(pa.y, gd[1], fma(pb.x, gd[2], fma(-gd[3], s_rinv[s_pr[q]], pb.y))))
+                                  : fma(pa.x, gd[0], fma(pa.y, gd[1], fma(pb.x, gd[2], pb.y + gd[3])));
           // Sv >= 0 read from the sign bit (integer pipe); -0.0 is skipped, its contribution is 0
           if (__double_as_longlong(Sv) >= 0) {
             double S1 = Sv * Sv;
@@ -1134,9 +1156,9 @@ constexpr int kCcCap = 256;       // hit-list entries per thread: a whole round 
 
 template <int N, bool MIXED>
 __device__ __forceinline__ void cc_eval(const double (*s_g)[4], const float4* s_gf, const uint8_t (*s_list)[kCcThreads],
-                                        int nh, const double p[3], const float pf[3], double& acc, float& accf) {
+                                        int nh, const double p[3], const float pf[3], double R2, double R2inv,
+                                        double& acc, float& accf) {
   const int t = threadIdx.x;
-  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
   for (int k = 0; k < nh; ++k) {
     const int d = s_list[k][t];
     if constexpr (MIXED) {
@@ -1175,7 +1197,10 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
   const int b0 = __ldg(off + s), cnt = __ldg(off + s + 1) - b0;
   const double* cs = L.dof_center + (size_t)s * 3;
   const double csx = __ldg(cs), csy = __ldg(cs + 1), csz = __ldg(cs + 2);
-  const float R2f = (float)(c_k.sf_r2 * (1.0 + 1.0e-4));
+  // radius of the source element (shape_function_adaptive) or the global one
+  double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  if (L.elem_r) { const double r = __ldg(L.elem_r + s); R2 = r * r; R2inv = 1.0 / R2; }
+  const float R2f = (float)(R2 * (1.0 + 1.0e-4));
   const int q0 = __ldg(L.t_off + s), npair = __ldg(L.t_off + s + 1) - q0;
   const int stride = (npair + cc_round<N>() - 1) / cc_round<N>();
   for (int base = 0; base < cnt; base += kCcThreads) {
@@ -1217,7 +1242,7 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
         const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
         if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[nh++][t] = (uint8_t)i;
       }
-      cc_eval<N, MIXED>(s_g, s_gf, s_list, nh, p, pf, acc, accf);
+      cc_eval<N, MIXED>(s_g, s_gf, s_list, nh, p, pf, R2, R2inv, acc, accf);
     }
     if (act) {
       const double tot = MIXED ? (double)accf : acc;
@@ -1477,7 +1502,8 @@ int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers
 template <int N, bool MIXED>
 static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
 #if PIC_SF_GATHER == 5
-  k_sf_gather5<N, MIXED><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  if (L.elem_r) k_sf_gather5<N, MIXED, true><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  else k_sf_gather5<N, MIXED, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #else
   k_sf_gather2<N, MIXED><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #endif

@@ -47,6 +47,7 @@ struct SfLists {
   const int* t_tgt;           // [n_pairs] target element (0-based)
   const int8_t* t_shift;      // [n_pairs][3] periodic image of the source particles
   const double* dof_w;        // [ne][nd] wGP(k) wGP(l) wGP(m) / sJ
+  const double* elem_r;       // [ne] shape_function_adaptive: radius of the source element (else NULL)
 };
 struct SfPack {
   double* pos;     // [cap][3] FP64 position (FP64 variant)

@@ -188,6 +188,7 @@ class BoxMesh:
     canonical_node: np.ndarray = field(default=None)  # 0-based periodic-unique id per unique node
     side_bc: np.ndarray = field(default=None)         # (6,nElems) 1 open / 2 reflective wall, 0 otherwise; None: no walls
     bc: tuple = ("periodic", "periodic", "periodic")  # particle boundary per axis
+    sf_elem_radius: np.ndarray = field(default=None)  # SFElemr2_Shared(1,:) for shape_function_adaptive
 
     @property
     def n_dof(self) -> int:

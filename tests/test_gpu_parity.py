@@ -434,3 +434,37 @@ def test_part_data_layout_and_restart(gpu_lib):
     assert np.array_equal(a["inside"][order], b["inside"])
     loop.close()
     loop2.close()
+
+
+def _adaptive_workload(n_cells=6, n_per_species=2000, seed=17):
+    w = workloads.curved_two_species(n_cells=n_cells, n_per_species=n_per_species, seed=seed, nsteps=2)
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE
+    h = 1.0 / n_cells
+    w.mesh.sf_elem_radius = np.random.default_rng(seed).uniform(1.2 * h, 1.8 * h, w.mesh.n_elems)
+    return w
+
+
+def test_shape_function_adaptive_against_oracle(gpu_lib, oracle_lib):
+    """Per-element radii between 1.2 h and 1.8 h: FP64 against the oracle, mixed within 1e-4."""
+    w = _adaptive_workload()
+    g = _run_gpu(w, 2)
+    st, PS = _run_oracle(oracle_lib, w, 2)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["PS"], PS) <= 1e-12
+    gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert g["status"]["error_word"] == 0
+
+
+def test_shape_function_adaptive_conserves_charge(gpu_lib, oracle_lib):
+    w = _adaptive_workload(n_cells=10, n_per_species=50_000, seed=6)
+    ms = capi.MeshStruct(w.mesh)
+    for prec, tol in ((capi.PIC_PREC_FP64, 1e-12), (capi.PIC_PREC_MIXED, 1e-5)):
+        loop = ParticleLoop(w.config(precision=prec), w.mesh)
+        loop.set_field(w.e_dof)
+        sel = w.part_species == 1
+        loop.upload_particles(w.part_state[sel], w.elem[sel], w.part_species[sel])
+        PS = loop.deposition()
+        loop.close()
+        q = w.species[0][0] * w.species[0][2] * int(sel.sum())
+        assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - q) <= tol * abs(q)

@@ -218,3 +218,18 @@ def test_open_walls_remove_the_leaving_particles(oracle_lib):
     assert (~expect).sum() > 300 and st.counters.n_lost == 0
     kept = st.inside.astype(bool)
     assert np.array_equal(st.elem[kept], workloads._elem_of_uniform(w.mesh, st.part_state[kept, :3]))
+
+
+def test_adaptive_with_uniform_radius_is_cc(oracle_lib):
+    """shape_function_adaptive with every element radius = R is shape_function_cc with radius R."""
+    w = workloads.curved_two_species(n_cells=5, n_per_species=800, seed=4, nsteps=1)
+    w.mesh.sf_elem_radius = np.full(w.mesh.n_elems, w.sf_radius)
+    out = {}
+    for dep in (capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE):
+        w.deposition = dep
+        cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+        st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+        PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+        oracle_lib.deposit(cfg, ms, st, PS)
+        out[dep] = PS
+    assert np.array_equal(out[capi.PIC_DEPO_SHAPE_FUNCTION_CC], out[capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
