@@ -116,6 +116,13 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
       (!m->fibgm_n_elems || !m->fibgm_offset || !m->fibgm_element || !m->eps_one_cell))
     return fail(PIC_ERR_INVALID_ARGUMENT, "FIBGM arrays required for RefTracking / shape function");
   if (sf && cfg->sf_alpha < 2) return fail(PIC_ERR_INVALID_ARGUMENT, "shape function alpha must be >= 2");
+  if (cfg->tracking == PIC_TRACK_REFMAPPING) {
+    // RefTracking sorts the candidates of one FIBGM cell in registers (at most 64, pic_device.cuh)
+    const size_t ncell = (size_t)std::max(m->fibgm_imax[0], 1) * std::max(m->fibgm_imax[1], 1) * std::max(m->fibgm_imax[2], 1);
+    for (size_t q = 0; q < ncell; ++q)
+      if (m->fibgm_n_elems[q] > 64)
+        return fail(PIC_ERR_INVALID_ARGUMENT, "a FIBGM cell holds more than 64 elements: refine the background mesh");
+  }
   if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE) {
     if (!m->sf_elem_radius) return fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_adaptive needs sf_elem_radius");
     for (int e = 0; e < m->n_elems; ++e)

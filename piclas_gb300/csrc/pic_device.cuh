@@ -776,7 +776,7 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
   const size_t cidx = (size_t)(cell[0] - 1) + (size_t)c_k.fib_imax[0] * ((cell[1] - 1) + (size_t)c_k.fib_imax[1] * (cell[2] - 1));
   int nBGM = __ldg(M.fib_n + cidx);
   const int off = __ldg(M.fib_off + cidx);
-  if (nBGM > kMaxBgmCand) nBGM = kMaxBgmCand;
+  if (nBGM > kMaxBgmCand) nBGM = kMaxBgmCand;      // pic_create rejects FIBGM cells with more
   double dist[kMaxBgmCand];
   int list[kMaxBgmCand];
   if (nBGM > 1) {
