@@ -109,17 +109,18 @@ def sf_hits_per_launch(w) -> float:
     return w.n * dof_density * 4.0 / 3.0 * math.pi * w.sf_radius ** 3
 
 
-def compute_roofline(w, mixed: bool, avg_ms: float):
-    """The FP64 gather is bound by GB300's FP64 pipe, not by HBM: FLOP/s of its hits against the
-    nominal FP64 rate (no measured FP64 peak exists for this GPU; 1.25 TFLOP/s nominal)."""
+def compute_roofline(w, mixed: bool, avg_ms: float, fp64_peak: float | None):
+    """The FP64 gather is bound by GB300's FP64 pipe, not by HBM: FLOP/s of its hits against the FP64 FMA
+    rate measured in the same run (pic_fp64_fma_rate; nominal 1.25 TFLOP/s if that failed)."""
     from piclas_gb300 import capi
     if w.deposition != capi.PIC_DEPO_SHAPE_FUNCTION or mixed:
         return None
     hits = sf_hits_per_launch(w)
     flops = 19.0 * hits     # per hit: r^2 (3 sub, 3 mul, 2 add), 1 - r^2/R^2 (2), ^2 (1), 4 x (mul, add)
     achieved = flops / (avg_ms / 1e3) / 1e9
-    return {"bound": "fp64", "achieved": achieved, "peak": 1250.0, "unit": "GFLOP/s", "frac": achieved / 1250.0,
-            "peak_kind": "nominal", "hits_per_launch": hits, "flops_per_hit": 19}
+    peak, kind = (fp64_peak, "measured (pic_fp64_fma_rate)") if fp64_peak else (1250.0, "nominal")
+    return {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "GFLOP/s", "frac": achieved / peak,
+            "peak_kind": kind, "nominal_peak": 1250.0, "hits_per_launch": hits, "flops_per_hit": 19}
 
 
 def hbm_peak():
@@ -336,6 +337,10 @@ def run_gpu(args, rank, world, local_rank):
     prof = loop.profile_read()
     loop.profile(False)
     kname, kbytes = dominant_kernel_bytes(w, mixed)
+    try:
+        fp64_peak = loop.fp64_fma_rate()
+    except Exception:
+        fp64_peak = None
     dom = prof["deposit_main"]
     avg_ms = dom["ms"] / max(dom["launches"], 1)
     peak, peak_kind = hbm_peak()
@@ -369,7 +374,7 @@ def run_gpu(args, rank, world, local_rank):
                      "note": ("bound by the FP64 pipe, not HBM (see compute_roofline)"
                               if kname.startswith("k_sf_gather") and not mixed else None)},
         "phases_ms": {k: round(v["ms"] / args.steps, 4) for k, v in prof.items() if v["launches"]},
-        "compute_roofline": compute_roofline(w, mixed, avg_ms),
+        "compute_roofline": compute_roofline(w, mixed, avg_ms, fp64_peak),
         "e2e": e2e,
         "status": st,
     }

@@ -191,6 +191,10 @@ int pic_step(pic_ctx_t* ctx, double dt, int32_t nsteps, double* part_source);
 
 int pic_get_status(pic_ctx_t* ctx, pic_status_t* status);
 
+/* Instrumentation (no reference counterpart): sustained FP64 fused multiply-add rate of this GPU in GFLOP/s,
+ * from independent FMA chains on every SM (~0.1 s); the peak the FP64-bound kernels are compared against. */
+int pic_fp64_fma_rate(pic_ctx_t* ctx, double* gflops);
+
 /* Particle state in the reference's checkpoint layout (FillParticleData, src/io_hdf5/hdf5_output_particle.f90:1531):
  * the particles inside the domain grouped by element, in ascending caller index within an element
  * (UpdateNextFreePosition order); part_data(1:7, n_out) = PartState(1:6), Species; part_int(1:2, nElems) =

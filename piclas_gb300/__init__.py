@@ -36,7 +36,7 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_upload_particles", "pic_download_particles", "pic_interpolate", "pic_push", "pic_track",
                     "pic_deposit", "pic_get_field_at_particles", "pic_step", "pic_get_status", "pic_reset_status",
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
-                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data"]
+                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data", "pic_fp64_fma_rate"]
 
 
 class PicError(RuntimeError):
@@ -80,6 +80,7 @@ def load_library(build_if_missing: bool = False):
     i64p = P(C.c_int64)
     L.pic_get_part_data.argtypes = [C.c_void_p, dp, i64p, C.c_int64, C.c_int32, P(C.c_int32)]
     L.pic_set_part_data.argtypes = [C.c_void_p, dp, i64p, C.c_int64, C.c_int32]
+    L.pic_fp64_fma_rate.argtypes = [C.c_void_p, dp]
     L.pic_step.argtypes = [C.c_void_p, C.c_double, C.c_int32, dp]
     L.pic_get_status.argtypes = [C.c_void_p, P(PicStatus)]
     L.pic_reset_status.argtypes = [C.c_void_p]
@@ -190,6 +191,12 @@ class ParticleLoop:
         ps = out if out is not None else np.zeros((self.mesh.n_elems, self.nd, 4))
         self._check(self.lib.pic_deposit(self.handle, capi.dptr(ps)), "pic_deposit")
         return ps
+
+    def fp64_fma_rate(self) -> float:
+        """Sustained FP64 FMA rate of the GPU (GFLOP/s), measured by the library."""
+        r = C.c_double(0.0)
+        self._check(self.lib.pic_fp64_fma_rate(self.handle, C.byref(r)), "pic_fp64_fma_rate")
+        return r.value
 
     def get_part_data(self, offset_npart: int = 0):
         """Checkpoint layout of the reference (FillParticleData): PartData (n, 7) = x, y, z, vx, vy, vz, species

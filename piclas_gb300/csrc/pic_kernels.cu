@@ -1519,6 +1519,40 @@ int launch_sf_cc_norm(const LaunchArgs& A, const SortBuffers& B, const SfLists& 
 
 int sf_gather_variant() { return PIC_SF_GATHER; }
 
+// FP64 fused multiply-add throughput probe: 8 independent chains per thread keep the FP64 pipe busy;
+// the result is stored only if it is non-finite, so the chains cannot be removed.
+__global__ void __launch_bounds__(256) k_fp64_fma_probe(int iters, double b, double c, double* sink) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (!isfinite(s)) sink[blockIdx.x] = s;
+}
+
+double fp64_fma_rate(cudaStream_t st, double* sink, int sms) {
+  const int blocks = sms * 8, iters = 4096;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_fma_probe<<<blocks, 256, 0, st>>>(iters / 8, 0.9999999, 1e-7, sink);     // warm-up
+  cudaEventRecord(e0, st);
+  k_fp64_fma_probe<<<blocks, 256, 0, st>>>(iters, 0.9999999, 1e-7, sink);
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double flops = 2.0 * 8.0 * (double)iters * 256.0 * (double)blocks;
+  return ms > 0.f ? flops / (ms * 1e-3) / 1e9 : 0.0;
+}
+
 int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
   switch (A.N) {
     case 1: if (A.mixed) launch_gather_n<1, true>(A, B, L, K, PS); else launch_gather_n<1, false>(A, B, L, K, PS); break;

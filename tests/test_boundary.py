@@ -17,7 +17,7 @@ HEADER = os.path.join(ROOT, "include", "piclas_gpu.h")
 def header_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(pic_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(pic_[a-z0-9_]+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")
@@ -32,7 +32,7 @@ def test_header_matches_python_binding():
 
 def test_library_exports_every_declared_symbol(lib):
     out = subprocess.run(["nm", "-D", "--defined-only", library_path()], capture_output=True, text=True, check=True).stdout
-    exported = set(re.findall(r"\bT (pic_[a-z_]+)\b", out))
+    exported = set(re.findall(r"\bT (pic_[a-z0-9_]+)\b", out))
     missing = [s for s in header_functions() if s not in exported]
     assert not missing, missing
     for s in header_functions():

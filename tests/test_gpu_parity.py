@@ -468,3 +468,48 @@ def test_shape_function_adaptive_conserves_charge(gpu_lib, oracle_lib):
         loop.close()
         q = w.species[0][0] * w.species[0][2] * int(sel.sum())
         assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - q) <= tol * abs(q)
+
+
+def test_fp64_fma_rate_probe(gpu_lib):
+    """The FP64 peak the FP64-bound kernels are compared against: a plausible GB300 figure (nominal
+    1.25 TFLOP/s) that repeats within 10 %."""
+    w = workloads.plasma_wave(n_cells=2, N=1, n_particles=10)
+    loop = ParticleLoop(w.config(), w.mesh)
+    r1, r2 = loop.fp64_fma_rate(), loop.fp64_fma_rate()
+    loop.close()
+    assert 200.0 < r1 < 20000.0, r1
+    assert abs(r1 - r2) <= 0.1 * max(r1, r2), (r1, r2)
+
+
+# ---- parity at the benchmark configurations --------------------------------------------------------
+def test_plasma_wave_full_size_100_steps_bitexact(gpu_lib, oracle_lib):
+    """The plasma-wave case as benchmarked (8^3, N=3, 200k electrons, 100 steps, re-sorting every 10):
+    FP64 element ids, positions and velocities bit-identical to the oracle after 100 steps."""
+    import os
+    w = workloads.plasma_wave()
+    g = _run_gpu(w, w.nsteps, sort_interval=10)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, w.nsteps, PS, os.cpu_count() or 1)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["n_lost"] == 0
+
+
+def test_curved_32cube_mesh_parity(gpu_lib, oracle_lib):
+    """The benchmark's 32^3 curved mesh (RefTracking + shape function, B_z = 0.1 T) with 400k particles,
+    2 steps: element ids exact, state and PartSource as in the small-mesh test."""
+    import os
+    w = workloads.curved_two_species(n_per_species=200_000, seed=9, nsteps=2)
+    g = _run_gpu(w, 2)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.map_particles(cfg, ms, st, os.cpu_count() or 1)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, 2, PS, os.cpu_count() or 1)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
+    assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
+    assert _rel(g["PS"], PS) <= 1e-12
