@@ -133,9 +133,9 @@ def hbm_peak():
 
 
 def read_traffic(key: str):
-    """DRAM bytes per launch from the committed ncu summary (profiles/ncu_traffic.md): the row whose
+    """DRAM bytes per launch from the committed ncu summary (profiles/ncu_traffic.txt): the row whose
     first cell is ``key`` ("kernel @ workload"), last cell = bytes per full-size launch."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.md")
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     try:
         for line in open(p):
             if line.startswith("|"):

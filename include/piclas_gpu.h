@@ -3,7 +3,7 @@
  *
  * The entry points replace the argument-less Fortran routines of PICLas's
  * Boris-Leapfrog particle loop.  A Fortran host binds them with ISO_C_BINDING
- * (see INTEGRATION.md); every pointer is a plain host pointer to a contiguous
+ * (BIND(C) interfaces with the same names); every pointer is a plain host pointer to a contiguous
  * array laid out exactly like the reference's Fortran array (column-major,
  * first index fastest).  Index arrays are 1-based, as in the reference.
  *
@@ -26,7 +26,13 @@
  *                          (timedisc_TimeStepPoissonByBorisLeapfrog.f90:32-286 minus HDG)
  *   pic_get_status         NbrOfLostParticles and the abort conditions of the loop
  *                          (particle_triatracking.f90:293-308, eval_xyz.f90:424-441)
+ *   pic_get_part_data / pic_set_part_data
+ *                          FillParticleData and the particle read-in of a restart
+ *                          (src/io_hdf5/hdf5_output_particle.f90:1531, src/particles/restart/particle_readin.f90)
+ *   pic_get_field_at_particles  FieldAtParticle(1:6,:) (src/particles/pic/interpolation/pic_interpolation_vars.f90:26)
  *   pic_adjoint_run        no reference counterpart (differentiable loop, see its comment)
+ *   pic_deposit_cvwm_noalloc, pic_profile*, pic_launch_count, pic_stream, pic_fp64_fma_rate
+ *                          no reference counterpart (allocation-free entry point, instrumentation)
  *
  * Error convention: every int-returning call returns PIC_OK (0) or a positive
  * pic_error_t.  The library never aborts the host process: where the reference
@@ -182,7 +188,7 @@ int pic_track(pic_ctx_t* ctx);
 /* Deposition on the current particle state.  part_source is PS_N(e)%PartSource(1:4,0:N,0:N,0:N)
  * for all elements (4*(N+1)^3*nElems doubles); NULL keeps the result on the device. */
 int pic_deposit(pic_ctx_t* ctx, double* part_source);
-/* FieldAtParticle(1:6,1:n) of the last pic_interpolate / pic_step, caller's particle order. */
+/* FieldAtParticle(1:6,1:n) of the last pic_interpolate (the fused pic_step keeps the field in registers), caller's particle order. */
 int pic_get_field_at_particles(pic_ctx_t* ctx, double* field, int32_t n);
 
 /* nsteps x {Deposition, InterpolateFieldToParticle, push, PerformTracking} with the field frozen.
