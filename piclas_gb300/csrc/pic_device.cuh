@@ -589,6 +589,13 @@ __device__ __forceinline__ bool certainly_inside_f32(const DevMesh& M, int e, co
   return true;
 }
 
+// A particle whose position or velocity overflowed in the push (extreme fields) leaves the loop with
+// PIC_STATUS_NOT_FINITE instead of walking the mesh with NaN coordinates (NaN passes no test, so the
+// inside test would keep it where it is and its deposit would poison PartSource).
+__device__ __forceinline__ bool state_finite(const double x[3], double v0, double v1, double v2) {
+  return isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(v0) && isfinite(v1) && isfinite(v2);
+}
+
 // CalcNormAndTangTriangle, particle_surfaces.f90:256-319 (TriaTracking): unit normal of triangle `tri`,
 // (P(tri+1)-P1) x (P(tri+2)-P1) normalised (the routine's two sign flips cancel)
 __device__ __forceinline__ void triangle_normal(const double* __restrict__ X, uint32_t info, int tri, double n[3]) {

@@ -137,8 +137,11 @@ __device__ __forceinline__ void boris_push_f(float v[3], const float F[6], int s
 #ifndef PIC_CVWM_MIXED_MINB
 #define PIC_CVWM_MIXED_MINB 4   // 4 x 256 threads: 64 registers, a few spills; 1.13x faster than 2 CTAs/SM
 #endif
+#ifndef PIC_CVWM_MINB
+#define PIC_CVWM_MINB 1         // FP64 variant
+#endif
 template <int N, bool MIXED>
-__global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : 1) k_step_cvwm_tria(DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
+__global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MINB) k_step_cvwm_tria(DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
                                                         const float* __restrict__ E32, double* __restrict__ NS,
                                                         double dt, DevStatus* st) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
@@ -191,6 +194,13 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : 1) k_step_c
     double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    if (!state_finite(x, v[0], v[1], v[2])) {
+      flag_status(st, 0x20u);
+      P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
+      P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+      P.flags[i] = (isnew ? (fl | kNew) : (fl & ~kNew)) & ~kInside;
+      return;
+    }
     int ne = tria_track(M, e, x, xl, v);
     P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
     uint8_t nf = isnew ? (fl | kNew) : (fl & ~kNew);
@@ -264,6 +274,13 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : 1) k_step_c
     double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    if (!state_finite(x, v[0], v[1], v[2])) {
+      flag_status(st, 0x20u);
+      P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
+      P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+      P.flags[i] = (isnew ? (fl | kNew) : (fl & ~kNew)) & ~kInside;
+      return;
+    }
     double vd[3] = {(double)v[0], (double)v[1], (double)v[2]};   // reflective walls mirror it in FP64
     int ne = tria_track(M, e, x, xl, vd);
     P.vxf[i] = (float)vd[0]; P.vyf[i] = (float)vd[1]; P.vzf[i] = (float)vd[2];
@@ -343,7 +360,7 @@ __global__ void __launch_bounds__(256) k_interpolate(DevMesh M, MeshF MF, DevPar
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_push(DevParticles P, double dt) {
+__global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
@@ -353,6 +370,7 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt) {
   P.lx[i] = x[0]; P.ly[i] = x[1]; P.lz[i] = x[2];      // LastPartPos (timedisc...:109-110)
   P.last_elem[i] = P.elem[i];
   bool isnew = (fl & kNew) != 0;
+  bool finite;
   if constexpr (!MIXED) {
     double F[6];
 #pragma unroll
@@ -362,6 +380,7 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
     P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
+    finite = state_finite(x, v[0], v[1], v[2]);
   } else {
     float F[6];
 #pragma unroll
@@ -371,9 +390,12 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
     P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
+    finite = state_finite(x, v[0], v[1], v[2]);
   }
   P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
-  P.flags[i] = isnew ? (fl | kNew) : (fl & ~kNew);
+  uint8_t nf = isnew ? (fl | kNew) : (fl & ~kNew);
+  if (!finite) { flag_status(st, 0x20u); nf &= ~kInside; }
+  P.flags[i] = nf;
 }
 
 template <bool MIXED>
@@ -1323,6 +1345,13 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
     P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
   }
   double xl[3] = {P.x[i], P.y[i], P.z[i]};
+  const bool finite = MIXED ? state_finite(x, P.vxf[i], P.vyf[i], P.vzf[i]) : state_finite(x, P.vx[i], P.vy[i], P.vz[i]);
+  if (!finite) {
+    flag_status(st, 0x20u);
+    P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
+    P.flags[i] = (isnew ? (fl | kNew) : (fl & ~kNew)) & ~kInside;
+    return;
+  }
   bool tol = false;
   const int ne = ref_track<MIXED>(M, e, x, xl, xi, tol);
   if (tol) { atomicAdd(&st->n_ref_tolerance, 1); flag_status(st, 0x08u); }
@@ -1452,8 +1481,8 @@ int launch_interpolate(const LaunchArgs& A, const DevParticles& P, bool refmap, 
 
 int launch_push(const LaunchArgs& A, const DevParticles& P, double dt) {
   if (P.n <= 0) return 0;
-  if (A.mixed) k_push<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt);
-  else k_push<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt);
+  if (A.mixed) k_push<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt, A.st);
+  else k_push<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt, A.st);
   return 1;
 }
 

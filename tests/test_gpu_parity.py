@@ -513,3 +513,64 @@ def test_curved_32cube_mesh_parity(gpu_lib, oracle_lib):
     assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
     assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
     assert _rel(g["PS"], PS) <= 1e-12
+
+
+
+# ---- fault injection on the host: bad inputs come back as error codes or status bits ---------------
+def test_nan_upload_rejected(gpu_lib):
+    w = workloads.plasma_wave(n_cells=4, N=2, n_particles=2000, seed=41)
+    loop = ParticleLoop(w.config(), w.mesh)
+    bad = w.part_state.copy()
+    bad[5, 4] = np.nan
+    with pytest.raises(PicError) as e:
+        loop.upload_particles(bad, w.elem, w.part_species)
+    assert e.value.code == 1
+    loop.close()
+
+
+@pytest.mark.parametrize("prec", [capi.PIC_PREC_FP64, capi.PIC_PREC_MIXED])
+@pytest.mark.parametrize("fused", [True, False])
+def test_non_finite_field_removes_particles(gpu_lib, prec, fused):
+    """A field solve that diverged (Inf in one element's DOFs): the particles in that element leave the
+    loop with PIC_STATUS_NOT_FINITE; every other particle and PartSource stay finite."""
+    w = workloads.plasma_wave(n_cells=4, N=2, n_particles=4000, seed=43)
+    hot = 7                                             # 0-based element with the diverged field
+    e_bad = w.e_dof.copy()
+    e_bad[hot] = np.inf
+    loop = ParticleLoop(w.config(precision=prec), w.mesh)
+    loop.set_field(e_bad)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    in_hot = w.elem == hot + 1
+    assert in_hot.any()
+    if fused:
+        loop.time_step(w.dt, 1)
+    else:
+        loop.interpolate_field_to_particle()
+        loop.push(w.dt)
+        loop.perform_tracking()
+    st = loop.status()
+    g = loop.download_particles()
+    assert st["error_word"] & capi.PIC_STATUS_NOT_FINITE
+    assert st["n_inside"] == w.n - int(in_hot.sum())
+    assert not g["inside"][in_hot].any() and g["inside"][~in_hot].all()
+    assert np.isfinite(g["part_state"][~in_hot]).all()
+    loop.set_field(w.e_dof)                             # the next field is sane again
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    loop.time_step(w.dt, 2, PS)
+    assert np.isfinite(PS).all() and loop.status()["n_inside"] == w.n - int(in_hot.sum())
+    loop.close()
+
+
+def test_wrong_start_element_matches_oracle(gpu_lib, oracle_lib):
+    """Particles uploaded with an element that does not contain them: TriaTracking walks (or loses) them
+    exactly as the oracle does."""
+    w = workloads.plasma_wave(n_cells=4, N=2, n_particles=3000, seed=47)
+    wrong = w.elem.copy()
+    wrong[:40] = (wrong[:40] % w.mesh.n_elems) + 1
+    w2 = workloads.Workload(**{**w.__dict__, "elem": wrong})
+    g = _run_gpu(w2, 2)
+    st, PS = _run_oracle(oracle_lib, w2, 2)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert g["status"]["n_lost"] == st.counters.n_lost
+    assert np.array_equal(g["part_state"], st.part_state)
