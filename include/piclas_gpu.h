@@ -30,6 +30,14 @@
  *                          FillParticleData and the particle read-in of a restart
  *                          (src/io_hdf5/hdf5_output_particle.f90:1531, src/particles/restart/particle_readin.f90)
  *   pic_get_field_at_particles  FieldAtParticle(1:6,:) (src/particles/pic/interpolation/pic_interpolation_vars.f90:26)
+ *   pic_hdg_init           InitHDG + Elem_Mat + BuildPrecond (src/hdg/hdg.f90:90, src/hdg/elem_mat.f90:42,513)
+ *   pic_hdg_set_dirichlet  the Dirichlet branch of HDGLinear (src/hdg/hdg_linear.f90:96-150)
+ *   pic_hdg_solve          HDG -> HDGLinear -> CG_solver + PostProcessGradientHDG
+ *                          (src/hdg/hdg.f90:734, hdg_linear.f90:37, src/hdg/hdg_tools.f90:41, elem_mat.f90:621);
+ *                          with pic_hdg_t.solve_in_step, pic_step calls it after every Deposition
+ *                          (timedisc_TimeStepPoissonByBorisLeapfrog.f90:99)
+ *   pic_hdg_get_lambda / pic_hdg_get_elem_mat
+ *                          HDG_Surf_N(:)%lambda, HDG_Vol_N(e)%Ehat/InvDhat/Smat (src/hdg/hdg_vars.f90)
  *   pic_adjoint_run        no reference counterpart (differentiable loop, see its comment)
  *   pic_deposit_cvwm_noalloc, pic_profile*, pic_launch_count, pic_stream, pic_fp64_fma_rate
  *                          no reference counterpart (allocation-free entry point, instrumentation)
@@ -65,6 +73,8 @@ typedef enum pic_error_t {
 #define PIC_STATUS_REF_TOLERANCE   0x08u  /* RefTracking: |xi| > epsOneCell (reference aborts) */
 #define PIC_STATUS_BAD_ELEMENT     0x10u  /* element index out of range in particle data   */
 #define PIC_STATUS_NOT_FINITE      0x20u  /* NaN/Inf position or velocity                  */
+#define PIC_STATUS_CG_NOT_CONVERGED 0x40u /* HDG CG reached MaxIterCG (reference: warning)    */
+#define PIC_STATUS_CG_BREAKDOWN    0x80u  /* HDG CG: v.z = 0 or NaN residual (reference aborts) */
 
 /* ---- option enums ------------------------------------------------------- */
 enum { PIC_TRACK_TRIA = 1, PIC_TRACK_REFMAPPING = 2 };     /* TrackingMethod           */
@@ -213,6 +223,51 @@ int pic_get_part_data(pic_ctx_t* ctx, double* part_data, int64_t* part_int, int6
 int pic_set_part_data(pic_ctx_t* ctx, const double* part_data, const int64_t* part_int, int64_t offset_npart,
                       int32_t n_part);
 
+/* ---- HDG Poisson solve (linear, PP_nVar = 1; src/hdg/) ----------------------------------------------
+ * Solves  -div(grad phi) = rho/eps0  (CalcSourceHDG: resu = -PartSource(4)/eps0) by PICLas's hybridised
+ * DG method: element matrices Ehat, InvDhat, Smat (Elem_Mat), the trace system for lambda on the sides by
+ * preconditioned CG (CG_solver, MatVec), the element-local potential U and E = PostProcessGradientHDG.
+ * Everything runs on the device in FP64; E is written into the context's field (as pic_set_field would),
+ * so InterpolateFieldToParticle sees it without a host round trip.  Conforming meshes with one N
+ * (1..4), vacuum (chi = identity), Dirichlet (BCType 2/4-8: values set by pic_hdg_set_dirichlet, default
+ * 0) and zero-gradient Neumann (BCType 10) sides; without Dirichlet sides the first DOF of
+ * ElemToSide(E2S_SIDE_ID,1,1) is pinned to 0 (ZeroPotentialSide).  lambda is kept between solves and is
+ * the start value of the next CG (as the reference's HDG_Surf_N(:)%lambda). */
+typedef struct pic_hdg_t {
+  int32_t n_sides;                /* nSides                                                           */
+  const int32_t* elem_to_side;    /* ElemToSide(1:2,1:6,nElems): E2S_SIDE_ID (1-based), E2S_FLIP      */
+  const int32_t* side_to_elem;    /* SideToElem(1:5,nSides): S2E_ELEM_ID, S2E_NB_ELEM_ID, S2E_LOC_SIDE_ID,
+                                     S2E_NB_LOC_SIDE_ID, S2E_FLIP; -1 where a side has no such element  */
+  const double* metrics_f;        /* N_VolMesh(e)%Metrics_fTilde(1:3,0:N,0:N,0:N) for all elements    */
+  const double* metrics_g;        /* N_VolMesh(e)%Metrics_gTilde                                       */
+  const double* metrics_h;        /* N_VolMesh(e)%Metrics_hTilde                                       */
+  const double* sj;               /* N_VolMesh(e)%sJ(0:N,0:N,0:N) for all elements                     */
+  int32_t n_dirichlet;            /* nDirichletBCSides                                                 */
+  const int32_t* dirichlet_sides; /* DirichletBC(1:nDirichletBCSides), 1-based SideIDs                 */
+  int32_t precond_type;           /* PrecondType: 0 none, 1 side-block Cholesky, 2 diagonal            */
+  int32_t max_iter_cg;            /* MaxIterCG                                                         */
+  double  eps_cg;                 /* epsCG                                                             */
+  int32_t use_relative_abort;     /* useRelativeAbortCrit                                              */
+  int32_t solve_in_step;          /* 1: pic_step solves after every Deposition (HDG(), :99)            */
+} pic_hdg_t;
+typedef struct pic_hdg_status_t {
+  int32_t iterations;             /* CG iterations of the last solve                                   */
+  int32_t converged;              /* 1: |r|^2 below the abort criterion                                */
+  double  norm_r;                 /* sqrt(r.r) at the end of the last solve                            */
+  int64_t n_solves;               /* solves since pic_hdg_init                                         */
+} pic_hdg_status_t;
+int pic_hdg_init(pic_ctx_t* ctx, const pic_hdg_t* hdg);
+/* lambda on the Dirichlet sides, (nGP_face, nDirichletBCSides) in DirichletBC order */
+int pic_hdg_set_dirichlet(pic_ctx_t* ctx, const double* lambda_bc);
+/* One HDGLinear solve.  source = NULL: the charge density of the last deposition on the device
+ * (resu = -PartSource(4)/eps0); otherwise resu itself, (0:N,0:N,0:N, nElems) on the host.  phi and e_field
+ * (U_N(e)%U(1,...), U_N(e)%E(1:3,...)) are copied to the host when non-NULL; status may be NULL. */
+int pic_hdg_solve(pic_ctx_t* ctx, const double* source, double* phi, double* e_field, pic_hdg_status_t* status);
+int pic_hdg_get_lambda(pic_ctx_t* ctx, double* lambda /* (nGP_face, nSides) */);
+/* Elem_Mat of one element (1-based): Ehat(nGP_face,nGP_vol,6), InvDhat(nGP_vol,nGP_vol), Smat(nGP_face,
+ * nGP_face,6,6); any pointer may be NULL */
+int pic_hdg_get_elem_mat(pic_ctx_t* ctx, int32_t elem, double* ehat, double* inv_dhat, double* smat);
+
 /* Differentiable loop (no reference counterpart; the reference has no adjoint).  Starting from the
  * uploaded particles (taken as x_0 and v_{-1/2}; IsNewPart is not applied), runs nsteps of
  * {interpolation, Boris push, TriaTracking} with the field frozen and B = b_scale * B_ext, deposits
@@ -243,8 +298,8 @@ int pic_synchronize(pic_ctx_t* ctx);
  * returns accumulated milliseconds and kernel launches per phase:
  *   0 dominant deposition kernel (shape-function gather, or the fused CVWM+push+tracking kernel)
  *   1 sort-by-element + pack   2 interpolation+push+tracking   3 node -> DOF
- *   4 particle reorder         5 stand-alone CVWM deposition */
-#define PIC_N_PHASES 6
+ *   4 particle reorder         5 stand-alone CVWM deposition   6 HDG solve */
+#define PIC_N_PHASES 7
 int pic_profile(pic_ctx_t* ctx, int32_t enable);
 int pic_profile_read(pic_ctx_t* ctx, double* ms, int64_t* launches, int32_t nphase);
 /* cell_volweight_mean deposition that makes no device allocation (no reference counterpart).

@@ -31,10 +31,17 @@ class OrcCounters(C.Structure):
                 ("n_hop_limit", C.c_int64)]
 
 
+class OrcHdgMesh(C.Structure):
+    _fields_ = [("N", C.c_int), ("ne", C.c_int), ("n_sides", C.c_int), ("e2s", C.POINTER(C.c_int32)),
+                ("s2e", C.POINTER(C.c_int32)), ("mf", C.POINTER(C.c_double)), ("mg", C.POINTER(C.c_double)),
+                ("mh", C.POINTER(C.c_double)), ("sj", C.POINTER(C.c_double)), ("xgp", C.POINTER(C.c_double)),
+                ("wgp", C.POINTER(C.c_double)), ("n_dir", C.c_int), ("dir_sides", C.POINTER(C.c_int32))]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
-    src = os.path.join(_HERE, "pic_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("pic_oracle.c", "pic_oracle_hdg.c", "pic_oracle.h")]
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(map(os.path.getmtime, srcs)):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -59,6 +66,10 @@ def lib():
         L.orc_get_position_in_ref_elem.argtypes = [P(PicConfig), P(PicMesh), P(C.c_double), P(C.c_double), C.c_int,
                                                    C.c_int]
         L.orc_max_threads.restype = C.c_int
+        L.orc_hdg_elem_mat.argtypes = [P(OrcHdgMesh), P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double)]
+        L.orc_hdg_solve.argtypes = [P(OrcHdgMesh), P(C.c_double), P(C.c_double), P(C.c_double), C.c_int, C.c_double,
+                                    C.c_int, C.c_int, P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double),
+                                    P(C.c_double), P(C.c_int), P(C.c_double)]
         _lib = L
     return _lib
 
@@ -136,3 +147,48 @@ def lagrange_polys(x, xgp, wbary):
     L = np.zeros(len(xgp))
     lib().orc_lagrange_polys(float(x), len(xgp) - 1, dptr(xgp), dptr(wb), dptr(L))
     return L
+
+
+# ---- HDG Poisson solve ----------------------------------------------------------------------------
+class HdgOracle:
+    """Elem_Mat + HDGLinear of the oracle for one (BoxMesh, HdgMesh) pair."""
+
+    def __init__(self, mesh, hmesh):
+        self._keep = [np.ascontiguousarray(a) for a in (hmesh.elem_to_side.astype(np.int32),
+                                                        hmesh.side_to_elem.astype(np.int32),
+                                                        hmesh.metrics_f, hmesh.metrics_g, hmesh.metrics_h,
+                                                        hmesh.sj, mesh.xgp, mesh.wgp,
+                                                        np.asarray(hmesh.dirichlet_sides, np.int32))]
+        e2s, s2e, mf, mg, mh, sj, xg, wg, ds = self._keep
+        self.N, self.ne, self.n_sides = mesh.N, mesh.n_elems, hmesh.n_sides
+        self.nd = mesh.N + 1
+        self.nv, self.nf = self.nd ** 3, self.nd ** 2
+        self.n_dir = len(ds)
+        self.s = OrcHdgMesh(self.N, self.ne, self.n_sides, iptr(e2s), iptr(s2e), dptr(mf), dptr(mg), dptr(mh),
+                            dptr(sj), dptr(xg), dptr(wg), self.n_dir, iptr(ds) if self.n_dir else C.POINTER(C.c_int32)())
+        self.ehat = np.zeros((self.ne, 6, self.nv, self.nf))      # Ehat(nf,nv,6) per element
+        self.inv_dhat = np.zeros((self.ne, self.nv, self.nv))
+        self.smat = np.zeros((self.ne, 6, 6, self.nf, self.nf))   # Smat(nf,nf,6,6) -> [jS][iS][b][a]
+        self.tau = np.zeros(self.ne)
+        rc = lib().orc_hdg_elem_mat(C.byref(self.s), dptr(self.ehat), dptr(self.inv_dhat), dptr(self.smat),
+                                    dptr(self.tau))
+        if rc:
+            raise RuntimeError(f"orc_hdg_elem_mat failed: {rc}")
+        self.lam = np.zeros((self.n_sides, self.nf))
+
+    def solve(self, resu, precond_type=0, eps_cg=1e-10, max_iter=10000, relative=False, lambda_dirichlet=None):
+        """resu: CalcSourceHDG at the volume points, C [e][k][j][i].  Returns (phi, E, iterations, norm, rc)."""
+        resu = np.ascontiguousarray(resu, dtype=np.float64).reshape(self.ne, self.nv)
+        ld = (np.ascontiguousarray(lambda_dirichlet, dtype=np.float64) if lambda_dirichlet is not None
+              else None)
+        U = np.zeros((self.ne, self.nv))
+        E = np.zeros((self.ne, self.nv, 3))
+        it = C.c_int(0)
+        nrm = C.c_double(0.0)
+        rc = lib().orc_hdg_solve(C.byref(self.s), dptr(self.ehat), dptr(self.inv_dhat), dptr(self.smat),
+                                 int(precond_type), float(eps_cg), int(max_iter), int(bool(relative)), dptr(resu),
+                                 dptr(ld) if ld is not None else C.POINTER(C.c_double)(), dptr(self.lam),
+                                 dptr(U), dptr(E), C.byref(it), C.byref(nrm))
+        if rc > 0:
+            raise RuntimeError(f"orc_hdg_solve failed: {rc}")
+        return U, E, it.value, nrm.value, rc

@@ -70,6 +70,33 @@ void orc_map_particles(const pic_config_t* cfg, const pic_mesh_t* m, orc_particl
 
 int orc_max_threads(void);
 
+/* ---- HDG Poisson solve (pic_oracle_hdg.c) --------------------------------------------------------- */
+#define ORC_HDG_MAXND 6
+#define ORC_HDG_MAXNF (ORC_HDG_MAXND * ORC_HDG_MAXND)
+#define ORC_HDG_MAXNV (ORC_HDG_MAXNF * ORC_HDG_MAXND)
+typedef struct OrcHdgMesh {
+  int N, ne, n_sides;
+  const int32_t* e2s;        /* ElemToSide(1:2,1:6,nElems): SideID (1-based), flip */
+  const int32_t* s2e;        /* SideToElem(1:5,nSides), -1 = none                  */
+  const double* mf;          /* Metrics_fTilde(1:3,0:N,0:N,0:N,nElems)             */
+  const double* mg;
+  const double* mh;
+  const double* sj;          /* sJ(0:N,0:N,0:N,nElems)                             */
+  const double* xgp;         /* Gauss nodes and weights                            */
+  const double* wgp;
+  int n_dir;                 /* nDirichletBCSides                                  */
+  const int32_t* dir_sides;  /* DirichletBC(:), 1-based                            */
+} OrcHdgMesh;
+/* Elem_Mat: Ehat(nf,nv,6), InvDhat(nv,nv), Smat(nf,nf,6,6) per element; Tau per element.  0 = ok */
+int orc_hdg_elem_mat(const OrcHdgMesh* H, double* ehat, double* inv_dhat, double* smat, double* tau);
+/* HDGLinear with CG_solver: resu = CalcSourceHDG at every volume point (nv,nElems); lambda (nf,nSides)
+ * is the start value and the result; U (nv,nElems), E (3,nv,nElems).  0 ok, -1 not converged,
+ * >0 failure (3 preconditioner, 4 vz = 0, 5 NaN residual) */
+int orc_hdg_solve(const OrcHdgMesh* H, const double* ehat, const double* inv_dhat, const double* smat,
+                  int precond_type, double eps_cg, int max_iter_cg, int use_relative, const double* resu,
+                  const double* lambda_dirichlet, double* lambda, double* U, double* E, int* iterations,
+                  double* norm_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,7 +36,9 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_upload_particles", "pic_download_particles", "pic_interpolate", "pic_push", "pic_track",
                     "pic_deposit", "pic_get_field_at_particles", "pic_step", "pic_get_status", "pic_reset_status",
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
-                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data", "pic_fp64_fma_rate"]
+                    "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data", "pic_fp64_fma_rate",
+                    "pic_hdg_init", "pic_hdg_set_dirichlet", "pic_hdg_solve", "pic_hdg_get_lambda",
+                    "pic_hdg_get_elem_mat"]
 
 
 class PicError(RuntimeError):
@@ -94,6 +96,11 @@ def load_library(build_if_missing: bool = False):
     L.pic_adjoint_run.argtypes = [C.c_void_p, P(capi.PicAdjointConfig), dp, dp, dp, dp]
     L.pic_stream.argtypes = [C.c_void_p]
     L.pic_stream.restype = C.c_void_p
+    L.pic_hdg_init.argtypes = [C.c_void_p, P(capi.PicHdg)]
+    L.pic_hdg_set_dirichlet.argtypes = [C.c_void_p, dp]
+    L.pic_hdg_solve.argtypes = [C.c_void_p, dp, dp, dp, P(capi.PicHdgStatus)]
+    L.pic_hdg_get_lambda.argtypes = [C.c_void_p, dp]
+    L.pic_hdg_get_elem_mat.argtypes = [C.c_void_p, C.c_int32, dp, dp, dp]
     _LIB = L
     return L
 
@@ -257,16 +264,70 @@ class ParticleLoop:
                                              C.byref(gb) if gradients else _null(C.c_double)), "pic_adjoint_run")
         return (loss.value, gv, gb.value) if gradients else loss.value
 
-    PHASES = ("deposit_main", "sort_pack", "particle_update", "node_to_dof", "reorder", "cvwm_deposit")
+    PHASES = ("deposit_main", "sort_pack", "particle_update", "node_to_dof", "reorder", "cvwm_deposit", "hdg")
 
     def profile(self, enable: bool):
         self._check(self.lib.pic_profile(self.handle, 1 if enable else 0), "pic_profile")
 
     def profile_read(self) -> dict:
-        ms = (C.c_double * 6)()
-        ln = (C.c_int64 * 6)()
-        self._check(self.lib.pic_profile_read(self.handle, ms, ln, 6), "pic_profile_read")
+        n = len(self.PHASES)
+        ms = (C.c_double * n)()
+        ln = (C.c_int64 * n)()
+        self._check(self.lib.pic_profile_read(self.handle, ms, ln, n), "pic_profile_read")
         return {name: dict(ms=float(ms[i]), launches=int(ln[i])) for i, name in enumerate(self.PHASES)}
+
+    # -- HDG Poisson solve --------------------------------------------------------------------
+    def hdg_init(self, hmesh, precond_type: int = 2, eps_cg: float = 1e-6, max_iter_cg: int = 500,
+                 relative: bool = False, solve_in_step: bool = False):
+        """InitHDG/Elem_Mat/BuildPrecond from a :class:`piclas_gb300.hdg_mesh.HdgMesh`."""
+        self._hdg_keep = [np.ascontiguousarray(hmesh.elem_to_side, dtype=np.int32),
+                          np.ascontiguousarray(hmesh.side_to_elem, dtype=np.int32),
+                          np.ascontiguousarray(hmesh.metrics_f, dtype=np.float64),
+                          np.ascontiguousarray(hmesh.metrics_g, dtype=np.float64),
+                          np.ascontiguousarray(hmesh.metrics_h, dtype=np.float64),
+                          np.ascontiguousarray(hmesh.sj, dtype=np.float64),
+                          np.ascontiguousarray(hmesh.dirichlet_sides, dtype=np.int32)]
+        e2s, s2e, mf, mg, mh, sj, ds = self._hdg_keep
+        h = capi.PicHdg(hmesh.n_sides, capi.iptr(e2s), capi.iptr(s2e), capi.dptr(mf), capi.dptr(mg), capi.dptr(mh),
+                        capi.dptr(sj), len(ds), capi.iptr(ds) if len(ds) else _null(C.c_int32), int(precond_type),
+                        int(max_iter_cg), float(eps_cg), int(bool(relative)), int(bool(solve_in_step)))
+        self._check(self.lib.pic_hdg_init(self.handle, C.byref(h)), "pic_hdg_init")
+        self.hdg_n_sides = hmesh.n_sides
+        self.hdg_n_dirichlet = len(ds)
+
+    def hdg_set_dirichlet(self, lambda_bc: np.ndarray):
+        lb = np.ascontiguousarray(lambda_bc, dtype=np.float64)
+        self._check(self.lib.pic_hdg_set_dirichlet(self.handle, capi.dptr(lb)), "pic_hdg_set_dirichlet")
+
+    def hdg_solve(self, source: np.ndarray | None = None, want_phi: bool = True, want_e: bool = True):
+        """One HDGLinear solve; source = CalcSourceHDG values (nElems, (N+1)^3) or None for the deposited
+        charge.  Returns (phi (nElems,(N+1)^3) | None, E (nElems,(N+1)^3,3) | None, status dict)."""
+        src = None if source is None else np.ascontiguousarray(source, dtype=np.float64)
+        phi = np.zeros((self.mesh.n_elems, self.nd)) if want_phi else None
+        E = np.zeros((self.mesh.n_elems, self.nd, 3)) if want_e else None
+        st = capi.PicHdgStatus()
+        self._check(self.lib.pic_hdg_solve(self.handle, capi.dptr(src) if src is not None else _null(C.c_double),
+                                           capi.dptr(phi) if phi is not None else _null(C.c_double),
+                                           capi.dptr(E) if E is not None else _null(C.c_double), C.byref(st)),
+                    "pic_hdg_solve")
+        return phi, E, dict(iterations=st.iterations, converged=st.converged, norm_r=st.norm_r, n_solves=st.n_solves)
+
+    def hdg_lambda(self) -> np.ndarray:
+        nf = (self.N + 1) ** 2
+        lam = np.zeros((self.hdg_n_sides, nf))
+        self._check(self.lib.pic_hdg_get_lambda(self.handle, capi.dptr(lam)), "pic_hdg_get_lambda")
+        return lam
+
+    def hdg_elem_mat(self, elem: int):
+        """(Ehat (6,nv,nf), InvDhat (nv,nv), Smat (6,6,nf,nf)) of 1-based element ``elem`` (C views of the
+        reference's Fortran arrays)."""
+        nv, nf = self.nd, (self.N + 1) ** 2
+        eh = np.zeros((6, nv, nf))
+        di = np.zeros((nv, nv))
+        sm = np.zeros((6, 6, nf, nf))
+        self._check(self.lib.pic_hdg_get_elem_mat(self.handle, int(elem), capi.dptr(eh), capi.dptr(di), capi.dptr(sm)),
+                    "pic_hdg_get_elem_mat")
+        return eh, di, sm
 
     def set_field_ptr(self, ptr: int):
         """Field from a host pointer (e.g. pinned memory)."""

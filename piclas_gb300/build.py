@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libpiclas_gpu.so")
-SOURCES = ["pic_kernels.cu", "pic_capi.cu", "pic_noalloc.cu", "pic_adjoint.cu"]
+SOURCES = ["pic_kernels.cu", "pic_capi.cu", "pic_noalloc.cu", "pic_adjoint.cu", "pic_hdg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -28,6 +28,8 @@ PIC_STATUS_HOP_LIMIT = 0x04
 PIC_STATUS_REF_TOLERANCE = 0x08
 PIC_STATUS_BAD_ELEMENT = 0x10
 PIC_STATUS_NOT_FINITE = 0x20
+PIC_STATUS_CG_NOT_CONVERGED = 0x40
+PIC_STATUS_CG_BREAKDOWN = 0x80
 
 ERROR_NAMES = {0: "PIC_OK", 1: "PIC_ERR_INVALID_ARGUMENT", 2: "PIC_ERR_CUDA", 3: "PIC_ERR_OUT_OF_MEMORY",
                4: "PIC_ERR_NO_DEVICE", 5: "PIC_ERR_STATE", 6: "PIC_ERR_CAPACITY"}
@@ -68,6 +70,18 @@ class PicMesh(C.Structure):
 class PicAdjointConfig(C.Structure):
     _fields_ = [("nsteps", C.c_int32), ("checkpoint_every", C.c_int32), ("precision", C.c_int32),
                 ("dt", C.c_double), ("rho_scale", C.c_double), ("b_scale", C.c_double)]
+
+
+class PicHdg(C.Structure):
+    _fields_ = [("n_sides", C.c_int32), ("elem_to_side", _ip), ("side_to_elem", _ip), ("metrics_f", _dp),
+                ("metrics_g", _dp), ("metrics_h", _dp), ("sj", _dp), ("n_dirichlet", C.c_int32),
+                ("dirichlet_sides", _ip), ("precond_type", C.c_int32), ("max_iter_cg", C.c_int32),
+                ("eps_cg", C.c_double), ("use_relative_abort", C.c_int32), ("solve_in_step", C.c_int32)]
+
+
+class PicHdgStatus(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("norm_r", C.c_double),
+                ("n_solves", C.c_int64)]
 
 
 class PicStatus(C.Structure):

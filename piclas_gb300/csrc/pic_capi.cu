@@ -480,6 +480,8 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   k.refmapping_eps = cfg->refmapping_eps > 0.0 ? cfg->refmapping_eps : 1e-4;
   const double c2 = 299792458.0 * 299792458.0;
   k.c2_inv = 1.0 / c2;
+  c->xgp_h.assign(m->xgp, m->xgp + n1);
+  c->wgp_h.assign(m->wgp, m->wgp + n1);
   for (int i = 0; i < n1; ++i) {
     k.xgp[i] = m->xgp[i]; k.wbary_gp[i] = m->wbary_gp[i];
     k.fac_gp[i] = (m->xgp[i] + 1.0) / 2.0;    // CellVolWeight%Fac, pic_depo.f90:274-275
@@ -545,6 +547,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
 void pic_destroy(pic_ctx_t* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  hdg_destroy(c);
   for (auto& r : c->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c->pool) cudaEventDestroy(e);
   for (void* p : c->allocs) cudaFree(p);
@@ -714,7 +717,7 @@ int pic_track(pic_ctx_t* c) {
   return PIC_OK;
 }
 
-enum { PH_MAIN = 0, PH_PACK = 1, PH_PARTICLE = 2, PH_NODE2DOF = 3, PH_REORDER = 4, PH_OTHER = 5 };
+enum { PH_MAIN = 0, PH_PACK = 1, PH_PARTICLE = 2, PH_NODE2DOF = 3, PH_REORDER = 4, PH_OTHER = 5, PH_HDG = 6 };
 
 static int deposit_device(pic_ctx* c) {
   const LaunchArgs A = c->args();
@@ -725,6 +728,7 @@ static int deposit_device(pic_ctx* c) {
   } else {
     c->phase(PH_OTHER, [&] { return launch_deposit_cvwm(A, c->P, c->PS); });
   }
+  c->ps_valid = true;
   return PIC_OK;
 }
 
@@ -824,7 +828,8 @@ int pic_get_field_at_particles(pic_ctx_t* c, double* field, int32_t n) {
 int pic_step(pic_ctx_t* c, double dt, int32_t nsteps, double* part_source) {
   if (!c) return fail(PIC_ERR_INVALID_ARGUMENT, "null context");
   if (nsteps < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "nsteps < 0");
-  if (!c->field_set || !c->have_particles) return fail(PIC_ERR_STATE, "field and particles must be set first");
+  const bool solve = hdg_solve_in_step(c);
+  if (!(c->field_set || solve) || !c->have_particles) return fail(PIC_ERR_STATE, "field and particles must be set first");
   const int sort_every = c->cfg.sort_interval;
   for (int it = 0; it < nsteps; ++it) {
     LaunchArgs A = c->args();
@@ -833,12 +838,18 @@ int pic_step(pic_ctx_t* c, double dt, int32_t nsteps, double* part_source) {
       swap_sorted(c);
       A = c->args();
     }
-    if (!c->sf && !c->refmap) {
+    if (!c->sf && !c->refmap && !solve) {
       // Deposition + InterpolateFieldToParticle + push + TriaTracking in one kernel, then node -> DOF
       c->phase(PH_MAIN, [&] { return launch_cvwm_fused(A, c->P, dt); });
       c->phase(PH_NODE2DOF, [&] { return launch_node_to_dof(A, c->PS); });
+      c->ps_valid = true;
     } else {
       deposit_device(c);                                  // Deposition on x_n
+      if (solve) {                                        // HDG(): the field of rho_n
+        int rc = PIC_OK;
+        c->phase(PH_HDG, [&] { rc = hdg_solve_device(c, c->PS, nullptr); return 0; });
+        if (rc) return rc;
+      }
       if (c->refmap) {
         c->phase(PH_PARTICLE, [&] { return launch_step_ref(A, c->P, dt); });   // interpolation + push + RefTracking
       } else {

@@ -6,6 +6,12 @@
 #include <string>
 #include <vector>
 
+struct HdgState;            // HDG Poisson solve (pic_hdg.cu)
+struct pic_ctx;
+int hdg_destroy(pic_ctx* c);
+int hdg_solve_device(pic_ctx* c, const double* part_source_dev, const double* resu_host);
+bool hdg_solve_in_step(const pic_ctx* c);
+
 namespace pic_internal {
 int dalloc_bytes(void** p, size_t bytes);   // cudaMalloc with the library's error reporting
 int set_error(int code, const std::string& msg);
@@ -31,6 +37,10 @@ struct pic_ctx {
   // deposition
   double* NS = nullptr;
   double* PS = nullptr;
+  bool ps_valid = false;        // PS holds a deposition
+  // HDG field solve (pic_hdg_init)
+  HdgState* hdg = nullptr;
+  std::vector<double> xgp_h, wgp_h;   // N_Inter(N)%xGP, wGP
   pic::SortBuffers sortb{};
   pic::SfLists sfl{};
   pic::SfPack sfk{};

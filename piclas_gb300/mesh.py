@@ -352,9 +352,10 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     dims = (nx, ny, nz)
     ijk = np.stack([ei, ej, ek], axis=1)
 
-    def grid_of(e, t):
+    def grid_of(base, t):
+        """Unwrapped grid position of corner t of the element whose first corner sits at ``base``."""
         a, b, c = t & 1, (t >> 1) & 1, (t >> 2) & 1
-        return ((int(ijk[e, 0]) + a) % nx, (int(ijk[e, 1]) + b) % ny, (int(ijk[e, 2]) + c) % nz)
+        return (base[0] + a, base[1] + b, base[2] + c)
 
     side_bc = np.zeros((ne, 6), dtype=np.int32)
     for e in range(ne):
@@ -381,11 +382,15 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                 side_flip[e, s] = 0
             else:
                 # slave side: rotate so that node 1 coincides with the master's node 1
-                sm = s_master = {0: 5, 1: 3, 4: 2}[s]
-                master_first = grid_of(en, CGNS_TO_TENSOR[SIDE_CGNS[sm][0] - 1])
+                # compare unwrapped grid positions: the neighbour sits at ijk(e) + offset, so that a
+                # box with one element along an axis (its own periodic neighbour) matches unambiguously
+                sm = {0: 5, 1: 3, 4: 2}[s]
+                base_e = tuple(int(ijk[e, d]) for d in range(3))
+                base_n = tuple(base_e[d] + off[d] for d in range(3))
+                master_first = grid_of(base_n, CGNS_TO_TENSOR[SIDE_CGNS[sm][0] - 1])
                 nstart = -1
                 for r in range(4):
-                    if grid_of(e, CGNS_TO_TENSOR[cg[r] - 1]) == master_first:
+                    if grid_of(base_e, CGNS_TO_TENSOR[cg[r] - 1]) == master_first:
                         nstart = r
                         break
                 assert nstart >= 0
