@@ -462,7 +462,104 @@ def extras(args, w_main):
     res["plasma_wave_mixed_per_step"] = precision_report.summarize(
         precision_report.mixed_vs_fp64_per_step(pw, pw.nsteps))
     res["adjoint"] = adjoint_timing()
+    res["hdg"] = hdg_timing()
     return res
+
+
+def hdg_timing(cells=(8, 32), reps: int = 3, self_consistent: bool = True):
+    """HDG Poisson solve (HDGLinear: RHS, CG_solver, PostProcessGradientHDG; Elem_Mat once at init) on periodic
+    boxes of 8^3 (the plasma-wave mesh) and 32^3 (the curved workload's mesh) hexahedra, N = 3, PrecondType 2,
+    epsCG 1e-6 relative to the first residual, each solve from lambda = 0.  The source is the periodic
+    manufactured case phi = sin(2pi x+1) sin(2pi y+2) sin(2pi z+3).  Reported: init time, solve time,
+    CG iterations, and the Smat bytes streamed per iteration over the CG time (the matvec reads every
+    element's 36 blocks once per iteration).  The oracle's single-threaded solve of the 8^3 case is timed
+    beside it.  Then the self-consistent plasma wave (200k electrons + 200k resting ions, CVWM,
+    TriaTracking, one solve per step from the previous lambda) in FP64 and mixed."""
+    import torch
+    from piclas_gb300 import ParticleLoop, capi, workloads
+    from piclas_gb300.hdg_mesh import build_hdg_mesh
+    from piclas_gb300.mesh import build_box_mesh
+    out = {}
+    tp = 2.0 * np.pi
+
+    def source(m):
+        x = tp * m.elem_xgp
+        phi = np.sin(x[..., 0] + 1.0) * np.sin(x[..., 1] + 2.0) * np.sin(x[..., 2] + 3.0)
+        return (-3.0 * tp * tp * phi).reshape(m.n_elems, -1)
+
+    for n in cells:
+        m = build_box_mesh(n, n, n, 3, perturb=0.05 if n == 32 else 0.0)
+        h = build_hdg_mesh(m)
+        cfg = capi.make_config(3, capi.PIC_TRACK_TRIA, capi.PIC_DEPO_CVWM, capi.PIC_PREC_FP64,
+                               [(-1.60217653e-19, 9.1093826e-31, 1.0)], 1)
+        loop = ParticleLoop(cfg, m)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loop.hdg_init(h, precond_type=2, eps_cg=1e-6, relative=True, max_iter_cg=5000)
+        t_init = time.perf_counter() - t0
+        src = source(m)
+        zero = np.zeros((h.n_sides, 16))
+        loop.hdg_set_lambda(zero)
+        loop.hdg_solve(src, want_phi=False, want_e=False)                  # warm-up
+        times, its = [], []
+        for _ in range(reps):
+            loop.hdg_set_lambda(zero)
+            t0 = time.perf_counter()
+            _, _, st = loop.hdg_solve(src, want_phi=False, want_e=False)
+            times.append(time.perf_counter() - t0)
+            its.append(st["iterations"])
+        tsol = float(np.median(times))
+        # the matvec is FP64-bound: 36 blocks of 16x16 per element, one fused multiply-add per entry
+        # (the 15 off-diagonal stored blocks are applied twice, S_ij and S_ij^T)
+        flops = 2.0 * 36 * 16 * 16 * m.n_elems
+        entry = {"mesh": f"{n}^3 hex, N=3, periodic", "elements": m.n_elems, "sides": h.n_sides,
+                 "init_s": t_init, "solve_ms": tsol * 1e3, "cg_iterations": int(its[0]),
+                 "ms_per_iteration": tsol * 1e3 / max(its[0], 1),
+                 "matvec_fp64_gflops_lower_bound": flops * its[0] / tsol / 1e9}
+        loop.close()
+        if n == cells[0]:
+            import oracle
+            o = oracle.HdgOracle(m, h)
+            t0 = time.perf_counter()
+            _, _, it_o, _, _ = o.solve(src, precond_type=2, eps_cg=1e-6, relative=True, max_iter=5000)
+            t_o = time.perf_counter() - t0
+            entry["oracle_cpu"] = {"solve_ms": t_o * 1e3, "cg_iterations": it_o, "cores": 1,
+                                   "kind": "port"}
+        out[f"{n}cube"] = entry
+
+    if not self_consistent:
+        return out
+    # self-consistent plasma wave: Deposition -> HDG -> push -> TriaTracking every step
+    pw = workloads.plasma_wave()
+    rng = np.random.default_rng(7)
+    xi = rng.random((pw.n, 3)) * (pw.mesh.hi - pw.mesh.lo) + pw.mesh.lo
+    q, mass, mpf = pw.species[0]
+    w = workloads.Workload(**{**pw.__dict__, "species": [pw.species[0], (-q, 1836.0 * mass, mpf)],
+                              "part_state": np.concatenate([pw.part_state, np.concatenate([xi, np.zeros((pw.n, 3))], 1)]),
+                              "elem": np.concatenate([pw.elem, workloads._elem_of_uniform(pw.mesh, xi)]).astype(np.int32),
+                              "part_species": np.concatenate([pw.part_species, np.full(pw.n, 2, np.int32)])})
+    h = build_hdg_mesh(w.mesh)
+    sc = {"workload": "plasma wave 8^3 N=3, 200k e- + 200k ions, CVWM, TriaTracking, HDG every step "
+                      "(PrecondType 2, epsCG 1e-6 relative, warm start)", "particles": w.n}
+    for name, prec in (("fp64", capi.PIC_PREC_FP64), ("mixed", capi.PIC_PREC_MIXED)):
+        loop = ParticleLoop(w.config(precision=prec), w.mesh)
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+        loop.hdg_init(h, precond_type=2, eps_cg=1e-6, relative=True, max_iter_cg=5000, solve_in_step=True)
+        loop.time_step(w.dt, 3)
+        loop.synchronize()
+        loop.profile(True)
+        steps = 20
+        t0 = time.perf_counter()
+        loop.time_step(w.dt, steps)
+        loop.synchronize()
+        t = time.perf_counter() - t0
+        prof = loop.profile_read()
+        loop.profile(False)
+        sc[name] = {"particle_steps_per_s": w.n * steps / t, "ms_per_step": t * 1e3 / steps,
+                    "hdg_ms_per_step": prof["hdg"]["ms"] / steps}
+        loop.close()
+    out["self_consistent_plasma_wave"] = sc
+    return out
 
 
 def adjoint_timing():
@@ -556,7 +653,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="curved", choices=["curved", "plasma_wave", "batch"])
+    ap.add_argument("--workload", default="curved", choices=["curved", "plasma_wave", "batch", "hdg"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--sort-interval", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -577,6 +674,12 @@ def main():
     if args.workload == "batch":
         if rank == 0:
             run_batch(args)
+        return
+    if args.workload == "hdg":
+        # the HDG field solve alone (also the extras' "hdg" entry); --cells picks one mesh size
+        if rank == 0:
+            cells = (args.cells,) if args.cells else (8, 32)
+            print(json.dumps({"hdg": hdg_timing(cells=cells, self_consistent=not args.no_extras)}), flush=True)
         return
     run_gpu(args, rank, world, local_rank)
 

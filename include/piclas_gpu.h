@@ -36,7 +36,7 @@
  *                          (src/hdg/hdg.f90:734, hdg_linear.f90:37, src/hdg/hdg_tools.f90:41, elem_mat.f90:621);
  *                          with pic_hdg_t.solve_in_step, pic_step calls it after every Deposition
  *                          (timedisc_TimeStepPoissonByBorisLeapfrog.f90:99)
- *   pic_hdg_get_lambda / pic_hdg_get_elem_mat
+ *   pic_hdg_get_lambda / pic_hdg_set_lambda / pic_hdg_get_elem_mat
  *                          HDG_Surf_N(:)%lambda, HDG_Vol_N(e)%Ehat/InvDhat/Smat (src/hdg/hdg_vars.f90)
  *   pic_adjoint_run        no reference counterpart (differentiable loop, see its comment)
  *   pic_deposit_cvwm_noalloc, pic_profile*, pic_launch_count, pic_stream, pic_fp64_fma_rate
@@ -264,6 +264,9 @@ int pic_hdg_set_dirichlet(pic_ctx_t* ctx, const double* lambda_bc);
  * (U_N(e)%U(1,...), U_N(e)%E(1:3,...)) are copied to the host when non-NULL; status may be NULL. */
 int pic_hdg_solve(pic_ctx_t* ctx, const double* source, double* phi, double* e_field, pic_hdg_status_t* status);
 int pic_hdg_get_lambda(pic_ctx_t* ctx, double* lambda /* (nGP_face, nSides) */);
+/* lambda from a restart state (DG_SolutionLambda, src/restart/restart_field.f90:652-672): the start value
+ * of the next CG */
+int pic_hdg_set_lambda(pic_ctx_t* ctx, const double* lambda /* (nGP_face, nSides) */);
 /* Elem_Mat of one element (1-based): Ehat(nGP_face,nGP_vol,6), InvDhat(nGP_vol,nGP_vol), Smat(nGP_face,
  * nGP_face,6,6); any pointer may be NULL */
 int pic_hdg_get_elem_mat(pic_ctx_t* ctx, int32_t elem, double* ehat, double* inv_dhat, double* smat);

@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
                     "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data", "pic_fp64_fma_rate",
                     "pic_hdg_init", "pic_hdg_set_dirichlet", "pic_hdg_solve", "pic_hdg_get_lambda",
-                    "pic_hdg_get_elem_mat"]
+                    "pic_hdg_get_elem_mat", "pic_hdg_set_lambda"]
 
 
 class PicError(RuntimeError):
@@ -100,6 +100,7 @@ def load_library(build_if_missing: bool = False):
     L.pic_hdg_set_dirichlet.argtypes = [C.c_void_p, dp]
     L.pic_hdg_solve.argtypes = [C.c_void_p, dp, dp, dp, P(capi.PicHdgStatus)]
     L.pic_hdg_get_lambda.argtypes = [C.c_void_p, dp]
+    L.pic_hdg_set_lambda.argtypes = [C.c_void_p, dp]
     L.pic_hdg_get_elem_mat.argtypes = [C.c_void_p, C.c_int32, dp, dp, dp]
     _LIB = L
     return L
@@ -317,6 +318,12 @@ class ParticleLoop:
         lam = np.zeros((self.hdg_n_sides, nf))
         self._check(self.lib.pic_hdg_get_lambda(self.handle, capi.dptr(lam)), "pic_hdg_get_lambda")
         return lam
+
+    def hdg_set_lambda(self, lam: np.ndarray):
+        lm = np.ascontiguousarray(lam, dtype=np.float64)
+        if lm.size != self.hdg_n_sides * (self.N + 1) ** 2:
+            raise ValueError("lambda has the wrong size")
+        self._check(self.lib.pic_hdg_set_lambda(self.handle, capi.dptr(lm)), "pic_hdg_set_lambda")
 
     def hdg_elem_mat(self, elem: int):
         """(Ehat (6,nv,nf), InvDhat (nv,nv), Smat (6,6,nf,nf)) of 1-based element ``elem`` (C views of the

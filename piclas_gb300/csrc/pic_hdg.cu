@@ -53,7 +53,8 @@ struct Dev {
   const uint8_t* masked;   // [side] Dirichlet
   const double *mf, *mg, *mh, *sj, *tau;
   double *ehat, *invd, *smat, *pre;
-  double *lam, *rhs, *R, *V, *Z, *rhs_vol, *contrib, *U;
+  double* smat_u;           // [e][stride]: the 21 blocks Smat(:,:,i,j), i <= j
+  double *lam, *rhs, *R, *Pr, *Ax, *V0, *V1, *rhs_vol, *contrib, *U;
   double* red;             // partial sums, one per CTA of a side-DOF kernel
   double* sc;              // CG scalars
   int* flags;
@@ -446,22 +447,35 @@ __global__ void k_set_dirichlet(Dev H, const double* __restrict__ vals, const in
 }
 
 // ---------------------------------------------------------------------------------------------------
-// CG (hdg_tools.f90:41-234)
+// CG (hdg_tools.f90:41-234).  One iteration = three kernels:
+//   k_matvec   (per element) V_new = P^{-1}R + beta V_old for the element's sides (the master element
+//              of a side writes it), y = S V_new from the 21 stored blocks of Smat
+//   k_gather   (per side DOF) Ax = the two elements' y, masked; v.Ax -> omega
+//   k_update   lambda += omega V, R -= omega Ax, Pr = P^{-1} R; r.r and r.Pr -> convergence, beta
+// The reference's order (MatVec, omega, update, test, ApplyPrecond, beta, V = Z + beta V) is kept; the
+// V update just moves to the start of the next iteration.  Two V buffers alternate between iterations.
+// The matvec is bound by the FP64 pipe (GB300: about 2 FP64 lanes per clock and SM), so its products
+// are explicit fused multiply-adds (one instruction, one rounding) although the library is built
+// with -fmad=false; the CG is compared with the oracle within a tolerance, not bit for bit.
 // ---------------------------------------------------------------------------------------------------
 constexpr int kRedThreads = 256;
 
-// block sum of v, then the last CTA to arrive sums the partials in index order and runs fin(total)
+// block sums of (v0, v1), then the last CTA to arrive sums the partials in index order and runs fin
 template <class Fin>
-__device__ inline void reduce_and_finish(const Dev& H, double v, Fin fin) {
-  __shared__ double ws[kRedThreads / 32];
+__device__ inline void reduce_and_finish(const Dev& H, double v0, double v1, Fin fin) {
+  __shared__ double ws[2][kRedThreads / 32];
   __shared__ bool last;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_down_sync(0xffffffffu, v0, o);
+    v1 += __shfl_down_sync(0xffffffffu, v1, o);
+  }
+  if ((threadIdx.x & 31) == 0) { ws[0][threadIdx.x >> 5] = v0; ws[1][threadIdx.x >> 5] = v1; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += ws[w];
-    H.red[blockIdx.x] = s;
+    double s0 = 0.0, s1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { s0 += ws[0][w]; s1 += ws[1][w]; }
+    H.red[2 * blockIdx.x] = s0;
+    H.red[2 * blockIdx.x + 1] = s1;
     __threadfence();
     const int ticket = atomicAdd(&H.flags[F_TICKET], 1);
     last = (ticket == (int)gridDim.x - 1);
@@ -469,67 +483,140 @@ __device__ inline void reduce_and_finish(const Dev& H, double v, Fin fin) {
   __syncthreads();
   if (!last) return;
   __threadfence();
-  double s = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(H.red + b);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  double s0 = 0.0, s1 = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    s0 += __ldcg(H.red + 2 * b);
+    s1 += __ldcg(H.red + 2 * b + 1);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  if ((threadIdx.x & 31) == 0) { ws[0][threadIdx.x >> 5] = s0; ws[1][threadIdx.x >> 5] = s1; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double tot = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += ws[w];
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t0 += ws[0][w]; t1 += ws[1][w]; }
     H.flags[F_TICKET] = 0;
-    fin(tot);
+    fin(t0, t1);
   }
 }
 
-// Z = S x (per element): out[e][jl][a] = sum_loc Smat(a,:,jl,loc) x(side(e,loc))
-template <int ND>
-__global__ void __launch_bounds__(6 * ND * ND < 64 ? 64 : ((6 * ND * ND + 31) / 32) * 32)
-k_matvec(Dev H, const double* __restrict__ x) {
-  constexpr int nf = ND * ND;
-  if (__ldcg(&H.flags[F_DONE])) return;
-  __shared__ double xs[6 * nf];
-  const int e = blockIdx.x, tid = threadIdx.x;
-  for (int t = tid; t < 6 * nf; t += blockDim.x) {
-    const int loc = t / nf, b = t % nf;
-    xs[t] = x[(size_t)H.e2s[12 * e + 2 * loc] * nf + b];
-  }
-  __syncthreads();
-  if (tid >= 6 * nf) return;
-  const int jl = tid / nf, a = tid % nf;
+// upper block (i <= j) index in the packed Smat: (0,0) (0,1) .. (0,5) (1,1) .. (5,5)
+__host__ __device__ constexpr int upper_block(int i, int j) { return i * 6 - (i * (i - 1)) / 2 + (j - i); }
+
+// copy the 21 blocks Smat(:,:,i,j), i <= j, of every element to the packed array used by k_matvec
+__global__ void k_pack_upper(Dev H, int nf, size_t stride) {
+  const int e = blockIdx.x;
   const double* Sm = H.smat + (size_t)nf * nf * 36 * e;
-  double acc = 0.0;
-#pragma unroll
-  for (int loc = 0; loc < 6; ++loc) {
-    const double* blk = Sm + (size_t)nf * nf * (jl + 6 * loc) + a;
-#pragma unroll
-    for (int b = 0; b < nf; ++b) acc = acc + __ldcs(blk + nf * b) * xs[loc * nf + b];
+  for (int t = threadIdx.x; t < 21 * nf * nf; t += blockDim.x) {
+    const int blk = t / (nf * nf), ab = t % (nf * nf);
+    int i = 0;
+    while (upper_block(i, 5) < blk) ++i;
+    const int j = i + (blk - upper_block(i, i));
+    H.smat_u[stride * e + t] = Sm[ab + (size_t)nf * nf * (i + 6 * j)];
   }
-  H.contrib[((size_t)6 * e + jl) * nf + a] = acc;
 }
 
-// mode 0: EvalResidual (R = RHS - S lambda, |R|^2, start test); mode 1: Z = S V and v.z -> omega
-template <int MODE>
-__global__ void __launch_bounds__(kRedThreads) k_gather(Dev H, int nf) {
+template <int ND>
+__host__ __device__ constexpr int matvec_threads_t() { return ((21 * ND * ND + 31) / 32) * 32; }
+
+// y = S x per element.  UPDATE: x = V_new = Pr + beta V_old (the side's master element stores it in Vnew);
+// otherwise x = xin.  Shared memory: the 21 blocks (column stride nf+1), x of the 6 sides, row/col parts.
+template <int ND, bool UPDATE>
+__global__ void __launch_bounds__(matvec_threads_t<ND>()) k_matvec(Dev H, const double* __restrict__ xin,
+                                                                   const double* __restrict__ vold,
+                                                                   double* __restrict__ vnew, size_t stride) {
+  constexpr int nf = ND * ND, ld = nf + 1;
   if (__ldcg(&H.flags[F_DONE])) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  double v = 0.0;
-  if (t < H.ns * nf) {
-    const int sid = t / nf, a = t % nf;
-    double y = side_sum(H, H.contrib, sid, a, nf);
-    if (H.masked[sid] || (sid == H.zero_side && a == 0)) y = 0.0;
-    if (MODE == 0) {
-      double r = H.rhs[t] - y;
-      if (H.masked[sid] || (sid == H.zero_side && a == 0)) r = 0.0;
-      H.R[t] = r;
-      v = r * r;
-    } else {
-      H.Z[t] = y;
-      v = H.V[t] * y;
+  extern __shared__ double sm[];
+  double* Sb = sm;                       // [21][nf][ld]
+  double* xs = Sb + 21 * nf * ld;        // [6][nf]
+  double* pr = xs + 6 * nf;              // [21][nf] row parts
+  double* pc = pr + 21 * nf;             // [21][nf] column parts
+  const int e = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const double* src = H.smat_u + stride * e;
+  // every load of the thread issued before the first store: 16..25 independent loads in flight per thread
+  // (launched with exactly matvec_threads_t<ND>() threads)
+  constexpr int NT = matvec_threads_t<ND>(), TOT = 21 * nf * nf, PER = (TOT + NT - 1) / NT;
+  double v[PER];
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int t = tid + k * NT;
+    v[k] = t < TOT ? src[t] : 0.0;
+  }
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int t = tid + k * NT;
+    if (t < TOT) {
+      const int blk = t / (nf * nf), ab = t % (nf * nf);
+      Sb[blk * nf * ld + (ab / nf) * ld + ab % nf] = v[k];
     }
   }
-  reduce_and_finish(H, v, [&](double tot) {
+  const int* e2s = H.e2s + 12 * e;
+  for (int t = tid; t < 6 * nf; t += nt) {
+    const int loc = t / nf, b = t % nf;
+    const int sid = e2s[2 * loc];
+    const size_t g = (size_t)sid * nf + b;
+    double x;
+    if (UPDATE) {
+      x = __fma_rn(__ldcg(&H.sc[S_BETA]), vold[g], H.Pr[g]);
+      const int* se = H.s2e + 4 * sid;
+      if (se[0] == e && se[2] == loc) vnew[g] = x;
+    } else {
+      x = xin[g];
+    }
+    xs[t] = x;
+  }
+  __syncthreads();
+  if (tid < 21 * nf) {
+    const int blk = tid / nf, t = tid % nf;
+    int i = 0;
+    while (upper_block(i, 5) < blk) ++i;
+    const int j = i + (blk - upper_block(i, i));
+    const double* B = Sb + blk * nf * ld;
+    double r = 0.0;
+#pragma unroll
+    for (int b = 0; b < nf; ++b) r = __fma_rn(B[b * ld + t], xs[j * nf + b], r);
+    pr[blk * nf + t] = r;
+    if (i != j) {
+      double c = 0.0;
+#pragma unroll
+      for (int a = 0; a < nf; ++a) c = __fma_rn(B[t * ld + a], xs[i * nf + a], c);
+      pc[blk * nf + t] = c;
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < 6 * nf; t += nt) {
+    const int i = t / nf, a = t % nf;
+    double y = 0.0;
+    for (int j = 0; j < 6; ++j) y = y + (j >= i ? pr[upper_block(i, j) * nf + a] : pc[upper_block(j, i) * nf + a]);
+    H.contrib[((size_t)6 * e + i) * nf + a] = y;
+  }
+}
+
+// MODE 0: EvalResidual (R = RHS - S lambda, |R|^2, start test); MODE 1: Ax = S V and v.Ax -> omega
+template <int MODE>
+__global__ void __launch_bounds__(kRedThreads) k_gather(Dev H, const double* __restrict__ v, int nf) {
+  if (__ldcg(&H.flags[F_DONE])) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (t < H.ns * nf) {
+    const int sid = t / nf, a = t % nf;
+    const bool zero = H.masked[sid] || (sid == H.zero_side && a == 0);
+    double y = side_sum(H, H.contrib, sid, a, nf);
+    if (zero) y = 0.0;
+    if (MODE == 0) {
+      const double r = zero ? 0.0 : H.rhs[t] - y;
+      H.R[t] = r;
+      acc = r * r;
+    } else {
+      H.Ax[t] = y;
+      acc = v[t] * y;
+    }
+  }
+  reduce_and_finish(H, acc, 0.0, [&](double tot, double) {
     if (MODE == 0) {
       H.sc[S_RR] = tot;
       const double e2 = H.eps_cg * H.eps_cg;
@@ -544,79 +631,88 @@ __global__ void __launch_bounds__(kRedThreads) k_gather(Dev H, int nf) {
   });
 }
 
-// lambda += omega V, R -= omega Z, |R|^2 and the convergence test
-__global__ void __launch_bounds__(kRedThreads) k_update(Dev H, int nf) {
-  if (__ldcg(&H.flags[F_DONE])) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const double om = __ldcg(&H.sc[S_OMEGA]);
+// Pr = P^{-1} r for one side (ApplyPrecond), returns r.Pr over the side
+__device__ inline double apply_precond_side(const Dev& H, int sid, int nf, const double* r, double* o) {
   double v = 0.0;
-  if (t < H.ns * nf) {
-    H.lam[t] = H.lam[t] + om * H.V[t];
-    const double r = H.R[t] - om * H.Z[t];
-    H.R[t] = r;
-    v = r * r;
+  if (H.precond == 0) {
+    for (int a = 0; a < nf; ++a) { o[a] = r[a]; v += r[a] * r[a]; }
+  } else if (H.masked[sid]) {
+    for (int a = 0; a < nf; ++a) o[a] = 0.0;
+  } else if (H.precond == 2) {
+    const double* P = H.pre + (size_t)nf * sid;
+    for (int a = 0; a < nf; ++a) { o[a] = P[a] * r[a]; v += r[a] * o[a]; }
+  } else {
+    const double* U = H.pre + (size_t)nf * nf * sid;        // DPOTRS with the upper factor
+    double y[kMaxND * kMaxND];
+    for (int i = 0; i < nf; ++i) {
+      double t = r[i];
+      for (int k = 0; k < i; ++k) t = t - U[k + nf * i] * y[k];
+      y[i] = t / U[i + nf * i];
+    }
+    for (int i = nf - 1; i >= 0; --i) {
+      double t = y[i];
+      for (int k = i + 1; k < nf; ++k) t = t - U[i + nf * k] * y[k];
+      y[i] = t / U[i + nf * i];
+    }
+    for (int a = 0; a < nf; ++a) { o[a] = y[a]; v += r[a] * y[a]; }
   }
-  reduce_and_finish(H, v, [&](double tot) {
-    const int it = H.flags[F_ITER] + 1;
-    H.flags[F_ITER] = it;
-    H.sc[S_RR] = tot;
-    if (isnan(tot)) { H.flags[F_STATUS] |= ST_BREAKDOWN; H.flags[F_DONE] = 1; }
-    else if (tot < H.sc[S_ABORT2]) { H.flags[F_CONV] = 1; H.flags[F_DONE] = 1; }
-    else if (it >= H.max_iter) { H.flags[F_STATUS] |= ST_NOT_CONVERGED; H.flags[F_DONE] = 1; }
-  });
+  return v;
 }
 
-// OUT = P^{-1} R and r.OUT; FIRST: rz1 = r.v, else beta = rz2/rz1, rz1 = rz2
+// FIRST (after EvalResidual): Pr = P^{-1}R, rz1 = r.Pr, beta = 0.
+// Otherwise: lambda += omega V, R -= omega Ax, |R|^2 and the tests, Pr = P^{-1}R, beta = rz2/rz1.
+// PrecondType 1 runs one thread per side, the others one thread per side DOF.
 template <bool FIRST>
-__global__ void __launch_bounds__(kRedThreads) k_precond(Dev H, int nf) {
+__global__ void __launch_bounds__(kRedThreads) k_update(Dev H, const double* __restrict__ v, int nf) {
   if (__ldcg(&H.flags[F_DONE])) return;
-  double* out = FIRST ? H.V : H.Z;
-  double v = 0.0;
+  const double om = FIRST ? 0.0 : __ldcg(&H.sc[S_OMEGA]);
+  double rr = 0.0, rz = 0.0;
   if (H.precond == 1) {
-    // one thread per side: the two triangular solves with the stored upper factor (DPOTRS)
     const int sid = blockIdx.x * blockDim.x + threadIdx.x;
     if (sid < H.ns) {
-      const double* r = H.R + (size_t)nf * sid;
-      double* o = out + (size_t)nf * sid;
-      if (H.masked[sid]) {
-        for (int a = 0; a < nf; ++a) o[a] = 0.0;
-      } else {
-        const double* U = H.pre + (size_t)nf * nf * sid;
-        double y[kMaxND * kMaxND];
-        for (int i = 0; i < nf; ++i) {
-          double t = r[i];
-          for (int k = 0; k < i; ++k) t = t - U[k + nf * i] * y[k];
-          y[i] = t / U[i + nf * i];
+      double r[kMaxND * kMaxND];
+      for (int a = 0; a < nf; ++a) {
+        const size_t g = (size_t)sid * nf + a;
+        if (!FIRST) {
+          H.lam[g] = H.lam[g] + om * v[g];
+          H.R[g] = H.R[g] - om * H.Ax[g];
         }
-        for (int i = nf - 1; i >= 0; --i) {
-          double t = y[i];
-          for (int k = i + 1; k < nf; ++k) t = t - U[i + nf * k] * y[k];
-          y[i] = t / U[i + nf * i];
-        }
-        for (int a = 0; a < nf; ++a) { o[a] = y[a]; v += r[a] * y[a]; }
+        r[a] = H.R[g];
+        rr += r[a] * r[a];
       }
+      rz = apply_precond_side(H, sid, nf, r, H.Pr + (size_t)sid * nf);
     }
   } else {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < H.ns * nf) {
-      const double r = H.R[t];
+      double r = H.R[t];
+      if (!FIRST) {
+        H.lam[t] = H.lam[t] + om * v[t];
+        r = r - om * H.Ax[t];
+        H.R[t] = r;
+      }
       double z = r;
       if (H.precond == 2) z = H.masked[t / nf] ? 0.0 : H.pre[t] * r;
-      out[t] = z;
-      v = r * z;
+      H.Pr[t] = z;
+      rr = r * r;
+      rz = r * z;
     }
   }
-  reduce_and_finish(H, v, [&](double tot) {
-    if (FIRST) H.sc[S_RZ1] = tot;
-    else { H.sc[S_BETA] = tot / H.sc[S_RZ1]; H.sc[S_RZ1] = tot; }
+  reduce_and_finish(H, rr, rz, [&](double trr, double trz) {
+    if (FIRST) {
+      H.sc[S_RZ1] = trz;
+      H.sc[S_BETA] = 0.0;
+      return;
+    }
+    const int it = H.flags[F_ITER] + 1;
+    H.flags[F_ITER] = it;
+    H.sc[S_RR] = trr;
+    if (isnan(trr)) { H.flags[F_STATUS] |= ST_BREAKDOWN; H.flags[F_DONE] = 1; return; }
+    if (trr < H.sc[S_ABORT2]) { H.flags[F_CONV] = 1; H.flags[F_DONE] = 1; return; }
+    if (it >= H.max_iter) { H.flags[F_STATUS] |= ST_NOT_CONVERGED; H.flags[F_DONE] = 1; return; }
+    H.sc[S_BETA] = trz / H.sc[S_RZ1];
+    H.sc[S_RZ1] = trz;
   });
-}
-
-__global__ void k_vupdate(Dev H, int nf) {
-  if (__ldcg(&H.flags[F_DONE])) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const double be = __ldcg(&H.sc[S_BETA]);
-  if (t < H.ns * nf) H.V[t] = H.Z[t] + be * H.V[t];
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -700,6 +796,7 @@ struct HdgState {
   int red_blocks = 0;
   cudaGraphExec_t chunk = nullptr;
   int chunk_iters = 0;
+  size_t upper_stride = 0;        // doubles per element in the packed Smat
   pic_hdg_status_t status{};
   std::vector<double> tau;
 };
@@ -741,31 +838,39 @@ void make_tabs(int N, const double* xgp, const double* wgp, Tabs& T) {
   }
 }
 
-int launch_chunk(HdgState* h, cudaStream_t s, int iters);
-
 #define HDG_DISPATCH(ND_, CALL) \
   switch (ND_) { case 2: { constexpr int ND = 2; CALL; } break; case 3: { constexpr int ND = 3; CALL; } break; \
                  case 4: { constexpr int ND = 4; CALL; } break; case 5: { constexpr int ND = 5; CALL; } break; default: break; }
 
 int side_blocks(const HdgState* h) { return (h->D.ns * h->nf + kRedThreads - 1) / kRedThreads; }
-int precond_blocks(const HdgState* h) {
+int update_blocks(const HdgState* h) {
   return h->D.precond == 1 ? (h->D.ns + kRedThreads - 1) / kRedThreads : side_blocks(h);
 }
-int matvec_threads(int nf) { int t = ((6 * nf + 31) / 32) * 32; return t < 64 ? 64 : t; }
+template <int ND>
+size_t matvec_smem() { constexpr int nf = ND * ND; return sizeof(double) * (21 * nf * (nf + 1) + 6 * nf + 42 * nf); }
+template <int ND>
+cudaError_t set_matvec_smem() {
+  cudaError_t e = cudaFuncSetAttribute(k_matvec<ND, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)matvec_smem<ND>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_matvec<ND, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)matvec_smem<ND>());
+  return e;
+}
 
-int launch_iteration(HdgState* h, cudaStream_t s) {
+// CG iteration `parity`: V_old = V[parity], V_new = V[1 - parity]
+int launch_iteration(HdgState* h, cudaStream_t s, int parity) {
   const int nf = h->nf;
-  HDG_DISPATCH(h->nd, (k_matvec<ND><<<h->D.ne, matvec_threads(nf), 0, s>>>(h->D, h->D.V)));
-  k_gather<1><<<side_blocks(h), kRedThreads, 0, s>>>(h->D, nf);
-  k_update<<<side_blocks(h), kRedThreads, 0, s>>>(h->D, nf);
-  k_precond<false><<<precond_blocks(h), kRedThreads, 0, s>>>(h->D, nf);
-  k_vupdate<<<side_blocks(h), kRedThreads, 0, s>>>(h->D, nf);
-  return 5;
+  double* vold = parity ? h->D.V1 : h->D.V0;
+  double* vnew = parity ? h->D.V0 : h->D.V1;
+  HDG_DISPATCH(h->nd, (k_matvec<ND, true><<<h->D.ne, matvec_threads_t<ND>(), matvec_smem<ND>(), s>>>(
+                           h->D, nullptr, vold, vnew, h->upper_stride)));
+  k_gather<1><<<side_blocks(h), kRedThreads, 0, s>>>(h->D, vnew, nf);
+  k_update<false><<<update_blocks(h), kRedThreads, 0, s>>>(h->D, vnew, nf);
+  return 3;
 }
 
 int launch_chunk(HdgState* h, cudaStream_t s, int iters) {
   int n = 0;
-  for (int i = 0; i < iters; ++i) n += launch_iteration(h, s);
+  for (int i = 0; i < iters; ++i) n += launch_iteration(h, s, i & 1);
   return n;
 }
 
@@ -867,13 +972,17 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
   rc = rc ? rc : c->alloc(&D.lam, nsf);
   rc = rc ? rc : c->alloc(&D.rhs, nsf);
   rc = rc ? rc : c->alloc(&D.R, nsf);
-  rc = rc ? rc : c->alloc(&D.V, nsf);
-  rc = rc ? rc : c->alloc(&D.Z, nsf);
+  rc = rc ? rc : c->alloc(&D.Pr, nsf);
+  rc = rc ? rc : c->alloc(&D.Ax, nsf);
+  rc = rc ? rc : c->alloc(&D.V0, nsf);
+  rc = rc ? rc : c->alloc(&D.V1, nsf);
+  h->upper_stride = ((size_t)21 * nf * nf + 1) / 2 * 2;
+  rc = rc ? rc : c->alloc(&D.smat_u, h->upper_stride * ne);
   rc = rc ? rc : c->alloc(&D.rhs_vol, (size_t)nv * ne);
   rc = rc ? rc : c->alloc(&D.contrib, (size_t)6 * nf * ne);
   rc = rc ? rc : c->alloc(&D.U, (size_t)nv * ne);
   const int nred = std::max((int)((nsf + kRedThreads - 1) / kRedThreads), 1);
-  rc = rc ? rc : c->alloc(&D.red, (size_t)nred);
+  rc = rc ? rc : c->alloc(&D.red, (size_t)2 * nred);
   rc = rc ? rc : c->alloc(&D.sc, 8);
   rc = rc ? rc : c->alloc(&D.flags, 8);
   if (g->n_dirichlet > 0) {
@@ -898,7 +1007,8 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
     CUDA_CHECK_HDG(cudaMemsetAsync(h->dir_vals, 0, sizeof(double) * nf * (size_t)g->n_dirichlet, s));
   }
   CUDA_CHECK_HDG(cudaMemsetAsync(D.lam, 0, sizeof(double) * nsf, s));
-  CUDA_CHECK_HDG(cudaMemsetAsync(D.V, 0, sizeof(double) * nsf, s));
+  CUDA_CHECK_HDG(cudaMemsetAsync(D.V0, 0, sizeof(double) * nsf, s));
+  CUDA_CHECK_HDG(cudaMemsetAsync(D.V1, 0, sizeof(double) * nsf, s));
   CUDA_CHECK_HDG(cudaMemsetAsync(D.flags, 0, sizeof(int) * 8, s));
   CUDA_CHECK_HDG(cudaMemsetAsync(D.sc, 0, sizeof(double) * 8, s));
   D.e2s = d_e2s; D.s2e = d_s2e; D.masked = d_mask; D.mf = mf; D.mg = mg; D.mh = mh; D.sj = sj; D.tau = tau;
@@ -910,7 +1020,14 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
   CUDA_CHECK_HDG(cudaGetLastError());
   k_build_precond<<<(ns + 127) / 128, 128, 0, s>>>(D, nf);
   CUDA_CHECK_HDG(cudaGetLastError());
-  c->launches += 2;
+  k_pack_upper<<<ne, 256, 0, s>>>(D, nf, h->upper_stride);
+  CUDA_CHECK_HDG(cudaGetLastError());
+  c->launches += 3;
+  {
+    cudaError_t ea = cudaSuccess;
+    HDG_DISPATCH(nd, (ea = set_matvec_smem<ND>()));
+    CUDA_CHECK_HDG(ea);
+  }
   int fl[8];
   CUDA_CHECK_HDG(cudaMemcpyAsync(fl, D.flags, sizeof(fl), cudaMemcpyDeviceToHost, s));
   CUDA_CHECK_HDG(cudaStreamSynchronize(s));
@@ -963,15 +1080,17 @@ int hdg_solve_device(pic_ctx_t* c, const double* ps_dev, const double* resu_host
   HDG_DISPATCH(h->nd, (k_rhs<ND><<<D.ne, 128, 0, s>>>(D, h->T, ps_dev, resu_dev))); ++n;
   k_rhs_face<<<(D.ns * nf + 255) / 256, 256, 0, s>>>(D, nf); ++n;
   cudaMemsetAsync(D.flags, 0, sizeof(int) * 8, s);
-  HDG_DISPATCH(h->nd, (k_matvec<ND><<<D.ne, matvec_threads(nf), 0, s>>>(D, D.lam))); ++n;
-  k_gather<0><<<side_blocks(h), kRedThreads, 0, s>>>(D, nf); ++n;
-  k_precond<true><<<precond_blocks(h), kRedThreads, 0, s>>>(D, nf); ++n;
+  cudaMemsetAsync(D.V0, 0, sizeof(double) * (size_t)D.ns * nf, s);    // V_old of the first iteration
+  HDG_DISPATCH(h->nd, (k_matvec<ND, false><<<D.ne, matvec_threads_t<ND>(), matvec_smem<ND>(), s>>>(
+                           D, D.lam, nullptr, nullptr, h->upper_stride))); ++n;
+  k_gather<0><<<side_blocks(h), kRedThreads, 0, s>>>(D, nullptr, nf); ++n;
+  k_update<true><<<update_blocks(h), kRedThreads, 0, s>>>(D, nullptr, nf); ++n;
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
   int fl[8] = {0};
   const int max_chunks = (D.max_iter + h->chunk_iters - 1) / h->chunk_iters + 1;
   for (int ch = 0; ch < max_chunks; ++ch) {
-    if (h->chunk) { err = cudaGraphLaunch(h->chunk, s); n += 5 * h->chunk_iters; }
+    if (h->chunk) { err = cudaGraphLaunch(h->chunk, s); n += 3 * h->chunk_iters; }
     else n += launch_chunk(h, s, h->chunk_iters);
     if (err == cudaSuccess) err = cudaMemcpyAsync(fl, D.flags, sizeof(fl), cudaMemcpyDeviceToHost, s);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
@@ -1030,6 +1149,17 @@ extern "C" int pic_hdg_get_lambda(pic_ctx_t* c, double* lambda) {
   if (!h) return fail(PIC_ERR_STATE, "pic_hdg_init first");
   cudaError_t err = cudaMemcpyAsync(lambda, h->D.lam, sizeof(double) * h->nf * (size_t)h->D.ns,
                                     cudaMemcpyDeviceToHost, c->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+  if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
+  return PIC_OK;
+}
+
+extern "C" int pic_hdg_set_lambda(pic_ctx_t* c, const double* lambda) {
+  if (!c || !lambda) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  HdgState* h = c->hdg;
+  if (!h) return fail(PIC_ERR_STATE, "pic_hdg_init first");
+  cudaError_t err = cudaMemcpyAsync(h->D.lam, lambda, sizeof(double) * h->nf * (size_t)h->D.ns,
+                                    cudaMemcpyHostToDevice, c->stream);
   if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
   if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
   return PIC_OK;

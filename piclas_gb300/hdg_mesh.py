@@ -61,15 +61,17 @@ def _face_xi(N: int, xgp, s: int, p: int, q: int):
             (xgp[N - p], 1.0, xgp[q]), (-1.0, xgp[q], xgp[p]), (xgp[p], xgp[q], 1.0)][s]
 
 
-def _map(mesh: BoxMesh, e: int, xi):
+def _map(mesh: BoxMesh, elems: np.ndarray, xi):
+    """x(xi) of the trilinear map of every element in ``elems`` (0-based), shape (len, 3)."""
     La = lagrange_polys(float(xi[0]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
     Lb = lagrange_polys(float(xi[1]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
     Lc = lagrange_polys(float(xi[2]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
-    x = np.zeros(3)
+    xc = mesh.xcl_ngeo[elems]
+    x = np.zeros((len(elems), 3))
     for c in range(2):
         for b in range(2):
             for a in range(2):
-                x = x + mesh.xcl_ngeo[e, c, b, a] * La[a] * Lb[b] * Lc[c]
+                x = x + xc[:, c, b, a] * (La[a] * Lb[b] * Lc[c])
     return x
 
 
@@ -142,24 +144,27 @@ def build_hdg_mesh(mesh: BoxMesh, field_bc=None) -> HdgMesh:
                 owners[sid].append((e, s, int(mesh.side_flip[e, s])))
     n_sides = len(owners)
 
-    # geometric check of the slave flips: master point (p,q) == slave point Flip_S2M^-1 (+ periodic shift)
+    # geometric check of the slave flips: the master point (p,q) is the slave point Flip_S2M^-1(p,q)
+    # (every flip is its own inverse), up to a periodic shift; checked at the four corners of each side
     pv = mesh.periodic_vectors
     shifts = [np.zeros(3)] + [sg * pv[:, k] for k in range(pv.shape[1]) for sg in (1.0, -1.0)]
-    for sid in range(n_sides):
-        if len(owners[sid]) < 2:
-            continue
-        (em, sm, _), (es, ss, fl) = owners[sid]
+    pairs = [(sid, o[0][0], o[0][1], o[1][0], o[1][1], o[1][2]) for sid, o in enumerate(owners) if len(o) > 1]
+    groups = {}
+    for sid, em, sm, es, ss, fl in pairs:
+        groups.setdefault((sm, ss, fl), []).append((em, es))
+    tol = 1e-12 * max(1.0, float(np.abs(mesh.node_coords).max()))
+    for (sm, ss, fl), lst in groups.items():
+        em = np.array([a for a, _ in lst])
+        es = np.array([b for _, b in lst])
         for q in (0, N):
             for p in (0, N):
+                ps, qs = flip_s2m(N, p, q, fl)
                 xm = _map(mesh, em, _face_xi(N, mesh.xgp, sm, p, q))
-                ok = False
-                for ps in range(nd):
-                    for qs in range(nd):
-                        if flip_s2m(N, ps, qs, fl) == (p, q):
-                            xs = _map(mesh, es, _face_xi(N, mesh.xgp, ss, ps, qs))
-                            ok = any(np.allclose(xm, xs + sh, rtol=0, atol=1e-12 * max(1.0, np.abs(xm).max()))
-                                     for sh in shifts)
-                assert ok, f"side {sid}: flip {fl} does not map the slave face onto the master face"
+                xs = _map(mesh, es, _face_xi(N, mesh.xgp, ss, ps, qs))
+                ok = np.zeros(len(lst), dtype=bool)
+                for sh in shifts:
+                    ok |= np.all(np.abs(xm - xs - sh) <= tol, axis=1)
+                assert ok.all(), f"flip {fl} does not map the slave face onto the master face (sides {sm},{ss})"
 
     e2s = np.zeros((ne, 6, 2), dtype=np.int32)
     s2e = -np.ones((n_sides, 5), dtype=np.int32)
@@ -178,11 +183,15 @@ def build_hdg_mesh(mesh: BoxMesh, field_bc=None) -> HdgMesh:
 
     f, g, h = metric_terms(mesh)
     face = np.zeros((n_sides, nd, nd, 3))
-    for sid, own in enumerate(owners):
-        em, sm, _ = own[0]
+    master_e = np.array([o[0][0] for o in owners])
+    master_s = np.array([o[0][1] for o in owners])
+    for sm in range(6):
+        sel = np.nonzero(master_s == sm)[0]
+        if len(sel) == 0:
+            continue
         for q in range(nd):
             for p in range(nd):
-                face[sid, q, p] = _map(mesh, em, _face_xi(N, mesh.xgp, sm, p, q))
+                face[sel, q, p] = _map(mesh, master_e[sel], _face_xi(N, mesh.xgp, sm, p, q))
     dirichlet = np.array([sid + 1 for sid in range(n_sides) if bc_kind[sid] == "dirichlet"], dtype=np.int32)
     neumann = np.array([sid + 1 for sid in range(n_sides) if bc_kind[sid] == "neumann"], dtype=np.int32)
     return HdgMesh(n_sides=n_sides, elem_to_side=e2s, side_to_elem=s2e,
