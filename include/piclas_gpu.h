@@ -159,6 +159,17 @@ typedef struct pic_mesh_t {
   /* shape_function_adaptive: SFElemr2_Shared(1,nElems), the shape-function radius of each element
    * (InitShapeFunctionAdaptive, pic_depo.f90:727-815); NULL otherwise */
   const double* sf_elem_radius;
+  /* RefTracking on meshes whose boundaries are all open/reflective walls (no periodic vectors): the
+   * BC-element lists of BuildBCElemDistance (particle_mesh_build.f90:645-1092).  elem_to_bc_sides(1:2,
+   * nElems) = (ELEM_NBR_BCSIDES, ELEM_FIRST_BCSIDE): the number of wall sides in reach of the element and
+   * the 0-based first entry, -1/-1 for none; entry k (sorted by distance within an element) is the wall
+   * side bc_side_elem_loc(1:2,k) = (element 1-based, local side 1..6) with SideBCMetrics(BCSIDE_DISTANCE)
+   * = bc_side_distance(k).  Wall sides must be planar rectangles (SideType PLANAR_RECT).  NULL/0 for
+   * TriaTracking or periodic meshes. */
+  int32_t n_bc_entries;
+  const int32_t* elem_to_bc_sides;
+  const int32_t* bc_side_elem_loc;
+  const double* bc_side_distance;
 } pic_mesh_t;
 
 typedef struct pic_status_t {

@@ -566,14 +566,176 @@ static double maxabs3(const double v[3]) { return fmax(fabs(v[0]), fmax(fabs(v[1
 
 static int almost_equal(double x, double y) { return fabs(x - y) <= fmax(fabs(x), fabs(y)) * 4.441e-16; }
 
-static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, int ip,
-                             int64_t* ntol) {
+/* ---- RefTracking with walls (meshes without periodic vectors) ----------------------------------------
+ * Wall side geometry of a planar rectangular side: BezierControlPoints3D at NGeo = 1 (the corner nodes in
+ * CGNS side order, particle_mesh_tools.f90:1748-1773), BaseVectors0-2 (particle_mesh_build.f90:1916-1925),
+ * SideNormVec / SideDistance oriented away from the element (particle_mesh_tools.f90:1011-1048). */
+typedef struct { double bv0[3], bv1[3], bv2[3], n[3], dist; int bc; } orc_bc_side_t;
+
+static void side_corner(const pic_mesh_t* m, int e, int s, int p, int q, double out[3]) {
+  int a, b, c;
+  switch (s) {
+    case 0: a = q; b = p; c = 0; break;
+    case 1: a = p; b = 0; c = q; break;
+    case 2: a = 1; b = p; c = q; break;
+    case 3: a = 1 - p; b = 1; c = q; break;
+    case 4: a = 0; b = q; c = p; break;
+    default: a = p; b = q; c = 1; break;
+  }
+  const double* X = m->xcl_ngeo + ((((size_t)e * 2 + c) * 2 + b) * 2 + a) * 3;
+  out[0] = X[0]; out[1] = X[1]; out[2] = X[2];
+}
+
+static void unit3(const double v[3], double u[3]) {
+  double l = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  if (fabs(l) > 0.0) { l = 1.0 / l; u[0] = v[0] * l; u[1] = v[1] * l; u[2] = v[2] * l; }
+  else { u[0] = u[1] = u[2] = 0.0; }
+}
+
+/* 0: planar rectangle (SideType PLANAR_RECT); 1 otherwise */
+static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t* g) {
+  double P00[3], P10[3], P01[3], P11[3];
+  side_corner(m, e, s, 0, 0, P00); side_corner(m, e, s, 1, 0, P10);
+  side_corner(m, e, s, 0, 1, P01); side_corner(m, e, s, 1, 1, P11);
+  double ctr[3];
+  for (int c = 0; c < 3; ++c) {
+    g->bv0[c] = ((+P00[c] + P10[c]) + P01[c]) + P11[c];
+    g->bv1[c] = ((-P00[c] + P10[c]) - P01[c]) + P11[c];
+    g->bv2[c] = ((-P00[c] - P10[c]) + P01[c]) + P11[c];
+    ctr[c] = 0.25 * (((P00[c] + P10[c]) + P01[c]) + P11[c]);
+  }
+  const double* v1 = g->bv1;
+  const double* v2 = g->bv2;
+  double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+  double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  for (int c = 0; c < 3; ++c) n[c] = n[c] / len;
+  const double* bary = &m->elem_bary[(size_t)e * 3];
+  double vb[3] = {ctr[0] - bary[0], ctr[1] - bary[1], ctr[2] - bary[2]};
+  if (vb[0] * n[0] + vb[1] * n[1] + vb[2] * n[2] < 0.0) for (int c = 0; c < 3; ++c) n[c] = -n[c];
+  for (int c = 0; c < 3; ++c) g->n[c] = n[c];
+  g->dist = ctr[0] * n[0] + ctr[1] * n[1] + ctr[2] * n[2];
+  g->bc = m->side_bc ? m->side_bc[(size_t)e * 6 + s] : 0;
+  /* planar: every corner on the plane; rectangular: the checks of particle_mesh_tools.f90:1026-1041 */
+  const double* Pc[4] = {P00, P10, P01, P11};
+  double scale = sqrt(g->bv1[0] * g->bv1[0] + g->bv1[1] * g->bv1[1] + g->bv1[2] * g->bv1[2]);
+  for (int k = 0; k < 4; ++k)
+    if (fabs(Pc[k][0] * n[0] + Pc[k][1] * n[1] + Pc[k][2] * n[2] - g->dist) > 1e-12 * scale) return 1;
+  double d1[3], d2[3], d3[3], d4[3], u1[3], u2[3], u3[3], u4[3];
+  for (int c = 0; c < 3; ++c) { d1[c] = P01[c] - P00[c]; d2[c] = P10[c] - P00[c]; d3[c] = P11[c] - P01[c]; d4[c] = P11[c] - P10[c]; }
+  unit3(d1, u1); unit3(d2, u2); unit3(d3, u3); unit3(d4, u4);
+#define DOT3(a, b) ((a)[0] * (b)[0] + (a)[1] * (b)[1] + (a)[2] * (b)[2])
+  if (!(fabs(DOT3(u1, u2)) <= 2.22e-16) || !(fabs(DOT3(u1, u3)) <= 2.22e-16)) return 1;
+  if (!(fabs(DOT3(u4, u2)) <= 2.22e-16) || !(fabs(DOT3(u4, u3)) <= 2.22e-16)) return 1;
+#undef DOT3
+  return 0;
+}
+
+/* ComputePlanarRectIntersection, particle_intersection.f90:515-684 (flip = 0: wall sides are masters);
+ * returns alpha or -1 */
+static double planar_rect_alpha(const orc_bc_side_t* g, const double xl[3], const double traj[3], double len) {
+  const double* n = g->n;
+  double coeffA = n[0] * traj[0] + n[1] * traj[1] + n[2] * traj[2];
+  if (fabs(coeffA) <= 2.22e-16) return -1.0;                       /* parallel to the side */
+  double locSideDistance = g->dist - (xl[0] * n[0] + xl[1] * n[1] + xl[2] * n[2]);
+  double alpha = locSideDistance / coeffA;
+  if (locSideDistance < -100.0 * EPS_MACH) return -1.0;
+  double alphaNorm = alpha / len;
+  if (alphaNorm > 1.0 || alphaNorm < -(100.0 * EPS_MACH)) return -1.0;   /* epsilontol = 100 epsMach */
+  double P0[3], P1[3], P2[3];
+  for (int c = 0; c < 3; ++c) {
+    double inter = xl[c] + alpha * traj[c];
+    P0[c] = -0.25 * g->bv0[c] + inter;
+    P1[c] = 0.25 * g->bv1[c];
+    P2[c] = 0.25 * g->bv2[c];
+  }
+  double A1 = P1[0] * P1[0] + P1[1] * P1[1] + P1[2] * P1[2];
+  double B1 = P2[0] * P1[0] + P2[1] * P1[1] + P2[2] * P1[2];
+  double C1 = P1[0] * P0[0] + P1[1] * P0[1] + P1[2] * P0[2];
+  double A2 = B1;
+  double B2 = P2[0] * P2[0] + P2[1] * P2[1] + P2[2] * P2[2];
+  double C2 = P2[0] * P0[0] + P2[1] * P0[1] + P2[2] * P0[2];
+  double sdet = A1 * B2 - A2 * B1;
+  if (fabs(sdet) == 0.0) return -1.0;                              /* the reference aborts */
+  sdet = 1.0 / sdet;
+  const double epsLoc = 1.0 + 100.0 * EPS_MACH;
+  double xi = (B2 * C1 - B1 * C2) * sdet;
+  if (fabs(xi) > epsLoc) return -1.0;
+  double eta = (-A2 * C1 + A1 * C2) * sdet;
+  if (fabs(eta) > epsLoc) return -1.0;
+  return alpha;
+}
+
+#define ORC_BC_CAP 32   /* wall sides within reach of one trajectory; more are not traced (same cap on the GPU) */
+
+/* ParticleBCTracking, particle_reftracking.f90:417-694, for wall sides only (the element never changes):
+ * returns 1 when the particle is done -- it has not moved (PARTHASMOVED) or an open wall removed it */
+static int bc_tracking(const pic_mesh_t* m, const orc_bc_side_t* geo, int elem, double x[3], double xl[3],
+                       double v[3], uint8_t* inside, double* len0, int64_t* ncap) {
+  const int e = elem - 1;
+  const int nloc = m->elem_to_bc_sides[2 * e], first = m->elem_to_bc_sides[2 * e + 1];
+  double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
+  double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+  if (fabs(len / m->elem_radius[e]) <= 2.22e-16) return 1;
+  for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+  *len0 = fmax(*len0, len);
+  int doubleCheck = 0;
+  for (int loop = 0; loop < ORC_MAX_TRACK_LOOPS; ++loop) {
+    double alpha[ORC_BC_CAP];
+    int list[ORC_BC_CAP];
+    int nc = 0, nInter = 0;
+    for (int i = 0; i < nloc; ++i) {
+      if (m->bc_side_distance[first + i] > *len0) break;
+      if (nc == ORC_BC_CAP) { (*ncap)++; break; }
+      alpha[nc] = planar_rect_alpha(&geo[first + i], xl, traj, len);
+      list[nc] = i;
+      if (alpha[nc] > -1.0) nInter++;
+      nc++;
+    }
+    if (nInter == 0) return 0;
+    for (int i = 1; i < nc; ++i) {              /* InsertionSort (stable) */
+      double t = alpha[i];
+      int ti = list[i], j = i - 1;
+      while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; j--; }
+      alpha[j + 1] = t; list[j + 1] = ti;
+    }
+    int reflected = 0;
+    for (int k = 0; k < nc; ++k) {
+      if (!(alpha[k] > -1.0)) continue;
+      const orc_bc_side_t* g = &geo[first + list[k]];
+      /* GetBoundaryInteraction (particle_boundary_condition.f90:35-221), REFMAPPING branch */
+      if (g->n[0] * traj[0] + g->n[1] * traj[1] + g->n[2] * traj[2] <= 0.0) { reflected = 0; continue; }
+      reflected = 1;
+      if (g->bc == 1) { *inside = 0; break; }                  /* RemoveParticle */
+      perfect_reflection(v, x, xl, traj, len, alpha[k], g->n);
+      for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
+      len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+      if (fabs(len) <= 2.22e-16) len = 0.0;
+      else for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+      break;
+    }
+    if (!*inside) return 1;
+    if (!reflected) {
+      if (!doubleCheck) doubleCheck = 1;
+      else return 0;
+    }
+  }
+  return 0;
+}
+
+static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, const orc_bc_side_t* geo,
+                             orc_particles_t* p, int ip, int64_t* ntol, int64_t* nhop) {
   double* x = &p->part_state[(size_t)ip * 6];
+  double* v = x + 3;
   double* xl = &p->last_part_pos[(size_t)ip * 3];
   double* xi = &p->part_pos_ref[(size_t)ip * 3];
   int elem = p->last_elem[ip];
-  /* no BC elements on a CartesianPeriodic box: PeriodicMovement until the position is stable */
-  if (m->n_periodic_vectors > 0) {
+  if (geo && m->elem_to_bc_sides[2 * (elem - 1)] > 0) {
+    /* BC element (particle_reftracking.f90:98-126) */
+    double len0 = 0.0;
+    if (bc_tracking(m, geo, elem, x, xl, v, &p->inside[ip], &len0, nhop)) { p->elem[ip] = elem; return; }
+    orc_get_position_in_ref_elem(cfg, m, x, xi, elem, 0);
+    if (maxabs3(xi) < 1.0) { p->elem[ip] = elem; return; }
+  } else if (m->n_periodic_vectors > 0) {
     double lp[3] = {x[0], x[1], x[2]};
     periodic_movement_fast(m, x, xl);
     int guard = 0;
@@ -583,8 +745,10 @@ static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, orc_p
       guard++;
     }
   }
-  orc_get_position_in_ref_elem(cfg, m, x, xi, elem, 0);
-  if (maxabs3(xi) < 1.0) { p->elem[ip] = elem; return; }
+  if (!(geo && m->elem_to_bc_sides[2 * (elem - 1)] > 0)) {
+    orc_get_position_in_ref_elem(cfg, m, x, xi, elem, 0);
+    if (maxabs3(xi) < 1.0) { p->elem[ip] = elem; return; }
+  }
   int oldElem = p->last_elem[ip];
   int cell[3];
   for (int d = 0; d < 3; ++d) {
@@ -646,11 +810,32 @@ static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, orc_p
   }
   int te = p->elem[ip];
   double epsElement = (te >= 1) ? m->eps_one_cell[te - 1] : 1.0;
-  if (te < 1 || maxabs3(xi) > epsElement) (*ntol)++;   /* the reference aborts here (internal element) */
+  if (te < 1 || maxabs3(xi) > epsElement) {
+    if (te >= 1 && geo && m->elem_to_bc_sides[2 * (te - 1)] > 0) {
+      /* BC element (particle_reftracking.f90:327-403): trace the walls again from TestElem */
+      double len0 = 0.0;
+      if (bc_tracking(m, geo, te, x, xl, v, &p->inside[ip], &len0, nhop)) return;
+      orc_get_position_in_ref_elem(cfg, m, x, xi, te, 0);
+      /* beyond epsOneCell the reference calls LocateParticleInElement and aborts when that fails */
+      if (maxabs3(xi) > m->eps_one_cell[te - 1]) (*ntol)++;
+    } else {
+      (*ntol)++;                                 /* the reference aborts here (internal element) */
+    }
+  }
+}
+
+/* the wall geometry of every BC entry, or NULL without RefTracking walls */
+static orc_bc_side_t* bc_geometry(const pic_mesh_t* m) {
+  if (!m->elem_to_bc_sides || m->n_bc_entries <= 0) return NULL;
+  orc_bc_side_t* geo = (orc_bc_side_t*)malloc(sizeof(orc_bc_side_t) * (size_t)m->n_bc_entries);
+  for (int k = 0; k < m->n_bc_entries; ++k)
+    orc_bc_side_geometry(m, m->bc_side_elem_loc[2 * k] - 1, m->bc_side_elem_loc[2 * k + 1] - 1, &geo[k]);
+  return geo;
 }
 
 void orc_track(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, orc_counters_t* c, int nthreads) {
   int64_t nlost = 0, nhop = 0, ntol = 0;
+  orc_bc_side_t* geo = cfg->tracking == PIC_TRACK_REFMAPPING ? bc_geometry(m) : NULL;
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) reduction(+ : nlost, nhop, ntol) schedule(static)
 #endif
@@ -660,9 +845,10 @@ void orc_track(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p,
       if (p->last_elem[ip] == 0) continue;    /* particle_triatracking.f90:101 */
       tria_track_single(cfg, m, p, ip, &nlost, &nhop);
     } else {
-      ref_track_single(cfg, m, p, ip, &ntol);
+      ref_track_single(cfg, m, geo, p, ip, &ntol, &nhop);
     }
   }
+  free(geo);
   (void)nthreads;
   if (c) { c->n_lost += nlost; c->n_hop_limit += nhop; c->n_ref_tolerance += ntol; }
 }

@@ -18,7 +18,8 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libpiclas_gpu.so")
 SOURCES = ["pic_kernels.cu", "pic_capi.cu", "pic_noalloc.cu", "pic_adjoint.cu", "pic_hdg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-ffp-contract=off"]   # host code: no FMA contraction on aarch64 either (same sums as the oracle)
 
 
 def nvcc() -> str:

@@ -64,6 +64,7 @@ class PicMesh(C.Structure):
         ("fibgm_imax", C.c_int32 * 3), ("fibgm_deltas", C.c_double * 3), ("fibgm_n_elems", _ip),
         ("fibgm_offset", _ip), ("fibgm_element", _ip), ("fibgm_n_total", C.c_int32),
         ("side_bc", _ip), ("sf_elem_radius", _dp),
+        ("n_bc_entries", C.c_int32), ("elem_to_bc_sides", _ip), ("bc_side_elem_loc", _ip), ("bc_side_distance", _dp),
     ]
 
 
@@ -193,6 +194,17 @@ class MeshStruct:
         s.side_bc = i("sbc", mesh.side_bc) if mesh.side_bc is not None else C.POINTER(C.c_int32)()
         sfr = getattr(mesh, "sf_elem_radius", None)
         s.sf_elem_radius = d("sfr", sfr) if sfr is not None else C.POINTER(C.c_double)()
+        e2b = getattr(mesh, "elem_to_bc_sides", None)
+        if e2b is not None:
+            s.n_bc_entries = int(len(mesh.bc_side_distance))
+            s.elem_to_bc_sides = i("e2b", e2b)
+            s.bc_side_elem_loc = i("bcl", mesh.bc_side_elem_loc)
+            s.bc_side_distance = d("bcd", mesh.bc_side_distance)
+        else:
+            s.n_bc_entries = 0
+            s.elem_to_bc_sides = C.POINTER(C.c_int32)()
+            s.bc_side_elem_loc = C.POINTER(C.c_int32)()
+            s.bc_side_distance = C.POINTER(C.c_double)()
         self.struct = s
         self._keep = keep
 

@@ -335,6 +335,59 @@ const char* pic_version(void) {
 }
 const char* pic_last_error(void) { return g_last_error.c_str(); }
 
+// Wall side of a BC element for RefTracking: BezierControlPoints3D at NGeo = 1 (the corner nodes in CGNS side
+// order, particle_mesh_tools.f90:1748-1773), BaseVectors0-2 (particle_mesh_build.f90:1916-1925), SideNormVec
+// and SideDistance oriented away from the element (particle_mesh_tools.f90:1011-1048).  Same operation
+// order as the oracle.  Returns false unless the side is a planar rectangle (SideType PLANAR_RECT).
+static bool wall_side_geometry(const double* xcl, const double* bary, int e, int s, double* g) {
+  auto corner = [&](int p, int q, double out[3]) {
+    int a, b, cc;
+    switch (s) {
+      case 0: a = q; b = p; cc = 0; break;
+      case 1: a = p; b = 0; cc = q; break;
+      case 2: a = 1; b = p; cc = q; break;
+      case 3: a = 1 - p; b = 1; cc = q; break;
+      case 4: a = 0; b = q; cc = p; break;
+      default: a = p; b = q; cc = 1; break;
+    }
+    const double* X = xcl + ((size_t)e * 8 + (a + 2 * b + 4 * cc)) * 3;
+    out[0] = X[0]; out[1] = X[1]; out[2] = X[2];
+  };
+  double P00[3], P10[3], P01[3], P11[3], ctr[3];
+  corner(0, 0, P00); corner(1, 0, P10); corner(0, 1, P01); corner(1, 1, P11);
+  for (int c = 0; c < 3; ++c) {
+    g[c] = ((+P00[c] + P10[c]) + P01[c]) + P11[c];
+    g[3 + c] = ((-P00[c] + P10[c]) - P01[c]) + P11[c];
+    g[6 + c] = ((-P00[c] - P10[c]) + P01[c]) + P11[c];
+    ctr[c] = 0.25 * (((P00[c] + P10[c]) + P01[c]) + P11[c]);
+  }
+  const double* v1 = g + 3;
+  const double* v2 = g + 6;
+  double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+  const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  for (int c = 0; c < 3; ++c) n[c] = n[c] / len;
+  const double* b = bary + (size_t)e * 3;
+  const double vb[3] = {ctr[0] - b[0], ctr[1] - b[1], ctr[2] - b[2]};
+  if (vb[0] * n[0] + vb[1] * n[1] + vb[2] * n[2] < 0.0)
+    for (int c = 0; c < 3; ++c) n[c] = -n[c];
+  for (int c = 0; c < 3; ++c) g[9 + c] = n[c];
+  g[12] = ctr[0] * n[0] + ctr[1] * n[1] + ctr[2] * n[2];
+  const double* Pc[4] = {P00, P10, P01, P11};
+  const double scale = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  for (int k = 0; k < 4; ++k)
+    if (std::fabs(Pc[k][0] * n[0] + Pc[k][1] * n[1] + Pc[k][2] * n[2] - g[12]) > 1e-12 * scale) return false;
+  auto unit = [](const double a[3], const double b0[3], double u[3]) {
+    double d[3] = {a[0] - b0[0], a[1] - b0[1], a[2] - b0[2]};
+    double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (std::fabs(l) > 0.0) { l = 1.0 / l; u[0] = d[0] * l; u[1] = d[1] * l; u[2] = d[2] * l; }
+    else { u[0] = u[1] = u[2] = 0.0; }
+  };
+  double u1[3], u2[3], u3[3], u4[3];
+  unit(P01, P00, u1); unit(P10, P00, u2); unit(P11, P01, u3); unit(P11, P10, u4);
+  auto dz = [](const double a[3], const double bb[3]) { return std::fabs(a[0] * bb[0] + a[1] * bb[1] + a[2] * bb[2]) <= 2.22e-16; };
+  return dz(u1, u2) && dz(u1, u3) && dz(u4, u2) && dz(u4, u3);
+}
+
 int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   if (!out) return fail(PIC_ERR_INVALID_ARGUMENT, "ctx_out is null");
   *out = nullptr;
@@ -389,8 +442,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       const bool wall = bc == 1 || bc == 2;
       if (wall ? nb != 0 : (nb < 1 || nb > ne))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_nb_elem must be 1..nElems, or 0 exactly at open/reflective sides"));
-      if (wall && (cfg->tracking != PIC_TRACK_TRIA || cfg->deposition != PIC_DEPO_CVWM))
-        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "open/reflective particle boundaries need TriaTracking + cell_volweight_mean"));
+      if (wall && cfg->deposition != PIC_DEPO_CVWM)
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "open/reflective particle boundaries need cell_volweight_mean"));
+      if (wall && cfg->tracking == PIC_TRACK_REFMAPPING && (m->n_periodic_vectors > 0 || !m->elem_to_bc_sides))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT,
+                         "RefTracking with walls needs a mesh without periodic sides and elem_to_bc_sides"));
       c->has_walls = c->has_walls || wall;
       side_nb[e * 6 + s] = wall ? -1 : nb - 1;
       uint32_t info = 0;
@@ -406,6 +462,31 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       info |= ((uint32_t)(uint8_t)(int8_t)pv) << 16;
       if (wall) info |= (uint32_t)bc << 24;     // 1 open, 2 reflective
       side_info[e * 6 + s] = info;
+    }
+  }
+  // ---- RefTracking wall sides: BC-element lists and planar-side geometry ------------------------
+  std::vector<int> bc_e2b;
+  std::vector<double> bc_geo;
+  if (c->has_walls && cfg->tracking == PIC_TRACK_REFMAPPING) {
+    const int nent = m->n_bc_entries;
+    if (nent < 1 || !m->bc_side_elem_loc || !m->bc_side_distance)
+      return bail(fail(PIC_ERR_INVALID_ARGUMENT, "n_bc_entries/bc_side_elem_loc/bc_side_distance missing"));
+    bc_e2b.assign(m->elem_to_bc_sides, m->elem_to_bc_sides + (size_t)ne * 2);
+    for (int e = 0; e < ne; ++e) {
+      const int n = bc_e2b[2 * e], f = bc_e2b[2 * e + 1];
+      if (n > 0 ? (f < 0 || f + n > nent) : (n != -1 && n != 0))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "elem_to_bc_sides out of range"));
+      if (n <= 0) { bc_e2b[2 * e] = -1; bc_e2b[2 * e + 1] = -1; }
+    }
+    bc_geo.assign((size_t)nent * kBcGeo, 0.0);
+    for (int k = 0; k < nent; ++k) {
+      const int e = m->bc_side_elem_loc[2 * k] - 1, sd = m->bc_side_elem_loc[2 * k + 1] - 1;
+      if (e < 0 || e >= ne || sd < 0 || sd > 5 || m->side_nb_elem[e * 6 + sd] != 0)
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "bc_side_elem_loc must name open/reflective wall sides"));
+      if (!wall_side_geometry(xcl.data(), bary.data(), e, sd, &bc_geo[(size_t)k * kBcGeo]))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "RefTracking walls must be planar rectangles (SideType PLANAR_RECT)"));
+      bc_geo[(size_t)k * kBcGeo + 13] = m->bc_side_distance[k];
+      bc_geo[(size_t)k * kBcGeo + 14] = (double)m->side_bc[e * 6 + sd];
     }
   }
   // ---- periodic-unique nodes (merge Periodic_Nodes twins) ----------------------------------
@@ -467,6 +548,13 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     return bail(rc);
   c->M = DevMesh{ne, d_xcl, d_dxcl, d_bary, d_xez, d_slen, d_rad, d_eps1, d_snb, d_sinfo, d_ecan, d_nvol, d_exgp,
                  d_fn, d_fo, d_fe, d_xclr};
+  if (!bc_e2b.empty()) {
+    int* d_be = nullptr;
+    double* d_bg = nullptr;
+    if ((rc = upload(c, &d_be, bc_e2b)) || (rc = upload(c, &d_bg, bc_geo))) return bail(rc);
+    c->M.bc_e2b = d_be;
+    c->M.bc_geo = d_bg;
+  }
   c->MF = MeshF{d_xclr, d_dxclf, d_xezf, d_slenf};
 
   // ---- constants -------------------------------------------------------------------------------

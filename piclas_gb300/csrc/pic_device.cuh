@@ -63,7 +63,15 @@ struct DevMesh {
   const int* fib_off;
   const int* fib_elem;     // 0-based
   const float* xclr;       // [ne][8][3] FP32 corners minus the barycentre (inside-test pre-filter)
+  // RefTracking with walls: per element (ELEM_NBR_BCSIDES, first entry) or (-1,-1); per entry kBcGeo doubles
+  const int* bc_e2b;
+  const double* bc_geo;
 };
+// one wall-side entry of a BC element: [0..2] BaseVectors0, [3..5] BaseVectors1, [6..8] BaseVectors2,
+// [9..11] SideNormVec (away from the domain), [12] SideDistance, [13] SideBCMetrics(BCSIDE_DISTANCE),
+// [14] boundary (1 open, 2 reflective)
+constexpr int kBcGeo = 16;
+constexpr int kBcCap = 32;   // wall sides traced per trajectory (entries within reach beyond it are not)
 
 // ---- particles (SoA) ---------------------------------------------------------------------
 struct DevParticles {
@@ -754,13 +762,122 @@ __device__ __forceinline__ bool almost_equal(double a, double b) { return fabs(a
 
 constexpr int kMaxBgmCand = 64;
 
-// Returns the new element (0-based); sets tol_fail when the reference would abort.  FAST selects
-// the mixed variant's Newton (ref_elem_newton_fast).
+// ComputePlanarRectIntersection, particle_intersection.f90:515-684 (flip 0: wall sides are master sides);
+// alpha or -1
+__device__ __forceinline__ double planar_rect_alpha(const double* __restrict__ g, const double xl[3],
+                                                    const double traj[3], double len) {
+  const double n0 = g[9], n1 = g[10], n2 = g[11];
+  const double coeffA = n0 * traj[0] + n1 * traj[1] + n2 * traj[2];
+  if (fabs(coeffA) <= 2.22e-16) return -1.0;
+  const double locSideDistance = g[12] - (xl[0] * n0 + xl[1] * n1 + xl[2] * n2);
+  const double alpha = locSideDistance / coeffA;
+  if (locSideDistance < -100.0 * kEpsMach) return -1.0;
+  const double alphaNorm = alpha / len;
+  if (alphaNorm > 1.0 || alphaNorm < -(100.0 * kEpsMach)) return -1.0;
+  double P0[3], P1[3], P2[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double inter = xl[c] + alpha * traj[c];
+    P0[c] = -0.25 * g[c] + inter;
+    P1[c] = 0.25 * g[3 + c];
+    P2[c] = 0.25 * g[6 + c];
+  }
+  const double A1 = P1[0] * P1[0] + P1[1] * P1[1] + P1[2] * P1[2];
+  const double B1 = P2[0] * P1[0] + P2[1] * P1[1] + P2[2] * P1[2];
+  const double C1 = P1[0] * P0[0] + P1[1] * P0[1] + P1[2] * P0[2];
+  const double A2 = B1;
+  const double B2 = P2[0] * P2[0] + P2[1] * P2[1] + P2[2] * P2[2];
+  const double C2 = P2[0] * P0[0] + P2[1] * P0[1] + P2[2] * P0[2];
+  double sdet = A1 * B2 - A2 * B1;
+  if (fabs(sdet) == 0.0) return -1.0;
+  sdet = 1.0 / sdet;
+  const double epsLoc = 1.0 + 100.0 * kEpsMach;
+  const double xi = (B2 * C1 - B1 * C2) * sdet;
+  if (fabs(xi) > epsLoc) return -1.0;
+  const double eta = (-A2 * C1 + A1 * C2) * sdet;
+  if (fabs(eta) > epsLoc) return -1.0;
+  return alpha;
+}
+
+// ParticleBCTracking, particle_reftracking.f90:417-694, for wall sides only (the element never changes).
+// Returns true when the particle is done: it has not moved (PARTHASMOVED) or an open wall removed it.
+static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int elem, double x[3], double xl[3], double v[3],
+                                         bool& removed, double& len0, bool& cap_hit) {
+  const int nloc = __ldg(M.bc_e2b + 2 * elem), first = __ldg(M.bc_e2b + 2 * elem + 1);
+  double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
+  double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+  if (fabs(len / __ldg(M.radius + elem)) <= 2.22e-16) return true;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+  len0 = fmax(len0, len);
+  bool doubleCheck = false;
+  for (int loop = 0; loop < 10000; ++loop) {
+    double alpha[kBcCap];
+    int list[kBcCap];
+    int nc = 0, nInter = 0;
+    for (int i = 0; i < nloc; ++i) {
+      const double* g = M.bc_geo + (size_t)kBcGeo * (first + i);
+      if (__ldg(g + 13) > len0) break;
+      if (nc == kBcCap) { cap_hit = true; break; }
+      alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+      list[nc] = i;
+      if (alpha[nc] > -1.0) nInter++;
+      nc++;
+    }
+    if (nInter == 0) return false;
+    for (int i = 1; i < nc; ++i) {                       // InsertionSort (stable)
+      const double t = alpha[i];
+      const int ti = list[i];
+      int j = i - 1;
+      while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; j--; }
+      alpha[j + 1] = t;
+      list[j + 1] = ti;
+    }
+    bool reflected = false;
+    for (int k = 0; k < nc; ++k) {
+      if (!(alpha[k] > -1.0)) continue;
+      const double* g = M.bc_geo + (size_t)kBcGeo * (first + list[k]);
+      const double n[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
+      // GetBoundaryInteraction, REFMAPPING branch (particle_boundary_condition.f90:35-221)
+      if (n[0] * traj[0] + n[1] * traj[1] + n[2] * traj[2] <= 0.0) { reflected = false; continue; }
+      reflected = true;
+      if (__ldg(g + 14) == 1.0) { removed = true; break; }          // RemoveParticle
+      perfect_reflection(v, x, xl, traj, len, alpha[k], n);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
+      len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+      if (fabs(len) <= 2.22e-16) len = 0.0;
+      else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+      }
+      break;
+    }
+    if (removed) return true;
+    if (!reflected) {
+      if (!doubleCheck) doubleCheck = true;
+      else return false;
+    }
+  }
+  return false;
+}
+
+// Returns the new element (0-based); sets tol_fail when the reference would abort, removed when an open
+// wall took the particle.  FAST selects the mixed variant's Newton (ref_elem_newton_fast).  v is only
+// changed by reflective walls.
 template <bool FAST>
 __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[3], double xl[3], double xi[3],
-                                      bool& tol_fail) {
+                                      double v[3], bool& tol_fail, bool& removed, bool& cap_hit) {
   tol_fail = false;
-  if (c_k.n_pv > 0) {
+  removed = false;
+  const bool bc_elem = M.bc_e2b && __ldg(M.bc_e2b + 2 * last_elem) > 0;
+  if (bc_elem) {
+    // BC element (particle_reftracking.f90:98-126)
+    double len0 = 0.0;
+    if (bc_tracking(M, last_elem, x, xl, v, removed, len0, cap_hit)) return last_elem;
+    position_in_ref_elem_t<FAST>(M, last_elem, x, xi);
+    if (maxabs3(xi) < 1.0) return last_elem;
+  } else if (c_k.n_pv > 0) {
     double lp[3] = {x[0], x[1], x[2]};
     periodic_movement_fast(x, xl);
     int guard = 0;
@@ -770,8 +887,10 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
       guard++;
     }
   }
-  position_in_ref_elem_t<FAST>(M, last_elem, x, xi);
-  if (maxabs3(xi) < 1.0) return last_elem;
+  if (!bc_elem) {
+    position_in_ref_elem_t<FAST>(M, last_elem, x, xi);
+    if (maxabs3(xi) < 1.0) return last_elem;
+  }
   const int oldElem = last_elem;
   int cell[3];
 #pragma unroll
@@ -832,7 +951,18 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
     xi[0] = newXi[0]; xi[1] = newXi[1]; xi[2] = newXi[2];
     te = newElem;
   }
-  if (te < 0 || maxabs3(xi) > __ldg(M.eps1 + te)) tol_fail = true;
+  if (te < 0 || maxabs3(xi) > __ldg(M.eps1 + te)) {
+    if (te >= 0 && M.bc_e2b && __ldg(M.bc_e2b + 2 * te) > 0) {
+      // BC element (particle_reftracking.f90:327-403): trace the walls again from TestElem
+      double len0 = 0.0;
+      if (bc_tracking(M, te, x, xl, v, removed, len0, cap_hit)) return te;
+      position_in_ref_elem_t<FAST>(M, te, x, xi);
+      // beyond epsOneCell the reference calls LocateParticleInElement and aborts when that fails
+      if (maxabs3(xi) > __ldg(M.eps1 + te)) tol_fail = true;
+    } else {
+      tol_fail = true;
+    }
+  }
   return te < 0 ? oldElem : te;
 }
 

@@ -425,6 +425,7 @@ __global__ void __launch_bounds__(256) k_track_tria(DevMesh M, DevParticles P, D
   P.elem[i] = ne;
 }
 
+template <bool MIXED>
 __global__ void __launch_bounds__(256) k_track_ref(DevMesh M, DevParticles P, DevStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
@@ -432,10 +433,17 @@ __global__ void __launch_bounds__(256) k_track_ref(DevMesh M, DevParticles P, De
   if (!(fl & kInside)) return;
   double x[3] = {P.x[i], P.y[i], P.z[i]};
   double xl[3] = {P.lx[i], P.ly[i], P.lz[i]};
-  double xi[3];
-  bool tol = false;
-  const int ne = ref_track<false>(M, P.last_elem[i], x, xl, xi, tol);
+  double xi[3] = {P.xi0[i], P.xi1[i], P.xi2[i]};
+  double v[3];
+  if constexpr (MIXED) { v[0] = P.vxf[i]; v[1] = P.vyf[i]; v[2] = P.vzf[i]; }
+  else { v[0] = P.vx[i]; v[1] = P.vy[i]; v[2] = P.vz[i]; }
+  bool tol = false, removed = false, cap = false;
+  const int ne = ref_track<false>(M, P.last_elem[i], x, xl, xi, v, tol, removed, cap);
   if (tol) { atomicAdd(&st->n_ref_tolerance, 1); flag_status(st, 0x08u); }
+  if (cap) flag_status(st, 0x04u);
+  if constexpr (MIXED) { P.vxf[i] = (float)v[0]; P.vyf[i] = (float)v[1]; P.vzf[i] = (float)v[2]; }
+  else { P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2]; }
+  if (removed) P.flags[i] = fl & ~kInside;
   P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
   P.lx[i] = xl[0]; P.ly[i] = xl[1]; P.lz[i] = xl[2];
   P.xi0[i] = xi[0]; P.xi1[i] = xi[1]; P.xi2[i] = xi[2];
@@ -1352,13 +1360,22 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
     P.flags[i] = (isnew ? (fl | kNew) : (fl & ~kNew)) & ~kInside;
     return;
   }
-  bool tol = false;
-  const int ne = ref_track<MIXED>(M, e, x, xl, xi, tol);
+  bool tol = false, removed = false, cap = false;
+  double v[3];
+  if constexpr (MIXED) { v[0] = P.vxf[i]; v[1] = P.vyf[i]; v[2] = P.vzf[i]; }
+  else { v[0] = P.vx[i]; v[1] = P.vy[i]; v[2] = P.vz[i]; }
+  const int ne = ref_track<MIXED>(M, e, x, xl, xi, v, tol, removed, cap);
   if (tol) { atomicAdd(&st->n_ref_tolerance, 1); flag_status(st, 0x08u); }
+  if (cap) flag_status(st, 0x04u);
+  if (M.bc_e2b) {                                   // reflective walls change v
+    if constexpr (MIXED) { P.vxf[i] = (float)v[0]; P.vyf[i] = (float)v[1]; P.vzf[i] = (float)v[2]; }
+    else { P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2]; }
+  }
   P.x[i] = x[0]; P.y[i] = x[1]; P.z[i] = x[2];
   P.xi0[i] = xi[0]; P.xi1[i] = xi[1]; P.xi2[i] = xi[2];
   P.elem[i] = ne;
-  P.flags[i] = isnew ? (fl | kNew) : (fl & ~kNew);
+  const uint8_t f2 = isnew ? (fl | kNew) : (fl & ~kNew);
+  P.flags[i] = removed ? (f2 & ~kInside) : f2;
 }
 
 // =============================================================================================
@@ -1488,7 +1505,8 @@ int launch_push(const LaunchArgs& A, const DevParticles& P, double dt) {
 
 int launch_track(const LaunchArgs& A, const DevParticles& P, bool refmap) {
   if (P.n <= 0) return 0;
-  if (refmap) k_track_ref<<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
+  if (refmap && A.mixed) k_track_ref<true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
+  else if (refmap) k_track_ref<false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
   else if (A.mixed) k_track_tria<true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
   else k_track_tria<false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.st);
   return 1;

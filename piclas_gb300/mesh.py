@@ -189,6 +189,10 @@ class BoxMesh:
     side_bc: np.ndarray = field(default=None)         # (6,nElems) 1 open / 2 reflective wall, 0 otherwise; None: no walls
     bc: tuple = ("periodic", "periodic", "periodic")  # particle boundary per axis
     sf_elem_radius: np.ndarray = field(default=None)  # SFElemr2_Shared(1,:) for shape_function_adaptive
+    # RefTracking with walls: BuildBCElemDistance output (see build_bc_elem_distance)
+    elem_to_bc_sides: np.ndarray = field(default=None)
+    bc_side_elem_loc: np.ndarray = field(default=None)
+    bc_side_distance: np.ndarray = field(default=None)
 
     @property
     def n_dof(self) -> int:
@@ -211,14 +215,15 @@ WALL_BC = {"open": 1, "reflective": 2}      # PartBound%TargetBoundCond
 
 def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
                    perturb: float = 0.0, refmapping_eps: float = 1.0e-4,
-                   bc=("periodic", "periodic", "periodic")) -> BoxMesh:
+                   bc=("periodic", "periodic", "periodic"), bc_halo_eps: float | None = None) -> BoxMesh:
     """Build a box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
 
     ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
     along each axis (h per axis); boundary nodes stay put so the periodic faces match.
     ``bc`` gives the particle boundary of both faces of each axis: "periodic" (a periodic vector, node
     twins for cell_volweight_mean), "open" or "reflective" (wall sides without a neighbour: SIDE_NBELEMID
-    = 0, master orientation, convex).
+    = 0, master orientation, convex).  Without periodic axes the BC-element lists of RefTracking are
+    built with halo ``bc_halo_eps`` (default: the largest element extent).
     """
     bc = tuple(bc)
     if len(bc) != 3 or any(b not in ("periodic", "open", "reflective") for b in bc):
@@ -486,7 +491,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     for d, q in pv_index.items():
         pv[d, q - 1] = L[d]
 
-    return BoxMesh(
+    mesh = BoxMesh(
         nx=nx, ny=ny, nz=nz, N=N, lo=lo, hi=hi, n_elems=ne, n_nodes=n_unique, n_geo=1,
         periodic_vectors=pv,
         xi_cl_ngeo=np.asarray(xi_cl), wbary_cl_ngeo=np.asarray(wb_cl),
@@ -504,6 +509,98 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         fibgm_element=fib_el, canonical_node=canon,
         side_bc=side_bc if side_bc.any() else None, bc=bc,
     )
+    if side_bc.any() and not any(periodic):
+        halo = float(hvec.max()) if bc_halo_eps is None else float(bc_halo_eps)
+        mesh.elem_to_bc_sides, mesh.bc_side_elem_loc, mesh.bc_side_distance = build_bc_elem_distance(mesh, halo)
+    return mesh
+
+
+# CGNS_SideToVol2 at NGeo = 1 for a master side: corner (p,q) of local side s -> tensor corner (a,b,c)
+_SIDE_CORNER = {
+    0: lambda p, q: (q, p, 0),        # ZETA_MINUS: (p,q) = (j,i)
+    1: lambda p, q: (p, 0, q),        # ETA_MINUS:  (p,q) = (i,k)
+    2: lambda p, q: (1, p, q),        # XI_PLUS:    (p,q) = (j,k)
+    3: lambda p, q: (1 - p, 1, q),    # ETA_PLUS:   (p,q) = (1-i,k)
+    4: lambda p, q: (0, q, p),        # XI_MINUS:   (p,q) = (k,j)
+    5: lambda p, q: (p, q, 1),        # ZETA_PLUS:  (p,q) = (i,j)
+}
+
+
+def side_control_points(mesh: BoxMesh, e: int, s: int) -> np.ndarray:
+    """BezierControlPoints3D(1:3,0:1,0:1) of local side s of element e (0-based), as [q][p][3]
+    (particle_mesh_tools.f90:1748-1773 at NGeo = 1, where the Bezier and CL corner points coincide)."""
+    out = np.zeros((2, 2, 3))
+    for q in range(2):
+        for p in range(2):
+            a, b, c = _SIDE_CORNER[s](p, q)
+            out[q, p] = mesh.xcl_ngeo[e, c, b, a]
+    return out
+
+
+def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float):
+    """ElemToBCSides / SideBCMetrics of BuildBCElemDistance (particle_mesh_build.f90:645-1092, the halo
+    branch of an MPI build): for every element its own wall sides (local side order), then every other
+    wall side whose element and side lie within bc_halo_eps (+ radii) of it, ordered by
+    SideBCMetrics(BCSIDE_DISTANCE) = |ElemBaryNGeo - origin| - ElemRadiusNGeo - side radius with the
+    reference's stable InsertionSort.  Side origin and radius: BuildSideOriginAndRadius
+    (particle_mesh_build.f90:1795-1820; DeCasteljauInterpolation at (0,0)).
+    Returns (elem_to_bc_sides (nElems,2) = (count or -1, 0-based first entry or -1),
+             entries (n,2) = (element 1-based, local side 1-based), distance (n))."""
+    ne = mesh.n_elems
+    walls = [(e, s) for e in range(ne) for s in range(6) if mesh.side_nb_elem[e, s] == 0]
+    if not walls:
+        return None
+    origin = np.zeros((len(walls), 3))
+    radius = np.zeros(len(walls))
+    for k, (e, s) in enumerate(walls):
+        P = side_control_points(mesh, e, s)
+        o = (((0.5 * P[0, 0]) * 0.5 + (0.5 * P[1, 0]) * 0.5) + (0.5 * P[0, 1]) * 0.5) + (0.5 * P[1, 1]) * 0.5
+        origin[k] = o
+        rmax = 0.0
+        for q in range(2):
+            for p in range(2):
+                v = P[q, p] - o
+                rmax = max(rmax, float(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]))
+        radius[k] = math.sqrt(rmax)
+    wall_elem = np.array([e for e, _ in walls])
+    bary = mesh.elem_bary
+    rad = mesh.elem_radius
+
+    def norm3(v):
+        return np.sqrt(v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1] + v[..., 2] * v[..., 2])
+
+    e2b = -np.ones((ne, 2), dtype=np.int32)
+    entries, dists = [], []
+    for e in range(ne):
+        own = [k for k, (we, _) in enumerate(walls) if we == e]
+        other = np.nonzero(wall_elem != e)[0]
+        d_el = norm3(bary[e] - bary[wall_elem[other]])
+        keep = d_el <= bc_halo_eps + rad[e] + rad[wall_elem[other]]
+        d_sd = norm3(bary[e] - origin[other])
+        keep &= d_sd <= bc_halo_eps + rad[e] + radius[other]
+        lst = own + [int(k) for k in other[keep]]
+        if not lst:
+            continue
+        vec = bary[e] - origin[lst]
+        dist = np.sqrt((vec[:, 0] * vec[:, 0] + vec[:, 1] * vec[:, 1]) + vec[:, 2] * vec[:, 2]) - rad[e] - radius[lst]
+        # InsertionSort (utils.f90:52-101): stable, ascending
+        order = list(range(len(lst)))
+        dv = list(dist)
+        for i in range(1, len(order)):
+            t, ti = dv[i], order[i]
+            j = i - 1
+            while j >= 0 and not (dv[j] <= t):
+                dv[j + 1] = dv[j]
+                order[j + 1] = order[j]
+                j -= 1
+            dv[j + 1] = t
+            order[j + 1] = ti
+        e2b[e] = (len(lst), len(entries))
+        for i in order:
+            we, ws = walls[lst[i]]
+            entries.append((we + 1, ws + 1))
+            dists.append(float(dist[i]))
+    return e2b, np.asarray(entries, dtype=np.int32), np.asarray(dists)
 
 
 def elem_map(mesh: BoxMesh, e: int, xi) -> np.ndarray:

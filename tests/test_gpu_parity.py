@@ -574,3 +574,68 @@ def test_wrong_start_element_matches_oracle(gpu_lib, oracle_lib):
     assert np.array_equal(g["elem"], st.elem)
     assert g["status"]["n_lost"] == st.counters.n_lost
     assert np.array_equal(g["part_state"], st.part_state)
+
+
+# ---- walls with RefTracking (ParticleBCTracking over planar wall sides) ------------------------------
+def _ref_wall_workload(bc, seed, n=4000, perturb=0.0, cells=5):
+    mesh = build_box_mesh(cells, cells, cells, 2, perturb=perturb, bc=bc)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=2000.0, seed=seed, dt=2e-10)
+    if perturb:
+        x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(seed))
+        w.part_state[:, :3] = x
+        w.elem = e
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    return w
+
+
+@pytest.mark.parametrize("bc,perturb", [(("reflective",) * 3, 0.0), (("reflective", "open", "reflective"), 0.05),
+                                        (("open", "reflective", "open"), 0.0)])
+def test_reftracking_walls_fp64_bitexact(gpu_lib, oracle_lib, bc, perturb):
+    w = _ref_wall_workload(bc, seed=31, perturb=perturb)
+    g = _run_gpu(w, 12)
+    st, PS = _run_oracle(oracle_lib, w, 12)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0 and st.counters.n_ref_tolerance == 0
+    assert (np.sign(st.part_state[:, 3:]) != np.sign(w.part_state[:, 3:])).any(axis=1).sum() > 100
+    if "open" in bc:
+        assert (st.inside == 0).sum() > 100
+
+
+def test_reftracking_walls_separate_routines_and_mixed(gpu_lib, oracle_lib):
+    w = _ref_wall_workload(("reflective", "open", "reflective"), seed=32, n=3000)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    loop = ParticleLoop(cfg, w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.map_particles(cfg, ms, st)
+    for _ in range(6):
+        oracle_lib.save_last(st)
+        oracle_lib.interpolate(cfg, ms, w.e_dof, st)
+        oracle_lib.push(cfg, st, w.dt)
+        oracle_lib.track(cfg, ms, st)
+        loop.interpolate_field_to_particle()
+        loop.push(w.dt)
+        loop.perform_tracking()
+    g = loop.download_particles()
+    loop.close()
+    assert np.array_equal(g["inside"], st.inside) and np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    gm = _run_gpu(w, 6, precision=capi.PIC_PREC_MIXED)
+    assert (gm["inside"] != st.inside).sum() <= 3
+    k = (gm["inside"] == 1) & (st.inside == 1)
+    assert np.max(np.abs(gm["part_state"][k, :3] - st.part_state[k, :3])) < 1e-6
+
+
+def test_reftracking_walls_rejected_where_unsupported(gpu_lib):
+    w = _ref_wall_workload(("reflective", "open", "periodic"), seed=33, n=100)
+    with pytest.raises(PicError) as e:
+        ParticleLoop(w.config(), w.mesh)                      # periodic sides + RefTracking walls
+    assert e.value.code == 1
+    w = _ref_wall_workload(("reflective",) * 3, seed=33, n=100)
+    w.mesh.elem_to_bc_sides = None
+    with pytest.raises(PicError):
+        ParticleLoop(w.config(), w.mesh)                      # no BC-element lists

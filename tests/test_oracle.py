@@ -233,3 +233,86 @@ def test_adaptive_with_uniform_radius_is_cc(oracle_lib):
         oracle_lib.deposit(cfg, ms, st, PS)
         out[dep] = PS
     assert np.array_equal(out[capi.PIC_DEPO_SHAPE_FUNCTION_CC], out[capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+
+
+# ---- walls with RefTracking (ParticleBCTracking over planar wall sides) -----------------------------
+def _ref_wall_steps(oracle_lib, w, nsteps):
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species, is_new=np.zeros(w.n, np.uint8))
+    oracle_lib.map_particles(cfg, ms, st)
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, nsteps)
+    return st
+
+
+def test_bc_elem_distance_lists():
+    m = build_box_mesh(4, 3, 3, 1, bc=("reflective", "open", "reflective"))
+    e2b, loc, dist = m.elem_to_bc_sides, m.bc_side_elem_loc, m.bc_side_distance
+    walls = {(e + 1, s + 1) for e in range(m.n_elems) for s in range(6) if m.side_nb_elem[e, s] == 0}
+    assert len(walls) == 2 * (9 + 12 + 12)
+    for e in range(m.n_elems):
+        n, f = e2b[e]
+        own = {(e + 1, s + 1) for s in range(6) if m.side_nb_elem[e, s] == 0}
+        if n < 0:
+            assert not own
+            continue
+        ent = [tuple(x) for x in loc[f:f + n]]
+        assert own <= set(ent) and set(ent) <= walls and len(set(ent)) == n
+        assert np.all(np.diff(dist[f:f + n]) >= 0.0)          # sorted by distance
+    assert (e2b[:, 0] > 0).sum() == m.n_elems                 # halo = one element extent: all elements in reach
+
+
+def test_reftracking_reflective_box_matches_triatracking(oracle_lib):
+    w = _wall_case(("reflective", "reflective", "reflective"), n=3000, seed=12)
+    tri = _oracle_steps(oracle_lib, w, 30)
+    ref = _ref_wall_steps(oracle_lib, w, 30)
+    assert ref.inside.all() and ref.counters.n_ref_tolerance == 0
+    x = ref.part_state[:, :3]
+    assert (x >= 0.0).all() and (x <= 1.0).all()
+    # both trackers reflect at the same planes with the same normal: velocities identical, positions
+    # equal up to the rounding of the two intersection formulas
+    assert np.array_equal(ref.part_state[:, 3:], tri.part_state[:, 3:])
+    assert np.max(np.abs(ref.part_state[:, :3] - tri.part_state[:, :3])) < 1e-13
+    assert (np.sign(ref.part_state[:, 3:]) != np.sign(w.part_state[:, 3:])).any(axis=1).sum() > 500
+    assert np.array_equal(ref.elem, workloads._elem_of_uniform(w.mesh, x))
+
+
+def test_reftracking_open_walls_remove_the_leaving_particles(oracle_lib):
+    w = _wall_case(("open", "open", "open"), n=3000, seed=13)
+    K = 20
+    ref = _ref_wall_steps(oracle_lib, w, K)
+    xf = w.part_state[:, :3] + w.part_state[:, 3:] * (w.dt * K)
+    clear = np.all((np.abs(xf) > 1e-9) & (np.abs(xf - 1.0) > 1e-9), axis=1)
+    expect = np.all((xf > 0.0) & (xf < 1.0), axis=1)
+    assert np.array_equal(ref.inside[clear].astype(bool), expect[clear])
+    assert (~expect).sum() > 300 and ref.counters.n_ref_tolerance == 0
+
+
+def test_reftracking_walls_curved_mesh(oracle_lib):
+    """Interior nodes displaced, planar walls (reflective in x and z, open in y), no field: every particle
+    follows the folded straight line, leaves iff its y path leaves (0,1), and ends in an element whose
+    reference coordinates hold it."""
+    mesh = build_box_mesh(4, 4, 4, 2, perturb=0.05, bc=("reflective", "open", "reflective"))
+    w = workloads.plasma_wave(mesh=mesh, n_particles=3000, T_eV=2000.0, seed=14, dt=2e-10)
+    w.e_dof[:] = 0.0
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(14))   # true (curved) elements
+    w.part_state[:, :3] = x
+    w.elem = e
+    K = 20
+    ref = _ref_wall_steps(oracle_lib, w, K)
+    assert ref.counters.n_ref_tolerance == 0
+    xs = w.part_state[:, :3] + w.part_state[:, 3:] * (w.dt * K)
+
+    def fold(u):
+        u = np.mod(u, 2.0)
+        return np.where(u > 1.0, 2.0 - u, u)
+
+    y = xs[:, 1]
+    clear = (np.abs(y) > 1e-9) & (np.abs(y - 1.0) > 1e-9)
+    expect = (y > 0.0) & (y < 1.0)
+    assert np.array_equal(ref.inside[clear].astype(bool), expect[clear]) and (~expect).sum() > 100
+    k = ref.inside.astype(bool)
+    assert np.max(np.abs(ref.part_state[k, 0] - fold(xs[k, 0]))) < 1e-12
+    assert np.max(np.abs(ref.part_state[k, 2] - fold(xs[k, 2]))) < 1e-12
+    assert np.max(np.abs(ref.part_state[k, 1] - y[k])) < 1e-12
+    assert np.max(np.abs(ref.part_pos_ref[k])) <= 1.0 + 1e-9
