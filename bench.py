@@ -466,7 +466,7 @@ def extras(args, w_main):
     return res
 
 
-def hdg_timing(cells=(8, 32), reps: int = 3, self_consistent: bool = True):
+def hdg_timing(cells=(8, 32), reps: int = 3, self_consistent: bool = True, cg_kernel: int = 0):
     """HDG Poisson solve (HDGLinear: RHS, CG_solver, PostProcessGradientHDG; Elem_Mat once at init) on periodic
     boxes of 8^3 (the plasma-wave mesh) and 32^3 (the curved workload's mesh) hexahedra, N = 3, PrecondType 2,
     epsCG 1e-6 relative to the first residual, each solve from lambda = 0.  The source is the periodic
@@ -495,7 +495,7 @@ def hdg_timing(cells=(8, 32), reps: int = 3, self_consistent: bool = True):
         loop = ParticleLoop(cfg, m)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        loop.hdg_init(h, precond_type=2, eps_cg=1e-6, relative=True, max_iter_cg=5000)
+        loop.hdg_init(h, precond_type=2, eps_cg=1e-6, relative=True, max_iter_cg=5000, cg_kernel=cg_kernel)
         t_init = time.perf_counter() - t0
         src = source(m)
         zero = np.zeros((h.n_sides, 16))
@@ -661,6 +661,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--particles", type=int, default=None, help="override the particle count (profiling cases)")
     ap.add_argument("--cells", type=int, default=None, help="override the elements per axis (profiling cases)")
+    ap.add_argument("--hdg-cg-kernel", type=int, default=0, choices=[0, 1, 2],
+                    help="HDG CG launch form: 0 auto, 1 kernel per phase (graph), 2 cooperative")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         log("warm-up raised to 3 steps")
@@ -679,7 +681,8 @@ def main():
         # the HDG field solve alone (also the extras' "hdg" entry); --cells picks one mesh size
         if rank == 0:
             cells = (args.cells,) if args.cells else (8, 32)
-            print(json.dumps({"hdg": hdg_timing(cells=cells, self_consistent=not args.no_extras)}), flush=True)
+            print(json.dumps({"hdg": hdg_timing(cells=cells, self_consistent=not args.no_extras,
+                                                cg_kernel=args.hdg_cg_kernel)}), flush=True)
         return
     run_gpu(args, rank, world, local_rank)
 

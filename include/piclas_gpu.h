@@ -260,6 +260,9 @@ typedef struct pic_hdg_t {
   double  eps_cg;                 /* epsCG                                                             */
   int32_t use_relative_abort;     /* useRelativeAbortCrit                                              */
   int32_t solve_in_step;          /* 1: pic_step solves after every Deposition (HDG(), :99)            */
+  int32_t cg_kernel;              /* CG launch form (no reference counterpart): 0 auto (= 1), 1 three
+                                     kernels per iteration replayed as a CUDA graph, 2 the whole CG in
+                                     one cooperative kernel with grid barriers (slower on GB300)        */
 } pic_hdg_t;
 typedef struct pic_hdg_status_t {
   int32_t iterations;             /* CG iterations of the last solve                                   */

@@ -279,7 +279,7 @@ class ParticleLoop:
 
     # -- HDG Poisson solve --------------------------------------------------------------------
     def hdg_init(self, hmesh, precond_type: int = 2, eps_cg: float = 1e-6, max_iter_cg: int = 500,
-                 relative: bool = False, solve_in_step: bool = False):
+                 relative: bool = False, solve_in_step: bool = False, cg_kernel: int = 0):
         """InitHDG/Elem_Mat/BuildPrecond from a :class:`piclas_gb300.hdg_mesh.HdgMesh`."""
         self._hdg_keep = [np.ascontiguousarray(hmesh.elem_to_side, dtype=np.int32),
                           np.ascontiguousarray(hmesh.side_to_elem, dtype=np.int32),
@@ -291,7 +291,8 @@ class ParticleLoop:
         e2s, s2e, mf, mg, mh, sj, ds = self._hdg_keep
         h = capi.PicHdg(hmesh.n_sides, capi.iptr(e2s), capi.iptr(s2e), capi.dptr(mf), capi.dptr(mg), capi.dptr(mh),
                         capi.dptr(sj), len(ds), capi.iptr(ds) if len(ds) else _null(C.c_int32), int(precond_type),
-                        int(max_iter_cg), float(eps_cg), int(bool(relative)), int(bool(solve_in_step)))
+                        int(max_iter_cg), float(eps_cg), int(bool(relative)), int(bool(solve_in_step)),
+                        int(cg_kernel))
         self._check(self.lib.pic_hdg_init(self.handle, C.byref(h)), "pic_hdg_init")
         self.hdg_n_sides = hmesh.n_sides
         self.hdg_n_dirichlet = len(ds)

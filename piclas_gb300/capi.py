@@ -77,7 +77,8 @@ class PicHdg(C.Structure):
     _fields_ = [("n_sides", C.c_int32), ("elem_to_side", _ip), ("side_to_elem", _ip), ("metrics_f", _dp),
                 ("metrics_g", _dp), ("metrics_h", _dp), ("sj", _dp), ("n_dirichlet", C.c_int32),
                 ("dirichlet_sides", _ip), ("precond_type", C.c_int32), ("max_iter_cg", C.c_int32),
-                ("eps_cg", C.c_double), ("use_relative_abort", C.c_int32), ("solve_in_step", C.c_int32)]
+                ("eps_cg", C.c_double), ("use_relative_abort", C.c_int32), ("solve_in_step", C.c_int32),
+                ("cg_kernel", C.c_int32)]
 
 
 class PicHdgStatus(C.Structure):

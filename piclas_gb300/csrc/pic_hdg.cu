@@ -41,7 +41,7 @@ struct Tabs {                                  // N_Inter(N) tables (hdg.f90:473
   double Dom[kMaxND][kMaxND], LLm[kMaxND][kMaxND], LLp[kMaxND][kMaxND];
 };
 
-enum { F_DONE = 0, F_ITER = 1, F_STATUS = 2, F_TICKET = 3, F_CONV = 4 };
+enum { F_DONE = 0, F_ITER = 1, F_STATUS = 2, F_TICKET = 3, F_CONV = 4, F_BARRIER = 5 };
 enum { S_RZ1 = 0, S_OMEGA = 1, S_BETA = 2, S_RR = 3, S_ABORT2 = 4 };
 enum { ST_NOT_CONVERGED = 1, ST_BREAKDOWN = 2, ST_ELEM_MAT = 4, ST_PRECOND = 8 };
 
@@ -55,7 +55,7 @@ struct Dev {
   double *ehat, *invd, *smat, *pre;
   double* smat_u;           // [e][stride]: the 21 blocks Smat(:,:,i,j), i <= j
   double *lam, *rhs, *R, *Pr, *Ax, *V0, *V1, *rhs_vol, *contrib, *U;
-  double* red;             // partial sums, one per CTA of a side-DOF kernel
+  double* red;             // partial sums, one per CTA of a side-DOF kernel (the cooperative kernel: 4 per CTA)
   double* sc;              // CG scalars
   int* flags;
 };
@@ -525,17 +525,15 @@ __host__ __device__ constexpr int matvec_threads_t() { return ((21 * ND * ND + 3
 // y = S x per element.  UPDATE: x = V_new = Pr + beta V_old (the side's master element stores it in Vnew);
 // otherwise x = xin.  Shared memory: the 21 blocks (column stride nf+1), x of the 6 sides, row/col parts.
 template <int ND, bool UPDATE>
-__global__ void __launch_bounds__(matvec_threads_t<ND>()) k_matvec(Dev H, const double* __restrict__ xin,
-                                                                   const double* __restrict__ vold,
-                                                                   double* __restrict__ vnew, size_t stride) {
+__device__ __forceinline__ void matvec_element(const Dev& H, int e, const double* __restrict__ xin,
+                                               const double* __restrict__ vold, double* __restrict__ vnew,
+                                               size_t stride, double beta, double* sm) {
   constexpr int nf = ND * ND, ld = nf + 1;
-  if (__ldcg(&H.flags[F_DONE])) return;
-  extern __shared__ double sm[];
   double* Sb = sm;                       // [21][nf][ld]
   double* xs = Sb + 21 * nf * ld;        // [6][nf]
   double* pr = xs + 6 * nf;              // [21][nf] row parts
   double* pc = pr + 21 * nf;             // [21][nf] column parts
-  const int e = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x;
   const double* src = H.smat_u + stride * e;
   // every load of the thread issued before the first store: 16..25 independent loads in flight per thread
   // (launched with exactly matvec_threads_t<ND>() threads)
@@ -561,7 +559,7 @@ __global__ void __launch_bounds__(matvec_threads_t<ND>()) k_matvec(Dev H, const 
     const size_t g = (size_t)sid * nf + b;
     double x;
     if (UPDATE) {
-      x = __fma_rn(__ldcg(&H.sc[S_BETA]), vold[g], H.Pr[g]);
+      x = __fma_rn(beta, vold[g], H.Pr[g]);
       const int* se = H.s2e + 4 * sid;
       if (se[0] == e && se[2] == loc) vnew[g] = x;
     } else {
@@ -594,6 +592,15 @@ __global__ void __launch_bounds__(matvec_threads_t<ND>()) k_matvec(Dev H, const 
     for (int j = 0; j < 6; ++j) y = y + (j >= i ? pr[upper_block(i, j) * nf + a] : pc[upper_block(j, i) * nf + a]);
     H.contrib[((size_t)6 * e + i) * nf + a] = y;
   }
+}
+
+template <int ND, bool UPDATE>
+__global__ void __launch_bounds__(matvec_threads_t<ND>()) k_matvec(Dev H, const double* __restrict__ xin,
+                                                                   const double* __restrict__ vold,
+                                                                   double* __restrict__ vnew, size_t stride) {
+  if (__ldcg(&H.flags[F_DONE])) return;
+  extern __shared__ double sm[];
+  matvec_element<ND, UPDATE>(H, blockIdx.x, xin, vold, vnew, stride, UPDATE ? __ldcg(&H.sc[S_BETA]) : 0.0, sm);
 }
 
 // MODE 0: EvalResidual (R = RHS - S lambda, |R|^2, start test); MODE 1: Ax = S V and v.Ax -> omega
@@ -716,6 +723,166 @@ __global__ void __launch_bounds__(kRedThreads) k_update(Dev H, const double* __r
 }
 
 // ---------------------------------------------------------------------------------------------------
+// The whole CG in one cooperative launch (every CTA resident): the three phases of an iteration are
+// separated by grid barriers instead of kernel boundaries.  Each CTA adds all CTAs' partial sums in the
+// same order, so every CTA takes the same decisions (omega, convergence, beta) from the same values.
+// The barrier wait is bounded: on timeout the CTA raises F_BARRIER and returns, and the others follow at
+// their next barrier; the host then restores lambda and solves with the kernel-per-phase path.
+// ---------------------------------------------------------------------------------------------------
+constexpr unsigned long long kBarrierSpins = 1ull << 22;   // x ~0.1-0.3 us per poll
+#ifndef PIC_HDG_COOP_MINB
+#define PIC_HDG_COOP_MINB 1
+#endif
+
+__device__ bool grid_barrier(const Dev& H, unsigned* bar) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* gen = bar + 1;
+    volatile int* err = H.flags + F_BARRIER;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(bar, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned long long it = 0;
+      while (*gen == g) {
+        if (*err || ++it > kBarrierSpins) { atomicExch(H.flags + F_BARRIER, 1); ok = 0; break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// sum of (a, b) over the block; the result in every thread
+__device__ inline void block_sum2(double& a, double& b, double* ws) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int nw = (int)(blockDim.x >> 5);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { ws[2 * (threadIdx.x >> 5)] = a; ws[2 * (threadIdx.x >> 5) + 1] = b; }
+  __syncthreads();
+  double s0 = 0.0, s1 = 0.0;
+  for (int w = 0; w < nw; ++w) { s0 += ws[2 * w]; s1 += ws[2 * w + 1]; }
+  a = s0;
+  b = s1;
+}
+
+// every CTA: the sum of all CTAs' partials in index order
+__device__ inline void grid_total2(const double* red, double& a, double& b, double* ws) {
+  double s0 = 0.0, s1 = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    s0 += __ldcg(red + 2 * k);
+    s1 += __ldcg(red + 2 * k + 1);
+  }
+  block_sum2(s0, s1, ws);
+  a = s0;
+  b = s1;
+}
+
+template <int ND>
+__global__ void __launch_bounds__(matvec_threads_t<ND>(), PIC_HDG_COOP_MINB) k_cg_persistent(Dev H, size_t stride, unsigned* bar) {
+  constexpr int nf = ND * ND;
+  extern __shared__ double sm[];
+  __shared__ double ws[2 * 32];
+  if (__ldcg(&H.flags[F_DONE])) return;                        // set before the launch: uniform
+  const int nthr = gridDim.x * blockDim.x, gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  double rz1 = __ldcg(&H.sc[S_RZ1]);
+  const double abort2 = __ldcg(&H.sc[S_ABORT2]);
+  double beta = 0.0;
+  int it = __ldcg(&H.flags[F_ITER]);
+  int par = 0;
+  double* redB = H.red;                                        // v.Ax partials
+  double* redC = H.red + 2 * gridDim.x;                        // r.r and r.Pr partials
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  for (;;) {
+    const double* vold = par ? H.V1 : H.V0;
+    double* vnew = par ? H.V0 : H.V1;
+    // A: V_new = P^{-1}R + beta V_old, y = S V_new (element by element)
+    for (int e = blockIdx.x; e < H.ne; e += gridDim.x) {
+      matvec_element<ND, true>(H, e, nullptr, vold, vnew, stride, beta, sm);
+      __syncthreads();
+    }
+    if (!grid_barrier(H, bar)) return;
+    // B: Ax = the two elements' y (masked), v.Ax
+    double acc = 0.0, dummy = 0.0;
+    for (int t = gtid; t < H.ns * nf; t += nthr) {
+      const int sid = t / nf, a = t % nf;
+      double y = side_sum(H, H.contrib, sid, a, nf);
+      if (H.masked[sid] || (sid == H.zero_side && a == 0)) y = 0.0;
+      H.Ax[t] = y;
+      acc += vnew[t] * y;
+    }
+    block_sum2(acc, dummy, ws);
+    if (threadIdx.x == 0) { redB[2 * blockIdx.x] = acc; redB[2 * blockIdx.x + 1] = 0.0; }
+    if (!grid_barrier(H, bar)) return;
+    double vz, unused;
+    grid_total2(redB, vz, unused, ws);
+    if (fabs(vz) <= 0.0) {
+      if (leader) { H.flags[F_STATUS] |= ST_BREAKDOWN; H.flags[F_DONE] = 1; H.flags[F_ITER] = it; }
+      return;
+    }
+    const double om = rz1 / vz;
+    // C: lambda += omega V, R -= omega Ax, Pr = P^{-1} R, r.r and r.Pr
+    double rr = 0.0, rz = 0.0;
+    if (H.precond == 1) {
+      for (int sid = gtid; sid < H.ns; sid += nthr) {
+        double r[kMaxND * kMaxND];
+        for (int a = 0; a < nf; ++a) {
+          const size_t g = (size_t)sid * nf + a;
+          H.lam[g] = H.lam[g] + om * vnew[g];
+          H.R[g] = H.R[g] - om * H.Ax[g];
+          r[a] = H.R[g];
+          rr += r[a] * r[a];
+        }
+        rz += apply_precond_side(H, sid, nf, r, H.Pr + (size_t)sid * nf);
+      }
+    } else {
+      for (int t = gtid; t < H.ns * nf; t += nthr) {
+        H.lam[t] = H.lam[t] + om * vnew[t];
+        const double r = H.R[t] - om * H.Ax[t];
+        H.R[t] = r;
+        double z = r;
+        if (H.precond == 2) z = H.masked[t / nf] ? 0.0 : H.pre[t] * r;
+        H.Pr[t] = z;
+        rr += r * r;
+        rz += r * z;
+      }
+    }
+    block_sum2(rr, rz, ws);
+    if (threadIdx.x == 0) { redC[2 * blockIdx.x] = rr; redC[2 * blockIdx.x + 1] = rz; }
+    if (!grid_barrier(H, bar)) return;
+    double trr, trz;
+    grid_total2(redC, trr, trz, ws);
+    ++it;
+    if (isnan(trr) || trr < abort2 || it >= H.max_iter) {
+      if (leader) {
+        H.flags[F_ITER] = it;
+        H.sc[S_RR] = trr;
+        if (isnan(trr)) H.flags[F_STATUS] |= ST_BREAKDOWN;
+        else if (trr < abort2) H.flags[F_CONV] = 1;
+        else H.flags[F_STATUS] |= ST_NOT_CONVERGED;
+        H.flags[F_DONE] = 1;
+      }
+      return;
+    }
+    beta = trz / rz1;
+    rz1 = trz;
+    par ^= 1;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------------
 // post processing (hdg_linear.f90:531-546) and PostProcessGradientHDG (elem_mat.f90:621-719)
 // ---------------------------------------------------------------------------------------------------
 template <int ND>
@@ -797,6 +964,10 @@ struct HdgState {
   cudaGraphExec_t chunk = nullptr;
   int chunk_iters = 0;
   size_t upper_stride = 0;        // doubles per element in the packed Smat
+  int coop_grid = 0;              // CTAs of the cooperative CG kernel (0: kernel-per-phase path only)
+  bool use_coop = true;           // cleared after a failed cooperative solve
+  unsigned* bar = nullptr;        // its grid barrier (count, generation)
+  double* lam_bak = nullptr;      // lambda at the start of a solve, for the fallback
   pic_hdg_status_t status{};
   std::vector<double> tau;
 };
@@ -856,6 +1027,25 @@ cudaError_t set_matvec_smem() {
   return e;
 }
 
+template <int ND>
+int coop_blocks_per_sm() {
+  int n = 0;
+  if (cudaFuncSetAttribute(k_cg_persistent<ND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)matvec_smem<ND>()) !=
+      cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_persistent<ND>, matvec_threads_t<ND>(), matvec_smem<ND>()) !=
+      cudaSuccess)
+    return 0;
+  return n;
+}
+
+template <int ND>
+cudaError_t launch_coop(HdgState* h, cudaStream_t s) {
+  void* args[] = {(void*)&h->D, (void*)&h->upper_stride, (void*)&h->bar};
+  return cudaLaunchCooperativeKernel((const void*)k_cg_persistent<ND>, dim3(h->coop_grid), dim3(matvec_threads_t<ND>()),
+                                     args, matvec_smem<ND>(), s);
+}
+
 // CG iteration `parity`: V_old = V[parity], V_new = V[1 - parity]
 int launch_iteration(HdgState* h, cudaStream_t s, int parity) {
   const int nf = h->nf;
@@ -895,6 +1085,7 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
     return fail(PIC_ERR_INVALID_ARGUMENT, "pic_hdg_t: missing array");
   if (g->precond_type < 0 || g->precond_type > 2) return fail(PIC_ERR_INVALID_ARGUMENT, "PrecondType must be 0, 1 or 2");
   if (g->max_iter_cg < 1 || !(g->eps_cg > 0.0)) return fail(PIC_ERR_INVALID_ARGUMENT, "MaxIterCG/epsCG");
+  if (g->cg_kernel < 0 || g->cg_kernel > 2) return fail(PIC_ERR_INVALID_ARGUMENT, "cg_kernel must be 0, 1 or 2");
   if (g->n_dirichlet < 0 || (g->n_dirichlet > 0 && !g->dirichlet_sides))
     return fail(PIC_ERR_INVALID_ARGUMENT, "dirichlet_sides");
   const int ns = g->n_sides;
@@ -982,7 +1173,12 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
   rc = rc ? rc : c->alloc(&D.contrib, (size_t)6 * nf * ne);
   rc = rc ? rc : c->alloc(&D.U, (size_t)nv * ne);
   const int nred = std::max((int)((nsf + kRedThreads - 1) / kRedThreads), 1);
-  rc = rc ? rc : c->alloc(&D.red, (size_t)2 * nred);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  rc = rc ? rc : c->alloc(&D.red, (size_t)std::max(2 * nred, 4 * 8 * std::max(sms, 1)));
+  rc = rc ? rc : c->alloc(&h->bar, 2);
+  rc = rc ? rc : c->alloc(&h->lam_bak, nsf);
   rc = rc ? rc : c->alloc(&D.sc, 8);
   rc = rc ? rc : c->alloc(&D.flags, 8);
   if (g->n_dirichlet > 0) {
@@ -1027,6 +1223,18 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
     cudaError_t ea = cudaSuccess;
     HDG_DISPATCH(nd, (ea = set_matvec_smem<ND>()));
     CUDA_CHECK_HDG(ea);
+    // the cooperative CG kernel: as many CTAs as can be resident at once (at most 8 per SM)
+    int coop = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (coop) {
+      HDG_DISPATCH(nd, (per_sm = coop_blocks_per_sm<ND>()));
+      h->coop_grid = std::min(per_sm, 8) * sms;
+    }
+    cudaGetLastError();
+    // auto = the graph of three kernels per iteration: on GB300 the cooperative form measured slower
+    // (8^3, N=3: 41 us per iteration with 2 CTAs/SM, 81 us with 4, against 34 us) -- the grid barriers
+    // cost more than the kernel boundaries of a replayed graph
+    h->use_coop = h->coop_grid > 0 && g->cg_kernel == 2;
   }
   int fl[8];
   CUDA_CHECK_HDG(cudaMemcpyAsync(fl, D.flags, sizeof(fl), cudaMemcpyDeviceToHost, s));
@@ -1079,16 +1287,44 @@ int hdg_solve_device(pic_ctx_t* c, const double* ps_dev, const double* resu_host
   k_set_dirichlet<<<(nd_t + 255) / 256, 256, 0, s>>>(D, h->dir_vals, h->dir_sides, h->n_dir, nf); ++n;
   HDG_DISPATCH(h->nd, (k_rhs<ND><<<D.ne, 128, 0, s>>>(D, h->T, ps_dev, resu_dev))); ++n;
   k_rhs_face<<<(D.ns * nf + 255) / 256, 256, 0, s>>>(D, nf); ++n;
-  cudaMemsetAsync(D.flags, 0, sizeof(int) * 8, s);
-  cudaMemsetAsync(D.V0, 0, sizeof(double) * (size_t)D.ns * nf, s);    // V_old of the first iteration
-  HDG_DISPATCH(h->nd, (k_matvec<ND, false><<<D.ne, matvec_threads_t<ND>(), matvec_smem<ND>(), s>>>(
-                           D, D.lam, nullptr, nullptr, h->upper_stride))); ++n;
-  k_gather<0><<<side_blocks(h), kRedThreads, 0, s>>>(D, nullptr, nf); ++n;
-  k_update<true><<<update_blocks(h), kRedThreads, 0, s>>>(D, nullptr, nf); ++n;
-  cudaError_t err = cudaGetLastError();
+  // EvalResidual and the first preconditioner application
+  auto cg_start = [&]() {
+    cudaMemsetAsync(D.flags, 0, sizeof(int) * 8, s);
+    cudaMemsetAsync(D.V0, 0, sizeof(double) * (size_t)D.ns * nf, s);    // V_old of the first iteration
+    HDG_DISPATCH(h->nd, (k_matvec<ND, false><<<D.ne, matvec_threads_t<ND>(), matvec_smem<ND>(), s>>>(
+                             D, D.lam, nullptr, nullptr, h->upper_stride))); ++n;
+    k_gather<0><<<side_blocks(h), kRedThreads, 0, s>>>(D, nullptr, nf); ++n;
+    k_update<true><<<update_blocks(h), kRedThreads, 0, s>>>(D, nullptr, nf); ++n;
+  };
+  cudaError_t err = cudaMemcpyAsync(h->lam_bak, D.lam, sizeof(double) * (size_t)D.ns * nf, cudaMemcpyDeviceToDevice, s);
+  if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
+  cg_start();
+  err = cudaGetLastError();
   if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
   int fl[8] = {0};
-  const int max_chunks = (D.max_iter + h->chunk_iters - 1) / h->chunk_iters + 1;
+  bool coop_done = false;
+  if (h->coop_grid > 0 && h->use_coop) {
+    // the whole CG in one cooperative launch; on a launch error or a barrier timeout: restore lambda
+    // and run the kernel-per-phase path below
+    cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), s);
+    HDG_DISPATCH(h->nd, (err = launch_coop<ND>(h, s)));
+    if (err == cudaSuccess) {
+      ++n;
+      err = cudaMemcpyAsync(fl, D.flags, sizeof(fl), cudaMemcpyDeviceToHost, s);
+      if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+      if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
+      coop_done = fl[F_DONE] && !fl[F_BARRIER];
+    } else {
+      cudaGetLastError();
+    }
+    if (!coop_done) {
+      h->use_coop = false;
+      err = cudaMemcpyAsync(D.lam, h->lam_bak, sizeof(double) * (size_t)D.ns * nf, cudaMemcpyDeviceToDevice, s);
+      if (err != cudaSuccess) return fail(PIC_ERR_CUDA, cudaGetErrorString(err));
+      cg_start();
+    }
+  }
+  const int max_chunks = coop_done ? 0 : (D.max_iter + h->chunk_iters - 1) / h->chunk_iters + 1;
   for (int ch = 0; ch < max_chunks; ++ch) {
     if (h->chunk) { err = cudaGraphLaunch(h->chunk, s); n += 3 * h->chunk_iters; }
     else n += launch_chunk(h, s, h->chunk_iters);

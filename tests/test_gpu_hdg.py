@@ -210,3 +210,18 @@ def test_hdg_rejects_bad_input(gpu_lib):
         loop.hdg_init(h)                                        # twice
     assert e.value.code == 5
     loop.close()
+
+
+def test_cooperative_cg_matches_graph_cg(gpu_lib, oracle_lib):
+    """cg_kernel = 2 (one cooperative kernel with grid barriers) gives the solution of the default path."""
+    m = build_box_mesh(4, 4, 4, 3, hi=(L2PI, L2PI, L2PI), perturb=0.05)
+    h = build_hdg_mesh(m)
+    resu = source_105(m.elem_xgp).reshape(m.n_elems, -1)
+    out = {}
+    for k in (1, 2):
+        loop = _loop(m)
+        loop.hdg_init(h, precond_type=2, eps_cg=1e-12, max_iter_cg=10000, cg_kernel=k)
+        out[k] = loop.hdg_solve(resu)
+        loop.close()
+    assert out[2][2]["converged"] == 1 and abs(out[1][2]["iterations"] - out[2][2]["iterations"]) <= 2
+    assert _rel(out[2][0], out[1][0]) <= 1e-9 and _rel(out[2][1], out[1][1]) <= 1e-9
