@@ -225,3 +225,26 @@ def test_cooperative_cg_matches_graph_cg(gpu_lib, oracle_lib):
         loop.close()
     assert out[2][2]["converged"] == 1 and abs(out[1][2]["iterations"] - out[2][2]["iterations"]) <= 2
     assert _rel(out[2][0], out[1][0]) <= 1e-9 and _rel(out[2][1], out[1][1]) <= 1e-9
+
+
+def test_self_consistent_step_between_electrodes(gpu_lib, oracle_lib):
+    """Reflective particle walls at x = 0, 1 that are grounded electrodes (Dirichlet phi = 0), periodic y/z:
+    Deposition -> HDG -> push -> TriaTracking with wall reflections, against the oracle."""
+    mesh = build_box_mesh(4, 4, 4, 2, bc=("reflective", "periodic", "periodic"))
+    w = workloads.plasma_wave(mesh=mesh, n_particles=3000, T_eV=2000.0, seed=8, dt=2e-10)
+    h = build_hdg_mesh(mesh)                                  # x faces: Dirichlet, lambda = 0
+    assert len(h.dirichlet_sides) == 2 * 16
+    loop = ParticleLoop(w.config(), w.mesh)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    loop.hdg_init(h, precond_type=1, eps_cg=1e-10, relative=True, max_iter_cg=10000, solve_in_step=True)
+    PSg = np.zeros((mesh.n_elems, mesh.n_dof, 4))
+    loop.time_step(w.dt, 5, PSg)
+    g = loop.download_particles()
+    stg = loop.status()
+    loop.close()
+    st, PS = _oracle_hdg_steps(w, h, 5, precond=1)
+    assert stg["error_word"] == 0 and st.inside.all()
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.max(np.abs(g["part_state"][:, :3] - st.part_state[:, :3])) <= 1e-12
+    assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-9
+    assert (np.sign(st.part_state[:, 3]) != np.sign(w.part_state[:, 3])).sum() > 20     # wall reflections
