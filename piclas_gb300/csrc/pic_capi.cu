@@ -442,8 +442,13 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       const bool wall = bc == 1 || bc == 2;
       if (wall ? nb != 0 : (nb < 1 || nb > ne))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_nb_elem must be 1..nElems, or 0 exactly at open/reflective sides"));
-      if (wall && cfg->deposition != PIC_DEPO_CVWM)
-        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "open/reflective particle boundaries need cell_volweight_mean"));
+      // shape_function near walls: no images, the kernel ends at the wall (calcSfSource with
+      // NbrOfPeriodicSFCases = 0); the reference's 3D shape function takes 0 or 3 periodic vectors
+      if (wall && !(cfg->deposition == PIC_DEPO_CVWM ||
+                    (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION && m->n_periodic_vectors == 0)))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT,
+                         "open/reflective particle boundaries need cell_volweight_mean, or shape_function on a mesh "
+                         "without periodic sides"));
       if (wall && cfg->tracking == PIC_TRACK_REFMAPPING && (m->n_periodic_vectors > 0 || !m->elem_to_bc_sides))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT,
                          "RefTracking with walls needs a mesh without periodic sides and elem_to_bc_sides"));

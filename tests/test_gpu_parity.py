@@ -639,3 +639,32 @@ def test_reftracking_walls_rejected_where_unsupported(gpu_lib):
     w.mesh.elem_to_bc_sides = None
     with pytest.raises(PicError):
         ParticleLoop(w.config(), w.mesh)                      # no BC-element lists
+
+
+# ---- shape_function next to walls (no periodic sides: no images, the kernel ends at the walls) ---------
+@pytest.mark.parametrize("tracking,bc", [(capi.PIC_TRACK_REFMAPPING, ("reflective",) * 3),
+                                         (capi.PIC_TRACK_TRIA, ("reflective", "open", "reflective"))])
+def test_shape_function_with_walls_fp64_bitexact(gpu_lib, oracle_lib, tracking, bc):
+    mesh = build_box_mesh(5, 5, 5, 2, bc=bc)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=3000, T_eV=2000.0, seed=35, dt=2e-10)
+    w.tracking = tracking
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION
+    w.sf_radius = 1.5 / 5
+    g = _run_gpu(w, 8)
+    st, PS = _run_oracle(oracle_lib, w, 8)
+    assert np.array_equal(g["inside"], st.inside) and np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0
+    gm = _run_gpu(w, 8, precision=capi.PIC_PREC_MIXED)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-6
+
+
+def test_shape_function_with_walls_needs_a_nonperiodic_mesh(gpu_lib):
+    mesh = build_box_mesh(4, 4, 4, 2, bc=("reflective", "open", "periodic"))
+    w = workloads.plasma_wave(mesh=mesh, n_particles=100, seed=36)
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION
+    w.sf_radius = 1.5 / 4
+    with pytest.raises(PicError) as e:
+        ParticleLoop(w.config(), w.mesh)
+    assert e.value.code == 1
