@@ -103,6 +103,13 @@ typedef struct pic_config_t {
   double  sf_radius;            /* PIC-shapefunction-radius                             */
   int32_t sf_alpha;             /* PIC-shapefunction-alpha (>=2)                        */
   int32_t sort_interval;        /* re-sort particles by element every k steps (0: never) */
+  /* PIC-shapefunction-dimension (1, 2, 3; 0 = 3), -direction (1D: the direction of the kernel, 2D: the
+   * direction in which it is constant) and -3D-deposition (1: charge over the volume, 0: over the line /
+   * area); 1D and 2D kernels with plain shape_function only (InitShapeFunctionDimensionalty,
+   * pic_depo_shapefunction_tools.f90:1131-1294) */
+  int32_t sf_dim;
+  int32_t sf_dir;
+  int32_t sf_depo3d;
 } pic_config_t;
 
 /* Mesh arrays as the reference holds them after init (NGeo = 1 hexahedra).

@@ -979,16 +979,77 @@ static int deposit_cvwm(const pic_config_t* cfg, const pic_mesh_t* m, orc_partic
 
 /* w_sf for the 3D shape function, pic_depo_shapefunction_tools.f90:1243-1246 with beta()
  * from pic_depo_tools.f90:491-511 */
-static double sf_w(double r_sf, int alpha) {
+/* shape-function dimension (InitShapeFunctionDimensionalty, pic_depo_shapefunction_tools.f90:1131-1294):
+ * dim 1: kernel along dir; dim 2: kernel in d1, d2, constant along dir (0-based directions) */
+typedef struct { int dim, dir, d1, d2; } sf_geom_t;
+static sf_geom_t sf_geom(const pic_config_t* cfg) {
+  sf_geom_t g;
+  g.dim = cfg->sf_dim ? cfg->sf_dim : 3;
+  g.dir = (cfg->sf_dir >= 1 && cfg->sf_dir <= 3 ? cfg->sf_dir : 1) - 1;
+  g.d1 = (g.dir == 1) ? 0 : 1;             /* dim_sf_dir1 = MERGE(1,2,dim_sf_dir.EQ.2) */
+  g.d2 = (g.dir == 2) ? 0 : 2;             /* dim_sf_dir2 = MERGE(1,3,dim_sf_dir.EQ.3) */
+  return g;
+}
+/* SFRadius2 and SFNorm (pic_depo_shapefunction_tools.f90:997-1058) */
+static double sf_radius2(const sf_geom_t* g, const double v[3]) {
+  if (g->dim == 1) return v[g->dir] * v[g->dir];
+  if (g->dim == 2) return v[g->d1] * v[g->d1] + v[g->d2] * v[g->d2];
+  return (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+}
+static double sf_norm(const sf_geom_t* g, const double v[3]) {
+  if (g->dim == 1) return fabs(v[g->dir]);
+  if (g->dim == 2) return sqrt(v[g->d1] * v[g->d1] + v[g->d2] * v[g->d2]);
+  return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+}
+
+static double sf_w(const pic_config_t* cfg, const pic_mesh_t* m, double r_sf, int alpha) {
   const double PI = acos(-1.0);
+  const sf_geom_t g = sf_geom(cfg);
+  const int depo3d = cfg->sf_dim == 0 || cfg->sf_depo3d;
+  double ext[3];
+  for (int d = 0; d < 3; ++d) ext[d] = m->xmax_glob[d] - m->xmin_glob[d];
+  if (g.dim == 1) {
+    double dimFactor = (g.dir == 0) ? ext[1] * ext[2] : (g.dir == 1) ? ext[0] * ext[2] : ext[0] * ext[1];
+    double a = tgamma((double)alpha + 1.5);
+    double b = sqrt(PI) * r_sf * tgamma((double)(alpha + 1));
+    return depo3d ? a / (b * dimFactor) : a / b;
+  }
+  if (g.dim == 2) {
+    double dimFactor = ext[g.dir];
+    return depo3d ? ((double)alpha + 1.0) / (PI * (r_sf * r_sf) * dimFactor) : ((double)alpha + 1.0) / (PI * (r_sf * r_sf));
+  }
   double BetaFac = tgamma(1.5) * tgamma((double)alpha + 1.0) / tgamma(1.5 + ((double)alpha + 1.0));
   return 1.0 / (2.0 * BetaFac * (double)alpha + 2.0 * BetaFac) * ((double)alpha + 1.0) / (PI * (r_sf * r_sf * r_sf));
 }
 
-/* depoChargeOnDOFsSF, pic_depo_shapefunction_tools.f90:292-422 (dim_sf = 3) */
+/* GetPartPosShifted (pic_depo_shapefunction_tools.f90:1061-1124) for periodic case ic (0-based) with
+ * PeriodicSFCaseMatrix (pic_depo.f90:865-888); dims 1 and 2 on a box with one periodic vector per axis */
+static void sf_shifted(const sf_geom_t* g, const pic_mesh_t* m, int ic, const double P[3], double Ps[3]) {
+#define PV(i, k) m->periodic_vectors[3 * (k) + (i)]
+  if (g->dim == 1) {
+    const double c = (double)(1 - ic);
+    Ps[0] = Ps[1] = Ps[2] = 0.0;
+    Ps[g->dir] = P[g->dir] + c * PV(g->dir, g->dir);
+  } else if (g->dim == 2) {
+    const double c1 = (double)(1 - ic / 3), c2 = (double)(1 - ic % 3);
+    const int v1 = g->d1, v2 = g->d2;          /* dim_periodic_vec1/2 for three periodic vectors */
+    Ps[g->dir] = P[g->dir];
+    Ps[g->d1] = P[g->d1] + c1 * PV(g->d1, v1);
+    Ps[g->d2] = P[g->d2] + c1 * PV(g->d2, v1);
+    Ps[g->d1] = Ps[g->d1] + c2 * PV(g->d1, v2);
+    Ps[g->d2] = Ps[g->d2] + c2 * PV(g->d2, v2);
+  } else {
+    const double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);
+    for (int d = 0; d < 3; ++d) Ps[d] = P[d] + c1 * PV(d, 0) + c2 * PV(d, 1) + c3 * PV(d, 2);
+  }
+#undef PV
+}
+
+/* depoChargeOnDOFsSF, pic_depo_shapefunction_tools.f90:292-422 */
 static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], const double Fac[4],
                                    double r_sf, double r2_sf, double r2_sf_inv, double* PS, uint8_t* done) {
   const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const sf_geom_t g = sf_geom(cfg);
   memset(done, 0, (size_t)m->n_elems);
   int kmax = (int)ceil((P[0] + r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0]);
   int kmin = (int)floor((P[0] - r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0] + 1);
@@ -996,6 +1057,15 @@ static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m,
   int lmin = (int)floor((P[1] - r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1] + 1);
   int mmax = (int)ceil((P[2] + r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2]);
   int mmin = (int)floor((P[2] - r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2] + 1);
+  /* 1D/2D: every background cell across the directions without kernel (:346-377) */
+  if (g.dim < 3) {
+    int full[3] = {0, 0, 0};
+    if (g.dim == 2) full[g.dir] = 1;
+    else { full[0] = full[1] = full[2] = 1; full[g.dir] = 0; }
+    if (full[0]) { kmin = 1; kmax = m->fibgm_imax[0]; }
+    if (full[1]) { lmin = 1; lmax = m->fibgm_imax[1]; }
+    if (full[2]) { mmin = 1; mmax = m->fibgm_imax[2]; }
+  }
   if (kmax > m->fibgm_imax[0]) kmax = m->fibgm_imax[0];
   if (kmin < 1) kmin = 1;
   if (lmax > m->fibgm_imax[1]) lmax = m->fibgm_imax[1];
@@ -1011,16 +1081,16 @@ static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m,
           int e = m->fibgm_element[off + q];
           if (done[e - 1]) continue;
           const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
-          double v0 = P[0] - b[0], v1 = P[1] - b[1], v2 = P[2] - b[2];
-          if (sqrt(v0 * v0 + v1 * v1 + v2 * v2) > (r_sf + m->elem_radius[e - 1])) continue;
+          const double vb[3] = {P[0] - b[0], P[1] - b[1], P[2] - b[2]};
+          if (sf_norm(&g, vb) > (r_sf + m->elem_radius[e - 1])) continue;
           const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
           double* ps = &PS[(size_t)(e - 1) * ndof * 4];
           for (int mz = 0; mz <= N; ++mz)
             for (int l = 0; l <= N; ++l)
               for (int k = 0; k <= N; ++k) {
                 int r = mz * n1 * n1 + l * n1 + k;
-                double d0 = P[0] - xg[(size_t)r * 3], d1 = P[1] - xg[(size_t)r * 3 + 1], d2 = P[2] - xg[(size_t)r * 3 + 2];
-                double radius2 = (d0 * d0 + d1 * d1) + d2 * d2;
+                const double dv[3] = {P[0] - xg[(size_t)r * 3], P[1] - xg[(size_t)r * 3 + 1], P[2] - xg[(size_t)r * 3 + 2]};
+                double radius2 = sf_radius2(&g, dv);
                 if (radius2 <= r2_sf) {
                   double S = 1.0 - r2_sf_inv * radius2;
                   double S1 = S * S;
@@ -1090,9 +1160,11 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
   const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
   const size_t nps = (size_t)m->n_elems * ndof * 4;
   const double r_sf = cfg->sf_radius, r2_sf = r_sf * r_sf, r2_sf_inv = 1.0 / r2_sf;
-  const double w_sf = sf_w(r_sf, cfg->sf_alpha);
+  const double w_sf = sf_w(cfg, m, r_sf, cfg->sf_alpha);
   int nt = nthreads > 0 ? nthreads : 1;
-  int nCases = (m->n_periodic_vectors > 0) ? 27 : 0;
+  const sf_geom_t gsf = sf_geom(cfg);
+  /* NbrOfPeriodicSFCases = 3**dim_sf with periodic vectors, else 0 (pic_depo.f90:849-861) */
+  int nCases = (m->n_periodic_vectors > 0) ? (gsf.dim == 1 ? 3 : gsf.dim == 2 ? 9 : 27) : 0;
   double* acc = PS;
   if (nt > 1) { acc = (double*)calloc(nps * (size_t)nt, sizeof(double)); if (!acc) return 1; }
   uint8_t* doneAll = (uint8_t*)malloc((size_t)m->n_elems * (size_t)nt);
@@ -1141,13 +1213,9 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
         } else {
           for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * w_sf;
         }
-        for (int ic = 0; ic < 27; ++ic) {
-          /* PeriodicSFCaseMatrix, pic_depo.f90:869-879: case = 9a + 3b + c -> (1-a, 1-b, 1-c) */
-          double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);
+        for (int ic = 0; ic < nCases; ++ic) {
           double Ps[3];
-          for (int d = 0; d < 3; ++d)
-            Ps[d] = s[d] + c1 * m->periodic_vectors[0 * 3 + d] + c2 * m->periodic_vectors[1 * 3 + d] +
-                    c3 * m->periodic_vectors[2 * 3 + d];
+          sf_shifted(&gsf, m, ic, s, Ps);
           depo_charge_on_dofs_sf(cfg, m, Ps, Fac, r_sf_p, r2_sf_p, r2_sf_inv_p, my, done);
         }
       } else {

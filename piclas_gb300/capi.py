@@ -46,7 +46,7 @@ class PicConfig(C.Structure):
         ("charge", C.c_double * PIC_MAX_SPECIES), ("mass", C.c_double * PIC_MAX_SPECIES),
         ("mpf", C.c_double * PIC_MAX_SPECIES), ("external_field", C.c_double * 6),
         ("refmapping_eps", C.c_double), ("sf_radius", C.c_double), ("sf_alpha", C.c_int32),
-        ("sort_interval", C.c_int32),
+        ("sort_interval", C.c_int32), ("sf_dim", C.c_int32), ("sf_dir", C.c_int32), ("sf_depo3d", C.c_int32),
     ]
 
 
@@ -108,7 +108,8 @@ def u8ptr(a: np.ndarray):
 
 def make_config(n_dg: int, tracking: int, deposition: int, precision: int, species, max_particles: int,
                 external_field=(0.0,) * 6, refmapping_eps: float = 1e-4, sf_radius: float = 0.0,
-                sf_alpha: int = 2, sort_interval: int = 0) -> PicConfig:
+                sf_alpha: int = 2, sort_interval: int = 0, sf_dim: int = 3, sf_dir: int = 1,
+                sf_depo3d: bool = True) -> PicConfig:
     """species: list of (charge, mass, mpf)."""
     cfg = PicConfig()
     cfg.n_dg = n_dg
@@ -127,6 +128,9 @@ def make_config(n_dg: int, tracking: int, deposition: int, precision: int, speci
     cfg.sf_radius = sf_radius
     cfg.sf_alpha = sf_alpha
     cfg.sort_interval = sort_interval
+    cfg.sf_dim = sf_dim
+    cfg.sf_dir = sf_dir
+    cfg.sf_depo3d = int(bool(sf_depo3d))
     return cfg
 
 

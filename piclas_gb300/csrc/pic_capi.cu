@@ -86,8 +86,41 @@ double sf_weight(double r, int alpha) {
   return 1.0 / (2.0 * beta * (double)alpha + 2.0 * beta) * ((double)alpha + 1.0) / (PI * (r * r * r));
 }
 
+// 1D / 2D shape-function weight (InitShapeFunctionDimensionalty, pic_depo_shapefunction_tools.f90:1162-1232):
+// the kernel normalised along its line / over its area, divided by the extent of the remaining
+// directions when the charge is spread over the volume (PIC-shapefunction-3D-deposition)
+double sf_weight_dim(const pic_config_t* cfg, const pic_mesh_t* m, double r, int alpha) {
+  const int dim = cfg->sf_dim ? cfg->sf_dim : 3, dir = cfg->sf_dir - 1;
+  if (dim == 3) return sf_weight(r, alpha);
+  const double PI = std::acos(-1.0);
+  double ext[3];
+  for (int d = 0; d < 3; ++d) ext[d] = m->xmax_glob[d] - m->xmin_glob[d];
+  if (dim == 1) {
+    const double dimFactor = (dir == 0) ? ext[1] * ext[2] : (dir == 1) ? ext[0] * ext[2] : ext[0] * ext[1];
+    const double a = std::tgamma((double)alpha + 1.5);
+    const double b = std::sqrt(PI) * r * std::tgamma((double)(alpha + 1));
+    return cfg->sf_depo3d ? a / (b * dimFactor) : a / b;
+  }
+  return cfg->sf_depo3d ? ((double)alpha + 1.0) / (PI * (r * r) * ext[dir]) : ((double)alpha + 1.0) / (PI * (r * r));
+}
+
+// directions in which a 1D/2D shape function has its kernel (the others are zeroed in the DOF and particle
+// coordinates the gather reads, so the kernel sees SFRadius2, pic_depo_shapefunction_tools.f90:1029-1058)
+void sf_kernel_dirs(const pic_config_t* cfg, bool keep[3]) {
+  const int dim = cfg->sf_dim ? cfg->sf_dim : 3, dir = cfg->sf_dir - 1;
+  for (int d = 0; d < 3; ++d) keep[d] = dim == 3 || (dim == 1 ? d == dir : d != dir);
+}
+
 int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   if (!cfg || !m) return fail(PIC_ERR_INVALID_ARGUMENT, "null config or mesh");
+  if (cfg->sf_dim < 0 || cfg->sf_dim > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "sf_dim must be 1, 2 or 3 (0 = 3)");
+  if (cfg->sf_dim == 1 || cfg->sf_dim == 2) {
+    if (cfg->deposition != PIC_DEPO_SHAPE_FUNCTION)
+      return fail(PIC_ERR_INVALID_ARGUMENT, "1D/2D shape functions are built for plain shape_function");
+    if (cfg->sf_dir < 1 || cfg->sf_dir > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "sf_dir must be 1..3");
+    if (m->n_periodic_vectors != 0 && m->n_periodic_vectors != 3)
+      return fail(PIC_ERR_INVALID_ARGUMENT, "1D/2D shape functions need a mesh with no or three periodic vectors");
+  }
   if (cfg->n_dg < 1 || cfg->n_dg > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg must be 1..4");
   if (cfg->tracking != PIC_TRACK_TRIA && cfg->tracking != PIC_TRACK_REFMAPPING)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown tracking method");
@@ -138,7 +171,8 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
 // pairs whose bounding box lies within R of at least one DOF of the target.  Enumerated from
 // the FIBGM cells covering the target's DOF box grown by R, with cell indices outside the grid
 // wrapped onto their periodic image.
-int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& dofc) {
+int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& dofc, const std::vector<double>& sfx,
+                   const bool kdir[3]) {
   const int ne = m->n_elems, nd = c->nd;
   const double R = c->sf_rmax;
   auto R2src = [&](int s) { const double r = c->adaptive ? m->sf_elem_radius[s] : c->cfg.sf_radius; return r * r; };
@@ -151,7 +185,7 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
         lo = std::min(lo, v); hi = std::max(hi, v);
       }
       for (int r = 0; r < nd; ++r) {
-        double v = m->elem_xgp[((size_t)e * nd + r) * 3 + d];
+        double v = sfx[((size_t)e * nd + r) * 3 + d];
         dl = std::min(dl, v); dh = std::max(dh, v);
       }
       bmin[e * 3 + d] = lo; bmax[e * 3 + d] = hi; dmin[e * 3 + d] = dl; dmax[e * 3 + d] = dh;
@@ -178,6 +212,7 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
   for (int e = 0; e < ne; ++e) {
     int clo[3], chi[3];
     for (int d = 0; d < 3; ++d) {
+      if (!kdir[d]) { clo[d] = 1; chi[d] = imax[d]; continue; }   // no kernel along d: every cell, no image
       clo[d] = (int)std::floor((dmin[e * 3 + d] - R - m->xmin_glob[d]) / m->fibgm_deltas[d]) + 1;
       chi[d] = (int)std::ceil((dmax[e * 3 + d] + R - m->xmin_glob[d]) / m->fibgm_deltas[d]);
     }
@@ -214,7 +249,8 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
       for (int r = 0; r < nd && !keep; ++r) {
         double d2 = 0.0;
         for (int d = 0; d < 3; ++d) {
-          const double p = m->elem_xgp[((size_t)e * nd + r) * 3 + d];
+          if (!kdir[d]) continue;
+          const double p = sfx[((size_t)e * nd + r) * 3 + d];
           const double lo = bmin[s * 3 + d] + shv[d], hi = bmax[s * 3 + d] + shv[d];
           const double q = p < lo ? lo - p : (p > hi ? p - hi : 0.0);
           d2 += q * q;
@@ -234,7 +270,7 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
     double r2 = 0.0;
     for (int r = 0; r < nd; ++r) {
       double q = 0.0;
-      for (int d = 0; d < 3; ++d) { double v = m->elem_xgp[((size_t)e * nd + r) * 3 + d] - dofc[(size_t)e * 3 + d]; q += v * v; }
+      for (int d = 0; d < 3; ++d) { double v = sfx[((size_t)e * nd + r) * 3 + d] - dofc[(size_t)e * 3 + d]; q += v * v; }
       r2 = std::max(r2, q);
     }
     drad[e] = (float)(std::sqrt(r2) * (1.0 + 1e-6));
@@ -553,6 +589,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     return bail(rc);
   c->M = DevMesh{ne, d_xcl, d_dxcl, d_bary, d_xez, d_slen, d_rad, d_eps1, d_snb, d_sinfo, d_ecan, d_nvol, d_exgp,
                  d_fn, d_fo, d_fe, d_xclr};
+  c->M.sf_xgp = d_exgp;
   if (!bc_e2b.empty()) {
     int* d_be = nullptr;
     double* d_bg = nullptr;
@@ -595,7 +632,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   if (c->sf) {
     // the largest radius (adaptive: the per-element radii bound the searches; exact per-particle radii in the kernels)
     k.sf_r = c->sf_rmax; k.sf_r2 = c->sf_rmax * c->sf_rmax; k.sf_r2_inv = 1.0 / k.sf_r2;
-    k.sf_alpha = cfg->sf_alpha; k.sf_w = c->cc ? 1.0 : sf_weight(cfg->sf_radius, cfg->sf_alpha);   // cc: Fac = q MPF (v,1), normalised later
+    k.sf_alpha = cfg->sf_alpha;
+    k.sf_w = c->cc ? 1.0 : sf_weight_dim(cfg, m, cfg->sf_radius, cfg->sf_alpha);   // cc: Fac = q MPF (v,1), normalised later
+    bool keep[3];
+    sf_kernel_dirs(cfg, keep);
+    for (int d = 0; d < 3; ++d) k.sf_keep[d] = keep[d] ? 1 : 0;
   }
   if (upload_consts(k) != cudaSuccess) return bail(fail(PIC_ERR_CUDA, "constant upload"));
   c->k = k;
@@ -616,14 +657,26 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   // the reorder buffer shares the auxiliary arrays (LastPartPos, field) of P
   c->Q.lx = c->P.lx; c->Q.ly = c->P.ly; c->Q.lz = c->P.lz; c->Q.field = c->P.field;
   if (c->sf) {
+    // DOF coordinates the gather reads: the kernel directions only (all three for a 3D shape function)
+    bool keep[3];
+    sf_kernel_dirs(cfg, keep);
+    std::vector<double> sfx(exgp);
+    if (!(keep[0] && keep[1] && keep[2])) {
+      for (size_t q = 0; q < (size_t)ne * nd; ++q)
+        for (int d = 0; d < 3; ++d)
+          if (!keep[d]) sfx[q * 3 + d] = 0.0;
+      double* d_sfx = nullptr;
+      if ((rc = upload(c, &d_sfx, sfx))) return bail(rc);
+      c->M.sf_xgp = d_sfx;
+    }
     std::vector<double> dofc((size_t)ne * 3);
     for (int e = 0; e < ne; ++e)
       for (int d = 0; d < 3; ++d) {
         double lo = 1e300, hi = -1e300;
-        for (int r = 0; r < nd; ++r) { double v = exgp[((size_t)e * nd + r) * 3 + d]; lo = std::min(lo, v); hi = std::max(hi, v); }
+        for (int r = 0; r < nd; ++r) { double v = sfx[((size_t)e * nd + r) * 3 + d]; lo = std::min(lo, v); hi = std::max(hi, v); }
         dofc[(size_t)e * 3 + d] = 0.5 * (lo + hi);
       }
-    if ((rc = build_sf_lists(c, m, dofc))) return bail(rc);
+    if ((rc = build_sf_lists(c, m, dofc, sfx, keep))) return bail(rc);
     const size_t cap = (size_t)std::max(cfg->max_particles, 1);
     if ((rc = c->alloc(&c->sfk.posf, cap * 4))) return bail(rc);
     if (c->mixed) {

@@ -40,6 +40,7 @@ struct Consts {
   double sf_r, sf_r2, sf_r2_inv, sf_w;
   int sf_alpha;
   int pv_dir[3];                               // periodic vector index per axis (-1: none)
+  int sf_keep[3];                              // 1D/2D shape function: 1 in the kernel directions
 };
 // one copy per translation unit; only pic_kernels.cu launches kernels that read it
 static __constant__ Consts c_k;
@@ -66,6 +67,8 @@ struct DevMesh {
   // RefTracking with walls: per element (ELEM_NBR_BCSIDES, first entry) or (-1,-1); per entry kBcGeo doubles
   const int* bc_e2b;
   const double* bc_geo;
+  // shape-function DOF coordinates: elem_xgp, or for a 1D/2D kernel its directions only (others zero)
+  const double* sf_xgp;
 };
 // one wall-side entry of a BC element: [0..2] BaseVectors0, [3..5] BaseVectors1, [6..8] BaseVectors2,
 // [9..11] SideNormVec (away from the domain), [12] SideDistance, [13] SideBCMetrics(BCSIDE_DISTANCE),

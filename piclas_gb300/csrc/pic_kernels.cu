@@ -580,7 +580,8 @@ __global__ void __launch_bounds__(256) k_sf_pack(DevParticles P, int* __restrict
   if (!valid) return;
   const int sp = P.species[i];
   const double qm = c_k.qm[sp];
-  const double x = P.x[i], y = P.y[i], z = P.z[i];
+  // 1D/2D shape function: the coordinates without kernel are zero, as in the DOF coordinates
+  const double x = c_k.sf_keep[0] ? P.x[i] : 0.0, y = c_k.sf_keep[1] ? P.y[i] : 0.0, z = c_k.sf_keep[2] ? P.z[i] : 0.0;
   const double* c = dofc + (size_t)e * 3;
   const float4 rel = make_float4((float)(x - __ldg(c)), (float)(y - __ldg(c + 1)), (float)(z - __ldg(c + 2)), 0.0f);
   reinterpret_cast<float4*>(K.posf)[slot] = rel;
@@ -627,7 +628,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh 
   double xg[3] = {0, 0, 0};
   float xgf[3] = {0, 0, 0};
   if (active) {
-    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
     xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
     xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
   }
@@ -717,7 +718,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh
   const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
   float xgf[3] = {0, 0, 0};
   if (active) {
-    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
     xgf[0] = (float)(__ldg(g) - cex); xgf[1] = (float)(__ldg(g + 1) - cey); xgf[2] = (float)(__ldg(g + 2) - cez);
   }
   const float R2 = (float)c_k.sf_r2, R2inv = (float)c_k.sf_r2_inv;
@@ -821,7 +822,7 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L
   double xg[3] = {0, 0, 0};
   float xgf[3] = {0, 0, 0};
   if (active) {
-    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
     xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
     xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
   }
@@ -990,7 +991,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
   double gd[4] = {0.0, 0.0, 0.0, 0.0};
   float gf[3] = {0.f, 0.f, 0.f};
   if (active) {
-    const double* g = M.elem_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
     const double gx = __ldg(g) - cex, gy = __ldg(g + 1) - cey, gz = __ldg(g + 2) - cez;
     gd[0] = gx; gd[1] = gy; gd[2] = gz;
     // B_g = 1 - |g|^2/R^2; adaptive: |g|^2 (the particle's own radius enters at each hit)
@@ -1258,7 +1259,7 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
           const int k = c_k.pv_dir[dd];
           sh[dd] = k >= 0 ? (double)L.t_shift[3 * q + dd] * c_k.pv[3 * k + dd] : 0.0;
         }
-        const double* g = M.elem_xgp + ((size_t)e * nd + d) * 3;
+        const double* g = M.sf_xgp + ((size_t)e * nd + d) * 3;
         const double gx = __ldg(g) - sh[0], gy = __ldg(g + 1) - sh[1], gz = __ldg(g + 2) - sh[2];
         const double wgt = __ldg(L.dof_w + (size_t)e * nd + d);
         if constexpr (!MIXED) { s_g[i][0] = gx; s_g[i][1] = gy; s_g[i][2] = gz; s_g[i][3] = wgt; }

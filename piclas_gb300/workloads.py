@@ -52,6 +52,9 @@ class Workload:
     external_field: tuple = (0.0,) * 6
     sf_radius: float = 0.0
     sf_alpha: int = 2
+    sf_dim: int = 3                 # PIC-shapefunction-dimension
+    sf_dir: int = 1                 # PIC-shapefunction-direction
+    sf_depo3d: bool = True          # PIC-shapefunction-3D-deposition
     info: dict = field(default_factory=dict)
 
     @property
@@ -63,7 +66,8 @@ class Workload:
         return capi.make_config(self.mesh.N, self.tracking, self.deposition, precision, self.species,
                                 max_particles if max_particles is not None else self.n,
                                 external_field=self.external_field, sf_radius=self.sf_radius,
-                                sf_alpha=self.sf_alpha, sort_interval=sort_interval)
+                                sf_alpha=self.sf_alpha, sort_interval=sort_interval, sf_dim=self.sf_dim,
+                                sf_dir=self.sf_dir, sf_depo3d=self.sf_depo3d)
 
 
 # --------------------------------------------------------------------------------------

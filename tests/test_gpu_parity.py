@@ -668,3 +668,18 @@ def test_shape_function_with_walls_needs_a_nonperiodic_mesh(gpu_lib):
     with pytest.raises(PicError) as e:
         ParticleLoop(w.config(), w.mesh)
     assert e.value.code == 1
+
+
+# ---- 1D and 2D shape functions -------------------------------------------------------------------------
+@pytest.mark.parametrize("dim,sf_dir,depo3d", [(1, 1, True), (1, 2, False), (2, 3, True), (2, 1, True)])
+def test_shape_function_1d_2d_against_oracle(gpu_lib, oracle_lib, dim, sf_dir, depo3d):
+    w = workloads.plasma_wave(n_cells=4, N=3, n_particles=3000, seed=41, T_eV=200.0)
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION
+    w.sf_radius, w.sf_alpha = 0.3, 4
+    w.sf_dim, w.sf_dir, w.sf_depo3d = dim, sf_dir, depo3d
+    g = _run_gpu(w, 4)
+    st, PS = _run_oracle(oracle_lib, w, 4)
+    assert np.array_equal(g["elem"], st.elem) and np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    gm = _run_gpu(w, 4, precision=capi.PIC_PREC_MIXED)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-6

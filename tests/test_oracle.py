@@ -316,3 +316,52 @@ def test_reftracking_walls_curved_mesh(oracle_lib):
     assert np.max(np.abs(ref.part_state[k, 2] - fold(xs[k, 2]))) < 1e-12
     assert np.max(np.abs(ref.part_state[k, 1] - y[k])) < 1e-12
     assert np.max(np.abs(ref.part_pos_ref[k])) <= 1.0 + 1e-9
+
+
+# ---- 1D and 2D shape functions (PIC-shapefunction-dimension / -direction) ---------------------------
+def _sf_dim_case(dim, sf_dir, n=400, seed=21, depo3d=True):
+    w = workloads.plasma_wave(n_cells=4, N=3, n_particles=n, seed=seed)
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION
+    w.sf_radius = 0.3
+    w.sf_alpha = 4
+    w.sf_dim, w.sf_dir, w.sf_depo3d = dim, sf_dir, depo3d
+    return w
+
+
+def test_sf_1d_single_particle_matches_the_analytic_kernel(oracle_lib):
+    from math import gamma, pi, sqrt
+    w = _sf_dim_case(1, 1, n=1)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS)
+    q = w.species[0][0] * w.species[0][2]
+    R, a = w.sf_radius, w.sf_alpha
+    wsf = gamma(a + 1.5) / (sqrt(pi) * R * gamma(a + 1)) / 1.0            # extent in y and z: 1 x 1
+    x0 = w.part_state[0, 0]
+    xg = w.mesh.elem_xgp.reshape(w.mesh.n_elems, -1, 3)[..., 0]
+    expect = np.zeros_like(xg)
+    for shift in (-1.0, 0.0, 1.0):                                        # the three periodic cases
+        d2 = (xg - (x0 + shift)) ** 2
+        expect += np.where(d2 <= R * R, (1.0 - d2 / (R * R)) ** a, 0.0) * wsf * q
+    assert np.allclose(PS[..., 3], expect, rtol=1e-12, atol=1e-12 * np.abs(expect).max())
+
+
+@pytest.mark.parametrize("dim,sf_dir", [(1, 1), (1, 3), (2, 1), (2, 2)])
+def test_sf_1d_2d_conserve_charge_and_are_constant_across(oracle_lib, dim, sf_dir):
+    w = _sf_dim_case(dim, sf_dir)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS)
+    total = w.n * w.species[0][0] * w.species[0][2]
+    assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - total) <= 2e-3 * abs(total)
+    # rho depends only on the kernel coordinates: equal at DOFs whose kernel coordinates are equal
+    xg = w.mesh.elem_xgp.reshape(-1, 3)
+    kdirs = [sf_dir - 1] if dim == 1 else [d for d in range(3) if d != sf_dir - 1]
+    key = np.round(xg[:, kdirs], 12)
+    rho = PS[..., 3].reshape(-1)
+    _, inv = np.unique(key, axis=0, return_inverse=True)
+    for k in range(inv.max() + 1):
+        v = rho[inv == k]
+        assert np.allclose(v, v[0], rtol=1e-11, atol=1e-11 * np.abs(rho).max())
