@@ -79,8 +79,10 @@ typedef enum pic_error_t {
 /* ---- option enums ------------------------------------------------------- */
 enum { PIC_TRACK_TRIA = 1, PIC_TRACK_REFMAPPING = 2 };     /* TrackingMethod           */
 /* PIC-Deposition-Type: cell_volweight_mean, shape_function, shape_function_cc (charge-corrected: each
- * particle's deposit scaled so that its quadrature integral is exactly q*MPF; periodic meshes),
- * shape_function_adaptive (as _cc with the radius of the particle's element, pic_mesh_t.sf_elem_radius) */
+ * particle's deposit scaled so that its quadrature integral is exactly q*MPF; with three periodic
+ * vectors over the 27 images, without any over the DOFs left inside the walls), shape_function_adaptive (as
+ * _cc with the radius of the particle's element, pic_mesh_t.sf_elem_radius; without periodic vectors only
+ * on the particle's element and the elements sharing a corner node with it) */
 enum { PIC_DEPO_CVWM = 1, PIC_DEPO_SHAPE_FUNCTION = 2, PIC_DEPO_SHAPE_FUNCTION_CC = 3,
        PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE = 4 };
 enum { PIC_PREC_FP64 = 0, PIC_PREC_MIXED = 1 };            /* arithmetic variant       */

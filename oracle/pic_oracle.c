@@ -1154,6 +1154,130 @@ static double total_charge_cc(const pic_config_t* cfg, const pic_mesh_t* m, cons
   return totalCharge;
 }
 
+/* ElemToElemMapping/ElemToElemInfo of particle_mesh_build.f90:1244-1380: for every element, the other
+ * elements sharing one of its unique corner nodes, in the order met when walking the corners (CGNS order)
+ * and, per node, the elements of NodeToElemInfo (ascending, :1150-1243).  off has n_elems + 1 entries. */
+static int build_elem_to_elem(const pic_mesh_t* m, int** off_out, int** info_out) {
+  const int ne = m->n_elems;
+  int nn = 0;
+  for (size_t q = 0; q < (size_t)ne * 8; ++q) nn = m->node_info[q] > nn ? m->node_info[q] : nn;
+  int* ncnt = (int*)calloc((size_t)nn + 1, sizeof(int));
+  int* noff = (int*)calloc((size_t)nn + 2, sizeof(int));
+  int* ninfo = (int*)malloc(sizeof(int) * (size_t)ne * 8);
+  int* off = (int*)calloc((size_t)ne + 1, sizeof(int));
+  int* info = (int*)malloc(sizeof(int) * (size_t)ne * 8 * 8);
+  if (!ncnt || !noff || !ninfo || !off || !info) {
+    free(ncnt); free(noff); free(ninfo); free(off); free(info);
+    return 1;
+  }
+  for (size_t q = 0; q < (size_t)ne * 8; ++q) ncnt[m->node_info[q]]++;
+  for (int u = 1; u <= nn; ++u) noff[u + 1] = noff[u] + ncnt[u];
+  memset(ncnt, 0, sizeof(int) * ((size_t)nn + 1));
+  for (int e = 0; e < ne; ++e)
+    for (int c = 0; c < 8; ++c) {
+      const int u = m->node_info[(size_t)e * 8 + c];
+      ninfo[noff[u] + ncnt[u]++] = e + 1;
+    }
+  int tot = 0;
+  for (int e = 0; e < ne; ++e) {
+    const int start = tot;
+    for (int c = 0; c < 8; ++c) {
+      const int u = m->node_info[(size_t)e * 8 + c];
+      for (int j = noff[u]; j < noff[u] + ncnt[u]; ++j) {
+        const int t = ninfo[j];
+        if (t == e + 1) continue;
+        int dup = 0;
+        for (int k = start; k < tot && !dup; ++k) dup = info[k] == t;
+        if (!dup) info[tot++] = t;
+      }
+    }
+    off[e + 1] = tot;
+  }
+  free(ncnt); free(noff); free(ninfo);
+  *off_out = off;
+  *info_out = info;
+  return 0;
+}
+
+/* depoChargeOnDOFsSFChargeCon (pic_depo_shapefunction_tools.f90:558-755; shape_function_cc without periodic
+ * vectors) and depoChargeOnDOFsSFAdaptive (:758-908; shape_function_adaptive without periodic vectors): the
+ * kernel Fac S1 at every DOF within R of the particle in the listed elements, its quadrature integral
+ * totalCharge = sum wGP(k) wGP(l) wGP(m) (Fac(4) S1) / sJ in visiting order, and the deposit
+ * (Fac(4)/totalCharge) * (Fac S1).  The elements are visited in list order, skipping repeats (ChargeSFDone)
+ * and those whose barycentre lies beyond R + ElemRadiusNGeo.  ChargeCon evaluates S = 1 - R^-2 r^2,
+ * Adaptive S = 1 - r^2/R^2.  The pass that deposits repeats the first pass's arithmetic. */
+static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], const double Fac[4],
+                            double r_sf, double r2_sf, double r2_sf_inv, int divide, const int* list, int nlist,
+                            double* PS, uint8_t* done, int* used) {
+  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  memset(done, 0, (size_t)m->n_elems);
+  int nused = 0;
+  double totalCharge = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    const double alpha = pass ? Fac[3] / totalCharge : 0.0;
+    const int n = pass ? nused : nlist;
+    for (int q = 0; q < n; ++q) {
+      const int e = pass ? used[q] : list[q];
+      if (!pass) {
+        if (done[e - 1]) continue;
+        const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
+        const double v0 = P[0] - b[0], v1 = P[1] - b[1], v2 = P[2] - b[2];
+        if (sqrt(v0 * v0 + v1 * v1 + v2 * v2) > (r_sf + m->elem_radius[e - 1])) continue;
+      }
+      const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
+      const double* sj = &m->elem_sj[(size_t)(e - 1) * ndof];
+      double* ps = &PS[(size_t)(e - 1) * ndof * 4];
+      int hit = 0;
+      for (int mz = 0; mz <= N; ++mz)
+        for (int l = 0; l <= N; ++l)
+          for (int k = 0; k <= N; ++k) {
+            const int r = mz * n1 * n1 + l * n1 + k;
+            const double d0 = P[0] - xg[(size_t)r * 3], d1 = P[1] - xg[(size_t)r * 3 + 1], d2 = P[2] - xg[(size_t)r * 3 + 2];
+            const double radius2 = (d0 * d0 + d1 * d1) + d2 * d2;
+            if (!(radius2 <= r2_sf)) continue;
+            hit = 1;
+            const double S = divide ? 1.0 - radius2 / r2_sf : 1.0 - r2_sf_inv * radius2;
+            double S1 = S * S;
+            for (int ex = 3; ex <= cfg->sf_alpha; ++ex) S1 = S * S1;
+            if (!pass) {
+              totalCharge = totalCharge + m->wgp[k] * m->wgp[l] * m->wgp[mz] * (Fac[3] * S1) / sj[r];
+            } else {
+              for (int v = 0; v < 4; ++v) ps[(size_t)r * 4 + v] = ps[(size_t)r * 4 + v] + alpha * (Fac[v] * S1);
+            }
+          }
+      if (!pass) {
+        if (hit) used[nused++] = e;
+        done[e - 1] = 1;
+      }
+    }
+    if (!nused) return;
+  }
+}
+
+/* the FIBGM cells within r_sf of P (clamped to the grid, dim_sf = 3), their elements in visiting order,
+ * each at its first appearance (a later one is skipped or fails the same barycentre test) */
+static int fibgm_visit_list(const pic_mesh_t* m, const double P[3], double r_sf, int* list, uint8_t* seen) {
+  int lo[3], hi[3], n = 0;
+  memset(seen, 0, (size_t)m->n_elems);
+  for (int d = 0; d < 3; ++d) {
+    hi[d] = (int)ceil((P[d] + r_sf - m->xmin_glob[d]) / m->fibgm_deltas[d]);
+    lo[d] = (int)floor((P[d] - r_sf - m->xmin_glob[d]) / m->fibgm_deltas[d] + 1);
+    if (hi[d] > m->fibgm_imax[d]) hi[d] = m->fibgm_imax[d];
+    if (lo[d] < 1) lo[d] = 1;
+  }
+  for (int kk = lo[0]; kk <= hi[0]; ++kk)
+    for (int ll = lo[1]; ll <= hi[1]; ++ll)
+      for (int mm = lo[2]; mm <= hi[2]; ++mm) {
+        size_t cidx = (size_t)(kk - 1) + (size_t)m->fibgm_imax[0] * ((ll - 1) + (size_t)m->fibgm_imax[1] * (mm - 1));
+        int nE = m->fibgm_n_elems[cidx], off = m->fibgm_offset[cidx];
+        for (int q = 0; q < nE; ++q) {
+          const int e = m->fibgm_element[off + q];
+          if (!seen[e - 1]) { seen[e - 1] = 1; list[n++] = e; }
+        }
+      }
+  return n;
+}
+
 /* DepositionMethod_SF, pic_depo_method.f90:851-1003 + calcSfSource (shapefunction_tools:30-164);
  * shape_function_cc with periodic images: calcSfSource:96-120 (totalChargePeriodicSF, Fac*Fac(4)/total) */
 static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* PS, int nthreads) {
@@ -1169,6 +1293,20 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
   if (nt > 1) { acc = (double*)calloc(nps * (size_t)nt, sizeof(double)); if (!acc) return 1; }
   uint8_t* doneAll = (uint8_t*)malloc((size_t)m->n_elems * (size_t)nt);
   if (!doneAll) { if (acc != PS) free(acc); return 1; }
+  /* the non-periodic charge-conserving branches of calcSfSource (:136-160): element lists and scratch */
+  const int con = nCases == 0 && (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC ||
+                                  cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE);
+  int *e2e_off = NULL, *e2e_info = NULL, *lists = NULL;
+  const int lcap = m->n_elems + 1;
+  if (con) {
+    if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE && build_elem_to_elem(m, &e2e_off, &e2e_info)) {
+      if (acc != PS) free(acc);
+      free(doneAll);
+      return 1;
+    }
+    lists = (int*)malloc(sizeof(int) * (size_t)lcap * 2 * (size_t)nt);
+    if (!lists) { if (acc != PS) free(acc); free(doneAll); free(e2e_off); free(e2e_info); return 1; }
+  }
 #ifdef _OPENMP
 #pragma omp parallel num_threads(nt)
 #endif
@@ -1218,6 +1356,19 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
           sf_shifted(&gsf, m, ic, s, Ps);
           depo_charge_on_dofs_sf(cfg, m, Ps, Fac, r_sf_p, r2_sf_p, r2_sf_inv_p, my, done);
         }
+      } else if (con) {
+        int* list = lists + (size_t)lcap * 2 * tid;
+        int* used = list + lcap;
+        int nl;
+        if (adaptive) {
+          const int e0 = p->elem[ip];
+          list[0] = e0;
+          nl = 1;
+          for (int j = e2e_off[e0 - 1]; j < e2e_off[e0]; ++j) list[nl++] = e2e_info[j];
+        } else {
+          nl = fibgm_visit_list(m, s, r_sf, list, done);
+        }
+        depo_charge_con(cfg, m, s, Fac, r_sf_p, r2_sf_p, r2_sf_inv_p, adaptive, list, nl, my, done, used);
       } else {
         double Fw[4];
         for (int v = 0; v < 4; ++v) Fw[v] = Fac[v] * w_sf;
@@ -1234,6 +1385,9 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
     free(acc);
   }
   free(doneAll);
+  free(lists);
+  free(e2e_off);
+  free(e2e_info);
   return 0;
 }
 

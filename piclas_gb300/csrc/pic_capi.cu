@@ -126,9 +126,10 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown tracking method");
   if (cfg->deposition < PIC_DEPO_CVWM || cfg->deposition > PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown deposition method");
-  if ((cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC || cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE) &&
-      m->n_periodic_vectors < 1)
-    return fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_cc/_adaptive are built for periodic meshes (the 27-image branch)");
+  // the 3D kernel visits 27 images (three periodic vectors) or none (InitPeriodicSFCaseMatrix, pic_depo.f90:828-910)
+  if (cfg->deposition != PIC_DEPO_CVWM && (cfg->sf_dim == 0 || cfg->sf_dim == 3) && m->n_periodic_vectors != 0 &&
+      m->n_periodic_vectors != 3)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "3D shape functions need a mesh with no or three periodic vectors");
   if (cfg->precision != PIC_PREC_FP64 && cfg->precision != PIC_PREC_MIXED)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown precision");
   if (cfg->n_species < 1 || cfg->n_species > PIC_MAX_SPECIES) return fail(PIC_ERR_INVALID_ARGUMENT, "n_species");
@@ -204,6 +205,25 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
     }
     Lax[d] = k >= 0 ? m->periodic_vectors[3 * k + d] : 0.0;
   }
+  // ElemToElemMapping as a set: elements sharing a unique corner node (particle_mesh_build.f90:1244-1380)
+  const bool near_only = c->adaptive && m->n_periodic_vectors == 0;
+  std::vector<std::vector<int>> node_elems;
+  if (near_only) {
+    int nn = 0;
+    for (size_t q = 0; q < (size_t)ne * 8; ++q) {
+      if (m->node_info[q] < 1) return fail(PIC_ERR_INVALID_ARGUMENT, "node_info out of range");
+      nn = std::max(nn, m->node_info[q]);
+    }
+    node_elems.resize((size_t)nn + 1);
+    for (int e = 0; e < ne; ++e)
+      for (int t = 0; t < 8; ++t) node_elems[m->node_info[(size_t)e * 8 + t]].push_back(e);
+  }
+  auto shares_node = [&](int a, int b) {
+    for (int t = 0; t < 8; ++t)
+      for (int x : node_elems[m->node_info[(size_t)a * 8 + t]])
+        if (x == b) return true;
+    return false;
+  };
   std::vector<int> off(ne + 1, 0), src;
   std::vector<int8_t> shift;
   std::vector<int> seen(ne, -1);
@@ -242,6 +262,9 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
     for (auto& pr : cand) {
       const int s = pr.first, pk = pr.second;
+      // shape_function_adaptive without periodic vectors deposits on the particle's element and the
+      // elements sharing a corner node with it only (depoChargeOnDOFsSFAdaptive over ElemToElemMapping)
+      if (near_only && s != e && !shares_node(s, e)) continue;
       const int sx = pk / 9 - 1, sy = (pk / 3) % 3 - 1, sz = pk % 3 - 1;
       const double shv[3] = {sx * Lax[0], sy * Lax[1], sz * Lax[2]};
       // exact-conservative test: min over target DOFs of the distance to the shifted source box
@@ -478,12 +501,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       const bool wall = bc == 1 || bc == 2;
       if (wall ? nb != 0 : (nb < 1 || nb > ne))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_nb_elem must be 1..nElems, or 0 exactly at open/reflective sides"));
-      // shape_function near walls: no images, the kernel ends at the wall (calcSfSource with
-      // NbrOfPeriodicSFCases = 0); the reference's 3D shape function takes 0 or 3 periodic vectors
-      if (wall && !(cfg->deposition == PIC_DEPO_CVWM ||
-                    (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION && m->n_periodic_vectors == 0)))
+      // shape functions near walls: no images, the kernel ends at the wall (calcSfSource with
+      // NbrOfPeriodicSFCases = 0; _cc and _adaptive renormalise what is left)
+      if (wall && !(cfg->deposition == PIC_DEPO_CVWM || m->n_periodic_vectors == 0))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT,
-                         "open/reflective particle boundaries need cell_volweight_mean, or shape_function on a mesh "
+                         "open/reflective particle boundaries need cell_volweight_mean, or a shape function on a mesh "
                          "without periodic sides"));
       if (wall && cfg->tracking == PIC_TRACK_REFMAPPING && (m->n_periodic_vectors > 0 || !m->elem_to_bc_sides))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT,

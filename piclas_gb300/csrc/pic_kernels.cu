@@ -1278,7 +1278,9 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
     if (act) {
       const double tot = MIXED ? (double)accf : acc;
       const bool ok = tot > 0.0;
-      if (!ok) flag_status(st, 0x20u);          // no DOF within R: the reference would divide by zero
+      // no DOF within R: with periodic images the reference divides by zero (calcSfSource:122); without,
+      // it deposits nothing (nUsedElems = 0), as the zero scale does here
+      if (!ok && c_k.n_pv > 0) flag_status(st, 0x20u);
       const double sc = ok ? 1.0 / tot : 0.0;
       if constexpr (MIXED) {
         float4* f = reinterpret_cast<float4*>(K.facf) + j;

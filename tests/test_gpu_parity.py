@@ -670,6 +670,48 @@ def test_shape_function_with_walls_needs_a_nonperiodic_mesh(gpu_lib):
     assert e.value.code == 1
 
 
+# ---- shape_function_cc / _adaptive without periodic vectors (walls all round) --------------------------
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+@pytest.mark.parametrize("tracking", [capi.PIC_TRACK_TRIA, capi.PIC_TRACK_REFMAPPING])
+def test_charge_conserving_sf_with_walls_against_oracle(gpu_lib, oracle_lib, dep, tracking):
+    """depoChargeOnDOFsSFChargeCon / depoChargeOnDOFsSFAdaptive: the kernel cut by the walls (adaptive: also
+    by the node neighbours of the particle's element) and renormalised to q MPF; FP64 within 1e-12 of the
+    oracle's maximum, mixed within 1e-6, particles and elements bit-exact."""
+    mesh = build_box_mesh(5, 5, 5, 2, bc=("reflective", "open", "reflective"))
+    w = workloads.plasma_wave(mesh=mesh, n_particles=3000, T_eV=2000.0, seed=37, dt=2e-10)
+    w.tracking, w.deposition = tracking, dep
+    w.sf_radius = 1.5 / 5
+    h = 1.0 / 5
+    w.mesh.sf_elem_radius = np.random.default_rng(37).uniform(1.2 * h, 2.4 * h, mesh.n_elems)
+    g = _run_gpu(w, 6)
+    st, PS = _run_oracle(oracle_lib, w, 6)
+    assert np.array_equal(g["inside"], st.inside) and np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0
+    gm = _run_gpu(w, 6, precision=capi.PIC_PREC_MIXED)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-6
+
+
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+def test_charge_conserving_sf_with_walls_conserves_charge(gpu_lib, oracle_lib, dep):
+    mesh = build_box_mesh(8, 8, 8, 3, bc=("reflective", "reflective", "open"))
+    w = workloads.plasma_wave(mesh=mesh, n_particles=100_000, seed=38)
+    w.deposition = dep
+    w.sf_radius = 2.0 / 8
+    w.mesh.sf_elem_radius = np.random.default_rng(38).uniform(1.2 / 8, 2.0 / 8, mesh.n_elems)
+    ms = capi.MeshStruct(w.mesh)
+    q = w.species[0][0] * w.species[0][2] * w.n
+    for prec, tol in ((capi.PIC_PREC_FP64, 1e-12), (capi.PIC_PREC_MIXED, 1e-5)):
+        loop = ParticleLoop(w.config(precision=prec), w.mesh)
+        loop.set_field(w.e_dof)
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+        PS = loop.deposition()
+        loop.close()
+        Q = oracle_lib.integrate_charge(ms, w.mesh.N, PS)
+        assert abs(Q - q) <= tol * abs(q), (prec, Q, q)
+
+
 # ---- 1D and 2D shape functions -------------------------------------------------------------------------
 @pytest.mark.parametrize("dim,sf_dir,depo3d", [(1, 1, True), (1, 2, False), (2, 3, True), (2, 1, True)])
 def test_shape_function_1d_2d_against_oracle(gpu_lib, oracle_lib, dim, sf_dir, depo3d):

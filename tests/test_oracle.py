@@ -365,3 +365,60 @@ def test_sf_1d_2d_conserve_charge_and_are_constant_across(oracle_lib, dim, sf_di
     for k in range(inv.max() + 1):
         v = rho[inv == k]
         assert np.allclose(v, v[0], rtol=1e-11, atol=1e-11 * np.abs(rho).max())
+
+
+# ---- shape_function_cc / _adaptive without periodic vectors (depoChargeOnDOFsSFChargeCon / ...Adaptive) ----
+def _walled_sf_case(dep, n=300, seed=5, cells=4, N=2):
+    mesh = build_box_mesh(cells, cells, cells, N, bc=("reflective", "open", "reflective"))
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, seed=seed)
+    w.deposition = dep
+    w.sf_radius = 0.4
+    w.sf_alpha = 3
+    h = 1.0 / cells
+    w.mesh.sf_elem_radius = np.random.default_rng(seed).uniform(1.2 * h, 2.6 * h, mesh.n_elems)
+    return w
+
+
+def _sf_con_numpy(mesh, P, fac, R, alpha, elems):
+    """The normalised kernel alpha (Fac S1) on the DOFs within R of P in the given elements (0-based)."""
+    ne, nd = mesh.n_elems, mesh.n_dof
+    xg = mesh.elem_xgp.reshape(ne, nd, 3)[elems]
+    sj = mesh.elem_sj.reshape(ne, nd)[elems]
+    w3 = np.einsum("k,j,i->kji", mesh.wgp, mesh.wgp, mesh.wgp).reshape(-1)
+    r2 = ((P - xg) ** 2).sum(-1)
+    S1 = np.where(r2 <= R * R, 1.0 - r2 / (R * R), 0.0) ** alpha
+    tot = (w3 * fac[3] * S1 / sj).sum()
+    out = np.zeros((ne, nd, 4))
+    out[elems] = (fac[3] / tot) * S1[..., None] * fac
+    return out
+
+
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+def test_charge_conserving_sf_without_periodic_vectors(oracle_lib, dep):
+    w = _walled_sf_case(dep)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS)
+    q, mpf = w.species[0][0], w.species[0][2]
+    total = w.n * q * mpf
+    # every particle's charge is kept, also where the kernel is cut by a wall
+    assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - total) <= 1e-12 * abs(total)
+    # single particles against an independent evaluation; adaptive: the particle's element and the
+    # elements sharing a corner node with it (ElemToElemMapping), radius of the particle's element
+    ni = w.mesh.node_info
+    for ip in range(0, w.n, 37):
+        e0 = int(w.elem[ip]) - 1
+        one = oracle_lib.OracleState(w.part_state[ip:ip + 1], w.elem[ip:ip + 1], w.part_species[ip:ip + 1])
+        ps1 = np.zeros_like(PS)
+        oracle_lib.deposit(cfg, ms, one, ps1)
+        P = w.part_state[ip, :3]
+        fac = np.array([*w.part_state[ip, 3:], 1.0]) * (q * mpf)
+        if dep == capi.PIC_DEPO_SHAPE_FUNCTION_CC:
+            ref = _sf_con_numpy(w.mesh, P, fac, w.sf_radius, w.sf_alpha, np.arange(w.mesh.n_elems))
+        else:
+            nb = np.flatnonzero(np.isin(ni, ni[e0]).any(axis=1))
+            ref = _sf_con_numpy(w.mesh, P, fac, w.mesh.sf_elem_radius[e0], w.sf_alpha, nb)
+            outside = np.setdiff1d(np.arange(w.mesh.n_elems), nb)
+            assert not ps1[outside].any()
+        assert np.allclose(ps1, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
