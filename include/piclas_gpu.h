@@ -173,7 +173,7 @@ typedef struct pic_mesh_t {
    * nElems) = (ELEM_NBR_BCSIDES, ELEM_FIRST_BCSIDE): the number of wall sides in reach of the element and
    * the 0-based first entry, -1/-1 for none; entry k (sorted by distance within an element) is the wall
    * side bc_side_elem_loc(1:2,k) = (element 1-based, local side 1..6) with SideBCMetrics(BCSIDE_DISTANCE)
-   * = bc_side_distance(k).  Wall sides must be planar rectangles (SideType PLANAR_RECT).  NULL/0 for
+   * = bc_side_distance(k).  Wall sides may be planar (rectangular or not) or bilinear.  NULL/0 for
    * TriaTracking or periodic meshes. */
   int32_t n_bc_entries;
   const int32_t* elem_to_bc_sides;

@@ -570,7 +570,11 @@ static int almost_equal(double x, double y) { return fabs(x - y) <= fmax(fabs(x)
  * Wall side geometry of a planar rectangular side: BezierControlPoints3D at NGeo = 1 (the corner nodes in
  * CGNS side order, particle_mesh_tools.f90:1748-1773), BaseVectors0-2 (particle_mesh_build.f90:1916-1925),
  * SideNormVec / SideDistance oriented away from the element (particle_mesh_tools.f90:1011-1048). */
-typedef struct { double bv0[3], bv1[3], bv2[3], n[3], dist; int bc; } orc_bc_side_t;
+typedef struct {
+  double bv0[3], bv1[3], bv2[3], bv3[3], n[3], dist, P[4][3];
+  int bc, type;                     /* type: SideType PLANAR_RECT (0), PLANAR_NONRECT (1), BILINEAR (2) */
+} orc_bc_side_t;
+enum { ORC_PLANAR_RECT = 0, ORC_PLANAR_NONRECT = 1, ORC_BILINEAR = 2 };
 
 static void side_corner(const pic_mesh_t* m, int e, int s, int p, int q, double out[3]) {
   int a, b, c;
@@ -592,7 +596,12 @@ static void unit3(const double v[3], double u[3]) {
   else { u[0] = u[1] = u[2] = 0.0; }
 }
 
-/* 0: planar rectangle (SideType PLANAR_RECT); 1 otherwise */
+/* GetSideType for NGeo = 1 (particle_mesh_tools.f90:1001-1053; linear elements are never curved): a side
+ * whose corners lie within 1e-6 of its extent of the averaged plane is planar (the slab test of
+ * GetSideSlabNormalsAndIntervals, particle_surfaces.f90:740-815, restated on the four corners) with
+ * SideNormVec oriented away from the element and SideDistance, PLANAR_RECT when its edges meet at right
+ * angles (:1026-1041), PLANAR_NONRECT otherwise; a non-planar side is BILINEAR with the non-oriented
+ * averaged normal.  Returns the type. */
 static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t* g) {
   double P00[3], P10[3], P01[3], P11[3];
   side_corner(m, e, s, 0, 0, P00); side_corner(m, e, s, 1, 0, P10);
@@ -602,32 +611,146 @@ static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t
     g->bv0[c] = ((+P00[c] + P10[c]) + P01[c]) + P11[c];
     g->bv1[c] = ((-P00[c] + P10[c]) - P01[c]) + P11[c];
     g->bv2[c] = ((-P00[c] - P10[c]) + P01[c]) + P11[c];
+    g->bv3[c] = ((+P00[c] - P10[c]) - P01[c]) + P11[c];
     ctr[c] = 0.25 * (((P00[c] + P10[c]) + P01[c]) + P11[c]);
+    g->P[0][c] = P00[c]; g->P[1][c] = P10[c]; g->P[2][c] = P01[c]; g->P[3][c] = P11[c];
   }
   const double* v1 = g->bv1;
   const double* v2 = g->bv2;
   double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
   double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
   for (int c = 0; c < 3; ++c) n[c] = n[c] / len;
+  g->bc = m->side_bc ? m->side_bc[(size_t)e * 6 + s] : 0;
+  /* slab thickness along the averaged normal against the side's extent */
+  const double* Pc[4] = {P00, P10, P01, P11};
+  double hmin = DBL_MAX, hmax = -DBL_MAX;
+  for (int k = 0; k < 4; ++k) {
+    const double d = Pc[k][0] * n[0] + Pc[k][1] * n[1] + Pc[k][2] * n[2];
+    hmin = fmin(hmin, d); hmax = fmax(hmax, d);
+  }
+  const double l1 = 0.5 * sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  const double l2 = 0.5 * sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const double h = hmax - hmin, dmax = fmax(h, fmax(l1, l2));
+  if (!(h < 1.0e-6 * dmax)) {
+    for (int c = 0; c < 3; ++c) g->n[c] = n[c];
+    g->dist = 0.0;
+    g->type = ORC_BILINEAR;
+    return g->type;
+  }
   const double* bary = &m->elem_bary[(size_t)e * 3];
   double vb[3] = {ctr[0] - bary[0], ctr[1] - bary[1], ctr[2] - bary[2]};
   if (vb[0] * n[0] + vb[1] * n[1] + vb[2] * n[2] < 0.0) for (int c = 0; c < 3; ++c) n[c] = -n[c];
   for (int c = 0; c < 3; ++c) g->n[c] = n[c];
   g->dist = ctr[0] * n[0] + ctr[1] * n[1] + ctr[2] * n[2];
-  g->bc = m->side_bc ? m->side_bc[(size_t)e * 6 + s] : 0;
-  /* planar: every corner on the plane; rectangular: the checks of particle_mesh_tools.f90:1026-1041 */
-  const double* Pc[4] = {P00, P10, P01, P11};
-  double scale = sqrt(g->bv1[0] * g->bv1[0] + g->bv1[1] * g->bv1[1] + g->bv1[2] * g->bv1[2]);
-  for (int k = 0; k < 4; ++k)
-    if (fabs(Pc[k][0] * n[0] + Pc[k][1] * n[1] + Pc[k][2] * n[2] - g->dist) > 1e-12 * scale) return 1;
   double d1[3], d2[3], d3[3], d4[3], u1[3], u2[3], u3[3], u4[3];
   for (int c = 0; c < 3; ++c) { d1[c] = P01[c] - P00[c]; d2[c] = P10[c] - P00[c]; d3[c] = P11[c] - P01[c]; d4[c] = P11[c] - P10[c]; }
   unit3(d1, u1); unit3(d2, u2); unit3(d3, u3); unit3(d4, u4);
 #define DOT3(a, b) ((a)[0] * (b)[0] + (a)[1] * (b)[1] + (a)[2] * (b)[2])
-  if (!(fabs(DOT3(u1, u2)) <= 2.22e-16) || !(fabs(DOT3(u1, u3)) <= 2.22e-16)) return 1;
-  if (!(fabs(DOT3(u4, u2)) <= 2.22e-16) || !(fabs(DOT3(u4, u3)) <= 2.22e-16)) return 1;
+  int rect = fabs(DOT3(u1, u2)) <= 2.22e-16 && fabs(DOT3(u1, u3)) <= 2.22e-16;
+  if (rect) rect = fabs(DOT3(u4, u2)) <= 2.22e-16 && fabs(DOT3(u4, u3)) <= 2.22e-16;
 #undef DOT3
+  g->type = rect ? ORC_PLANAR_RECT : ORC_PLANAR_NONRECT;
+  return g->type;
+}
+
+/* QuadraticSolver, utils.f90:401-465 */
+static int quadratic_solver(double A, double B, double C, double* r1, double* r2) {
+  *r1 = 0.0; *r2 = 0.0;
+  if (A != 0.0 && B == 0.0 && C == 0.0) return 1;
+  if (A != 0.0) {
+    const double q = 0.5 * B / A, radicant = q * q - (C / A);
+    if (radicant < 0.0) return 0;
+    const double ba = B / A;
+    *r1 = -(0.5 * ba) - copysign(1.0, ba) * sqrt(radicant);
+    *r2 = (C / A) / *r1;
+    return 2;
+  }
+  if (B != 0.0) { *r1 = -C / B; return 1; }
   return 0;
+}
+
+/* ComputeXi, particle_intersection.f90:2241-2273; HUGE when the denominator vanishes */
+static double compute_xi(double eta, const double A1[4], const double A2[4]) {
+  const double a = eta * A2[0] + A2[1];
+  const double b = (eta * (A2[0] - A1[0]) + A2[1]) - A1[1];
+  if (fabs(b) >= fabs(a)) {
+    if (fabs(b) <= 2.22e-16) return DBL_MAX;
+    return (-(eta * (A2[2] - A1[2])) - (A2[3] - A1[3])) / b;
+  }
+  return (-(eta * A2[2]) - A2[3]) / a;
+}
+
+/* ComputeSurfaceDistance2, particle_intersection.f90:2209-2238 */
+static double surface_distance2(const double BLC[4][3], double xi, double eta, const double traj[3]) {
+  double v[3];
+  for (int c = 0; c < 3; ++c) v[c] = (((xi * eta) * BLC[0][c] + xi * BLC[1][c]) + eta * BLC[2][c]) + BLC[3][c];
+  return (v[0] * traj[0] + v[1] * traj[1]) + v[2] * traj[2];
+}
+
+/* ComputeBiLinearIntersection, particle_intersection.f90:855-1240, RefTracking on a wall side (BCID > 0):
+ * the bilinear patch X(xi,eta) met by the line xl + t traj, eta from the quadratic of the two components
+ * normal to the trajectory, xi from ComputeXi, t the distance along traj; of two hits the nearer.  alpha2 > -1
+ * (the double check) drops a hit at alpha2.  Returns alpha or -1, and xi/eta of the hit; *bad is set where
+ * the reference aborts ('Invalid intersection with bilinear side'). */
+static double bilinear_alpha(const orc_bc_side_t* g, const double xl[3], const double traj[3], double len,
+                             double alpha2, double* xi_out, double* eta_out, int* bad) {
+  double BLC[4][3];
+  for (int c = 0; c < 3; ++c) {
+    BLC[0][c] = 0.25 * g->bv3[c]; BLC[1][c] = 0.25 * g->bv1[c];
+    BLC[2][c] = 0.25 * g->bv2[c]; BLC[3][c] = 0.25 * g->bv0[c];
+  }
+  const double scaleFac = traj[0] * g->n[0] + traj[1] * g->n[1] + traj[2] * g->n[2];
+  if (fabs(scaleFac) < 100.0 * EPS_MACH) return -1.0;                      /* epsilontol */
+  for (int c = 0; c < 3; ++c) BLC[3][c] = BLC[3][c] - xl[c];
+  double NC[4][3];
+  for (int i = 0; i < 4; ++i) {
+    const double d = (BLC[i][0] * traj[0] + BLC[i][1] * traj[1]) + BLC[i][2] * traj[2];
+    for (int c = 0; c < 3; ++c) NC[i][c] = BLC[i][c] - d * traj[c];
+  }
+  double A1[4], A2[4];
+  for (int i = 0; i < 4; ++i) { A1[i] = NC[i][2] - NC[i][0]; A2[i] = NC[i][2] - NC[i][1]; }
+  const double A = A1[0] * A2[2] - A2[0] * A1[2];
+  const double B = ((A1[0] * A2[3] - A2[0] * A1[3]) + A1[1] * A2[2]) - A2[1] * A1[2];
+  const double C = A1[1] * A2[3] - A2[1] * A1[3];
+  double eta[2], xi[2] = {0.0, 0.0}, t[2] = {-1.0, -1.0};
+  const int nRoot = quadratic_solver(A, B, C, &eta[0], &eta[1]);
+  int inter = 0;
+  for (int r = 0; r < nRoot; ++r) {
+    if (!(fabs(eta[r]) <= 1.0)) continue;
+    xi[r] = compute_xi(eta[r], A1, A2);
+    if (xi[r] == DBL_MAX) { *bad = 1; return -1.0; }
+    if (!(fabs(xi[r]) <= 1.0)) continue;
+    t[r] = surface_distance2(BLC, xi[r], eta[r], traj);
+    if (alpha2 > -1.0 && almost_equal(t[r], alpha2)) t[r] = -1.0;
+    const double alphaNorm = t[r] / len;
+    if (alphaNorm <= 1.0 && alphaNorm >= 0.0) inter |= 1 << r;
+    if (nRoot == 1) break;
+  }
+  int k;
+  if (inter == 0) return -1.0;
+  else if (inter == 1) k = 0;
+  else if (inter == 2) k = 1;
+  else k = t[0] < t[1] ? 0 : 1;
+  *xi_out = xi[k];
+  *eta_out = eta[k];
+  return t[k];
+}
+
+/* CalcNormAndTangBilinear, particle_surfaces.f90:404-440: the unit normal d/dxi x d/deta at (xi,eta) */
+static void bilinear_normal(const orc_bc_side_t* g, double xi, double eta, double nv[3]) {
+  const double* P00 = g->P[0];
+  const double* P10 = g->P[1];
+  const double* P01 = g->P[2];
+  const double* P11 = g->P[3];
+  double a[3], b[3];
+  for (int c = 0; c < 3; ++c) {
+    const double twist = ((P00[c] - P10[c]) + P11[c]) - P01[c];
+    b[c] = (xi * 0.25) * twist + 0.25 * (((-P00[c] - P10[c]) + P11[c]) + P01[c]);
+    a[c] = (eta * 0.25) * twist + 0.25 * (((-P00[c] + P10[c]) + P11[c]) - P01[c]);
+  }
+  double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  const double l = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  for (int c = 0; c < 3; ++c) nv[c] = n[c] / l;
 }
 
 /* ComputePlanarRectIntersection, particle_intersection.f90:515-684 (flip = 0: wall sides are masters);
@@ -679,34 +802,50 @@ static int bc_tracking(const pic_mesh_t* m, const orc_bc_side_t* geo, int elem, 
   for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
   *len0 = fmax(*len0, len);
   int doubleCheck = 0;
+  double alphaOld = -1.0;
   for (int loop = 0; loop < ORC_MAX_TRACK_LOOPS; ++loop) {
-    double alpha[ORC_BC_CAP];
+    double alpha[ORC_BC_CAP], sxi[ORC_BC_CAP], seta[ORC_BC_CAP];
     int list[ORC_BC_CAP];
     int nc = 0, nInter = 0;
     for (int i = 0; i < nloc; ++i) {
       if (m->bc_side_distance[first + i] > *len0) break;
       if (nc == ORC_BC_CAP) { (*ncap)++; break; }
-      alpha[nc] = planar_rect_alpha(&geo[first + i], xl, traj, len);
+      const orc_bc_side_t* g = &geo[first + i];
+      sxi[nc] = 0.0; seta[nc] = 0.0;
+      if (g->type == ORC_PLANAR_RECT) {
+        alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+      } else {
+        int bad = 0;
+        alpha[nc] = bilinear_alpha(g, xl, traj, len, doubleCheck ? alphaOld : -1.0, &sxi[nc], &seta[nc], &bad);
+        if (bad) (*ncap)++;
+      }
       list[nc] = i;
       if (alpha[nc] > -1.0) nInter++;
       nc++;
     }
     if (nInter == 0) return 0;
+    int slot[ORC_BC_CAP];
+    for (int i = 0; i < nc; ++i) slot[i] = i;
     for (int i = 1; i < nc; ++i) {              /* InsertionSort (stable) */
       double t = alpha[i];
-      int ti = list[i], j = i - 1;
-      while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; j--; }
-      alpha[j + 1] = t; list[j + 1] = ti;
+      int ti = list[i], ts = slot[i], j = i - 1;
+      while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; slot[j + 1] = slot[j]; j--; }
+      alpha[j + 1] = t; list[j + 1] = ti; slot[j + 1] = ts;
     }
+    for (int k = 0; k < nc; ++k)
+      if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
     int reflected = 0;
     for (int k = 0; k < nc; ++k) {
       if (!(alpha[k] > -1.0)) continue;
       const orc_bc_side_t* g = &geo[first + list[k]];
-      /* GetBoundaryInteraction (particle_boundary_condition.f90:35-221), REFMAPPING branch */
-      if (g->n[0] * traj[0] + g->n[1] * traj[1] + g->n[2] * traj[2] <= 0.0) { reflected = 0; continue; }
+      /* GetBoundaryInteraction (particle_boundary_condition.f90:35-221), REFMAPPING branch: SideNormVec of
+       * planar sides, CalcNormAndTangBilinear at the hit of bilinear ones */
+      double nl[3] = {g->n[0], g->n[1], g->n[2]};
+      if (g->type == ORC_BILINEAR) bilinear_normal(g, sxi[slot[k]], seta[slot[k]], nl);
+      if (nl[0] * traj[0] + nl[1] * traj[1] + nl[2] * traj[2] <= 0.0) { reflected = 0; continue; }
       reflected = 1;
       if (g->bc == 1) { *inside = 0; break; }                  /* RemoveParticle */
-      perfect_reflection(v, x, xl, traj, len, alpha[k], g->n);
+      perfect_reflection(v, x, xl, traj, len, alpha[k], nl);
       for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
       len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
       if (fabs(len) <= 2.22e-16) len = 0.0;

@@ -394,11 +394,13 @@ const char* pic_version(void) {
 }
 const char* pic_last_error(void) { return g_last_error.c_str(); }
 
-// Wall side of a BC element for RefTracking: BezierControlPoints3D at NGeo = 1 (the corner nodes in CGNS side
-// order, particle_mesh_tools.f90:1748-1773), BaseVectors0-2 (particle_mesh_build.f90:1916-1925), SideNormVec
-// and SideDistance oriented away from the element (particle_mesh_tools.f90:1011-1048).  Same operation
-// order as the oracle.  Returns false unless the side is a planar rectangle (SideType PLANAR_RECT).
-static bool wall_side_geometry(const double* xcl, const double* bary, int e, int s, double* g) {
+// Wall side geometry of a BC element for RefTracking, in the oracle's operation order: GetSideType for
+// NGeo = 1 (particle_mesh_tools.f90:1001-1053) and BaseVectors0-3 (particle_mesh_build.f90:1916-1925);
+// corners in the side's BezierControlPoints3D order (CGNS side order, particle_mesh_tools.f90:1748-1773),
+// planar when they lie within 1e-6 of the side's extent of the
+// averaged plane (then SideNormVec oriented away from the element, SideDistance, PLANAR_RECT or
+// PLANAR_NONRECT), else BILINEAR with the non-oriented averaged normal.  Fills kBcGeo doubles.
+static void wall_side_geometry(const double* xcl, const double* bary, int e, int s, double* g) {
   auto corner = [&](int p, int q, double out[3]) {
     int a, b, cc;
     switch (s) {
@@ -418,23 +420,36 @@ static bool wall_side_geometry(const double* xcl, const double* bary, int e, int
     g[c] = ((+P00[c] + P10[c]) + P01[c]) + P11[c];
     g[3 + c] = ((-P00[c] + P10[c]) - P01[c]) + P11[c];
     g[6 + c] = ((-P00[c] - P10[c]) + P01[c]) + P11[c];
+    g[16 + c] = ((+P00[c] - P10[c]) - P01[c]) + P11[c];
     ctr[c] = 0.25 * (((P00[c] + P10[c]) + P01[c]) + P11[c]);
+    g[19 + c] = P00[c]; g[22 + c] = P10[c]; g[25 + c] = P01[c]; g[28 + c] = P11[c];
   }
   const double* v1 = g + 3;
   const double* v2 = g + 6;
   double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
   const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
   for (int c = 0; c < 3; ++c) n[c] = n[c] / len;
+  const double* Pc[4] = {P00, P10, P01, P11};
+  double hmin = 1e300, hmax = -1e300;
+  for (int k = 0; k < 4; ++k) {
+    const double d = Pc[k][0] * n[0] + Pc[k][1] * n[1] + Pc[k][2] * n[2];
+    hmin = std::min(hmin, d); hmax = std::max(hmax, d);
+  }
+  const double l1 = 0.5 * std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  const double l2 = 0.5 * std::sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const double h = hmax - hmin, dmax = std::max(h, std::max(l1, l2));
+  if (!(h < 1.0e-6 * dmax)) {
+    for (int c = 0; c < 3; ++c) g[9 + c] = n[c];
+    g[12] = 0.0;
+    g[15] = 2.0;                                   // BILINEAR
+    return;
+  }
   const double* b = bary + (size_t)e * 3;
   const double vb[3] = {ctr[0] - b[0], ctr[1] - b[1], ctr[2] - b[2]};
   if (vb[0] * n[0] + vb[1] * n[1] + vb[2] * n[2] < 0.0)
     for (int c = 0; c < 3; ++c) n[c] = -n[c];
   for (int c = 0; c < 3; ++c) g[9 + c] = n[c];
   g[12] = ctr[0] * n[0] + ctr[1] * n[1] + ctr[2] * n[2];
-  const double* Pc[4] = {P00, P10, P01, P11};
-  const double scale = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
-  for (int k = 0; k < 4; ++k)
-    if (std::fabs(Pc[k][0] * n[0] + Pc[k][1] * n[1] + Pc[k][2] * n[2] - g[12]) > 1e-12 * scale) return false;
   auto unit = [](const double a[3], const double b0[3], double u[3]) {
     double d[3] = {a[0] - b0[0], a[1] - b0[1], a[2] - b0[2]};
     double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -444,7 +459,8 @@ static bool wall_side_geometry(const double* xcl, const double* bary, int e, int
   double u1[3], u2[3], u3[3], u4[3];
   unit(P01, P00, u1); unit(P10, P00, u2); unit(P11, P01, u3); unit(P11, P10, u4);
   auto dz = [](const double a[3], const double bb[3]) { return std::fabs(a[0] * bb[0] + a[1] * bb[1] + a[2] * bb[2]) <= 2.22e-16; };
-  return dz(u1, u2) && dz(u1, u3) && dz(u4, u2) && dz(u4, u3);
+  const bool rect = dz(u1, u2) && dz(u1, u3) && dz(u4, u2) && dz(u4, u3);
+  g[15] = rect ? 0.0 : 1.0;                        // PLANAR_RECT / PLANAR_NONRECT
 }
 
 int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
@@ -546,8 +562,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       const int e = m->bc_side_elem_loc[2 * k] - 1, sd = m->bc_side_elem_loc[2 * k + 1] - 1;
       if (e < 0 || e >= ne || sd < 0 || sd > 5 || m->side_nb_elem[e * 6 + sd] != 0)
         return bail(fail(PIC_ERR_INVALID_ARGUMENT, "bc_side_elem_loc must name open/reflective wall sides"));
-      if (!wall_side_geometry(xcl.data(), bary.data(), e, sd, &bc_geo[(size_t)k * kBcGeo]))
-        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "RefTracking walls must be planar rectangles (SideType PLANAR_RECT)"));
+      wall_side_geometry(xcl.data(), bary.data(), e, sd, &bc_geo[(size_t)k * kBcGeo]);
       bc_geo[(size_t)k * kBcGeo + 13] = m->bc_side_distance[k];
       bc_geo[(size_t)k * kBcGeo + 14] = (double)m->side_bc[e * 6 + sd];
     }

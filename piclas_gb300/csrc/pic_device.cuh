@@ -73,7 +73,10 @@ struct DevMesh {
 // one wall-side entry of a BC element: [0..2] BaseVectors0, [3..5] BaseVectors1, [6..8] BaseVectors2,
 // [9..11] SideNormVec (away from the domain), [12] SideDistance, [13] SideBCMetrics(BCSIDE_DISTANCE),
 // [14] boundary (1 open, 2 reflective)
-constexpr int kBcGeo = 16;
+// per wall entry: BaseVectors0-2 [0..8], SideNormVec [9..11], SideDistance [12], BCSIDE_DISTANCE [13],
+// boundary (1 open, 2 reflective) [14], SideType [15] (0 PLANAR_RECT, 1 PLANAR_NONRECT, 2 BILINEAR),
+// BaseVectors3 [16..18], the corners P00, P10, P01, P11 [19..30]
+constexpr int kBcGeo = 32;
 constexpr int kBcCap = 32;   // wall sides traced per trajectory (entries within reach beyond it are not)
 
 // ---- particles (SoA) ---------------------------------------------------------------------
@@ -802,6 +805,99 @@ __device__ __forceinline__ double planar_rect_alpha(const double* __restrict__ g
   return alpha;
 }
 
+// QuadraticSolver, utils.f90:401-465
+__device__ __forceinline__ int quadratic_solver(double A, double B, double C, double& r1, double& r2) {
+  r1 = 0.0;
+  r2 = 0.0;
+  if (A != 0.0 && B == 0.0 && C == 0.0) return 1;
+  if (A != 0.0) {
+    const double q = 0.5 * B / A, radicant = q * q - (C / A);
+    if (radicant < 0.0) return 0;
+    const double ba = B / A;
+    r1 = -(0.5 * ba) - copysign(1.0, ba) * sqrt(radicant);
+    r2 = (C / A) / r1;
+    return 2;
+  }
+  if (B != 0.0) { r1 = -C / B; return 1; }
+  return 0;
+}
+
+// ComputeBiLinearIntersection, particle_intersection.f90:855-1240 (RefTracking, wall side): eta from the
+// quadratic of the trajectory-normal components, xi from ComputeXi (:2241-2273), t from
+// ComputeSurfaceDistance2 (:2209-2238); of two hits the nearer; alpha2 > -1 drops a hit at alpha2.  Returns
+// alpha or -1 with xi/eta of the hit; bad where the reference aborts (ComputeXi's HUGE).
+static __device__ __noinline__ double bilinear_alpha(const double* __restrict__ g, const double xl[3], const double traj[3],
+                                              double len, double alpha2, double& xi_out, double& eta_out, bool& bad) {
+  double BLC[4][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    BLC[0][c] = 0.25 * __ldg(g + 16 + c);
+    BLC[1][c] = 0.25 * __ldg(g + 3 + c);
+    BLC[2][c] = 0.25 * __ldg(g + 6 + c);
+    BLC[3][c] = 0.25 * __ldg(g + c);
+  }
+  const double scaleFac = traj[0] * __ldg(g + 9) + traj[1] * __ldg(g + 10) + traj[2] * __ldg(g + 11);
+  if (fabs(scaleFac) < 100.0 * kEpsMach) return -1.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) BLC[3][c] = BLC[3][c] - xl[c];
+  double A1[4], A2[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double d = (BLC[i][0] * traj[0] + BLC[i][1] * traj[1]) + BLC[i][2] * traj[2];
+    const double n0 = BLC[i][0] - d * traj[0], n1 = BLC[i][1] - d * traj[1], n2 = BLC[i][2] - d * traj[2];
+    A1[i] = n2 - n0;
+    A2[i] = n2 - n1;
+  }
+  const double A = A1[0] * A2[2] - A2[0] * A1[2];
+  const double B = ((A1[0] * A2[3] - A2[0] * A1[3]) + A1[1] * A2[2]) - A2[1] * A1[2];
+  const double C = A1[1] * A2[3] - A2[1] * A1[3];
+  double eta[2], xi[2] = {0.0, 0.0}, t[2] = {-1.0, -1.0};
+  const int nRoot = quadratic_solver(A, B, C, eta[0], eta[1]);
+  int inter = 0;
+  for (int r = 0; r < nRoot; ++r) {
+    if (!(fabs(eta[r]) <= 1.0)) continue;
+    const double e = eta[r];
+    const double a = e * A2[0] + A2[1];
+    const double b = (e * (A2[0] - A1[0]) + A2[1]) - A1[1];
+    if (fabs(b) >= fabs(a)) {
+      if (fabs(b) <= 2.22e-16) { bad = true; return -1.0; }
+      xi[r] = (-(e * (A2[2] - A1[2])) - (A2[3] - A1[3])) / b;
+    } else {
+      xi[r] = (-(e * A2[2]) - A2[3]) / a;
+    }
+    if (!(fabs(xi[r]) <= 1.0)) continue;
+    double sv[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) sv[c] = (((xi[r] * e) * BLC[0][c] + xi[r] * BLC[1][c]) + e * BLC[2][c]) + BLC[3][c];
+    t[r] = (sv[0] * traj[0] + sv[1] * traj[1]) + sv[2] * traj[2];
+    if (alpha2 > -1.0 && almost_equal(t[r], alpha2)) t[r] = -1.0;
+    const double alphaNorm = t[r] / len;
+    if (alphaNorm <= 1.0 && alphaNorm >= 0.0) inter |= 1 << r;
+    if (nRoot == 1) break;
+  }
+  if (inter == 0) return -1.0;
+  const int k = inter == 1 ? 0 : inter == 2 ? 1 : (t[0] < t[1] ? 0 : 1);
+  xi_out = xi[k];
+  eta_out = eta[k];
+  return t[k];
+}
+
+// CalcNormAndTangBilinear, particle_surfaces.f90:404-440: unit d/dxi x d/deta at (xi, eta)
+__device__ __forceinline__ void bilinear_normal(const double* __restrict__ g, double xi, double eta, double nv[3]) {
+  double a[3], b[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double P00 = __ldg(g + 19 + c), P10 = __ldg(g + 22 + c), P01 = __ldg(g + 25 + c), P11 = __ldg(g + 28 + c);
+    const double twist = ((P00 - P10) + P11) - P01;
+    b[c] = (xi * 0.25) * twist + 0.25 * (((-P00 - P10) + P11) + P01);
+    a[c] = (eta * 0.25) * twist + 0.25 * (((-P00 + P10) + P11) - P01);
+  }
+  const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  const double l = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) nv[c] = n[c] / l;
+}
+
 // ParticleBCTracking, particle_reftracking.f90:417-694, for wall sides only (the element never changes).
 // Returns true when the particle is done: it has not moved (PARTHASMOVED) or an open wall removed it.
 static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int elem, double x[3], double xl[3], double v[3],
@@ -814,15 +910,24 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int elem, doub
   for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
   len0 = fmax(len0, len);
   bool doubleCheck = false;
+  double alphaOld = -1.0;
   for (int loop = 0; loop < 10000; ++loop) {
     double alpha[kBcCap];
     int list[kBcCap];
     int nc = 0, nInter = 0;
+    const double alpha2 = doubleCheck ? alphaOld : -1.0;
     for (int i = 0; i < nloc; ++i) {
       const double* g = M.bc_geo + (size_t)kBcGeo * (first + i);
       if (__ldg(g + 13) > len0) break;
       if (nc == kBcCap) { cap_hit = true; break; }
-      alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+      if (__ldg(g + 15) == 0.0) {
+        alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+      } else {
+        double sxi, seta;
+        bool bad = false;
+        alpha[nc] = bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
+        if (bad) cap_hit = true;
+      }
       list[nc] = i;
       if (alpha[nc] > -1.0) nInter++;
       nc++;
@@ -836,11 +941,20 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int elem, doub
       alpha[j + 1] = t;
       list[j + 1] = ti;
     }
+    for (int k = 0; k < nc; ++k)
+      if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
     bool reflected = false;
     for (int k = 0; k < nc; ++k) {
       if (!(alpha[k] > -1.0)) continue;
       const double* g = M.bc_geo + (size_t)kBcGeo * (first + list[k]);
-      const double n[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
+      double n[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
+      if (__ldg(g + 15) == 2.0) {
+        // the hit's xi/eta: the same call as above (xl, traj, len and alpha2 are unchanged until a reflection)
+        double sxi = 0.0, seta = 0.0;
+        bool bad = false;
+        bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
+        bilinear_normal(g, sxi, seta, n);
+      }
       // GetBoundaryInteraction, REFMAPPING branch (particle_boundary_condition.f90:35-221)
       if (n[0] * traj[0] + n[1] * traj[1] + n[2] * traj[2] <= 0.0) { reflected = false; continue; }
       reflected = true;

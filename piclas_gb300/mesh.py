@@ -215,7 +215,8 @@ WALL_BC = {"open": 1, "reflective": 2}      # PartBound%TargetBoundCond
 
 def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
                    perturb: float = 0.0, refmapping_eps: float = 1.0e-4,
-                   bc=("periodic", "periodic", "periodic"), bc_halo_eps: float | None = None) -> BoxMesh:
+                   bc=("periodic", "periodic", "periodic"), bc_halo_eps: float | None = None,
+                   wall_bulge: float = 0.0, wall_shear: float = 0.0) -> BoxMesh:
     """Build a box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
 
     ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
@@ -224,6 +225,11 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     twins for cell_volweight_mean), "open" or "reflective" (wall sides without a neighbour: SIDE_NBELEMID
     = 0, master orientation, convex).  Without periodic axes the BC-element lists of RefTracking are
     built with halo ``bc_halo_eps`` (default: the largest element extent).
+    ``wall_bulge`` moves the nodes of each open/reflective face inwards along its normal by
+    ``wall_bulge*h*sin(pi u)sin(pi v)`` (u, v in [0,1] across the face): the wall sides become bilinear
+    (SideType BILINEAR).  ``wall_shear`` moves them within the face plane by ``wall_shear*h`` times the
+    same bump along the first in-plane axis: planar sides that are no longer rectangles (PLANAR_NONRECT).
+    The face edges stay put.
     """
     bc = tuple(bc)
     if len(bc) != 3 or any(b not in ("periodic", "open", "reflective") for b in bc):
@@ -254,6 +260,20 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
              * np.sin(2.0 * np.pi * (X[..., 2] - lo[2]) / L[2]))
         for d in range(3):
             X[..., d] = np.where(interior, X[..., d] + perturb * hvec[d] * s, X[..., d])
+    if wall_bulge != 0.0 or wall_shear != 0.0:
+        U = [(X[..., d] - lo[d]) / L[d] for d in range(3)]
+        for d in range(3):
+            if periodic[d]:
+                continue
+            o1, o2 = [a for a in range(3) if a != d]
+            bump = np.sin(np.pi * U[o1]) * np.sin(np.pi * U[o2])
+            for face, sign in ((0, 1.0), (-1, -1.0)):
+                sl = [slice(None)] * 3
+                sl[2 - d] = face                       # X is indexed [k][j][i]
+                sl = tuple(sl)
+                b = bump[sl]
+                X[sl + (d,)] = X[sl + (d,)] + sign * wall_bulge * hvec[d] * b
+                X[sl + (o1,)] = X[sl + (o1,)] + wall_shear * hvec[o1] * b
     n_unique = (nx + 1) * (ny + 1) * (nz + 1)
 
     def uid(i, j, k):  # 0-based unique node id of grid node (i,j,k)

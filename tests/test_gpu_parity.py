@@ -577,10 +577,10 @@ def test_wrong_start_element_matches_oracle(gpu_lib, oracle_lib):
 
 
 # ---- walls with RefTracking (ParticleBCTracking over planar wall sides) ------------------------------
-def _ref_wall_workload(bc, seed, n=4000, perturb=0.0, cells=5):
-    mesh = build_box_mesh(cells, cells, cells, 2, perturb=perturb, bc=bc)
+def _ref_wall_workload(bc, seed, n=4000, perturb=0.0, cells=5, bulge=0.0, shear=0.0):
+    mesh = build_box_mesh(cells, cells, cells, 2, perturb=perturb, bc=bc, wall_bulge=bulge, wall_shear=shear)
     w = workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=2000.0, seed=seed, dt=2e-10)
-    if perturb:
+    if perturb or bulge or shear:
         x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(seed))
         w.part_state[:, :3] = x
         w.elem = e
@@ -625,6 +625,27 @@ def test_reftracking_walls_separate_routines_and_mixed(gpu_lib, oracle_lib):
     assert np.array_equal(g["inside"], st.inside) and np.array_equal(g["elem"], st.elem)
     assert np.array_equal(g["part_state"], st.part_state)
     gm = _run_gpu(w, 6, precision=capi.PIC_PREC_MIXED)
+    assert (gm["inside"] != st.inside).sum() <= 3
+    k = (gm["inside"] == 1) & (st.inside == 1)
+    assert np.max(np.abs(gm["part_state"][k, :3] - st.part_state[k, :3])) < 1e-6
+
+
+@pytest.mark.parametrize("bc,bulge,shear", [(("reflective",) * 3, 0.2, 0.0), (("open", "reflective", "open"), 0.2, 0.0),
+                                             (("reflective", "open", "reflective"), 0.0, 0.15),
+                                             (("reflective",) * 3, 0.15, 0.1)])
+def test_reftracking_nonplanar_walls_fp64_bitexact(gpu_lib, oracle_lib, bc, bulge, shear):
+    """Bilinear wall sides (ComputeBiLinearIntersection, CalcNormAndTangBilinear) and planar non-rectangular
+    ones: 12 fused steps bit-exact against the oracle; mixed: the same particles inside, positions close."""
+    w = _ref_wall_workload(bc, seed=34, perturb=0.03, bulge=bulge, shear=shear)
+    g = _run_gpu(w, 12)
+    st, PS = _run_oracle(oracle_lib, w, 12)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0 and st.counters.n_ref_tolerance == 0
+    assert (np.sign(st.part_state[:, 3:]) != np.sign(w.part_state[:, 3:])).any(axis=1).sum() > 100
+    gm = _run_gpu(w, 12, precision=capi.PIC_PREC_MIXED)
     assert (gm["inside"] != st.inside).sum() <= 3
     k = (gm["inside"] == 1) & (st.inside == 1)
     assert np.max(np.abs(gm["part_state"][k, :3] - st.part_state[k, :3])) < 1e-6

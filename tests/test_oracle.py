@@ -422,3 +422,119 @@ def test_charge_conserving_sf_without_periodic_vectors(oracle_lib, dep):
             outside = np.setdiff1d(np.arange(w.mesh.n_elems), nb)
             assert not ps1[outside].any()
         assert np.allclose(ps1, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+# ---- RefTracking walls that are bilinear (SideType BILINEAR) or planar non-rectangles -------------------
+_FACES = {  # tensor-corner layout of the six hexahedron faces: axis, side (0 low / 1 high)
+    "x-": (0, 0), "x+": (0, 1), "y-": (1, 0), "y+": (1, 1), "z-": (2, 0), "z+": (2, 1)}
+
+
+def _face_corners(mesh, e, axis, hi):
+    """The four corners of a face as X(u,v) = sum corner * (bilinear weights), u/v along the other axes."""
+    C = mesh.xcl_ngeo.reshape(mesh.n_elems, 2, 2, 2, 3)[e]       # [k][j][i]
+    o1, o2 = [a for a in range(3) if a != axis]
+    P = np.zeros((2, 2, 3))
+    for a in range(2):
+        for b in range(2):
+            idx = [0, 0, 0]
+            idx[axis], idx[o1], idx[o2] = hi, a, b
+            P[a, b] = C[idx[2], idx[1], idx[0]]
+    return P
+
+
+def _patch_hit(P, xl, d, tmax):
+    """Newton for X(u,v) = xl + t d on the bilinear patch with corners P[a][b], u,v in [0,1]."""
+    u = v = 0.5
+    t = 0.0
+    for _ in range(60):
+        X = (P[0, 0] * (1 - u) * (1 - v) + P[1, 0] * u * (1 - v) + P[0, 1] * (1 - u) * v + P[1, 1] * u * v)
+        Xu = (P[1, 0] - P[0, 0]) * (1 - v) + (P[1, 1] - P[0, 1]) * v
+        Xv = (P[0, 1] - P[0, 0]) * (1 - u) + (P[1, 1] - P[1, 0]) * u
+        F = X - xl - t * d
+        J = np.stack([Xu, Xv, -d], axis=1)
+        du, dv, dt = np.linalg.solve(J, -F)
+        u, v, t = u + du, v + dv, t + dt
+        if max(abs(du), abs(dv), abs(dt)) < 1e-16:
+            break
+    ok = -1e-12 <= u <= 1 + 1e-12 and -1e-12 <= v <= 1 + 1e-12 and 0.0 <= t <= tmax
+    n = np.cross(Xu, Xv)
+    return ok, t, n / np.linalg.norm(n)
+
+
+def _walled_case(bulge=0.0, shear=0.0, bc=("reflective",) * 3, n=2000, seed=15):
+    mesh = build_box_mesh(4, 4, 4, 2, bc=bc, wall_bulge=bulge, wall_shear=shear)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=2000.0, seed=seed, dt=2e-10)
+    w.e_dof[:] = 0.0
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(seed))
+    w.part_state[:, :3] = x
+    w.elem = e
+    return w
+
+
+@pytest.mark.parametrize("bulge,shear", [(0.2, 0.0), (0.0, 0.15), (0.15, 0.1)])
+def test_reftracking_nonplanar_reflective_walls_keep_particles(oracle_lib, bulge, shear):
+    w = _walled_case(bulge, shear)
+    ref = _ref_wall_steps(oracle_lib, w, 25)
+    v0, v = w.part_state[:, 3:], ref.part_state[:, 3:]
+    assert ref.inside.all() and ref.counters.n_lost == 0 and ref.counters.n_ref_tolerance == 0
+    assert np.max(np.abs(ref.part_pos_ref)) <= 1.0 + 1e-9
+    assert np.allclose(np.linalg.norm(v, axis=1), np.linalg.norm(v0, axis=1), rtol=1e-13, atol=0.0)
+    assert (np.abs(v - v0).max(axis=1) > 0).sum() > 300          # many reflections
+
+
+@pytest.mark.parametrize("bulge,shear", [(0.2, 0.0), (0.0, 0.15)])
+@pytest.mark.parametrize("face", ["x-", "y+", "z-"])
+def test_reftracking_nonplanar_wall_single_reflection(oracle_lib, bulge, shear, face):
+    """One particle against one wall side: the hit point, the normal there (bilinear: d/dxi x d/deta at the
+    hit; planar: the side normal) and the reflected state against an independent Newton solve."""
+    w = _walled_case(bulge, shear, n=1)
+    m = w.mesh
+    axis, hi = _FACES[face]
+    ijk = [2, 1, 2]
+    ijk[axis] = 3 if hi else 0
+    e = ijk[0] + 4 * (ijk[1] + 4 * ijk[2])
+    P = _face_corners(m, e, axis, hi)
+    target = P.mean(axis=(0, 1)) + 0.1 * (P[1, 0] - P[0, 0]) - 0.05 * (P[0, 1] - P[0, 0])
+    start = m.elem_bary[e] + 0.2 * (m.elem_bary[e] - target)
+    d = target - start
+    L = np.linalg.norm(d)
+    d /= L
+    step = L + 0.4 * 0.25                                          # crosses the wall by 0.4 h
+    w.dt = 1e-9
+    w.part_state[0, :3] = start
+    w.part_state[0, 3:] = d * step / w.dt
+    w.elem = np.array([e + 1], np.int32)
+    ok, t, n = _patch_hit(P, start, d, step)
+    assert ok
+    if np.dot(n, target - m.elem_bary[e]) < 0:
+        n = -n
+    poi = start + t * d
+    d2 = d - 2.0 * np.dot(d, n) * n
+    x_exp = poi + d2 * (step - t)
+    v_exp = w.part_state[0, 3:] - 2.0 * np.dot(w.part_state[0, 3:], n) * n
+    ref = _ref_wall_steps(oracle_lib, w, 1)
+    assert ref.inside[0] == 1
+    assert np.max(np.abs(ref.part_state[0, :3] - x_exp)) < 1e-12
+    assert np.max(np.abs(ref.part_state[0, 3:] - v_exp)) < 1e-9 * np.linalg.norm(v_exp)
+    if bulge:
+        assert abs(abs(n[axis]) - 1.0) > 1e-6                       # the wall is tilted at the hit
+
+
+def test_reftracking_bilinear_open_wall_removes(oracle_lib):
+    """A particle that crosses the bulged open wall is removed; one stopping short of it stays."""
+    for frac, kept in ((0.4, False), (-0.05, True)):
+        w = _walled_case(0.2, 0.0, bc=("open", "reflective", "reflective"), n=1)
+        m = w.mesh
+        e = 0 + 4 * (2 + 4 * 1)
+        P = _face_corners(m, e, 0, 0)
+        target = P.mean(axis=(0, 1))
+        start = m.elem_bary[e]
+        d = target - start
+        L = np.linalg.norm(d)
+        d /= L
+        w.dt = 1e-9
+        w.part_state[0, :3] = start
+        w.part_state[0, 3:] = d * (L + frac * 0.25) / w.dt
+        w.elem = np.array([e + 1], np.int32)
+        ref = _ref_wall_steps(oracle_lib, w, 1)
+        assert bool(ref.inside[0]) == kept
