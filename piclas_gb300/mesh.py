@@ -557,6 +557,69 @@ def side_control_points(mesh: BoxMesh, e: int, s: int) -> np.ndarray:
     return out
 
 
+def elem_to_elem(mesh: BoxMesh) -> list[list[int]]:
+    """ElemToElemMapping/ElemToElemInfo (particle_mesh_build.f90:1244-1380): per element (0-based) the other
+    elements sharing one of its unique corner nodes, in the order met walking its corners (CGNS order) and,
+    per node, the elements in ascending order (NodeToElemInfo, :1150-1243)."""
+    ni = mesh.node_info
+    node_elems: dict[int, list[int]] = {}
+    for e in range(mesh.n_elems):
+        for c in range(8):
+            node_elems.setdefault(int(ni[e, c]), []).append(e)
+    out = []
+    for e in range(mesh.n_elems):
+        seen: list[int] = []
+        for c in range(8):
+            for t in node_elems[int(ni[e, c])]:
+                if t != e and t not in seen:
+                    seen.append(t)
+        out.append(seen)
+    return out
+
+
+def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothing: bool = False) -> np.ndarray:
+    """SFElemr2_Shared(1,:) of InitShapeFunctionAdaptive (pic_depo.f90:727-815) for the 3D kernel: the shortest
+    distance from the element's corners to the corners of its node neighbours that it does not share (else
+    the mid point to its corners), averaged with the bounding-box length BoxVolume^(1/3) when that is shorter
+    (always with ``smoothing``, PIC-shapefunction-adaptive-smoothing), times SFDepoScaling/(N+1) with
+    SFDepoScaling = (3 DOF/(4 pi))^(1/3), DOF = PIC-shapefunction-adaptive-DOF (default (4/3) pi 2^3)."""
+    if adaptive_dof is None:
+        adaptive_dof = (4.0 / 3.0) * math.pi * (1.0 + 1.0) ** 3
+    dof_max = (4.0 / 3.0) * math.pi * (mesh.N + 1.0) ** 3
+    if adaptive_dof > dof_max:
+        raise ValueError(f"PIC-shapefunction-adaptive-DOF > (4/3)*PI*(N+1)**3 = {dof_max} is not allowed")
+    scaling = (3.0 * adaptive_dof / (4.0 * math.pi)) ** (1.0 / 3.0)
+    nb = elem_to_elem(mesh)
+    ni = mesh.node_info
+    corners = mesh.node_coords.reshape(mesh.n_elems, 8, 3)[:, CGNS_TO_TENSOR, :]     # CGNS corner order
+    r = np.full(mesh.n_elems, np.finfo(np.float64).max)
+    for e in range(mesh.n_elems):
+        done = False
+        own = set(int(u) for u in ni[e])
+        for t in nb[e]:
+            for jn in range(8):
+                if int(ni[t, jn]) in own:
+                    continue
+                done = True
+                v2 = corners[t, jn]
+                for i in range(8):
+                    d = corners[e, i] - v2
+                    rt = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+                    if rt < r[e]:
+                        r[e] = rt
+        if not done:
+            mid = corners[e].sum(axis=0) / 8.0
+            for i in range(8):
+                d = mid - corners[e, i]
+                r[e] = min(r[e], math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]))
+        lo, hi = corners[e].min(axis=0), corners[e].max(axis=0)
+        char_len = ((hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2])) ** (1.0 / 3.0)
+        if char_len < r[e] or smoothing:
+            r[e] = (r[e] + char_len) / 2.0
+        r[e] = r[e] * scaling / (mesh.N + 1.0)
+    return r
+
+
 def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float):
     """ElemToBCSides / SideBCMetrics of BuildBCElemDistance (particle_mesh_build.f90:645-1092, the halo
     branch of an MPI build): for every element its own wall sides (local side order), then every other

@@ -538,3 +538,42 @@ def test_reftracking_bilinear_open_wall_removes(oracle_lib):
         w.elem = np.array([e + 1], np.int32)
         ref = _ref_wall_steps(oracle_lib, w, 1)
         assert bool(ref.inside[0]) == kept
+
+
+def test_sf_adaptive_radius_init():
+    """InitShapeFunctionAdaptive on uniform boxes: the nearest unshared neighbour corner is h away and the
+    bounding-box length is h, so R = h (3 DOF/(4 pi))^(1/3) / (N+1) = 2h/(N+1) at the default DOF (4/3)pi 2^3;
+    smoothing averages with the same h; a larger DOF scales R by the cube root."""
+    from piclas_gb300.mesh import elem_to_elem, sf_adaptive_radius
+    for N in (1, 2, 3):
+        m = build_box_mesh(4, 3, 5, N, bc=("reflective", "open", "periodic"))
+        h = float(np.min(m.h))
+        r = sf_adaptive_radius(m)
+        hmin = np.minimum.reduce([m.h[0], m.h[1], m.h[2]])
+        assert np.allclose(r, 2.0 * hmin / (N + 1), rtol=1e-14)
+        assert np.allclose(sf_adaptive_radius(m, smoothing=True), r * 0 + (hmin + np.prod(m.h) ** (1 / 3)) / 2 * 2 / (N + 1),
+                           rtol=1e-14)
+        if N > 1:
+            assert np.allclose(sf_adaptive_radius(m, adaptive_dof=(4 / 3) * np.pi * 8 * 1.728), 1.2 * r, rtol=1e-12)
+        assert h > 0
+    nb = elem_to_elem(build_box_mesh(3, 3, 3, 1, bc=("open",) * 3))
+    assert len(nb[13]) == 26 and len(nb[0]) == 7 and 13 not in nb[13]
+    with pytest.raises(ValueError):
+        sf_adaptive_radius(build_box_mesh(2, 2, 2, 1), adaptive_dof=40.0)
+
+
+def test_adaptive_with_initialised_radius_conserves_charge(oracle_lib):
+    from piclas_gb300.mesh import sf_adaptive_radius
+    mesh = build_box_mesh(5, 5, 5, 3, bc=("reflective", "open", "reflective"), perturb=0.05)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=400, seed=16)
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(16))
+    w.part_state[:, :3] = x
+    w.elem = e
+    w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE
+    w.mesh.sf_elem_radius = sf_adaptive_radius(mesh)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS)
+    total = w.n * w.species[0][0] * w.species[0][2]
+    assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - total) <= 1e-12 * abs(total)
