@@ -84,7 +84,10 @@ def dominant_kernel_bytes(w, mixed: bool) -> tuple[str, float]:
     if w.deposition == capi.PIC_DEPO_SHAPE_FUNCTION:
         # gather: each packed particle record read once, PartSource written once
         rec = 32 if mixed else 16 + 24 + 32
-        name = f"k_sf_gather{5 if sf_gather_variant() == 5 else 2}<{w.mesh.N},{int(mixed)}>"
+        if sf_gather_variant() == 5:
+            name = f"k_sf_gather5<{w.mesh.N},{int(mixed)},0,{int(w.sf_alpha == 2)}>"
+        else:
+            name = f"k_sf_gather2<{w.mesh.N},{int(mixed)}>"
         return name, float(w.n * rec + w.mesh.n_elems * w.mesh.n_dof * 4 * 8)
     s_state = (24 + 12) if mixed else 48
     b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_elems * w.mesh.n_dof * 3 * (4 if mixed else 8)

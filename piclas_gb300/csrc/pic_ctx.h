@@ -101,7 +101,7 @@ struct pic_ctx {
   }
   pic::LaunchArgs args() const {
     pic::LaunchArgs a;
-    a.M = M; a.MF = MF; a.N = N; a.nd = nd; a.n_canon = n_canon; a.mixed = mixed;
+    a.M = M; a.MF = MF; a.N = N; a.nd = nd; a.n_canon = n_canon; a.mixed = mixed; a.sf_alpha = cfg.sf_alpha;
     a.E = E; a.E32 = E32; a.NS = NS; a.st = st; a.s = stream;
     return a;
   }

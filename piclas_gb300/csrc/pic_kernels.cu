@@ -954,7 +954,16 @@ constexpr int kSf5Chunk = 256;
 constexpr int kSf5Threads = 128;
 constexpr int kSf5Pairs = 160;
 
-template <int N, bool MIXED, bool ADAPT>
+// (1 - r^2/R^2)^alpha from Sv = 1 - r^2/R^2: S*S, then alpha - 2 more factors (runtime alpha unless A2)
+template <bool A2, typename T>
+__device__ __forceinline__ T sf_power(T Sv) {
+  T S1 = Sv * Sv;
+  if constexpr (!A2)
+    for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+  return S1;
+}
+
+template <int N, bool MIXED, bool ADAPT, bool A2>
 __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L, const int* __restrict__ off,
                                                             SfPack K, double* __restrict__ PS) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
@@ -1108,8 +1117,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
           const float2 rp = ADAPT ? s_rp[q] : make_float2((float)c_k.sf_r2, (float)R2inv);
           if (r2 <= rp.x) {
             const float Sv = fmaf(-rp.y, r2, 1.0f);
-            float S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            const float S1 = sf_power<A2>(Sv);
             const float4 f = s_facf[q];
             part[0] = fmaf(S1, f.x, part[0]);
             part[1] = fmaf(S1, f.y, part[1]);
@@ -1122,8 +1130,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
                                   : fma(pa.x, gd[0], fma(pa.y, gd[1], fma(pb.x, gd[2], pb.y + gd[3])));
           // Sv >= 0 read from the sign bit (integer pipe); -0.0 is skipped, its contribution is 0
           if (__double_as_longlong(Sv) >= 0) {
-            double S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            const double S1 = sf_power<A2>(Sv);
             const double2 f01 = s_fac[2 * q], f23 = s_fac[2 * q + 1];
             acc[0] = fma(S1, f01.x, acc[0]);
             acc[1] = fma(S1, f01.y, acc[1]);
@@ -1552,8 +1559,9 @@ int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers
 template <int N, bool MIXED>
 static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
 #if PIC_SF_GATHER == 5
-  if (L.elem_r) k_sf_gather5<N, MIXED, true><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-  else k_sf_gather5<N, MIXED, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  if (L.elem_r) k_sf_gather5<N, MIXED, true, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  else if (A.sf_alpha == 2) k_sf_gather5<N, MIXED, false, true><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  else k_sf_gather5<N, MIXED, false, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #else
   k_sf_gather2<N, MIXED><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #endif

@@ -18,6 +18,7 @@ struct LaunchArgs {
   MeshF MF;
   int N, nd, n_canon;
   bool mixed;
+  int sf_alpha;          // PIC-shapefunction-alpha (the gather has a compile-time branch for 2)
   const double* E;       // [ne][nd][3]
   const float* E32;      // [ne][nd][3] (mixed)
   double* NS;            // [n_canon][4] CVWM node sums
