@@ -669,6 +669,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   if (c->sf) {
     // the largest radius (adaptive: the per-element radii bound the searches; exact per-particle radii in the kernels)
     k.sf_r = c->sf_rmax; k.sf_r2 = c->sf_rmax * c->sf_rmax; k.sf_r2_inv = 1.0 / k.sf_r2;
+    k.sf_r_inv = (float)(1.0 / c->sf_rmax);
     k.sf_alpha = cfg->sf_alpha;
     k.sf_w = c->cc ? 1.0 : sf_weight_dim(cfg, m, cfg->sf_radius, cfg->sf_alpha);   // cc: Fac = q MPF (v,1), normalised later
     bool keep[3];

@@ -6,6 +6,7 @@
 #include "pic_kernels.cuh"
 
 #include <cstdio>
+#include <cuda_fp16.h>
 
 namespace pic {
 
@@ -985,8 +986,15 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
   __shared__ double s_rinv[ADAPT && !MIXED ? kSf5Pairs : 1];      // 1/R_s^2
   __shared__ float2 s_rpf[ADAPT && MIXED ? kSf5Pairs : 1];        // (R_s^2, 1/R_s^2)
   __shared__ float2 s_rp[ADAPT && MIXED ? kSf5Chunk : 1];         // the same per staged particle
+  // mixed, one radius: the pre-test on two staged particles per instruction in packed FP16, positions in
+  // units of R relative to the target's DOF centre; entry i*npar + p holds the slots p + npar*2i and
+  // p + npar*(2i+1) of parity p (see the comment at phase A)
+  // (mixed uses s_pq only for the final per-DOF sums, so the FP16 copy lives there)
+  constexpr bool H2 = MIXED && !ADAPT;
   __shared__ int s_cnt, s_max;
   static_assert(sizeof(double) * 4 * npar * (halves * 32) <= sizeof(double2) * 2 * kSf5Chunk, "sums alias s_pq");
+  static_assert(sizeof(__half2) * 3 * (kSf5Chunk / 2 + 4) <= sizeof(double2) * 2 * kSf5Chunk, "FP16 set aliases s_pq");
+  __half2 (*s_h)[3] = reinterpret_cast<__half2 (*)[3]>(s_pq);
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int dof = (w % halves) * 32 + lane, parity = w / halves;
   const bool active = dof < nd;
@@ -997,6 +1005,8 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
   const float R2f = (float)(c_k.sf_r2 * (1.0 + 1.0e-4));
   const float cull = (float)c_k.sf_r + __ldg(L.dof_radius + e);
   const float cull2 = cull * cull * 1.0001f;
+  // FP16 pre-test where |p|/R + |g|/R <= 5 (DOF-box radius <= 2R), which bounds its r^2/R^2 error by 1.5e-2
+  const bool h2 = H2 && __ldg(L.dof_radius + e) <= 2.0f * (float)c_k.sf_r;
   double gd[4] = {0.0, 0.0, 0.0, 0.0};
   float gf[3] = {0.f, 0.f, 0.f};
   if (active) {
@@ -1098,13 +1108,46 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
         }
         __syncthreads();
       }
+      const int nper = (nst + npar - 1) / npar, np2 = (nper + 1) / 2;   // slots and slot pairs per parity
+      if (h2) {
+        // packed FP16 copy of the set for the pre-test (a missing partner sits far away: r^2 overflows)
+        for (int i = t; i < npar * np2; i += kSf5Threads) {
+          const int p = i % npar, k = i / npar;
+          const int a = p + npar * (2 * k), b = a + npar;
+          const float4 ra = a < nst ? s_rel[a] : make_float4(1e3f, 1e3f, 1e3f, 0.f);
+          const float4 rb = b < nst ? s_rel[b] : make_float4(1e3f, 1e3f, 1e3f, 0.f);
+          const float ir = c_k.sf_r_inv;
+          s_h[i][0] = __floats2half2_rn(ra.x * ir, rb.x * ir);
+          s_h[i][1] = __floats2half2_rn(ra.y * ir, rb.y * ir);
+          s_h[i][2] = __floats2half2_rn(ra.z * ir, rb.z * ir);
+        }
+        __syncthreads();
+      }
       if (!active) continue;
-      // phase A: FP32 test of this lane's DOF against its parity's particles
+      // phase A: test of this lane's DOF against its parity's particles, into the lane's hit list (slot
+      // index / npar, ascending).  FP32 with (1+1e-4) R^2; mixed with one radius and a DOF box within 2R:
+      // packed FP16 in units of R against 1.05 (error of r^2/R^2 below 1.5e-2 near the threshold), two
+      // particles per instruction.  Either way phase B repeats the exact test, so only the work changes.
       int nh = 0;
-      for (int m = 0; parity + npar * m < nst; ++m) {
-        const float4 r = s_rel[parity + npar * m];
-        const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f)) s_list[w][nh++][lane] = (uint8_t)m;
+      if (h2) {
+        const float ir = c_k.sf_r_inv;
+        const __half2 gx = __float2half2_rn(gf[0] * ir), gy = __float2half2_rn(gf[1] * ir),
+                      gz = __float2half2_rn(gf[2] * ir);
+        const __half2 thr = __float2half2_rn(1.05f);
+        for (int k = 0; k < np2; ++k) {
+          const __half2* e = s_h[k * npar + parity];
+          const __half2 dx = __hsub2(e[0], gx), dy = __hsub2(e[1], gy), dz = __hsub2(e[2], gz);
+          const __half2 r2 = __hfma2(dx, dx, __hfma2(dy, dy, __hmul2(dz, dz)));
+          const unsigned msk = __hle2_mask(r2, thr);
+          if (msk & 0xFFFFu) s_list[w][nh++][lane] = (uint8_t)(2 * k);
+          if (msk & 0xFFFF0000u) s_list[w][nh++][lane] = (uint8_t)(2 * k + 1);
+        }
+      } else {
+        for (int m = 0; parity + npar * m < nst; ++m) {
+          const float4 r = s_rel[parity + npar * m];
+          const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
+          if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f)) s_list[w][nh++][lane] = (uint8_t)m;
+        }
       }
       // phase B: this lane's hits
       float part[4] = {0.f, 0.f, 0.f, 0.f};      // mixed: this staged set's FP32 partial sums
