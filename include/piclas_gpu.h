@@ -107,7 +107,7 @@ typedef struct pic_config_t {
   int32_t sort_interval;        /* re-sort particles by element every k steps (0: never) */
   /* PIC-shapefunction-dimension (1, 2, 3; 0 = 3), -direction (1D: the direction of the kernel, 2D: the
    * direction in which it is constant) and -3D-deposition (1: charge over the volume, 0: over the line /
-   * area); 1D and 2D kernels with plain shape_function only (InitShapeFunctionDimensionalty,
+   * area); for every shape-function deposition (InitShapeFunctionDimensionalty,
    * pic_depo_shapefunction_tools.f90:1131-1294) */
   int32_t sf_dim;
   int32_t sf_dir;

@@ -1141,6 +1141,22 @@ static double sf_norm(const sf_geom_t* g, const double v[3]) {
   return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
 }
 
+/* dimFactorSF (InitShapeFunctionDimensionalty): 1D the cross-section across the kernel direction, 2D the
+ * extent along the constant direction; 1 for the 3D kernel.  sf_charge_on_line: 1D/2D kernels with
+ * PIC-shapefunction-3D-deposition = F, whose charge-conserving totals are divided by it */
+static double sf_dim_factor(const pic_config_t* cfg, const pic_mesh_t* m) {
+  const sf_geom_t g = sf_geom(cfg);
+  double ext[3];
+  for (int d = 0; d < 3; ++d) ext[d] = m->xmax_glob[d] - m->xmin_glob[d];
+  if (g.dim == 1) return (g.dir == 0) ? ext[1] * ext[2] : (g.dir == 1) ? ext[0] * ext[2] : ext[0] * ext[1];
+  if (g.dim == 2) return ext[g.dir];
+  return 1.0;
+}
+static int sf_charge_on_line(const pic_config_t* cfg) {
+  const sf_geom_t g = sf_geom(cfg);
+  return g.dim < 3 && !cfg->sf_depo3d;
+}
+
 static double sf_w(const pic_config_t* cfg, const pic_mesh_t* m, double r_sf, int alpha) {
   const double PI = acos(-1.0);
   const sf_geom_t g = sf_geom(cfg);
@@ -1242,44 +1258,51 @@ static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m,
       }
 }
 
-/* calcTotalChargePeriodic_cc, pic_depo_shapefunction_tools.f90:425-555 (dim_sf = 3): the quadrature
- * integral sum wGP(k) wGP(l) wGP(m) Fac S1 / sJ over the DOFs within r_sf of one (shifted) position, added
- * term by term to the running total (totalChargePeriodicSF is INOUT across the 27 images) */
+/* the FIBGM cell range of calcTotalChargePeriodic_cc / depoChargeOnDOFsSF(ChargeCon)
+ * (pic_depo_shapefunction_tools.f90:330-377): within r_sf of P along the kernel directions, every cell
+ * across the others, clamped to the grid */
+static void sf_cell_range(const sf_geom_t* g, const pic_mesh_t* m, const double P[3], double r_sf, int lo[3], int hi[3]) {
+  int full[3] = {0, 0, 0};
+  if (g->dim == 2) full[g->dir] = 1;
+  else if (g->dim == 1) { full[0] = full[1] = full[2] = 1; full[g->dir] = 0; }
+  for (int d = 0; d < 3; ++d) {
+    hi[d] = (int)ceil((P[d] + r_sf - m->xmin_glob[d]) / m->fibgm_deltas[d]);
+    lo[d] = (int)floor((P[d] - r_sf - m->xmin_glob[d]) / m->fibgm_deltas[d] + 1);
+    if (full[d]) { lo[d] = 1; hi[d] = m->fibgm_imax[d]; }
+    if (hi[d] > m->fibgm_imax[d]) hi[d] = m->fibgm_imax[d];
+    if (lo[d] < 1) lo[d] = 1;
+  }
+}
+
+/* calcTotalChargePeriodic_cc, pic_depo_shapefunction_tools.f90:425-555: the quadrature integral
+ * sum wGP(k) wGP(l) wGP(m) Fac S1 / sJ over the DOFs within r_sf (SFRadius2) of one (shifted) position, added
+ * term by term to the running total (totalChargePeriodicSF is INOUT across the periodic cases) */
 static double total_charge_cc(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], double Fac4,
                               double totalCharge, double r_sf, double r2_sf, double r2_sf_inv, uint8_t* done) {
   const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const sf_geom_t g = sf_geom(cfg);
   memset(done, 0, (size_t)m->n_elems);
-  int kmax = (int)ceil((P[0] + r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0]);
-  int kmin = (int)floor((P[0] - r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0] + 1);
-  int lmax = (int)ceil((P[1] + r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1]);
-  int lmin = (int)floor((P[1] - r_sf - m->xmin_glob[1]) / m->fibgm_deltas[1] + 1);
-  int mmax = (int)ceil((P[2] + r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2]);
-  int mmin = (int)floor((P[2] - r_sf - m->xmin_glob[2]) / m->fibgm_deltas[2] + 1);
-  if (kmax > m->fibgm_imax[0]) kmax = m->fibgm_imax[0];
-  if (kmin < 1) kmin = 1;
-  if (lmax > m->fibgm_imax[1]) lmax = m->fibgm_imax[1];
-  if (lmin < 1) lmin = 1;
-  if (mmax > m->fibgm_imax[2]) mmax = m->fibgm_imax[2];
-  if (mmin < 1) mmin = 1;
-  for (int kk = kmin; kk <= kmax; ++kk)
-    for (int ll = lmin; ll <= lmax; ++ll)
-      for (int mm = mmin; mm <= mmax; ++mm) {
+  int lo[3], hi[3];
+  sf_cell_range(&g, m, P, r_sf, lo, hi);
+  for (int kk = lo[0]; kk <= hi[0]; ++kk)
+    for (int ll = lo[1]; ll <= hi[1]; ++ll)
+      for (int mm = lo[2]; mm <= hi[2]; ++mm) {
         size_t cidx = (size_t)(kk - 1) + (size_t)m->fibgm_imax[0] * ((ll - 1) + (size_t)m->fibgm_imax[1] * (mm - 1));
         int nE = m->fibgm_n_elems[cidx], off = m->fibgm_offset[cidx];
         for (int q = 0; q < nE; ++q) {
           int e = m->fibgm_element[off + q];
           if (done[e - 1]) continue;
           const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
-          double v0 = P[0] - b[0], v1 = P[1] - b[1], v2 = P[2] - b[2];
-          if (sqrt(v0 * v0 + v1 * v1 + v2 * v2) > (r_sf + m->elem_radius[e - 1])) continue;
+          const double vb[3] = {P[0] - b[0], P[1] - b[1], P[2] - b[2]};
+          if (sf_norm(&g, vb) > (r_sf + m->elem_radius[e - 1])) continue;
           const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
           const double* sj = &m->elem_sj[(size_t)(e - 1) * ndof];
           for (int mz = 0; mz <= N; ++mz)
             for (int l = 0; l <= N; ++l)
               for (int k = 0; k <= N; ++k) {
                 int r = mz * n1 * n1 + l * n1 + k;
-                double d0 = P[0] - xg[(size_t)r * 3], d1 = P[1] - xg[(size_t)r * 3 + 1], d2 = P[2] - xg[(size_t)r * 3 + 2];
-                double radius2 = (d0 * d0 + d1 * d1) + d2 * d2;
+                const double dv[3] = {P[0] - xg[(size_t)r * 3], P[1] - xg[(size_t)r * 3 + 1], P[2] - xg[(size_t)r * 3 + 2]};
+                double radius2 = sf_radius2(&g, dv);
                 if (radius2 <= r2_sf) {
                   double S = 1.0 - r2_sf_inv * radius2;
                   double S1 = S * S;
@@ -1346,13 +1369,15 @@ static int build_elem_to_elem(const pic_mesh_t* m, int** off_out, int** info_out
  * and those whose barycentre lies beyond R + ElemRadiusNGeo.  ChargeCon evaluates S = 1 - R^-2 r^2,
  * Adaptive S = 1 - r^2/R^2.  The pass that deposits repeats the first pass's arithmetic. */
 static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], const double Fac[4],
-                            double r_sf, double r2_sf, double r2_sf_inv, int divide, const int* list, int nlist,
-                            double* PS, uint8_t* done, int* used) {
+                            double r_sf, double r2_sf, double r2_sf_inv, int divide, double total_div,
+                            const int* list, int nlist, double* PS, uint8_t* done, int* used) {
   const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const sf_geom_t g = sf_geom(cfg);
   memset(done, 0, (size_t)m->n_elems);
   int nused = 0;
   double totalCharge = 0.0;
   for (int pass = 0; pass < 2; ++pass) {
+    if (pass && total_div != 1.0) totalCharge = totalCharge / total_div;     /* the Adaptive branch, :881-884 */
     const double alpha = pass ? Fac[3] / totalCharge : 0.0;
     const int n = pass ? nused : nlist;
     for (int q = 0; q < n; ++q) {
@@ -1360,8 +1385,8 @@ static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const 
       if (!pass) {
         if (done[e - 1]) continue;
         const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
-        const double v0 = P[0] - b[0], v1 = P[1] - b[1], v2 = P[2] - b[2];
-        if (sqrt(v0 * v0 + v1 * v1 + v2 * v2) > (r_sf + m->elem_radius[e - 1])) continue;
+        const double vb[3] = {P[0] - b[0], P[1] - b[1], P[2] - b[2]};
+        if (sf_norm(&g, vb) > (r_sf + m->elem_radius[e - 1])) continue;
       }
       const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
       const double* sj = &m->elem_sj[(size_t)(e - 1) * ndof];
@@ -1371,8 +1396,8 @@ static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const 
         for (int l = 0; l <= N; ++l)
           for (int k = 0; k <= N; ++k) {
             const int r = mz * n1 * n1 + l * n1 + k;
-            const double d0 = P[0] - xg[(size_t)r * 3], d1 = P[1] - xg[(size_t)r * 3 + 1], d2 = P[2] - xg[(size_t)r * 3 + 2];
-            const double radius2 = (d0 * d0 + d1 * d1) + d2 * d2;
+            const double dv[3] = {P[0] - xg[(size_t)r * 3], P[1] - xg[(size_t)r * 3 + 1], P[2] - xg[(size_t)r * 3 + 2]};
+            const double radius2 = sf_radius2(&g, dv);
             if (!(radius2 <= r2_sf)) continue;
             hit = 1;
             const double S = divide ? 1.0 - radius2 / r2_sf : 1.0 - r2_sf_inv * radius2;
@@ -1393,17 +1418,14 @@ static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const 
   }
 }
 
-/* the FIBGM cells within r_sf of P (clamped to the grid, dim_sf = 3), their elements in visiting order,
+/* the FIBGM cells of sf_cell_range, their elements in visiting order,
  * each at its first appearance (a later one is skipped or fails the same barycentre test) */
-static int fibgm_visit_list(const pic_mesh_t* m, const double P[3], double r_sf, int* list, uint8_t* seen) {
+static int fibgm_visit_list(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], double r_sf, int* list,
+                            uint8_t* seen) {
   int lo[3], hi[3], n = 0;
+  const sf_geom_t g = sf_geom(cfg);
   memset(seen, 0, (size_t)m->n_elems);
-  for (int d = 0; d < 3; ++d) {
-    hi[d] = (int)ceil((P[d] + r_sf - m->xmin_glob[d]) / m->fibgm_deltas[d]);
-    lo[d] = (int)floor((P[d] - r_sf - m->xmin_glob[d]) / m->fibgm_deltas[d] + 1);
-    if (hi[d] > m->fibgm_imax[d]) hi[d] = m->fibgm_imax[d];
-    if (lo[d] < 1) lo[d] = 1;
-  }
+  sf_cell_range(&g, m, P, r_sf, lo, hi);
   for (int kk = lo[0]; kk <= hi[0]; ++kk)
     for (int ll = lo[1]; ll <= hi[1]; ++ll)
       for (int mm = lo[2]; mm <= hi[2]; ++mm) {
@@ -1477,14 +1499,12 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
       if (nCases > 1) {
         if (cfg->deposition == PIC_DEPO_SHAPE_FUNCTION_CC || adaptive) {
           double totalCharge = 0.0;
-          for (int ic = 0; ic < 27; ++ic) {
-            double c1 = (double)(1 - ic / 9), c2 = (double)(1 - (ic / 3) % 3), c3 = (double)(1 - ic % 3);
+          for (int ic = 0; ic < nCases; ++ic) {
             double Ps[3];
-            for (int d = 0; d < 3; ++d)
-              Ps[d] = s[d] + c1 * m->periodic_vectors[0 * 3 + d] + c2 * m->periodic_vectors[1 * 3 + d] +
-                      c3 * m->periodic_vectors[2 * 3 + d];
+            sf_shifted(&gsf, m, ic, s, Ps);
             totalCharge = total_charge_cc(cfg, m, Ps, Fac[3], totalCharge, r_sf_p, r2_sf_p, r2_sf_inv_p, done);
           }
+          if (sf_charge_on_line(cfg)) totalCharge = totalCharge / sf_dim_factor(cfg, m);   /* :117-119 */
           const double f4 = Fac[3];
           for (int v = 0; v < 4; ++v) Fac[v] = Fac[v] * f4 / totalCharge;
         } else {
@@ -1505,9 +1525,11 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
           nl = 1;
           for (int j = e2e_off[e0 - 1]; j < e2e_off[e0]; ++j) list[nl++] = e2e_info[j];
         } else {
-          nl = fibgm_visit_list(m, s, r_sf, list, done);
+          nl = fibgm_visit_list(cfg, m, s, r_sf, list, done);
         }
-        depo_charge_con(cfg, m, s, Fac, r_sf_p, r2_sf_p, r2_sf_inv_p, adaptive, list, nl, my, done, used);
+        /* only the Adaptive branch divides its total by dimFactorSF (:881-884; ChargeCon does not) */
+        const double tdiv = adaptive && sf_charge_on_line(cfg) ? sf_dim_factor(cfg, m) : 1.0;
+        depo_charge_con(cfg, m, s, Fac, r_sf_p, r2_sf_p, r2_sf_inv_p, adaptive, tdiv, list, nl, my, done, used);
       } else {
         double Fw[4];
         for (int v = 0; v < 4; ++v) Fw[v] = Fac[v] * w_sf;

@@ -104,6 +104,17 @@ double sf_weight_dim(const pic_config_t* cfg, const pic_mesh_t* m, double r, int
   return cfg->sf_depo3d ? ((double)alpha + 1.0) / (PI * (r * r) * ext[dir]) : ((double)alpha + 1.0) / (PI * (r * r));
 }
 
+// dimFactorSF (InitShapeFunctionDimensionalty): 1D the cross-section across the kernel direction, 2D the
+// extent along the constant direction, 1 for the 3D kernel
+static double sf_dim_factor(const pic_config_t* cfg, const pic_mesh_t* m) {
+  const int dim = cfg->sf_dim ? cfg->sf_dim : 3, dir = cfg->sf_dir - 1;
+  double ext[3];
+  for (int d = 0; d < 3; ++d) ext[d] = m->xmax_glob[d] - m->xmin_glob[d];
+  if (dim == 1) return (dir == 0) ? ext[1] * ext[2] : (dir == 1) ? ext[0] * ext[2] : ext[0] * ext[1];
+  if (dim == 2) return ext[dir];
+  return 1.0;
+}
+
 // directions in which a 1D/2D shape function has its kernel (the others are zeroed in the DOF and particle
 // coordinates the gather reads, so the kernel sees SFRadius2, pic_depo_shapefunction_tools.f90:1029-1058)
 void sf_kernel_dirs(const pic_config_t* cfg, bool keep[3]) {
@@ -115,8 +126,8 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   if (!cfg || !m) return fail(PIC_ERR_INVALID_ARGUMENT, "null config or mesh");
   if (cfg->sf_dim < 0 || cfg->sf_dim > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "sf_dim must be 1, 2 or 3 (0 = 3)");
   if (cfg->sf_dim == 1 || cfg->sf_dim == 2) {
-    if (cfg->deposition != PIC_DEPO_SHAPE_FUNCTION)
-      return fail(PIC_ERR_INVALID_ARGUMENT, "1D/2D shape functions are built for plain shape_function");
+    if (cfg->deposition == PIC_DEPO_CVWM)
+      return fail(PIC_ERR_INVALID_ARGUMENT, "sf_dim applies to the shape-function depositions");
     if (cfg->sf_dir < 1 || cfg->sf_dir > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "sf_dir must be 1..3");
     if (m->n_periodic_vectors != 0 && m->n_periodic_vectors != 3)
       return fail(PIC_ERR_INVALID_ARGUMENT, "1D/2D shape functions need a mesh with no or three periodic vectors");
@@ -672,6 +683,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     k.sf_r_inv = (float)(1.0 / c->sf_rmax);
     k.sf_alpha = cfg->sf_alpha;
     k.sf_w = c->cc ? 1.0 : sf_weight_dim(cfg, m, cfg->sf_radius, cfg->sf_alpha);   // cc: Fac = q MPF (v,1), normalised later
+    // 1D/2D charge-conserving kernels with the charge on a line / an area (PIC-shapefunction-3D-deposition
+    // = F): the periodic branch and the Adaptive routine divide their totals by dimFactorSF
+    // (calcSfSource:117-119, depoChargeOnDOFsSFAdaptive:881-884); depoChargeOnDOFsSFChargeCon does not
+    const bool on_line = (cfg->sf_dim == 1 || cfg->sf_dim == 2) && !cfg->sf_depo3d;
+    k.sf_cc_div = (c->cc && on_line && (m->n_periodic_vectors > 0 || c->adaptive)) ? sf_dim_factor(cfg, m) : 1.0;
     bool keep[3];
     sf_kernel_dirs(cfg, keep);
     for (int d = 0; d < 3; ++d) k.sf_keep[d] = keep[d] ? 1 : 0;

@@ -1326,7 +1326,7 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
       cc_eval<N, MIXED>(s_g, s_gf, s_list, nh, p, pf, R2, R2inv, acc, accf);
     }
     if (act) {
-      const double tot = MIXED ? (double)accf : acc;
+      const double tot = (MIXED ? (double)accf : acc) / c_k.sf_cc_div;
       const bool ok = tot > 0.0;
       // no DOF within R: with periodic images the reference divides by zero (calcSfSource:122); without,
       // it deposits nothing (nUsedElems = 0), as the zero scale does here

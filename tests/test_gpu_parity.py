@@ -771,3 +771,25 @@ def test_shape_function_1d_2d_against_oracle(gpu_lib, oracle_lib, dim, sf_dir, d
     assert _rel(g["PS"], PS) <= 1e-12
     gm = _run_gpu(w, 4, precision=capi.PIC_PREC_MIXED)
     assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-6
+
+
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+@pytest.mark.parametrize("walls,dim,sf_dir,depo3d", [(False, 1, 1, False), (False, 2, 3, True),
+                                                     (True, 1, 2, True), (True, 2, 1, False)])
+def test_charge_conserving_sf_1d_2d_against_oracle(gpu_lib, oracle_lib, dep, walls, dim, sf_dir, depo3d):
+    """1D/2D shape_function_cc / _adaptive (periodic images or walls, charge on the volume or on the line /
+    area): FP64 within 1e-12 of the oracle's maximum, mixed within 1e-6, particles bit-exact."""
+    bc = ("reflective", "open", "reflective") if walls else ("periodic",) * 3
+    mesh = build_box_mesh(4, 4, 4, 2, hi=(1.0, 0.5, 0.8), bc=bc)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=3000, seed=42, T_eV=200.0)
+    w.deposition = dep
+    w.sf_radius, w.sf_alpha = 0.3, 3
+    w.sf_dim, w.sf_dir, w.sf_depo3d = dim, sf_dir, depo3d
+    w.mesh.sf_elem_radius = np.random.default_rng(42).uniform(0.25, 0.45, mesh.n_elems)
+    g = _run_gpu(w, 4)
+    st, PS = _run_oracle(oracle_lib, w, 4)
+    assert np.array_equal(g["elem"], st.elem) and np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0
+    gm = _run_gpu(w, 4, precision=capi.PIC_PREC_MIXED)
+    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-6

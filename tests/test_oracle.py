@@ -577,3 +577,38 @@ def test_adaptive_with_initialised_radius_conserves_charge(oracle_lib):
     oracle_lib.deposit(cfg, ms, st, PS)
     total = w.n * w.species[0][0] * w.species[0][2]
     assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - total) <= 1e-12 * abs(total)
+
+
+# ---- 1D/2D shape_function_cc / _adaptive -------------------------------------------------------------
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+@pytest.mark.parametrize("walls", [False, True])
+@pytest.mark.parametrize("dim,sf_dir,depo3d", [(1, 1, True), (1, 3, False), (2, 2, True), (2, 1, False)])
+def test_sf_1d_2d_charge_conserving(oracle_lib, dep, walls, dim, sf_dir, depo3d):
+    """Integrated deposit per particle: q MPF, times dimFactorSF where the charge sits on a line / an area
+    (3D-deposition = F) and the branch divides its total by it (the periodic branch and the Adaptive routine;
+    ChargeCon without periodic vectors does not).  rho depends on the kernel coordinates only."""
+    hi = (1.0, 0.5, 0.8)
+    bc = ("reflective", "open", "reflective") if walls else ("periodic",) * 3
+    mesh = build_box_mesh(4, 4, 4, 2, hi=hi, bc=bc)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=300, seed=22)
+    w.deposition = dep
+    w.sf_radius, w.sf_alpha = 0.3, 3
+    w.sf_dim, w.sf_dir, w.sf_depo3d = dim, sf_dir, depo3d
+    w.mesh.sf_elem_radius = np.random.default_rng(22).uniform(0.25, 0.45, mesh.n_elems)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS)
+    d = sf_dir - 1
+    dim_factor = float(np.prod([hi[a] for a in range(3) if a != d])) if dim == 1 else hi[d]
+    divides = not depo3d and (not walls or dep == capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE)
+    total = w.n * w.species[0][0] * w.species[0][2] * (dim_factor if divides else 1.0)
+    assert abs(oracle_lib.integrate_charge(ms, w.mesh.N, PS) - total) <= 1e-12 * abs(total)
+    if dep == capi.PIC_DEPO_SHAPE_FUNCTION_CC:
+        xg = w.mesh.elem_xgp.reshape(-1, 3)
+        kdirs = [d] if dim == 1 else [a for a in range(3) if a != d]
+        _, inv = np.unique(np.round(xg[:, kdirs], 12), axis=0, return_inverse=True)
+        rho = PS[..., 3].reshape(-1)
+        for k in range(inv.max() + 1):
+            v = rho[inv == k]
+            assert np.allclose(v, v[0], rtol=1e-11, atol=1e-11 * np.abs(rho).max())
