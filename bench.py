@@ -57,11 +57,14 @@ def make_workload(name: str, seed: int, n_override: int | None = None, cells: in
 def workload_config(w, name):
     m = w.mesh
     if name == "curved":
-        return {"workload": "plain FP64 at scale: 32^3 curved hex, N=3, 8M e- + 8M ions, B_z=0.1 T, "
-                            "RefTracking, shape_function r=1.5h, dt=5e-12",
+        cells = round(m.n_elems ** (1.0 / 3.0))
+        tag = "plain FP64 at scale: " if (cells == 32 and w.n == 16_000_000) else "profiling case of plain FP64 at scale: "
+        return {"workload": f"{tag}{cells}^3 curved hex, N={m.N}, {w.n // 2} e- + {w.n - w.n // 2} ions, "
+                            "B_z=0.1 T, RefTracking, shape_function r=1.5h, dt=5e-12",
                 "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "shape_function",
                 "tracking": "RefTracking (CartesianPeriodic/FastPeriodic)", "l2": "inputs larger than L2 (no flush)"}
-    return {"workload": "plasma wave: 8^3 hex, N=3, 200k e-, CVWM, TriaTracking, dt=1e-11",
+    cells = round(m.n_elems ** (1.0 / 3.0))
+    return {"workload": f"plasma wave: {cells}^3 hex, N={m.N}, {w.n} e-, CVWM, TriaTracking, dt=1e-11",
             "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "cell_volweight_mean",
             "tracking": "TriaTracking", "l2": "L2 flushed between timed steps"}
 
