@@ -637,6 +637,16 @@ def run_batch(args):
                       "max_rho_rel_err": max(r["rho_rel_err_vs_fp64"] for r in out)}), flush=True)
 
 
+def reference_config(args):
+    """The config of this arm's line for the same flags (the reference computes in FP64 whatever the
+    precision flag says)."""
+    from types import SimpleNamespace as NS
+    cells, n = {"curved": (32, 16_000_000), "plasma_wave": (8, 200_000)}.get(args.workload, (8, 200_000))
+    stand_in = NS(mesh=NS(n_elems=cells ** 3, N=3), n=n)
+    return dict(workload_config(stand_in, args.workload if args.workload == "curved" else "plasma_wave"),
+                precision=args.precision, parallelism=f"replicas x{args.gpus}")
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -647,7 +657,7 @@ def run_reference(args, rank):
     out = {"metric": METRIC, "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded), frozen field",
-           "impl": "reference", "config": {"workload": args.workload, "precision": "fp64"},
+           "impl": "reference", "config": reference_config(args),
            "cpu_baseline": base,
            "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
