@@ -1235,9 +1235,9 @@ template <int N>
 __host__ __device__ constexpr int cc_round() { return (N + 1) * (N + 1) * (N + 1) > 64 ? 2 : 4; }
 constexpr int kCcCap = 256;       // hit-list entries per thread: a whole round (ns <= 256), so no lane flushes alone
 
-template <int N, bool MIXED>
-__device__ __forceinline__ void cc_eval(const double (*s_g)[4], const float4* s_gf, const uint8_t (*s_list)[kCcThreads],
-                                        int nh, const double p[3], const float pf[3], double R2, double R2inv,
+template <int N, bool MIXED, bool A2>
+__device__ __forceinline__ void cc_eval(const double (*s_g)[5], const float4* s_gf, const uint8_t (*s_list)[kCcThreads],
+                                        int nh, const double p[4], const float pf[3], double R2, double R2inv,
                                         double& acc, float& accf) {
   const int t = threadIdx.x;
   for (int k = 0; k < nh; ++k) {
@@ -1248,28 +1248,23 @@ __device__ __forceinline__ void cc_eval(const double (*s_g)[4], const float4* s_
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       if (r2 <= (float)R2) {
         const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
-        float S1 = Sv * Sv;
-        for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
-        accf = fmaf(g.w, S1, accf);
+        accf = fmaf(g.w, sf_power<A2>(Sv), accf);
       }
     } else {
-      const double d0 = p[0] - s_g[d][0], d1 = p[1] - s_g[d][1], d2 = p[2] - s_g[d][2];
-      const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
-      if (r2 <= R2) {
-        const double Sv = fma(-R2inv, r2, 1.0);
-        double S1 = Sv * Sv;
-        for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
-        acc = fma(s_g[d][3], S1, acc);
-      }
+      // 1 - |p-g|^2/R^2 = A_p + p'.g + B_g (p' = 2p/R^2, A_p = 1 - |p|^2/R^2, B_g = -|g|^2/R^2, all relative to
+      // the source's DOF centre): one add and three fused multiply-adds; r^2 <= R^2 read from the sign
+      const double Sv = fma(p[0], s_g[d][0], fma(p[1], s_g[d][1], fma(p[2], s_g[d][2], p[3] + s_g[d][4])));
+      if (__double_as_longlong(Sv) >= 0) acc = fma(s_g[d][3], sf_power<A2>(Sv), acc);
     }
   }
 }
 
-template <int N, bool MIXED>
+template <int N, bool MIXED, bool A2>
 __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L, const int* __restrict__ off, SfPack K,
                                                            DevStatus* st) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1, ns = cc_round<N>() * nd;
-  __shared__ double s_g[MIXED ? 1 : ns][4];     // DOF position minus the image shift; wGP^3/sJ
+  __shared__ double s_g[MIXED ? 1 : ns][5];     // DOF position minus the image shift, relative to the source's
+                                                // DOF centre; wGP^3/sJ; -|g|^2/R^2
   __shared__ float4 s_gf[ns];                   // FP32 position relative to the source's DOF centre; w = weight
   __shared__ uint8_t s_list[kCcCap][kCcThreads];
   static_assert(ns <= kCcCap, "a round's DOFs must fit one hit list");
@@ -1287,12 +1282,18 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
   for (int base = 0; base < cnt; base += kCcThreads) {
     const int j = b0 + base + t;
     const bool act = base + t < cnt;
-    double p[3] = {0.0, 0.0, 0.0};
+    double p[4] = {0.0, 0.0, 0.0, 0.0};           // FP64: p' = 2p/R^2 and A_p = 1 - |p|^2/R^2
     float pf[3] = {0.f, 0.f, 0.f};
     if (act) {
       const float4 r = reinterpret_cast<const float4*>(K.posf)[j];     // relative to the source DOF centre
       pf[0] = r.x; pf[1] = r.y; pf[2] = r.z;
-      if constexpr (!MIXED) { p[0] = K.pos[3 * (size_t)j]; p[1] = K.pos[3 * (size_t)j + 1]; p[2] = K.pos[3 * (size_t)j + 2]; }
+      if constexpr (!MIXED) {
+        const double px = K.pos[3 * (size_t)j] - csx, py = K.pos[3 * (size_t)j + 1] - csy,
+                     pz = K.pos[3 * (size_t)j + 2] - csz;
+        const double t2 = 2.0 * R2inv;
+        p[0] = px * t2; p[1] = py * t2; p[2] = pz * t2;
+        p[3] = fma(-R2inv, fma(px, px, fma(py, py, pz * pz)), 1.0);
+      }
     }
     double acc = 0.0;
     float accf = 0.f;
@@ -1312,8 +1313,12 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
         const double* g = M.sf_xgp + ((size_t)e * nd + d) * 3;
         const double gx = __ldg(g) - sh[0], gy = __ldg(g + 1) - sh[1], gz = __ldg(g + 2) - sh[2];
         const double wgt = __ldg(L.dof_w + (size_t)e * nd + d);
-        if constexpr (!MIXED) { s_g[i][0] = gx; s_g[i][1] = gy; s_g[i][2] = gz; s_g[i][3] = wgt; }
-        s_gf[i] = make_float4((float)(gx - csx), (float)(gy - csy), (float)(gz - csz), (float)wgt);
+        const double rx = gx - csx, ry = gy - csy, rz = gz - csz;
+        if constexpr (!MIXED) {
+          s_g[i][0] = rx; s_g[i][1] = ry; s_g[i][2] = rz; s_g[i][3] = wgt;
+          s_g[i][4] = -R2inv * fma(rx, rx, fma(ry, ry, rz * rz));
+        }
+        s_gf[i] = make_float4((float)rx, (float)ry, (float)rz, (float)wgt);
       }
       __syncthreads();
       if (!act) continue;
@@ -1323,7 +1328,7 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
         const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
         if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[nh++][t] = (uint8_t)i;
       }
-      cc_eval<N, MIXED>(s_g, s_gf, s_list, nh, p, pf, R2, R2inv, acc, accf);
+      cc_eval<N, MIXED, A2>(s_g, s_gf, s_list, nh, p, pf, R2, R2inv, acc, accf);
     }
     if (act) {
       const double tot = (MIXED ? (double)accf : acc) / c_k.sf_cc_div;
@@ -1612,8 +1617,13 @@ static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfL
 
 int launch_sf_cc_norm(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K) {
   PIC_DISPATCH_N(A.N, {
-    if (A.mixed) k_sf_cc_norm<NN, true><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
-    else k_sf_cc_norm<NN, false><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+    if (A.sf_alpha == 2) {
+      if (A.mixed) k_sf_cc_norm<NN, true, true><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+      else k_sf_cc_norm<NN, false, true><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+    } else {
+      if (A.mixed) k_sf_cc_norm<NN, true, false><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+      else k_sf_cc_norm<NN, false, false><<<A.M.ne, kCcThreads, 0, A.s>>>(A.M, L, B.offset, K, A.st);
+    }
   });
   return 1;
 }
