@@ -112,6 +112,10 @@ typedef struct pic_config_t {
   int32_t sf_dim;
   int32_t sf_dir;
   int32_t sf_depo3d;
+  /* Part-Species[s]-TimeStepFactor with Part-VariableTimeStep-...-Species (VarTimeStep%UseSpeciesSpecific):
+   * the push of species s advances by dt * factor (timedisc_TimeStepPoissonByBorisLeapfrog.f90:130-135);
+   * 0 = not set = 1 */
+  double  time_step_factor[PIC_MAX_SPECIES];
 } pic_config_t;
 
 /* Mesh arrays as the reference holds them after init (NGeo = 1 hexahedra).

@@ -275,7 +275,9 @@ static void push_single(const pic_config_t* cfg, orc_particles_t* p, int ip, dou
   const double* F = &p->field[(size_t)ip * 6];
   const int sp = p->species[ip] - 1;
   const double q = cfg->charge[sp], mass = cfg->mass[sp];
-  const double dtVar = dt, dtFrac = dtVar;
+  /* dtVar = dt * Species(s)%TimeStepFactor (timedisc_TimeStepPoissonByBorisLeapfrog.f90:130-135; 0 = unset) */
+  const double fac = cfg->time_step_factor[sp] > 0.0 ? cfg->time_step_factor[sp] : 1.0;
+  const double dtVar = dt * fac, dtFrac = dtVar;
   const int push = fabs(q) > 0.0;               /* isPushParticle */
   if (p->is_new[ip]) {
     if (push) {

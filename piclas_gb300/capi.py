@@ -47,6 +47,7 @@ class PicConfig(C.Structure):
         ("mpf", C.c_double * PIC_MAX_SPECIES), ("external_field", C.c_double * 6),
         ("refmapping_eps", C.c_double), ("sf_radius", C.c_double), ("sf_alpha", C.c_int32),
         ("sort_interval", C.c_int32), ("sf_dim", C.c_int32), ("sf_dir", C.c_int32), ("sf_depo3d", C.c_int32),
+        ("time_step_factor", C.c_double * PIC_MAX_SPECIES),
     ]
 
 
@@ -109,8 +110,8 @@ def u8ptr(a: np.ndarray):
 def make_config(n_dg: int, tracking: int, deposition: int, precision: int, species, max_particles: int,
                 external_field=(0.0,) * 6, refmapping_eps: float = 1e-4, sf_radius: float = 0.0,
                 sf_alpha: int = 2, sort_interval: int = 0, sf_dim: int = 3, sf_dir: int = 1,
-                sf_depo3d: bool = True) -> PicConfig:
-    """species: list of (charge, mass, mpf)."""
+                sf_depo3d: bool = True, time_step_factor=None) -> PicConfig:
+    """species: list of (charge, mass, mpf); time_step_factor: per species (Species%TimeStepFactor), None = 1."""
     cfg = PicConfig()
     cfg.n_dg = n_dg
     cfg.tracking = tracking
@@ -122,6 +123,8 @@ def make_config(n_dg: int, tracking: int, deposition: int, precision: int, speci
         cfg.charge[s] = q
         cfg.mass[s] = m
         cfg.mpf[s] = w
+    for s, f in enumerate(time_step_factor or []):
+        cfg.time_step_factor[s] = float(f)
     for i in range(6):
         cfg.external_field[i] = float(external_field[i])
     cfg.refmapping_eps = refmapping_eps

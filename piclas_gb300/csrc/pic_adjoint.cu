@@ -513,6 +513,9 @@ extern "C" int pic_adjoint_run(pic_ctx_t* c, const pic_adjoint_cfg_t* a, const d
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "adjoint precision");
   if (c->has_walls)
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs a mesh without open/reflective sides");
+  for (int s = 0; s < c->cfg.n_species; ++s)
+    if (c->k.dt_fac[s] != 1.0)
+      return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs one time step for all species");
   if (!c->field_set || !c->have_particles) return pic_internal::set_error(PIC_ERR_STATE, "field and particles must be set first");
   if (cudaMemcpyToSymbolAsync(c_k, &c->k, sizeof(Consts), 0, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
     return pic_internal::set_error(PIC_ERR_CUDA, "adjoint constants");

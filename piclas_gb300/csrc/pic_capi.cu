@@ -145,8 +145,11 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown precision");
   if (cfg->n_species < 1 || cfg->n_species > PIC_MAX_SPECIES) return fail(PIC_ERR_INVALID_ARGUMENT, "n_species");
   if (cfg->max_particles < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "max_particles");
-  for (int s = 0; s < cfg->n_species; ++s)
+  for (int s = 0; s < cfg->n_species; ++s) {
     if (!(cfg->mass[s] > 0.0)) return fail(PIC_ERR_INVALID_ARGUMENT, "species mass must be > 0");
+    if (!(cfg->time_step_factor[s] >= 0.0) || !std::isfinite(cfg->time_step_factor[s]))
+      return fail(PIC_ERR_INVALID_ARGUMENT, "time_step_factor must be finite and >= 0 (0: 1)");
+  }
   if (m->n_elems < 1 || m->n_geo != 1) return fail(PIC_ERR_INVALID_ARGUMENT, "only NGeo = 1 meshes are supported");
   if (m->n_periodic_vectors < 0 || m->n_periodic_vectors > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "n_periodic_vectors");
   const void* req[] = {m->xi_cl_ngeo, m->wbary_cl_ngeo, m->xgp, m->wgp, m->wbary_gp, m->xcl_ngeo, m->dxcl_ngeo,
@@ -650,9 +653,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   // ---- constants -------------------------------------------------------------------------------
   Consts k{};
   k.N = c->N; k.n1 = n1; k.ndof = nd; k.n_species = cfg->n_species;
+  for (int s = 0; s < 8; ++s) k.dt_fac[s] = 1.0;
   for (int s = 0; s < cfg->n_species; ++s) {
     k.q[s] = cfg->charge[s]; k.m[s] = cfg->mass[s]; k.mpf[s] = cfg->mpf[s];
     k.qm[s] = cfg->charge[s] * cfg->mpf[s];
+    if (cfg->time_step_factor[s] > 0.0) k.dt_fac[s] = cfg->time_step_factor[s];
   }
   for (int q = 0; q < 6; ++q) k.ext[q] = cfg->external_field[q];
   k.refmapping_eps = cfg->refmapping_eps > 0.0 ? cfg->refmapping_eps : 1e-4;

@@ -39,6 +39,7 @@ struct Consts {
   double fib_delta[3];
   double sf_r, sf_r2, sf_r2_inv, sf_w;
   float sf_r_inv;                              // 1/R (FP16 pre-test of the mixed gather)
+  double dt_fac[8];                            // Species(s)%TimeStepFactor (1 unless set)
   double sf_cc_div;                            // charge-conserving total divided by dimFactorSF (else 1)
   int sf_alpha;
   int pv_dir[3];                               // periodic vector index per axis (-1: none)

@@ -191,10 +191,11 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
       for (int c = 3; c < 6; ++c) Fd[c] = Fd[c] + 0.0;
     }
     bool isnew = (fl & kNew) != 0;
-    boris_push(v, Fd, sp, isnew, dt);
+    const double dtv = dt * c_k.dt_fac[sp];
+    boris_push(v, Fd, sp, isnew, dtv);
     double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dtv;
     if (!state_finite(x, v[0], v[1], v[2])) {
       flag_status(st, 0x20u);
       P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
@@ -271,10 +272,11 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
       for (int c = 0; c < 3; ++c) Ff[c] += Eo[c];
     }
     bool isnew = (fl & kNew) != 0;
-    boris_push_f(v, Ff, sp, isnew, (float)dt);
+    const double dtv = dt * c_k.dt_fac[sp];
+    boris_push_f(v, Ff, sp, isnew, (float)dtv);
     double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dtv;
     if (!state_finite(x, v[0], v[1], v[2])) {
       flag_status(st, 0x20u);
       P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
@@ -377,9 +379,10 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStat
 #pragma unroll
     for (int c = 0; c < 6; ++c) F[c] = P.field[(size_t)c * P.cap + i];
     double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
-    boris_push(v, F, sp, isnew, dt);
+    const double dtv = dt * c_k.dt_fac[sp];
+    boris_push(v, F, sp, isnew, dtv);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dtv;
     P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
     finite = state_finite(x, v[0], v[1], v[2]);
   } else {
@@ -387,9 +390,10 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStat
 #pragma unroll
     for (int c = 0; c < 6; ++c) F[c] = (float)P.field[(size_t)c * P.cap + i];
     float v[3] = {P.vxf[i], P.vyf[i], P.vzf[i]};
-    boris_push_f(v, F, sp, isnew, (float)dt);
+    const double dtv = dt * c_k.dt_fac[sp];
+    boris_push_f(v, F, sp, isnew, (float)dtv);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dtv;
     P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
     finite = state_finite(x, v[0], v[1], v[2]);
   }
@@ -1389,9 +1393,10 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
       for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
     }
     double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
-    boris_push(v, F, sp, isnew, dt);
+    const double dtv = dt * c_k.dt_fac[sp];
+    boris_push(v, F, sp, isnew, dtv);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dt;
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dtv;
     P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
   } else {
     float F[6];
@@ -1405,9 +1410,10 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
       for (int c = 0; c < 3; ++c) F[c] += Eo[c];
     }
     float v[3] = {P.vxf[i], P.vyf[i], P.vzf[i]};
-    boris_push_f(v, F, sp, isnew, (float)dt);
+    const double dtv = dt * c_k.dt_fac[sp];
+    boris_push_f(v, F, sp, isnew, (float)dtv);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dt;
+    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dtv;
     P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
   }
   double xl[3] = {P.x[i], P.y[i], P.z[i]};

@@ -55,6 +55,7 @@ class Workload:
     sf_dim: int = 3                 # PIC-shapefunction-dimension
     sf_dir: int = 1                 # PIC-shapefunction-direction
     sf_depo3d: bool = True          # PIC-shapefunction-3D-deposition
+    time_step_factor: tuple | None = None   # Species(s)%TimeStepFactor per species (None: 1)
     info: dict = field(default_factory=dict)
 
     @property
@@ -67,7 +68,8 @@ class Workload:
                                 max_particles if max_particles is not None else self.n,
                                 external_field=self.external_field, sf_radius=self.sf_radius,
                                 sf_alpha=self.sf_alpha, sort_interval=sort_interval, sf_dim=self.sf_dim,
-                                sf_dir=self.sf_dir, sf_depo3d=self.sf_depo3d)
+                                sf_dir=self.sf_dir, sf_depo3d=self.sf_depo3d,
+                                time_step_factor=self.time_step_factor)
 
 
 # --------------------------------------------------------------------------------------

@@ -69,5 +69,5 @@ def test_bad_options_rejected(lib):
 
 def test_struct_sizes_match_c():
     # pic_config_t: 6 ints + 3*8 + 6 doubles + 2 doubles + 5 ints + 4 bytes tail padding (8-byte alignment)
-    assert C.sizeof(capi.PicConfig) == 6 * 4 + 3 * 8 * 8 + 6 * 8 + 2 * 8 + 5 * 4 + 4
+    assert C.sizeof(capi.PicConfig) == 6 * 4 + 3 * 8 * 8 + 6 * 8 + 2 * 8 + 5 * 4 + 4 + 8 * 8
     assert C.sizeof(capi.PicStatus) == 24

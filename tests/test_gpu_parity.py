@@ -793,3 +793,39 @@ def test_charge_conserving_sf_1d_2d_against_oracle(gpu_lib, oracle_lib, dep, wal
     assert g["status"]["error_word"] == 0
     gm = _run_gpu(w, 4, precision=capi.PIC_PREC_MIXED)
     assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-6
+
+
+@pytest.mark.parametrize("kind", ["cvwm_tria", "sf_ref"])
+def test_species_time_step_factor(gpu_lib, oracle_lib, kind):
+    """Species(s)%TimeStepFactor: each species pushed with dt * factor; FP64 bit-exact against the oracle,
+    mixed within one particle; the adjoint refuses it."""
+    if kind == "cvwm_tria":
+        w = workloads.plasma_wave(n_cells=4, N=3, n_particles=6000, seed=43, T_eV=200.0)
+        q, m, mpf = w.species[0]
+        w.species = [(q, m, mpf), (-q, 1836.0 * m, mpf)]
+        w.part_species = np.where(np.arange(w.n) % 3 == 0, 2, 1).astype(np.int32)
+    else:
+        w = workloads.curved_two_species(n_cells=4, n_per_species=3000, seed=43, nsteps=4)
+    w.time_step_factor = (1.0, 3.0)
+    g = _run_gpu(w, 6)
+    st, PS = _run_oracle(oracle_lib, w, 6)
+    assert np.array_equal(g["elem"], st.elem)
+    if kind == "cvwm_tria":
+        assert np.array_equal(g["part_state"], st.part_state)
+    else:   # B_z = 0.1 T: the Boris rotation's tan differs in the last bit between device and host libm
+        assert _rel(g["part_state"], st.part_state) <= 1e-12
+    assert _rel(g["PS"], PS) <= 1e-12 and g["status"]["error_word"] == 0
+    w1 = workloads.Workload(**{**w.__dict__, "time_step_factor": None})
+    st1, _ = _run_oracle(oracle_lib, w1, 6)
+    sp2 = w.part_species == 2
+    assert not np.array_equal(st1.part_state[sp2], st.part_state[sp2])          # the factor acted
+    assert np.array_equal(st1.part_state[~sp2], st.part_state[~sp2])          # frozen field: others unchanged
+    gm = _run_gpu(w, 6, precision=capi.PIC_PREC_MIXED)
+    assert (gm["elem"] != st.elem).sum() <= 2
+    if kind == "cvwm_tria":
+        loop = ParticleLoop(w.config(), w.mesh)
+        loop.set_field(w.e_dof)
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+        with pytest.raises(PicError):
+            loop.adjoint(2, w.dt, np.zeros((w.mesh.n_elems, w.mesh.n_dof)), 1.0)
+        loop.close()

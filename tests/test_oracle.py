@@ -612,3 +612,26 @@ def test_sf_1d_2d_charge_conserving(oracle_lib, dep, walls, dim, sf_dir, depo3d)
         for k in range(inv.max() + 1):
             v = rho[inv == k]
             assert np.allclose(v, v[0], rtol=1e-11, atol=1e-11 * np.abs(rho).max())
+
+
+# ---- species-specific time step (VarTimeStep%UseSpeciesSpecific, Species%TimeStepFactor) ----------------
+def test_species_time_step_factor_free_streaming(oracle_lib):
+    """No field: species s moves by v dt factor_s per step (timedisc_TimeStepPoissonByBorisLeapfrog.f90:130-135),
+    factor 0 meaning 1; through periodic faces with TriaTracking."""
+    w = workloads.plasma_wave(n_cells=4, N=2, n_particles=600, seed=31, T_eV=500.0)
+    w.e_dof[:] = 0.0
+    q, m, mpf = w.species[0]
+    w.species = [(q, m, mpf), (q, 4.0 * m, mpf)]
+    w.part_species = np.where(np.arange(w.n) % 2 == 0, 1, 2).astype(np.int32)
+    w.time_step_factor = (0.0, 0.25)
+    K = 5
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species, is_new=np.zeros(w.n, np.uint8))
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, K)
+    fac = np.where(w.part_species == 1, 1.0, 0.25)[:, None]
+    x = w.part_state[:, :3]
+    for _ in range(K):
+        x = x + w.part_state[:, 3:] * (w.dt * fac)
+    x = np.mod(x, 1.0)
+    assert np.max(np.abs(np.mod(st.part_state[:, :3] - x + 0.5, 1.0) - 0.5)) < 1e-12
+    assert st.inside.all() and np.array_equal(st.elem, workloads._elem_of_uniform(w.mesh, st.part_state[:, :3]))
