@@ -51,3 +51,20 @@ def test_replica_rate_single_process():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.replica_rate(1000, 4, 2.0) == (2000.0, 2.0)
+
+
+def test_reference_arm_reports_the_gpu_arms_config():
+    """bench.py --impl reference prints the config of the GPU arm for the same flags (full workload sizes)."""
+    import argparse
+    import bench
+    from piclas_gb300 import workloads
+    from piclas_gb300.mesh import build_box_mesh
+    for name, cells, n in (("curved", 32, 16_000_000), ("plasma_wave", 8, 200_000)):
+        args = argparse.Namespace(workload=name, precision="fp64", gpus=1)
+        ref = bench.reference_config(args)
+        mesh = build_box_mesh(2, 2, 2, 3)
+        stand_in = workloads.Workload(**{**workloads.plasma_wave(mesh=mesh, n_particles=10).__dict__})
+        stand_in.mesh = type("M", (), {"n_elems": cells ** 3, "N": 3})()
+        stand_in.part_state = type("P", (), {"shape": (n, 6)})()
+        gpu = dict(bench.workload_config(stand_in, name), precision="fp64", parallelism="replicas x1")
+        assert ref == gpu
