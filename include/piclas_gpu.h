@@ -30,6 +30,7 @@
  *                          FillParticleData and the particle read-in of a restart
  *                          (src/io_hdf5/hdf5_output_particle.f90:1531, src/particles/restart/particle_readin.f90)
  *   pic_get_field_at_particles  FieldAtParticle(1:6,:) (src/particles/pic/interpolation/pic_interpolation_vars.f90:26)
+ *   pic_verify_deposited_charge VerifyDepositedCharge (src/particles/pic/analyze/pic_analyze.f90:41)
  *   pic_hdg_init           InitHDG + Elem_Mat + BuildPrecond (src/hdg/hdg.f90:90, src/hdg/elem_mat.f90:42,513)
  *   pic_hdg_set_dirichlet  the Dirichlet branch of HDGLinear (src/hdg/hdg_linear.f90:96-150)
  *   pic_hdg_solve          HDG -> HDGLinear -> CG_solver + PostProcessGradientHDG
@@ -114,7 +115,8 @@ typedef struct pic_config_t {
   int32_t sf_depo3d;
   /* Part-Species[s]-TimeStepFactor with Part-VariableTimeStep-...-Species (VarTimeStep%UseSpeciesSpecific):
    * the push of species s advances by dt * factor (timedisc_TimeStepPoissonByBorisLeapfrog.f90:130-135);
-   * 0 = not set = 1 */
+   * 0 = not set = 1; a factor above 1 is rejected (PIC_ERR_INVALID_ARGUMENT), as the reference stops on it
+   * (particle_emission_init.f90:218-219) */
   double  time_step_factor[PIC_MAX_SPECIES];
 } pic_config_t;
 
@@ -231,6 +233,15 @@ int pic_step(pic_ctx_t* ctx, double dt, int32_t nsteps, double* part_source);
 
 int pic_get_status(pic_ctx_t* ctx, pic_status_t* status);
 
+/* VerifyDepositedCharge (src/particles/pic/analyze/pic_analyze.f90:41-133; called by Deposition with
+ * PIC-VerifyCharge = T, pic_depo.f90:1012-1015) on the last deposition of this context:
+ * charge_numerical = the integral of PartSource(4) over the mesh (sum over elements and DOFs of
+ * wGP(k) wGP(l) wGP(m) / sJ * PartSource(4)), charge_analytical = the sum of ChargeIC * MacroParticleFactor over
+ * the particles inside (times dimFactorSF for a 1D/2D shape function with PIC-shapefunction-3D-deposition = F).
+ * Needs pic_mesh_t.elem_sj at pic_create and a deposition (pic_deposit or pic_step) before the call;
+ * PIC_ERR_STATE otherwise.  Synchronises the context's stream. */
+int pic_verify_deposited_charge(pic_ctx_t* ctx, double* charge_numerical, double* charge_analytical);
+
 /* Instrumentation (no reference counterpart): sustained FP64 fused multiply-add rate of this GPU in GFLOP/s,
  * from independent FMA chains on every SM (~0.1 s); the peak the FP64-bound kernels are compared against. */
 int pic_fp64_fma_rate(pic_ctx_t* ctx, double* gflops);
@@ -336,14 +347,20 @@ int pic_profile_read(pic_ctx_t* ctx, double* ms, int64_t* launches, int32_t npha
  * For callers that cannot call cudaMalloc while their time loop runs (e.g. a host whose device
  * memory belongs to another runtime or to a fixed pool): the particles and the result stay in the
  * caller's device arrays -- d_part_state is PartState(1:6,n), d_elem / d_species are 1-based
- * PEM%GlobalElemID / PartSpecies, d_part_source receives PartSource(1:4,0:N,0:N,0:N,nElems) -- and
- * the node-sum scratch is a fixed file-scope device array for at most 131072 periodic-unique mesh
- * nodes (4 MiB per GPU, held until the process exits; larger meshes return PIC_ERR_CAPACITY).
- * The work is queued on `stream` (a cudaStream_t, NULL = default stream) and not waited for.
+ * PEM%GlobalElemID / PartSpecies, d_inside is PDM%ParticleInside as 0/1 bytes (NULL: every particle
+ * inside; particles with 0 are skipped, as the reference skips them, pic_depo_method.f90:472),
+ * d_part_source receives PartSource(1:4,0:N,0:N,0:N,nElems) -- and the node-sum scratch is a fixed
+ * file-scope device array for at most 131072 periodic-unique mesh nodes (4 MiB per GPU, held until
+ * the process exits; larger meshes return PIC_ERR_CAPACITY).  Element or species ids out of range
+ * skip the particle and set PIC_STATUS_BAD_ELEMENT.
+ * The work is queued on `stream` (a cudaStream_t, NULL = default stream) and not waited for; the
+ * context's own stream is made to wait for it, so a later pic_get_status reports its status bits
+ * (except while `stream` is being captured: then synchronise `stream` before pic_get_status).
  * Calls share the array: calls that overlap on the GPU race, so order them on one stream.  The
  * first call on a device looks up the array's address; make it before any stream capture. */
 int pic_deposit_cvwm_noalloc(pic_ctx_t* ctx, const double* d_part_state, const int32_t* d_elem,
-                             const int32_t* d_species, int32_t n, double* d_part_source, void* stream);
+                             const int32_t* d_species, const uint8_t* d_inside, int32_t n, double* d_part_source,
+                             void* stream);
 /* Kernels launched through this context so far (no reference counterpart: instrumentation). */
 int64_t pic_launch_count(pic_ctx_t* ctx);
 /* The cudaStream_t the context enqueues on, as void* (no reference counterpart: lets a caller

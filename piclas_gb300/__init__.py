@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
                     "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data", "pic_fp64_fma_rate",
                     "pic_hdg_init", "pic_hdg_set_dirichlet", "pic_hdg_solve", "pic_hdg_get_lambda",
-                    "pic_hdg_get_elem_mat", "pic_hdg_set_lambda"]
+                    "pic_hdg_get_elem_mat", "pic_hdg_set_lambda", "pic_verify_deposited_charge"]
 
 
 class PicError(RuntimeError):
@@ -91,9 +91,10 @@ def load_library(build_if_missing: bool = False):
     L.pic_launch_count.restype = C.c_int64
     L.pic_profile.argtypes = [C.c_void_p, C.c_int32]
     L.pic_profile_read.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), C.c_int32]
-    L.pic_deposit_cvwm_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
-                                           C.c_void_p]
+    L.pic_deposit_cvwm_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.c_void_p]
     L.pic_adjoint_run.argtypes = [C.c_void_p, P(capi.PicAdjointConfig), dp, dp, dp, dp]
+    L.pic_verify_deposited_charge.argtypes = [C.c_void_p, dp, dp]
     L.pic_stream.argtypes = [C.c_void_p]
     L.pic_stream.restype = C.c_void_p
     L.pic_hdg_init.argtypes = [C.c_void_p, P(capi.PicHdg)]
@@ -243,6 +244,13 @@ class ParticleLoop:
         self._check(self.lib.pic_get_status(self.handle, C.byref(s)), "pic_get_status")
         return dict(error_word=int(s.error_word), n_lost=int(s.n_lost), n_inside=int(s.n_inside),
                     n_newton_failed=int(s.n_newton_failed), n_steps=int(s.n_steps))
+
+    def verify_deposited_charge(self) -> tuple[float, float]:
+        """VerifyDepositedCharge of the last deposition: (ChargeNumerical, ChargeAnalytical) in C."""
+        num, ana = C.c_double(0.0), C.c_double(0.0)
+        self._check(self.lib.pic_verify_deposited_charge(self.handle, C.byref(num), C.byref(ana)),
+                    "pic_verify_deposited_charge")
+        return num.value, ana.value
 
     def reset_status(self):
         self._check(self.lib.pic_reset_status(self.handle), "pic_reset_status")

@@ -19,17 +19,17 @@ using namespace pic;
 
 namespace {
 
-// Lagrange values and derivatives at x (product form), nodes c_k.xgp[0..NP-1]
+// Lagrange values and derivatives at x (product form), nodes kc.xgp[0..NP-1]
 template <int NP, class T>
-__device__ __forceinline__ void lagrange_d(T x, T L[NP], T dL[NP]) {
+__device__ __forceinline__ void lagrange_d(const Consts& kc, T x, T L[NP], T dL[NP]) {
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
     T l = T(1), d = T(0);
 #pragma unroll
     for (int m = 0; m < NP; ++m) {
       if (m == i) continue;
-      const T den = T(c_k.xgp[i] - c_k.xgp[m]);
-      const T f = (x - T(c_k.xgp[m])) / den;
+      const T den = T(kc.xgp[i] - kc.xgp[m]);
+      const T f = (x - T(kc.xgp[m])) / den;
       d = d * f + l / den;      // product rule, running
       l = l * f;
     }
@@ -40,11 +40,11 @@ __device__ __forceinline__ void lagrange_d(T x, T L[NP], T dL[NP]) {
 
 // E(xi) and dE/dxi (3x3: [component][direction])
 template <int N, class T>
-__device__ __forceinline__ void field_and_grad(const T* __restrict__ U, const double xi[3], T E[3], T G[3][3]) {
+__device__ __forceinline__ void field_and_grad(const Consts& kc, const T* __restrict__ U, const double xi[3], T E[3], T G[3][3]) {
   constexpr int n1 = N + 1;
   T L[3][n1], D[3][n1];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) lagrange_d<n1, T>(T(xi[d]), L[d], D[d]);
+  for (int d = 0; d < 3; ++d) lagrange_d<n1, T>(kc, T(xi[d]), L[d], D[d]);
 #pragma unroll
   for (int c = 0; c < 3; ++c) { E[c] = T(0); G[c][0] = G[c][1] = G[c][2] = T(0); }
   for (int k = 0; k < n1; ++k)
@@ -198,8 +198,9 @@ struct Rec {
 };
 
 template <int N, class T, bool RECORD>
-__global__ void __launch_bounds__(128) k_adj_fwd(DevMesh M, AdjState S, const T* __restrict__ E, double dt, double b_scale,
+__global__ void __launch_bounds__(128) k_adj_fwd(const __grid_constant__ DevMesh M, AdjState S, const T* __restrict__ E, double dt, double b_scale,
                                                  Rec<T> R, int slot, DevStatus* st) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.n) return;
@@ -217,13 +218,13 @@ __global__ void __launch_bounds__(128) k_adj_fwd(DevMesh M, AdjState S, const T*
   double xi[3];
   position_in_ref_elem(M, e, x, xi);
   T Ef[3], G[3][3];
-  field_and_grad<N, T>(E + (size_t)e * nd * 3, xi, Ef, G);
+  field_and_grad<N, T>(kc, E + (size_t)e * nd * 3, xi, Ef, G);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) Ef[c] += T(c_k.ext[c]);
-  const double Bx = c_k.ext[3] * b_scale, By = c_k.ext[4] * b_scale, Bz = c_k.ext[5] * b_scale;
+  for (int c = 0; c < 3; ++c) Ef[c] += T(kc.ext[c]);
+  const double Bx = kc.ext[3] * b_scale, By = kc.ext[4] * b_scale, Bz = kc.ext[5] * b_scale;
   const double Bn = sqrt(Bx * Bx + By * By + Bz * Bz);
   const T bh[3] = {T(Bn > 0 ? Bx / Bn : 0), T(Bn > 0 ? By / Bn : 0), T(Bn > 0 ? Bz / Bn : 0)};
-  const T c1 = T(c_k.q[sp] * dt / (c_k.m[sp] * 2.0)), c2i = T(c_k.c2_inv);
+  const T c1 = T(kc.q[sp] * dt / (kc.m[sp] * 2.0)), c2i = T(kc.c2_inv);
   BorisTape<T> tape;
   boris_fwd<T>(tape, v, Ef, T(Bn), bh, c1, c2i);
 #pragma unroll
@@ -241,7 +242,8 @@ __global__ void __launch_bounds__(128) k_adj_fwd(DevMesh M, AdjState S, const T*
 
 // CVWM charge only (component 4): node sums of q*MPF*w
 template <class T>
-__global__ void __launch_bounds__(128) k_adj_deposit(DevMesh M, AdjState S, double* __restrict__ NS1) {
+__global__ void __launch_bounds__(128) k_adj_deposit(const __grid_constant__ DevMesh M, AdjState S, double* __restrict__ NS1) {
+  const Consts& kc = M.k;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.n) return;
   const double x[3] = {S.x[i], S.y[i], S.z[i]};
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(DevMesh M, AdjState S, doub
   double xi[3];
   position_in_ref_elem(M, e, x, xi);
   const T a[3] = {T(0.5 * (xi[0] + 1.0)), T(0.5 * (xi[1] + 1.0)), T(0.5 * (xi[2] + 1.0))};
-  const T ch = T(c_k.qm[sp]);
+  const T ch = T(kc.qm[sp]);
   const int cg2t[8] = {0, 1, 3, 2, 4, 5, 7, 6};
   for (int c = 0; c < 8; ++c) {
     const int t = cg2t[c];
@@ -259,13 +261,14 @@ __global__ void __launch_bounds__(128) k_adj_deposit(DevMesh M, AdjState S, doub
 }
 
 // rho at the DOFs, loss, and dL/drho
-__global__ void k_adj_loss(DevMesh M, int nd, int n1, const double* __restrict__ NS1, const double* __restrict__ target,
+__global__ void k_adj_loss(const __grid_constant__ DevMesh M, int nd, int n1, const double* __restrict__ NS1, const double* __restrict__ target,
                            double rho_scale, double* __restrict__ grho, double* __restrict__ loss) {
+  const Consts& kc = M.k;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   double l = 0.0;
   if (tid < M.ne * nd) {
     const int e = tid / nd, r = tid - e * nd;
-    const double a1 = c_k.fac_gp[r % n1], a2 = c_k.fac_gp[(r / n1) % n1], a3 = c_k.fac_gp[r / (n1 * n1)];
+    const double a1 = kc.fac_gp[r % n1], a2 = kc.fac_gp[(r / n1) % n1], a3 = kc.fac_gp[r / (n1 * n1)];
     const double tri[8] = {(1 - a1) * (1 - a2) * (1 - a3), a1 * (1 - a2) * (1 - a3), a1 * a2 * (1 - a3), (1 - a1) * a2 * (1 - a3),
                            (1 - a1) * (1 - a2) * a3, a1 * (1 - a2) * a3, a1 * a2 * a3, (1 - a1) * a2 * a3};
     double rho = 0.0;
@@ -281,11 +284,12 @@ __global__ void k_adj_loss(DevMesh M, int nd, int n1, const double* __restrict__
   if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(loss, l);
 }
 
-__global__ void k_adj_node_grad(DevMesh M, int nd, int n1, const double* __restrict__ grho, double* __restrict__ gN) {
+__global__ void k_adj_node_grad(const __grid_constant__ DevMesh M, int nd, int n1, const double* __restrict__ grho, double* __restrict__ gN) {
+  const Consts& kc = M.k;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= M.ne * nd) return;
   const int e = tid / nd, r = tid - e * nd;
-  const double a1 = c_k.fac_gp[r % n1], a2 = c_k.fac_gp[(r / n1) % n1], a3 = c_k.fac_gp[r / (n1 * n1)];
+  const double a1 = kc.fac_gp[r % n1], a2 = kc.fac_gp[(r / n1) % n1], a3 = kc.fac_gp[r / (n1 * n1)];
   const double tri[8] = {(1 - a1) * (1 - a2) * (1 - a3), a1 * (1 - a2) * (1 - a3), a1 * a2 * (1 - a3), (1 - a1) * a2 * (1 - a3),
                          (1 - a1) * (1 - a2) * a3, a1 * (1 - a2) * a3, a1 * a2 * a3, (1 - a1) * a2 * a3};
   for (int c = 0; c < 8; ++c) {
@@ -296,8 +300,9 @@ __global__ void k_adj_node_grad(DevMesh M, int nd, int n1, const double* __restr
 
 // dL/dx at the final positions from the CVWM weights
 template <class T>
-__global__ void __launch_bounds__(128) k_adj_deposit_bwd(DevMesh M, AdjState S, const double* __restrict__ gN, T* gx,
+__global__ void __launch_bounds__(128) k_adj_deposit_bwd(const __grid_constant__ DevMesh M, AdjState S, const double* __restrict__ gN, T* gx,
                                                          T* gy, T* gz) {
+  const Consts& kc = M.k;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.n) return;
   const double x[3] = {S.x[i], S.y[i], S.z[i]};
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit_bwd(DevMesh M, AdjState S, 
   double xi[3];
   position_in_ref_elem(M, e, x, xi);
   const double a[3] = {0.5 * (xi[0] + 1.0), 0.5 * (xi[1] + 1.0), 0.5 * (xi[2] + 1.0)};
-  const double ch = c_k.qm[sp];
+  const double ch = kc.qm[sp];
   const int cg2t[8] = {0, 1, 3, 2, 4, 5, 7, 6};
   double gxi[3] = {0, 0, 0};
   for (int c = 0; c < 8; ++c) {
@@ -324,9 +329,10 @@ __global__ void __launch_bounds__(128) k_adj_deposit_bwd(DevMesh M, AdjState S, 
 
 // one reverse step: from (dL/dx_{n+1}, dL/dv_{n+1/2}) to (dL/dx_n, dL/dv_{n-1/2})
 template <int N, class T>
-__global__ void __launch_bounds__(128) k_adj_bwd(DevMesh M, int n, const uint8_t* __restrict__ spv, const T* __restrict__ E,
+__global__ void __launch_bounds__(128) k_adj_bwd(const __grid_constant__ DevMesh M, int n, const uint8_t* __restrict__ spv, const T* __restrict__ E,
                                                  double dt, double b_scale, Rec<T> R, int slot, T* gx, T* gy, T* gz,
                                                  T* gvx, T* gvy, T* gvz, double* gB) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double gBl = 0.0;
@@ -344,13 +350,13 @@ __global__ void __launch_bounds__(128) k_adj_bwd(DevMesh M, int n, const uint8_t
     double xi[3];
     position_in_ref_elem(M, e, x, xi);
     T Ef[3], G[3][3];
-    field_and_grad<N, T>(E + (size_t)e * nd * 3, xi, Ef, G);
+    field_and_grad<N, T>(kc, E + (size_t)e * nd * 3, xi, Ef, G);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) Ef[c] += T(c_k.ext[c]);
-    const double Bx = c_k.ext[3] * b_scale, By = c_k.ext[4] * b_scale, Bz = c_k.ext[5] * b_scale;
+    for (int c = 0; c < 3; ++c) Ef[c] += T(kc.ext[c]);
+    const double Bx = kc.ext[3] * b_scale, By = kc.ext[4] * b_scale, Bz = kc.ext[5] * b_scale;
     const double Bn = sqrt(Bx * Bx + By * By + Bz * Bz);
     const T bh[3] = {T(Bn > 0 ? Bx / Bn : 0), T(Bn > 0 ? By / Bn : 0), T(Bn > 0 ? Bz / Bn : 0)};
-    const T c1 = T(c_k.q[sp] * dt / (c_k.m[sp] * 2.0)), c2i = T(c_k.c2_inv);
+    const T c1 = T(kc.q[sp] * dt / (kc.m[sp] * 2.0)), c2i = T(kc.c2_inv);
     BorisTape<T> tape;
     boris_fwd<T>(tape, v, Ef, T(Bn), bh, c1, c2i);
     T gv[3], gE[3], gBn;
@@ -514,11 +520,9 @@ extern "C" int pic_adjoint_run(pic_ctx_t* c, const pic_adjoint_cfg_t* a, const d
   if (c->has_walls)
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs a mesh without open/reflective sides");
   for (int s = 0; s < c->cfg.n_species; ++s)
-    if (c->k.dt_fac[s] != 1.0)
+    if (c->M.k.dt_fac[s] != 1.0)
       return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs one time step for all species");
   if (!c->field_set || !c->have_particles) return pic_internal::set_error(PIC_ERR_STATE, "field and particles must be set first");
-  if (cudaMemcpyToSymbolAsync(c_k, &c->k, sizeof(Consts), 0, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
-    return pic_internal::set_error(PIC_ERR_CUDA, "adjoint constants");
   const bool f32 = a->precision == PIC_PREC_MIXED;
   switch (c->N) {
     case 1: return f32 ? run<1, float>(c, a, rho_target, loss, dL_dv0, dL_dB) : run<1, double>(c, a, rho_target, loss, dL_dv0, dL_dB);

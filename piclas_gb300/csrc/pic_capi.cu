@@ -147,8 +147,11 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   if (cfg->max_particles < 0) return fail(PIC_ERR_INVALID_ARGUMENT, "max_particles");
   for (int s = 0; s < cfg->n_species; ++s) {
     if (!(cfg->mass[s] > 0.0)) return fail(PIC_ERR_INVALID_ARGUMENT, "species mass must be > 0");
-    if (!(cfg->time_step_factor[s] >= 0.0) || !std::isfinite(cfg->time_step_factor[s]))
-      return fail(PIC_ERR_INVALID_ARGUMENT, "time_step_factor must be finite and >= 0 (0: 1)");
+    // Species(s)%TimeStepFactor: the reference stops on factors above 1 ('Species-specific time step only
+    // allows factors below 1!', particle_emission_init.f90:218-219)
+    if (!(cfg->time_step_factor[s] >= 0.0) || !(cfg->time_step_factor[s] <= 1.0))
+      return fail(PIC_ERR_INVALID_ARGUMENT, "time_step_factor must lie in [0, 1] (0: not set = 1); the reference "
+                                            "only allows species-specific factors below 1");
   }
   if (m->n_elems < 1 || m->n_geo != 1) return fail(PIC_ERR_INVALID_ARGUMENT, "only NGeo = 1 meshes are supported");
   if (m->n_periodic_vectors < 0 || m->n_periodic_vectors > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "n_periodic_vectors");
@@ -506,6 +509,8 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(PIC_ERR_CUDA, "cudaStreamCreate failed"));
+  if (cudaEventCreateWithFlags(&c->noalloc_done, cudaEventDisableTiming) != cudaSuccess)
+    return bail(fail(PIC_ERR_CUDA, "cudaEventCreate failed"));
 
   // ---- element geometry -------------------------------------------------------------------
   std::vector<double> xcl(m->xcl_ngeo, m->xcl_ngeo + (size_t)ne * 24);
@@ -697,8 +702,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     sf_kernel_dirs(cfg, keep);
     for (int d = 0; d < 3; ++d) k.sf_keep[d] = keep[d] ? 1 : 0;
   }
-  if (upload_consts(k) != cudaSuccess) return bail(fail(PIC_ERR_CUDA, "constant upload"));
-  c->k = k;
+  c->M.k = k;   // travels with every launch (kernel parameter), so contexts do not share constants
 
   // ---- work arrays -------------------------------------------------------------------------------
   if ((rc = c->alloc(&c->E, (size_t)ne * nd * 3)) || (rc = c->alloc(&c->E32, (size_t)ne * nd * 3)) ||
@@ -744,6 +748,22 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       if ((rc = c->alloc(&c->sfk.pos, cap * 3)) || (rc = c->alloc(&c->sfk.fac, cap * 4))) return bail(rc);
     }
   }
+  // VerifyDepositedCharge (pic_analyze.f90:41-133): quadrature weight wGP(k) wGP(l) wGP(m) / sJ of every DOF, and the
+  // factor of the analytical charge (dimFactorSF for a 1D/2D shape function whose charge sits on a line / area)
+  if (m->elem_sj) {
+    std::vector<double> wq((size_t)ne * nd);
+    for (int e = 0; e < ne; ++e)
+      for (int mm = 0; mm < n1; ++mm)
+        for (int l = 0; l < n1; ++l)
+          for (int k = 0; k < n1; ++k) {
+            const int r = k + n1 * (l + n1 * mm);
+            wq[(size_t)e * nd + r] = m->wgp[k] * m->wgp[l] * m->wgp[mm] * (1.0 / m->elem_sj[(size_t)e * nd + r]);
+          }
+    if ((rc = upload(c, &c->charge_w, wq)) || (rc = c->alloc(&c->charge_elem, ne)) ||
+        (rc = c->alloc(&c->charge_out, 1)) || (rc = c->alloc(&c->species_count, PIC_MAX_SPECIES)))
+      return bail(rc);
+  }
+  c->charge_dim_factor = (c->sf && (cfg->sf_dim == 1 || cfg->sf_dim == 2) && !cfg->sf_depo3d) ? sf_dim_factor(cfg, m) : 1.0;
   if ((rc = device_sync(c))) return bail(rc);
   *out = c;
   return PIC_OK;
@@ -756,6 +776,7 @@ void pic_destroy(pic_ctx_t* c) {
   for (auto& r : c->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : c->pool) cudaEventDestroy(e);
   for (void* p : c->allocs) cudaFree(p);
+  if (c->noalloc_done) cudaEventDestroy(c->noalloc_done);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1101,6 +1122,26 @@ int pic_get_status(pic_ctx_t* c, pic_status_t* out) {
   out->n_inside = cnt;
   out->n_newton_failed = s.n_newton_failed;
   out->n_steps = c->n_steps;
+  return PIC_OK;
+}
+
+int pic_verify_deposited_charge(pic_ctx_t* c, double* charge_numerical, double* charge_analytical) {
+  if (!c || !charge_numerical || !charge_analytical) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c->charge_w) return fail(PIC_ERR_STATE, "the charge check needs pic_mesh_t.elem_sj at pic_create");
+  if (!c->ps_valid) return fail(PIC_ERR_STATE, "no deposition to check: call pic_deposit or pic_step first");
+  if (!c->have_particles) return fail(PIC_ERR_STATE, "particles must be uploaded first");
+  launch_charge_integral(c->args(), c->PS, c->charge_w, c->charge_elem, c->charge_out);
+  launch_count_species(c->args(), c->P, c->species_count);
+  double num = 0.0;
+  int cnt[PIC_MAX_SPECIES] = {0};
+  CUDA_TRY(cudaMemcpyAsync(&num, c->charge_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(cnt, c->species_count, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+  int rc = device_sync(c);
+  if (rc) return rc;
+  double ana = 0.0;   // ChargeAnalytical: sum over particles inside of ChargeIC * MacroParticleFactor
+  for (int s = 0; s < c->cfg.n_species; ++s) ana = ana + (double)cnt[s] * (c->cfg.charge[s] * c->cfg.mpf[s]);
+  *charge_numerical = num;
+  *charge_analytical = ana * c->charge_dim_factor;
   return PIC_OK;
 }
 

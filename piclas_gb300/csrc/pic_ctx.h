@@ -26,6 +26,7 @@ struct pic_ctx {
   bool adaptive = false;        // shape_function_adaptive: radius per source element (SfLists::elem_r)
   double sf_rmax = 0.0;         // largest shape-function radius
   cudaStream_t stream = nullptr;
+  cudaEvent_t noalloc_done = nullptr;   // orders the context's stream after pic_deposit_cvwm_noalloc
   std::vector<void*> allocs;
   // mesh
   pic::DevMesh M{};
@@ -38,6 +39,12 @@ struct pic_ctx {
   double* NS = nullptr;
   double* PS = nullptr;
   bool ps_valid = false;        // PS holds a deposition
+  // VerifyDepositedCharge: wGP^3/sJ per DOF, per-element partial integrals, result, inside particles per species
+  double* charge_w = nullptr;
+  double* charge_elem = nullptr;
+  double* charge_out = nullptr;
+  int* species_count = nullptr;
+  double charge_dim_factor = 1.0;
   // HDG field solve (pic_hdg_init)
   HdgState* hdg = nullptr;
   std::vector<double> xgp_h, wgp_h;   // N_Inter(N)%xGP, wGP
@@ -62,7 +69,6 @@ struct pic_ctx {
   double prof_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t prof_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
-  pic::Consts k{};      // device constants, kept for kernels of other translation units
   template <class T>
   int alloc(T** p, size_t n) {
     if (n == 0) n = 1;

@@ -45,8 +45,6 @@ struct Consts {
   int pv_dir[3];                               // periodic vector index per axis (-1: none)
   int sf_keep[3];                              // 1D/2D shape function: 1 in the kernel directions
 };
-// one copy per translation unit; only pic_kernels.cu launches kernels that read it
-static __constant__ Consts c_k;
 
 // ---- mesh (device arrays) ---------------------------------------------------------------
 struct DevMesh {
@@ -72,6 +70,9 @@ struct DevMesh {
   const double* bc_geo;
   // shape-function DOF coordinates: elem_xgp, or for a 1D/2D kernel its directions only (others zero)
   const double* sf_xgp;
+  // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
+  // read from the launch's parameter bank (each launch carries its own context's copy)
+  Consts k;
 };
 // one wall-side entry of a BC element: [0..2] BaseVectors0, [3..5] BaseVectors1, [6..8] BaseVectors2,
 // [9..11] SideNormVec (away from the domain), [12] SideDistance, [13] SideBCMetrics(BCSIDE_DISTANCE),
@@ -150,7 +151,8 @@ __device__ __forceinline__ void lagrange_f(float x, const float* xgp, const floa
 // x -> xi: GetRefNewtonStartValue (guess 1, eval_xyz.f90:549-562) + RefElemNewton (:298-445)
 // ==========================================================================================
 __device__ __forceinline__ void newton_start(const DevMesh& M, int e, const double x[3], double xi[3]) {
-  const double epsOne = 1.0 + c_k.refmapping_eps;
+  const Consts& kc = M.k;
+  const double epsOne = 1.0 + kc.refmapping_eps;
   const double* b = M.bary + (size_t)e * 3;
   double P0 = x[0] - __ldg(b + 0), P1 = x[1] - __ldg(b + 1), P2 = x[2] - __ldg(b + 2);
   double xil[6];
@@ -172,6 +174,7 @@ __device__ __forceinline__ void newton_start(const DevMesh& M, int e, const doub
 
 // Returns isSuccessful (false when the iterate left |xi| <= 1.5).
 static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
   const double* X = M.xcl + (size_t)e * 24;
   const double* DX = M.dxcl + (size_t)e * 72;
   double Xl[24];
@@ -179,7 +182,7 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
   for (int q = 0; q < 24; ++q) Xl[q] = __ldg(X + q);
   double L[3][2];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) lagrange<2>(xi[d], c_k.xi_cl, c_k.wbary_cl, L[d]);
+  for (int d = 0; d < 3; ++d) lagrange<2>(xi[d], kc.xi_cl, kc.wbary_cl, L[d]);
   double F[3] = {-x[0], -x[1], -x[2]};
 #pragma unroll
   for (int k = 0; k < 2; ++k)
@@ -197,7 +200,7 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
   double normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
   int iter = 0;
   bool success = true;
-  while (deltaXi2 > c_k.refmapping_eps && iter < 100) {
+  while (deltaXi2 > kc.refmapping_eps && iter < 100) {
     iter = iter + 1;
     double J[3][3];
 #pragma unroll
@@ -245,7 +248,7 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
 #pragma unroll
       for (int d = 0; d < 3; ++d) xi[d] = xo[d] - lambda * dxi[d];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) lagrange<2>(xi[d], c_k.xi_cl, c_k.wbary_cl, L[d]);
+      for (int d = 0; d < 3; ++d) lagrange<2>(xi[d], kc.xi_cl, kc.wbary_cl, L[d]);
       F[0] = -x[0]; F[1] = -x[1]; F[2] = -x[2];
 #pragma unroll
       for (int k = 0; k < 2; ++k)
@@ -274,6 +277,7 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
 // shape functions written as (1 -+ xi)/2 (no barycentric divisions), fused multiply-adds and one
 // reciprocal of det(J) per iteration.  Converges to the same xi up to rounding.
 static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
   const double* X = M.xcl + (size_t)e * 24;
   const double* DX = M.dxcl + (size_t)e * 72;
   double Xl[24];
@@ -295,7 +299,7 @@ static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e
   double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
   double normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
   bool success = true;
-  for (int iter = 0; iter < 100 && deltaXi2 > c_k.refmapping_eps; ++iter) {
+  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
     const double l[3][2] = {{0.5 * (1.0 - xi[0]), 0.5 * (1.0 + xi[0])}, {0.5 * (1.0 - xi[1]), 0.5 * (1.0 + xi[1])},
                             {0.5 * (1.0 - xi[2]), 0.5 * (1.0 + xi[2])}};
     double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -354,11 +358,11 @@ __device__ __forceinline__ bool position_in_ref_elem_t(const DevMesh& M, int e, 
 // Field at a reference position: EvaluateFieldAtRefPos, eval_xyz.f90:167-215 (NVar_in = 3)
 // ==========================================================================================
 template <int N>
-__device__ __forceinline__ void eval_field(const double* __restrict__ U, const double xi[3], double out[3]) {
+__device__ __forceinline__ void eval_field(const Consts& kc, const double* __restrict__ U, const double xi[3], double out[3]) {
   constexpr int n1 = N + 1;
   double L[3][n1];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) lagrange<n1>(xi[d], c_k.xgp, c_k.wbary_gp, L[d]);
+  for (int d = 0; d < 3; ++d) lagrange<n1>(xi[d], kc.xgp, kc.wbary_gp, L[d]);
   out[0] = out[1] = out[2] = 0.0;
 #pragma unroll
   for (int k = 0; k < n1; ++k)
@@ -412,8 +416,8 @@ static __device__ __noinline__ void eval_field_dw(const DevMesh& M, const double
 // ==========================================================================================
 // Boris-Leapfrog push, timedisc_TimeStepPoissonByBorisLeapfrog.f90:128-197 (FP64)
 // ==========================================================================================
-__device__ __forceinline__ void boris_push(double v[3], const double F[6], int sp, bool& is_new, double dt) {
-  const double q = c_k.q[sp], mass = c_k.m[sp];
+__device__ __forceinline__ void boris_push(const Consts& kc, double v[3], const double F[6], int sp, bool& is_new, double dt) {
+  const double q = kc.q[sp], mass = kc.m[sp];
   const bool push = fabs(q) > 0.0;
   if (is_new) {
     if (push) {
@@ -424,7 +428,7 @@ __device__ __forceinline__ void boris_push(double v[3], const double F[6], int s
     is_new = false;
   }
   if (!push) return;
-  const double c2_inv = c_k.c2_inv;
+  const double c2_inv = kc.c2_inv;
   double c1 = (q * dt) / (mass * 2.0);
   double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
   double gamma = 1.0 / sqrt(1.0 - (vv * c2_inv));
@@ -654,6 +658,7 @@ __device__ __forceinline__ void perfect_reflection(double v[3], double x[3], dou
 // Returns the new element, -1 if the particle is lost, -2 if the hop cap was hit, -3 if it left through an
 // open boundary (RemoveParticle; not a lost particle).
 static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double x[3], double xl[3], double v[3]) {
+  const Consts& kc = M.k;
   if (certainly_inside_f32(M, elem, x)) return elem;     // same decision as the FP64 test below
   int doneE[6] = {0, 0, 0, 0, 0, 0}, doneS[6] = {0, 0, 0, 0, 0, 0}, doneT[6] = {0, 0, 0, 0, 0, 0};
   // doneE/doneS/doneT hold DoneLastElem(1/4/3, 1:6) with 1-based element and side ids (0 = empty)
@@ -733,7 +738,7 @@ static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double
 #pragma unroll
       for (int c = 0; c < 3; ++c) xl[c] = xl[c] + traj[c] * alpha;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) xl[c] = xl[c] + copysign(c_k.pv[3 * k + c], sg);
+      for (int c = 0; c < 3; ++c) xl[c] = xl[c] + copysign(kc.pv[3 * k + c], sg);
 #pragma unroll
       for (int c = 0; c < 3; ++c) x[c] = xl[c] + (len - alpha) * traj[c];
     }
@@ -745,20 +750,20 @@ static __device__ __noinline__ int tria_track(const DevMesh& M, int elem, double
 // ==========================================================================================
 // RefTracking with CartesianPeriodic = FastPeriodic = T (particle_reftracking.f90:30-414, 697-985)
 // ==========================================================================================
-__device__ __forceinline__ void periodic_movement_fast(double x[3], double xl[3]) {
+__device__ __forceinline__ void periodic_movement_fast(const Consts& kc, double x[3], double xl[3]) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int k = c_k.pv_dir[d];
+    const int k = kc.pv_dir[d];
     if (k < 0) continue;
-    const double* pv = c_k.pv + 3 * k;
-    if (x[d] > c_k.xmax[d]) {
-      double n = ceil(fabs(x[d] - c_k.xmax[d]) / fabs(pv[d]));
+    const double* pv = kc.pv + 3 * k;
+    if (x[d] > kc.xmax[d]) {
+      double n = ceil(fabs(x[d] - kc.xmax[d]) / fabs(pv[d]));
       double mv[3] = {n * pv[0], n * pv[1], n * pv[2]};
       if (pv[d] > 0.0) { for (int c = 0; c < 3; ++c) { x[c] = x[c] - mv[c]; xl[c] = xl[c] - mv[c]; } }
       else { for (int c = 0; c < 3; ++c) { x[c] = x[c] + mv[c]; xl[c] = xl[c] + mv[c]; } }
     }
-    if (x[d] < c_k.xmin[d]) {
-      double n = ceil(fabs(x[d] - c_k.xmin[d]) / fabs(pv[d]));
+    if (x[d] < kc.xmin[d]) {
+      double n = ceil(fabs(x[d] - kc.xmin[d]) / fabs(pv[d]));
       double mv[3] = {n * pv[0], n * pv[1], n * pv[2]};
       if (pv[d] > 0.0) { for (int c = 0; c < 3; ++c) { x[c] = x[c] + mv[c]; xl[c] = xl[c] + mv[c]; } }
       else { for (int c = 0; c < 3; ++c) { x[c] = x[c] - mv[c]; xl[c] = xl[c] - mv[c]; } }
@@ -988,6 +993,7 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int elem, doub
 template <bool FAST>
 __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[3], double xl[3], double xi[3],
                                       double v[3], bool& tol_fail, bool& removed, bool& cap_hit) {
+  const Consts& kc = M.k;
   tol_fail = false;
   removed = false;
   const bool bc_elem = M.bc_e2b && __ldg(M.bc_e2b + 2 * last_elem) > 0;
@@ -997,13 +1003,13 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
     if (bc_tracking(M, last_elem, x, xl, v, removed, len0, cap_hit)) return last_elem;
     position_in_ref_elem_t<FAST>(M, last_elem, x, xi);
     if (maxabs3(xi) < 1.0) return last_elem;
-  } else if (c_k.n_pv > 0) {
+  } else if (kc.n_pv > 0) {
     double lp[3] = {x[0], x[1], x[2]};
-    periodic_movement_fast(x, xl);
+    periodic_movement_fast(kc, x, xl);
     int guard = 0;
     while ((!almost_equal(lp[0], x[0]) || !almost_equal(lp[1], x[1]) || !almost_equal(lp[2], x[2])) && guard < 16) {
       lp[0] = x[0]; lp[1] = x[1]; lp[2] = x[2];
-      periodic_movement_fast(x, xl);
+      periodic_movement_fast(kc, x, xl);
       guard++;
     }
   }
@@ -1015,11 +1021,11 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
   int cell[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    int cc = (int)floor((x[d] - c_k.xmin[d]) / c_k.fib_delta[d]);
+    int cc = (int)floor((x[d] - kc.xmin[d]) / kc.fib_delta[d]);
     cc = (cc > 0 ? cc : 0) + 1;
-    cell[d] = cc < c_k.fib_imax[d] ? cc : c_k.fib_imax[d];
+    cell[d] = cc < kc.fib_imax[d] ? cc : kc.fib_imax[d];
   }
-  const size_t cidx = (size_t)(cell[0] - 1) + (size_t)c_k.fib_imax[0] * ((cell[1] - 1) + (size_t)c_k.fib_imax[1] * (cell[2] - 1));
+  const size_t cidx = (size_t)(cell[0] - 1) + (size_t)kc.fib_imax[0] * ((cell[1] - 1) + (size_t)kc.fib_imax[1] * (cell[2] - 1));
   int nBGM = __ldg(M.fib_n + cidx);
   const int off = __ldg(M.fib_off + cidx);
   if (nBGM > kMaxBgmCand) nBGM = kMaxBgmCand;      // pic_create rejects FIBGM cells with more
@@ -1236,13 +1242,14 @@ static __global__ void k_node_normalize(const double* __restrict__ node_vol, dou
 // Node sums -> DOFs (pic_depo_method.f90:692-733): PartSource(1:4,k,l,m) of every element.
 // NORMALIZED: NS already holds NodeSource / NodeVolume (k_node_normalize ran first).
 template <int N, bool NORMALIZED = false>
-__global__ void k_node_to_dof(DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
+__global__ void k_node_to_dof(const __grid_constant__ DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.ne * nd) return;
   const int e = t / nd, r = t - e * nd;
   const int kk = r % n1, ll = (r / n1) % n1, mm = r / (n1 * n1);
-  const double a1 = c_k.fac_gp[kk], a2 = c_k.fac_gp[ll], a3 = c_k.fac_gp[mm];
+  const double a1 = kc.fac_gp[kk], a2 = kc.fac_gp[ll], a3 = kc.fac_gp[mm];
   double S[8][4];
 #pragma unroll
   for (int n = 0; n < 8; ++n) {

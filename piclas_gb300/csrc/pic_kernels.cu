@@ -19,7 +19,7 @@ namespace pic {
 // ---------------------------------------------------------------------------------------------
 
 
-__device__ __forceinline__ bool position_in_ref_elem_f(const MeshF& F, int e, const float p[3], float xi[3]) {
+__device__ __forceinline__ bool position_in_ref_elem_f(const Consts& kc, const MeshF& F, int e, const float p[3], float xi[3]) {
   const float* B = F.xez + (size_t)e * 18;
   const float* S = F.slen + (size_t)e * 6;
   float xil[6];
@@ -28,7 +28,7 @@ __device__ __forceinline__ bool position_in_ref_elem_f(const MeshF& F, int e, co
     xil[d] = fmaf(p[0], __ldg(B + 3 * d), fmaf(p[1], __ldg(B + 3 * d + 1), p[2] * __ldg(B + 3 * d + 2))) * __ldg(S + d);
 #pragma unroll
   for (int d = 0; d < 3; ++d) xi[d] = 0.5f * (xil[d] - xil[d + 3]);
-  const float epsOne = 1.0f + (float)c_k.refmapping_eps;
+  const float epsOne = 1.0f + (float)kc.refmapping_eps;
   if (fmaxf(fabsf(xi[0]), fmaxf(fabsf(xi[1]), fabsf(xi[2]))) > epsOne) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) xi[d] = fmaxf(fminf(1.0f, xi[d]), -1.0f);
@@ -37,7 +37,7 @@ __device__ __forceinline__ bool position_in_ref_elem_f(const MeshF& F, int e, co
   const float* DX = F.dxcl + (size_t)e * 72;
   bool success = true;
   float deltaXi2 = 1.0f;
-  for (int iter = 0; iter < 100 && deltaXi2 > (float)c_k.refmapping_eps; ++iter) {
+  for (int iter = 0; iter < 100 && deltaXi2 > (float)kc.refmapping_eps; ++iter) {
     float l[3][2];
 #pragma unroll
     for (int d = 0; d < 3; ++d) { l[d][0] = 0.5f * (1.0f - xi[d]); l[d][1] = 0.5f * (1.0f + xi[d]); }
@@ -71,11 +71,11 @@ __device__ __forceinline__ bool position_in_ref_elem_f(const MeshF& F, int e, co
 }
 
 template <int N>
-__device__ __forceinline__ void eval_field_f(const float* __restrict__ U, const float xi[3], float out[3]) {
+__device__ __forceinline__ void eval_field_f(const Consts& kc, const float* __restrict__ U, const float xi[3], float out[3]) {
   constexpr int n1 = N + 1;
   float L[3][n1];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) lagrange_f<n1>(xi[d], c_k.xgp_f, c_k.wbary_gp_f, L[d]);
+  for (int d = 0; d < 3; ++d) lagrange_f<n1>(xi[d], kc.xgp_f, kc.wbary_gp_f, L[d]);
   out[0] = out[1] = out[2] = 0.0f;
 #pragma unroll
   for (int k = 0; k < n1; ++k)
@@ -93,8 +93,8 @@ __device__ __forceinline__ void eval_field_f(const float* __restrict__ U, const 
 }
 
 // FP32 Boris push (mixed variant)
-__device__ __forceinline__ void boris_push_f(float v[3], const float F[6], int sp, bool& is_new, float dt) {
-  const float q = (float)c_k.q[sp], qmt = (float)(c_k.q[sp] / c_k.m[sp]);
+__device__ __forceinline__ void boris_push_f(const Consts& kc, float v[3], const float F[6], int sp, bool& is_new, float dt) {
+  const float q = (float)kc.q[sp], qmt = (float)(kc.q[sp] / kc.m[sp]);
   const bool push = fabsf(q) > 0.0f;
   if (is_new) {
     if (push) {
@@ -104,7 +104,7 @@ __device__ __forceinline__ void boris_push_f(float v[3], const float F[6], int s
     is_new = false;
   }
   if (!push) return;
-  const float c2i = (float)c_k.c2_inv;
+  const float c2i = (float)kc.c2_inv;
   const float c1 = 0.5f * qmt * dt;
   const float vv = fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2]));
   const float gamma = rsqrtf(1.0f - vv * c2i);
@@ -142,16 +142,17 @@ __device__ __forceinline__ void boris_push_f(float v[3], const float F[6], int s
 #define PIC_CVWM_MINB 1         // FP64 variant
 #endif
 template <int N, bool MIXED>
-__global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MINB) k_step_cvwm_tria(DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
+__global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MINB) k_step_cvwm_tria(const __grid_constant__ DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
                                                         const float* __restrict__ E32, double* __restrict__ NS,
                                                         double dt, DevStatus* st) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool in_range = i < P.n;
   const uint8_t fl = in_range ? P.flags[i] : 0;
   const bool inside = (fl & kInside) != 0;
   const int sp = inside ? P.species[i] : 0;
-  const bool charged = inside && (c_k.q[sp] != 0.0);
+  const bool charged = inside && (kc.q[sp] != 0.0);
   int e = inside ? P.elem[i] : 0;
   double x[3] = {0.0, 0.0, 0.0};
   if (inside) { x[0] = P.x[i]; x[1] = P.y[i]; x[2] = P.z[i]; }
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     {
       double contrib[32];
       if (charged) {
-        const double ch = c_k.qm[sp];
+        const double ch = kc.qm[sp];
         const double TS[4] = {v[0] * ch, v[1] * ch, v[2] * ch, ch};
         cvwm_contrib(M, e, suc, xi, x, TS, contrib);
       }
@@ -179,11 +180,11 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     }
     if (!inside) return;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) Fd[c] = c_k.ext[c];
+    for (int c = 0; c < 6; ++c) Fd[c] = kc.ext[c];
     if (charged) {
       double Eo[3];
       const double* U = E + (size_t)e * nd * 3;
-      if (suc) eval_field<N>(U, xi, Eo);
+      if (suc) eval_field<N>(kc, U, xi, Eo);
       else eval_field_dw<N>(M, U, e, x, Eo);
 #pragma unroll
       for (int c = 0; c < 3; ++c) Fd[c] = Fd[c] + Eo[c];
@@ -191,8 +192,8 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
       for (int c = 3; c < 6; ++c) Fd[c] = Fd[c] + 0.0;
     }
     bool isnew = (fl & kNew) != 0;
-    const double dtv = dt * c_k.dt_fac[sp];
-    boris_push(v, Fd, sp, isnew, dtv);
+    const double dtv = dt * kc.dt_fac[sp];
+    boris_push(kc, v, Fd, sp, isnew, dtv);
     double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dtv;
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     if (charged) {
       const double* b = M.bary + (size_t)e * 3;
       const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
-      suc = position_in_ref_elem_f(MF, e, p, xi);
+      suc = position_in_ref_elem_f(kc, MF, e, p, xi);
       if (!suc) {
         // fall back to the FP64 mapping so that the inverse-distance branch matches the reference's
         double xd[3];
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     {
       float hi[32];
       if (charged) {
-        const float ch = (float)c_k.qm[sp];
+        const float ch = (float)kc.qm[sp];
         const float TS[4] = {v[0] * ch, v[1] * ch, v[2] * ch, ch};
         if (suc) {
           const float a1 = 0.5f * (xi[0] + 1.0f), a2 = 0.5f * (xi[1] + 1.0f), a3 = 0.5f * (xi[2] + 1.0f);
@@ -258,11 +259,11 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     }
     if (!inside) return;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) Ff[c] = (float)c_k.ext[c];
+    for (int c = 0; c < 6; ++c) Ff[c] = (float)kc.ext[c];
     if (charged) {
       float Eo[3];
       if (suc) {
-        eval_field_f<N>(E32 + (size_t)e * nd * 3, xi, Eo);
+        eval_field_f<N>(kc, E32 + (size_t)e * nd * 3, xi, Eo);
       } else {
         double Ed[3];
         eval_field_dw<N>(M, E + (size_t)e * nd * 3, e, x, Ed);
@@ -272,8 +273,8 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
       for (int c = 0; c < 3; ++c) Ff[c] += Eo[c];
     }
     bool isnew = (fl & kNew) != 0;
-    const double dtv = dt * c_k.dt_fac[sp];
-    boris_push_f(v, Ff, sp, isnew, (float)dtv);
+    const double dtv = dt * kc.dt_fac[sp];
+    boris_push_f(kc, v, Ff, sp, isnew, (float)dtv);
     double xl[3] = {x[0], x[1], x[2]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dtv;
@@ -304,21 +305,22 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
 // Separate loop pieces (the reference's individual routines)
 // =============================================================================================
 template <int N, bool MIXED>
-__global__ void __launch_bounds__(256) k_interpolate(DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
+__global__ void __launch_bounds__(256) k_interpolate(const __grid_constant__ DevMesh M, MeshF MF, DevParticles P, const double* __restrict__ E,
                                                      const float* __restrict__ E32, DevStatus* st, bool refmap,
                                                      bool cvwm) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
   if (!(fl & kInside)) return;
   const int sp = P.species[i];
-  if (c_k.q[sp] == 0.0) return;   // isInterpolateParticle
+  if (kc.q[sp] == 0.0) return;   // isInterpolateParticle
   const int e = P.elem[i];
   const double x[3] = {P.x[i], P.y[i], P.z[i]};
   double F[6];
 #pragma unroll
-  for (int c = 0; c < 6; ++c) F[c] = c_k.ext[c];
+  for (int c = 0; c < 6; ++c) F[c] = kc.ext[c];
   double Eo[3];
   if constexpr (!MIXED) {
     double xi[3];
@@ -331,14 +333,14 @@ __global__ void __launch_bounds__(256) k_interpolate(DevMesh M, MeshF MF, DevPar
     }
     const double* U = E + (size_t)e * nd * 3;
     if (!suc && cvwm) eval_field_dw<N>(M, U, e, x, Eo);
-    else eval_field<N>(U, xi, Eo);
+    else eval_field<N>(kc, U, xi, Eo);
   } else {
     float xi[3];
     bool suc = true;
     if (!refmap) {
       const double* b = M.bary + (size_t)e * 3;
       const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
-      suc = position_in_ref_elem_f(MF, e, p, xi);
+      suc = position_in_ref_elem_f(kc, MF, e, p, xi);
       if (!suc) {
         double xd[3];
         suc = position_in_ref_elem(M, e, x, xd);
@@ -352,7 +354,7 @@ __global__ void __launch_bounds__(256) k_interpolate(DevMesh M, MeshF MF, DevPar
       eval_field_dw<N>(M, E + (size_t)e * nd * 3, e, x, Eo);
     } else {
       float Ef[3];
-      eval_field_f<N>(E32 + (size_t)e * nd * 3, xi, Ef);
+      eval_field_f<N>(kc, E32 + (size_t)e * nd * 3, xi, Ef);
       Eo[0] = Ef[0]; Eo[1] = Ef[1]; Eo[2] = Ef[2];
     }
   }
@@ -363,7 +365,7 @@ __global__ void __launch_bounds__(256) k_interpolate(DevMesh M, MeshF MF, DevPar
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStatus* st) {
+__global__ void __launch_bounds__(256) k_push(const __grid_constant__ Consts kc, DevParticles P, double dt, DevStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
@@ -379,8 +381,8 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStat
 #pragma unroll
     for (int c = 0; c < 6; ++c) F[c] = P.field[(size_t)c * P.cap + i];
     double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
-    const double dtv = dt * c_k.dt_fac[sp];
-    boris_push(v, F, sp, isnew, dtv);
+    const double dtv = dt * kc.dt_fac[sp];
+    boris_push(kc, v, F, sp, isnew, dtv);
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dtv;
     P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
@@ -390,8 +392,8 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStat
 #pragma unroll
     for (int c = 0; c < 6; ++c) F[c] = (float)P.field[(size_t)c * P.cap + i];
     float v[3] = {P.vxf[i], P.vyf[i], P.vzf[i]};
-    const double dtv = dt * c_k.dt_fac[sp];
-    boris_push_f(v, F, sp, isnew, (float)dtv);
+    const double dtv = dt * kc.dt_fac[sp];
+    boris_push_f(kc, v, F, sp, isnew, (float)dtv);
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dtv;
     P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(256) k_push(DevParticles P, double dt, DevStat
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_track_tria(DevMesh M, DevParticles P, DevStatus* st) {
+__global__ void __launch_bounds__(256) k_track_tria(const __grid_constant__ DevMesh M, DevParticles P, DevStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
@@ -431,7 +433,7 @@ __global__ void __launch_bounds__(256) k_track_tria(DevMesh M, DevParticles P, D
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_track_ref(DevMesh M, DevParticles P, DevStatus* st) {
+__global__ void __launch_bounds__(256) k_track_ref(const __grid_constant__ DevMesh M, DevParticles P, DevStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
@@ -456,14 +458,15 @@ __global__ void __launch_bounds__(256) k_track_ref(DevMesh M, DevParticles P, De
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_deposit_cvwm(DevMesh M, MeshF MF, DevParticles P, double* __restrict__ NS,
+__global__ void __launch_bounds__(256) k_deposit_cvwm(const __grid_constant__ DevMesh M, MeshF MF, DevParticles P, double* __restrict__ NS,
                                                       DevStatus* st) {
+  const Consts& kc = M.k;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool in_range = i < P.n;
   const uint8_t fl = in_range ? P.flags[i] : 0;
   const bool inside = (fl & kInside) != 0;
   const int sp = inside ? P.species[i] : 0;
-  const bool charged = inside && (c_k.q[sp] != 0.0);
+  const bool charged = inside && (kc.q[sp] != 0.0);
   const int e = inside ? P.elem[i] : 0;
   double x[3] = {0.0, 0.0, 0.0};
   if (inside) { x[0] = P.x[i]; x[1] = P.y[i]; x[2] = P.z[i]; }
@@ -473,7 +476,7 @@ __global__ void __launch_bounds__(256) k_deposit_cvwm(DevMesh M, MeshF MF, DevPa
       double xi[3];
       const bool suc = position_in_ref_elem(M, e, x, xi);
       if (!suc) { atomicAdd(&st->n_newton_failed, 1); flag_status(st, 0x02u); }
-      const double ch = c_k.qm[sp];
+      const double ch = kc.qm[sp];
       const double TS[4] = {P.vx[i] * ch, P.vy[i] * ch, P.vz[i] * ch, ch};
       cvwm_contrib(M, e, suc, xi, x, TS, contrib);
     }
@@ -484,8 +487,8 @@ __global__ void __launch_bounds__(256) k_deposit_cvwm(DevMesh M, MeshF MF, DevPa
       const double* b = M.bary + (size_t)e * 3;
       const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
       float xi[3];
-      bool suc = position_in_ref_elem_f(MF, e, p, xi);
-      const float ch = (float)c_k.qm[sp];
+      bool suc = position_in_ref_elem_f(kc, MF, e, p, xi);
+      const float ch = (float)kc.qm[sp];
       const float TS[4] = {P.vxf[i] * ch, P.vyf[i] * ch, P.vzf[i] * ch, ch};
       if (!suc) {
         double xd[3];
@@ -576,7 +579,7 @@ __global__ void __launch_bounds__(1024) k_scan(const int* __restrict__ count, in
 // Shape-function deposition: pack particles by element, then gather per target element
 // =============================================================================================
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_sf_pack(DevParticles P, int* __restrict__ cursor, const double* __restrict__ dofc,
+__global__ void __launch_bounds__(256) k_sf_pack(const __grid_constant__ Consts kc, DevParticles P, int* __restrict__ cursor, const double* __restrict__ dofc,
                                                  SfPack K) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < P.n && (P.flags[i] & kInside);
@@ -584,14 +587,14 @@ __global__ void __launch_bounds__(256) k_sf_pack(DevParticles P, int* __restrict
   const int slot = warp_slot(cursor, e, valid);
   if (!valid) return;
   const int sp = P.species[i];
-  const double qm = c_k.qm[sp];
+  const double qm = kc.qm[sp];
   // 1D/2D shape function: the coordinates without kernel are zero, as in the DOF coordinates
-  const double x = c_k.sf_keep[0] ? P.x[i] : 0.0, y = c_k.sf_keep[1] ? P.y[i] : 0.0, z = c_k.sf_keep[2] ? P.z[i] : 0.0;
+  const double x = kc.sf_keep[0] ? P.x[i] : 0.0, y = kc.sf_keep[1] ? P.y[i] : 0.0, z = kc.sf_keep[2] ? P.z[i] : 0.0;
   const double* c = dofc + (size_t)e * 3;
   const float4 rel = make_float4((float)(x - __ldg(c)), (float)(y - __ldg(c + 1)), (float)(z - __ldg(c + 2)), 0.0f);
   reinterpret_cast<float4*>(K.posf)[slot] = rel;
   if constexpr (!MIXED) {
-    const double w = c_k.sf_w;
+    const double w = kc.sf_w;
     // Fac(1:3) = PartVelo*ChargeMPF, Fac(4) = ChargeMPF, Fac = Fac*w_sf (shapefunction_tools:78-100)
     const double f0 = (P.vx[i] * qm) * w, f1 = (P.vy[i] * qm) * w, f2 = (P.vz[i] * qm) * w, f3 = qm * w;
     K.pos[(size_t)slot * 3] = x; K.pos[(size_t)slot * 3 + 1] = y; K.pos[(size_t)slot * 3 + 2] = z;
@@ -599,7 +602,7 @@ __global__ void __launch_bounds__(256) k_sf_pack(DevParticles P, int* __restrict
     fp[0] = make_double2(f0, f1);
     fp[1] = make_double2(f2, f3);
   } else {
-    const float w = (float)(c_k.sf_w * qm);
+    const float w = (float)(kc.sf_w * qm);
     reinterpret_cast<float4*>(K.facf)[slot] = make_float4(P.vxf[i] * w, P.vyf[i] * w, P.vzf[i] * w, w);
   }
 }
@@ -616,8 +619,9 @@ struct SfShape {
 // FP64 gather.  An FP32 pre-test on coordinates relative to the target element's DOF centre
 // discards pairs outside (1+1e-4) R; the rest is evaluated exactly as the reference does in FP64.
 template <int N>
-__global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh M, SfLists L, const int* __restrict__ off,
+__global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(const __grid_constant__ DevMesh M, SfLists L, const int* __restrict__ off,
                                                                         SfPack K, double* __restrict__ PS) {
+  const Consts& kc = M.k;
   using S = SfShape<N>;
   constexpr int nd = S::nd, split = S::split;
   __shared__ double s_pos[kSfChunk][3];
@@ -637,7 +641,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh 
     xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
     xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
   }
-  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  const double R2 = kc.sf_r2, R2inv = kc.sf_r2_inv;
   const float R2f = (float)(R2 * (1.0 + 1.0e-4));
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   const int p0 = __ldg(L.nb_off + e), p1 = __ldg(L.nb_off + e + 1);
@@ -646,8 +650,8 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh 
     double sh[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int k = c_k.pv_dir[d];
-      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+      const int k = kc.pv_dir[d];
+      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * kc.pv[3 * k + d] : 0.0;
     }
     const double* cs = L.dof_center + (size_t)s * 3;
     const float ox = (float)((__ldg(cs) + sh[0]) - cex), oy = (float)((__ldg(cs + 1) + sh[1]) - cey),
@@ -679,7 +683,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh 
             if (r2 <= R2) {
               const double Sv = 1.0 - R2inv * r2;
               double S1 = Sv * Sv;
-              for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+              for (int ex = 3; ex <= kc.sf_alpha; ++ex) S1 = Sv * S1;
 #pragma unroll
               for (int c = 0; c < 4; ++c) acc[c] = acc[c] + S1 * s_fac[q][c];
             }
@@ -708,8 +712,9 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(DevMesh 
 
 // Mixed gather: FP32 distances and weights, per-DOF TwoSum-compensated FP32 sums, FP64 result.
 template <int N>
-__global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh M, SfLists L, const int* __restrict__ off,
+__global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(const __grid_constant__ DevMesh M, SfLists L, const int* __restrict__ off,
                                                                          SfPack K, double* __restrict__ PS) {
+  const Consts& kc = M.k;
   using S = SfShape<N>;
   constexpr int nd = S::nd, split = S::split;
   __shared__ float4 s_rel[kSfChunk];
@@ -726,7 +731,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh
     const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
     xgf[0] = (float)(__ldg(g) - cex); xgf[1] = (float)(__ldg(g + 1) - cey); xgf[2] = (float)(__ldg(g + 2) - cez);
   }
-  const float R2 = (float)c_k.sf_r2, R2inv = (float)c_k.sf_r2_inv;
+  const float R2 = (float)kc.sf_r2, R2inv = (float)kc.sf_r2_inv;
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
   const int p0 = __ldg(L.nb_off + e), p1 = __ldg(L.nb_off + e + 1);
   for (int p = p0; p < p1; ++p) {
@@ -734,8 +739,8 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh
     double sh[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int k = c_k.pv_dir[d];
-      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+      const int k = kc.pv_dir[d];
+      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * kc.pv[3 * k + d] : 0.0;
     }
     const double* cs = L.dof_center + (size_t)s * 3;
     const float ox = (float)((__ldg(cs) + sh[0]) - cex), oy = (float)((__ldg(cs + 1) + sh[1]) - cey),
@@ -759,7 +764,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh
           if (r2 <= R2) {
             const float Sv = fmaf(-R2inv, r2, 1.0f);
             float S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            for (int ex = 3; ex <= kc.sf_alpha; ++ex) S1 = Sv * S1;
             const float4 f = s_fac[q];
             const float fc[4] = {f.x, f.y, f.z, f.w};
 #pragma unroll
@@ -807,8 +812,9 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(DevMesh
 constexpr int kSf2Threads = 128;   // 4 warps: (DOF half) x (particle parity)
 
 template <int N, bool MIXED>
-__global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L, const int* __restrict__ off,
+__global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(const __grid_constant__ DevMesh M, SfLists L, const int* __restrict__ off,
                                                             SfPack K, double* __restrict__ PS) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   static_assert(nd <= 64, "two-phase gather holds at most 64 DOFs per element");
   __shared__ float4 s_rel[kSf2Chunk];
@@ -831,9 +837,9 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L
     xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
     xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
   }
-  const double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  const double R2 = kc.sf_r2, R2inv = kc.sf_r2_inv;
   const float R2f = (float)(R2 * (1.0 + 1.0e-4));
-  const float cull = (float)c_k.sf_r + __ldg(L.dof_radius + e);
+  const float cull = (float)kc.sf_r + __ldg(L.dof_radius + e);
   const float cull2 = cull * cull * 1.0001f;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
@@ -843,8 +849,8 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L
     double sh[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int k = c_k.pv_dir[d];
-      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+      const int k = kc.pv_dir[d];
+      sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * kc.pv[3 * k + d] : 0.0;
     }
     const double* cs = L.dof_center + (size_t)s * 3;
     const float ox = (float)((__ldg(cs) + sh[0]) - cex), oy = (float)((__ldg(cs + 1) + sh[1]) - cey),
@@ -895,7 +901,7 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L
           if (r2 <= (float)R2) {
             const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
             float S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            for (int ex = 3; ex <= kc.sf_alpha; ++ex) S1 = Sv * S1;
             const float4 f = s_facf[q];
             const float fc[4] = {f.x, f.y, f.z, f.w};
 #pragma unroll
@@ -914,7 +920,7 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(DevMesh M, SfLists L
           if (r2 <= R2) {
             const double Sv = fma(-R2inv, r2, 1.0);
             double S1 = Sv * Sv;
-            for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+            for (int ex = 3; ex <= kc.sf_alpha; ++ex) S1 = Sv * S1;
 #pragma unroll
             for (int c = 0; c < 4; ++c) acc[c] = fma(S1, s_fac[q][c], acc[c]);
           }
@@ -961,16 +967,17 @@ constexpr int kSf5Pairs = 160;
 
 // (1 - r^2/R^2)^alpha from Sv = 1 - r^2/R^2: S*S, then alpha - 2 more factors (runtime alpha unless A2)
 template <bool A2, typename T>
-__device__ __forceinline__ T sf_power(T Sv) {
+__device__ __forceinline__ T sf_power(const Consts& kc, T Sv) {
   T S1 = Sv * Sv;
   if constexpr (!A2)
-    for (int ex = 3; ex <= c_k.sf_alpha; ++ex) S1 = Sv * S1;
+    for (int ex = 3; ex <= kc.sf_alpha; ++ex) S1 = Sv * S1;
   return S1;
 }
 
 template <int N, bool MIXED, bool ADAPT, bool A2>
-__global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L, const int* __restrict__ off,
+__global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constant__ DevMesh M, SfLists L, const int* __restrict__ off,
                                                             SfPack K, double* __restrict__ PS) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   static_assert(nd <= 64, "one DOF per lane, at most two DOF halves");
   constexpr int halves = nd > 32 ? 2 : 1, npar = 4 / halves;
@@ -1005,12 +1012,12 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
   const int e = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
   const double* ce = L.dof_center + (size_t)e * 3;
   const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
-  const double R2inv = c_k.sf_r2_inv;
-  const float R2f = (float)(c_k.sf_r2 * (1.0 + 1.0e-4));
-  const float cull = (float)c_k.sf_r + __ldg(L.dof_radius + e);
+  const double R2inv = kc.sf_r2_inv;
+  const float R2f = (float)(kc.sf_r2 * (1.0 + 1.0e-4));
+  const float cull = (float)kc.sf_r + __ldg(L.dof_radius + e);
   const float cull2 = cull * cull * 1.0001f;
   // FP16 pre-test where |p|/R + |g|/R <= 5 (DOF-box radius <= 2R), which bounds its r^2/R^2 error by 1.5e-2
-  const bool h2 = H2 && __ldg(L.dof_radius + e) <= 2.0f * (float)c_k.sf_r;
+  const bool h2 = H2 && __ldg(L.dof_radius + e) <= 2.0f * (float)kc.sf_r;
   double gd[4] = {0.0, 0.0, 0.0, 0.0};
   float gf[3] = {0.f, 0.f, 0.f};
   if (active) {
@@ -1036,8 +1043,8 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
       double sh[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const int k = c_k.pv_dir[d];
-        sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * c_k.pv[3 * k + d] : 0.0;
+        const int k = kc.pv_dir[d];
+        sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * kc.pv[3 * k + d] : 0.0;
       }
       const double* cs = L.dof_center + (size_t)src * 3;
       s_o[i][0] = (float)((__ldg(cs) + sh[0]) - cex);
@@ -1120,7 +1127,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
           const int a = p + npar * (2 * k), b = a + npar;
           const float4 ra = a < nst ? s_rel[a] : make_float4(1e3f, 1e3f, 1e3f, 0.f);
           const float4 rb = b < nst ? s_rel[b] : make_float4(1e3f, 1e3f, 1e3f, 0.f);
-          const float ir = c_k.sf_r_inv;
+          const float ir = kc.sf_r_inv;
           s_h[i][0] = __floats2half2_rn(ra.x * ir, rb.x * ir);
           s_h[i][1] = __floats2half2_rn(ra.y * ir, rb.y * ir);
           s_h[i][2] = __floats2half2_rn(ra.z * ir, rb.z * ir);
@@ -1134,7 +1141,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
       // particles per instruction.  Either way phase B repeats the exact test, so only the work changes.
       int nh = 0;
       if (h2) {
-        const float ir = c_k.sf_r_inv;
+        const float ir = kc.sf_r_inv;
         const __half2 gx = __float2half2_rn(gf[0] * ir), gy = __float2half2_rn(gf[1] * ir),
                       gz = __float2half2_rn(gf[2] * ir);
         const __half2 thr = __float2half2_rn(1.05f);
@@ -1161,10 +1168,10 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
           const float4 r = s_rel[q];
           const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const float2 rp = ADAPT ? s_rp[q] : make_float2((float)c_k.sf_r2, (float)R2inv);
+          const float2 rp = ADAPT ? s_rp[q] : make_float2((float)kc.sf_r2, (float)R2inv);
           if (r2 <= rp.x) {
             const float Sv = fmaf(-rp.y, r2, 1.0f);
-            const float S1 = sf_power<A2>(Sv);
+            const float S1 = sf_power<A2>(kc, Sv);
             const float4 f = s_facf[q];
             part[0] = fmaf(S1, f.x, part[0]);
             part[1] = fmaf(S1, f.y, part[1]);
@@ -1177,7 +1184,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(DevMesh M, SfLists L
                                   : fma(pa.x, gd[0], fma(pa.y, gd[1], fma(pb.x, gd[2], pb.y + gd[3])));
           // Sv >= 0 read from the sign bit (integer pipe); -0.0 is skipped, its contribution is 0
           if (__double_as_longlong(Sv) >= 0) {
-            const double S1 = sf_power<A2>(Sv);
+            const double S1 = sf_power<A2>(kc, Sv);
             const double2 f01 = s_fac[2 * q], f23 = s_fac[2 * q + 1];
             acc[0] = fma(S1, f01.x, acc[0]);
             acc[1] = fma(S1, f01.y, acc[1]);
@@ -1240,7 +1247,7 @@ __host__ __device__ constexpr int cc_round() { return (N + 1) * (N + 1) * (N + 1
 constexpr int kCcCap = 256;       // hit-list entries per thread: a whole round (ns <= 256), so no lane flushes alone
 
 template <int N, bool MIXED, bool A2>
-__device__ __forceinline__ void cc_eval(const double (*s_g)[5], const float4* s_gf, const uint8_t (*s_list)[kCcThreads],
+__device__ __forceinline__ void cc_eval(const Consts& kc, const double (*s_g)[5], const float4* s_gf, const uint8_t (*s_list)[kCcThreads],
                                         int nh, const double p[4], const float pf[3], double R2, double R2inv,
                                         double& acc, float& accf) {
   const int t = threadIdx.x;
@@ -1252,20 +1259,21 @@ __device__ __forceinline__ void cc_eval(const double (*s_g)[5], const float4* s_
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       if (r2 <= (float)R2) {
         const float Sv = fmaf(-(float)R2inv, r2, 1.0f);
-        accf = fmaf(g.w, sf_power<A2>(Sv), accf);
+        accf = fmaf(g.w, sf_power<A2>(kc, Sv), accf);
       }
     } else {
       // 1 - |p-g|^2/R^2 = A_p + p'.g + B_g (p' = 2p/R^2, A_p = 1 - |p|^2/R^2, B_g = -|g|^2/R^2, all relative to
       // the source's DOF centre): one add and three fused multiply-adds; r^2 <= R^2 read from the sign
       const double Sv = fma(p[0], s_g[d][0], fma(p[1], s_g[d][1], fma(p[2], s_g[d][2], p[3] + s_g[d][4])));
-      if (__double_as_longlong(Sv) >= 0) acc = fma(s_g[d][3], sf_power<A2>(Sv), acc);
+      if (__double_as_longlong(Sv) >= 0) acc = fma(s_g[d][3], sf_power<A2>(kc, Sv), acc);
     }
   }
 }
 
 template <int N, bool MIXED, bool A2>
-__global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L, const int* __restrict__ off, SfPack K,
+__global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(const __grid_constant__ DevMesh M, SfLists L, const int* __restrict__ off, SfPack K,
                                                            DevStatus* st) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1, ns = cc_round<N>() * nd;
   __shared__ double s_g[MIXED ? 1 : ns][5];     // DOF position minus the image shift, relative to the source's
                                                 // DOF centre; wGP^3/sJ; -|g|^2/R^2
@@ -1278,7 +1286,7 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
   const double* cs = L.dof_center + (size_t)s * 3;
   const double csx = __ldg(cs), csy = __ldg(cs + 1), csz = __ldg(cs + 2);
   // radius of the source element (shape_function_adaptive) or the global one
-  double R2 = c_k.sf_r2, R2inv = c_k.sf_r2_inv;
+  double R2 = kc.sf_r2, R2inv = kc.sf_r2_inv;
   if (L.elem_r) { const double r = __ldg(L.elem_r + s); R2 = r * r; R2inv = 1.0 / R2; }
   const float R2f = (float)(R2 * (1.0 + 1.0e-4));
   const int q0 = __ldg(L.t_off + s), npair = __ldg(L.t_off + s + 1) - q0;
@@ -1311,8 +1319,8 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
         double sh[3];
 #pragma unroll
         for (int dd = 0; dd < 3; ++dd) {
-          const int k = c_k.pv_dir[dd];
-          sh[dd] = k >= 0 ? (double)L.t_shift[3 * q + dd] * c_k.pv[3 * k + dd] : 0.0;
+          const int k = kc.pv_dir[dd];
+          sh[dd] = k >= 0 ? (double)L.t_shift[3 * q + dd] * kc.pv[3 * k + dd] : 0.0;
         }
         const double* g = M.sf_xgp + ((size_t)e * nd + d) * 3;
         const double gx = __ldg(g) - sh[0], gy = __ldg(g + 1) - sh[1], gz = __ldg(g + 2) - sh[2];
@@ -1332,14 +1340,14 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
         const float dx = pf[0] - g.x, dy = pf[1] - g.y, dz = pf[2] - g.z;
         if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= R2f) s_list[nh++][t] = (uint8_t)i;
       }
-      cc_eval<N, MIXED, A2>(s_g, s_gf, s_list, nh, p, pf, R2, R2inv, acc, accf);
+      cc_eval<N, MIXED, A2>(kc, s_g, s_gf, s_list, nh, p, pf, R2, R2inv, acc, accf);
     }
     if (act) {
-      const double tot = (MIXED ? (double)accf : acc) / c_k.sf_cc_div;
+      const double tot = (MIXED ? (double)accf : acc) / kc.sf_cc_div;
       const bool ok = tot > 0.0;
       // no DOF within R: with periodic images the reference divides by zero (calcSfSource:122); without,
       // it deposits nothing (nUsedElems = 0), as the zero scale does here
-      if (!ok && c_k.n_pv > 0) flag_status(st, 0x20u);
+      if (!ok && kc.n_pv > 0) flag_status(st, 0x20u);
       const double sc = ok ? 1.0 / tot : 0.0;
       if constexpr (MIXED) {
         float4* f = reinterpret_cast<float4*>(K.facf) + j;
@@ -1369,15 +1377,16 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(DevMesh M, SfLists L,
 #define PIC_REF_MIXED_MINB 2
 #endif
 template <int N, bool MIXED>
-__global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB) k_step_ref(DevMesh M, DevParticles P, const double* __restrict__ E,
+__global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB) k_step_ref(const __grid_constant__ DevMesh M, DevParticles P, const double* __restrict__ E,
                                                   const float* __restrict__ E32, double dt, DevStatus* st) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
   if (!(fl & kInside)) return;
   const int sp = P.species[i];
-  const bool charged = c_k.q[sp] != 0.0;
+  const bool charged = kc.q[sp] != 0.0;
   const int e = P.elem[i];
   double x[3] = {P.x[i], P.y[i], P.z[i]};
   double xi[3] = {P.xi0[i], P.xi1[i], P.xi2[i]};
@@ -1385,33 +1394,33 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
   if constexpr (!MIXED) {
     double F[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) F[c] = c_k.ext[c];
+    for (int c = 0; c < 6; ++c) F[c] = kc.ext[c];
     if (charged) {
       double Eo[3];
-      eval_field<N>(E + (size_t)e * nd * 3, xi, Eo);
+      eval_field<N>(kc, E + (size_t)e * nd * 3, xi, Eo);
 #pragma unroll
       for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
     }
     double v[3] = {P.vx[i], P.vy[i], P.vz[i]};
-    const double dtv = dt * c_k.dt_fac[sp];
-    boris_push(v, F, sp, isnew, dtv);
+    const double dtv = dt * kc.dt_fac[sp];
+    boris_push(kc, v, F, sp, isnew, dtv);
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + v[c] * dtv;
     P.vx[i] = v[0]; P.vy[i] = v[1]; P.vz[i] = v[2];
   } else {
     float F[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) F[c] = (float)c_k.ext[c];
+    for (int c = 0; c < 6; ++c) F[c] = (float)kc.ext[c];
     if (charged) {
       float Eo[3];
       const float xf[3] = {(float)xi[0], (float)xi[1], (float)xi[2]};
-      eval_field_f<N>(E32 + (size_t)e * nd * 3, xf, Eo);
+      eval_field_f<N>(kc, E32 + (size_t)e * nd * 3, xf, Eo);
 #pragma unroll
       for (int c = 0; c < 3; ++c) F[c] += Eo[c];
     }
     float v[3] = {P.vxf[i], P.vyf[i], P.vzf[i]};
-    const double dtv = dt * c_k.dt_fac[sp];
-    boris_push_f(v, F, sp, isnew, (float)dtv);
+    const double dtv = dt * kc.dt_fac[sp];
+    boris_push_f(kc, v, F, sp, isnew, (float)dtv);
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)v[c] * dtv;
     P.vxf[i] = v[0]; P.vyf[i] = v[1]; P.vzf[i] = v[2];
@@ -1465,7 +1474,7 @@ __global__ void __launch_bounds__(256) k_reorder(DevParticles P, DevParticles Q,
   perm_out[j] = perm_in[i];
 }
 
-__global__ void __launch_bounds__(256) k_map_particles(DevMesh M, DevParticles P) {
+__global__ void __launch_bounds__(256) k_map_particles(const __grid_constant__ DevMesh M, DevParticles P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   if (!(P.flags[i] & kInside)) return;
@@ -1480,6 +1489,42 @@ __global__ void k_count_inside(DevParticles P, int* out) {
   int v = (i < P.n && (P.flags[i] & kInside)) ? 1 : 0;
   v = __reduce_add_sync(kFull, v);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
+}
+
+// VerifyDepositedCharge (pic_analyze.f90:72-91; the change of basis to NAnalyze is left out: for Gauss nodes the
+// N+1-point rule already integrates PartSource(4)/sJ, a product of two degree-N interpolants, exactly).  One warp
+// per element sums w * PartSource(4) over its DOFs; one block then adds the element sums in index order, so the
+// result does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_charge_elem(const double* __restrict__ PS, const double* __restrict__ w, int ne,
+                                                     int nd, double* __restrict__ elem_sum) {
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (e >= ne) return;
+  double s = 0.0;
+  for (int r = lane; r < nd; r += 32) s = s + __ldg(w + (size_t)e * nd + r) * __ldg(PS + ((size_t)e * nd + r) * 4 + 3);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = s + __shfl_down_sync(kFull, s, o);
+  if (lane == 0) elem_sum[e] = s;
+}
+
+__global__ void __launch_bounds__(1024) k_sum_ordered(const double* __restrict__ a, int n, double* __restrict__ out) {
+  __shared__ double part[1024];
+  const int t = threadIdx.x;
+  const int per = (n + 1023) / 1024, b = t * per, end = min(n, b + per);
+  double s = 0.0;
+  for (int i = b; i < end; ++i) s = s + a[i];
+  part[t] = s;
+  __syncthreads();
+  for (int h = 512; h > 0; h >>= 1) {
+    if (t < h) part[t] = part[t] + part[t + h];
+    __syncthreads();
+  }
+  if (t == 0) *out = part[0];
+}
+
+__global__ void k_count_species(DevParticles P, int* __restrict__ counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n || !(P.flags[i] & kInside)) return;
+  atomicAdd(counts + P.species[i], 1);
 }
 
 // =============================================================================================
@@ -1499,12 +1544,13 @@ static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 // Mixed variant of node -> DOF: the node sums stay FP64; NodeSource / NodeVolume and the trilinear node ->
 // DOF weights (deposition weights) in FP32, one kernel; PartSource written in FP64.
 template <int N>
-__global__ void __launch_bounds__(256) k_node_to_dof_f(DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
+__global__ void __launch_bounds__(256) k_node_to_dof_f(const __grid_constant__ DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
+  const Consts& kc = M.k;
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.ne * nd) return;
   const int e = t / nd, r = t - e * nd;
-  const float a1 = (float)c_k.fac_gp[r % n1], a2 = (float)c_k.fac_gp[(r / n1) % n1], a3 = (float)c_k.fac_gp[r / (n1 * n1)];
+  const float a1 = (float)kc.fac_gp[r % n1], a2 = (float)kc.fac_gp[(r / n1) % n1], a3 = (float)kc.fac_gp[r / (n1 * n1)];
   const float w[8] = {(1 - a1) * (1 - a2) * (1 - a3), a1 * (1 - a2) * (1 - a3), a1 * a2 * (1 - a3), (1 - a1) * a2 * (1 - a3),
                       (1 - a1) * (1 - a2) * a3,       a1 * (1 - a2) * a3,       a1 * a2 * a3,       (1 - a1) * a2 * a3};
   float out[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1562,8 +1608,8 @@ int launch_interpolate(const LaunchArgs& A, const DevParticles& P, bool refmap, 
 
 int launch_push(const LaunchArgs& A, const DevParticles& P, double dt) {
   if (P.n <= 0) return 0;
-  if (A.mixed) k_push<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt, A.st);
-  else k_push<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, dt, A.st);
+  if (A.mixed) k_push<true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, dt, A.st);
+  else k_push<false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, dt, A.st);
   return 1;
 }
 
@@ -1597,8 +1643,8 @@ int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBu
 int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K) {
   int launches = launch_sort_offsets(A, P, B);
   if (P.n > 0) {
-    if (A.mixed) k_sf_pack<true><<<nblk(P.n, 256), 256, 0, A.s>>>(P, B.cursor, L.dof_center, K);
-    else k_sf_pack<false><<<nblk(P.n, 256), 256, 0, A.s>>>(P, B.cursor, L.dof_center, K);
+    if (A.mixed) k_sf_pack<true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, B.cursor, L.dof_center, K);
+    else k_sf_pack<false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, B.cursor, L.dof_center, K);
     launches++;
   }
   return launches;
@@ -1711,7 +1757,20 @@ int launch_map_particles(const LaunchArgs& A, const DevParticles& P) {
   return 1;
 }
 
-cudaError_t upload_consts(const Consts& k) { return cudaMemcpyToSymbol(c_k, &k, sizeof(Consts)); }
+
+int launch_charge_integral(const LaunchArgs& A, const double* PS, const double* w, double* elem_sum, double* out) {
+  const int ne = A.M.ne;
+  k_charge_elem<<<nblk(ne * 32, 256), 256, 0, A.s>>>(PS, w, ne, A.nd, elem_sum);
+  k_sum_ordered<<<1, 1024, 0, A.s>>>(elem_sum, ne, out);
+  return 2;
+}
+
+int launch_count_species(const LaunchArgs& A, const DevParticles& P, int* counts) {
+  cudaMemsetAsync(counts, 0, sizeof(int) * 8, A.s);
+  if (P.n <= 0) return 0;
+  k_count_species<<<nblk(P.n, 256), 256, 0, A.s>>>(P, counts);
+  return 1;
+}
 
 int launch_count_inside(const LaunchArgs& A, const DevParticles& P, int* out) {
   cudaMemsetAsync(out, 0, sizeof(int), A.s);

@@ -82,6 +82,8 @@ int launch_reorder(const LaunchArgs& A, DevParticles& P, DevParticles& Q, int* p
                    const SortBuffers& B);
 int launch_map_particles(const LaunchArgs& A, const DevParticles& P);
 int launch_count_inside(const LaunchArgs& A, const DevParticles& P, int* out);
-cudaError_t upload_consts(const Consts& k);
+// VerifyDepositedCharge: sum over elements (in index order) of sum_DOF w * PartSource(4); inside particles per species
+int launch_charge_integral(const LaunchArgs& A, const double* PS, const double* w, double* elem_sum, double* out);
+int launch_count_species(const LaunchArgs& A, const DevParticles& P, int* counts);
 
 }  // namespace pic

@@ -15,7 +15,10 @@
 //   * calls that overlap on the GPU (different streams, or different host threads) race on the
 //     array: order them on one stream or serialise them;
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current; make that first call before any stream capture.
+//     that device current; make that first call before any stream capture;
+//   * particles whose ParticleInside flag is 0 (optional mask) are skipped; element or species ids out
+//     of range skip the particle and set PIC_STATUS_BAD_ELEMENT, which pic_get_status reports (the
+//     context's stream waits for the call).
 #include "pic_ctx.h"
 
 #include <mutex>
@@ -51,22 +54,26 @@ int scratch_for_current_device(double** out) {
   return PIC_OK;
 }
 
-// Same corner scatter as the context's FP64 CVWM kernel, reading the caller's PartState(1:6,n)
-// and 1-based element / species ids straight from device memory.
-__global__ void __launch_bounds__(256) k_noalloc_cvwm(DevMesh M, const double* __restrict__ ps,
+// Same corner scatter as the context's FP64 CVWM kernel, reading the caller's PartState(1:6,n),
+// 1-based element / species ids and (optionally) PDM%ParticleInside straight from device memory.
+// Particles with ParticleInside = .FALSE. are skipped before their element is read, as the reference
+// skips them (pic_depo_method.f90:472): a removed particle keeps a stale element id.
+__global__ void __launch_bounds__(256) k_noalloc_cvwm(const __grid_constant__ DevMesh M, const double* __restrict__ ps,
                                                       const int32_t* __restrict__ elem1,
-                                                      const int32_t* __restrict__ spec1, int n,
+                                                      const int32_t* __restrict__ spec1,
+                                                      const uint8_t* __restrict__ inside, int n,
                                                       double* __restrict__ NS, DevStatus* st) {
+  const Consts& kc = M.k;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool valid = i < n;
+  bool valid = i < n && (inside == nullptr || inside[i] != 0);
   int e = valid ? elem1[i] - 1 : 0;
   int sp = valid ? spec1[i] - 1 : 0;
-  if (valid && (e < 0 || e >= M.ne || sp < 0 || sp >= c_k.n_species)) {
+  if (valid && (e < 0 || e >= M.ne || sp < 0 || sp >= kc.n_species)) {
     flag_status(st, 0x10u);            // PIC_STATUS_BAD_ELEMENT: skipped, nothing read out of range
     valid = false;
   }
   if (!valid) { e = 0; sp = 0; }
-  const bool charged = valid && (c_k.q[sp] != 0.0);
+  const bool charged = valid && (kc.q[sp] != 0.0);
   double contrib[32];
   if (charged) {
     const double* s = ps + (size_t)i * 6;
@@ -74,7 +81,7 @@ __global__ void __launch_bounds__(256) k_noalloc_cvwm(DevMesh M, const double* _
     double xi[3];
     const bool suc = position_in_ref_elem(M, e, x, xi);
     if (!suc) flag_status(st, 0x02u);
-    const double ch = c_k.qm[sp];
+    const double ch = kc.qm[sp];
     const double TS[4] = {s[3] * ch, s[4] * ch, s[5] * ch, ch};
     cvwm_contrib(M, e, suc, xi, x, TS, contrib);
   }
@@ -84,7 +91,8 @@ __global__ void __launch_bounds__(256) k_noalloc_cvwm(DevMesh M, const double* _
 }  // namespace
 
 extern "C" int pic_deposit_cvwm_noalloc(pic_ctx_t* ctx, const double* d_part_state, const int32_t* d_elem,
-                                        const int32_t* d_species, int32_t n, double* d_part_source, void* stream) {
+                                        const int32_t* d_species, const uint8_t* d_inside, int32_t n,
+                                        double* d_part_source, void* stream) {
   if (!ctx) return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "null context");
   if (ctx->cfg.deposition != PIC_DEPO_CVWM)
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the allocation-free deposition is cell_volweight_mean only");
@@ -99,11 +107,10 @@ extern "C" int pic_deposit_cvwm_noalloc(pic_ctx_t* ctx, const double* d_part_sta
   int rc = scratch_for_current_device(&NS);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemcpyToSymbolAsync(c_k, &ctx->k, sizeof(Consts), 0, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(NS, 0, sizeof(double) * 4 * (size_t)ctx->n_canon, s);
+  cudaError_t e = cudaMemsetAsync(NS, 0, sizeof(double) * 4 * (size_t)ctx->n_canon, s);
   if (e != cudaSuccess) return pic_internal::set_error(PIC_ERR_CUDA, std::string("set-up: ") + cudaGetErrorString(e));
   if (n > 0)
-    k_noalloc_cvwm<<<(n + 255) / 256, 256, 0, s>>>(ctx->M, d_part_state, d_elem, d_species, n, NS, ctx->st);
+    k_noalloc_cvwm<<<(n + 255) / 256, 256, 0, s>>>(ctx->M, d_part_state, d_elem, d_species, d_inside, n, NS, ctx->st);
   const int tot = ctx->M.ne * ctx->nd;
   switch (ctx->N) {
     case 1: k_node_to_dof<1><<<(tot + 255) / 256, 256, 0, s>>>(ctx->M, NS, d_part_source); break;
@@ -114,5 +121,18 @@ extern "C" int pic_deposit_cvwm_noalloc(pic_ctx_t* ctx, const double* d_part_sta
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return pic_internal::set_error(PIC_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  // The kernels above set status bits (PIC_STATUS_BAD_ELEMENT, _NEWTON_FAILED) in the context's status word
+  // from the caller's stream.  pic_get_status and pic_reset_status work on the context's own stream, so that
+  // stream waits for this call (an event, no allocation): a later pic_get_status sees this call's bits.
+  // While the caller's stream is being captured the wait is not added (it would pull the context's stream
+  // into the capture); the caller then synchronises its stream before reading the status.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+    e = cudaEventRecord(ctx->noalloc_done, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->noalloc_done, 0);
+    if (e != cudaSuccess) return pic_internal::set_error(PIC_ERR_CUDA, std::string("status ordering: ") + cudaGetErrorString(e));
+  } else {
+    (void)cudaGetLastError();
+  }
   return PIC_OK;
 }

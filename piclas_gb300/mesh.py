@@ -577,18 +577,66 @@ def elem_to_elem(mesh: BoxMesh) -> list[list[int]]:
     return out
 
 
-def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothing: bool = False) -> np.ndarray:
-    """SFElemr2_Shared(1,:) of InitShapeFunctionAdaptive (pic_depo.f90:727-815) for the 3D kernel: the shortest
-    distance from the element's corners to the corners of its node neighbours that it does not share (else
-    the mid point to its corners), averaged with the bounding-box length BoxVolume^(1/3) when that is shorter
-    (always with ``smoothing``, PIC-shapefunction-adaptive-smoothing), times SFDepoScaling/(N+1) with
-    SFDepoScaling = (3 DOF/(4 pi))^(1/3), DOF = PIC-shapefunction-adaptive-DOF (default (4/3) pi 2^3)."""
+def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothing: bool = False, dim: int = 3,
+                       direction: int = 1) -> np.ndarray:
+    """SFElemr2_Shared(1,:) of InitShapeFunctionAdaptive (pic_depo.f90:680-815): the shortest distance (SFNorm)
+    from the element's corners to the corners of its node neighbours that it does not share and that do not
+    coincide with them in the kernel's projection (SFMeasureDistance, pic_depo.f90:1080-1109; else the mid
+    point to its corners), averaged with the characteristic length when that is shorter (always with
+    ``smoothing``, PIC-shapefunction-adaptive-smoothing), times SFDepoScaling/(N+1).  ``dim`` and ``direction``
+    are PIC-shapefunction-dimension and -direction: SFNorm is |v(dir)| in 1D, the norm in the plane normal to
+    dir in 2D (components dim_sf_dir1, dim_sf_dir2 of InitShapeFunctionDimensionalty), the 3D norm otherwise;
+    the characteristic length is BoxVolume/dimFactorSF (1D), sqrt(BoxVolume/dimFactorSF) (2D) or
+    BoxVolume^(1/3) (3D); SFDepoScaling = DOF/2, sqrt(DOF/pi), (3 DOF/(4 pi))^(1/3) with DOF =
+    PIC-shapefunction-adaptive-DOF (defaults 2*2, pi*2^2, (4/3) pi 2^3; at most 2(N+1), pi(N+1)^2,
+    (4/3) pi (N+1)^3)."""
+    N1 = mesh.N + 1.0
+    if dim == 1:
+        default, dof_max, name = 2.0 * 2.0, 2.0 * N1, "2*(N+1)"
+    elif dim == 2:
+        default, dof_max, name = math.pi * 2.0 ** 2, math.pi * N1 ** 2, "PI*(N+1)**2"
+    elif dim == 3:
+        default, dof_max, name = (4.0 / 3.0) * math.pi * 2.0 ** 3, (4.0 / 3.0) * math.pi * N1 ** 3, "(4/3)*PI*(N+1)**3"
+    else:
+        raise ValueError("dim must be 1, 2 or 3")
     if adaptive_dof is None:
-        adaptive_dof = (4.0 / 3.0) * math.pi * (1.0 + 1.0) ** 3
-    dof_max = (4.0 / 3.0) * math.pi * (mesh.N + 1.0) ** 3
+        adaptive_dof = default
     if adaptive_dof > dof_max:
-        raise ValueError(f"PIC-shapefunction-adaptive-DOF > (4/3)*PI*(N+1)**3 = {dof_max} is not allowed")
-    scaling = (3.0 * adaptive_dof / (4.0 * math.pi)) ** (1.0 / 3.0)
+        raise ValueError(f"PIC-shapefunction-adaptive-DOF > {name} = {dof_max} is not allowed")
+    d0 = direction - 1
+    d1 = 0 if direction == 2 else 1                    # dim_sf_dir1 = MERGE(1,2,dim_sf_dir.EQ.2)
+    d2 = 0 if direction == 3 else 2                    # dim_sf_dir2 = MERGE(1,3,dim_sf_dir.EQ.3)
+    if dim == 1:
+        scaling = adaptive_dof / 2.0
+    elif dim == 2:
+        scaling = math.sqrt(adaptive_dof / math.pi)
+    else:
+        scaling = (3.0 * adaptive_dof / (4.0 * math.pi)) ** (1.0 / 3.0)
+    ext = mesh.hi - mesh.lo
+    if dim == 1:
+        dim_factor = float((ext[1] * ext[2]) if d0 == 0 else (ext[0] * ext[2]) if d0 == 1 else (ext[0] * ext[1]))
+    elif dim == 2:
+        dim_factor = float(ext[d0])
+    else:
+        dim_factor = 1.0
+
+    def sf_norm(v):
+        if dim == 1:
+            return abs(v[d0])
+        if dim == 2:
+            return math.sqrt(v[d1] ** 2 + v[d2] ** 2)
+        return math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+
+    def almost_equal_rel(a, b, tol=1e-6):
+        return abs(a - b) <= max(abs(a), abs(b)) * tol
+
+    def measure(v1, v2):
+        if dim == 1:
+            return not almost_equal_rel(v1[d0], v2[d0])
+        if dim == 2:
+            return not (almost_equal_rel(v1[d1], v2[d1]) and almost_equal_rel(v1[d2], v2[d2]))
+        return True
+
     nb = elem_to_elem(mesh)
     ni = mesh.node_info
     corners = mesh.node_coords.reshape(mesh.n_elems, 8, 3)[:, CGNS_TO_TENSOR, :]     # CGNS corner order
@@ -603,17 +651,22 @@ def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothi
                 done = True
                 v2 = corners[t, jn]
                 for i in range(8):
-                    d = corners[e, i] - v2
-                    rt = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
-                    if rt < r[e]:
-                        r[e] = rt
+                    if measure(corners[e, i], v2):
+                        rt = sf_norm(corners[e, i] - v2)
+                        if rt < r[e]:
+                            r[e] = rt
         if not done:
             mid = corners[e].sum(axis=0) / 8.0
             for i in range(8):
-                d = mid - corners[e, i]
-                r[e] = min(r[e], math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]))
+                r[e] = min(r[e], sf_norm(mid - corners[e, i]))
         lo, hi = corners[e].min(axis=0), corners[e].max(axis=0)
-        char_len = ((hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2])) ** (1.0 / 3.0)
+        vol = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2])
+        if dim == 1:
+            char_len = vol / dim_factor
+        elif dim == 2:
+            char_len = math.sqrt(vol / dim_factor)
+        else:
+            char_len = vol ** (1.0 / 3.0)
         if char_len < r[e] or smoothing:
             r[e] = (r[e] + char_len) / 2.0
         r[e] = r[e] * scaling / (mesh.N + 1.0)

@@ -107,3 +107,45 @@ def test_torch_autograd_wrapper(case):
     # a fresh upload regroups particles, so atomic summation order (and the last bits) may differ
     assert np.linalg.norm(v0.grad.numpy() - gv) <= 1e-9 * np.linalg.norm(gv)
     assert abs(b.grad.item() - gb * w.info["Bz"]) <= 1e-9 * abs(gb * w.info["Bz"])
+
+
+def test_adjoint_forward_matches_oracle(gpu_lib, oracle_lib):
+    """The adjoint's forward pass is the reference loop: its loss equals the loss of the oracle's nsteps of
+    interpolation + Boris push + TriaTracking (B scaled by b_scale, IsNewPart off) followed by
+    cell_volweight_mean deposition of the final state, and of the GPU's own pic_step + pic_deposit on the
+    same inputs.  FP64 within 1e-12; FP32 within 2e-6 relative.  The FP32 bound is the loss's
+    sensitivity: dL/L ~ 2 max|d rho^| / |rho^ - target| with |rho^ - target| ~ 0.2 here (particle noise),
+    so 2e-6 on the loss holds rho^ to about 2e-7."""
+    import os
+    from piclas_gb300 import capi
+    w = workloads.differentiable_loop(n_cells=8, N=2, n_particles=20000, nsteps=20, seed=3)
+    b_scale = 1.3
+    tgt, rs = w.info["rho_target"], w.info["rho_scale"]
+    loop = ParticleLoop(w.config(), w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species, is_new=np.zeros(w.n, np.uint8))
+    L64 = loop.adjoint(w.nsteps, w.dt, tgt, rs, b_scale=b_scale, checkpoint_every=5, gradients=False)
+    L32 = loop.adjoint(w.nsteps, w.dt, tgt, rs, b_scale=b_scale, checkpoint_every=5, precision=PIC_PREC_MIXED,
+                       gradients=False)
+    loop.close()
+    ext = list(w.external_field)
+    ext[3:] = [b * b_scale for b in ext[3:]]
+    w2 = workloads.Workload(**{**w.__dict__, "external_field": tuple(ext)})
+    cfg, ms, nt = w2.config(), capi.MeshStruct(w2.mesh), os.cpu_count() or 1
+    st = oracle_lib.OracleState(w2.part_state, w2.elem, w2.part_species, is_new=np.zeros(w2.n, np.uint8))
+    oracle_lib.step(cfg, ms, w2.e_dof, st, w2.dt, w2.nsteps, None, nt)
+    PS = np.zeros((w2.mesh.n_elems, w2.mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS, nt)
+    Lo = float(np.sum((PS[..., 3] / rs - tgt) ** 2))
+    assert st.counters.n_lost == 0
+    assert abs(L64 - Lo) <= 1e-12 * Lo, (L64, Lo)
+    assert abs(L32 - Lo) <= 2e-6 * Lo, (L32, Lo)
+    # the same through the drop-in loop
+    lp = ParticleLoop(w2.config(), w2.mesh)
+    lp.set_field(w2.e_dof)
+    lp.upload_particles(w2.part_state, w2.elem, w2.part_species, is_new=np.zeros(w2.n, np.uint8))
+    lp.time_step(w2.dt, w2.nsteps)
+    PSg = lp.deposition()
+    lp.close()
+    Lg = float(np.sum((PSg[..., 3] / rs - tgt) ** 2))
+    assert abs(Lg - Lo) <= 1e-12 * Lo, (Lg, Lo)

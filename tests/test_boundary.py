@@ -67,6 +67,18 @@ def test_bad_options_rejected(lib):
     assert b"radius" in lib.pic_last_error()
 
 
+def test_time_step_factor_above_one_rejected(lib):
+    """The reference stops with 'Species-specific time step only allows factors below 1!'
+    (particle_emission_init.f90:218-219); pic_create rejects such a factor before any device work."""
+    from piclas_gb300.mesh import build_box_mesh
+    ms = capi.MeshStruct(build_box_mesh(2, 2, 2, 1))
+    h = C.c_void_p()
+    for f in (1.0000001, 3.0, float("inf"), float("nan"), -0.5):
+        cfg = capi.make_config(1, 1, 1, 0, [(-1.0, 1.0, 1.0), (1.0, 1836.0, 1.0)], 10, time_step_factor=(1.0, f))
+        assert lib.pic_create(C.byref(cfg), ms.ptr, C.byref(h)) == 1, f
+        assert b"time_step_factor" in lib.pic_last_error()
+
+
 def test_struct_sizes_match_c():
     # pic_config_t: 6 ints + 3*8 + 6 doubles + 2 doubles + 5 ints + 4 bytes tail padding (8-byte alignment)
     assert C.sizeof(capi.PicConfig) == 6 * 4 + 3 * 8 * 8 + 6 * 8 + 2 * 8 + 5 * 4 + 4 + 8 * 8

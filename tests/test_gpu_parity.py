@@ -44,6 +44,29 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
+def _rho_species_scale(oracle, w, st, nthreads=1):
+    """max over DOFs of sum_s |rho_s|: the oracle's charge density of each species deposited on its own from
+    the final oracle state.  Electrons and ions cancel in the summed rho, so a mixed-precision error is
+    measured against the magnitude the species deposit, not against their small difference."""
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    tot = np.zeros((w.mesh.n_elems, w.mesh.n_dof))
+    for s in np.unique(st.species):
+        k = (st.species == s) & (st.inside == 1)
+        if not k.any():
+            continue
+        sub = oracle.OracleState(st.part_state[k], st.elem[k], st.species[k], is_new=np.zeros(int(k.sum()), np.uint8),
+                                 part_pos_ref=st.part_pos_ref[k])
+        PSs = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+        oracle.deposit(cfg, ms, sub, PSs, nthreads)
+        tot += np.abs(PSs[..., 3])
+    return float(tot.max())
+
+
+def _rho_err_species(oracle, w, st, ps_gpu, ps_oracle, nthreads=1):
+    """Mixed charge-density error: max |rho_gpu - rho_oracle| / max sum_s |rho_s| (bound: 1e-6)."""
+    return float(np.max(np.abs(ps_gpu[..., 3] - ps_oracle[..., 3])) / _rho_species_scale(oracle, w, st, nthreads))
+
+
 def test_plasma_wave_fp64_bitexact(gpu_lib, oracle_lib):
     w = workloads.plasma_wave(n_cells=8, N=3, n_particles=20000, nsteps=10, seed=0, T_eV=200.0)
     g = _run_gpu(w, 10)
@@ -116,7 +139,42 @@ def test_cvwm_kat_on_gpu(gpu_lib):
     PS = loop.deposition()
     q = oracle.integrate_charge(capi.MeshStruct(mesh), mesh.N, PS)
     assert abs(q - k["total_charge"]) <= k["tolerance_abs"]
+    # the same check on the device (VerifyDepositedCharge through the C-ABI)
+    num, ana = loop.verify_deposited_charge()
+    assert abs(num - k["total_charge"]) <= k["tolerance_abs"]
+    assert abs(ana - k["total_charge"]) <= k["tolerance_abs"]
     loop.close()
+
+
+@pytest.mark.parametrize("kind", ["cvwm", "sf_1d_line"])
+def test_verify_deposited_charge(gpu_lib, oracle_lib, kind):
+    """pic_verify_deposited_charge (VerifyDepositedCharge, pic_analyze.f90:41-133) after pic_step: the numerical
+    charge equals the oracle's integral of the same PartSource to 1e-12, the analytical one the sum of
+    q * MPF over the particles inside (times dimFactorSF for a 1D kernel with its charge on a line)."""
+    if kind == "cvwm":
+        w = workloads.plasma_wave(n_cells=4, N=3, n_particles=8000, seed=61, T_eV=100.0)
+        factor = 1.0
+    else:
+        mesh = build_box_mesh(6, 4, 4, 2, lo=(0.0, 0.0, 0.0), hi=(1.0, 0.5, 0.8))
+        w = workloads.plasma_wave(mesh=mesh, n_particles=6000, seed=62, T_eV=100.0)
+        w.deposition, w.sf_radius, w.sf_dim, w.sf_dir, w.sf_depo3d = capi.PIC_DEPO_SHAPE_FUNCTION, 0.25, 1, 1, False
+        factor = 0.5 * 0.8                                   # dimFactorSF: the cross-section of the 1D kernel
+    loop = ParticleLoop(w.config(), w.mesh)
+    with pytest.raises(PicError):
+        loop.verify_deposited_charge()                       # no particles / deposition yet
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    loop.time_step(w.dt, 2, PS)
+    num, ana = loop.verify_deposited_charge()
+    n_in = loop.status()["n_inside"]
+    loop.close()
+    qo = oracle_lib.integrate_charge(capi.MeshStruct(w.mesh), w.mesh.N, PS)
+    assert abs(num - qo) <= 1e-12 * abs(qo)
+    q, _, mpf = w.species[0]
+    assert abs(ana - n_in * q * mpf * factor) <= 1e-12 * abs(ana)
+    if kind == "cvwm":
+        assert abs(num - ana) <= 1e-10 * abs(ana)           # CVWM conserves charge
 
 
 def test_mixed_precision_rho_error(gpu_lib, oracle_lib):
@@ -134,8 +192,7 @@ def test_mixed_sf_rho_error(gpu_lib, oracle_lib):
     w = workloads.curved_two_species(n_cells=6, n_per_species=3000, seed=5, nsteps=2)
     g = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
     st, PS = _run_oracle(oracle_lib, w, 2)
-    # electrons and ions cancel; compare each output against the species-summed magnitude
-    assert _rel(g["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert _rho_err_species(oracle_lib, w, st, g["PS"], PS) <= 1e-6
     assert np.array_equal(g["elem"], st.elem)
 
 
@@ -293,7 +350,7 @@ def test_sf_gather_low_order(gpu_lib, oracle_lib, N):
     assert _rel(g["PS"], PS) <= 1e-12
     gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
     assert np.array_equal(gm["elem"], st.elem)
-    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert _rho_err_species(oracle_lib, w, st, gm["PS"], PS) <= 1e-6
 
 
 # ---- particle boundaries: open and reflective walls --------------------------------------------
@@ -391,7 +448,7 @@ def test_shape_function_cc_against_oracle(gpu_lib, oracle_lib):
     assert np.array_equal(g["elem"], st.elem)
     assert _rel(g["PS"], PS) <= 1e-12
     gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
-    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert _rho_err_species(oracle_lib, w, st, gm["PS"], PS) <= 1e-6
     assert g["status"]["error_word"] == 0
 
 
@@ -470,14 +527,15 @@ def _adaptive_workload(n_cells=6, n_per_species=2000, seed=17):
 
 
 def test_shape_function_adaptive_against_oracle(gpu_lib, oracle_lib):
-    """Per-element radii between 1.2 h and 1.8 h: FP64 against the oracle, mixed within 1e-4."""
+    """Per-element radii between 1.2 h and 1.8 h: FP64 against the oracle, mixed rho within 1e-6 of the
+    species-summed magnitude."""
     w = _adaptive_workload()
     g = _run_gpu(w, 2)
     st, PS = _run_oracle(oracle_lib, w, 2)
     assert np.array_equal(g["elem"], st.elem)
     assert _rel(g["PS"], PS) <= 1e-12
     gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
-    assert _rel(gm["PS"][..., 3], PS[..., 3]) <= 1e-4
+    assert _rho_err_species(oracle_lib, w, st, gm["PS"], PS) <= 1e-6
     assert g["status"]["error_word"] == 0
 
 
@@ -525,7 +583,7 @@ def test_plasma_wave_full_size_100_steps_bitexact(gpu_lib, oracle_lib):
 
 def test_curved_32cube_mesh_parity(gpu_lib, oracle_lib):
     """The benchmark's 32^3 curved mesh (RefTracking + shape function, B_z = 0.1 T) with 400k particles,
-    2 steps: element ids exact, state and PartSource as in the small-mesh test."""
+    2 steps: element ids exact, state and PartSource as in the small-mesh test; mixed rho within 1e-6."""
     import os
     w = workloads.curved_two_species(n_per_species=200_000, seed=9, nsteps=2)
     g = _run_gpu(w, 2)
@@ -538,6 +596,11 @@ def test_curved_32cube_mesh_parity(gpu_lib, oracle_lib):
     assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
     assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
     assert _rel(g["PS"], PS) <= 1e-12
+    # the mixed variant on the same mesh and particles: element ids exact, rho within 1e-6 of the
+    # species-summed magnitude
+    gm = _run_gpu(w, 2, precision=capi.PIC_PREC_MIXED)
+    assert np.array_equal(gm["elem"], st.elem)
+    assert _rho_err_species(oracle_lib, w, st, gm["PS"], PS, os.cpu_count() or 1) <= 1e-6
 
 
 
@@ -588,7 +651,8 @@ def test_non_finite_field_removes_particles(gpu_lib, prec, fused):
 
 def test_wrong_start_element_matches_oracle(gpu_lib, oracle_lib):
     """Particles uploaded with an element that does not contain them: TriaTracking walks (or loses) them
-    exactly as the oracle does."""
+    exactly as the oracle does, and the deposition's inverse-distance fallback for failed Newton calls gives
+    the oracle's PartSource."""
     w = workloads.plasma_wave(n_cells=4, N=2, n_particles=3000, seed=47)
     wrong = w.elem.copy()
     wrong[:40] = (wrong[:40] % w.mesh.n_elems) + 1
@@ -599,6 +663,17 @@ def test_wrong_start_element_matches_oracle(gpu_lib, oracle_lib):
     assert np.array_equal(g["elem"], st.elem)
     assert g["status"]["n_lost"] == st.counters.n_lost
     assert np.array_equal(g["part_state"], st.part_state)
+    assert _rel(g["PS"], PS) <= 1e-12
+    # one step: its Deposition (before tracking) runs the Newton of the wrongly labelled particles in the
+    # wrong element; where it fails, cell_volweight_mean falls back to inverse-distance weights of the
+    # element's corner nodes (pic_depo_method.f90:512-539) and the interpolation to GetEMFieldDW
+    # (pic_interpolation_tools.f90:458-527) -- the same PartSource and state as the oracle
+    g1 = _run_gpu(w2, 1)
+    st1, PS1 = _run_oracle(oracle_lib, w2, 1)
+    assert st1.counters.n_newton_failed > 0
+    assert g1["status"]["n_newton_failed"] > 0
+    assert _rel(g1["PS"], PS1) <= 1e-12
+    assert np.array_equal(g1["elem"], st1.elem) and np.array_equal(g1["part_state"], st1.part_state)
 
 
 # ---- walls with RefTracking (ParticleBCTracking over planar wall sides) ------------------------------
@@ -806,7 +881,7 @@ def test_species_time_step_factor(gpu_lib, oracle_lib, kind):
         w.part_species = np.where(np.arange(w.n) % 3 == 0, 2, 1).astype(np.int32)
     else:
         w = workloads.curved_two_species(n_cells=4, n_per_species=3000, seed=43, nsteps=4)
-    w.time_step_factor = (1.0, 3.0)
+    w.time_step_factor = (1.0, 0.25)     # the reference allows factors in (0, 1] only
     g = _run_gpu(w, 6)
     st, PS = _run_oracle(oracle_lib, w, 6)
     assert np.array_equal(g["elem"], st.elem)
@@ -829,3 +904,135 @@ def test_species_time_step_factor(gpu_lib, oracle_lib, kind):
         with pytest.raises(PicError):
             loop.adjoint(2, w.dt, np.zeros((w.mesh.n_elems, w.mesh.n_dof)), 1.0)
         loop.close()
+
+
+# ---- several live contexts -----------------------------------------------------------------------------
+def test_two_contexts_interleaved(gpu_lib, oracle_lib):
+    """Two contexts with different meshes, species, external fields and methods (CVWM + TriaTracking on a
+    4^3 plasma wave; shape function + RefTracking with B_z on a 6^3 curved box) live at the same time, their
+    steps interleaved, one of them mixed: each matches its own oracle run (FP64 bit-exact / within 1e-12,
+    mixed rho within 1e-6).  Every launch carries its own context's constants, so neither sees the other's
+    charges, masses, periodic vectors, field or shape-function radius."""
+    wa = workloads.plasma_wave(n_cells=4, N=3, n_particles=5000, seed=51, T_eV=300.0)
+    wb = workloads.curved_two_species(n_cells=6, n_per_species=2500, seed=52, nsteps=4)
+    wc = workloads.curved_two_species(n_cells=6, n_per_species=2500, seed=53, nsteps=4)
+    loops = []
+    for w, prec in ((wa, capi.PIC_PREC_FP64), (wb, capi.PIC_PREC_FP64), (wc, capi.PIC_PREC_MIXED)):
+        lp = ParticleLoop(w.config(precision=prec), w.mesh)
+        lp.set_field(w.e_dof)
+        lp.upload_particles(w.part_state, w.elem, w.part_species)
+        loops.append(lp)
+    PSs = [np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4)) for w in (wa, wb, wc)]
+    for _ in range(4):
+        for lp, w, PS in zip(loops, (wa, wb, wc), PSs):
+            lp.time_step(w.dt, 1, PS)
+    outs = [lp.download_particles(with_ref=True) for lp in loops]
+    stats = [lp.status() for lp in loops]
+    for lp in loops:
+        lp.close()
+    st_a, PS_a = _run_oracle(oracle_lib, wa, 4)
+    st_b, PS_b = _run_oracle(oracle_lib, wb, 4)
+    st_c, PS_c = _run_oracle(oracle_lib, wc, 4)
+    assert np.array_equal(outs[0]["elem"], st_a.elem) and np.array_equal(outs[0]["part_state"], st_a.part_state)
+    assert _rel(PSs[0], PS_a) <= 1e-12
+    assert np.array_equal(outs[1]["elem"], st_b.elem)
+    assert _rel(outs[1]["part_state"], st_b.part_state) <= 1e-13
+    assert _rel(PSs[1], PS_b) <= 1e-12
+    assert np.array_equal(outs[2]["elem"], st_c.elem)
+    assert _rho_err_species(oracle_lib, wc, st_c, PSs[2], PS_c) <= 1e-6
+    assert all(s["error_word"] == 0 for s in stats)
+
+
+def test_mixed_gather_hits_in_the_kernel_shell(gpu_lib, oracle_lib):
+    """The mixed shape-function gather pre-tests candidates in packed FP16 (units of R, threshold 1.05) before
+    its exact FP32 test.  Particles are placed at 0.98 R ... 0.9999 R from a DOF, so every particle has
+    DOFs in the outer shell of its kernel, and kept more than 2 R apart, so each DOF sees at most one
+    particle: the set of DOFs that receive charge is then each particle's hit set.  That set must equal
+    the FP64 oracle's (DOFs within 1e-5 R of the kernel edge excluded: FP32 and FP64 may round them
+    differently, with a weight below 1e-9), and the values must agree to 1e-6 of their maximum."""
+    mesh = build_box_mesh(12, 12, 12, 3)
+    R = 1.5 * float(mesh.h[0])
+    xg = mesh.elem_xgp.reshape(-1, 3)
+    L = mesh.hi - mesh.lo
+    rng = np.random.default_rng(77)
+    n_shell = 0
+    for trial in range(3):
+        pts = []
+        for _ in range(4000):
+            g = xg[rng.integers(len(xg))]
+            u = rng.normal(size=3)
+            u /= np.linalg.norm(u)
+            x = g + R * rng.uniform(0.98, 0.9999) * u
+            x = mesh.lo + np.mod(x - mesh.lo, L)
+            if all(np.linalg.norm((x - p) - L * np.round((x - p) / L)) > 2.0 * R + 1e-9 for p in pts):
+                pts.append(x)
+        x = np.array(pts)
+        n = len(x)
+        assert n >= 25
+        w = workloads.plasma_wave(mesh=mesh, n_particles=n, seed=trial)
+        v = rng.normal(0.0, 1e5, size=(n, 3))
+        w.part_state = np.ascontiguousarray(np.concatenate([x, v], axis=1))
+        w.elem = workloads._elem_of_uniform(mesh, x)
+        w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION
+        w.sf_radius = R
+        loop = ParticleLoop(w.config(precision=capi.PIC_PREC_MIXED), mesh)
+        loop.upload_particles(w.part_state, w.elem, w.part_species)
+        PSg = loop.deposition()
+        loop.close()
+        st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species, is_new=np.zeros(n, np.uint8))
+        PSo = np.zeros_like(PSg)
+        oracle_lib.deposit(w.config(), capi.MeshStruct(mesh), st, PSo)
+        # exact distance of every DOF to its nearest particle (minimum image), in units of R
+        d = np.full(len(xg), np.inf)
+        for p in x:
+            dv = xg - p
+            dv -= L * np.round(dv / L)
+            d = np.minimum(d, np.linalg.norm(dv, axis=1) / R)
+        keep = np.abs(d - 1.0) > 1e-5
+        hit_g = (PSg[..., 3].reshape(-1) != 0.0)
+        hit_o = (PSo[..., 3].reshape(-1) != 0.0)
+        assert np.array_equal(hit_g[keep], hit_o[keep])
+        assert np.array_equal(hit_o[keep], d[keep] <= 1.0)
+        h = hit_o & keep
+        rg, ro = PSg[..., 3].reshape(-1)[h], PSo[..., 3].reshape(-1)[h]
+        assert np.max(np.abs(rg - ro)) <= 1e-6 * np.max(np.abs(ro))
+        n_shell += int(((d >= 0.98) & (d < 1.0) & keep).sum())
+    assert n_shell > 2000
+
+
+@pytest.mark.parametrize("case", ["1d_x-dir", "1d_x-dir-cc", "1d_x-dir-adaptive", "2d_z-dir", "2d_z-dir-cc",
+                                  "2d_z-dir-adaptive"])
+def test_sf_plasma_ball_kat_on_gpu(gpu_lib, oracle_lib, case):
+    """The reference's shape-function plasma-ball known answers on the GPU (Plasma_Ball_Shape-function-xDir:
+    1D x / 2D z kernels of shape_function, _cc and _adaptive on a 4 x 4 x 1 periodic box): the integrated
+    charge, from the oracle's integral of the GPU PartSource and from pic_verify_deposited_charge, within the
+    reference's tolerance (plain 5e-2 relative, charge-conserving 1e-9 C absolute); PartSource within 1e-12
+    of the oracle's; mixed within the plain tolerance and, charge-conserving, within 1e-5 relative."""
+    import json
+    import os
+    from test_oracle import sf_ball_charge_ok, sf_plasma_ball
+    kat = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")))
+    k = kat["sf_plasma_ball"]
+    mesh, cfg, ps, elem = sf_plasma_ball(kat, case)
+    ms = capi.MeshStruct(mesh)
+    spec = np.ones(len(elem), np.int32)
+    st = oracle_lib.OracleState(ps, elem, spec)
+    PSo = np.zeros((mesh.n_elems, mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PSo, os.cpu_count() or 1)
+    for prec in (capi.PIC_PREC_FP64, capi.PIC_PREC_MIXED):
+        cfg.precision = prec
+        loop = ParticleLoop(cfg, mesh)
+        loop.upload_particles(ps, elem, spec)
+        PS = loop.deposition()
+        num, ana = loop.verify_deposited_charge()
+        loop.close()
+        q = oracle_lib.integrate_charge(ms, mesh.N, PS)
+        assert abs(num - q) <= 1e-12 * abs(q)
+        assert abs(ana - len(elem) * k["charge_ic"] * k["mpf"]) <= 1e-12 * abs(ana)
+        if prec == capi.PIC_PREC_FP64:
+            assert sf_ball_charge_ok(k, case, q), (case, q)
+            assert _rel(PS, PSo) <= 1e-12
+        elif k["cases"][case]["tolerance_type"] == "relative":
+            assert sf_ball_charge_ok(k, case, q), (case, q)
+        else:
+            assert abs(q - k["cases"][case]["total_charge"]) <= 1e-5 * abs(q), (case, q)

@@ -8,7 +8,7 @@ import pytest
 
 from piclas_gb300 import capi, workloads
 from piclas_gb300.mesh import (barycentric_weights, build_box_mesh, cheby_gauss_lobatto_nodes, elem_map,
-                               lagrange_polys, legendre_gauss_nodes)
+                               lagrange_polys, legendre_gauss_nodes, sf_adaptive_radius)
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")
 
@@ -72,6 +72,55 @@ def test_cvwm_total_charge_kat(oracle_lib, kat):
     oracle_lib.deposit(cfg, ms, st, PS)
     q = oracle_lib.integrate_charge(ms, mesh.N, PS)
     assert abs(q - k["total_charge"]) <= k["tolerance_abs"], (q, k["total_charge"])
+
+
+SF_BALL_CASES = ["1d_x-dir", "1d_x-dir-cc", "1d_x-dir-adaptive", "2d_z-dir", "2d_z-dir-cc", "2d_z-dir-adaptive"]
+
+
+def sf_plasma_ball(kat, case, seed=0):
+    """Plasma_Ball_Shape-function-xDir: 100000 resting particles in a ball of radius 0.5 at the origin on the
+    4 x 4 x 1 periodic box [-5,5]^3, N = 3, deposited with the case's kernel (1D along x or 2D constant in z;
+    shape_function, _cc, or _adaptive with smoothing).  Returns (mesh, cfg, part_state, elem)."""
+    k = kat["sf_plasma_ball"]
+    c = k["cases"][case]
+    mesh = build_box_mesh(*k["n_elems"], k["N"], lo=tuple(k["box_lo"]), hi=tuple(k["box_hi"]))
+    rng = np.random.default_rng(seed)
+    n = k["n_particles"]
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    x = np.asarray(k["base_point"]) + d * (k["sphere_radius"] * rng.random(n) ** (1.0 / 3.0))[:, None]
+    ps = np.concatenate([x, np.zeros((n, 3))], axis=1)
+    elem = workloads._elem_of_uniform(mesh, x)
+    dep = {"shape_function": capi.PIC_DEPO_SHAPE_FUNCTION, "shape_function_cc": capi.PIC_DEPO_SHAPE_FUNCTION_CC,
+           "shape_function_adaptive": capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE}[c["deposition"]]
+    if dep == capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE:
+        mesh.sf_elem_radius = sf_adaptive_radius(mesh, smoothing=k["adaptive_smoothing"], dim=c["dimension"],
+                                                 direction=c["direction"])
+    cfg = capi.make_config(k["N"], capi.PIC_TRACK_REFMAPPING, dep, capi.PIC_PREC_FP64,
+                           [(k["charge_ic"], 1.0, k["mpf"]), (workloads.Q_ELECTRON, workloads.M_ELECTRON, k["mpf"])],
+                           n, sf_radius=k["sf_radius"], sf_alpha=k["sf_alpha"], sf_dim=c["dimension"],
+                           sf_dir=c["direction"], sf_depo3d=k["depo3d"])
+    return mesh, cfg, ps, elem
+
+
+def sf_ball_charge_ok(k, case, q):
+    c = k["cases"][case]
+    if c["tolerance_type"] == "relative":
+        return abs(q - c["total_charge"]) <= c["tolerance"] * abs(c["total_charge"])
+    return abs(q - c["total_charge"]) <= c["tolerance"]
+
+
+@pytest.mark.parametrize("case", SF_BALL_CASES)
+def test_sf_plasma_ball_total_charge_kat(oracle_lib, kat, case):
+    """The reference's shape-function plasma-ball known answers (1D x / 2D z kernels, plain within 5e-2
+    relative, charge-conserving and adaptive within 1e-9 C absolute of 320.435306 C)."""
+    mesh, cfg, ps, elem = sf_plasma_ball(kat, case)
+    ms = capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(ps, elem, np.ones(len(elem), np.int32))
+    PS = np.zeros((mesh.n_elems, mesh.n_dof, 4))
+    oracle_lib.deposit(cfg, ms, st, PS, os.cpu_count() or 1)
+    q = oracle_lib.integrate_charge(ms, mesh.N, PS)
+    assert sf_ball_charge_ok(kat["sf_plasma_ball"], case, q), (case, q)
 
 
 def test_cvwm_charge_conservation_periodic_twins(oracle_lib):
