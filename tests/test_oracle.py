@@ -684,3 +684,28 @@ def test_species_time_step_factor_free_streaming(oracle_lib):
     x = np.mod(x, 1.0)
     assert np.max(np.abs(np.mod(st.part_state[:, :3] - x + 0.5, 1.0) - 0.5)) < 1e-12
     assert st.inside.all() and np.array_equal(st.elem, workloads._elem_of_uniform(w.mesh, st.part_state[:, :3]))
+
+
+def test_timing_build_matches_checker(oracle_lib):
+    """The CPU baseline is timed with the oracle built like the reference's release build (-O3, FMA
+    contraction).  It computes the same loop: element ids identical and the state within rounding of the
+    checker build after 5 steps of the plasma wave and of the curved RefTracking/shape-function box."""
+    for w in (workloads.plasma_wave(n_cells=4, N=3, n_particles=4000, seed=71, T_eV=200.0),
+              workloads.curved_two_species(n_cells=4, n_per_species=2000, seed=72, nsteps=5)):
+        cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+        res = []
+        for timing in (False, True):
+            oracle_lib.set_timing_build(timing)
+            try:
+                st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+                if w.tracking == capi.PIC_TRACK_REFMAPPING:
+                    oracle_lib.map_particles(cfg, ms, st)
+                PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+                oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, 5, PS)
+                res.append((st, PS))
+            finally:
+                oracle_lib.set_timing_build(False)
+        (a, pa), (b, pb) = res
+        assert np.array_equal(a.elem, b.elem)
+        assert np.max(np.abs(a.part_state - b.part_state)) <= 1e-10 * np.max(np.abs(a.part_state))
+        assert np.max(np.abs(pa - pb)) <= 1e-10 * np.max(np.abs(pa))
