@@ -40,7 +40,7 @@
  *   pic_hdg_get_lambda / pic_hdg_set_lambda / pic_hdg_get_elem_mat
  *                          HDG_Surf_N(:)%lambda, HDG_Vol_N(e)%Ehat/InvDhat/Smat (src/hdg/hdg_vars.f90)
  *   pic_adjoint_run        no reference counterpart (differentiable loop, see its comment)
- *   pic_deposit_cvwm_noalloc, pic_profile*, pic_launch_count, pic_stream, pic_fp64_fma_rate
+ *   pic_deposit_cvwm_noalloc, pic_profile*, pic_launch_count, pic_stream, pic_fp64_fma_rate, pic_fp32_fma_rate
  *                          no reference counterpart (allocation-free entry point, instrumentation)
  *
  * Error convention: every int-returning call returns PIC_OK (0) or a positive
@@ -76,6 +76,8 @@ typedef enum pic_error_t {
 #define PIC_STATUS_NOT_FINITE      0x20u  /* NaN/Inf position or velocity                  */
 #define PIC_STATUS_CG_NOT_CONVERGED 0x40u /* HDG CG reached MaxIterCG (reference: warning)    */
 #define PIC_STATUS_CG_BREAKDOWN    0x80u  /* HDG CG: v.z = 0 or NaN residual (reference aborts) */
+#define PIC_STATUS_WAIT_TIMEOUT    0x100u /* a kernel's bounded wait on its own copies gave up (no reference
+                                             counterpart; the kernel's output is then incomplete)         */
 
 /* ---- option enums ------------------------------------------------------- */
 enum { PIC_TRACK_TRIA = 1, PIC_TRACK_REFMAPPING = 2 };     /* TrackingMethod           */
@@ -245,6 +247,8 @@ int pic_verify_deposited_charge(pic_ctx_t* ctx, double* charge_numerical, double
 /* Instrumentation (no reference counterpart): sustained FP64 fused multiply-add rate of this GPU in GFLOP/s,
  * from independent FMA chains on every SM (~0.1 s); the peak the FP64-bound kernels are compared against. */
 int pic_fp64_fma_rate(pic_ctx_t* ctx, double* gflops);
+/* The same for FP32 fused multiply-adds (fmaf chains): the peak of the mixed variant's FP32 work. */
+int pic_fp32_fma_rate(pic_ctx_t* ctx, double* gflops);
 
 /* Particle state in the reference's checkpoint layout (FillParticleData, src/io_hdf5/hdf5_output_particle.f90:1531):
  * the particles inside the domain grouped by element, in ascending caller index within an element

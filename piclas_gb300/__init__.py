@@ -38,7 +38,8 @@ EXPORTED_SYMBOLS = ["pic_version", "pic_last_error", "pic_create", "pic_destroy"
                     "pic_synchronize", "pic_launch_count", "pic_stream", "pic_profile", "pic_profile_read",
                     "pic_deposit_cvwm_noalloc", "pic_adjoint_run", "pic_get_part_data", "pic_set_part_data", "pic_fp64_fma_rate",
                     "pic_hdg_init", "pic_hdg_set_dirichlet", "pic_hdg_solve", "pic_hdg_get_lambda",
-                    "pic_hdg_get_elem_mat", "pic_hdg_set_lambda", "pic_verify_deposited_charge"]
+                    "pic_hdg_get_elem_mat", "pic_hdg_set_lambda", "pic_verify_deposited_charge",
+                    "pic_fp32_fma_rate"]
 
 
 class PicError(RuntimeError):
@@ -83,6 +84,7 @@ def load_library(build_if_missing: bool = False):
     L.pic_get_part_data.argtypes = [C.c_void_p, dp, i64p, C.c_int64, C.c_int32, P(C.c_int32)]
     L.pic_set_part_data.argtypes = [C.c_void_p, dp, i64p, C.c_int64, C.c_int32]
     L.pic_fp64_fma_rate.argtypes = [C.c_void_p, dp]
+    L.pic_fp32_fma_rate.argtypes = [C.c_void_p, dp]
     L.pic_step.argtypes = [C.c_void_p, C.c_double, C.c_int32, dp]
     L.pic_get_status.argtypes = [C.c_void_p, P(PicStatus)]
     L.pic_reset_status.argtypes = [C.c_void_p]
@@ -205,6 +207,12 @@ class ParticleLoop:
         """Sustained FP64 FMA rate of the GPU (GFLOP/s), measured by the library."""
         r = C.c_double(0.0)
         self._check(self.lib.pic_fp64_fma_rate(self.handle, C.byref(r)), "pic_fp64_fma_rate")
+        return r.value
+
+    def fp32_fma_rate(self) -> float:
+        """Sustained FP32 FMA rate of the GPU (GFLOP/s), measured by the library."""
+        r = C.c_double(0.0)
+        self._check(self.lib.pic_fp32_fma_rate(self.handle, C.byref(r)), "pic_fp32_fma_rate")
         return r.value
 
     def get_part_data(self, offset_npart: int = 0):

@@ -30,6 +30,7 @@ PIC_STATUS_BAD_ELEMENT = 0x10
 PIC_STATUS_NOT_FINITE = 0x20
 PIC_STATUS_CG_NOT_CONVERGED = 0x40
 PIC_STATUS_CG_BREAKDOWN = 0x80
+PIC_STATUS_WAIT_TIMEOUT = 0x100
 
 ERROR_NAMES = {0: "PIC_OK", 1: "PIC_ERR_INVALID_ARGUMENT", 2: "PIC_ERR_CUDA", 3: "PIC_ERR_OUT_OF_MEMORY",
                4: "PIC_ERR_NO_DEVICE", 5: "PIC_ERR_STATE", 6: "PIC_ERR_CAPACITY"}

@@ -1108,6 +1108,19 @@ int pic_fp64_fma_rate(pic_ctx_t* c, double* gflops) {
   return PIC_OK;
 }
 
+int pic_fp32_fma_rate(pic_ctx_t* c, double* gflops) {
+  if (!c || !gflops) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  float* sink = nullptr;
+  int rc = c->alloc(&sink, (size_t)sms * 8);
+  if (rc) return rc;
+  *gflops = pic::fp32_fma_rate(c->stream, sink, sms);
+  CUDA_TRY(cudaGetLastError());
+  return PIC_OK;
+}
+
 int pic_get_status(pic_ctx_t* c, pic_status_t* out) {
   if (!c || !out) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
   launch_count_inside(c->args(), c->P, c->d_count);

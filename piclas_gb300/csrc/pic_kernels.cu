@@ -1716,6 +1716,40 @@ double fp64_fma_rate(cudaStream_t st, double* sink, int sms) {
   return ms > 0.f ? flops / (ms * 1e-3) / 1e9 : 0.0;
 }
 
+// FP32 counterpart: independent fmaf chains (16 per thread), the peak the FP32 work of the mixed kernels is
+// compared against
+__global__ void __launch_bounds__(256) k_fp32_fma_probe(int iters, float b, float c, float* sink) {
+  float a[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) a[k] = 1.0f + 1e-3f * (float)(threadIdx.x + k);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = fmaf(a[k], b, c);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) s += a[k];
+  if (!isfinite(s)) sink[blockIdx.x] = s;
+}
+
+double fp32_fma_rate(cudaStream_t st, float* sink, int sms) {
+  const int blocks = sms * 8, iters = 8192;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp32_fma_probe<<<blocks, 256, 0, st>>>(iters / 8, 0.9999999f, 1e-7f, sink);     // warm-up
+  cudaEventRecord(e0, st);
+  k_fp32_fma_probe<<<blocks, 256, 0, st>>>(iters, 0.9999999f, 1e-7f, sink);
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double flops = 2.0 * 16.0 * (double)iters * 256.0 * (double)blocks;
+  return ms > 0.f ? flops / (ms * 1e-3) / 1e9 : 0.0;
+}
+
 int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
   switch (A.N) {
     case 1: if (A.mixed) launch_gather_n<1, true>(A, B, L, K, PS); else launch_gather_n<1, false>(A, B, L, K, PS); break;

@@ -70,6 +70,7 @@ int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBu
 int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K);
 int sf_gather_variant();   // compile-time shape-function gather variant (PIC_SF_GATHER)
 double fp64_fma_rate(cudaStream_t st, double* sink, int sms);   // GFLOP/s of independent FP64 FMA chains
+double fp32_fma_rate(cudaStream_t st, float* sink, int sms);    // GFLOP/s of independent FP32 FMA chains
 // shape_function_cc: scales each packed particle's Fac by q*MPF / (its quadrature charge over all DOFs
 // within R), so that every particle deposits exactly its charge
 int launch_sf_cc_norm(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K);

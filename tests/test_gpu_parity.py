@@ -564,6 +564,19 @@ def test_fp64_fma_rate_probe(gpu_lib):
     assert abs(r1 - r2) <= 0.1 * max(r1, r2), (r1, r2)
 
 
+def test_fp32_fma_rate_probe(gpu_lib):
+    """The FP32 peak the mixed kernels are compared against: plausible for GB300 (nominal 152 SMs x 128 lanes
+    x 2 FLOP x 2.07 GHz = 80.5 TFLOP/s), repeatable within 10 %, far above the FP64 rate."""
+    w = workloads.plasma_wave(n_cells=2, N=1, n_particles=10)
+    loop = ParticleLoop(w.config(), w.mesh)
+    r1, r2 = loop.fp32_fma_rate(), loop.fp32_fma_rate()
+    r64 = loop.fp64_fma_rate()
+    loop.close()
+    assert 10000.0 < r1 < 200000.0, r1
+    assert abs(r1 - r2) <= 0.1 * max(r1, r2), (r1, r2)
+    assert r1 > 20.0 * r64
+
+
 # ---- parity at the benchmark configurations --------------------------------------------------------
 def test_plasma_wave_full_size_100_steps_bitexact(gpu_lib, oracle_lib):
     """The plasma-wave case as benchmarked (8^3, N=3, 200k electrons, 100 steps, re-sorting every 10):
