@@ -330,6 +330,27 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
   for (int e = 0; e < ne; ++e) order[e] = mort[e].second;
   int* d_off; int* d_src; int8_t* d_sh; double* d_c; float* d_r; int* d_o;
   int rc;
+  if (c->mixed && c->N == 3 && !c->adaptive && pic::sf_gather_variant() == 5) {
+    // the particle box of every element relative to its DOF centre (kernel directions only): the corners'
+    // bounding box, padded by 5 % of its extent on every side (RefTracking keeps particles within
+    // epsOneCell ~ 1 + sqrt(3 RefMappingEps) of the element), for the sub-cell culling of the mixed gather
+    std::vector<float> ebox((size_t)ne * 8, 0.0f);
+    for (int e = 0; e < ne; ++e)
+      for (int d = 0; d < 3; ++d) {
+        if (!kdir[d]) continue;
+        double lo = 1e300, hi = -1e300;
+        for (int q = 0; q < 8; ++q) {
+          const double v = m->xcl_ngeo[((size_t)e * 8 + q) * 3 + d] - dofc[(size_t)e * 3 + d];
+          lo = std::min(lo, v); hi = std::max(hi, v);
+        }
+        const double pad = 0.05 * (hi - lo);
+        ebox[(size_t)e * 8 + d] = (float)(lo - pad);
+        ebox[(size_t)e * 8 + 4 + d] = (float)(hi + pad);
+      }
+    float* d_eb;
+    if ((rc = upload(c, &d_eb, ebox))) return rc;
+    c->sfl.elem_box = d_eb;
+  }
   if (c->cc) {
     // the pairs transposed to (source -> target, image), and wGP(k) wGP(l) wGP(m) / sJ per DOF
     const int n1 = c->N + 1;
@@ -744,6 +765,10 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     if ((rc = c->alloc(&c->sfk.posf, cap * 4))) return bail(rc);
     if (c->mixed) {
       if ((rc = c->alloc(&c->sfk.facf, cap * 4))) return bail(rc);
+      if (c->sfl.elem_box &&
+          ((rc = c->alloc(&c->sfk.sub_count, 8 * (size_t)ne + 1)) || (rc = c->alloc(&c->sfk.sub_off, 8 * (size_t)ne + 1)) ||
+           (rc = c->alloc(&c->sfk.sub_cursor, 8 * (size_t)ne + 1))))
+        return bail(rc);
     } else {
       if ((rc = c->alloc(&c->sfk.pos, cap * 3)) || (rc = c->alloc(&c->sfk.fac, cap * 4))) return bail(rc);
     }

@@ -578,13 +578,62 @@ __global__ void __launch_bounds__(1024) k_scan(const int* __restrict__ count, in
 // =============================================================================================
 // Shape-function deposition: pack particles by element, then gather per target element
 // =============================================================================================
-template <bool MIXED>
+// Sub-cell binning of the pack (mixed gather with octant warps): key 8 e + octant of the FP32 position relative to
+// the element's DOF centre, computed exactly as the pack computes the record (same conversion, same sign test).
+__device__ __forceinline__ int sf_sub_key(const Consts& kc, const DevParticles& P, int i, int e,
+                                          const double* __restrict__ dofc) {
+  const double x = kc.sf_keep[0] ? P.x[i] : 0.0, y = kc.sf_keep[1] ? P.y[i] : 0.0, z = kc.sf_keep[2] ? P.z[i] : 0.0;
+  const double* c = dofc + (size_t)e * 3;
+  const float rx = (float)(x - __ldg(c)), ry = (float)(y - __ldg(c + 1)), rz = (float)(z - __ldg(c + 2));
+  return 8 * e + (rx > 0.0f ? 1 : 0) + (ry > 0.0f ? 2 : 0) + (rz > 0.0f ? 4 : 0);
+}
+
+__global__ void __launch_bounds__(256) k_hist8(const __grid_constant__ Consts kc, DevParticles P,
+                                               const double* __restrict__ dofc, int* __restrict__ count8, int ne) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;      // the grid covers whole warps: no early return
+  const bool valid = i < P.n;
+  const bool in = valid && (P.flags[i] & kInside);
+  const int key = in ? sf_sub_key(kc, P, i, P.elem[i], dofc) : 8 * ne;
+  warp_slot(count8, key, valid);
+}
+
+// element counts from the sub-cell counts (count[ne] = particles not inside)
+__global__ void __launch_bounds__(256) k_sum8(const int* __restrict__ count8, int* __restrict__ count, int ne) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e > ne) return;
+  int sum = 0;
+  if (e < ne) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) sum += count8[8 * e + c];
+  } else {
+    sum = count8[8 * ne];
+  }
+  count[e] = sum;
+}
+
+// sub-cell offsets inside each element's range, and the pack cursors
+__global__ void __launch_bounds__(256) k_sub_offsets(const int* __restrict__ count8, const int* __restrict__ offset,
+                                                     int* __restrict__ off8, int* __restrict__ cursor8, int ne) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e > ne) return;
+  if (e == ne) { off8[8 * ne] = offset[ne]; cursor8[8 * ne] = offset[ne]; return; }
+  int o = offset[e];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    off8[8 * e + c] = o;
+    cursor8[8 * e + c] = o;
+    o += count8[8 * e + c];
+  }
+}
+
+template <bool MIXED, bool SUB>
 __global__ void __launch_bounds__(256) k_sf_pack(const __grid_constant__ Consts kc, DevParticles P, int* __restrict__ cursor, const double* __restrict__ dofc,
                                                  SfPack K) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < P.n && (P.flags[i] & kInside);
   const int e = valid ? P.elem[i] : 0;
-  const int slot = warp_slot(cursor, e, valid);
+  // SUB: records ordered by (element, sub-cell) through the sub-cell cursors
+  const int slot = warp_slot(cursor, SUB && valid ? sf_sub_key(kc, P, i, e, dofc) : e, valid);
   if (!valid) return;
   const int sp = P.species[i];
   const double qm = kc.qm[sp];
@@ -1231,6 +1280,337 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
 }
 
 // =============================================================================================
+// Mixed shape-function gather for N = 3 with one radius, fed by a TMA bulk-copy ring.
+//
+// The particle records of the target's (source element, periodic image) pairs are contiguous per source
+// element (the pack sorts them by element, and inside an element by 2x2x2 sub-cell), so their concatenation
+// is a stream of 16-byte records (position relative to the source's DOF centre, and w q MPF (v, 1)).
+// Thread 0 copies that stream into a ring of kSf7Stages shared-memory stages of kSf7Cap records with one
+// cp.async.bulk per (pair, stage) segment; each stage has a "full" mbarrier (the copies complete their
+// bytes on it) and an "empty" one (each of the 8 warps arrives when it is done with the stage).  The
+// producer keeps kSf7Ahead fills in flight and refills a stage only after every warp released it, so warps
+// may drift apart by a few fills and the global loads are never waited for by the CTA as a whole.
+// The 8 warps each own one DOF octant (2x2x2 DOFs in registers).  Per stage a warp skips the sub-cells whose
+// box lies beyond R + (octant radius) of its octant's centre, culls the records of the others to that
+// radius (about 1.5 candidates per hit), compacts the survivors with a ballot and evaluates them
+// lane-parallel without branches: with p and g relative to the target's DOF centre,
+// 1 - r^2/R^2 = A_p + B_g + p'.g (A_p = 1 - |p|^2/R^2, p' = 2 p/R^2, B_g = -|g|^2/R^2), then
+// S = max(., 0)^alpha and 4 fused multiply-adds: 10 FP32 instructions per pair.  Each lane sums its pairs in
+// FP32 for at most kSf7Fold particles; the warp then reduce-scatters the 32 partials (8 DOFs x 4 components)
+// so that lane k holds value k, which joins the lane's (hi, lo) pair through TwoSum: the FP64 result
+// hi + lo carries every fold exactly, FP32 rounding stays within windows of 16 x 32 terms.
+// Every wait is bounded (kMbarPolls polls); a wait that gives up sets PIC_STATUS_WAIT_TIMEOUT, the CTA
+// skips the rest of its work, and thread 0 waits (bounded) for the copies it issued before it returns.
+// =============================================================================================
+constexpr int kSf7Warps = 8, kSf7Threads = kSf7Warps * 32;
+constexpr int kSf7Stages = 4, kSf7Cap = 512, kSf7Ahead = 2;   // refill the stage released kStages-kAhead fills ago
+constexpr int kSf7Pairs = 160;
+constexpr int kSf7Fold = 16;
+constexpr int kMbarPolls = 1 << 22;
+constexpr unsigned kStatusWaitTimeout = 0x100u;               // PIC_STATUS_WAIT_TIMEOUT
+static_assert(kSf7Ahead < kSf7Stages, "the producer must refill a stage released earlier");
+static_assert(kSf7Cap <= 65536 && kSf7Pairs <= 65536, "compacted entries pack slot and pair in 16 bits each");
+
+struct Sf7Smem {
+  float4 pos[kSf7Stages][kSf7Cap];       // 16-byte aligned (bulk-copy destinations)
+  float4 fac[kSf7Stages][kSf7Cap];
+  uint32_t list[kSf7Warps][kSf7Cap];     // compacted (slot | pair << 16) per warp
+  float4 off[kSf7Pairs];                 // source DOF centre + image shift - target DOF centre
+  float4 blo[kSf7Pairs], bhi[kSf7Pairs]; // the source's padded particle box in the target frame
+  int sub[kSf7Pairs][9];                 // first record of each sub-cell relative to the pair's first record
+  int b0[kSf7Pairs], n[kSf7Pairs], g[kSf7Pairs + 1];
+  int sp[kSf7Stages];                    // first pair of the fill a stage holds
+  unsigned long long full[kSf7Stages], empty[kSf7Stages];
+  int abort_flag;
+};
+
+__device__ __forceinline__ float reduce_scatter32f(float v[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool upper = (lane & h) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const float a = v[j], b = v[j + h];
+      const float recv = __shfl_xor_sync(kFull, upper ? a : b, h);
+      v[j] = __fadd_rn(upper ? b : a, recv);
+    }
+  }
+  return v[0];
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait for the phase of the given parity; false after kMbarPolls polls
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (int i = 0; i < kMbarPolls; ++i)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+// 1D bulk copy global -> shared (TMA), completion counted in bytes on the mbarrier
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+template <bool A2>
+__global__ void __launch_bounds__(kSf7Threads, 2) k_sf_gather7(const __grid_constant__ DevMesh M, SfLists L,
+                                                               const int* __restrict__ off, SfPack K,
+                                                               double* __restrict__ PS, DevStatus* st) {
+  const Consts& kc = M.k;
+  constexpr int nd = 64;
+  extern __shared__ __align__(128) unsigned char sf7_raw[];
+  Sf7Smem& S = *reinterpret_cast<Sf7Smem*>(sf7_raw);
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int e = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
+  const double* ce = L.dof_center + (size_t)e * 3;
+  const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
+  const float R = (float)kc.sf_r, R2inv = (float)kc.sf_r2_inv, tR2 = 2.0f * R2inv;
+  // this warp's octant: DOF (i, j, k) = (2 ox + a, 2 oy + b, 2 oz + c), r = i + 4 (j + 4 k)
+  const int ox = w & 1, oy = (w >> 1) & 1, oz = w >> 2;
+  float gx[8], gy[8], gz[8], bg[8];
+  float lo3[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi3[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+#pragma unroll
+  for (int d = 0; d < 8; ++d) {
+    const int r = (2 * ox + (d & 1)) + 4 * ((2 * oy + ((d >> 1) & 1)) + 4 * (2 * oz + (d >> 2)));
+    const double* g = M.sf_xgp + ((size_t)e * nd + r) * 3;
+    gx[d] = (float)(__ldg(g) - cex); gy[d] = (float)(__ldg(g + 1) - cey); gz[d] = (float)(__ldg(g + 2) - cez);
+    bg[d] = -R2inv * fmaf(gx[d], gx[d], fmaf(gy[d], gy[d], gz[d] * gz[d]));
+    lo3[0] = fminf(lo3[0], gx[d]); hi3[0] = fmaxf(hi3[0], gx[d]);
+    lo3[1] = fminf(lo3[1], gy[d]); hi3[1] = fmaxf(hi3[1], gy[d]);
+    lo3[2] = fminf(lo3[2], gz[d]); hi3[2] = fmaxf(hi3[2], gz[d]);
+  }
+  const float ocx = 0.5f * (lo3[0] + hi3[0]), ocy = 0.5f * (lo3[1] + hi3[1]), ocz = 0.5f * (lo3[2] + hi3[2]);
+  float orad2 = 0.0f;
+#pragma unroll
+  for (int d = 0; d < 8; ++d) {
+    const float dx = gx[d] - ocx, dy = gy[d] - ocy, dz = gz[d] - ocz;
+    orad2 = fmaxf(orad2, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+  }
+  const float ocull = R + sqrtf(orad2);
+  const float ocull2 = ocull * ocull * 1.0001f;
+  if (t == 0) {
+    for (int q = 0; q < kSf7Stages; ++q) {
+      mbar_init(&S.full[q], 1);
+      mbar_init(&S.empty[q], kSf7Warps);
+    }
+    S.abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  float part[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) part[k] = 0.0f;
+  float hi = 0.0f, lo = 0.0f;
+  int since_fold = 0;
+  auto fold = [&]() {
+    float v = reduce_scatter32f(part);
+    float sm, er;
+    two_sum(hi, v, sm, er);
+    hi = sm;
+    lo = __fadd_rn(lo, er);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) part[k] = 0.0f;
+  };
+  volatile int* abort_flag = &S.abort_flag;
+  auto give_up = [&]() {
+    *abort_flag = 1;
+    flag_status(st, kStatusWaitTimeout);
+  };
+  int fill = 0;            // global fill index (fills continue across pair windows)
+  int issued = 0;          // thread 0: fills issued so far
+  int pc = 0;              // thread 0: first pair not yet fully copied in this window
+  const int p0 = __ldg(L.nb_off + e), p1 = __ldg(L.nb_off + e + 1);
+  for (int pw = p0; pw < p1; pw += kSf7Pairs) {
+    const int npw = min(kSf7Pairs, p1 - pw);
+    __syncthreads();                       // every warp is done with the previous window's tables
+    for (int i = t; i < npw; i += kSf7Threads) {
+      const int p = pw + i;
+      const int src = __ldg(L.nb_src + p);
+      double sh[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int k = kc.pv_dir[d];
+        sh[d] = k >= 0 ? (double)L.nb_shift[3 * p + d] * kc.pv[3 * k + d] : 0.0;
+      }
+      const double* cs = L.dof_center + (size_t)src * 3;
+      const float4 o = make_float4((float)((__ldg(cs) + sh[0]) - cex), (float)((__ldg(cs + 1) + sh[1]) - cey),
+                                   (float)((__ldg(cs + 2) + sh[2]) - cez), 0.0f);
+      S.off[i] = o;
+      const float4 bl = __ldg(reinterpret_cast<const float4*>(L.elem_box) + 2 * (size_t)src);
+      const float4 bh = __ldg(reinterpret_cast<const float4*>(L.elem_box) + 2 * (size_t)src + 1);
+      S.blo[i] = make_float4(bl.x + o.x, bl.y + o.y, bl.z + o.z, 0.0f);
+      S.bhi[i] = make_float4(bh.x + o.x, bh.y + o.y, bh.z + o.z, 0.0f);
+      const int b0 = __ldg(K.sub_off + 8 * (size_t)src);
+      S.b0[i] = b0;
+#pragma unroll
+      for (int c = 0; c <= 8; ++c) S.sub[i][c] = __ldg(K.sub_off + 8 * (size_t)src + c) - b0;
+      S.n[i] = S.sub[i][8];
+    }
+    __syncthreads();
+    if (t == 0) {
+      S.g[0] = 0;
+      for (int i = 0; i < npw; ++i) S.g[i + 1] = S.g[i] + S.n[i];
+    }
+    __syncthreads();
+    const int total = S.g[npw];
+    const int nfill = (total + kSf7Cap - 1) / kSf7Cap;
+    const int f0 = fill;
+    // thread 0: issue fill jj (window-relative jj - f0) after every warp released the stage's previous fill
+    auto issue = [&](int jj) {
+      const int s = jj % kSf7Stages;
+      if (*abort_flag) return;
+      if (jj >= kSf7Stages && !mbar_wait(&S.empty[s], (unsigned)((jj / kSf7Stages) - 1) & 1u)) {
+        give_up();
+        return;
+      }
+      const int r0 = (jj - f0) * kSf7Cap, r1 = min(r0 + kSf7Cap, total);
+      while (S.g[pc + 1] <= r0) ++pc;
+      S.sp[s] = pc;
+      mbar_arrive_expect_tx(&S.full[s], (unsigned)(r1 - r0) * 32u);
+      for (int p = pc; p < npw && S.g[p] < r1; ++p) {
+        const int a = max(S.g[p], r0), b = min(S.g[p + 1], r1);
+        if (b > a) {
+          const size_t src0 = (size_t)S.b0[p] + (size_t)(a - S.g[p]);
+          bulk_g2s(&S.pos[s][a - r0], reinterpret_cast<const float4*>(K.posf) + src0, (unsigned)(b - a) * 16u, &S.full[s]);
+          bulk_g2s(&S.fac[s][a - r0], reinterpret_cast<const float4*>(K.facf) + src0, (unsigned)(b - a) * 16u, &S.full[s]);
+        }
+      }
+      issued = jj + 1;
+    };
+    if (t == 0) {
+      pc = 0;
+      for (int i = 0; i < min(nfill, kSf7Ahead); ++i) issue(f0 + i);
+    }
+    for (int i = 0; i < nfill; ++i) {
+      const int j = f0 + i, s = j % kSf7Stages;
+      if (t == 0 && i + kSf7Ahead < nfill) issue(j + kSf7Ahead);
+      __syncwarp();
+      if (*abort_flag) continue;
+      // every lane observes the phase itself (acquire of the bulk-copied bytes); the outcome is made uniform
+      if (!__all_sync(kFull, mbar_wait(&S.full[s], (unsigned)(j / kSf7Stages) & 1u))) {
+        if (lane == 0) give_up();
+        __syncwarp();
+        continue;
+      }
+      const int r0 = i * kSf7Cap, r1 = min(r0 + kSf7Cap, total);
+      // this warp's octant: compact the stage's records within R + octant radius of its centre.  Sub-cells
+      // whose box lies beyond that reach are skipped; consecutive kept sub-cells form one run of records,
+      // tested 4 x 32 at a time (independent shared-memory loads in flight).
+      int cnt = 0;
+      for (int p = S.sp[s]; p < npw && S.g[p] < r1; ++p) {
+        const float4 o = S.off[p], bl = S.blo[p], bh = S.bhi[p];
+        unsigned keep = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          // the sub-cell's box, split at the source's DOF centre o
+          const float lx = (c & 1) ? o.x : bl.x, hx = (c & 1) ? bh.x : o.x;
+          const float ly = (c & 2) ? o.y : bl.y, hy = (c & 2) ? bh.y : o.y;
+          const float lz = (c & 4) ? o.z : bl.z, hz = (c & 4) ? bh.z : o.z;
+          const float ex = fmaxf(fmaxf(lx - ocx, ocx - hx), 0.0f), ey = fmaxf(fmaxf(ly - ocy, ocy - hy), 0.0f),
+                      ez = fmaxf(fmaxf(lz - ocz, ocz - hz), 0.0f);
+          if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= ocull2) keep |= 1u << c;
+        }
+        const float qx = o.x - ocx, qy = o.y - ocy, qz = o.z - ocz;   // record -> octant-centre frame
+        const uint32_t tag = (uint32_t)p << 16;
+        while (keep) {
+          const int c0 = __ffs(keep) - 1;
+          const int c1 = c0 + __ffs(~(keep >> c0)) - 1;                 // end of the run of kept sub-cells
+          keep &= ~((c1 >= 32 ? 0u : (1u << c1)) - (1u << c0));
+          const int a = max(S.g[p] + S.sub[p][c0], r0) - r0, b = min(S.g[p] + S.sub[p][c1], r1) - r0;
+          for (int base = a; base < b; base += 128) {
+            float4 rr[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int k = base + 32 * u + lane;
+              rr[u] = k < b ? S.pos[s][k] : make_float4(3e18f, 3e18f, 3e18f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float dx = rr[u].x + qx, dy = rr[u].y + qy, dz = rr[u].z + qz;
+              const bool ok = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= ocull2;
+              const unsigned m = __ballot_sync(kFull, ok);
+              if (ok) S.list[w][cnt + __popc(m & ((1u << lane) - 1u))] = (uint32_t)(base + 32 * u + lane) | tag;
+              cnt += __popc(m);
+            }
+          }
+        }
+      }
+      __syncwarp();
+      // evaluation, with the next entry's records loaded while the current one is evaluated
+      const int qend = (cnt + 31) & ~31;
+      float4 rn = make_float4(0.f, 0.f, 0.f, 0.f), on = rn, fn = rn;
+      bool vn = false;
+      if (lane < cnt) {
+        const uint32_t v = S.list[w][lane];
+        rn = S.pos[s][v & 0xFFFFu]; on = S.off[v >> 16]; fn = S.fac[s][v & 0xFFFFu];
+        vn = true;
+      }
+      for (int q = lane; q < qend; q += 32) {
+        const float4 r = rn, o = on, f = vn ? fn : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool valid = vn;
+        vn = false;
+        if (q + 32 < cnt) {
+          const uint32_t v = S.list[w][q + 32];
+          rn = S.pos[s][v & 0xFFFFu]; on = S.off[v >> 16]; fn = S.fac[s][v & 0xFFFFu];
+          vn = true;
+        }
+        const float x = r.x + o.x, y = r.y + o.y, z = r.z + o.z;
+        const float A = valid ? fmaf(-R2inv, fmaf(x, x, fmaf(y, y, z * z)), 1.0f) : -1.0f;
+        const float px = valid ? tR2 * x : 0.f, py = valid ? tR2 * y : 0.f, pz = valid ? tR2 * z : 0.f;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+          const float Sv = fmaxf(fmaf(pz, gz[d], fmaf(py, gy[d], fmaf(px, gx[d], bg[d]))) + A, 0.0f);
+          const float S1 = sf_power<A2>(kc, Sv);
+          part[4 * d] = fmaf(S1, f.x, part[4 * d]);
+          part[4 * d + 1] = fmaf(S1, f.y, part[4 * d + 1]);
+          part[4 * d + 2] = fmaf(S1, f.z, part[4 * d + 2]);
+          part[4 * d + 3] = fmaf(S1, f.w, part[4 * d + 3]);
+        }
+        if (++since_fold == kSf7Fold) {    // warp-uniform: every lane runs the same iterations
+          fold();
+          since_fold = 0;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S.empty[s]);
+    }
+    fill = f0 + nfill;
+  }
+  if (*abort_flag) {
+    // give the copies this CTA issued time to land before its shared memory goes away
+    if (t == 0)
+      for (int jj = max(issued - kSf7Stages, 0); jj < issued; ++jj)
+        (void)mbar_wait(&S.full[jj % kSf7Stages], (unsigned)(jj / kSf7Stages) & 1u);
+    return;
+  }
+  fold();
+  // lane k holds value k = 4 d + c of this octant
+  const int dl = lane >> 2;
+  const int r_out = (2 * ox + (dl & 1)) + 4 * ((2 * oy + ((dl >> 1) & 1)) + 4 * (2 * oz + (dl >> 2)));
+  PS[((size_t)e * nd + r_out) * 4 + (lane & 3)] = (double)hi + (double)lo;
+}
+
+// =============================================================================================
 // shape_function_cc normalisation (calcSfSource:96-120 with calcTotalChargePeriodic_cc:425-555).
 // One CTA per source element, one thread per packed particle of it.  Per round the CTA stages the DOFs
 // of four (target, image) pairs of the source, taken at stride npairs/4 so that they lie on different
@@ -1641,10 +2021,22 @@ int launch_sort_offsets(const LaunchArgs& A, const DevParticles& P, const SortBu
 }
 
 int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L, const SfPack& K) {
+  if (L.elem_box) {
+    // (element, sub-cell) bins: sub-cell histogram, element counts and offsets (B, as the other kernels read
+    // them), then the sub-cell offsets and cursors inside each element
+    const int ne = B.ne;
+    cudaMemsetAsync(K.sub_count, 0, sizeof(int) * (8 * (size_t)ne + 1), A.s);
+    if (P.n > 0) k_hist8<<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, L.dof_center, K.sub_count, ne);
+    k_sum8<<<nblk(ne + 1, 256), 256, 0, A.s>>>(K.sub_count, B.count, ne);
+    k_scan<<<1, 1024, 0, A.s>>>(B.count, B.offset, B.cursor, ne + 1);
+    k_sub_offsets<<<nblk(ne + 1, 256), 256, 0, A.s>>>(K.sub_count, B.offset, K.sub_off, K.sub_cursor, ne);
+    if (P.n > 0) k_sf_pack<true, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, K.sub_cursor, L.dof_center, K);
+    return P.n > 0 ? 5 : 3;
+  }
   int launches = launch_sort_offsets(A, P, B);
   if (P.n > 0) {
-    if (A.mixed) k_sf_pack<true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, B.cursor, L.dof_center, K);
-    else k_sf_pack<false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, B.cursor, L.dof_center, K);
+    if (A.mixed) k_sf_pack<true, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, B.cursor, L.dof_center, K);
+    else k_sf_pack<false, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M.k, P, B.cursor, L.dof_center, K);
     launches++;
   }
   return launches;
@@ -1659,6 +2051,17 @@ int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers
 template <int N, bool MIXED>
 static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
 #if PIC_SF_GATHER == 5
+  if constexpr (N == 3 && MIXED) {
+    // one radius: octant warps fed by the bulk-copy ring (sub-cell culling, no hit lists)
+    if (!L.elem_r && L.elem_box) {
+      const bool a2 = A.sf_alpha == 2;     // the attribute is per device: set it at every launch (cheap)
+      if (a2) cudaFuncSetAttribute(k_sf_gather7<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sf7Smem));
+      else cudaFuncSetAttribute(k_sf_gather7<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sf7Smem));
+      if (a2) k_sf_gather7<true><<<A.M.ne, kSf7Threads, sizeof(Sf7Smem), A.s>>>(A.M, L, B.offset, K, PS, A.st);
+      else k_sf_gather7<false><<<A.M.ne, kSf7Threads, sizeof(Sf7Smem), A.s>>>(A.M, L, B.offset, K, PS, A.st);
+      return;
+    }
+  }
   if (L.elem_r) k_sf_gather5<N, MIXED, true, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
   else if (A.sf_alpha == 2) k_sf_gather5<N, MIXED, false, true><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
   else k_sf_gather5<N, MIXED, false, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);

@@ -49,12 +49,20 @@ struct SfLists {
   const int8_t* t_shift;      // [n_pairs][3] periodic image of the source particles
   const double* dof_w;        // [ne][nd] wGP(k) wGP(l) wGP(m) / sJ
   const double* elem_r;       // [ne] shape_function_adaptive: radius of the source element (else NULL)
+  // particle box of each element relative to its DOF centre, padded (lo.xyz, 0, hi.xyz, 0); set where the
+  // pack bins particles into 2x2x2 sub-cells (mixed N = 3 with one radius), else NULL
+  const float* elem_box;      // [ne][8]
 };
 struct SfPack {
   double* pos;     // [cap][3] FP64 position (FP64 variant)
   double* fac;     // [cap][4] w_sf*q*MPF*(v,1) (FP64 variant)
   float* posf;     // [cap][4] position relative to the source element's DOF centre (FP32), 4th = pad
   float* facf;     // [cap][4] (mixed variant)
+  // sub-cell binning (SfLists::elem_box set): records ordered by (element, sub-cell), sub-cell = the octant of
+  // the position relative to the element's DOF centre (bit 0: x > 0, bit 1: y > 0, bit 2: z > 0)
+  int* sub_count;  // [8 ne + 1] (last: particles not inside)
+  int* sub_off;    // [8 ne + 1] first record of each (element, sub-cell); sub_off[8 ne] = records inside
+  int* sub_cursor; // [8 ne + 1]
 };
 
 // Launch wrappers; each returns the number of kernels it launched.
