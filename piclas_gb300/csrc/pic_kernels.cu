@@ -1319,6 +1319,7 @@ struct Sf7Smem {
   float4 blo[kSf7Pairs], bhi[kSf7Pairs]; // the source's padded particle box in the target frame
   int sub[kSf7Pairs][9];                 // first record of each sub-cell relative to the pair's first record
   int b0[kSf7Pairs], n[kSf7Pairs], g[kSf7Pairs + 1];
+  uint8_t okeep[kSf7Warps][kSf7Pairs];   // per warp (octant): the pair's sub-cells within its reach
   int sp[kSf7Stages];                    // first pair of the fill a stage holds
   unsigned long long full[kSf7Stages], empty[kSf7Stages];
   int abort_flag;
@@ -1471,6 +1472,22 @@ __global__ void __launch_bounds__(kSf7Threads, 2) k_sf_gather7(const __grid_cons
       S.g[0] = 0;
       for (int i = 0; i < npw; ++i) S.g[i + 1] = S.g[i] + S.n[i];
     }
+    // each warp: which sub-cells of every pair come within R + (octant radius) of its octant's centre (the
+    // sub-cell's box is the source's padded particle box split at the source's DOF centre o), once per window
+    for (int i = lane; i < npw; i += 32) {
+      const float4 o = S.off[i], bl = S.blo[i], bh = S.bhi[i];
+      unsigned keep = 0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const float lx = (c & 1) ? o.x : bl.x, hx = (c & 1) ? bh.x : o.x;
+        const float ly = (c & 2) ? o.y : bl.y, hy = (c & 2) ? bh.y : o.y;
+        const float lz = (c & 4) ? o.z : bl.z, hz = (c & 4) ? bh.z : o.z;
+        const float ex = fmaxf(fmaxf(lx - ocx, ocx - hx), 0.0f), ey = fmaxf(fmaxf(ly - ocy, ocy - hy), 0.0f),
+                    ez = fmaxf(fmaxf(lz - ocz, ocz - hz), 0.0f);
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= ocull2 && S.sub[i][c + 1] > S.sub[i][c]) keep |= 1u << c;
+      }
+      S.okeep[w][i] = (uint8_t)keep;
+    }
     __syncthreads();
     const int total = S.g[npw];
     const int nfill = (total + kSf7Cap - 1) / kSf7Cap;
@@ -1514,22 +1531,12 @@ __global__ void __launch_bounds__(kSf7Threads, 2) k_sf_gather7(const __grid_cons
       }
       const int r0 = i * kSf7Cap, r1 = min(r0 + kSf7Cap, total);
       // this warp's octant: compact the stage's records within R + octant radius of its centre.  Sub-cells
-      // whose box lies beyond that reach are skipped; consecutive kept sub-cells form one run of records,
-      // tested 4 x 32 at a time (independent shared-memory loads in flight).
+      // whose box lies beyond that reach are skipped (masks of the window); consecutive kept sub-cells form one
+      // run of records, tested 4 x 32 at a time (independent shared-memory loads in flight).
       int cnt = 0;
       for (int p = S.sp[s]; p < npw && S.g[p] < r1; ++p) {
-        const float4 o = S.off[p], bl = S.blo[p], bh = S.bhi[p];
-        unsigned keep = 0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          // the sub-cell's box, split at the source's DOF centre o
-          const float lx = (c & 1) ? o.x : bl.x, hx = (c & 1) ? bh.x : o.x;
-          const float ly = (c & 2) ? o.y : bl.y, hy = (c & 2) ? bh.y : o.y;
-          const float lz = (c & 4) ? o.z : bl.z, hz = (c & 4) ? bh.z : o.z;
-          const float ex = fmaxf(fmaxf(lx - ocx, ocx - hx), 0.0f), ey = fmaxf(fmaxf(ly - ocy, ocy - hy), 0.0f),
-                      ez = fmaxf(fmaxf(lz - ocz, ocz - hz), 0.0f);
-          if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= ocull2) keep |= 1u << c;
-        }
+        const float4 o = S.off[p];
+        unsigned keep = S.okeep[w][p];
         const float qx = o.x - ocx, qy = o.y - ocy, qz = o.z - ocz;   // record -> octant-centre frame
         const uint32_t tag = (uint32_t)p << 16;
         while (keep) {
