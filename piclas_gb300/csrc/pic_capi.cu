@@ -675,6 +675,21 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     c->M.bc_geo = d_bg;
   }
   c->MF = MeshF{d_xclr, d_dxclf, d_xezf, d_slenf};
+  if (c->mixed) {
+    // the NGeo = 1 map in monomial form for the mixed Newton: x = 1/8 sum_t X_t (1 + s_a xi1)(1 + s_b xi2)(1 + s_c xi3),
+    // s = -1 / +1 for the corner's low / high index; coefficients (c0, c1, c2, c3, c12, c13, c23, c123)
+    std::vector<double> tc((size_t)ne * 24, 0.0);
+    for (int e = 0; e < ne; ++e)
+      for (int t = 0; t < 8; ++t) {
+        const double sa = (t & 1) ? 1.0 : -1.0, sb = (t & 2) ? 1.0 : -1.0, sc = (t & 4) ? 1.0 : -1.0;
+        const double w[8] = {1.0, sa, sb, sc, sa * sb, sa * sc, sb * sc, sa * sb * sc};
+        for (int q = 0; q < 8; ++q)
+          for (int k = 0; k < 3; ++k) tc[(size_t)e * 24 + 3 * q + k] += 0.125 * w[q] * xcl[(size_t)e * 24 + 3 * t + k];
+      }
+    double* d_tc = nullptr;
+    if ((rc = upload(c, &d_tc, tc))) return bail(rc);
+    c->M.tcoef = d_tc;
+  }
 
   // ---- constants -------------------------------------------------------------------------------
   Consts k{};

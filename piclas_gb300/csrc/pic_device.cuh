@@ -70,6 +70,9 @@ struct DevMesh {
   const double* bc_geo;
   // shape-function DOF coordinates: elem_xgp, or for a 1D/2D kernel its directions only (others zero)
   const double* sf_xgp;
+  // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
+  // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3, [ne][8][3] in that order (from the corners at pic_create)
+  const double* tcoef;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
@@ -273,25 +276,26 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
 }
 
 // FP64 Newton of the mixed variant: same start value, stopping rule (||dxi||^2 <= RefMappingEps,
-// 100 iterations), Armijo damping and plausibility bound as RefElemNewton, but with the NGeo = 1
-// shape functions written as (1 -+ xi)/2 (no barycentric divisions), fused multiply-adds and one
-// reciprocal of det(J) per iteration.  Converges to the same xi up to rounding.
+// 100 iterations), Armijo damping and plausibility bound as RefElemNewton, but with the NGeo = 1 map in
+// monomial form (DevMesh::tcoef): the residual in 18 and the Jacobian in 30 fused multiply-adds instead of
+// the tensor-product sums over 8 corners (about half the FP64 work per iteration), and one reciprocal of
+// det(J) per iteration.  The same map, so it converges to the same xi up to rounding.
 static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
   const Consts& kc = M.k;
-  const double* X = M.xcl + (size_t)e * 24;
-  const double* DX = M.dxcl + (size_t)e * 72;
-  double Xl[24];
+  const double* Cg = M.tcoef + (size_t)e * 24;
+  double c[8][3];
 #pragma unroll
-  for (int q = 0; q < 24; ++q) Xl[q] = __ldg(X + q);
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[q][k] = __ldg(Cg + 3 * q + k);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c[0][k] = c[0][k] - x[k];     // the residual x(xi) - x is the polynomial itself
   auto residual = [&](const double z[3], double F[3]) {
-    const double l[3][2] = {{0.5 * (1.0 - z[0]), 0.5 * (1.0 + z[0])}, {0.5 * (1.0 - z[1]), 0.5 * (1.0 + z[1])},
-                            {0.5 * (1.0 - z[2]), 0.5 * (1.0 + z[2])}};
-    F[0] = -x[0]; F[1] = -x[1]; F[2] = -x[2];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const double w = l[0][t & 1] * l[1][(t >> 1) & 1] * l[2][t >> 2];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) F[c] = fma(Xl[3 * t + c], w, F[c]);
+    for (int k = 0; k < 3; ++k) {
+      const double t = fma(z[1], fma(z[2], c[7][k], c[4][k]), fma(z[2], c[5][k], c[1][k]));
+      const double u = fma(z[2], c[6][k], c[2][k]);
+      F[k] = fma(z[0], t, fma(z[1], u, fma(z[2], c[3][k], c[0][k])));
     }
   };
   double F[3];
@@ -300,16 +304,13 @@ static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e
   double normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
   bool success = true;
   for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
-    const double l[3][2] = {{0.5 * (1.0 - xi[0]), 0.5 * (1.0 + xi[0])}, {0.5 * (1.0 - xi[1]), 0.5 * (1.0 + xi[1])},
-                            {0.5 * (1.0 - xi[2]), 0.5 * (1.0 + xi[2])}};
-    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const double z12 = xi[0] * xi[1], z13 = xi[0] * xi[2], z23 = xi[1] * xi[2];
+    double J[3][3];                                      // J[nn][dd] = d x_nn / d xi_dd
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const double w = l[0][t & 1] * l[1][(t >> 1) & 1] * l[2][t >> 2];
-#pragma unroll
-      for (int nn = 0; nn < 3; ++nn)
-#pragma unroll
-        for (int dd = 0; dd < 3; ++dd) J[nn][dd] = fma(__ldg(DX + 9 * t + 3 * nn + dd), w, J[nn][dd]);
+    for (int k = 0; k < 3; ++k) {
+      J[k][0] = fma(z23, c[7][k], fma(xi[2], c[5][k], fma(xi[1], c[4][k], c[1][k])));
+      J[k][1] = fma(z13, c[7][k], fma(xi[2], c[6][k], fma(xi[0], c[4][k], c[2][k])));
+      J[k][2] = fma(z12, c[7][k], fma(xi[1], c[6][k], fma(xi[0], c[5][k], c[3][k])));
     }
     const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
     const double c01 = fma(J[0][2], J[2][1], -J[0][1] * J[2][2]);

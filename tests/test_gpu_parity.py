@@ -1049,3 +1049,18 @@ def test_sf_plasma_ball_kat_on_gpu(gpu_lib, oracle_lib, case):
             assert sf_ball_charge_ok(k, case, q), (case, q)
         else:
             assert abs(q - k["cases"][case]["total_charge"]) <= 1e-5 * abs(q), (case, q)
+
+
+def test_mixed_reftracking_100_steps_against_fp64(gpu_lib, oracle_lib):
+    """Mixed RefTracking (FP32 field and push, FP64 positions, the NGeo = 1 map in monomial form with fused
+    multiply-adds for the Newton) on the curved 16^3 box over 100 steps of the benchmark's time step: element
+    ids identical to the FP64 run, and PartPosRef equal, within 1e-10, to the reference Newton (oracle) at
+    the mixed run's own positions."""
+    w = workloads.curved_two_species(n_cells=16, n_per_species=100_000, seed=81, nsteps=100)
+    g64 = _run_gpu(w, 100)
+    g32 = _run_gpu(w, 100, precision=capi.PIC_PREC_MIXED)
+    assert np.array_equal(g32["elem"], g64["elem"])
+    assert g32["status"]["error_word"] == 0
+    st = oracle_lib.OracleState(g32["part_state"], g32["elem"], w.part_species)
+    oracle_lib.map_particles(w.config(), capi.MeshStruct(w.mesh), st)
+    assert np.max(np.abs(g32["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
