@@ -40,13 +40,21 @@ def log(*a):
 
 
 # ----------------------------------------------------------------------------------------------
-def make_workload(name: str, seed: int, n_override: int | None = None, cells: int | None = None):
+def make_workload(name: str, seed: int, n_override: int | None = None, cells: int | None = None,
+                  periodic_tracing: bool = False):
     from piclas_gb300 import workloads
+    from piclas_gb300.mesh import build_box_mesh
     kw = {} if cells is None else {"n_cells": cells}
     if name == "curved":
         if n_override is not None:
             kw["n_per_species"] = n_override // 2
-        return workloads.curved_two_species(seed=seed, **kw)
+        if periodic_tracing:
+            # the reference's default periodic RefTracking (CartesianPeriodic = F): BC lists with the periodic sides
+            nc = kw.pop("n_cells", 32)
+            kw["mesh"] = build_box_mesh(nc, nc, nc, 3, perturb=0.05, periodic_tracing=True)
+        w = workloads.curved_two_species(seed=seed, **kw)
+        w.periodic_tracing = periodic_tracing
+        return w
     if name == "plasma_wave":
         if n_override is not None:
             kw["n_particles"] = n_override
@@ -59,10 +67,12 @@ def workload_config(w, name):
     if name == "curved":
         cells = round(m.n_elems ** (1.0 / 3.0))
         tag = "plain FP64 at scale: " if (cells == 32 and w.n == 16_000_000) else "profiling case of plain FP64 at scale: "
+        trk = ("RefTracking (CartesianPeriodic = F: periodic sides traced as BC sides)"
+               if getattr(w, "periodic_tracing", False) else "RefTracking (CartesianPeriodic/FastPeriodic)")
         return {"workload": f"{tag}{cells}^3 curved hex, N={m.N}, {w.n // 2} e- + {w.n - w.n // 2} ions, "
                             "B_z=0.1 T, RefTracking, shape_function r=1.5h, dt=5e-12",
                 "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "shape_function",
-                "tracking": "RefTracking (CartesianPeriodic/FastPeriodic)", "l2": "inputs larger than L2 (no flush)"}
+                "tracking": trk, "l2": "inputs larger than L2 (no flush)"}
     cells = round(m.n_elems ** (1.0 / 3.0))
     return {"workload": f"plasma wave: {cells}^3 hex, N={m.N}, {w.n} e-, CVWM, TriaTracking, dt=1e-11",
             "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "cell_volweight_mean",
@@ -322,7 +332,8 @@ def run_gpu(args, rank, world, local_rank):
     mixed = args.precision == "mixed"
     prec = capi.PIC_PREC_MIXED if mixed else capi.PIC_PREC_FP64
     t0 = time.time()
-    w = make_workload(args.workload, seed=rank, n_override=args.particles, cells=args.cells)
+    w = make_workload(args.workload, seed=rank, n_override=args.particles, cells=args.cells,
+                      periodic_tracing=args.periodic_tracing)
     log(f"[rank {rank}] workload {w.name} built in {time.time() - t0:.1f}s")
     cfg = w.config(precision=prec, sort_interval=args.sort_interval)
     loop = ParticleLoop(cfg, w.mesh)
@@ -838,6 +849,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--particles", type=int, default=None, help="override the particle count (profiling cases)")
     ap.add_argument("--cells", type=int, default=None, help="override the elements per axis (profiling cases)")
+    ap.add_argument("--periodic-tracing", action="store_true",
+                    help="RefTracking traces the periodic sides as BC sides (the reference's default CartesianPeriodic = F)")
     ap.add_argument("--hdg-cg-kernel", type=int, default=0, choices=[0, 1, 2],
                     help="HDG CG launch form: 0 auto, 1 kernel per phase (graph), 2 cooperative")
     args = ap.parse_args()

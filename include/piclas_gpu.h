@@ -120,6 +120,15 @@ typedef struct pic_config_t {
    * 0 = not set = 1; a factor above 1 is rejected (PIC_ERR_INVALID_ARGUMENT), as the reference stops on it
    * (particle_emission_init.f90:218-219) */
   double  time_step_factor[PIC_MAX_SPECIES];
+  /* RefTracking on meshes with periodic sides: 0 = CartesianPeriodic = T with FastPeriodic (a particle that
+   * left the box is moved back by the periodic vectors, PeriodicMovement, particle_reftracking.f90:697-985);
+   * 1 = CartesianPeriodic = F, the reference's default (particle_mesh.f90:97-101): periodic sides are BC
+   * sides traced by ParticleBCTracking, a crossing moves the particle by the side's periodic vector into the
+   * neighbour element (GetBoundaryInteraction -> PeriodicBoundary, particle_boundary_condition.f90:184-186,
+   * 224-284).  With 1 the BC-element lists (pic_mesh_t.elem_to_bc_sides ...) must include the periodic sides
+   * (BuildBCElemDistance counts every side with SIDE_BCID > 0); open/reflective walls may then be combined
+   * with periodic sides. */
+  int32_t periodic_tracing;
 } pic_config_t;
 
 /* Mesh arrays as the reference holds them after init (NGeo = 1 hexahedra).
@@ -176,13 +185,13 @@ typedef struct pic_mesh_t {
   /* shape_function_adaptive: SFElemr2_Shared(1,nElems), the shape-function radius of each element
    * (InitShapeFunctionAdaptive, pic_depo.f90:727-815); NULL otherwise */
   const double* sf_elem_radius;
-  /* RefTracking on meshes whose boundaries are all open/reflective walls (no periodic vectors): the
-   * BC-element lists of BuildBCElemDistance (particle_mesh_build.f90:645-1092).  elem_to_bc_sides(1:2,
-   * nElems) = (ELEM_NBR_BCSIDES, ELEM_FIRST_BCSIDE): the number of wall sides in reach of the element and
-   * the 0-based first entry, -1/-1 for none; entry k (sorted by distance within an element) is the wall
-   * side bc_side_elem_loc(1:2,k) = (element 1-based, local side 1..6) with SideBCMetrics(BCSIDE_DISTANCE)
-   * = bc_side_distance(k).  Wall sides may be planar (rectangular or not) or bilinear.  NULL/0 for
-   * TriaTracking or periodic meshes. */
+  /* RefTracking with BC sides -- open/reflective walls, and with pic_config_t.periodic_tracing = 1 also the
+   * periodic sides: the BC-element lists of BuildBCElemDistance (particle_mesh_build.f90:645-1092).
+   * elem_to_bc_sides(1:2, nElems) = (ELEM_NBR_BCSIDES, ELEM_FIRST_BCSIDE): the number of BC sides in reach of
+   * the element and the 0-based first entry, -1/-1 for none; entry k (sorted by distance within an element)
+   * is the BC side bc_side_elem_loc(1:2,k) = (element 1-based, local side 1..6) with
+   * SideBCMetrics(BCSIDE_DISTANCE) = bc_side_distance(k).  Sides may be planar (rectangular or not) or
+   * bilinear.  NULL/0 for TriaTracking, or for periodic meshes with periodic_tracing = 0. */
   int32_t n_bc_entries;
   const int32_t* elem_to_bc_sides;
   const int32_t* bc_side_elem_loc;

@@ -575,6 +575,7 @@ static int almost_equal(double x, double y) { return fabs(x - y) <= fmax(fabs(x)
 typedef struct {
   double bv0[3], bv1[3], bv2[3], bv3[3], n[3], dist, P[4][3];
   int bc, type;                     /* type: SideType PLANAR_RECT (0), PLANAR_NONRECT (1), BILINEAR (2) */
+  int pvid, nb;                     /* bc = 3 (periodic): BoundaryType(BC_ALPHA) and SIDE_NBELEMID (1-based) */
 } orc_bc_side_t;
 enum { ORC_PLANAR_RECT = 0, ORC_PLANAR_NONRECT = 1, ORC_BILINEAR = 2 };
 
@@ -623,6 +624,9 @@ static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t
   double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
   for (int c = 0; c < 3; ++c) n[c] = n[c] / len;
   g->bc = m->side_bc ? m->side_bc[(size_t)e * 6 + s] : 0;
+  g->pvid = m->side_pvid[(size_t)e * 6 + s];
+  g->nb = m->side_nb_elem[(size_t)e * 6 + s];
+  if (g->bc == 0 && g->pvid != 0) g->bc = 3;     /* a periodic side traced as a BC side */
   /* slab thickness along the averaged normal against the side's extent */
   const double* Pc[4] = {P00, P10, P01, P11};
   double hmin = DBL_MAX, hmax = -DBL_MAX;
@@ -792,73 +796,104 @@ static double planar_rect_alpha(const orc_bc_side_t* g, const double xl[3], cons
 
 #define ORC_BC_CAP 32   /* wall sides within reach of one trajectory; more are not traced (same cap on the GPU) */
 
-/* ParticleBCTracking, particle_reftracking.f90:417-694, for wall sides only (the element never changes):
- * returns 1 when the particle is done -- it has not moved (PARTHASMOVED) or an open wall removed it */
-static int bc_tracking(const pic_mesh_t* m, const orc_bc_side_t* geo, int elem, double x[3], double xl[3],
+/* ParticleBCTracking, particle_reftracking.f90:417-694: trace the trajectory against the BC sides of the
+ * element's list (sorted by SideBCMetrics distance, stopping beyond the trajectory length) -- open and
+ * reflective walls, and with periodic_tracing the periodic sides.  A periodic crossing (GetBoundaryInteraction
+ * -> PeriodicBoundary, particle_boundary_condition.f90:184-186, 224-284) moves LastPartPos to the crossing
+ * point plus the periodic vector and the particle by the rest of its trajectory, and continues the trace in
+ * the neighbour element (the reference's recursive call, here a loop).  *elem is that element on return.
+ * Returns 1 when the particle is done -- it has not moved (PARTHASMOVED) or an open wall removed it. */
+static int bc_tracking(const pic_mesh_t* m, const orc_bc_side_t* geo, int* elem, double x[3], double xl[3],
                        double v[3], uint8_t* inside, double* len0, int64_t* ncap) {
-  const int e = elem - 1;
-  const int nloc = m->elem_to_bc_sides[2 * e], first = m->elem_to_bc_sides[2 * e + 1];
-  double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
-  double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
-  if (fabs(len / m->elem_radius[e]) <= 2.22e-16) return 1;
-  for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
-  *len0 = fmax(*len0, len);
-  int doubleCheck = 0;
-  double alphaOld = -1.0;
-  for (int loop = 0; loop < ORC_MAX_TRACK_LOOPS; ++loop) {
-    double alpha[ORC_BC_CAP], sxi[ORC_BC_CAP], seta[ORC_BC_CAP];
-    int list[ORC_BC_CAP];
-    int nc = 0, nInter = 0;
-    for (int i = 0; i < nloc; ++i) {
-      if (m->bc_side_distance[first + i] > *len0) break;
-      if (nc == ORC_BC_CAP) { (*ncap)++; break; }
-      const orc_bc_side_t* g = &geo[first + i];
-      sxi[nc] = 0.0; seta[nc] = 0.0;
-      if (g->type == ORC_PLANAR_RECT) {
-        alpha[nc] = planar_rect_alpha(g, xl, traj, len);
-      } else {
-        int bad = 0;
-        alpha[nc] = bilinear_alpha(g, xl, traj, len, doubleCheck ? alphaOld : -1.0, &sxi[nc], &seta[nc], &bad);
-        if (bad) (*ncap)++;
+  for (int call = 0; call < ORC_MAX_TRACK_LOOPS; ++call) {
+    const int e = *elem - 1;
+    const int nloc = m->elem_to_bc_sides[2 * e] > 0 ? m->elem_to_bc_sides[2 * e] : 0;
+    const int first = m->elem_to_bc_sides[2 * e + 1];
+    double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
+    double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+    if (fabs(len / m->elem_radius[e]) <= 2.22e-16) return 1;
+    for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+    *len0 = fmax(*len0, len);
+    int doubleCheck = 0, moved_elem = 0;
+    double alphaOld = -1.0;
+    for (int loop = 0; loop < ORC_MAX_TRACK_LOOPS; ++loop) {
+      double alpha[ORC_BC_CAP], sxi[ORC_BC_CAP], seta[ORC_BC_CAP];
+      int list[ORC_BC_CAP];
+      int nc = 0, nInter = 0;
+      for (int i = 0; i < nloc; ++i) {
+        if (m->bc_side_distance[first + i] > *len0) break;
+        if (nc == ORC_BC_CAP) { (*ncap)++; break; }
+        const orc_bc_side_t* g = &geo[first + i];
+        sxi[nc] = 0.0; seta[nc] = 0.0;
+        if (g->type == ORC_PLANAR_RECT) {
+          alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+        } else {
+          int bad = 0;
+          alpha[nc] = bilinear_alpha(g, xl, traj, len, doubleCheck ? alphaOld : -1.0, &sxi[nc], &seta[nc], &bad);
+          if (bad) (*ncap)++;
+        }
+        list[nc] = i;
+        if (alpha[nc] > -1.0) nInter++;
+        nc++;
       }
-      list[nc] = i;
-      if (alpha[nc] > -1.0) nInter++;
-      nc++;
+      if (nInter == 0) return 0;
+      int slot[ORC_BC_CAP];
+      for (int i = 0; i < nc; ++i) slot[i] = i;
+      for (int i = 1; i < nc; ++i) {              /* InsertionSort (stable) */
+        double t = alpha[i];
+        int ti = list[i], ts = slot[i], j = i - 1;
+        while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; slot[j + 1] = slot[j]; j--; }
+        alpha[j + 1] = t; list[j + 1] = ti; slot[j + 1] = ts;
+      }
+      for (int k = 0; k < nc; ++k)
+        if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
+      int reflected = 0;
+      for (int k = 0; k < nc; ++k) {
+        if (!(alpha[k] > -1.0)) continue;
+        const orc_bc_side_t* g = &geo[first + list[k]];
+        /* GetBoundaryInteraction (particle_boundary_condition.f90:35-221), REFMAPPING branch: SideNormVec of
+         * planar sides, CalcNormAndTangBilinear at the hit of bilinear ones */
+        double nl[3] = {g->n[0], g->n[1], g->n[2]};
+        if (g->type == ORC_BILINEAR) bilinear_normal(g, sxi[slot[k]], seta[slot[k]], nl);
+        if (nl[0] * traj[0] + nl[1] * traj[1] + nl[2] * traj[2] <= 0.0) { reflected = 0; continue; }
+        reflected = 1;
+        if (g->bc == 1) { *inside = 0; break; }                  /* RemoveParticle */
+        if (g->bc == 3) {
+          /* PeriodicBoundary: LastPartPos at the crossing plus the periodic vector, the rest of the trajectory */
+          const int k3 = (g->pvid < 0 ? -g->pvid : g->pvid) - 1;
+          const double sg = g->pvid < 0 ? -1.0 : 1.0;
+          for (int c = 0; c < 3; ++c) xl[c] = xl[c] + traj[c] * alpha[k];
+          for (int c = 0; c < 3; ++c) xl[c] = xl[c] + copysign(m->periodic_vectors[3 * k3 + c], sg);
+          for (int c = 0; c < 3; ++c) x[c] = xl[c] + (len - alpha[k]) * traj[c];
+          len = len - alpha[k];
+          if (g->nb != *elem) {
+            /* the trace continues in the neighbour; lengthPartTrajectory0 = the largest SideBCMetrics distance
+             * of the element it left */
+            if (m->n_periodic_vectors > 0) {
+              double mx = -DBL_MAX;
+              for (int i = 0; i < nloc; ++i) mx = fmax(mx, m->bc_side_distance[first + i]);
+              *len0 = mx;
+            }
+            *elem = g->nb;
+            moved_elem = 1;
+          }
+          break;
+        }
+        perfect_reflection(v, x, xl, traj, len, alpha[k], nl);
+        for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
+        len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+        if (fabs(len) <= 2.22e-16) len = 0.0;
+        else for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+        break;
+      }
+      if (moved_elem) break;
+      if (!*inside) return 1;
+      if (!reflected) {
+        if (!doubleCheck) doubleCheck = 1;
+        else return 0;
+      }
     }
-    if (nInter == 0) return 0;
-    int slot[ORC_BC_CAP];
-    for (int i = 0; i < nc; ++i) slot[i] = i;
-    for (int i = 1; i < nc; ++i) {              /* InsertionSort (stable) */
-      double t = alpha[i];
-      int ti = list[i], ts = slot[i], j = i - 1;
-      while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; slot[j + 1] = slot[j]; j--; }
-      alpha[j + 1] = t; list[j + 1] = ti; slot[j + 1] = ts;
-    }
-    for (int k = 0; k < nc; ++k)
-      if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
-    int reflected = 0;
-    for (int k = 0; k < nc; ++k) {
-      if (!(alpha[k] > -1.0)) continue;
-      const orc_bc_side_t* g = &geo[first + list[k]];
-      /* GetBoundaryInteraction (particle_boundary_condition.f90:35-221), REFMAPPING branch: SideNormVec of
-       * planar sides, CalcNormAndTangBilinear at the hit of bilinear ones */
-      double nl[3] = {g->n[0], g->n[1], g->n[2]};
-      if (g->type == ORC_BILINEAR) bilinear_normal(g, sxi[slot[k]], seta[slot[k]], nl);
-      if (nl[0] * traj[0] + nl[1] * traj[1] + nl[2] * traj[2] <= 0.0) { reflected = 0; continue; }
-      reflected = 1;
-      if (g->bc == 1) { *inside = 0; break; }                  /* RemoveParticle */
-      perfect_reflection(v, x, xl, traj, len, alpha[k], nl);
-      for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
-      len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
-      if (fabs(len) <= 2.22e-16) len = 0.0;
-      else for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
-      break;
-    }
-    if (!*inside) return 1;
-    if (!reflected) {
-      if (!doubleCheck) doubleCheck = 1;
-      else return 0;
-    }
+    if (!moved_elem) return 0;
   }
   return 0;
 }
@@ -870,13 +905,14 @@ static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, const
   double* xl = &p->last_part_pos[(size_t)ip * 3];
   double* xi = &p->part_pos_ref[(size_t)ip * 3];
   int elem = p->last_elem[ip];
-  if (geo && m->elem_to_bc_sides[2 * (elem - 1)] > 0) {
-    /* BC element (particle_reftracking.f90:98-126) */
+  const int bc_elem = geo && m->elem_to_bc_sides[2 * (elem - 1)] > 0;
+  if (bc_elem) {
+    /* BC element (particle_reftracking.f90:98-126); a periodic crossing changes the element */
     double len0 = 0.0;
-    if (bc_tracking(m, geo, elem, x, xl, v, &p->inside[ip], &len0, nhop)) { p->elem[ip] = elem; return; }
+    if (bc_tracking(m, geo, &elem, x, xl, v, &p->inside[ip], &len0, nhop)) { p->elem[ip] = elem; return; }
     orc_get_position_in_ref_elem(cfg, m, x, xi, elem, 0);
     if (maxabs3(xi) < 1.0) { p->elem[ip] = elem; return; }
-  } else if (m->n_periodic_vectors > 0) {
+  } else if (m->n_periodic_vectors > 0 && !cfg->periodic_tracing) {
     double lp[3] = {x[0], x[1], x[2]};
     periodic_movement_fast(m, x, xl);
     int guard = 0;
@@ -886,7 +922,7 @@ static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, const
       guard++;
     }
   }
-  if (!(geo && m->elem_to_bc_sides[2 * (elem - 1)] > 0)) {
+  if (!bc_elem) {
     orc_get_position_in_ref_elem(cfg, m, x, xi, elem, 0);
     if (maxabs3(xi) < 1.0) { p->elem[ip] = elem; return; }
   }
@@ -953,12 +989,15 @@ static void ref_track_single(const pic_config_t* cfg, const pic_mesh_t* m, const
   double epsElement = (te >= 1) ? m->eps_one_cell[te - 1] : 1.0;
   if (te < 1 || maxabs3(xi) > epsElement) {
     if (te >= 1 && geo && m->elem_to_bc_sides[2 * (te - 1)] > 0) {
-      /* BC element (particle_reftracking.f90:327-403): trace the walls again from TestElem */
+      /* BC element (particle_reftracking.f90:327-403): trace the BC sides again from TestElem (a periodic
+       * crossing changes it; epsOneCell stays the one of the element the trace started in) */
       double len0 = 0.0;
-      if (bc_tracking(m, geo, te, x, xl, v, &p->inside[ip], &len0, nhop)) return;
+      const double eps_te = m->eps_one_cell[te - 1];
+      if (bc_tracking(m, geo, &te, x, xl, v, &p->inside[ip], &len0, nhop)) { p->elem[ip] = te; return; }
       orc_get_position_in_ref_elem(cfg, m, x, xi, te, 0);
       /* beyond epsOneCell the reference calls LocateParticleInElement and aborts when that fails */
-      if (maxabs3(xi) > m->eps_one_cell[te - 1]) (*ntol)++;
+      if (maxabs3(xi) > eps_te) (*ntol)++;
+      else p->elem[ip] = te;
     } else {
       (*ntol)++;                                 /* the reference aborts here (internal element) */
     }
@@ -976,7 +1015,7 @@ static orc_bc_side_t* bc_geometry(const pic_mesh_t* m) {
 
 void orc_track(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, orc_counters_t* c, int nthreads) {
   int64_t nlost = 0, nhop = 0, ntol = 0;
-  orc_bc_side_t* geo = cfg->tracking == PIC_TRACK_REFMAPPING ? bc_geometry(m) : NULL;
+  orc_bc_side_t* geo = (cfg->tracking == PIC_TRACK_REFMAPPING && (m->n_periodic_vectors == 0 || cfg->periodic_tracing)) ? bc_geometry(m) : NULL;
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) reduction(+ : nlost, nhop, ntol) schedule(static)
 #endif

@@ -49,6 +49,7 @@ class PicConfig(C.Structure):
         ("refmapping_eps", C.c_double), ("sf_radius", C.c_double), ("sf_alpha", C.c_int32),
         ("sort_interval", C.c_int32), ("sf_dim", C.c_int32), ("sf_dir", C.c_int32), ("sf_depo3d", C.c_int32),
         ("time_step_factor", C.c_double * PIC_MAX_SPECIES),
+        ("periodic_tracing", C.c_int32),
     ]
 
 
@@ -111,8 +112,9 @@ def u8ptr(a: np.ndarray):
 def make_config(n_dg: int, tracking: int, deposition: int, precision: int, species, max_particles: int,
                 external_field=(0.0,) * 6, refmapping_eps: float = 1e-4, sf_radius: float = 0.0,
                 sf_alpha: int = 2, sort_interval: int = 0, sf_dim: int = 3, sf_dir: int = 1,
-                sf_depo3d: bool = True, time_step_factor=None) -> PicConfig:
-    """species: list of (charge, mass, mpf); time_step_factor: per species (Species%TimeStepFactor), None = 1."""
+                sf_depo3d: bool = True, time_step_factor=None, periodic_tracing: bool = False) -> PicConfig:
+    """species: list of (charge, mass, mpf); time_step_factor: per species (Species%TimeStepFactor), None = 1;
+    periodic_tracing: RefTracking traces periodic sides as BC sides (CartesianPeriodic = F)."""
     cfg = PicConfig()
     cfg.n_dg = n_dg
     cfg.tracking = tracking
@@ -126,6 +128,7 @@ def make_config(n_dg: int, tracking: int, deposition: int, precision: int, speci
         cfg.mpf[s] = w
     for s, f in enumerate(time_step_factor or []):
         cfg.time_step_factor[s] = float(f)
+    cfg.periodic_tracing = 1 if periodic_tracing else 0
     for i in range(6):
         cfg.external_field[i] = float(external_field[i])
     cfg.refmapping_eps = refmapping_eps

@@ -563,9 +563,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
         return bail(fail(PIC_ERR_INVALID_ARGUMENT,
                          "open/reflective particle boundaries need cell_volweight_mean, or a shape function on a mesh "
                          "without periodic sides"));
-      if (wall && cfg->tracking == PIC_TRACK_REFMAPPING && (m->n_periodic_vectors > 0 || !m->elem_to_bc_sides))
+      if (wall && cfg->tracking == PIC_TRACK_REFMAPPING &&
+          ((m->n_periodic_vectors > 0 && !cfg->periodic_tracing) || !m->elem_to_bc_sides))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT,
-                         "RefTracking with walls needs a mesh without periodic sides and elem_to_bc_sides"));
+                         "RefTracking with walls needs elem_to_bc_sides, and periodic_tracing = 1 on a mesh with "
+                         "periodic sides"));
       c->has_walls = c->has_walls || wall;
       side_nb[e * 6 + s] = wall ? -1 : nb - 1;
       uint32_t info = 0;
@@ -586,10 +588,14 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   // ---- RefTracking wall sides: BC-element lists and planar-side geometry ------------------------
   std::vector<int> bc_e2b;
   std::vector<double> bc_geo;
-  if (c->has_walls && cfg->tracking == PIC_TRACK_REFMAPPING) {
+  // BC sides: the open/reflective walls, and with periodic_tracing (CartesianPeriodic = F) the periodic sides
+  const bool bc_lists = cfg->tracking == PIC_TRACK_REFMAPPING &&
+                        (m->n_periodic_vectors > 0 ? cfg->periodic_tracing != 0 : c->has_walls);
+  if (bc_lists) {
     const int nent = m->n_bc_entries;
-    if (nent < 1 || !m->bc_side_elem_loc || !m->bc_side_distance)
-      return bail(fail(PIC_ERR_INVALID_ARGUMENT, "n_bc_entries/bc_side_elem_loc/bc_side_distance missing"));
+    if (nent < 1 || !m->elem_to_bc_sides || !m->bc_side_elem_loc || !m->bc_side_distance)
+      return bail(fail(PIC_ERR_INVALID_ARGUMENT,
+                       "elem_to_bc_sides/n_bc_entries/bc_side_elem_loc/bc_side_distance missing"));
     bc_e2b.assign(m->elem_to_bc_sides, m->elem_to_bc_sides + (size_t)ne * 2);
     for (int e = 0; e < ne; ++e) {
       const int n = bc_e2b[2 * e], f = bc_e2b[2 * e + 1];
@@ -600,11 +606,21 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     bc_geo.assign((size_t)nent * kBcGeo, 0.0);
     for (int k = 0; k < nent; ++k) {
       const int e = m->bc_side_elem_loc[2 * k] - 1, sd = m->bc_side_elem_loc[2 * k + 1] - 1;
-      if (e < 0 || e >= ne || sd < 0 || sd > 5 || m->side_nb_elem[e * 6 + sd] != 0)
-        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "bc_side_elem_loc must name open/reflective wall sides"));
+      const bool periodic_side = e >= 0 && e < ne && sd >= 0 && sd <= 5 && cfg->periodic_tracing &&
+                                 m->side_pvid[e * 6 + sd] != 0 && m->side_nb_elem[e * 6 + sd] != 0;
+      if (e < 0 || e >= ne || sd < 0 || sd > 5 || (m->side_nb_elem[e * 6 + sd] != 0 && !periodic_side))
+        return bail(fail(PIC_ERR_INVALID_ARGUMENT, "bc_side_elem_loc must name open/reflective wall sides, or "
+                                                   "periodic sides with periodic_tracing"));
       wall_side_geometry(xcl.data(), bary.data(), e, sd, &bc_geo[(size_t)k * kBcGeo]);
       bc_geo[(size_t)k * kBcGeo + 13] = m->bc_side_distance[k];
-      bc_geo[(size_t)k * kBcGeo + 14] = (double)m->side_bc[e * 6 + sd];
+      if (periodic_side) {
+        // PeriodicBC: the neighbour element (0-based) and BoundaryType(BC_ALPHA) of the side
+        bc_geo[(size_t)k * kBcGeo + 14] = 3.0;
+        bc_geo[(size_t)k * kBcGeo + 31] =
+            (double)(m->side_nb_elem[e * 6 + sd] - 1) * 16.0 + (double)(m->side_pvid[e * 6 + sd] + 8);
+      } else {
+        bc_geo[(size_t)k * kBcGeo + 14] = (double)m->side_bc[e * 6 + sd];
+      }
     }
   }
   // ---- periodic-unique nodes (merge Periodic_Nodes twins) ----------------------------------
@@ -701,6 +717,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     if (cfg->time_step_factor[s] > 0.0) k.dt_fac[s] = cfg->time_step_factor[s];
   }
   for (int q = 0; q < 6; ++q) k.ext[q] = cfg->external_field[q];
+  k.periodic_tracing = (cfg->tracking == PIC_TRACK_REFMAPPING && cfg->periodic_tracing) ? 1 : 0;
   k.refmapping_eps = cfg->refmapping_eps > 0.0 ? cfg->refmapping_eps : 1e-4;
   const double c2 = 299792458.0 * 299792458.0;
   k.c2_inv = 1.0 / c2;

@@ -44,6 +44,7 @@ struct Consts {
   int sf_alpha;
   int pv_dir[3];                               // periodic vector index per axis (-1: none)
   int sf_keep[3];                              // 1D/2D shape function: 1 in the kernel directions
+  int periodic_tracing;                        // RefTracking: periodic sides traced as BC sides (CartesianPeriodic = F)
 };
 
 // ---- mesh (device arrays) ---------------------------------------------------------------
@@ -77,12 +78,10 @@ struct DevMesh {
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
 };
-// one wall-side entry of a BC element: [0..2] BaseVectors0, [3..5] BaseVectors1, [6..8] BaseVectors2,
-// [9..11] SideNormVec (away from the domain), [12] SideDistance, [13] SideBCMetrics(BCSIDE_DISTANCE),
-// [14] boundary (1 open, 2 reflective)
-// per wall entry: BaseVectors0-2 [0..8], SideNormVec [9..11], SideDistance [12], BCSIDE_DISTANCE [13],
-// boundary (1 open, 2 reflective) [14], SideType [15] (0 PLANAR_RECT, 1 PLANAR_NONRECT, 2 BILINEAR),
-// BaseVectors3 [16..18], the corners P00, P10, P01, P11 [19..30]
+// per BC-side entry: BaseVectors0-2 [0..8], SideNormVec (away from the element) [9..11], SideDistance [12],
+// SideBCMetrics(BCSIDE_DISTANCE) [13], boundary [14] (1 open, 2 reflective, 3 periodic), SideType [15]
+// (0 PLANAR_RECT, 1 PLANAR_NONRECT, 2 BILINEAR), BaseVectors3 [16..18], the corners P00, P10, P01, P11
+// [19..30], periodic sides: 16 (neighbour element, 0-based) + (BoundaryType(BC_ALPHA) + 8) [31]
 constexpr int kBcGeo = 32;
 constexpr int kBcCap = 32;   // wall sides traced per trajectory (entries within reach beyond it are not)
 
@@ -909,81 +908,117 @@ __device__ __forceinline__ void bilinear_normal(const double* __restrict__ g, do
 
 // ParticleBCTracking, particle_reftracking.f90:417-694, for wall sides only (the element never changes).
 // Returns true when the particle is done: it has not moved (PARTHASMOVED) or an open wall removed it.
-static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int elem, double x[3], double xl[3], double v[3],
+static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int& elem, double x[3], double xl[3], double v[3],
                                          bool& removed, double& len0, bool& cap_hit) {
-  const int nloc = __ldg(M.bc_e2b + 2 * elem), first = __ldg(M.bc_e2b + 2 * elem + 1);
-  double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
-  double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
-  if (fabs(len / __ldg(M.radius + elem)) <= 2.22e-16) return true;
+  const Consts& kc = M.k;
+  // each pass is one call of the reference's recursive ParticleBCTracking; a periodic crossing into another
+  // element starts the next pass (the recursion is a tail call)
+  for (int call = 0; call < 10000; ++call) {
+    const int nl0 = __ldg(M.bc_e2b + 2 * elem);
+    const int nloc = nl0 > 0 ? nl0 : 0, first = __ldg(M.bc_e2b + 2 * elem + 1);
+    double traj[3] = {x[0] - xl[0], x[1] - xl[1], x[2] - xl[2]};
+    double len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+    if (fabs(len / __ldg(M.radius + elem)) <= 2.22e-16) return true;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
-  len0 = fmax(len0, len);
-  bool doubleCheck = false;
-  double alphaOld = -1.0;
-  for (int loop = 0; loop < 10000; ++loop) {
-    double alpha[kBcCap];
-    int list[kBcCap];
-    int nc = 0, nInter = 0;
-    const double alpha2 = doubleCheck ? alphaOld : -1.0;
-    for (int i = 0; i < nloc; ++i) {
-      const double* g = M.bc_geo + (size_t)kBcGeo * (first + i);
-      if (__ldg(g + 13) > len0) break;
-      if (nc == kBcCap) { cap_hit = true; break; }
-      if (__ldg(g + 15) == 0.0) {
-        alpha[nc] = planar_rect_alpha(g, xl, traj, len);
-      } else {
-        double sxi, seta;
-        bool bad = false;
-        alpha[nc] = bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
-        if (bad) cap_hit = true;
+    for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+    len0 = fmax(len0, len);
+    bool doubleCheck = false, moved_elem = false;
+    double alphaOld = -1.0;
+    for (int loop = 0; loop < 10000; ++loop) {
+      double alpha[kBcCap];
+      int list[kBcCap];
+      int nc = 0, nInter = 0;
+      const double alpha2 = doubleCheck ? alphaOld : -1.0;
+      for (int i = 0; i < nloc; ++i) {
+        const double* g = M.bc_geo + (size_t)kBcGeo * (first + i);
+        if (__ldg(g + 13) > len0) break;
+        if (nc == kBcCap) { cap_hit = true; break; }
+        if (__ldg(g + 15) == 0.0) {
+          alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+        } else {
+          double sxi, seta;
+          bool bad = false;
+          alpha[nc] = bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
+          if (bad) cap_hit = true;
+        }
+        list[nc] = i;
+        if (alpha[nc] > -1.0) nInter++;
+        nc++;
       }
-      list[nc] = i;
-      if (alpha[nc] > -1.0) nInter++;
-      nc++;
-    }
-    if (nInter == 0) return false;
-    for (int i = 1; i < nc; ++i) {                       // InsertionSort (stable)
-      const double t = alpha[i];
-      const int ti = list[i];
-      int j = i - 1;
-      while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; j--; }
-      alpha[j + 1] = t;
-      list[j + 1] = ti;
-    }
-    for (int k = 0; k < nc; ++k)
-      if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
-    bool reflected = false;
-    for (int k = 0; k < nc; ++k) {
-      if (!(alpha[k] > -1.0)) continue;
-      const double* g = M.bc_geo + (size_t)kBcGeo * (first + list[k]);
-      double n[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
-      if (__ldg(g + 15) == 2.0) {
-        // the hit's xi/eta: the same call as above (xl, traj, len and alpha2 are unchanged until a reflection)
-        double sxi = 0.0, seta = 0.0;
-        bool bad = false;
-        bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
-        bilinear_normal(g, sxi, seta, n);
+      if (nInter == 0) return false;
+      for (int i = 1; i < nc; ++i) {                       // InsertionSort (stable)
+        const double t = alpha[i];
+        const int ti = list[i];
+        int j = i - 1;
+        while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; j--; }
+        alpha[j + 1] = t;
+        list[j + 1] = ti;
       }
-      // GetBoundaryInteraction, REFMAPPING branch (particle_boundary_condition.f90:35-221)
-      if (n[0] * traj[0] + n[1] * traj[1] + n[2] * traj[2] <= 0.0) { reflected = false; continue; }
-      reflected = true;
-      if (__ldg(g + 14) == 1.0) { removed = true; break; }          // RemoveParticle
-      perfect_reflection(v, x, xl, traj, len, alpha[k], n);
+      for (int k = 0; k < nc; ++k)
+        if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
+      bool reflected = false;
+      for (int k = 0; k < nc; ++k) {
+        if (!(alpha[k] > -1.0)) continue;
+        const double* g = M.bc_geo + (size_t)kBcGeo * (first + list[k]);
+        double n[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
+        if (__ldg(g + 15) == 2.0) {
+          // the hit's xi/eta: the same call as above (xl, traj, len and alpha2 are unchanged until an interaction)
+          double sxi = 0.0, seta = 0.0;
+          bool bad = false;
+          bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
+          bilinear_normal(g, sxi, seta, n);
+        }
+        // GetBoundaryInteraction, REFMAPPING branch (particle_boundary_condition.f90:35-221)
+        if (n[0] * traj[0] + n[1] * traj[1] + n[2] * traj[2] <= 0.0) { reflected = false; continue; }
+        reflected = true;
+        const double bc = __ldg(g + 14);
+        if (bc == 1.0) { removed = true; break; }                    // RemoveParticle
+        if (bc == 3.0) {
+          // PeriodicBoundary (particle_boundary_condition.f90:224-284): LastPartPos at the crossing plus the
+          // periodic vector, the particle at the rest of its trajectory, the trace goes on in the neighbour
+          const double code = __ldg(g + 31);
+          const int nb = (int)(code / 16.0);
+          const int pvid = (int)(code - 16.0 * (double)nb) - 8;
+          const int k3 = (pvid < 0 ? -pvid : pvid) - 1;
+          const double sg = pvid < 0 ? -1.0 : 1.0;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
-      len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
-      if (fabs(len) <= 2.22e-16) len = 0.0;
-      else {
+          for (int c = 0; c < 3; ++c) xl[c] = xl[c] + traj[c] * alpha[k];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+          for (int c = 0; c < 3; ++c) xl[c] = xl[c] + copysign(kc.pv[3 * k3 + c], sg);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) x[c] = xl[c] + (len - alpha[k]) * traj[c];
+          len = len - alpha[k];
+          if (nb != elem) {
+            // lengthPartTrajectory0 = the largest SideBCMetrics distance of the element left behind
+            if (kc.n_pv > 0) {
+              double mx = -1.7976931348623157e308;
+              for (int i = 0; i < nloc; ++i) mx = fmax(mx, __ldg(M.bc_geo + (size_t)kBcGeo * (first + i) + 13));
+              len0 = mx;
+            }
+            elem = nb;
+            moved_elem = true;
+          }
+          break;
+        }
+        perfect_reflection(v, x, xl, traj, len, alpha[k], n);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) traj[c] = x[c] - xl[c];
+        len = sqrt(traj[0] * traj[0] + traj[1] * traj[1] + traj[2] * traj[2]);
+        if (fabs(len) <= 2.22e-16) len = 0.0;
+        else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) traj[c] = traj[c] / len;
+        }
+        break;
       }
-      break;
+      if (moved_elem) break;
+      if (removed) return true;
+      if (!reflected) {
+        if (!doubleCheck) doubleCheck = true;
+        else return false;
+      }
     }
-    if (removed) return true;
-    if (!reflected) {
-      if (!doubleCheck) doubleCheck = true;
-      else return false;
-    }
+    if (!moved_elem) return false;
   }
   return false;
 }
@@ -998,13 +1033,14 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
   tol_fail = false;
   removed = false;
   const bool bc_elem = M.bc_e2b && __ldg(M.bc_e2b + 2 * last_elem) > 0;
+  int elem = last_elem;
   if (bc_elem) {
-    // BC element (particle_reftracking.f90:98-126)
+    // BC element (particle_reftracking.f90:98-126); a periodic crossing changes the element
     double len0 = 0.0;
-    if (bc_tracking(M, last_elem, x, xl, v, removed, len0, cap_hit)) return last_elem;
-    position_in_ref_elem_t<FAST>(M, last_elem, x, xi);
-    if (maxabs3(xi) < 1.0) return last_elem;
-  } else if (kc.n_pv > 0) {
+    if (bc_tracking(M, elem, x, xl, v, removed, len0, cap_hit)) return elem;
+    position_in_ref_elem_t<FAST>(M, elem, x, xi);
+    if (maxabs3(xi) < 1.0) return elem;
+  } else if (kc.n_pv > 0 && !kc.periodic_tracing) {
     double lp[3] = {x[0], x[1], x[2]};
     periodic_movement_fast(kc, x, xl);
     int guard = 0;
@@ -1080,12 +1116,16 @@ __device__ __noinline__ int ref_track(const DevMesh& M, int last_elem, double x[
   }
   if (te < 0 || maxabs3(xi) > __ldg(M.eps1 + te)) {
     if (te >= 0 && M.bc_e2b && __ldg(M.bc_e2b + 2 * te) > 0) {
-      // BC element (particle_reftracking.f90:327-403): trace the walls again from TestElem
+      // BC element (particle_reftracking.f90:327-403): trace the BC sides again from TestElem (a periodic
+      // crossing changes it; epsOneCell stays the one of the element the trace started in)
       double len0 = 0.0;
-      if (bc_tracking(M, te, x, xl, v, removed, len0, cap_hit)) return te;
-      position_in_ref_elem_t<FAST>(M, te, x, xi);
+      const double eps_te = __ldg(M.eps1 + te);
+      int tn = te;
+      if (bc_tracking(M, tn, x, xl, v, removed, len0, cap_hit)) return tn;
+      position_in_ref_elem_t<FAST>(M, tn, x, xi);
       // beyond epsOneCell the reference calls LocateParticleInElement and aborts when that fails
-      if (maxabs3(xi) > __ldg(M.eps1 + te)) tol_fail = true;
+      if (maxabs3(xi) > eps_te) tol_fail = true;
+      else te = tn;
     } else {
       tol_fail = true;
     }

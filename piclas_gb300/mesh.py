@@ -216,7 +216,7 @@ WALL_BC = {"open": 1, "reflective": 2}      # PartBound%TargetBoundCond
 def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
                    perturb: float = 0.0, refmapping_eps: float = 1.0e-4,
                    bc=("periodic", "periodic", "periodic"), bc_halo_eps: float | None = None,
-                   wall_bulge: float = 0.0, wall_shear: float = 0.0) -> BoxMesh:
+                   wall_bulge: float = 0.0, wall_shear: float = 0.0, periodic_tracing: bool = False) -> BoxMesh:
     """Build a box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
 
     ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
@@ -224,7 +224,8 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     ``bc`` gives the particle boundary of both faces of each axis: "periodic" (a periodic vector, node
     twins for cell_volweight_mean), "open" or "reflective" (wall sides without a neighbour: SIDE_NBELEMID
     = 0, master orientation, convex).  Without periodic axes the BC-element lists of RefTracking are
-    built with halo ``bc_halo_eps`` (default: the largest element extent).
+    built with halo ``bc_halo_eps`` (default: the largest element extent); with ``periodic_tracing``
+    (CartesianPeriodic = F) they include the periodic sides, and walls may be combined with periodic axes.
     ``wall_bulge`` moves the nodes of each open/reflective face inwards along its normal by
     ``wall_bulge*h*sin(pi u)sin(pi v)`` (u, v in [0,1] across the face): the wall sides become bilinear
     (SideType BILINEAR).  ``wall_shear`` moves them within the face plane by ``wall_shear*h`` times the
@@ -529,9 +530,10 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         fibgm_element=fib_el, canonical_node=canon,
         side_bc=side_bc if side_bc.any() else None, bc=bc,
     )
-    if side_bc.any() and not any(periodic):
+    if (side_bc.any() and not any(periodic)) or (periodic_tracing and any(periodic)):
         halo = float(hvec.max()) if bc_halo_eps is None else float(bc_halo_eps)
-        mesh.elem_to_bc_sides, mesh.bc_side_elem_loc, mesh.bc_side_distance = build_bc_elem_distance(mesh, halo)
+        mesh.elem_to_bc_sides, mesh.bc_side_elem_loc, mesh.bc_side_distance = build_bc_elem_distance(
+            mesh, halo, include_periodic=periodic_tracing)
     return mesh
 
 
@@ -673,23 +675,28 @@ def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothi
     return r
 
 
-def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float):
+def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float, include_periodic: bool = False):
     """ElemToBCSides / SideBCMetrics of BuildBCElemDistance (particle_mesh_build.f90:645-1092, the halo
-    branch of an MPI build): for every element its own wall sides (local side order), then every other
-    wall side whose element and side lie within bc_halo_eps (+ radii) of it, ordered by
+    branch of an MPI build): for every element its own BC sides (local side order), then every other
+    BC side whose element and side lie within bc_halo_eps (+ radii) of it, ordered by
     SideBCMetrics(BCSIDE_DISTANCE) = |ElemBaryNGeo - origin| - ElemRadiusNGeo - side radius with the
-    reference's stable InsertionSort.  Side origin and radius: BuildSideOriginAndRadius
-    (particle_mesh_build.f90:1795-1820; DeCasteljauInterpolation at (0,0)).
+    reference's stable InsertionSort.  BC sides are the open/reflective walls and, with ``include_periodic``
+    (CartesianPeriodic = F: every side with SIDE_BCID > 0 counts), the periodic sides.  Side origin and radius:
+    BuildSideOriginAndRadius (particle_mesh_build.f90:1795-1820; DeCasteljauInterpolation at (0,0)).
     Returns (elem_to_bc_sides (nElems,2) = (count or -1, 0-based first entry or -1),
              entries (n,2) = (element 1-based, local side 1-based), distance (n))."""
     ne = mesh.n_elems
-    walls = [(e, s) for e in range(ne) for s in range(6) if mesh.side_nb_elem[e, s] == 0]
-    if not walls:
+    isbc = mesh.side_nb_elem == 0
+    if include_periodic:
+        isbc = isbc | (mesh.side_pvid != 0)
+    we_arr, ws_arr = np.nonzero(isbc)                  # element-major, local side order
+    nbc = len(we_arr)
+    if nbc == 0:
         return None
-    origin = np.zeros((len(walls), 3))
-    radius = np.zeros(len(walls))
-    for k, (e, s) in enumerate(walls):
-        P = side_control_points(mesh, e, s)
+    origin = np.zeros((nbc, 3))
+    radius = np.zeros(nbc)
+    for k in range(nbc):
+        P = side_control_points(mesh, int(we_arr[k]), int(ws_arr[k]))
         o = (((0.5 * P[0, 0]) * 0.5 + (0.5 * P[1, 0]) * 0.5) + (0.5 * P[0, 1]) * 0.5) + (0.5 * P[1, 1]) * 0.5
         origin[k] = o
         rmax = 0.0
@@ -698,44 +705,38 @@ def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float):
                 v = P[q, p] - o
                 rmax = max(rmax, float(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]))
         radius[k] = math.sqrt(rmax)
-    wall_elem = np.array([e for e, _ in walls])
     bary = mesh.elem_bary
     rad = mesh.elem_radius
 
     def norm3(v):
         return np.sqrt(v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1] + v[..., 2] * v[..., 2])
 
+    own_first = np.searchsorted(we_arr, np.arange(ne), side="left")
+    own_last = np.searchsorted(we_arr, np.arange(ne), side="right")
     e2b = -np.ones((ne, 2), dtype=np.int32)
     entries, dists = [], []
-    for e in range(ne):
-        own = [k for k, (we, _) in enumerate(walls) if we == e]
-        other = np.nonzero(wall_elem != e)[0]
-        d_el = norm3(bary[e] - bary[wall_elem[other]])
-        keep = d_el <= bc_halo_eps + rad[e] + rad[wall_elem[other]]
-        d_sd = norm3(bary[e] - origin[other])
-        keep &= d_sd <= bc_halo_eps + rad[e] + radius[other]
-        lst = own + [int(k) for k in other[keep]]
-        if not lst:
-            continue
-        vec = bary[e] - origin[lst]
-        dist = np.sqrt((vec[:, 0] * vec[:, 0] + vec[:, 1] * vec[:, 1]) + vec[:, 2] * vec[:, 2]) - rad[e] - radius[lst]
-        # InsertionSort (utils.f90:52-101): stable, ascending
-        order = list(range(len(lst)))
-        dv = list(dist)
-        for i in range(1, len(order)):
-            t, ti = dv[i], order[i]
-            j = i - 1
-            while j >= 0 and not (dv[j] <= t):
-                dv[j + 1] = dv[j]
-                order[j + 1] = order[j]
-                j -= 1
-            dv[j + 1] = t
-            order[j + 1] = ti
-        e2b[e] = (len(lst), len(entries))
-        for i in order:
-            we, ws = walls[lst[i]]
-            entries.append((we + 1, ws + 1))
-            dists.append(float(dist[i]))
+    chunk = max(1, 4_000_000 // nbc)
+    for c0 in range(0, ne, chunk):
+        es = np.arange(c0, min(ne, c0 + chunk))
+        d_el = norm3(bary[es][:, None, :] - bary[we_arr][None, :, :])
+        keep = d_el <= bc_halo_eps + rad[es][:, None] + rad[we_arr][None, :]
+        d_sd = norm3(bary[es][:, None, :] - origin[None, :, :])
+        keep &= d_sd <= bc_halo_eps + rad[es][:, None] + radius[None, :]
+        keep &= we_arr[None, :] != es[:, None]
+        for r, e in enumerate(es):
+            own = list(range(own_first[e], own_last[e]))
+            lst = own + [int(k) for k in np.nonzero(keep[r])[0]]
+            if not lst:
+                continue
+            lst = np.asarray(lst)
+            vec = bary[e] - origin[lst]
+            dist = np.sqrt((vec[:, 0] * vec[:, 0] + vec[:, 1] * vec[:, 1]) + vec[:, 2] * vec[:, 2]) - rad[e] - radius[lst]
+            order = np.argsort(dist, kind="stable")     # InsertionSort (utils.f90:52-101): stable, ascending
+            e2b[e] = (len(lst), len(entries))
+            for i in order:
+                k = int(lst[i])
+                entries.append((int(we_arr[k]) + 1, int(ws_arr[k]) + 1))
+                dists.append(float(dist[i]))
     return e2b, np.asarray(entries, dtype=np.int32), np.asarray(dists)
 
 

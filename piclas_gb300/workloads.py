@@ -56,6 +56,7 @@ class Workload:
     sf_dir: int = 1                 # PIC-shapefunction-direction
     sf_depo3d: bool = True          # PIC-shapefunction-3D-deposition
     time_step_factor: tuple | None = None   # Species(s)%TimeStepFactor per species (None: 1)
+    periodic_tracing: bool = False          # RefTracking: periodic sides traced as BC sides (CartesianPeriodic = F)
     info: dict = field(default_factory=dict)
 
     @property
@@ -69,7 +70,7 @@ class Workload:
                                 external_field=self.external_field, sf_radius=self.sf_radius,
                                 sf_alpha=self.sf_alpha, sort_interval=sort_interval, sf_dim=self.sf_dim,
                                 sf_dir=self.sf_dir, sf_depo3d=self.sf_depo3d,
-                                time_step_factor=self.time_step_factor)
+                                time_step_factor=self.time_step_factor, periodic_tracing=self.periodic_tracing)
 
 
 # --------------------------------------------------------------------------------------

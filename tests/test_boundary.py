@@ -81,5 +81,6 @@ def test_time_step_factor_above_one_rejected(lib):
 
 def test_struct_sizes_match_c():
     # pic_config_t: 6 ints + 3*8 + 6 doubles + 2 doubles + 5 ints + 4 bytes tail padding (8-byte alignment)
-    assert C.sizeof(capi.PicConfig) == 6 * 4 + 3 * 8 * 8 + 6 * 8 + 2 * 8 + 5 * 4 + 4 + 8 * 8
+    # ... + time_step_factor[8] + periodic_tracing (int32, 4 bytes tail padding)
+    assert C.sizeof(capi.PicConfig) == 6 * 4 + 3 * 8 * 8 + 6 * 8 + 2 * 8 + 5 * 4 + 4 + 8 * 8 + 4 + 4
     assert C.sizeof(capi.PicStatus) == 24

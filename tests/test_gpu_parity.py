@@ -1064,3 +1064,56 @@ def test_mixed_reftracking_100_steps_against_fp64(gpu_lib, oracle_lib):
     st = oracle_lib.OracleState(g32["part_state"], g32["elem"], w.part_species)
     oracle_lib.map_particles(w.config(), capi.MeshStruct(w.mesh), st)
     assert np.max(np.abs(g32["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
+
+
+# ---- RefTracking with periodic sides traced as BC sides (periodic_tracing, CartesianPeriodic = F) ---------
+@pytest.mark.parametrize("bc", [("periodic", "periodic", "periodic"), ("reflective", "periodic", "periodic"),
+                                ("open", "reflective", "periodic")])
+def test_periodic_tracing_against_oracle(gpu_lib, oracle_lib, bc):
+    """The reference's default periodic RefTracking: periodic sides are BC sides of ParticleBCTracking, a
+    crossing moves the particle by the periodic vector into the neighbour element (PeriodicBoundary), also
+    together with open and reflective walls.  FP64 bit-exact against the oracle over 8 fast steps on curved
+    boxes; mixed within 1e-6 m of it with at most two differing element ids."""
+    mesh = build_box_mesh(6, 6, 6, 2, perturb=0.05, bc=bc, periodic_tracing=True)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=4000, T_eV=3000.0, seed=93, dt=1e-10)
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(93))
+    w.part_state[:, :3] = x
+    w.elem = e
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    w.periodic_tracing = True
+    g = _run_gpu(w, 8)
+    st, PS = _run_oracle(oracle_lib, w, 8)
+    assert np.array_equal(g["inside"], st.inside) and np.array_equal(g["elem"], st.elem)
+    assert np.array_equal(g["part_state"], st.part_state)
+    assert np.max(np.abs(g["part_pos_ref"] - st.part_pos_ref)) <= 1e-12
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert st.counters.n_ref_tolerance == 0 and g["status"]["error_word"] == 0
+    if bc[0] == "open":
+        assert (st.inside == 0).sum() > 30                   # the open wall removed particles
+    gm = _run_gpu(w, 8, precision=capi.PIC_PREC_MIXED)
+    k = (gm["inside"] == 1) & (st.inside == 1)
+    assert (gm["elem"][k] != st.elem[k]).sum() <= 2
+    d = gm["part_state"][k, :3] - st.part_state[k, :3]
+    d -= np.round(d)                                          # a particle may sit on either side of a period
+    assert np.max(np.abs(d)) < 1e-6
+
+
+def test_periodic_tracing_curved_32cube(gpu_lib, oracle_lib):
+    """The benchmark's 32^3 curved mesh (RefTracking + shape function, B_z = 0.1 T) with the periodic sides
+    traced as BC sides: 200k particles, 2 steps, element ids exact, state within 1e-13, PartSource within
+    1e-12 of the oracle's."""
+    import os
+    mesh = build_box_mesh(32, 32, 32, 3, perturb=0.05, periodic_tracing=True)
+    w = workloads.curved_two_species(mesh=mesh, n_per_species=100_000, seed=94, nsteps=2)
+    w.periodic_tracing = True
+    g = _run_gpu(w, 2)
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.map_particles(cfg, ms, st, os.cpu_count() or 1)
+    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, 2, PS, os.cpu_count() or 1)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
+    assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0

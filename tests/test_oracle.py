@@ -709,3 +709,69 @@ def test_timing_build_matches_checker(oracle_lib):
         assert np.array_equal(a.elem, b.elem)
         assert np.max(np.abs(a.part_state - b.part_state)) <= 1e-10 * np.max(np.abs(a.part_state))
         assert np.max(np.abs(pa - pb)) <= 1e-10 * np.max(np.abs(pa))
+
+
+# ---- RefTracking with periodic sides traced as BC sides (CartesianPeriodic = F) ------------------------
+def _periodic_tracing_steps(oracle_lib, w, nsteps, tracing):
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    w.periodic_tracing = tracing
+    cfg, ms = w.config(), capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species, is_new=np.zeros(w.n, np.uint8))
+    oracle_lib.map_particles(cfg, ms, st)
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, nsteps)
+    return st
+
+
+def test_periodic_tracing_lists_hold_the_periodic_sides():
+    m = build_box_mesh(4, 4, 4, 1, perturb=0.05, periodic_tracing=True)
+    e2b, loc, dist = m.elem_to_bc_sides, m.bc_side_elem_loc, m.bc_side_distance
+    per = {(e + 1, s + 1) for e in range(m.n_elems) for s in range(6) if m.side_pvid[e, s] != 0}
+    assert len(per) == 6 * 16
+    for e in range(m.n_elems):
+        n, f = e2b[e]
+        own = {(e + 1, s + 1) for s in range(6) if m.side_pvid[e, s] != 0}
+        if n < 0:
+            assert not own
+            continue
+        ent = [tuple(x) for x in loc[f:f + n]]
+        assert own <= set(ent) and set(ent) <= per and len(set(ent)) == n
+        assert np.all(np.diff(dist[f:f + n]) >= 0.0)
+
+
+def test_periodic_tracing_matches_cartesian_periodic(oracle_lib):
+    """The reference's default periodic RefTracking (periodic sides traced as BC sides, PeriodicBoundary) and
+    the CartesianPeriodic/FastPeriodic variant move particles across the periodic box alike: the same elements,
+    velocities identical, positions equal up to the rounding of the two shift formulas."""
+    mesh = build_box_mesh(6, 6, 6, 2, perturb=0.05, periodic_tracing=True)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=4000, T_eV=3000.0, seed=91, dt=1e-10)
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(91))
+    w.part_state[:, :3] = x
+    w.elem = e
+    a = _periodic_tracing_steps(oracle_lib, w, 12, False)
+    b = _periodic_tracing_steps(oracle_lib, w, 12, True)
+    assert np.array_equal(a.elem, b.elem)
+    assert np.array_equal(a.part_state[:, 3:], b.part_state[:, 3:])
+    assert np.max(np.abs(a.part_state[:, :3] - b.part_state[:, :3])) < 1e-13
+    assert np.max(np.abs(a.part_pos_ref - b.part_pos_ref)) < 1e-10
+    assert b.counters.n_ref_tolerance == 0 and b.inside.all()
+    crossed = np.any(np.abs(b.part_state[:, :3] - (w.part_state[:, :3] + w.part_state[:, 3:] * w.dt * 12)) > 0.5, axis=1)
+    assert crossed.sum() > 200                              # many particles crossed a periodic side
+
+
+def test_periodic_tracing_with_walls_free_streaming(oracle_lib):
+    """Reflective walls in x, periodic y and z traced as BC sides, no field: every particle follows the straight
+    line folded at x = 0, 1 and wrapped in y, z, and ends in the element that holds it."""
+    mesh = build_box_mesh(5, 4, 4, 2, bc=("reflective", "periodic", "periodic"), periodic_tracing=True)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=4000, T_eV=3000.0, seed=92, dt=2e-10)
+    w.e_dof[:] = 0.0
+    K = 20
+    st = _periodic_tracing_steps(oracle_lib, w, K, True)
+    assert st.inside.all() and st.counters.n_ref_tolerance == 0
+    xs = w.part_state[:, :3] + w.part_state[:, 3:] * (w.dt * K)
+    u = np.mod(xs[:, 0], 2.0)
+    fx = np.where(u > 1.0, 2.0 - u, u)
+    want = np.stack([fx, np.mod(xs[:, 1], 1.0), np.mod(xs[:, 2], 1.0)], axis=1)
+    d = st.part_state[:, :3] - want
+    d[:, 1:] -= np.round(d[:, 1:])                           # y, z: modulo the period
+    assert np.max(np.abs(d)) < 1e-12
+    assert np.array_equal(st.elem, workloads._elem_of_uniform(w.mesh, st.part_state[:, :3]))
