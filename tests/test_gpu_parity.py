@@ -1117,3 +1117,43 @@ def test_periodic_tracing_curved_32cube(gpu_lib, oracle_lib):
     assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
     assert _rel(g["PS"], PS) <= 1e-12
     assert g["status"]["error_word"] == 0
+
+
+# ---- the 32-instance mixed-precision batch --------------------------------------------------------------
+def test_batch_instances_mixed_vs_fp64_and_concurrent(gpu_lib):
+    """Eight instances of the mixed-precision batch (the batch's own meshes, amplitudes and seeds, particle
+    counts capped at 200k, 30 steps): each instance's mixed charge density within 1e-6 of its FP64 run, and the
+    eight mixed contexts run concurrently, each on its own stream with all launches enqueued before any
+    synchronisation, end with the same element ids and states as the same contexts run one after another
+    (contexts carry their own constants) and PartSource within 1e-12 (node-sum atomic order)."""
+    inst = workloads.batch_instances(32)[:8]
+    ws = [workloads.plasma_wave(n_cells=p["n_cells"], N=3, n_particles=min(p["n_particles"], 200_000),
+                                amp=p["amp"], seed=p["seed"], nsteps=30) for p in inst]
+    seq = []
+    for w in ws:
+        g32 = _run_gpu(w, w.nsteps, precision=capi.PIC_PREC_MIXED, sort_interval=10)
+        g64 = _run_gpu(w, w.nsteps, precision=capi.PIC_PREC_FP64, sort_interval=10)
+        err = float(np.max(np.abs(g32["PS"][..., 3] - g64["PS"][..., 3])) / np.max(np.abs(g64["PS"][..., 3])))
+        assert err <= 1e-6, (w.mesh.n_elems, w.n, err)
+        assert (g32["elem"] != g64["elem"]).sum() <= 2
+        assert g32["status"]["error_word"] == 0
+        seq.append(g32)
+    loops, out = [], []
+    for w in ws:
+        lp = ParticleLoop(w.config(precision=capi.PIC_PREC_MIXED, sort_interval=10), w.mesh)
+        lp.set_field(w.e_dof)
+        lp.upload_particles(w.part_state, w.elem, w.part_species)
+        loops.append(lp)
+    for lp in loops:
+        lp.synchronize()
+    PSs = [np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4)) for w in ws]
+    for lp, w in zip(loops, ws):
+        lp.time_step(w.dt, w.nsteps - 1)           # enqueued on each context's stream, no wait in between
+    for lp, w, PS in zip(loops, ws, PSs):
+        lp.time_step(w.dt, 1, PS)
+    for lp, PS, g in zip(loops, PSs, seq):
+        c = lp.download_particles()
+        assert np.array_equal(c["elem"], g["elem"])
+        assert np.array_equal(c["part_state"], g["part_state"])
+        assert _rel(PS, g["PS"]) <= 1e-12
+        lp.close()
