@@ -94,7 +94,7 @@ enum { PIC_PREC_FP64 = 0, PIC_PREC_MIXED = 1 };            /* arithmetic variant
 
 /* Run-time options (the ini parameters the path reads). */
 typedef struct pic_config_t {
-  int32_t n_dg;                 /* N: DG polynomial degree (1..5)                       */
+  int32_t n_dg;                 /* N: DG polynomial degree (1..4; NMax with p-adaption)  */
   int32_t tracking;             /* PIC_TRACK_*                                          */
   int32_t deposition;           /* PIC_DEPO_*                                           */
   int32_t precision;            /* PIC_PREC_*                                           */
@@ -129,6 +129,11 @@ typedef struct pic_config_t {
    * (BuildBCElemDistance counts every side with SIDE_BCID > 0); open/reflective walls may then be combined
    * with periodic sides. */
   int32_t periodic_tracing;
+  /* RefMappingGuess, the start value of the Newton x -> xi (GetRefNewtonStartValue, eval_xyz.f90:498-612):
+   * 1 = linear pseudo-Cartesian coordinates (the reference's default on linear meshes, particle_mesh.f90:
+   * 350-366), 2 = xi of the element's closest Gauss point (Elem_xGP at the element's degree), 3 = xi of the
+   * closest XCL_NGeo point (the corners at NGeo = 1), 4 = (0,0,0); 0 = 1. */
+  int32_t ref_mapping_guess;
 } pic_config_t;
 
 /* Mesh arrays as the reference holds them after init (NGeo = 1 hexahedra).
@@ -196,6 +201,18 @@ typedef struct pic_mesh_t {
   const int32_t* elem_to_bc_sides;
   const int32_t* bc_side_elem_loc;
   const double* bc_side_distance;
+  /* per-element polynomial degree (p-adaption, dg_vars.f90:38): N_DG_Mapping(1:3, nElems) -- row 1 the
+   * element's 0-based offset into the DOF arrays (the running sum of (Nloc+1)^3 over the elements before it,
+   * Set_N_DG_Mapping, mesh_pAdaption.f90:391-414), row 2 its degree Nloc in 1..pic_config_t.n_dg (n_dg is
+   * then NMax), row 3 (the compute-node offset) is not read -- and n_inter = N_Inter(Nloc)%xGP(0:Nloc),
+   * %wGP(0:Nloc), %wBary(0:Nloc) for Nloc = 1..n_dg, one block of 3 (Nloc+1) values per degree in that order.
+   * With a mapping every per-DOF array is packed by row 1 (each element's (0:Nloc)^3 block in turn,
+   * nDofsMapping DOFs in all): elem_xgp, elem_sj, the field of pic_set_field (U_N(e)%E) and PartSource
+   * (PS_N(e)%PartSource); node_volume is CalcCellLocNodeVolumes with each element's own Nloc.  NULL: every
+   * element has degree n_dg, with xgp/wgp/wbary_gp = N_Inter(n_dg).  Rejected by the HDG solve (the
+   * reference builds p-adaption with HDG only on PETSc) and the differentiable loop. */
+  const int32_t* n_dg_mapping;
+  const double* n_inter;
 } pic_mesh_t;
 
 typedef struct pic_status_t {

@@ -65,11 +65,78 @@ void orc_lagrange_polys(double x, int n, const double* xgp, const double* wbary,
 #define NODE(m, c, n)              ((m)->node_coords[((size_t)(n) - 1) * 3 + (c)])
 #define SIDENODE(m, q, s, e)       ((m)->elem_side_node[((size_t)((e) - 1) * 6 + (s)) * 4 + (q)])
 
+/* per-element polynomial degree: Nloc = N_DG_Mapping(2,e) and the DOF offset N_DG_Mapping(1,e) (dg_vars.f90:38,
+ * set by Set_N_DG_Mapping, mesh_pAdaption.f90:391-414); without a mapping every element has degree N */
+static int elem_n(const pic_mesh_t* m, int N, int e) {
+  return m->n_dg_mapping ? m->n_dg_mapping[(size_t)(e - 1) * 3 + 1] : N;
+}
+static size_t dof_off(const pic_mesh_t* m, int N, int e) {
+  return m->n_dg_mapping ? (size_t)m->n_dg_mapping[(size_t)(e - 1) * 3] : (size_t)(e - 1) * (N + 1) * (N + 1) * (N + 1);
+}
+/* N_Inter(Nloc)%xGP (which 0), %wGP (1), %wBary (2) */
+static const double* n_inter(const pic_mesh_t* m, int nloc, int which) {
+  if (!m->n_dg_mapping) return which == 0 ? m->xgp : which == 1 ? m->wgp : m->wbary_gp;
+  return m->n_inter + (size_t)3 * ((nloc - 1) * (nloc + 2) / 2) + (size_t)which * (nloc + 1);
+}
+size_t orc_n_dofs(const pic_mesh_t* m, int N) {
+  const int nl = elem_n(m, N, m->n_elems);
+  return dof_off(m, N, m->n_elems) + (size_t)(nl + 1) * (nl + 1) * (nl + 1);
+}
+
 /* ---------------------------------------------------------------------------------------
  * Reference mapping x -> xi (eval_xyz.f90)
  * ------------------------------------------------------------------------------------- */
-/* GetRefNewtonStartValue, RefMappingGuess = 1, eval_xyz.f90:549-562 */
+static int elem_n(const pic_mesh_t* m, int N, int e);
+static size_t dof_off(const pic_mesh_t* m, int N, int e);
+static const double* n_inter(const pic_mesh_t* m, int nloc, int which);
+
+/* GetRefNewtonStartValue, eval_xyz.f90:498-612: RefMappingGuess 1 (linear pseudo-Cartesian coordinates,
+ * :549-562), 2 (xi of the closest Gauss point of the element's degree, :564-583), 3 (xi of the closest XCL_NGeo
+ * point, :585-601), 4 (zero, :603-605) */
 static void ref_newton_start(const pic_config_t* cfg, const pic_mesh_t* m, const double x[3], double xi[3], int e) {
+  const int guess = cfg->ref_mapping_guess ? cfg->ref_mapping_guess : 1;
+  if (guess == 2) {
+    const int nl = elem_n(m, cfg->n_dg, e), n1 = nl + 1;
+    const double* xg = n_inter(m, nl, 0);
+    const double* P = &m->elem_xgp[dof_off(m, cfg->n_dg, e) * 3];
+    double d0[3] = {x[0] - P[0], x[1] - P[1], x[2] - P[2]};
+    double winner = sqrt(d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
+    xi[0] = xi[1] = xi[2] = xg[0];
+    for (int i = 0; i <= nl; ++i)
+      for (int j = 0; j <= nl; ++j)
+        for (int k = 0; k <= nl; ++k) {
+          const double* Q = &P[(size_t)(k * n1 * n1 + j * n1 + i) * 3];
+          double dX = fabs(x[0] - Q[0]);
+          if (dX > winner) continue;
+          double dY = fabs(x[1] - Q[1]);
+          if (dY > winner) continue;
+          double dZ = fabs(x[2] - Q[2]);
+          if (dZ > winner) continue;
+          double dist = sqrt(dX * dX + dY * dY + dZ * dZ);
+          if (dist < winner) { winner = dist; xi[0] = xg[i]; xi[1] = xg[j]; xi[2] = xg[k]; }
+        }
+    return;
+  }
+  if (guess == 3) {
+    double d0[3] = {x[0] - XCL(m, 0, 0, 0, 0, e), x[1] - XCL(m, 1, 0, 0, 0, e), x[2] - XCL(m, 2, 0, 0, 0, e)};
+    double winner = sqrt(d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
+    const double* xc = m->xi_cl_ngeo;
+    xi[0] = xi[1] = xi[2] = xc[0];
+    for (int i = 0; i <= 1; ++i)
+      for (int j = 0; j <= 1; ++j)
+        for (int k = 0; k <= 1; ++k) {
+          double dX = fabs(x[0] - XCL(m, 0, i, j, k, e));
+          if (dX > winner) continue;
+          double dY = fabs(x[1] - XCL(m, 1, i, j, k, e));
+          if (dY > winner) continue;
+          double dZ = fabs(x[2] - XCL(m, 2, i, j, k, e));
+          if (dZ > winner) continue;
+          double dist = sqrt(dX * dX + dY * dY + dZ * dZ);
+          if (dist < winner) { winner = dist; xi[0] = xc[i]; xi[1] = xc[j]; xi[2] = xc[k]; }
+        }
+    return;
+  }
+  if (guess == 4) { xi[0] = xi[1] = xi[2] = 0.0; return; }
   const double epsOne = 1.0 + cfg->refmapping_eps;
   double Ptild[3], xil[6];
   for (int c = 0; c < 3; ++c) Ptild[c] = x[c] - m->elem_bary[(size_t)(e - 1) * 3 + c];
@@ -191,6 +258,8 @@ void orc_evaluate_field_at_ref_pos(const double xi[3], int N, const double* xgp,
 
 /* GetEMFieldDW, pic_interpolation_tools.f90:458-527 (components 1:3) */
 static void get_em_field_dw(const pic_mesh_t* m, int N, int e, const double* Ue, const double x[3], double out[3]) {
+  const size_t e0 = dof_off(m, N, e);
+  N = elem_n(m, N, e);
   const int n1 = N + 1, ndof = n1 * n1 * n1;
   double dist[512];
   for (int r = 0; r < ndof; ++r) dist[r] = 0.0;
@@ -200,7 +269,7 @@ static void get_em_field_dw(const pic_mesh_t* m, int N, int e, const double* Ue,
     for (int l = 0; l <= N; ++l)
       for (int mm = 0; mm <= N; ++mm) {
         int r = k + n1 * (l + n1 * mm);
-        const double* xg = &m->elem_xgp[((size_t)(e - 1) * ndof + r) * 3];
+        const double* xg = &m->elem_xgp[(e0 + r) * 3];
         double v0 = xg[0] - x[0], v1 = xg[1] - x[1], v2 = xg[2] - x[2];
         double norm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
         if (norm > 0.0) {
@@ -227,7 +296,7 @@ static void get_em_field_dw(const pic_mesh_t* m, int N, int e, const double* Ue,
  * ------------------------------------------------------------------------------------- */
 static void interpolate_single(const pic_config_t* cfg, const pic_mesh_t* m, const double* e_dof, orc_particles_t* p,
                                int ip, int64_t* nfail) {
-  const int N = cfg->n_dg, ndof = (N + 1) * (N + 1) * (N + 1);
+  const int N = cfg->n_dg;
   double* F = &p->field[(size_t)ip * 6];
   const double* x = &p->part_state[(size_t)ip * 6];
   const int e = p->elem[ip];
@@ -241,11 +310,12 @@ static void interpolate_single(const pic_config_t* cfg, const pic_mesh_t* m, con
     for (int d = 0; d < 3; ++d) xi[d] = p->part_pos_ref[(size_t)ip * 3 + d];
   }
   double Eo[3];
-  const double* Ue = &e_dof[(size_t)(e - 1) * ndof * 3];
+  const double* Ue = &e_dof[dof_off(m, N, e) * 3];
+  const int nl = elem_n(m, N, e);   /* Nloc = N_DG_Mapping(2,ElemID), pic_interpolation_tools.f90:430 */
   if (!suc && cfg->deposition == PIC_DEPO_CVWM)
     get_em_field_dw(m, N, e, Ue, x, Eo);
   else
-    orc_evaluate_field_at_ref_pos(xi, N, m->xgp, m->wbary_gp, Ue, Eo);
+    orc_evaluate_field_at_ref_pos(xi, nl, n_inter(m, nl, 0), n_inter(m, nl, 2), Ue, Eo);
   for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
   /* components 4:6 of GetEMField are zero for PP_nVar = 1 */
   for (int c = 3; c < 6; ++c) F[c] = F[c] + 0.0;
@@ -1096,7 +1166,7 @@ static void cvwm_particle(const pic_config_t* cfg, const pic_mesh_t* m, const or
 /* DepositionMethod_CVWM, pic_depo_method.f90:373-744 */
 static int deposit_cvwm(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* PS, orc_counters_t* c,
                         int nthreads) {
-  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const int N0 = cfg->n_dg;
   const size_t nn = (size_t)m->n_nodes * 4;
   int nt = nthreads > 0 ? nthreads : 1;
   double* NS = (double*)calloc(nn * (size_t)nt, sizeof(double));
@@ -1128,11 +1198,14 @@ static int deposit_cvwm(const pic_config_t* cfg, const pic_mesh_t* m, orc_partic
     double V = m->node_volume[node];
     if (V > 0.0) for (int v = 0; v < 4; ++v) NS[(size_t)node * 4 + v] = NS[(size_t)node * 4 + v] / V;
   }
-  double Fac[8];
-  for (int i = 0; i <= N; ++i) Fac[i] = (m->xgp[i] + 1.0) / 2.0;     /* pic_depo.f90:274-275 */
   for (int e = 1; e <= m->n_elems; ++e) {                            /* :710-733 */
+    /* CellVolWeight(Nloc)%Fac, pic_depo.f90:274-275, with Nloc = N_DG_Mapping(2,e) (:714) */
+    const int N = elem_n(m, N0, e), n1 = N + 1;
+    const double* xgp = n_inter(m, N, 0);
+    double Fac[8];
+    for (int i = 0; i <= N; ++i) Fac[i] = (xgp[i] + 1.0) / 2.0;
     const int32_t* ni = &m->node_info[(size_t)(e - 1) * 8];
-    double* ps = &PS[(size_t)(e - 1) * ndof * 4];
+    double* ps = &PS[dof_off(m, N0, e) * 4];
     for (int kk = 0; kk <= N; ++kk)
       for (int ll = 0; ll <= N; ++ll)
         for (int mm = 0; mm <= N; ++mm) {
@@ -1244,7 +1317,7 @@ static void sf_shifted(const sf_geom_t* g, const pic_mesh_t* m, int ic, const do
 /* depoChargeOnDOFsSF, pic_depo_shapefunction_tools.f90:292-422 */
 static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], const double Fac[4],
                                    double r_sf, double r2_sf, double r2_sf_inv, double* PS, uint8_t* done) {
-  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const int N0 = cfg->n_dg;
   const sf_geom_t g = sf_geom(cfg);
   memset(done, 0, (size_t)m->n_elems);
   int kmax = (int)ceil((P[0] + r_sf - m->xmin_glob[0]) / m->fibgm_deltas[0]);
@@ -1279,8 +1352,9 @@ static void depo_charge_on_dofs_sf(const pic_config_t* cfg, const pic_mesh_t* m,
           const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
           const double vb[3] = {P[0] - b[0], P[1] - b[1], P[2] - b[2]};
           if (sf_norm(&g, vb) > (r_sf + m->elem_radius[e - 1])) continue;
-          const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
-          double* ps = &PS[(size_t)(e - 1) * ndof * 4];
+          const int N = elem_n(m, N0, e), n1 = N + 1;       /* Nloc, offSetDof: :398-399 */
+          const double* xg = &m->elem_xgp[dof_off(m, N0, e) * 3];
+          double* ps = &PS[dof_off(m, N0, e) * 4];
           for (int mz = 0; mz <= N; ++mz)
             for (int l = 0; l <= N; ++l)
               for (int k = 0; k <= N; ++k) {
@@ -1320,7 +1394,7 @@ static void sf_cell_range(const sf_geom_t* g, const pic_mesh_t* m, const double 
  * term by term to the running total (totalChargePeriodicSF is INOUT across the periodic cases) */
 static double total_charge_cc(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], double Fac4,
                               double totalCharge, double r_sf, double r2_sf, double r2_sf_inv, uint8_t* done) {
-  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const int N0 = cfg->n_dg;
   const sf_geom_t g = sf_geom(cfg);
   memset(done, 0, (size_t)m->n_elems);
   int lo[3], hi[3];
@@ -1336,8 +1410,10 @@ static double total_charge_cc(const pic_config_t* cfg, const pic_mesh_t* m, cons
           const double* b = &m->elem_bary[(size_t)(e - 1) * 3];
           const double vb[3] = {P[0] - b[0], P[1] - b[1], P[2] - b[2]};
           if (sf_norm(&g, vb) > (r_sf + m->elem_radius[e - 1])) continue;
-          const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
-          const double* sj = &m->elem_sj[(size_t)(e - 1) * ndof];
+          const int N = elem_n(m, N0, e), n1 = N + 1;       /* Nloc, offSetDof(Node): :530-532 */
+          const double* wgp = n_inter(m, N, 1);
+          const double* xg = &m->elem_xgp[dof_off(m, N0, e) * 3];
+          const double* sj = &m->elem_sj[dof_off(m, N0, e)];
           for (int mz = 0; mz <= N; ++mz)
             for (int l = 0; l <= N; ++l)
               for (int k = 0; k <= N; ++k) {
@@ -1348,7 +1424,7 @@ static double total_charge_cc(const pic_config_t* cfg, const pic_mesh_t* m, cons
                   double S = 1.0 - r2_sf_inv * radius2;
                   double S1 = S * S;
                   for (int ex = 3; ex <= cfg->sf_alpha; ++ex) S1 = S * S1;
-                  totalCharge = totalCharge + m->wgp[k] * m->wgp[l] * m->wgp[mz] * Fac4 * S1 / sj[r];
+                  totalCharge = totalCharge + wgp[k] * wgp[l] * wgp[mz] * Fac4 * S1 / sj[r];
                 }
               }
           done[e - 1] = 1;
@@ -1412,7 +1488,7 @@ static int build_elem_to_elem(const pic_mesh_t* m, int** off_out, int** info_out
 static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const double P[3], const double Fac[4],
                             double r_sf, double r2_sf, double r2_sf_inv, int divide, double total_div,
                             const int* list, int nlist, double* PS, uint8_t* done, int* used) {
-  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
+  const int N0 = cfg->n_dg;
   const sf_geom_t g = sf_geom(cfg);
   memset(done, 0, (size_t)m->n_elems);
   int nused = 0;
@@ -1429,9 +1505,11 @@ static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const 
         const double vb[3] = {P[0] - b[0], P[1] - b[1], P[2] - b[2]};
         if (sf_norm(&g, vb) > (r_sf + m->elem_radius[e - 1])) continue;
       }
-      const double* xg = &m->elem_xgp[(size_t)(e - 1) * ndof * 3];
-      const double* sj = &m->elem_sj[(size_t)(e - 1) * ndof];
-      double* ps = &PS[(size_t)(e - 1) * ndof * 4];
+      const int N = elem_n(m, N0, e), n1 = N + 1;           /* Nloc, offSetDof(Node): :682-684 */
+      const double* wgp = n_inter(m, N, 1);
+      const double* xg = &m->elem_xgp[dof_off(m, N0, e) * 3];
+      const double* sj = &m->elem_sj[dof_off(m, N0, e)];
+      double* ps = &PS[dof_off(m, N0, e) * 4];
       int hit = 0;
       for (int mz = 0; mz <= N; ++mz)
         for (int l = 0; l <= N; ++l)
@@ -1445,7 +1523,7 @@ static void depo_charge_con(const pic_config_t* cfg, const pic_mesh_t* m, const 
             double S1 = S * S;
             for (int ex = 3; ex <= cfg->sf_alpha; ++ex) S1 = S * S1;
             if (!pass) {
-              totalCharge = totalCharge + m->wgp[k] * m->wgp[l] * m->wgp[mz] * (Fac[3] * S1) / sj[r];
+              totalCharge = totalCharge + wgp[k] * wgp[l] * wgp[mz] * (Fac[3] * S1) / sj[r];
             } else {
               for (int v = 0; v < 4; ++v) ps[(size_t)r * 4 + v] = ps[(size_t)r * 4 + v] + alpha * (Fac[v] * S1);
             }
@@ -1483,8 +1561,7 @@ static int fibgm_visit_list(const pic_config_t* cfg, const pic_mesh_t* m, const 
 /* DepositionMethod_SF, pic_depo_method.f90:851-1003 + calcSfSource (shapefunction_tools:30-164);
  * shape_function_cc with periodic images: calcSfSource:96-120 (totalChargePeriodicSF, Fac*Fac(4)/total) */
 static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* PS, int nthreads) {
-  const int N = cfg->n_dg, n1 = N + 1, ndof = n1 * n1 * n1;
-  const size_t nps = (size_t)m->n_elems * ndof * 4;
+  const size_t nps = orc_n_dofs(m, cfg->n_dg) * 4;
   const double r_sf = cfg->sf_radius, r2_sf = r_sf * r_sf, r2_sf_inv = 1.0 / r2_sf;
   const double w_sf = sf_w(cfg, m, r_sf, cfg->sf_alpha);
   int nt = nthreads > 0 ? nthreads : 1;
@@ -1595,8 +1672,7 @@ static int deposit_sf(const pic_config_t* cfg, const pic_mesh_t* m, orc_particle
 
 int orc_deposit(const pic_config_t* cfg, const pic_mesh_t* m, orc_particles_t* p, double* part_source,
                 orc_counters_t* c, int nthreads) {
-  const int n1 = cfg->n_dg + 1;
-  memset(part_source, 0, sizeof(double) * (size_t)m->n_elems * n1 * n1 * n1 * 4);   /* pic_depo.f90:1004-1007 */
+  memset(part_source, 0, sizeof(double) * orc_n_dofs(m, cfg->n_dg) * 4);   /* pic_depo.f90:1004-1007 */
   if (cfg->deposition == PIC_DEPO_CVWM) return deposit_cvwm(cfg, m, p, part_source, c, nthreads);
   return deposit_sf(cfg, m, p, part_source, nthreads);
 }
@@ -1620,19 +1696,24 @@ int orc_step(const pic_config_t* cfg, const pic_mesh_t* m, const double* e_dof, 
   return 0;
 }
 
-/* VerifyDepositedCharge, pic_analyze.f90:72-91 with NAnalyze = N (identity change of basis) */
-double orc_integrate_charge(const pic_mesh_t* m, int N, const double* PS) {
-  const int n1 = N + 1, ndof = n1 * n1 * n1;
+/* VerifyDepositedCharge, pic_analyze.f90:72-91, integrating each element on its own Gauss nodes (NAnalyze =
+ * Nloc, an identity change of basis): the integrand -- the degree-Nloc interpolants of PartSource(4) and
+ * 1/sJ -- has degree 2 Nloc per direction, which both this rule and the reference's NAnalyze grid with
+ * NAnalyze > Nloc integrate exactly, so the two agree up to rounding */
+double orc_integrate_charge(const pic_mesh_t* m, int N0, const double* PS) {
   double total = 0.0;
   for (int e = 0; e < m->n_elems; ++e) {
+    const int N = elem_n(m, N0, e + 1), n1 = N + 1;
+    const double* wgp = n_inter(m, N, 1);
+    const size_t e0 = dof_off(m, N0, e + 1);
     double loc = 0.0;
     for (int mm = 0; mm <= N; ++mm)
       for (int l = 0; l <= N; ++l)
         for (int k = 0; k <= N; ++k) {
           int r = k + n1 * (l + n1 * mm);
-          double J = 1.0 / m->elem_sj[(size_t)e * ndof + r];
-          double w = m->wgp[k] * m->wgp[l] * m->wgp[mm] * J;
-          loc = loc + w * PS[((size_t)e * ndof + r) * 4 + 3];
+          double J = 1.0 / m->elem_sj[e0 + r];
+          double w = wgp[k] * wgp[l] * wgp[mm] * J;
+          loc = loc + w * PS[(e0 + r) * 4 + 3];
         }
     total = total + loc;
   }

@@ -152,9 +152,10 @@ class ParticleLoop:
 
     # -- state hand-over -------------------------------------------------------------------
     def set_field(self, e_dof: np.ndarray):
-        """U_N(e)%E(1:3,0:N,0:N,0:N) for all elements: array (nElems, (N+1)^3, 3)."""
+        """U_N(e)%E(1:3,0:Nloc,0:Nloc,0:Nloc) for all elements: array (nElems, (N+1)^3, 3), or on a p-adapted
+        mesh packed (nDofs, 3) (mesh.dof_shape(3))."""
         e = np.ascontiguousarray(e_dof, dtype=np.float64)
-        if e.size != self.mesh.n_elems * self.nd * 3:
+        if e.size != self.mesh.n_dofs * 3:
             raise ValueError("field has the wrong size")
         self._check(self.lib.pic_set_field(self.handle, capi.dptr(e), self.mesh.n_elems), "pic_set_field")
 
@@ -195,11 +196,12 @@ class ParticleLoop:
         self._check(self.lib.pic_track(self.handle), "pic_track")
 
     def deposition(self, out: np.ndarray | None = None, copy: bool = True):
-        """PS_N(e)%PartSource(1:4,...) for all elements as (nElems, (N+1)^3, 4)."""
+        """PS_N(e)%PartSource(1:4,...) for all elements as (nElems, (N+1)^3, 4), or on a p-adapted mesh packed
+        (nDofs, 4) (mesh.dof_shape(4))."""
         if not copy:
             self._check(self.lib.pic_deposit(self.handle, _null(C.c_double)), "pic_deposit")
             return None
-        ps = out if out is not None else np.zeros((self.mesh.n_elems, self.nd, 4))
+        ps = out if out is not None else np.zeros(self.mesh.dof_shape(4))
         self._check(self.lib.pic_deposit(self.handle, capi.dptr(ps)), "pic_deposit")
         return ps
 

@@ -49,7 +49,7 @@ class PicConfig(C.Structure):
         ("refmapping_eps", C.c_double), ("sf_radius", C.c_double), ("sf_alpha", C.c_int32),
         ("sort_interval", C.c_int32), ("sf_dim", C.c_int32), ("sf_dir", C.c_int32), ("sf_depo3d", C.c_int32),
         ("time_step_factor", C.c_double * PIC_MAX_SPECIES),
-        ("periodic_tracing", C.c_int32),
+        ("periodic_tracing", C.c_int32), ("ref_mapping_guess", C.c_int32),
     ]
 
 
@@ -68,6 +68,7 @@ class PicMesh(C.Structure):
         ("fibgm_offset", _ip), ("fibgm_element", _ip), ("fibgm_n_total", C.c_int32),
         ("side_bc", _ip), ("sf_elem_radius", _dp),
         ("n_bc_entries", C.c_int32), ("elem_to_bc_sides", _ip), ("bc_side_elem_loc", _ip), ("bc_side_distance", _dp),
+        ("n_dg_mapping", _ip), ("n_inter", _dp),
     ]
 
 
@@ -112,9 +113,11 @@ def u8ptr(a: np.ndarray):
 def make_config(n_dg: int, tracking: int, deposition: int, precision: int, species, max_particles: int,
                 external_field=(0.0,) * 6, refmapping_eps: float = 1e-4, sf_radius: float = 0.0,
                 sf_alpha: int = 2, sort_interval: int = 0, sf_dim: int = 3, sf_dir: int = 1,
-                sf_depo3d: bool = True, time_step_factor=None, periodic_tracing: bool = False) -> PicConfig:
+                sf_depo3d: bool = True, time_step_factor=None, periodic_tracing: bool = False,
+                ref_mapping_guess: int = 0) -> PicConfig:
     """species: list of (charge, mass, mpf); time_step_factor: per species (Species%TimeStepFactor), None = 1;
-    periodic_tracing: RefTracking traces periodic sides as BC sides (CartesianPeriodic = F)."""
+    periodic_tracing: RefTracking traces periodic sides as BC sides (CartesianPeriodic = F); ref_mapping_guess:
+    RefMappingGuess 1..4 (0 = 1)."""
     cfg = PicConfig()
     cfg.n_dg = n_dg
     cfg.tracking = tracking
@@ -129,6 +132,7 @@ def make_config(n_dg: int, tracking: int, deposition: int, precision: int, speci
     for s, f in enumerate(time_step_factor or []):
         cfg.time_step_factor[s] = float(f)
     cfg.periodic_tracing = 1 if periodic_tracing else 0
+    cfg.ref_mapping_guess = int(ref_mapping_guess)
     for i in range(6):
         cfg.external_field[i] = float(external_field[i])
     cfg.refmapping_eps = refmapping_eps
@@ -217,6 +221,13 @@ class MeshStruct:
             s.elem_to_bc_sides = C.POINTER(C.c_int32)()
             s.bc_side_elem_loc = C.POINTER(C.c_int32)()
             s.bc_side_distance = C.POINTER(C.c_double)()
+        ndg = getattr(mesh, "n_dg_mapping", None)
+        if ndg is not None:
+            s.n_dg_mapping = i("ndg", ndg)
+            s.n_inter = d("ninter", mesh.n_inter)
+        else:
+            s.n_dg_mapping = C.POINTER(C.c_int32)()
+            s.n_inter = C.POINTER(C.c_double)()
         self.struct = s
         self._keep = keep
 

@@ -133,6 +133,9 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
       return fail(PIC_ERR_INVALID_ARGUMENT, "1D/2D shape functions need a mesh with no or three periodic vectors");
   }
   if (cfg->n_dg < 1 || cfg->n_dg > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg must be 1..4");
+  // 'Wrong guessing method for mapping from physical space in reference space.' (particle_mesh.f90:374-376)
+  if (cfg->ref_mapping_guess < 0 || cfg->ref_mapping_guess > 4)
+    return fail(PIC_ERR_INVALID_ARGUMENT, "ref_mapping_guess must be 1..4 (0: 1)");
   if (cfg->tracking != PIC_TRACK_TRIA && cfg->tracking != PIC_TRACK_REFMAPPING)
     return fail(PIC_ERR_INVALID_ARGUMENT, "unknown tracking method");
   if (cfg->deposition < PIC_DEPO_CVWM || cfg->deposition > PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE)
@@ -182,7 +185,28 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   } else if (sf && !(cfg->sf_radius > 0.0)) {
     return fail(PIC_ERR_INVALID_ARGUMENT, "shape function radius");
   }
+  if (m->n_dg_mapping) {
+    // N_DG_Mapping(1:3,:): degrees 1..NMax and the DOF offsets of Set_N_DG_Mapping (mesh_pAdaption.f90:391-414)
+    if (!m->n_inter) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg_mapping needs n_inter (N_Inter(1..n_dg))");
+    int64_t off = 0;
+    for (int e = 0; e < m->n_elems; ++e) {
+      const int nl = m->n_dg_mapping[(size_t)e * 3 + 1];
+      if (nl < 1 || nl > cfg->n_dg)
+        return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg_mapping: element degrees must lie in 1..n_dg");
+      if (m->n_dg_mapping[(size_t)e * 3] != off)
+        return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg_mapping: DOF offsets must be the running sum of (Nloc+1)^3");
+      off += (int64_t)(nl + 1) * (nl + 1) * (nl + 1);
+      if (off > INT32_MAX) return fail(PIC_ERR_INVALID_ARGUMENT, "n_dg_mapping: more than 2^31 DOFs");
+    }
+  }
   return PIC_OK;
+}
+
+// N_Inter(Nloc)%wGP of element e (N_Inter(N) without a mapping)
+const double* elem_wgp(const pic_ctx* c, const pic_mesh_t* m, int e) {
+  if (!c->var_n) return m->wgp;
+  const int kd = c->elem_n_h[e];
+  return m->n_inter + 3 * ((kd - 1) * (kd + 2) / 2) + (kd + 1);
 }
 
 // Shape-function gather lists: for every target element, the (source element, periodic image)
@@ -191,7 +215,7 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
 // wrapped onto their periodic image.
 int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& dofc, const std::vector<double>& sfx,
                    const bool kdir[3]) {
-  const int ne = m->n_elems, nd = c->nd;
+  const int ne = m->n_elems;
   const double R = c->sf_rmax;
   auto R2src = [&](int s) { const double r = c->adaptive ? m->sf_elem_radius[s] : c->cfg.sf_radius; return r * r; };
   std::vector<double> bmin((size_t)ne * 3), bmax((size_t)ne * 3), dmin((size_t)ne * 3), dmax((size_t)ne * 3);
@@ -202,8 +226,8 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
         double v = m->xcl_ngeo[((size_t)e * 8 + t) * 3 + d];
         lo = std::min(lo, v); hi = std::max(hi, v);
       }
-      for (int r = 0; r < nd; ++r) {
-        double v = sfx[((size_t)e * nd + r) * 3 + d];
+      for (int r = 0; r < c->nd_of(e); ++r) {
+        double v = sfx[((size_t)c->dof_off_h[e] + r) * 3 + d];
         dl = std::min(dl, v); dh = std::max(dh, v);
       }
       bmin[e * 3 + d] = lo; bmax[e * 3 + d] = hi; dmin[e * 3 + d] = dl; dmax[e * 3 + d] = dh;
@@ -286,11 +310,11 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
       const double shv[3] = {sx * Lax[0], sy * Lax[1], sz * Lax[2]};
       // exact-conservative test: min over target DOFs of the distance to the shifted source box
       bool keep = false;
-      for (int r = 0; r < nd && !keep; ++r) {
+      for (int r = 0; r < c->nd_of(e) && !keep; ++r) {
         double d2 = 0.0;
         for (int d = 0; d < 3; ++d) {
           if (!kdir[d]) continue;
-          const double p = sfx[((size_t)e * nd + r) * 3 + d];
+          const double p = sfx[((size_t)c->dof_off_h[e] + r) * 3 + d];
           const double lo = bmin[s * 3 + d] + shv[d], hi = bmax[s * 3 + d] + shv[d];
           const double q = p < lo ? lo - p : (p > hi ? p - hi : 0.0);
           d2 += q * q;
@@ -308,9 +332,12 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
   std::vector<std::pair<uint64_t, int>> mort(ne);
   for (int e = 0; e < ne; ++e) {
     double r2 = 0.0;
-    for (int r = 0; r < nd; ++r) {
+    for (int r = 0; r < c->nd_of(e); ++r) {
       double q = 0.0;
-      for (int d = 0; d < 3; ++d) { double v = sfx[((size_t)e * nd + r) * 3 + d] - dofc[(size_t)e * 3 + d]; q += v * v; }
+      for (int d = 0; d < 3; ++d) {
+        const double v = sfx[((size_t)c->dof_off_h[e] + r) * 3 + d] - dofc[(size_t)e * 3 + d];
+        q += v * v;
+      }
       r2 = std::max(r2, q);
     }
     drad[e] = (float)(std::sqrt(r2) * (1.0 + 1e-6));
@@ -323,14 +350,19 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
     }
     for (int b = 19; b >= 0; --b)
       for (int d = 2; d >= 0; --d) code = (code << 1) | ((ic[d] >> b) & 1u);
+    // p-adapted mesh: grouped by degree (one gather launch per degree), Morton order within a group
+    if (c->var_n) code |= (uint64_t)c->elem_n_h[e] << 60;
     mort[e] = {code, e};
   }
   std::sort(mort.begin(), mort.end());
   std::vector<int> order(ne);
   for (int e = 0; e < ne; ++e) order[e] = mort[e].second;
+  for (int k = 0; k <= kMaxN + 1; ++k) c->sfl.grp_off[k] = 0;
+  for (int e = 0; e < ne; ++e) c->sfl.grp_off[c->elem_n_h[e] + 1]++;
+  for (int k = 1; k <= kMaxN + 1; ++k) c->sfl.grp_off[k] += c->sfl.grp_off[k - 1];
   int* d_off; int* d_src; int8_t* d_sh; double* d_c; float* d_r; int* d_o;
   int rc;
-  if (c->mixed && c->N == 3 && !c->adaptive && pic::sf_gather_variant() == 5) {
+  if (c->mixed && c->N == 3 && !c->var_n && !c->adaptive && pic::sf_gather_variant() == 5) {
     // the particle box of every element relative to its DOF centre (kernel directions only): the corners'
     // bounding box, padded by 5 % of its extent on every side (RefTracking keeps particles within
     // epsOneCell ~ 1 + sqrt(3 RefMappingEps) of the element), for the sub-cell culling of the mixed gather
@@ -353,7 +385,6 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
   }
   if (c->cc) {
     // the pairs transposed to (source -> target, image), and wGP(k) wGP(l) wGP(m) / sJ per DOF
-    const int n1 = c->N + 1;
     std::vector<int> toff(ne + 1, 0), ttgt(src.size());
     std::vector<int8_t> tsh(shift.size());
     for (size_t q = 0; q < src.size(); ++q) toff[src[q] + 1]++;
@@ -365,12 +396,16 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
         ttgt[t] = e;
         for (int d = 0; d < 3; ++d) tsh[3 * (size_t)t + d] = shift[3 * (size_t)q + d];
       }
-    std::vector<double> dw((size_t)ne * nd);
-    for (int e = 0; e < ne; ++e)
-      for (int r = 0; r < nd; ++r) {
+    std::vector<double> dw(c->ndofs);
+    for (int e = 0; e < ne; ++e) {
+      const int n1 = c->elem_n_h[e] + 1;
+      const double* wg = elem_wgp(c, m, e);
+      const size_t b = (size_t)c->dof_off_h[e];
+      for (int r = 0; r < c->nd_of(e); ++r) {
         const int k = r % n1, l = (r / n1) % n1, mm = r / (n1 * n1);
-        dw[(size_t)e * nd + r] = m->wgp[k] * m->wgp[l] * m->wgp[mm] / m->elem_sj[(size_t)e * nd + r];
+        dw[b + r] = wg[k] * wg[l] * wg[mm] / m->elem_sj[b + r];
       }
+    }
     int* d_toff; int* d_ttgt; int8_t* d_tsh; double* d_dw;
     if ((rc = upload(c, &d_toff, toff)) || (rc = upload(c, &d_ttgt, ttgt)) || (rc = upload(c, &d_tsh, tsh)) ||
         (rc = upload(c, &d_dw, dw)))
@@ -522,6 +557,15 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   c->sf_rmax = cfg->sf_radius;
   const int ne = c->ne, nd = c->nd;
   auto bail = [&](int code) { pic_destroy(c); return code; };
+  // degree and DOF offset of every element (N_DG_Mapping rows 2 and 1; e (N+1)^3 without a mapping)
+  c->var_n = m->n_dg_mapping != nullptr;
+  c->elem_n_h.assign(ne, c->N);
+  c->dof_off_h.assign(ne + 1, 0);
+  for (int e = 0; e < ne; ++e) {
+    if (c->var_n) c->elem_n_h[e] = m->n_dg_mapping[(size_t)e * 3 + 1];
+    c->dof_off_h[e + 1] = c->dof_off_h[e] + c->nd_of(e);
+  }
+  c->ndofs = (size_t)c->dof_off_h[ne];
   if (c->adaptive && (cfg->n_dg > 3 || pic::sf_gather_variant() != 5))
     return bail(fail(PIC_ERR_INVALID_ARGUMENT, "shape_function_adaptive needs N <= 3 and the round-robin gather"));
   if (c->adaptive) {
@@ -542,7 +586,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   std::vector<double> rad(m->elem_radius, m->elem_radius + ne);
   std::vector<double> eps1(ne, 1.0);
   if (m->eps_one_cell) eps1.assign(m->eps_one_cell, m->eps_one_cell + ne);
-  std::vector<double> exgp(m->elem_xgp, m->elem_xgp + (size_t)ne * nd * 3);
+  std::vector<double> exgp(m->elem_xgp, m->elem_xgp + c->ndofs * 3);
   std::vector<int> side_nb((size_t)ne * 6);
   std::vector<uint32_t> side_info((size_t)ne * 6);
   for (int e = 0; e < ne; ++e) {
@@ -683,6 +727,12 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   c->M = DevMesh{ne, d_xcl, d_dxcl, d_bary, d_xez, d_slen, d_rad, d_eps1, d_snb, d_sinfo, d_ecan, d_nvol, d_exgp,
                  d_fn, d_fo, d_fe, d_xclr};
   c->M.sf_xgp = d_exgp;
+  if (c->var_n) {
+    int *d_doff = nullptr, *d_en = nullptr;
+    if ((rc = upload(c, &d_doff, c->dof_off_h)) || (rc = upload(c, &d_en, c->elem_n_h))) return bail(rc);
+    c->M.dof_off = d_doff;
+    c->M.elem_n = d_en;
+  }
   if (!bc_e2b.empty()) {
     int* d_be = nullptr;
     double* d_bg = nullptr;
@@ -718,6 +768,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   }
   for (int q = 0; q < 6; ++q) k.ext[q] = cfg->external_field[q];
   k.periodic_tracing = (cfg->tracking == PIC_TRACK_REFMAPPING && cfg->periodic_tracing) ? 1 : 0;
+  k.ref_guess = cfg->ref_mapping_guess ? cfg->ref_mapping_guess : 1;
   k.refmapping_eps = cfg->refmapping_eps > 0.0 ? cfg->refmapping_eps : 1e-4;
   const double c2 = 299792458.0 * 299792458.0;
   k.c2_inv = 1.0 / c2;
@@ -727,6 +778,17 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     k.xgp[i] = m->xgp[i]; k.wbary_gp[i] = m->wbary_gp[i];
     k.fac_gp[i] = (m->xgp[i] + 1.0) / 2.0;    // CellVolWeight%Fac, pic_depo.f90:274-275
     k.xgp_f[i] = (float)m->xgp[i]; k.wbary_gp_f[i] = (float)m->wbary_gp[i];
+  }
+  // the tables per degree: N_Inter(1..NMax) of a p-adapted mesh, else row N = N_Inter(N)
+  for (int kd = 1; kd <= c->N; ++kd) {
+    if (!c->var_n && kd != c->N) continue;
+    const double* xg = c->var_n ? m->n_inter + 3 * ((kd - 1) * (kd + 2) / 2) : m->xgp;
+    const double* wb = c->var_n ? xg + 2 * (kd + 1) : m->wbary_gp;
+    for (int i = 0; i <= kd; ++i) {
+      k.xgp_n[kd][i] = xg[i]; k.wbary_n[kd][i] = wb[i];
+      k.fac_n[kd][i] = (xg[i] + 1.0) / 2.0;   // CellVolWeight(Nloc)%Fac
+      k.xgp_nf[kd][i] = (float)xg[i]; k.wbary_nf[kd][i] = (float)wb[i];
+    }
   }
   k.xi_cl[0] = m->xi_cl_ngeo[0]; k.xi_cl[1] = m->xi_cl_ngeo[1];
   k.wbary_cl[0] = m->wbary_cl_ngeo[0]; k.wbary_cl[1] = m->wbary_cl_ngeo[1];
@@ -758,15 +820,15 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   c->M.k = k;   // travels with every launch (kernel parameter), so contexts do not share constants
 
   // ---- work arrays -------------------------------------------------------------------------------
-  if ((rc = c->alloc(&c->E, (size_t)ne * nd * 3)) || (rc = c->alloc(&c->E32, (size_t)ne * nd * 3)) ||
-      (rc = c->alloc(&c->NS, (size_t)ncanon * 4)) || (rc = c->alloc(&c->PS, (size_t)ne * nd * 4)) ||
+  if ((rc = c->alloc(&c->E, c->ndofs * 3)) || (rc = c->alloc(&c->E32, c->ndofs * 3)) ||
+      (rc = c->alloc(&c->NS, (size_t)ncanon * 4)) || (rc = c->alloc(&c->PS, c->ndofs * 4)) ||
       (rc = c->alloc(&c->st, 1)) || (rc = c->alloc(&c->d_count, 1)) ||
       (rc = c->alloc(&c->sortb.count, ne + 1)) || (rc = c->alloc(&c->sortb.offset, ne + 2)) ||
       (rc = c->alloc(&c->sortb.cursor, ne + 1)))
     return bail(rc);
   c->sortb.ne = ne;
   cudaMemset(c->st, 0, sizeof(DevStatus));
-  cudaMemset(c->PS, 0, sizeof(double) * (size_t)ne * nd * 4);
+  cudaMemset(c->PS, 0, sizeof(double) * c->ndofs * 4);
   if ((rc = alloc_particles(c, c->P, cfg->max_particles, true)) || (rc = alloc_particles(c, c->Q, cfg->max_particles, false)) ||
       (rc = c->alloc(&c->perm, std::max(cfg->max_particles, 1))) || (rc = c->alloc(&c->perm_tmp, std::max(cfg->max_particles, 1))))
     return bail(rc);
@@ -778,7 +840,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     sf_kernel_dirs(cfg, keep);
     std::vector<double> sfx(exgp);
     if (!(keep[0] && keep[1] && keep[2])) {
-      for (size_t q = 0; q < (size_t)ne * nd; ++q)
+      for (size_t q = 0; q < c->ndofs; ++q)
         for (int d = 0; d < 3; ++d)
           if (!keep[d]) sfx[q * 3 + d] = 0.0;
       double* d_sfx = nullptr;
@@ -789,7 +851,10 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     for (int e = 0; e < ne; ++e)
       for (int d = 0; d < 3; ++d) {
         double lo = 1e300, hi = -1e300;
-        for (int r = 0; r < nd; ++r) { double v = sfx[((size_t)e * nd + r) * 3 + d]; lo = std::min(lo, v); hi = std::max(hi, v); }
+        for (int r = 0; r < c->nd_of(e); ++r) {
+          const double v = sfx[((size_t)c->dof_off_h[e] + r) * 3 + d];
+          lo = std::min(lo, v); hi = std::max(hi, v);
+        }
         dofc[(size_t)e * 3 + d] = 0.5 * (lo + hi);
       }
     if ((rc = build_sf_lists(c, m, dofc, sfx, keep))) return bail(rc);
@@ -808,14 +873,18 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   // VerifyDepositedCharge (pic_analyze.f90:41-133): quadrature weight wGP(k) wGP(l) wGP(m) / sJ of every DOF, and the
   // factor of the analytical charge (dimFactorSF for a 1D/2D shape function whose charge sits on a line / area)
   if (m->elem_sj) {
-    std::vector<double> wq((size_t)ne * nd);
-    for (int e = 0; e < ne; ++e)
-      for (int mm = 0; mm < n1; ++mm)
-        for (int l = 0; l < n1; ++l)
-          for (int k = 0; k < n1; ++k) {
-            const int r = k + n1 * (l + n1 * mm);
-            wq[(size_t)e * nd + r] = m->wgp[k] * m->wgp[l] * m->wgp[mm] * (1.0 / m->elem_sj[(size_t)e * nd + r]);
+    std::vector<double> wq(c->ndofs);
+    for (int e = 0; e < ne; ++e) {
+      const int n1e = c->elem_n_h[e] + 1;
+      const double* wg = elem_wgp(c, m, e);
+      const size_t b = (size_t)c->dof_off_h[e];
+      for (int mm = 0; mm < n1e; ++mm)
+        for (int l = 0; l < n1e; ++l)
+          for (int k = 0; k < n1e; ++k) {
+            const int r = k + n1e * (l + n1e * mm);
+            wq[b + r] = wg[k] * wg[l] * wg[mm] * (1.0 / m->elem_sj[b + r]);
           }
+    }
     if ((rc = upload(c, &c->charge_w, wq)) || (rc = c->alloc(&c->charge_elem, ne)) ||
         (rc = c->alloc(&c->charge_out, 1)) || (rc = c->alloc(&c->species_count, PIC_MAX_SPECIES)))
       return bail(rc);
@@ -841,7 +910,7 @@ void pic_destroy(pic_ctx_t* c) {
 int pic_set_field(pic_ctx_t* c, const double* e_dof, int32_t n_elems) {
   if (!c || !e_dof) return fail(PIC_ERR_INVALID_ARGUMENT, "null argument");
   if (n_elems != c->ne) return fail(PIC_ERR_INVALID_ARGUMENT, "n_elems does not match the mesh");
-  const size_t n = (size_t)c->ne * c->nd * 3;
+  const size_t n = c->ndofs * 3;
   CUDA_TRY(cudaMemcpyAsync(c->E, e_dof, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   if (c->mixed) k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->E, c->E32, n);
   CUDA_TRY(cudaGetLastError());
@@ -1021,7 +1090,7 @@ int pic_deposit(pic_ctx_t* c, double* part_source) {
   deposit_device(c);
   CUDA_TRY(cudaGetLastError());
   if (part_source) {
-    CUDA_TRY(cudaMemcpyAsync(part_source, c->PS, sizeof(double) * (size_t)c->ne * c->nd * 4, cudaMemcpyDeviceToHost,
+    CUDA_TRY(cudaMemcpyAsync(part_source, c->PS, sizeof(double) * c->ndofs * 4, cudaMemcpyDeviceToHost,
                              c->stream));
     return device_sync(c);
   }
@@ -1145,7 +1214,7 @@ int pic_step(pic_ctx_t* c, double dt, int32_t nsteps, double* part_source) {
   }
   CUDA_TRY(cudaGetLastError());
   if (part_source) {
-    CUDA_TRY(cudaMemcpyAsync(part_source, c->PS, sizeof(double) * (size_t)c->ne * c->nd * 4, cudaMemcpyDeviceToHost,
+    CUDA_TRY(cudaMemcpyAsync(part_source, c->PS, sizeof(double) * c->ndofs * 4, cudaMemcpyDeviceToHost,
                              c->stream));
     return device_sync(c);
   }

@@ -25,6 +25,12 @@ struct pic_ctx {
   bool cc = false;              // shape_function_cc or _adaptive: per-particle charge normalisation
   bool adaptive = false;        // shape_function_adaptive: radius per source element (SfLists::elem_r)
   double sf_rmax = 0.0;         // largest shape-function radius
+  // per-element polynomial degree (pic_mesh_t.n_dg_mapping): each element's degree and DOF offset (without a
+  // mapping N and e (N+1)^3), and the DOFs of all elements; var_n when the mesh is p-adapted (N is then NMax)
+  bool var_n = false;
+  std::vector<int> elem_n_h, dof_off_h;    // [ne], [ne+1]
+  size_t ndofs = 0;
+  int nd_of(int e) const { const int k = elem_n_h[e] + 1; return k * k * k; }
   cudaStream_t stream = nullptr;
   cudaEvent_t noalloc_done = nullptr;   // orders the context's stream after pic_deposit_cvwm_noalloc
   std::vector<void*> allocs;

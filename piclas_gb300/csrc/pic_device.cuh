@@ -45,6 +45,11 @@ struct Consts {
   int pv_dir[3];                               // periodic vector index per axis (-1: none)
   int sf_keep[3];                              // 1D/2D shape function: 1 in the kernel directions
   int periodic_tracing;                        // RefTracking: periodic sides traced as BC sides (CartesianPeriodic = F)
+  int ref_guess;                               // RefMappingGuess 1..4
+  // N_Inter(k)%xGP, %wBary and CellVolWeight(k)%Fac for every degree k (row k; rows up to NMax are set), FP64
+  // and FP32: the kernels of degree k read row k, so elements of different degrees (p-adaption) share them
+  double xgp_n[kMaxN + 1][kMaxN + 1], wbary_n[kMaxN + 1][kMaxN + 1], fac_n[kMaxN + 1][kMaxN + 1];
+  float xgp_nf[kMaxN + 1][kMaxN + 1], wbary_nf[kMaxN + 1][kMaxN + 1];
 };
 
 // ---- mesh (device arrays) ---------------------------------------------------------------
@@ -74,6 +79,10 @@ struct DevMesh {
   // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
   // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3, [ne][8][3] in that order (from the corners at pic_create)
   const double* tcoef;
+  // per-element polynomial degree (p-adaption): N_DG_Mapping(1,:) as 0-based DOF offsets [ne+1] and
+  // N_DG_Mapping(2,:) [ne]; both null when every element has degree N (DOF offset e (N+1)^3)
+  const int* dof_off;
+  const int* elem_n;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
@@ -150,10 +159,60 @@ __device__ __forceinline__ void lagrange_f(float x, const float* xgp, const floa
 }
 
 // ==========================================================================================
-// x -> xi: GetRefNewtonStartValue (guess 1, eval_xyz.f90:549-562) + RefElemNewton (:298-445)
+// x -> xi: GetRefNewtonStartValue (eval_xyz.f90:498-612) + RefElemNewton (:298-445)
 // ==========================================================================================
+// RefMappingGuess 2 and 3 (:564-601): xi of the closest Gauss point of the element's degree, or of the closest
+// corner (XCL_NGeo at NGeo = 1); distances in the reference's order with its per-axis early exits
+static __device__ __noinline__ void newton_start_closest(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
+  if (kc.ref_guess == 2) {
+    const int nl = M.elem_n ? __ldg(M.elem_n + e) : kc.N, n1 = nl + 1;
+    const double* xg = kc.xgp_n[nl];
+    const double* P = M.elem_xgp + (M.dof_off ? (size_t)__ldg(M.dof_off + e) : (size_t)e * kc.ndof) * 3;
+    const double d0 = x[0] - __ldg(P), d1 = x[1] - __ldg(P + 1), d2 = x[2] - __ldg(P + 2);
+    double winner = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    xi[0] = xi[1] = xi[2] = xg[0];
+    for (int i = 0; i < n1; ++i)
+      for (int j = 0; j < n1; ++j)
+        for (int k = 0; k < n1; ++k) {
+          const double* Q = P + (size_t)(k * n1 * n1 + j * n1 + i) * 3;
+          const double dX = fabs(x[0] - __ldg(Q));
+          if (dX > winner) continue;
+          const double dY = fabs(x[1] - __ldg(Q + 1));
+          if (dY > winner) continue;
+          const double dZ = fabs(x[2] - __ldg(Q + 2));
+          if (dZ > winner) continue;
+          const double dist = sqrt(dX * dX + dY * dY + dZ * dZ);
+          if (dist < winner) { winner = dist; xi[0] = xg[i]; xi[1] = xg[j]; xi[2] = xg[k]; }
+        }
+    return;
+  }
+  const double* X = M.xcl + (size_t)e * 24;      // corner (i, j, k) at tensor index i + 2 j + 4 k
+  const double d0 = x[0] - __ldg(X), d1 = x[1] - __ldg(X + 1), d2 = x[2] - __ldg(X + 2);
+  double winner = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+  xi[0] = xi[1] = xi[2] = kc.xi_cl[0];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j)
+      for (int k = 0; k < 2; ++k) {
+        const double* Q = X + (i + 2 * j + 4 * k) * 3;
+        const double dX = fabs(x[0] - __ldg(Q));
+        if (dX > winner) continue;
+        const double dY = fabs(x[1] - __ldg(Q + 1));
+        if (dY > winner) continue;
+        const double dZ = fabs(x[2] - __ldg(Q + 2));
+        if (dZ > winner) continue;
+        const double dist = sqrt(dX * dX + dY * dY + dZ * dZ);
+        if (dist < winner) { winner = dist; xi[0] = kc.xi_cl[i]; xi[1] = kc.xi_cl[j]; xi[2] = kc.xi_cl[k]; }
+      }
+}
+
 __device__ __forceinline__ void newton_start(const DevMesh& M, int e, const double x[3], double xi[3]) {
   const Consts& kc = M.k;
+  if (kc.ref_guess != 1) {
+    if (kc.ref_guess == 4) { xi[0] = xi[1] = xi[2] = 0.0; return; }
+    newton_start_closest(M, e, x, xi);
+    return;
+  }
   const double epsOne = 1.0 + kc.refmapping_eps;
   const double* b = M.bary + (size_t)e * 3;
   double P0 = x[0] - __ldg(b + 0), P1 = x[1] - __ldg(b + 1), P2 = x[2] - __ldg(b + 2);
@@ -362,7 +421,7 @@ __device__ __forceinline__ void eval_field(const Consts& kc, const double* __res
   constexpr int n1 = N + 1;
   double L[3][n1];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) lagrange<n1>(xi[d], kc.xgp, kc.wbary_gp, L[d]);
+  for (int d = 0; d < 3; ++d) lagrange<n1>(xi[d], kc.xgp_n[N], kc.wbary_n[N], L[d]);
   out[0] = out[1] = out[2] = 0.0;
 #pragma unroll
   for (int k = 0; k < n1; ++k)
@@ -379,15 +438,15 @@ __device__ __forceinline__ void eval_field(const Consts& kc, const double* __res
 }
 
 // GetEMFieldDW, pic_interpolation_tools.f90:458-527 (inverse-distance fallback when Newton failed)
+// (U and xg: the element's field and DOF coordinates)
 template <int N>
-static __device__ __noinline__ void eval_field_dw(const DevMesh& M, const double* __restrict__ U, int e, const double x[3],
-                                          double out[3]) {
+static __device__ __noinline__ void eval_field_dw(const double* __restrict__ U, const double* __restrict__ xg,
+                                                  const double x[3], double out[3]) {
   constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   double dist[nd];
 #pragma unroll
   for (int r = 0; r < nd; ++r) dist[r] = 0.0;
   double DistSum = 0.0;
-  const double* xg = M.elem_xgp + (size_t)e * nd * 3;
   for (int k = 0; k < n1; ++k)
     for (int l = 0; l < n1; ++l)
       for (int mm = 0; mm < n1; ++mm) {
@@ -411,6 +470,51 @@ static __device__ __noinline__ void eval_field_dw(const DevMesh& M, const double
         int r = k + n1 * (l + n1 * mm);
         for (int c = 0; c < 3; ++c) out[c] = out[c] + dist[r] / DistSum * __ldg(U + 3 * r + c);
       }
+}
+
+// ---- per-element polynomial degree (p-adaption) ---------------------------------------------
+// Kernels instantiated for a degree N > 0 address the DOFs of element e at e (N+1)^3, or at its
+// N_DG_Mapping(1,e) offset on a p-adapted mesh (element-parallel kernels run per degree group there).
+// N = 0 instantiates the particle kernels for p-adapted meshes: they dispatch on the element's own degree.
+template <int N>
+__device__ __forceinline__ size_t dof_base(const DevMesh& M, int e) {
+  if constexpr (N == 0) return (size_t)__ldg(M.dof_off + e);
+  else return M.dof_off ? (size_t)__ldg(M.dof_off + e) : (size_t)e * ((N + 1) * (N + 1) * (N + 1));
+}
+
+// EvaluateFieldAtRefPos with Nloc (pic_interpolation_tools.f90:427-433): E of element e at xi
+template <int N>
+__device__ __forceinline__ void field_at(const DevMesh& M, const double* __restrict__ E, int e, const double xi[3],
+                                         double out[3]) {
+  if constexpr (N > 0) {
+    eval_field<N>(M.k, E + (size_t)e * ((N + 1) * (N + 1) * (N + 1)) * 3, xi, out);
+  } else {
+    const double* U = E + (size_t)__ldg(M.dof_off + e) * 3;
+    switch (__ldg(M.elem_n + e)) {
+      case 1: eval_field<1>(M.k, U, xi, out); break;
+      case 2: eval_field<2>(M.k, U, xi, out); break;
+      case 3: eval_field<3>(M.k, U, xi, out); break;
+      default: eval_field<4>(M.k, U, xi, out); break;     // degrees are 1..4 (checked at pic_create)
+    }
+  }
+}
+
+// GetEMFieldDW with Nloc: the inverse-distance fallback of element e at x
+template <int N>
+__device__ __forceinline__ void field_dw_at(const DevMesh& M, const double* __restrict__ E, int e, const double x[3],
+                                            double out[3]) {
+  if constexpr (N > 0) {
+    const size_t b = (size_t)e * ((N + 1) * (N + 1) * (N + 1));
+    eval_field_dw<N>(E + b * 3, M.elem_xgp + b * 3, x, out);
+  } else {
+    const size_t b = (size_t)__ldg(M.dof_off + e);
+    switch (__ldg(M.elem_n + e)) {
+      case 1: eval_field_dw<1>(E + b * 3, M.elem_xgp + b * 3, x, out); break;
+      case 2: eval_field_dw<2>(E + b * 3, M.elem_xgp + b * 3, x, out); break;
+      case 3: eval_field_dw<3>(E + b * 3, M.elem_xgp + b * 3, x, out); break;
+      default: eval_field_dw<4>(E + b * 3, M.elem_xgp + b * 3, x, out); break;
+    }
+  }
 }
 
 // ==========================================================================================
@@ -1282,15 +1386,19 @@ static __global__ void k_node_normalize(const double* __restrict__ node_vol, dou
 
 // Node sums -> DOFs (pic_depo_method.f90:692-733): PartSource(1:4,k,l,m) of every element.
 // NORMALIZED: NS already holds NodeSource / NodeVolume (k_node_normalize ran first).
+// N = 0 (p-adaption): threads cover (NMax+1)^3 DOFs per element; each element uses CellVolWeight(Nloc)%Fac
+// (pic_depo_method.f90:714-720) and writes its (Nloc+1)^3 DOFs at its N_DG_Mapping offset.
 template <int N, bool NORMALIZED = false>
 __global__ void k_node_to_dof(const __grid_constant__ DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
   const Consts& kc = M.k;
-  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int nmax1 = N > 0 ? N + 1 : kc.N + 1, ndmax = nmax1 * nmax1 * nmax1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= M.ne * nd) return;
-  const int e = t / nd, r = t - e * nd;
+  if (t >= M.ne * ndmax) return;
+  const int e = t / ndmax, r = t - e * ndmax;
+  const int nl = N > 0 ? N : __ldg(M.elem_n + e), n1 = nl + 1;
+  if (r >= n1 * n1 * n1) return;
   const int kk = r % n1, ll = (r / n1) % n1, mm = r / (n1 * n1);
-  const double a1 = kc.fac_gp[kk], a2 = kc.fac_gp[ll], a3 = kc.fac_gp[mm];
+  const double a1 = kc.fac_n[nl][kk], a2 = kc.fac_n[nl][ll], a3 = kc.fac_n[nl][mm];
   double S[8][4];
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
@@ -1314,7 +1422,7 @@ __global__ void k_node_to_dof(const __grid_constant__ DevMesh M, const double* _
              S[2][c] * (a1) * (a2) * (1 - a3) + S[3][c] * (1 - a1) * (a2) * (1 - a3) +
              S[4][c] * (1 - a1) * (1 - a2) * (a3) + S[5][c] * (a1) * (1 - a2) * (a3) +
              S[6][c] * (a1) * (a2) * (a3) + S[7][c] * (1 - a1) * (a2) * (a3);
-  double2* o = reinterpret_cast<double2*>(PS + (size_t)t * 4);
+  double2* o = reinterpret_cast<double2*>(PS + (N > 0 ? (size_t)t : dof_base<0>(M, e) + r) * 4);
   o[0] = make_double2(out[0], out[1]);
   o[1] = make_double2(out[2], out[3]);
 }

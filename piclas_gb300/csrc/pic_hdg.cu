@@ -1080,6 +1080,8 @@ extern "C" int pic_hdg_init(pic_ctx_t* c, const pic_hdg_t* g) {
   if (c->hdg) return fail(PIC_ERR_STATE, "HDG already initialised for this context");
   const int N = c->N, nd = N + 1, nv = nd * nd * nd, nf = nd * nd, ne = c->ne;
   if (N < 1 || N > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "the HDG solve supports N = 1..4");
+  // p-adaption with HDG needs PETSc in the reference (mesh_pAdaption.f90:83-85); this solve has one N
+  if (c->var_n) return fail(PIC_ERR_INVALID_ARGUMENT, "the HDG solve needs one polynomial degree for all elements");
   if (g->n_sides <= 0 || !g->elem_to_side || !g->side_to_elem || !g->metrics_f || !g->metrics_g || !g->metrics_h ||
       !g->sj)
     return fail(PIC_ERR_INVALID_ARGUMENT, "pic_hdg_t: missing array");

@@ -19,19 +19,28 @@ namespace pic {
 // ---------------------------------------------------------------------------------------------
 
 
-__device__ __forceinline__ bool position_in_ref_elem_f(const Consts& kc, const MeshF& F, int e, const float p[3], float xi[3]) {
-  const float* B = F.xez + (size_t)e * 18;
-  const float* S = F.slen + (size_t)e * 6;
-  float xil[6];
+// RefMappingGuess 1 in FP32; the other guesses take the FP64 start value of x (newton_start)
+__device__ __forceinline__ bool position_in_ref_elem_f(const DevMesh& M, const MeshF& F, int e, const double x[3],
+                                                       const float p[3], float xi[3]) {
+  const Consts& kc = M.k;
+  if (kc.ref_guess != 1) {
+    double xs[3];
+    newton_start(M, e, x, xs);
+    xi[0] = (float)xs[0]; xi[1] = (float)xs[1]; xi[2] = (float)xs[2];
+  } else {
+    const float* B = F.xez + (size_t)e * 18;
+    const float* S = F.slen + (size_t)e * 6;
+    float xil[6];
 #pragma unroll
-  for (int d = 0; d < 6; ++d)
-    xil[d] = fmaf(p[0], __ldg(B + 3 * d), fmaf(p[1], __ldg(B + 3 * d + 1), p[2] * __ldg(B + 3 * d + 2))) * __ldg(S + d);
+    for (int d = 0; d < 6; ++d)
+      xil[d] = fmaf(p[0], __ldg(B + 3 * d), fmaf(p[1], __ldg(B + 3 * d + 1), p[2] * __ldg(B + 3 * d + 2))) * __ldg(S + d);
 #pragma unroll
-  for (int d = 0; d < 3; ++d) xi[d] = 0.5f * (xil[d] - xil[d + 3]);
-  const float epsOne = 1.0f + (float)kc.refmapping_eps;
-  if (fmaxf(fabsf(xi[0]), fmaxf(fabsf(xi[1]), fabsf(xi[2]))) > epsOne) {
+    for (int d = 0; d < 3; ++d) xi[d] = 0.5f * (xil[d] - xil[d + 3]);
+    const float epsOne = 1.0f + (float)kc.refmapping_eps;
+    if (fmaxf(fabsf(xi[0]), fmaxf(fabsf(xi[1]), fabsf(xi[2]))) > epsOne) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) xi[d] = fmaxf(fminf(1.0f, xi[d]), -1.0f);
+      for (int d = 0; d < 3; ++d) xi[d] = fmaxf(fminf(1.0f, xi[d]), -1.0f);
+    }
   }
   const float* X = F.xclr + (size_t)e * 24;
   const float* DX = F.dxcl + (size_t)e * 72;
@@ -75,7 +84,7 @@ __device__ __forceinline__ void eval_field_f(const Consts& kc, const float* __re
   constexpr int n1 = N + 1;
   float L[3][n1];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) lagrange_f<n1>(xi[d], kc.xgp_f, kc.wbary_gp_f, L[d]);
+  for (int d = 0; d < 3; ++d) lagrange_f<n1>(xi[d], kc.xgp_nf[N], kc.wbary_nf[N], L[d]);
   out[0] = out[1] = out[2] = 0.0f;
 #pragma unroll
   for (int k = 0; k < n1; ++k)
@@ -90,6 +99,23 @@ __device__ __forceinline__ void eval_field_f(const Consts& kc, const float* __re
         for (int c = 0; c < 3; ++c) out[c] = fmaf(__ldg(u + c), w, out[c]);
       }
     }
+}
+
+// FP32 field of element e at xi (mixed variant); N = 0 dispatches on the element's degree (p-adaption)
+template <int N>
+__device__ __forceinline__ void field_at_f(const DevMesh& M, const float* __restrict__ E32, int e, const float xi[3],
+                                           float out[3]) {
+  if constexpr (N > 0) {
+    eval_field_f<N>(M.k, E32 + (size_t)e * ((N + 1) * (N + 1) * (N + 1)) * 3, xi, out);
+  } else {
+    const float* U = E32 + (size_t)__ldg(M.dof_off + e) * 3;
+    switch (__ldg(M.elem_n + e)) {
+      case 1: eval_field_f<1>(M.k, U, xi, out); break;
+      case 2: eval_field_f<2>(M.k, U, xi, out); break;
+      case 3: eval_field_f<3>(M.k, U, xi, out); break;
+      default: eval_field_f<4>(M.k, U, xi, out); break;
+    }
+  }
 }
 
 // FP32 Boris push (mixed variant)
@@ -146,7 +172,6 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
                                                         const float* __restrict__ E32, double* __restrict__ NS,
                                                         double dt, DevStatus* st) {
   const Consts& kc = M.k;
-  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool in_range = i < P.n;
   const uint8_t fl = in_range ? P.flags[i] : 0;
@@ -183,9 +208,8 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     for (int c = 0; c < 6; ++c) Fd[c] = kc.ext[c];
     if (charged) {
       double Eo[3];
-      const double* U = E + (size_t)e * nd * 3;
-      if (suc) eval_field<N>(kc, U, xi, Eo);
-      else eval_field_dw<N>(M, U, e, x, Eo);
+      if (suc) field_at<N>(M, E, e, xi, Eo);
+      else field_dw_at<N>(M, E, e, x, Eo);
 #pragma unroll
       for (int c = 0; c < 3; ++c) Fd[c] = Fd[c] + Eo[c];
 #pragma unroll
@@ -224,7 +248,7 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     if (charged) {
       const double* b = M.bary + (size_t)e * 3;
       const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
-      suc = position_in_ref_elem_f(kc, MF, e, p, xi);
+      suc = position_in_ref_elem_f(M, MF, e, x, p, xi);
       if (!suc) {
         // fall back to the FP64 mapping so that the inverse-distance branch matches the reference's
         double xd[3];
@@ -263,10 +287,10 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_CVWM_MIXED_MINB : PIC_CVWM_MI
     if (charged) {
       float Eo[3];
       if (suc) {
-        eval_field_f<N>(kc, E32 + (size_t)e * nd * 3, xi, Eo);
+        field_at_f<N>(M, E32, e, xi, Eo);
       } else {
         double Ed[3];
-        eval_field_dw<N>(M, E + (size_t)e * nd * 3, e, x, Ed);
+        field_dw_at<N>(M, E, e, x, Ed);
         Eo[0] = (float)Ed[0]; Eo[1] = (float)Ed[1]; Eo[2] = (float)Ed[2];
       }
 #pragma unroll
@@ -309,7 +333,6 @@ __global__ void __launch_bounds__(256) k_interpolate(const __grid_constant__ Dev
                                                      const float* __restrict__ E32, DevStatus* st, bool refmap,
                                                      bool cvwm) {
   const Consts& kc = M.k;
-  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
@@ -331,16 +354,15 @@ __global__ void __launch_bounds__(256) k_interpolate(const __grid_constant__ Dev
     } else {
       xi[0] = P.xi0[i]; xi[1] = P.xi1[i]; xi[2] = P.xi2[i];
     }
-    const double* U = E + (size_t)e * nd * 3;
-    if (!suc && cvwm) eval_field_dw<N>(M, U, e, x, Eo);
-    else eval_field<N>(kc, U, xi, Eo);
+    if (!suc && cvwm) field_dw_at<N>(M, E, e, x, Eo);
+    else field_at<N>(M, E, e, xi, Eo);
   } else {
     float xi[3];
     bool suc = true;
     if (!refmap) {
       const double* b = M.bary + (size_t)e * 3;
       const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
-      suc = position_in_ref_elem_f(kc, MF, e, p, xi);
+      suc = position_in_ref_elem_f(M, MF, e, x, p, xi);
       if (!suc) {
         double xd[3];
         suc = position_in_ref_elem(M, e, x, xd);
@@ -351,10 +373,10 @@ __global__ void __launch_bounds__(256) k_interpolate(const __grid_constant__ Dev
       xi[0] = (float)P.xi0[i]; xi[1] = (float)P.xi1[i]; xi[2] = (float)P.xi2[i];
     }
     if (!suc && cvwm) {
-      eval_field_dw<N>(M, E + (size_t)e * nd * 3, e, x, Eo);
+      field_dw_at<N>(M, E, e, x, Eo);
     } else {
       float Ef[3];
-      eval_field_f<N>(kc, E32 + (size_t)e * nd * 3, xi, Ef);
+      field_at_f<N>(M, E32, e, xi, Ef);
       Eo[0] = Ef[0]; Eo[1] = Ef[1]; Eo[2] = Ef[2];
     }
   }
@@ -487,7 +509,7 @@ __global__ void __launch_bounds__(256) k_deposit_cvwm(const __grid_constant__ De
       const double* b = M.bary + (size_t)e * 3;
       const float p[3] = {(float)(x[0] - __ldg(b)), (float)(x[1] - __ldg(b + 1)), (float)(x[2] - __ldg(b + 2))};
       float xi[3];
-      bool suc = position_in_ref_elem_f(kc, MF, e, p, xi);
+      bool suc = position_in_ref_elem_f(M, MF, e, x, p, xi);
       const float ch = (float)kc.qm[sp];
       const float TS[4] = {P.vxf[i] * ch, P.vyf[i] * ch, P.vzf[i] * ch, ch};
       if (!suc) {
@@ -677,7 +699,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(const __
   __shared__ double s_fac[kSfChunk][4];
   __shared__ float4 s_rel[kSfChunk];
   __shared__ double s_red[split > 1 ? S::threads : 1][4];
-  const int e = blockIdx.x;
+  const int e = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
   const int t = threadIdx.x;
   const int dof = t % nd, part = t / nd;
   const bool active = t < nd * split;
@@ -686,7 +708,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(const __
   double xg[3] = {0, 0, 0};
   float xgf[3] = {0, 0, 0};
   if (active) {
-    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + (dof_base<N>(M, e) + dof) * 3;
     xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
     xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
   }
@@ -753,7 +775,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_fp64(const __
     }
   }
   if (t < nd) {
-    double2* o = reinterpret_cast<double2*>(PS + ((size_t)e * nd + dof) * 4);
+    double2* o = reinterpret_cast<double2*>(PS + (dof_base<N>(M, e) + dof) * 4);
     o[0] = make_double2(acc[0], acc[1]);
     o[1] = make_double2(acc[2], acc[3]);
   }
@@ -769,7 +791,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(const _
   __shared__ float4 s_rel[kSfChunk];
   __shared__ float4 s_fac[kSfChunk];
   __shared__ float s_red[split > 1 ? S::threads : 1][8];
-  const int e = blockIdx.x;
+  const int e = L.order ? __ldg(L.order + blockIdx.x) : blockIdx.x;
   const int t = threadIdx.x;
   const int dof = t % nd, part = t / nd;
   const bool active = t < nd * split;
@@ -777,7 +799,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(const _
   const double cex = __ldg(ce), cey = __ldg(ce + 1), cez = __ldg(ce + 2);
   float xgf[3] = {0, 0, 0};
   if (active) {
-    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + (dof_base<N>(M, e) + dof) * 3;
     xgf[0] = (float)(__ldg(g) - cex); xgf[1] = (float)(__ldg(g + 1) - cey); xgf[2] = (float)(__ldg(g + 2) - cez);
   }
   const float R2 = (float)kc.sf_r2, R2inv = (float)kc.sf_r2_inv;
@@ -843,7 +865,7 @@ __global__ void __launch_bounds__(SfShape<N>::threads) k_sf_gather_mixed(const _
     }
   }
   if (t < nd) {
-    double2* o = reinterpret_cast<double2*>(PS + ((size_t)e * nd + dof) * 4);
+    double2* o = reinterpret_cast<double2*>(PS + (dof_base<N>(M, e) + dof) * 4);
     o[0] = make_double2(acc[0], acc[1]);
     o[1] = make_double2(acc[2], acc[3]);
   }
@@ -882,7 +904,7 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(const __grid_constan
   double xg[3] = {0, 0, 0};
   float xgf[3] = {0, 0, 0};
   if (active) {
-    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + (dof_base<N>(M, e) + dof) * 3;
     xg[0] = __ldg(g); xg[1] = __ldg(g + 1); xg[2] = __ldg(g + 2);
     xgf[0] = (float)(xg[0] - cex); xgf[1] = (float)(xg[1] - cey); xgf[2] = (float)(xg[2] - cez);
   }
@@ -988,7 +1010,7 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(const __grid_constan
   }
   __syncthreads();
   if (active && parity == 0) {
-    double2* o = reinterpret_cast<double2*>(PS + ((size_t)e * nd + dof) * 4);
+    double2* o = reinterpret_cast<double2*>(PS + (dof_base<N>(M, e) + dof) * 4);
     const double* rr = s_red[w & 1][lane];
     o[0] = make_double2(acc[0] + rr[0], acc[1] + rr[1]);
     o[1] = make_double2(acc[2] + rr[2], acc[3] + rr[3]);
@@ -1070,7 +1092,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
   double gd[4] = {0.0, 0.0, 0.0, 0.0};
   float gf[3] = {0.f, 0.f, 0.f};
   if (active) {
-    const double* g = M.sf_xgp + ((size_t)e * nd + dof) * 3;
+    const double* g = M.sf_xgp + (dof_base<N>(M, e) + dof) * 3;
     const double gx = __ldg(g) - cex, gy = __ldg(g + 1) - cey, gz = __ldg(g + 2) - cez;
     gd[0] = gx; gd[1] = gy; gd[2] = gz;
     // B_g = 1 - |g|^2/R^2; adaptive: |g|^2 (the particle's own radius enters at each hit)
@@ -1273,7 +1295,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
       o[c] = s_red[0][t][c];
       for (int k = 1; k < npar; ++k) o[c] = o[c] + s_red[k][t][c];
     }
-    double2* out = reinterpret_cast<double2*>(PS + ((size_t)e * nd + t) * 4);
+    double2* out = reinterpret_cast<double2*>(PS + (dof_base<N>(M, e) + t) * 4);
     out[0] = make_double2(o[0], o[1]);
     out[1] = make_double2(o[2], o[3]);
   }
@@ -1378,7 +1400,6 @@ __global__ void __launch_bounds__(kSf7Threads, 2) k_sf_gather7(const __grid_cons
                                                                const int* __restrict__ off, SfPack K,
                                                                double* __restrict__ PS, DevStatus* st) {
   const Consts& kc = M.k;
-  constexpr int nd = 64;
   extern __shared__ __align__(128) unsigned char sf7_raw[];
   Sf7Smem& S = *reinterpret_cast<Sf7Smem*>(sf7_raw);
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -1393,7 +1414,7 @@ __global__ void __launch_bounds__(kSf7Threads, 2) k_sf_gather7(const __grid_cons
 #pragma unroll
   for (int d = 0; d < 8; ++d) {
     const int r = (2 * ox + (d & 1)) + 4 * ((2 * oy + ((d >> 1) & 1)) + 4 * (2 * oz + (d >> 2)));
-    const double* g = M.sf_xgp + ((size_t)e * nd + r) * 3;
+    const double* g = M.sf_xgp + (dof_base<3>(M, e) + r) * 3;
     gx[d] = (float)(__ldg(g) - cex); gy[d] = (float)(__ldg(g + 1) - cey); gz[d] = (float)(__ldg(g + 2) - cez);
     bg[d] = -R2inv * fmaf(gx[d], gx[d], fmaf(gy[d], gy[d], gz[d] * gz[d]));
     lo3[0] = fminf(lo3[0], gx[d]); hi3[0] = fmaxf(hi3[0], gx[d]);
@@ -1614,7 +1635,7 @@ __global__ void __launch_bounds__(kSf7Threads, 2) k_sf_gather7(const __grid_cons
   // lane k holds value k = 4 d + c of this octant
   const int dl = lane >> 2;
   const int r_out = (2 * ox + (dl & 1)) + 4 * ((2 * oy + ((dl >> 1) & 1)) + 4 * (2 * oz + (dl >> 2)));
-  PS[((size_t)e * nd + r_out) * 4 + (lane & 3)] = (double)hi + (double)lo;
+  PS[(dof_base<3>(M, e) + r_out) * 4 + (lane & 3)] = (double)hi + (double)lo;
 }
 
 // =============================================================================================
@@ -1703,15 +1724,19 @@ __global__ void __launch_bounds__(kCcThreads) k_sf_cc_norm(const __grid_constant
         if (pi >= npair) { s_gf[i] = make_float4(1e30f, 1e30f, 1e30f, 0.0f); continue; }   // never a hit
         const int q = q0 + pi;
         const int e = __ldg(L.t_tgt + q);
+        if (M.elem_n) {          // p-adaption: slots beyond the target's (Nloc+1)^3 DOFs hold no DOF
+          const int nl1 = __ldg(M.elem_n + e) + 1;
+          if (d >= nl1 * nl1 * nl1) { s_gf[i] = make_float4(1e30f, 1e30f, 1e30f, 0.0f); continue; }
+        }
         double sh[3];
 #pragma unroll
         for (int dd = 0; dd < 3; ++dd) {
           const int k = kc.pv_dir[dd];
           sh[dd] = k >= 0 ? (double)L.t_shift[3 * q + dd] * kc.pv[3 * k + dd] : 0.0;
         }
-        const double* g = M.sf_xgp + ((size_t)e * nd + d) * 3;
+        const double* g = M.sf_xgp + (dof_base<N>(M, e) + d) * 3;
         const double gx = __ldg(g) - sh[0], gy = __ldg(g + 1) - sh[1], gz = __ldg(g + 2) - sh[2];
-        const double wgt = __ldg(L.dof_w + (size_t)e * nd + d);
+        const double wgt = __ldg(L.dof_w + dof_base<N>(M, e) + d);
         const double rx = gx - csx, ry = gy - csy, rz = gz - csz;
         if constexpr (!MIXED) {
           s_g[i][0] = rx; s_g[i][1] = ry; s_g[i][2] = rz; s_g[i][3] = wgt;
@@ -1767,7 +1792,6 @@ template <int N, bool MIXED>
 __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB) k_step_ref(const __grid_constant__ DevMesh M, DevParticles P, const double* __restrict__ E,
                                                   const float* __restrict__ E32, double dt, DevStatus* st) {
   const Consts& kc = M.k;
-  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const uint8_t fl = P.flags[i];
@@ -1784,7 +1808,7 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
     for (int c = 0; c < 6; ++c) F[c] = kc.ext[c];
     if (charged) {
       double Eo[3];
-      eval_field<N>(kc, E + (size_t)e * nd * 3, xi, Eo);
+      field_at<N>(M, E, e, xi, Eo);
 #pragma unroll
       for (int c = 0; c < 3; ++c) F[c] = F[c] + Eo[c];
     }
@@ -1801,7 +1825,7 @@ __global__ void __launch_bounds__(256, MIXED ? PIC_REF_MIXED_MINB : PIC_REF_MINB
     if (charged) {
       float Eo[3];
       const float xf[3] = {(float)xi[0], (float)xi[1], (float)xi[2]};
-      eval_field_f<N>(kc, E32 + (size_t)e * nd * 3, xf, Eo);
+      field_at_f<N>(M, E32, e, xf, Eo);
 #pragma unroll
       for (int c = 0; c < 3; ++c) F[c] += Eo[c];
     }
@@ -1882,12 +1906,15 @@ __global__ void k_count_inside(DevParticles P, int* out) {
 // N+1-point rule already integrates PartSource(4)/sJ, a product of two degree-N interpolants, exactly).  One warp
 // per element sums w * PartSource(4) over its DOFs; one block then adds the element sums in index order, so the
 // result does not depend on scheduling.
+// dof_off: the elements' DOF offsets on a p-adapted mesh (else null: nd DOFs each)
 __global__ void __launch_bounds__(256) k_charge_elem(const double* __restrict__ PS, const double* __restrict__ w, int ne,
-                                                     int nd, double* __restrict__ elem_sum) {
+                                                     int nd, const int* __restrict__ dof_off, double* __restrict__ elem_sum) {
   const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (e >= ne) return;
+  const size_t b = dof_off ? (size_t)__ldg(dof_off + e) : (size_t)e * nd;
+  const int nde = dof_off ? __ldg(dof_off + e + 1) - __ldg(dof_off + e) : nd;
   double s = 0.0;
-  for (int r = lane; r < nd; r += 32) s = s + __ldg(w + (size_t)e * nd + r) * __ldg(PS + ((size_t)e * nd + r) * 4 + 3);
+  for (int r = lane; r < nde; r += 32) s = s + __ldg(w + b + r) * __ldg(PS + (b + r) * 4 + 3);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s = s + __shfl_down_sync(kFull, s, o);
   if (lane == 0) elem_sum[e] = s;
@@ -1927,17 +1954,25 @@ static inline int nblk(int n, int b) { return (n + b - 1) / b; }
     case 4: { constexpr int NN = 4; __VA_ARGS__; } break;     \
     default: break;                                           \
   }
+// the same for kernels with a per-element-degree instance (NN = 0 on p-adapted meshes)
+#define PIC_DISPATCH_NV(A, ...)                                             \
+  if ((A).M.dof_off) { constexpr int NN = 0; __VA_ARGS__; }                 \
+  else { PIC_DISPATCH_N((A).N, __VA_ARGS__); }
 
 // Mixed variant of node -> DOF: the node sums stay FP64; NodeSource / NodeVolume and the trilinear node ->
 // DOF weights (deposition weights) in FP32, one kernel; PartSource written in FP64.
+// N = 0 (p-adaption): as k_node_to_dof, each element with its own degree.
 template <int N>
 __global__ void __launch_bounds__(256) k_node_to_dof_f(const __grid_constant__ DevMesh M, const double* __restrict__ NS, double* __restrict__ PS) {
   const Consts& kc = M.k;
-  constexpr int n1 = N + 1, nd = n1 * n1 * n1;
+  const int nmax1 = N > 0 ? N + 1 : kc.N + 1, ndmax = nmax1 * nmax1 * nmax1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= M.ne * nd) return;
-  const int e = t / nd, r = t - e * nd;
-  const float a1 = (float)kc.fac_gp[r % n1], a2 = (float)kc.fac_gp[(r / n1) % n1], a3 = (float)kc.fac_gp[r / (n1 * n1)];
+  if (t >= M.ne * ndmax) return;
+  const int e = t / ndmax, r = t - e * ndmax;
+  const int nl = N > 0 ? N : __ldg(M.elem_n + e), n1 = nl + 1;
+  if (r >= n1 * n1 * n1) return;
+  const float a1 = (float)kc.fac_n[nl][r % n1], a2 = (float)kc.fac_n[nl][(r / n1) % n1],
+              a3 = (float)kc.fac_n[nl][r / (n1 * n1)];
   const float w[8] = {(1 - a1) * (1 - a2) * (1 - a3), a1 * (1 - a2) * (1 - a3), a1 * a2 * (1 - a3), (1 - a1) * a2 * (1 - a3),
                       (1 - a1) * (1 - a2) * a3,       a1 * (1 - a2) * a3,       a1 * a2 * a3,       (1 - a1) * a2 * a3};
   float out[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1953,25 +1988,26 @@ __global__ void __launch_bounds__(256) k_node_to_dof_f(const __grid_constant__ D
     out[2] = fmaf((float)b.x, s, out[2]);
     out[3] = fmaf((float)b.y, s, out[3]);
   }
-  double2* o = reinterpret_cast<double2*>(PS + (size_t)t * 4);
+  double2* o = reinterpret_cast<double2*>(PS + (N > 0 ? (size_t)t : dof_base<0>(M, e) + r) * 4);
   o[0] = make_double2(out[0], out[1]);
   o[1] = make_double2(out[2], out[3]);
 }
 
 int launch_node_to_dof(const LaunchArgs& A, double* PS) {
+  // A.nd = (NMax+1)^3: on a p-adapted mesh the NN = 0 instance skips each element's DOFs beyond its degree
   if (A.mixed) {
-    PIC_DISPATCH_N(A.N, { k_node_to_dof_f<NN><<<nblk(A.M.ne * A.nd, 256), 256, 0, A.s>>>(A.M, A.NS, PS); });
+    PIC_DISPATCH_NV(A, { k_node_to_dof_f<NN><<<nblk(A.M.ne * A.nd, 256), 256, 0, A.s>>>(A.M, A.NS, PS); });
     return 1;
   }
   k_node_normalize<<<nblk(A.n_canon * 4, 256), 256, 0, A.s>>>(A.M.node_vol, A.NS, A.n_canon);
-  PIC_DISPATCH_N(A.N, { k_node_to_dof<NN, true><<<nblk(A.M.ne * A.nd, 256), 256, 0, A.s>>>(A.M, A.NS, PS); });
+  PIC_DISPATCH_NV(A, { k_node_to_dof<NN, true><<<nblk(A.M.ne * A.nd, 256), 256, 0, A.s>>>(A.M, A.NS, PS); });
   return 2;
 }
 
 int launch_cvwm_fused(const LaunchArgs& A, const DevParticles& P, double dt) {
   cudaMemsetAsync(A.NS, 0, sizeof(double) * 4 * (size_t)A.n_canon, A.s);
   if (P.n <= 0) return 0;
-  PIC_DISPATCH_N(A.N, {
+  PIC_DISPATCH_NV(A, {
     if (A.mixed) k_step_cvwm_tria<NN, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.NS, dt, A.st);
     else k_step_cvwm_tria<NN, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.NS, dt, A.st);
   });
@@ -1986,7 +2022,7 @@ int launch_step_cvwm_tria(const LaunchArgs& A, const DevParticles& P, double* PS
 
 int launch_interpolate(const LaunchArgs& A, const DevParticles& P, bool refmap, bool cvwm) {
   if (P.n <= 0) return 0;
-  PIC_DISPATCH_N(A.N, {
+  PIC_DISPATCH_NV(A, {
     if (A.mixed) k_interpolate<NN, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.st, refmap, cvwm);
     else k_interpolate<NN, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, A.MF, P, A.E, A.E32, A.st, refmap, cvwm);
   });
@@ -2055,8 +2091,15 @@ int launch_sf_pack(const LaunchArgs& A, const DevParticles& P, const SortBuffers
 #define PIC_SF_GATHER 5
 #endif
 
+// ntgt target elements: L.order[0 .. ntgt), all of degree N
 template <int N, bool MIXED>
-static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
+static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS,
+                            int ntgt) {
+  if constexpr (N >= 4) {   // nd > 64: one thread per DOF, single phase
+    if (MIXED) k_sf_gather_mixed<N><<<ntgt, SfShape<N>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+    else k_sf_gather_fp64<N><<<ntgt, SfShape<N>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+    return;
+  } else {
 #if PIC_SF_GATHER == 5
   if constexpr (N == 3 && MIXED) {
     // one radius: octant warps fed by the bulk-copy ring (sub-cell culling, no hit lists)
@@ -2064,17 +2107,18 @@ static void launch_gather_n(const LaunchArgs& A, const SortBuffers& B, const SfL
       const bool a2 = A.sf_alpha == 2;     // the attribute is per device: set it at every launch (cheap)
       if (a2) cudaFuncSetAttribute(k_sf_gather7<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sf7Smem));
       else cudaFuncSetAttribute(k_sf_gather7<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sf7Smem));
-      if (a2) k_sf_gather7<true><<<A.M.ne, kSf7Threads, sizeof(Sf7Smem), A.s>>>(A.M, L, B.offset, K, PS, A.st);
-      else k_sf_gather7<false><<<A.M.ne, kSf7Threads, sizeof(Sf7Smem), A.s>>>(A.M, L, B.offset, K, PS, A.st);
+      if (a2) k_sf_gather7<true><<<ntgt, kSf7Threads, sizeof(Sf7Smem), A.s>>>(A.M, L, B.offset, K, PS, A.st);
+      else k_sf_gather7<false><<<ntgt, kSf7Threads, sizeof(Sf7Smem), A.s>>>(A.M, L, B.offset, K, PS, A.st);
       return;
     }
   }
-  if (L.elem_r) k_sf_gather5<N, MIXED, true, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-  else if (A.sf_alpha == 2) k_sf_gather5<N, MIXED, false, true><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-  else k_sf_gather5<N, MIXED, false, false><<<A.M.ne, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  if (L.elem_r) k_sf_gather5<N, MIXED, true, false><<<ntgt, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  else if (A.sf_alpha == 2) k_sf_gather5<N, MIXED, false, true><<<ntgt, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  else k_sf_gather5<N, MIXED, false, false><<<ntgt, kSf5Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #else
-  k_sf_gather2<N, MIXED><<<A.M.ne, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  k_sf_gather2<N, MIXED><<<ntgt, kSf2Threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
 #endif
+  }
 }
 
 int launch_sf_cc_norm(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K) {
@@ -2161,15 +2205,27 @@ double fp32_fma_rate(cudaStream_t st, float* sink, int sms) {
 }
 
 int launch_sf_gather(const LaunchArgs& A, const SortBuffers& B, const SfLists& L, const SfPack& K, double* PS) {
-  switch (A.N) {
-    case 1: if (A.mixed) launch_gather_n<1, true>(A, B, L, K, PS); else launch_gather_n<1, false>(A, B, L, K, PS); break;
-    case 2: if (A.mixed) launch_gather_n<2, true>(A, B, L, K, PS); else launch_gather_n<2, false>(A, B, L, K, PS); break;
-    case 3: if (A.mixed) launch_gather_n<3, true>(A, B, L, K, PS); else launch_gather_n<3, false>(A, B, L, K, PS); break;
-    default:   // nd > 64: one thread per DOF, single phase
-      if (A.mixed) k_sf_gather_mixed<4><<<A.M.ne, SfShape<4>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
-      else k_sf_gather_fp64<4><<<A.M.ne, SfShape<4>::threads, 0, A.s>>>(A.M, L, B.offset, K, PS);
+  if (!A.M.dof_off) {
+    PIC_DISPATCH_N(A.N, {
+      if (A.mixed) launch_gather_n<NN, true>(A, B, L, K, PS, A.M.ne);
+      else launch_gather_n<NN, false>(A, B, L, K, PS, A.M.ne);
+    });
+    return 1;
   }
-  return 1;
+  // p-adapted mesh: one launch per degree over that degree's targets
+  int launches = 0;
+  for (int k = 1; k <= kMaxN; ++k) {
+    const int ntgt = L.grp_off[k + 1] - L.grp_off[k];
+    if (ntgt <= 0) continue;
+    SfLists Lk = L;
+    Lk.order = L.order + L.grp_off[k];
+    PIC_DISPATCH_N(k, {
+      if (A.mixed) launch_gather_n<NN, true>(A, B, Lk, K, PS, ntgt);
+      else launch_gather_n<NN, false>(A, B, Lk, K, PS, ntgt);
+    });
+    ++launches;
+  }
+  return launches;
 }
 
 int launch_deposit_sf(const LaunchArgs& A, const DevParticles& P, const SortBuffers& B, const SfLists& L,
@@ -2179,7 +2235,7 @@ int launch_deposit_sf(const LaunchArgs& A, const DevParticles& P, const SortBuff
 
 int launch_step_ref(const LaunchArgs& A, const DevParticles& P, double dt) {
   if (P.n <= 0) return 0;
-  PIC_DISPATCH_N(A.N, {
+  PIC_DISPATCH_NV(A, {
     if (A.mixed) k_step_ref<NN, true><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.E, A.E32, dt, A.st);
     else k_step_ref<NN, false><<<nblk(P.n, 256), 256, 0, A.s>>>(A.M, P, A.E, A.E32, dt, A.st);
   });
@@ -2204,7 +2260,7 @@ int launch_map_particles(const LaunchArgs& A, const DevParticles& P) {
 
 int launch_charge_integral(const LaunchArgs& A, const double* PS, const double* w, double* elem_sum, double* out) {
   const int ne = A.M.ne;
-  k_charge_elem<<<nblk(ne * 32, 256), 256, 0, A.s>>>(PS, w, ne, A.nd, elem_sum);
+  k_charge_elem<<<nblk(ne * 32, 256), 256, 0, A.s>>>(PS, w, ne, A.nd, A.M.dof_off, elem_sum);
   k_sum_ordered<<<1, 1024, 0, A.s>>>(elem_sum, ne, out);
   return 2;
 }

@@ -42,12 +42,14 @@ struct SfLists {
   int n_pairs;
   const double* dof_center;   // [ne][3] centre of the element's DOF bounding box
   const float* dof_radius;    // [ne] largest distance of a DOF from dof_center
-  const int* order;           // [ne] target elements in Morton order of their DOF centres (L2 reuse)
+  const int* order;           // [ne] target elements in Morton order of their DOF centres (L2 reuse); on a
+                              // p-adapted mesh grouped by degree, Morton order within each group
+  int grp_off[kMaxN + 2];     // p-adapted mesh: the degree-k targets are order[grp_off[k] .. grp_off[k+1])
   // shape_function_cc: the same pairs seen from the source element, and the quadrature weight per DOF
   const int* t_off;           // [ne+1] per source element
   const int* t_tgt;           // [n_pairs] target element (0-based)
   const int8_t* t_shift;      // [n_pairs][3] periodic image of the source particles
-  const double* dof_w;        // [ne][nd] wGP(k) wGP(l) wGP(m) / sJ
+  const double* dof_w;        // per DOF (packed like PartSource): wGP(k) wGP(l) wGP(m) / sJ of the element's degree
   const double* elem_r;       // [ne] shape_function_adaptive: radius of the source element (else NULL)
   // particle box of each element relative to its DOF centre, padded (lo.xyz, 0, hi.xyz, 0); set where the
   // pack bins particles into 2x2x2 sub-cells (mixed N = 3 with one radius), else NULL

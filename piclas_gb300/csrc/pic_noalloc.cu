@@ -112,7 +112,8 @@ extern "C" int pic_deposit_cvwm_noalloc(pic_ctx_t* ctx, const double* d_part_sta
   if (n > 0)
     k_noalloc_cvwm<<<(n + 255) / 256, 256, 0, s>>>(ctx->M, d_part_state, d_elem, d_species, d_inside, n, NS, ctx->st);
   const int tot = ctx->M.ne * ctx->nd;
-  switch (ctx->N) {
+  switch (ctx->var_n ? 0 : ctx->N) {
+    case 0: k_node_to_dof<0><<<(tot + 255) / 256, 256, 0, s>>>(ctx->M, NS, d_part_source); break;   // p-adapted
     case 1: k_node_to_dof<1><<<(tot + 255) / 256, 256, 0, s>>>(ctx->M, NS, d_part_source); break;
     case 2: k_node_to_dof<2><<<(tot + 255) / 256, 256, 0, s>>>(ctx->M, NS, d_part_source); break;
     case 3: k_node_to_dof<3><<<(tot + 255) / 256, 256, 0, s>>>(ctx->M, NS, d_part_source); break;

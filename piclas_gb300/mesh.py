@@ -165,8 +165,8 @@ class BoxMesh:
     slen_basis: np.ndarray                # (6,nElems)
     elem_radius: np.ndarray               # (nElems)
     eps_one_cell: np.ndarray              # (nElems)
-    elem_xgp: np.ndarray                  # (3,0:N,0:N,0:N,nElems) -> C [e][k][j][i][3]
-    elem_sj: np.ndarray                   # (0:N,0:N,0:N,nElems)
+    elem_xgp: np.ndarray                  # (3,0:N,0:N,0:N,nElems) -> C [e][k][j][i][3]; with n_loc: packed (nDofs, 3)
+    elem_sj: np.ndarray                   # (0:N,0:N,0:N,nElems); with n_loc: packed (nDofs)
     node_coords: np.ndarray               # (3,8*nElems): tensor-ordered element corners
     elem_node: np.ndarray                 # (8,nElems) CGNS order, 1-based into node_coords
     elem_side_node: np.ndarray            # (4,6,nElems) 1-based into node_coords
@@ -190,13 +190,50 @@ class BoxMesh:
     bc: tuple = ("periodic", "periodic", "periodic")  # particle boundary per axis
     sf_elem_radius: np.ndarray = field(default=None)  # SFElemr2_Shared(1,:) for shape_function_adaptive
     # RefTracking with walls: BuildBCElemDistance output (see build_bc_elem_distance)
+    n_loc: np.ndarray = field(default=None)          # per-element degree Nloc (p-adaption); None: N everywhere
+    dof_offset: np.ndarray = field(default=None)     # N_DG_Mapping(1,:): 0-based DOF offset of each element (nElems+1)
     elem_to_bc_sides: np.ndarray = field(default=None)
     bc_side_elem_loc: np.ndarray = field(default=None)
     bc_side_distance: np.ndarray = field(default=None)
 
     @property
     def n_dof(self) -> int:
+        """(N+1)^3: the DOFs per element (with n_loc: of an element of the largest degree)."""
         return (self.N + 1) ** 3
+
+    @property
+    def n_dofs(self) -> int:
+        """nDofsMapping: the DOFs of all elements."""
+        return int(self.dof_offset[-1]) if self.n_loc is not None else self.n_elems * self.n_dof
+
+    def dof_shape(self, ncomp: int) -> tuple:
+        """Shape of a per-DOF array with ncomp components: (nElems, (N+1)^3, ncomp), or packed (nDofs, ncomp)."""
+        return (self.n_dofs, ncomp) if self.n_loc is not None else (self.n_elems, self.n_dof, ncomp)
+
+    def elem_dofs(self, a: np.ndarray, e: int) -> np.ndarray:
+        """The (Nloc+1)^3 DOFs of element e (0-based) of a per-DOF array in either layout, as rows (DOF, component)."""
+        if self.n_loc is None:
+            return a.reshape(self.n_elems, self.n_dof, -1)[e]
+        return a.reshape(self.n_dofs, -1)[self.dof_offset[e]:self.dof_offset[e + 1]]
+
+    @property
+    def n_dg_mapping(self) -> np.ndarray | None:
+        """N_DG_Mapping(1:3, nElems): DOF offset, Nloc, compute-node offset (= the DOF offset on one process)."""
+        if self.n_loc is None:
+            return None
+        off = self.dof_offset[:-1]
+        return np.ascontiguousarray(np.stack([off, self.n_loc, off], axis=1), dtype=np.int32)
+
+    @property
+    def n_inter(self) -> np.ndarray | None:
+        """N_Inter(Nloc)%xGP, %wGP, %wBary for Nloc = 1..N, one block of 3 (Nloc+1) values per degree."""
+        if self.n_loc is None:
+            return None
+        out = []
+        for k in range(1, self.N + 1):
+            xg, wg = legendre_gauss_nodes(k)
+            out += [np.asarray(xg), np.asarray(wg), np.asarray(barycentric_weights(xg))]
+        return np.ascontiguousarray(np.concatenate(out), dtype=np.float64)
 
     @property
     def h(self) -> np.ndarray:
@@ -216,8 +253,12 @@ WALL_BC = {"open": 1, "reflective": 2}      # PartBound%TargetBoundCond
 def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
                    perturb: float = 0.0, refmapping_eps: float = 1.0e-4,
                    bc=("periodic", "periodic", "periodic"), bc_halo_eps: float | None = None,
-                   wall_bulge: float = 0.0, wall_shear: float = 0.0, periodic_tracing: bool = False) -> BoxMesh:
+                   wall_bulge: float = 0.0, wall_shear: float = 0.0, periodic_tracing: bool = False,
+                   n_loc=None) -> BoxMesh:
     """Build a box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
+
+    ``n_loc`` (p-adaption): the degree Nloc of every element (1..N, N is then NMax); the DOF arrays are then
+    packed element by element (N_DG_Mapping offsets), and NodeVolume and ElemEpsOneCell use each element's Nloc.
 
     ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
     along each axis (h per axis); boundary nodes stay put so the periodic faces match.
@@ -344,29 +385,56 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     radius = np.sqrt(np.max(np.sum((node_coords - bary[:, None, :]) ** 2, axis=2), axis=1))
 
     # ---- Gauss points, Jacobian (trilinear map) -------------------------------------
-    lg = [lagrange_polys(float(x), xi_cl, wb_cl) for x in xgp]   # lg[p][a]
-    nd = N + 1
-    elem_xgp = np.zeros((ne, nd, nd, nd, 3))    # [e][k][j][i][3]
-    jac = np.zeros((ne, nd, nd, nd, 3, 3))      # J[a][b] = d x_a / d xi_b
-    for k in range(nd):
-        for j in range(nd):
-            for i in range(nd):
-                xp = np.zeros((ne, 3))
-                J = np.zeros((ne, 3, 3))
-                for c in range(2):
-                    for b in range(2):
-                        for a in range(2):
-                            w = lg[i][a] * lg[j][b] * lg[k][c]
-                            xp = xp + xcl[:, c, b, a, :] * w
-                            J = J + dxcl[:, c, b, a, :, :] * w      # [nn][dd]
-                elem_xgp[:, k, j, i, :] = xp
-                jac[:, k, j, i] = J
-    Jm = jac
-    detJ = (Jm[..., 0, 0] * (Jm[..., 1, 1] * Jm[..., 2, 2] - Jm[..., 2, 1] * Jm[..., 1, 2])
-            + Jm[..., 0, 1] * (Jm[..., 1, 2] * Jm[..., 2, 0] - Jm[..., 1, 0] * Jm[..., 2, 2])
-            + Jm[..., 0, 2] * (Jm[..., 1, 0] * Jm[..., 2, 1] - Jm[..., 1, 1] * Jm[..., 2, 0]))
-    sJ = 1.0 / detJ                               # [e][k][j][i]
-    scaleJ = sJ.reshape(ne, -1).max(axis=1) / sJ.reshape(ne, -1).min(axis=1)
+    def dof_geometry(sel, Nd):
+        """Elem_xGP [e][k][j][i][3] and sJ [e][k][j][i] of the elements sel at degree Nd."""
+        xg_d, _ = legendre_gauss_nodes(Nd)
+        lg = [lagrange_polys(float(x), xi_cl, wb_cl) for x in xg_d]   # lg[p][a]
+        nd = Nd + 1
+        m = len(sel)
+        exg = np.zeros((m, nd, nd, nd, 3))
+        jac = np.zeros((m, nd, nd, nd, 3, 3))      # J[a][b] = d x_a / d xi_b
+        for k in range(nd):
+            for j in range(nd):
+                for i in range(nd):
+                    xp = np.zeros((m, 3))
+                    J = np.zeros((m, 3, 3))
+                    for c in range(2):
+                        for b in range(2):
+                            for a in range(2):
+                                w = lg[i][a] * lg[j][b] * lg[k][c]
+                                xp = xp + xcl[sel, c, b, a, :] * w
+                                J = J + dxcl[sel, c, b, a, :, :] * w      # [nn][dd]
+                    exg[:, k, j, i, :] = xp
+                    jac[:, k, j, i] = J
+        Jm = jac
+        detJ = (Jm[..., 0, 0] * (Jm[..., 1, 1] * Jm[..., 2, 2] - Jm[..., 2, 1] * Jm[..., 1, 2])
+                + Jm[..., 0, 1] * (Jm[..., 1, 2] * Jm[..., 2, 0] - Jm[..., 1, 0] * Jm[..., 2, 2])
+                + Jm[..., 0, 2] * (Jm[..., 1, 0] * Jm[..., 2, 1] - Jm[..., 1, 1] * Jm[..., 2, 0]))
+        return exg, 1.0 / detJ
+
+    if n_loc is None:
+        elem_xgp, sJ = dof_geometry(np.arange(ne), N)
+        groups_n = [(N, np.arange(ne))]
+        scaleJ = sJ.reshape(ne, -1).max(axis=1) / sJ.reshape(ne, -1).min(axis=1)
+        dof_offset = None
+    else:
+        n_loc = np.ascontiguousarray(n_loc, dtype=np.int32).reshape(-1)
+        if n_loc.shape != (ne,) or n_loc.min() < 1 or n_loc.max() > N:
+            raise ValueError(f"n_loc must hold one degree in 1..{N} per element")
+        dof_offset = np.zeros(ne + 1, dtype=np.int64)
+        dof_offset[1:] = np.cumsum((n_loc.astype(np.int64) + 1) ** 3)        # Set_N_DG_Mapping
+        elem_xgp = np.zeros((int(dof_offset[-1]), 3))
+        sJ = np.zeros(int(dof_offset[-1]))
+        scaleJ = np.zeros(ne)
+        groups_n = [(int(k), np.nonzero(n_loc == k)[0]) for k in np.unique(n_loc)]
+        for k, sel in groups_n:
+            exg, sj = dof_geometry(sel, k)
+            nd3 = (k + 1) ** 3
+            idx = (dof_offset[sel][:, None] + np.arange(nd3)[None, :]).reshape(-1)
+            elem_xgp[idx] = exg.reshape(-1, 3)
+            sJ[idx] = sj.reshape(-1)
+            scaleJ[sel] = sj.reshape(len(sel), -1).max(axis=1) / sj.reshape(len(sel), -1).min(axis=1)
+    # ElemEpsOneCell from the element's own ElemsJ (particle_mesh_build.f90:625)
     eps_one_cell = 1.0 + np.sqrt(3.0 * scaleJ * refmapping_eps)
 
     # ---- sides: neighbours, periodic vectors, node maps, concavity -----------------
@@ -452,19 +520,27 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         elem_node[:, c] = 8 * np.arange(ne) + t + 1
         node_info[:, c] = corner_uid[:, t] + 1
 
-    # ---- NodeVolume (pic_depo_tools.f90:282-303) ---------------------------------------
-    xg = np.asarray(xgp)
-    wg = np.asarray(wgp)
+    # ---- NodeVolume (pic_depo_tools.f90:282-303, each element with its own Nloc) ----------
     NV = np.zeros(n_unique)
     signs = ((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1))
-    for i in range(nd):
-        for j in range(nd):
-            for k in range(nd):
-                sjv = sJ[:, k, j, i]
-                for c in range(8):
-                    sx, sy, sz = signs[c]
-                    w = (1.0 + sx * xg[i]) * (1.0 + sy * xg[j]) * (1.0 + sz * xg[k]) * wg[i] * wg[j] * wg[k] / 8.0
-                    np.add.at(NV, node_info[:, c] - 1, 1.0 / sjv * w)
+    for kd, sel in groups_n:
+        xg_d, wg_d = legendre_gauss_nodes(kd)
+        xg = np.asarray(xg_d)
+        wg = np.asarray(wg_d)
+        nd = kd + 1
+        if dof_offset is None:
+            sj_sel = sJ
+        else:
+            idx = dof_offset[sel][:, None] + np.arange(nd ** 3)[None, :]
+            sj_sel = sJ[idx].reshape(len(sel), nd, nd, nd)
+        for i in range(nd):
+            for j in range(nd):
+                for k in range(nd):
+                    sjv = sj_sel[:, k, j, i]
+                    for c in range(8):
+                        sx, sy, sz = signs[c]
+                        w = (1.0 + sx * xg[i]) * (1.0 + sy * xg[j]) * (1.0 + sz * xg[k]) * wg[i] * wg[j] * wg[k] / 8.0
+                        np.add.at(NV, node_info[sel, c] - 1, 1.0 / sjv * w)
 
     # ---- periodic twins (pic_depo.f90:1218-2089) --------------------------------------
     canon = np.empty(n_unique, dtype=np.int64)
@@ -528,13 +604,31 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         periodic_n_nodes=per_n, periodic_offset=per_off, periodic_nodes=per_nodes,
         fibgm_imax=fib_imax, fibgm_deltas=fib_d, fibgm_n_elems=fib_n, fibgm_offset=fib_off,
         fibgm_element=fib_el, canonical_node=canon,
-        side_bc=side_bc if side_bc.any() else None, bc=bc,
+        side_bc=side_bc if side_bc.any() else None, bc=bc, n_loc=n_loc, dof_offset=dof_offset,
     )
     if (side_bc.any() and not any(periodic)) or (periodic_tracing and any(periodic)):
         halo = float(hvec.max()) if bc_halo_eps is None else float(bc_halo_eps)
         mesh.elem_to_bc_sides, mesh.bc_side_elem_loc, mesh.bc_side_distance = build_bc_elem_distance(
             mesh, halo, include_periodic=periodic_tracing)
     return mesh
+
+
+def p_adaption_degrees(nx: int, ny: int, nz: int, kind: str, nmin: int, nmax: int, lo=(0.0, 0.0, 0.0),
+                       hi=(1.0, 1.0, 1.0), seed: int = 0) -> np.ndarray:
+    """Initial element degrees of InitpAdaption (mesh_pAdaption.f90:98-145) for the box of build_box_mesh:
+    "random" -- NMin + INT(U (NMax - NMin + 1)) per element (U from a seeded generator in place of the
+    reference's RANDOM_NUMBER); "half-half" -- NMax where the element's x centre is above 0, else NMin (the
+    reference takes (max + min)/2 of the node x coordinates; here the cell centre of the unperturbed grid)."""
+    ne = nx * ny * nz
+    if kind == "random":
+        u = np.random.default_rng(seed).random(ne)
+        return (nmin + (u * (nmax - nmin + 1)).astype(np.int64)).astype(np.int32)
+    if kind == "half-half":
+        i = np.arange(ne) % nx
+        h = (hi[0] - lo[0]) / nx
+        xc = lo[0] + (i + 0.5) * h
+        return np.where(xc > 0.0, nmax, nmin).astype(np.int32)
+    raise ValueError("kind must be 'random' or 'half-half'")
 
 
 # CGNS_SideToVol2 at NGeo = 1 for a master side: corner (p,q) of local side s -> tensor corner (a,b,c)
@@ -585,7 +679,8 @@ def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothi
     from the element's corners to the corners of its node neighbours that it does not share and that do not
     coincide with them in the kernel's projection (SFMeasureDistance, pic_depo.f90:1080-1109; else the mid
     point to its corners), averaged with the characteristic length when that is shorter (always with
-    ``smoothing``, PIC-shapefunction-adaptive-smoothing), times SFDepoScaling/(N+1).  ``dim`` and ``direction``
+    ``smoothing``, PIC-shapefunction-adaptive-smoothing), times SFDepoScaling/(minN_PP+1), minN_PP the lowest
+    degree of the element and its node neighbours (N without p-adaption).  ``dim`` and ``direction``
     are PIC-shapefunction-dimension and -direction: SFNorm is |v(dir)| in 1D, the norm in the plane normal to
     dir in 2D (components dim_sf_dir1, dim_sf_dir2 of InitShapeFunctionDimensionalty), the 3D norm otherwise;
     the characteristic length is BoxVolume/dimFactorSF (1D), sqrt(BoxVolume/dimFactorSF) (2D) or
@@ -671,7 +766,8 @@ def sf_adaptive_radius(mesh: BoxMesh, adaptive_dof: float | None = None, smoothi
             char_len = vol ** (1.0 / 3.0)
         if char_len < r[e] or smoothing:
             r[e] = (r[e] + char_len) / 2.0
-        r[e] = r[e] * scaling / (mesh.N + 1.0)
+        min_n = mesh.N if mesh.n_loc is None else int(min([mesh.n_loc[e]] + [mesh.n_loc[t] for t in nb[e]]))
+        r[e] = r[e] * scaling / (min_n + 1.0)
     return r
 
 

@@ -46,7 +46,7 @@ class Workload:
     part_state: np.ndarray          # (n, 6)  PartState(1:6, n)
     elem: np.ndarray                # (n,)    1-based GlobalElemID
     part_species: np.ndarray        # (n,)    1-based
-    e_dof: np.ndarray               # (nElems, nDOF, 3)
+    e_dof: np.ndarray               # (nElems, nDOF, 3); with p-adaption packed (nDofs, 3)
     dt: float
     nsteps: int
     external_field: tuple = (0.0,) * 6
@@ -116,7 +116,7 @@ def plasma_wave(n_cells: int = 8, N: int = 3, n_particles: int = 200_000, amp: f
     mpf = n0 * vol / n
     # field of the perturbation with a neutralising background: dE_x/dx = rho/eps0
     ex0 = (-Q_ELECTRON) * n0 * amp / (2.0 * math.pi * EPS0)
-    xg = mesh.elem_xgp.reshape(mesh.n_elems, -1, 3)
+    xg = mesh.elem_xgp.reshape(mesh.dof_shape(3))
     e_dof = np.zeros_like(xg)
     e_dof[..., 0] = ex0 * np.cos(2.0 * math.pi * (xg[..., 0] - mesh.lo[0]) / (mesh.hi[0] - mesh.lo[0]))
     return Workload(name=f"plasma_wave_{mesh.nx}^3_N{mesh.N}_{n}", mesh=mesh,
@@ -188,7 +188,7 @@ def curved_two_species(n_cells: int = 32, N: int = 3, n_per_species: int = 8_000
     ps = np.ascontiguousarray(np.concatenate([x, v], axis=1))
     vol = float(np.prod(mesh.hi - mesh.lo))
     mpf = n0 * vol / n_per_species
-    xg = mesh.elem_xgp.reshape(mesh.n_elems, -1, 3)
+    xg = mesh.elem_xgp.reshape(mesh.dof_shape(3))
     Lb = mesh.hi - mesh.lo
     e_dof = np.empty_like(xg)
     e_dof[..., 0] = E0 * np.sin(2.0 * math.pi * (xg[..., 1] - mesh.lo[1]) / Lb[1])
@@ -233,7 +233,7 @@ def differentiable_loop(n_cells: int = 16, N: int = 2, n_particles: int = 1_000_
     elem = _elem_of_uniform(mesh, x)
     vol = float(np.prod(mesh.hi - mesh.lo))
     mpf = n0 * vol / n
-    xg = mesh.elem_xgp.reshape(mesh.n_elems, -1, 3)
+    xg = mesh.elem_xgp.reshape(mesh.dof_shape(3))
     Ly = mesh.hi[1] - mesh.lo[1]
     e_dof = np.zeros_like(xg)
     e_dof[..., 1] = E0 * np.sin(2.0 * math.pi * (xg[..., 1] - mesh.lo[1]) / Ly)

@@ -20,7 +20,7 @@ def _run_gpu(w, nsteps, precision=capi.PIC_PREC_FP64, dt=None, sort_interval=0):
     loop = ParticleLoop(cfg, w.mesh)
     loop.set_field(w.e_dof)
     loop.upload_particles(w.part_state, w.elem, w.part_species)
-    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    PS = np.zeros(w.mesh.dof_shape(4))
     loop.time_step(dt or w.dt, nsteps, PS)
     out = loop.download_particles(with_ref=True)
     out["PS"] = PS
@@ -35,7 +35,7 @@ def _run_oracle(oracle, w, nsteps, dt=None):
     st = oracle.OracleState(w.part_state, w.elem, w.part_species)
     if w.tracking == capi.PIC_TRACK_REFMAPPING:
         oracle.map_particles(cfg, ms, st)
-    PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+    PS = np.zeros(w.mesh.dof_shape(4))
     oracle.step(cfg, ms, w.e_dof, st, dt or w.dt, nsteps, PS)
     return st, PS
 
@@ -49,14 +49,14 @@ def _rho_species_scale(oracle, w, st, nthreads=1):
     the final oracle state.  Electrons and ions cancel in the summed rho, so a mixed-precision error is
     measured against the magnitude the species deposit, not against their small difference."""
     cfg, ms = w.config(), capi.MeshStruct(w.mesh)
-    tot = np.zeros((w.mesh.n_elems, w.mesh.n_dof))
+    tot = np.zeros(w.mesh.dof_shape(4)[:-1])
     for s in np.unique(st.species):
         k = (st.species == s) & (st.inside == 1)
         if not k.any():
             continue
         sub = oracle.OracleState(st.part_state[k], st.elem[k], st.species[k], is_new=np.zeros(int(k.sum()), np.uint8),
                                  part_pos_ref=st.part_pos_ref[k])
-        PSs = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+        PSs = np.zeros(w.mesh.dof_shape(4))
         oracle.deposit(cfg, ms, sub, PSs, nthreads)
         tot += np.abs(PSs[..., 3])
     return float(tot.max())
@@ -1157,3 +1157,134 @@ def test_batch_instances_mixed_vs_fp64_and_concurrent(gpu_lib):
         assert np.array_equal(c["part_state"], g["part_state"])
         assert _rel(PS, g["PS"]) <= 1e-12
         lp.close()
+
+
+# ---- per-element polynomial degree (p-adaption, N_DG_Mapping) ---------------------------------------------
+def _p_adapted(kind, seed, n=6000, precision_fp64=True):
+    from piclas_gb300.mesh import p_adaption_degrees
+    nl = p_adaption_degrees(5, 5, 5, "random", 1, 3, seed=seed)
+    if kind == "cvwm":          # TriaTracking on the straight-sided box
+        mesh = build_box_mesh(5, 5, 5, 3, n_loc=nl)
+        return workloads.plasma_wave(mesh=mesh, n_particles=n, seed=seed, T_eV=2000.0, nsteps=6)
+    mesh = build_box_mesh(5, 5, 5, 3, perturb=0.05, n_loc=nl)
+    w = workloads.curved_two_species(mesh=mesh, n_per_species=n // 2, seed=seed, Te_eV=1000.0, nsteps=4)
+    w.dt *= 10.0
+    if kind == "cc":
+        w.deposition = capi.PIC_DEPO_SHAPE_FUNCTION_CC
+    return w
+
+
+@pytest.mark.parametrize("kind", ["cvwm", "sf", "cc"])
+def test_p_adaption_against_oracle(gpu_lib, oracle_lib, kind):
+    """Degrees 1..3 at random over a curved 5^3 box (NMax = 3): the particle kernels dispatch on each element's
+    degree, the node -> DOF and gather kernels run per degree group.  FP64 against the oracle: CVWM +
+    TriaTracking bit-exact (elements, positions, velocities), RefTracking + shape function (B_z) elements exact
+    and states within 1e-13, PartSource within 1e-12 of its maximum.  Mixed: elements within two, rho within
+    1e-6 of max sum_s |rho_s|.  The integrated charge (pic_verify_deposited_charge) equals the oracle's
+    element-by-element integral."""
+    w = _p_adapted(kind, seed=31)
+    g = _run_gpu(w, w.nsteps)
+    st, PS = _run_oracle(oracle_lib, w, w.nsteps)
+    assert np.array_equal(g["elem"], st.elem) and np.array_equal(g["inside"], st.inside)
+    if kind == "cvwm":
+        assert np.array_equal(g["part_state"], st.part_state)
+    else:
+        assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
+        assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0
+    assert (st.elem != w.elem).sum() > 20                 # particles crossed into elements of other degrees
+    loop = ParticleLoop(w.config(), w.mesh)
+    loop.upload_particles(st.part_state, st.elem, st.species, inside=st.inside, is_new=st.is_new)
+    PSd = loop.deposition()
+    num, _ = loop.verify_deposited_charge()
+    loop.close()
+    q = oracle_lib.integrate_charge(capi.MeshStruct(w.mesh), w.mesh.N, PSd)
+    scale = sum(abs(w.species[s - 1][0] * w.species[s - 1][2]) * int((st.species == s).sum()) for s in np.unique(st.species))
+    assert abs(num - q) <= 1e-12 * scale
+    gm = _run_gpu(w, w.nsteps, precision=capi.PIC_PREC_MIXED)
+    assert (gm["elem"] != st.elem).sum() <= 2
+    assert _rho_err_species(oracle_lib, w, st, gm["PS"], PS) <= 1e-6
+
+
+@pytest.mark.parametrize("kind", ["cvwm", "sf"])
+def test_p_adaption_one_degree_equals_fixed_n_on_gpu(gpu_lib, kind):
+    """A p-adapted mesh whose elements all have degree 3 runs on the GPU exactly as the uniform N = 3 mesh:
+    the degree-dispatching kernels and the grouped launches give identical elements and states, and
+    PartSource within 1e-12 (atomic order)."""
+    res = []
+    for nl in (None, np.full(125, 3, np.int32)):
+        mesh = build_box_mesh(5, 5, 5, 3, perturb=0.05, n_loc=nl)
+        if kind == "cvwm":
+            w = workloads.plasma_wave(mesh=mesh, n_particles=6000, seed=8, T_eV=50.0, nsteps=4)
+        else:
+            w = workloads.curved_two_species(mesh=mesh, n_per_species=3000, seed=8, nsteps=4)
+        res.append(_run_gpu(w, 4))
+    assert np.array_equal(res[0]["elem"], res[1]["elem"])
+    assert np.array_equal(res[0]["part_state"], res[1]["part_state"])
+    assert _rel(res[1]["PS"].reshape(res[0]["PS"].shape), res[0]["PS"]) <= 1e-12
+
+
+def test_p_adaption_rejected_by_hdg_and_adjoint(gpu_lib):
+    """The HDG solve and the differentiable loop need one degree for all elements: both return
+    PIC_ERR_INVALID_ARGUMENT on a p-adapted mesh (the reference builds p-adaption with HDG only on PETSc)."""
+    w = _p_adapted("cvwm", seed=3, n=2000)
+    loop = ParticleLoop(w.config(), w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    with pytest.raises(PicError):
+        loop.adjoint(2, w.dt, np.zeros(w.mesh.n_elems * loop.nd), 1.0)
+    import ctypes as C
+    hdg = capi.PicHdg()
+    hdg.n_sides = 1
+    rc = gpu_lib.pic_hdg_init(loop.handle, C.byref(hdg))
+    assert rc == 1
+    loop.close()
+
+
+# ---- RefMappingGuess 1..4 ----------------------------------------------------------------------------------
+@pytest.mark.parametrize("guess", [2, 3, 4])
+@pytest.mark.parametrize("kind", ["tria", "ref", "ref_padapt"])
+def test_ref_mapping_guess_against_oracle(gpu_lib, oracle_lib, guess, kind):
+    """The Newton start values of GetRefNewtonStartValue on the GPU: CVWM + TriaTracking (the Newton of the
+    deposition and the interpolation) bit-exact, RefTracking + shape function (B_z) on a curved box and on a
+    p-adapted one with exact elements and states within 1e-13, PartPosRef within 1e-10; mixed elements within
+    two of the oracle's."""
+    from piclas_gb300.mesh import p_adaption_degrees
+    if kind == "tria":
+        w = workloads.plasma_wave(n_cells=5, N=3, n_particles=6000, seed=17, T_eV=50.0, nsteps=4)
+    else:
+        nl = p_adaption_degrees(5, 5, 5, "random", 1, 3, seed=5) if kind == "ref_padapt" else None
+        mesh = build_box_mesh(5, 5, 5, 3, perturb=0.08, n_loc=nl)
+        w = workloads.curved_two_species(mesh=mesh, n_per_species=3000, seed=17, Te_eV=1000.0, nsteps=4)
+    cfg = w.config()
+    cfg.ref_mapping_guess = guess
+    loop = ParticleLoop(cfg, w.mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    PS = np.zeros(w.mesh.dof_shape(4))
+    loop.time_step(w.dt, w.nsteps, PS)
+    g = loop.download_particles(with_ref=True)
+    loop.close()
+    ms = capi.MeshStruct(w.mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    if kind != "tria":
+        oracle_lib.map_particles(cfg, ms, st)
+    PSo = np.zeros(w.mesh.dof_shape(4))
+    oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, w.nsteps, PSo)
+    assert np.array_equal(g["elem"], st.elem)
+    if kind == "tria":
+        assert np.array_equal(g["part_state"], st.part_state)
+    else:
+        assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
+        assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
+        assert np.max(np.abs(g["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
+    assert _rel(PS, PSo) <= 1e-12
+    cfg.precision = capi.PIC_PREC_MIXED
+    lm = ParticleLoop(cfg, w.mesh)
+    lm.set_field(w.e_dof)
+    lm.upload_particles(w.part_state, w.elem, w.part_species)
+    lm.time_step(w.dt, w.nsteps)
+    gm = lm.download_particles()
+    lm.close()
+    assert (gm["elem"] != st.elem).sum() <= 2

@@ -775,3 +775,134 @@ def test_periodic_tracing_with_walls_free_streaming(oracle_lib):
     d[:, 1:] -= np.round(d[:, 1:])                           # y, z: modulo the period
     assert np.max(np.abs(d)) < 1e-12
     assert np.array_equal(st.elem, workloads._elem_of_uniform(w.mesh, st.part_state[:, :3]))
+
+
+# ---- per-element polynomial degree (p-adaption, N_DG_Mapping) --------------------------------------------
+def test_p_adaption_mapping_layout():
+    """N_DG_Mapping(1:3,:) of Set_N_DG_Mapping: row 1 the running DOF offsets, row 2 the degrees, row 3 = row 1 on
+    one process; N_Inter(1..NMax) blocks hold the Gauss nodes, weights and barycentric weights of each degree;
+    Elem_xGP and sJ of an element of degree k equal those of the same element in a uniform degree-k mesh."""
+    from piclas_gb300.mesh import p_adaption_degrees
+    nl = p_adaption_degrees(4, 3, 2, "random", 1, 3, seed=4)
+    assert set(np.unique(nl)) <= {1, 2, 3} and len(np.unique(nl)) == 3
+    m = build_box_mesh(4, 3, 2, 3, perturb=0.05, n_loc=nl)
+    g = m.n_dg_mapping
+    assert np.array_equal(g[:, 1], nl) and np.array_equal(g[:, 0], g[:, 2])
+    assert np.array_equal(g[:, 0], np.concatenate([[0], np.cumsum((nl + 1) ** 3)[:-1]]))
+    assert m.n_dofs == int(((nl + 1) ** 3).sum())
+    ni, off = m.n_inter, 0
+    for k in (1, 2, 3):
+        xg, wg = legendre_gauss_nodes(k)
+        assert np.array_equal(ni[off:off + k + 1], xg)
+        assert np.array_equal(ni[off + k + 1:off + 2 * (k + 1)], wg)
+        assert np.array_equal(ni[off + 2 * (k + 1):off + 3 * (k + 1)], barycentric_weights(xg))
+        off += 3 * (k + 1)
+        mu = build_box_mesh(4, 3, 2, k, perturb=0.05)
+        for e in np.nonzero(nl == k)[0]:
+            assert np.array_equal(m.elem_dofs(m.elem_xgp, e), mu.elem_dofs(mu.elem_xgp, e))
+            assert np.array_equal(m.elem_dofs(m.elem_sj, e), mu.elem_dofs(mu.elem_sj, e))
+            assert m.eps_one_cell[e] == mu.eps_one_cell[e]
+    hh = p_adaption_degrees(4, 1, 1, "half-half", 1, 3, lo=(-1, 0, 0), hi=(1, 1, 1))
+    assert list(hh) == [1, 1, 3, 3]
+
+
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_CVWM, capi.PIC_DEPO_SHAPE_FUNCTION, capi.PIC_DEPO_SHAPE_FUNCTION_CC])
+def test_p_adaption_one_degree_equals_fixed_n(oracle_lib, dep):
+    """A p-adapted mesh whose elements all have degree 2 (NMax = 3) runs the loop exactly as the uniform N = 2
+    mesh: identical positions, velocities, elements, PartSource and integrated charge after 3 steps."""
+    res = []
+    for mesh in (build_box_mesh(4, 4, 4, 2, perturb=0.05), build_box_mesh(4, 4, 4, 3, perturb=0.05, n_loc=np.full(64, 2))):
+        w = workloads.plasma_wave(mesh=mesh, n_particles=3000, seed=5, deposition=dep)
+        w.sf_radius = 0.3
+        cfg, ms = w.config(), capi.MeshStruct(mesh)
+        st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+        PS = np.zeros(mesh.dof_shape(4))
+        oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, 3, PS)
+        res.append((st.part_state.copy(), st.elem.copy(), PS.reshape(-1), oracle_lib.integrate_charge(ms, mesh.N, PS)))
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    assert np.array_equal(res[0][2], res[1][2]) and res[0][3] == res[1][3]
+
+
+@pytest.mark.parametrize("dep", [capi.PIC_DEPO_CVWM, capi.PIC_DEPO_SHAPE_FUNCTION_CC, capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE])
+def test_p_adaption_deposition_conserves_charge(oracle_lib, dep):
+    """Degrees 1..3 at random: cell_volweight_mean (NodeVolume and CellVolWeight(Nloc) per element) and the
+    charge-conserving shape functions integrate, element by element with each element's own Gauss rule, to the
+    deposited charge within 1e-12."""
+    from piclas_gb300.mesh import p_adaption_degrees
+    nl = p_adaption_degrees(5, 5, 5, "random", 1, 3, seed=7)
+    mesh = build_box_mesh(5, 5, 5, 3, perturb=0.05, n_loc=nl)
+    if dep == capi.PIC_DEPO_SHAPE_FUNCTION_ADAPTIVE:
+        mesh.sf_elem_radius = sf_adaptive_radius(mesh)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=4000, seed=9, deposition=dep)
+    w.sf_radius = 0.25
+    cfg, ms = w.config(), capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    PS = np.zeros(mesh.dof_shape(4))
+    oracle_lib.deposit(cfg, ms, st, PS, os.cpu_count() or 1)
+    total = w.n * w.species[0][0] * w.species[0][2]
+    assert abs(oracle_lib.integrate_charge(ms, mesh.N, PS) - total) <= 1e-12 * abs(total)
+
+
+def test_p_adaption_interpolation_reproduces_trilinear_field(oracle_lib):
+    """A field trilinear in the reference coordinates (here E linear in x on an unperturbed box) lies in every
+    degree's polynomial space: EvaluateFieldAtRefPos with each element's Nloc returns it at the particles to
+    rounding, for degrees 1..3 side by side."""
+    from piclas_gb300.mesh import p_adaption_degrees
+    nl = p_adaption_degrees(4, 4, 4, "random", 1, 3, seed=2)
+    mesh = build_box_mesh(4, 4, 4, 3, n_loc=nl)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=2000, seed=3)
+    A = np.array([[1.0, -2.0, 0.5], [0.3, 0.7, -1.1], [2.0, 0.1, 0.4]])
+    b = np.array([0.2, -0.3, 0.9])
+    e_dof = mesh.elem_xgp.reshape(-1, 3) @ A.T + b
+    cfg, ms = w.config(), capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.interpolate(cfg, ms, e_dof, st)
+    want = w.part_state[:, :3] @ A.T + b
+    assert np.max(np.abs(st.field[:, :3] - want)) <= 1e-13 * np.max(np.abs(want))
+
+
+# ---- RefMappingGuess 1..4 (GetRefNewtonStartValue) ----------------------------------------------------------
+@pytest.mark.parametrize("guess", [1, 2, 3, 4])
+def test_ref_mapping_guess_maps_particles(oracle_lib, guess):
+    """Every start value of the Newton (linear guess, closest Gauss point, closest corner, zero) maps particles on
+    a curved box and on a p-adapted one to xi with x(xi) = x within 1e-5 h (the Newton stops once
+    |dxi|^2 <= RefMappingEps = 1e-4, so the last iterate carries the quadratic remainder), and RefTracking over 3
+    steps gives the same elements as the default guess, states within 1e-9 (the field at slightly different xi)."""
+    from piclas_gb300.mesh import p_adaption_degrees
+    for nl in (None, p_adaption_degrees(4, 4, 4, "random", 1, 3, seed=6)):
+        mesh = build_box_mesh(4, 4, 4, 3, perturb=0.08, n_loc=nl)
+        w = workloads.curved_two_species(mesh=mesh, n_per_species=1000, seed=12, nsteps=3)
+        ms = capi.MeshStruct(mesh)
+        cfg = w.config()
+        cfg.ref_mapping_guess = guess
+        st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+        oracle_lib.map_particles(cfg, ms, st)
+        x = np.array([elem_map(mesh, e - 1, xi) for e, xi in zip(w.elem, st.part_pos_ref)])
+        assert np.max(np.abs(x - w.part_state[:, :3])) <= 1e-5 * float(mesh.h[0])
+        oracle_lib.step(cfg, ms, w.e_dof, st, w.dt, 3, None)
+        cfg1 = w.config()
+        st1 = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+        oracle_lib.map_particles(cfg1, ms, st1)
+        oracle_lib.step(cfg1, ms, w.e_dof, st1, w.dt, 3, None)
+        assert np.array_equal(st.elem, st1.elem)
+        assert np.max(np.abs(st.part_state - st1.part_state) / np.max(np.abs(st1.part_state), axis=0)) <= 1e-9
+
+
+def test_ref_mapping_guess_start_values(oracle_lib):
+    """The start values themselves: with a Newton limited to no iteration effect (a particle exactly at a Gauss
+    point, or at a corner) guesses 2 and 3 return that node's xi exactly."""
+    mesh = build_box_mesh(2, 2, 2, 2, perturb=0.05)
+    ms = capi.MeshStruct(mesh)
+    xg, _ = legendre_gauss_nodes(2)
+    e = 5
+    P = mesh.elem_dofs(mesh.elem_xgp, e)
+    r = 2 * 9 + 1 * 3 + 0                         # (i, j, k) = (0, 1, 2)
+    cfg = capi.make_config(2, capi.PIC_TRACK_REFMAPPING, capi.PIC_DEPO_CVWM, 0, [(-1.0, 1.0, 1.0)], 1, ref_mapping_guess=2)
+    st = oracle_lib.OracleState(np.concatenate([P[r], [0, 0, 0]])[None, :], np.array([e + 1]), np.array([1]))
+    oracle_lib.map_particles(cfg, ms, st)
+    assert np.array_equal(st.part_pos_ref[0], [xg[0], xg[1], xg[2]])
+    X = mesh.xcl_ngeo.reshape(mesh.n_elems, 2, 2, 2, 3)[e]
+    cfg.ref_mapping_guess = 3
+    st = oracle_lib.OracleState(np.concatenate([X[1, 0, 1], [0, 0, 0]])[None, :], np.array([e + 1]), np.array([1]))
+    oracle_lib.map_particles(cfg, ms, st)
+    assert np.array_equal(st.part_pos_ref[0], [1.0, -1.0, 1.0])      # corner (i, j, k) = (1, 0, 1): X[k][j][i]
