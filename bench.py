@@ -41,17 +41,20 @@ def log(*a):
 
 # ----------------------------------------------------------------------------------------------
 def make_workload(name: str, seed: int, n_override: int | None = None, cells: int | None = None,
-                  periodic_tracing: bool = False):
+                  periodic_tracing: bool = False, n_geo: int = 1, p_adaption: str | None = None):
     from piclas_gb300 import workloads
-    from piclas_gb300.mesh import build_box_mesh
+    from piclas_gb300.mesh import build_box_mesh, p_adaption_degrees
     kw = {} if cells is None else {"n_cells": cells}
     if name == "curved":
         if n_override is not None:
             kw["n_per_species"] = n_override // 2
-        if periodic_tracing:
-            # the reference's default periodic RefTracking (CartesianPeriodic = F): BC lists with the periodic sides
+        if periodic_tracing or n_geo > 1 or p_adaption:
+            # periodic_tracing: the reference's default periodic RefTracking (CartesianPeriodic = F), BC lists with
+            # the periodic sides; n_geo: curved elements of that geometry degree; p_adaption: degrees 1..3 per element
             nc = kw.pop("n_cells", 32)
-            kw["mesh"] = build_box_mesh(nc, nc, nc, 3, perturb=0.05, periodic_tracing=True)
+            n_loc = p_adaption_degrees(nc, nc, nc, p_adaption, 1, 3, seed=seed) if p_adaption else None
+            kw["mesh"] = build_box_mesh(nc, nc, nc, 3, perturb=0.05, periodic_tracing=periodic_tracing, n_geo=n_geo,
+                                        n_loc=n_loc)
         w = workloads.curved_two_species(seed=seed, **kw)
         w.periodic_tracing = periodic_tracing
         return w
@@ -69,10 +72,17 @@ def workload_config(w, name):
         tag = "plain FP64 at scale: " if (cells == 32 and w.n == 16_000_000) else "profiling case of plain FP64 at scale: "
         trk = ("RefTracking (CartesianPeriodic = F: periodic sides traced as BC sides)"
                if getattr(w, "periodic_tracing", False) else "RefTracking (CartesianPeriodic/FastPeriodic)")
-        return {"workload": f"{tag}{cells}^3 curved hex, N={m.N}, {w.n // 2} e- + {w.n - w.n // 2} ions, "
-                            "B_z=0.1 T, RefTracking, shape_function r=1.5h, dt=5e-12",
-                "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "shape_function",
-                "tracking": trk, "l2": "inputs larger than L2 (no flush)"}
+        geo = "curved hex" if m.n_geo == 1 else f"curved NGeo={m.n_geo} hex"
+        deg = f"N={m.N}" if m.n_loc is None else f"N_loc random 1..{m.N} ({m.n_dofs} DOFs)"
+        out = {"workload": f"{tag}{cells}^3 {geo}, {deg}, {w.n // 2} e- + {w.n - w.n // 2} ions, "
+                           "B_z=0.1 T, RefTracking, shape_function r=1.5h, dt=5e-12",
+               "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "shape_function",
+               "tracking": trk, "l2": "inputs larger than L2 (no flush)"}
+        if m.n_geo > 1:
+            out["n_geo"] = m.n_geo
+        if m.n_loc is not None:
+            out["p_adaption"] = "random 1..3"
+        return out
     cells = round(m.n_elems ** (1.0 / 3.0))
     return {"workload": f"plasma wave: {cells}^3 hex, N={m.N}, {w.n} e-, CVWM, TriaTracking, dt=1e-11",
             "elements": m.n_elems, "N": m.N, "particles": w.n, "deposition": "cell_volweight_mean",
@@ -85,7 +95,7 @@ def algorithmic_bytes_per_step(w, mixed: bool) -> float:
     s_state = (24 + 12) if mixed else 48
     if w.tracking == capi.PIC_TRACK_REFMAPPING:
         s_state += 24                                   # PartPosRef
-    b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_elems * w.mesh.n_dof * (3 * 8 + 8)
+    b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_dofs * (3 * 8 + 8)
     if w.deposition == capi.PIC_DEPO_CVWM:
         b += w.mesh.n_nodes * (2 * 4 * 8)
     return float(b)
@@ -97,15 +107,17 @@ def dominant_kernel_bytes(w, mixed: bool) -> tuple[str, float]:
     if w.deposition == capi.PIC_DEPO_SHAPE_FUNCTION:
         # gather: each packed particle record read once, PartSource written once
         rec = 32 if mixed else 16 + 24 + 32
-        if sf_gather_variant() == 5 and mixed and w.mesh.N == 3:
+        if w.mesh.n_loc is not None:
+            name = f"k_sf_gather5<Nloc,{int(mixed)},0,{int(w.sf_alpha == 2)}> (one launch per degree)"
+        elif sf_gather_variant() == 5 and mixed and w.mesh.N == 3:
             name = f"k_sf_gather7<{int(w.sf_alpha == 2)}>"
         elif sf_gather_variant() == 5:
             name = f"k_sf_gather5<{w.mesh.N},{int(mixed)},0,{int(w.sf_alpha == 2)}>"
         else:
             name = f"k_sf_gather2<{w.mesh.N},{int(mixed)}>"
-        return name, float(w.n * rec + w.mesh.n_elems * w.mesh.n_dof * 4 * 8)
+        return name, float(w.n * rec + w.mesh.n_dofs * 4 * 8)
     s_state = (24 + 12) if mixed else 48
-    b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_elems * w.mesh.n_dof * 3 * (4 if mixed else 8)
+    b = w.n * (2 * s_state + 2 * 4 + 1) + w.mesh.n_dofs * 3 * (4 if mixed else 8)
     b += w.mesh.n_nodes * 4 * 8
     return f"k_step_cvwm_tria<{w.mesh.N},{int(mixed)}>", float(b)
 
@@ -123,7 +135,7 @@ def sf_gather_variant() -> int:
 def sf_hits_per_launch(w) -> float:
     """Expected (particle, DOF) pairs with r <= R: particles x DOF density x sphere volume."""
     vol = float(np.prod(np.asarray(w.mesh.hi) - np.asarray(w.mesh.lo)))
-    dof_density = w.mesh.n_elems * w.mesh.n_dof / vol
+    dof_density = w.mesh.n_dofs / vol
     return w.n * dof_density * 4.0 / 3.0 * math.pi * w.sf_radius ** 3
 
 
@@ -279,7 +291,7 @@ def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0
         st = oracle.OracleState(wk.part_state, wk.elem, wk.part_species)
         if wk.tracking == capi.PIC_TRACK_REFMAPPING:
             oracle.map_particles(cfg, ms, st, nthreads)
-        PS = np.zeros((wk.mesh.n_elems, wk.mesh.n_dof, 4))
+        PS = np.zeros(wk.mesh.dof_shape(4))
         t0 = time.perf_counter()
         oracle.step(cfg, ms, wk.e_dof, st, wk.dt, nsteps, PS, nthreads)
         return time.perf_counter() - t0
@@ -333,7 +345,7 @@ def run_gpu(args, rank, world, local_rank):
     prec = capi.PIC_PREC_MIXED if mixed else capi.PIC_PREC_FP64
     t0 = time.time()
     w = make_workload(args.workload, seed=rank, n_override=args.particles, cells=args.cells,
-                      periodic_tracing=args.periodic_tracing)
+                      periodic_tracing=args.periodic_tracing, n_geo=args.ngeo, p_adaption=args.p_adaption)
     log(f"[rank {rank}] workload {w.name} built in {time.time() - t0:.1f}s")
     cfg = w.config(precision=prec, sort_interval=args.sort_interval)
     loop = ParticleLoop(cfg, w.mesh)
@@ -424,7 +436,7 @@ def run_gpu(args, rank, world, local_rank):
 
     # end-to-end through the C-ABI with host buffers: per step the HDG hand-over (E in, PartSource out)
     E_host = torch.from_numpy(np.ascontiguousarray(w.e_dof)).pin_memory()
-    PS_host = torch.zeros((w.mesh.n_elems, w.mesh.n_dof, 4), dtype=torch.float64).pin_memory()
+    PS_host = torch.zeros(w.mesh.dof_shape(4), dtype=torch.float64).pin_memory()
     loop.synchronize()
     te0 = time.perf_counter()
     for _ in range(args.steps):
@@ -479,7 +491,7 @@ def rho_species_scale(w, g):
     """max over DOFs of sum_s |rho_s|: each species of the state g deposited on its own (FP64).  Electrons and
     ions cancel in the summed rho; a precision error is measured against what the species deposit."""
     from piclas_gb300 import ParticleLoop, capi
-    tot = np.zeros((w.mesh.n_elems, w.mesh.n_dof))
+    tot = np.zeros(w.mesh.dof_shape(4)[:-1])
     for s in np.unique(w.part_species):
         k = (w.part_species == s) & (g["inside"] == 1)
         loop = ParticleLoop(w.config(precision=capi.PIC_PREC_FP64), w.mesh)
@@ -530,7 +542,7 @@ def mixed_arm(args, w):
         lp = ParticleLoop(w.config(precision=prec), w.mesh)
         lp.set_field(w.e_dof)
         lp.upload_particles(w.part_state, w.elem, w.part_species)
-        PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+        PS = np.zeros(w.mesh.dof_shape(4))
         lp.time_step(w.dt, 2, PS)
         g = lp.download_particles()
         lp.close()
@@ -579,7 +591,7 @@ def extras(args, w_main):
         loop = ParticleLoop(w.config(precision=prec), w.mesh)
         loop.set_field(w.e_dof)
         loop.upload_particles(w.part_state, w.elem, w.part_species)
-        PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+        PS = np.zeros(w.mesh.dof_shape(4))
         loop.time_step(w.dt, 2, PS)
         g = loop.download_particles()
         loop.close()
@@ -747,7 +759,7 @@ def batch_run(args):
             loop.set_field(w.e_dof)
             loop.upload_particles(w.part_state, w.elem, w.part_species)
             s = torch.cuda.ExternalStream(loop.stream_ptr)
-            PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+            PS = np.zeros(w.mesh.dof_shape(4))
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             loop.synchronize()
@@ -849,6 +861,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--particles", type=int, default=None, help="override the particle count (profiling cases)")
     ap.add_argument("--cells", type=int, default=None, help="override the elements per axis (profiling cases)")
+    ap.add_argument("--ngeo", type=int, default=1, choices=[1, 2, 3, 4],
+                    help="curved workload on elements of this geometry degree (NGeo > 1: curved elements)")
+    ap.add_argument("--p-adaption", default=None, choices=["random", "half-half"],
+                    help="curved workload with per-element degrees 1..3 (N_DG_Mapping)")
     ap.add_argument("--periodic-tracing", action="store_true",
                     help="RefTracking traces the periodic sides as BC sides (the reference's default CartesianPeriodic = F)")
     ap.add_argument("--hdg-cg-kernel", type=int, default=0, choices=[0, 1, 2],

@@ -140,7 +140,7 @@ typedef struct pic_config_t {
  * Shapes are given in the reference's Fortran notation; memory is column-major. */
 typedef struct pic_mesh_t {
   int32_t n_elems;              /* nElems                                               */
-  int32_t n_geo;                /* NGeo (must be 1)                                     */
+  int32_t n_geo;                /* NGeo (1..4; NGeo > 1: see elem_curved)                */
   int32_t n_nodes;              /* nUniqueGlobalNodes (periodic copies are distinct)    */
   int32_t n_periodic_vectors;   /* GEO%nPeriodicVectors (0..3)                          */
   double  periodic_vectors[9];  /* GEO%PeriodicVectors(1:3,1:3)                         */
@@ -152,7 +152,7 @@ typedef struct pic_mesh_t {
   const double* wgp;            /* N_Inter(N)%wGP(0:N)                                  */
   const double* wbary_gp;       /* N_Inter(N)%wBary(0:N)                                */
   /* element geometry */
-  const double* xcl_ngeo;       /* XCL_NGeo(1:3,0:NGeo,0:NGeo,0:NGeo,nElems)             */
+  const double* xcl_ngeo;       /* XCL_NGeo(1:3,0:NGeo,0:NGeo,0:NGeo,nElems) at XiCL_NGeo */
   const double* dxcl_ngeo;      /* dXCL_NGeo(1:3,1:3,0:NGeo,0:NGeo,0:NGeo,nElems)        */
   const double* elem_bary;      /* ElemBaryNGeo(1:3,nElems)                             */
   const double* xez_basis;      /* XiEtaZetaBasis(1:3,1:6,nElems)                       */
@@ -213,6 +213,15 @@ typedef struct pic_mesh_t {
    * reference builds p-adaption with HDG only on PETSc) and the differentiable loop. */
   const int32_t* n_dg_mapping;
   const double* n_inter;
+  /* curved elements (NGeo > 1): ElemCurved(nElems) as 0/1 (IdentifyElemAndSideType, particle_mesh_tools.f90:
+   * 848-1235: the element's XCL_NGeo differs from the trilinear interpolation of its corners).  The Newton x -> xi
+   * runs on XCL_NGeo/dXCL_NGeo at NGeo for a curved element and on its eight corners (with dXCL_NGeo of the
+   * corners) otherwise (GetPositionInRefElem, eval_xyz.f90:87-117); NULL: every element curved.  node_coords
+   * holds the corners; elem_bary, xez_basis, slen_basis, elem_radius, elem_xgp, elem_sj and the FIBGM are
+   * those of the curved map.  NGeo > 1 is built for meshes without open/reflective walls and with
+   * CartesianPeriodic (periodic_tracing = 0): curved side intersections (ComputeCurvedIntersection,
+   * particle_intersection.f90) are not built; the differentiable loop needs NGeo = 1. */
+  const int32_t* elem_curved;
 } pic_mesh_t;
 
 typedef struct pic_status_t {

@@ -59,9 +59,11 @@ void orc_lagrange_polys(double x, int n, const double* xgp, const double* wbary,
 /* ---------------------------------------------------------------------------------------
  * mesh accessors (reference layouts, 1-based element ids)
  * ------------------------------------------------------------------------------------- */
-#define XCL(m, c, i, j, k, e)      ((m)->xcl_ngeo[((((size_t)((e) - 1) * 2 + (k)) * 2 + (j)) * 2 + (i)) * 3 + (c)])
+#define NG1(m)                     ((m)->n_geo + 1)
+#define XCL(m, c, i, j, k, e) \
+  ((m)->xcl_ngeo[((((size_t)((e) - 1) * NG1(m) + (k)) * NG1(m) + (j)) * NG1(m) + (i)) * 3 + (c)])
 #define DXCL(m, dd, nn, i, j, k, e) \
-  ((m)->dxcl_ngeo[(((((size_t)((e) - 1) * 2 + (k)) * 2 + (j)) * 2 + (i)) * 3 + (nn)) * 3 + (dd)])
+  ((m)->dxcl_ngeo[(((((size_t)((e) - 1) * NG1(m) + (k)) * NG1(m) + (j)) * NG1(m) + (i)) * 3 + (nn)) * 3 + (dd)])
 #define NODE(m, c, n)              ((m)->node_coords[((size_t)(n) - 1) * 3 + (c)])
 #define SIDENODE(m, q, s, e)       ((m)->elem_side_node[((size_t)((e) - 1) * 6 + (s)) * 4 + (q)])
 
@@ -122,9 +124,9 @@ static void ref_newton_start(const pic_config_t* cfg, const pic_mesh_t* m, const
     double winner = sqrt(d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
     const double* xc = m->xi_cl_ngeo;
     xi[0] = xi[1] = xi[2] = xc[0];
-    for (int i = 0; i <= 1; ++i)
-      for (int j = 0; j <= 1; ++j)
-        for (int k = 0; k <= 1; ++k) {
+    for (int i = 0; i <= m->n_geo; ++i)
+      for (int j = 0; j <= m->n_geo; ++j)
+        for (int k = 0; k <= m->n_geo; ++k) {
           double dX = fabs(x[0] - XCL(m, 0, i, j, k, e));
           if (dX > winner) continue;
           double dY = fabs(x[1] - XCL(m, 1, i, j, k, e));
@@ -151,25 +153,22 @@ static void ref_newton_start(const pic_config_t* cfg, const pic_mesh_t* m, const
     for (int d = 0; d < 3; ++d) xi[d] = fmax(fmin(1.0, xi[d]), -1.0);
 }
 
-/* F(xi) = x(xi) - x_in with F = F + XCL*Lag(1,i)*buff (eval_xyz.f90:342-350) */
-static void newton_residual_first(const pic_mesh_t* m, int e, const double Lag[3][2], const double x[3], double F[3]) {
-  for (int c = 0; c < 3; ++c) F[c] = -x[c];
-  for (int k = 0; k <= 1; ++k)
-    for (int j = 0; j <= 1; ++j) {
-      double buff = Lag[1][j] * Lag[2][k];
-      for (int i = 0; i <= 1; ++i)
-        for (int c = 0; c < 3; ++c) F[c] = F[c] + XCL(m, c, i, j, k, e) * Lag[0][i] * buff;
-    }
-}
-
-/* RefElemNewton, eval_xyz.f90:298-445 (N_In = NGeo = 1). Returns isSuccessful. */
-static int ref_elem_newton(const pic_config_t* cfg, const pic_mesh_t* m, double xi[3], const double x[3], int e) {
-  const double* xcl = m->xi_cl_ngeo;
-  const double* wb = m->wbary_cl_ngeo;
-  double Lag[3][2], F[3], xiOld[3], dxi[3], Jac[3][3], sJac[3][3];
+/* RefElemNewton, eval_xyz.f90:298-445, for N_In <= 4: X (N_In+1)^3 CL points [k][j][i][3] and their
+ * derivatives D [k][j][i][nn][dd], on the nodes XiCL with barycentric weights wb.  Returns isSuccessful. */
+static int ref_elem_newton_n(const pic_config_t* cfg, double xi[3], const double x[3], int nIn, const double* X,
+                             const double* D, const double* xiCL, const double* wb) {
+  const int n1 = nIn + 1;
+  double Lag[3][5], F[3], xiOld[3], dxi[3], Jac[3][3], sJac[3][3];
   int success = 1;
-  for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], 1, xcl, wb, Lag[d]);
-  newton_residual_first(m, e, (const double(*)[2])Lag, x, F);
+  for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], nIn, xiCL, wb, Lag[d]);
+  /* F(xi) = x(xi) - x_in with F = F + XCL*Lag(1,i)*buff (:342-350) */
+  for (int c = 0; c < 3; ++c) F[c] = -x[c];
+  for (int k = 0; k <= nIn; ++k)
+    for (int j = 0; j <= nIn; ++j) {
+      double buff = Lag[1][j] * Lag[2][k];
+      for (int i = 0; i <= nIn; ++i)
+        for (int c = 0; c < 3; ++c) F[c] = F[c] + X[((size_t)(k * n1 + j) * n1 + i) * 3 + c] * Lag[0][i] * buff;
+    }
   double deltaXi2 = (fabs(F[0]) < EPS_MACH && fabs(F[1]) < EPS_MACH && fabs(F[2]) < EPS_MACH) ? 0.0 : 1.0;
   double normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
   double normFold;
@@ -177,13 +176,14 @@ static int ref_elem_newton(const pic_config_t* cfg, const pic_mesh_t* m, double 
   while (deltaXi2 > cfg->refmapping_eps && iter < 100) {
     iter = iter + 1;
     for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) Jac[a][b] = 0.0;
-    for (int k = 0; k <= 1; ++k)
-      for (int j = 0; j <= 1; ++j) {
+    for (int k = 0; k <= nIn; ++k)
+      for (int j = 0; j <= nIn; ++j) {
         double buff = Lag[1][j] * Lag[2][k];
-        for (int i = 0; i <= 1; ++i) {
+        for (int i = 0; i <= nIn; ++i) {
           double buff2 = Lag[0][i] * buff;
+          const double* Dp = &D[((size_t)(k * n1 + j) * n1 + i) * 9];
           for (int nn = 0; nn < 3; ++nn)
-            for (int dd = 0; dd < 3; ++dd) Jac[nn][dd] = Jac[nn][dd] + DXCL(m, dd, nn, i, j, k, e) * buff2;
+            for (int dd = 0; dd < 3; ++dd) Jac[nn][dd] = Jac[nn][dd] + Dp[nn * 3 + dd] * buff2;
         }
       }
     /* getDet, eval_xyz.f90:464-466 */
@@ -210,14 +210,14 @@ static int ref_elem_newton(const pic_config_t* cfg, const pic_mesh_t* m, double 
     int iArmijo = 1;
     while (normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8) {
       for (int d = 0; d < 3; ++d) xi[d] = xiOld[d] - lambda * dxi[d];
-      for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], 1, xcl, wb, Lag[d]);
+      for (int d = 0; d < 3; ++d) orc_lagrange_polys(xi[d], nIn, xiCL, wb, Lag[d]);
       for (int c = 0; c < 3; ++c) F[c] = -x[c];
-      for (int k = 0; k <= 1; ++k)
-        for (int j = 0; j <= 1; ++j) {
+      for (int k = 0; k <= nIn; ++k)
+        for (int j = 0; j <= nIn; ++j) {
           double buff = Lag[1][j] * Lag[2][k];
-          for (int i = 0; i <= 1; ++i) {
+          for (int i = 0; i <= nIn; ++i) {
             double buff2 = Lag[0][i] * buff;
-            for (int c = 0; c < 3; ++c) F[c] = F[c] + XCL(m, c, i, j, k, e) * buff2;
+            for (int c = 0; c < 3; ++c) F[c] = F[c] + X[((size_t)(k * n1 + j) * n1 + i) * 3 + c] * buff2;
           }
         }
       lambda = 0.2 * lambda;
@@ -227,6 +227,27 @@ static int ref_elem_newton(const pic_config_t* cfg, const pic_mesh_t* m, double 
     if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = 0; break; }
   }
   return success;
+}
+
+/* The Newton of GetPositionInRefElem (eval_xyz.f90:87-117): on XCL_NGeo at NGeo for NGeo = 1 or a curved
+ * element, else on the element's eight corners with their dXCL_NGeo (XCL_NGeo1, dXCL_NGeo1 on XiCL_NGeo1). */
+static int ref_elem_newton(const pic_config_t* cfg, const pic_mesh_t* m, double xi[3], const double x[3], int e) {
+  const int ng = m->n_geo, n1 = ng + 1;
+  const size_t n3 = (size_t)n1 * n1 * n1;
+  if (ng == 1 || !m->elem_curved || m->elem_curved[e - 1])
+    return ref_elem_newton_n(cfg, xi, x, ng, &m->xcl_ngeo[(size_t)(e - 1) * n3 * 3],
+                             &m->dxcl_ngeo[(size_t)(e - 1) * n3 * 9], m->xi_cl_ngeo, m->wbary_cl_ngeo);
+  double X1[24], D1[72];
+  static const double xi1[2] = {-1.0, 1.0}, wb1[2] = {-0.5, 0.5};   /* ChebyGaussLobNodes(1), BarycentricWeights */
+  for (int k = 0; k <= 1; ++k)
+    for (int j = 0; j <= 1; ++j)
+      for (int i = 0; i <= 1; ++i) {
+        const int q = (k * 2 + j) * 2 + i;
+        for (int c = 0; c < 3; ++c) X1[q * 3 + c] = XCL(m, c, i * ng, j * ng, k * ng, e);
+        for (int nn = 0; nn < 3; ++nn)
+          for (int dd = 0; dd < 3; ++dd) D1[q * 9 + nn * 3 + dd] = DXCL(m, dd, nn, i * ng, j * ng, k * ng, e);
+      }
+  return ref_elem_newton_n(cfg, xi, x, 1, X1, D1, xi1, wb1);
 }
 
 /* GetPositionInRefElem, eval_xyz.f90:35-123 (NGeo = 1 branch).  Without isSuccessful the

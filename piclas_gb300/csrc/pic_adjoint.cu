@@ -521,6 +521,8 @@ extern "C" int pic_adjoint_run(pic_ctx_t* c, const pic_adjoint_cfg_t* a, const d
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs a mesh without open/reflective sides");
   if (c->var_n)
     return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs one polynomial degree for all elements");
+  if (c->M.xcl_ng)
+    return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs NGeo = 1 (trilinear elements)");
   for (int s = 0; s < c->cfg.n_species; ++s)
     if (c->M.k.dt_fac[s] != 1.0)
       return pic_internal::set_error(PIC_ERR_INVALID_ARGUMENT, "the adjoint loop needs one time step for all species");

@@ -156,7 +156,12 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
       return fail(PIC_ERR_INVALID_ARGUMENT, "time_step_factor must lie in [0, 1] (0: not set = 1); the reference "
                                             "only allows species-specific factors below 1");
   }
-  if (m->n_elems < 1 || m->n_geo != 1) return fail(PIC_ERR_INVALID_ARGUMENT, "only NGeo = 1 meshes are supported");
+  if (m->n_elems < 1) return fail(PIC_ERR_INVALID_ARGUMENT, "n_elems must be positive");
+  if (m->n_geo < 1 || m->n_geo > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "NGeo must be 1..4");
+  if (m->n_geo > 1 && (m->side_bc || cfg->periodic_tracing))
+    return fail(PIC_ERR_INVALID_ARGUMENT, "curved elements (NGeo > 1) need a mesh without open/reflective sides and "
+                                          "CartesianPeriodic (periodic_tracing = 0): curved side intersections are "
+                                          "not built");
   if (m->n_periodic_vectors < 0 || m->n_periodic_vectors > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "n_periodic_vectors");
   const void* req[] = {m->xi_cl_ngeo, m->wbary_cl_ngeo, m->xgp, m->wgp, m->wbary_gp, m->xcl_ngeo, m->dxcl_ngeo,
                        m->elem_bary, m->xez_basis, m->slen_basis, m->elem_radius, m->elem_xgp, m->node_coords,
@@ -202,6 +207,57 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   return PIC_OK;
 }
 
+// Bounding box of element e: its corners (NGeo = 1), or the Bezier control points of its NGeo map (Bernstein
+// coefficients of the Lagrange interpolant on the CL points, which hold the element by the convex hull property)
+void elem_bbox(const pic_mesh_t* m, int e, double lo[3], double hi[3]) {
+  const int ng = m->n_geo, n1 = ng + 1;
+  for (int d = 0; d < 3; ++d) { lo[d] = 1e300; hi[d] = -1e300; }
+  if (ng == 1) {
+    for (int t = 0; t < 8; ++t)
+      for (int d = 0; d < 3; ++d) {
+        const double v = m->xcl_ngeo[((size_t)e * 8 + t) * 3 + d];
+        lo[d] = std::min(lo[d], v); hi[d] = std::max(hi[d], v);
+      }
+    return;
+  }
+  // V(i,j) = B_j(t_i), t = (xi_i + 1)/2 on the CL points; Vi = V^-1 (Gauss-Jordan, n1 <= 5)
+  double V[5][10];
+  for (int i = 0; i < n1; ++i) {
+    const double t = 0.5 * (m->xi_cl_ngeo[i] + 1.0);
+    for (int j = 0; j < n1; ++j) {
+      double b = 1.0;
+      for (int q = 0; q < j; ++q) b = b * (double)(ng - q) / (double)(q + 1);
+      V[i][j] = b * std::pow(t, j) * std::pow(1.0 - t, ng - j);
+      V[i][n1 + j] = i == j ? 1.0 : 0.0;
+    }
+  }
+  for (int c = 0; c < n1; ++c) {
+    int p = c;
+    for (int r = c + 1; r < n1; ++r) if (std::fabs(V[r][c]) > std::fabs(V[p][c])) p = r;
+    for (int k = 0; k < 2 * n1; ++k) std::swap(V[c][k], V[p][k]);
+    const double piv = V[c][c];
+    for (int k = 0; k < 2 * n1; ++k) V[c][k] /= piv;
+    for (int r = 0; r < n1; ++r)
+      if (r != c) { const double f = V[r][c]; for (int k = 0; k < 2 * n1; ++k) V[r][k] -= f * V[c][k]; }
+  }
+  const double* X = m->xcl_ngeo + (size_t)e * n1 * n1 * n1 * 3;
+  for (int d = 0; d < 3; ++d) {
+    double A[125], B[125];
+    for (int q = 0; q < n1 * n1 * n1; ++q) A[q] = X[(size_t)q * 3 + d];
+    for (int ax = 0; ax < 3; ++ax) {              // apply Vi along i, then j, then k
+      const int st = ax == 0 ? 1 : ax == 1 ? n1 : n1 * n1;
+      for (int q = 0; q < n1 * n1 * n1; ++q) {
+        const int a = (q / st) % n1, base = q - a * st;
+        double v = 0.0;
+        for (int l = 0; l < n1; ++l) v += V[a][n1 + l] * A[base + l * st];
+        B[q] = v;
+      }
+      for (int q = 0; q < n1 * n1 * n1; ++q) A[q] = B[q];
+    }
+    for (int q = 0; q < n1 * n1 * n1; ++q) { lo[d] = std::min(lo[d], A[q]); hi[d] = std::max(hi[d], A[q]); }
+  }
+}
+
 // N_Inter(Nloc)%wGP of element e (N_Inter(N) without a mapping)
 const double* elem_wgp(const pic_ctx* c, const pic_mesh_t* m, int e) {
   if (!c->var_n) return m->wgp;
@@ -221,10 +277,11 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
   std::vector<double> bmin((size_t)ne * 3), bmax((size_t)ne * 3), dmin((size_t)ne * 3), dmax((size_t)ne * 3);
   for (int e = 0; e < ne; ++e)
     for (int d = 0; d < 3; ++d) {
-      double lo = 1e300, hi = -1e300, dl = 1e300, dh = -1e300;
-      for (int t = 0; t < 8; ++t) {
-        double v = m->xcl_ngeo[((size_t)e * 8 + t) * 3 + d];
-        lo = std::min(lo, v); hi = std::max(hi, v);
+      double lo, hi, dl = 1e300, dh = -1e300;
+      {
+        double blo[3], bhi[3];
+        elem_bbox(m, e, blo, bhi);
+        lo = blo[d]; hi = bhi[d];
       }
       for (int r = 0; r < c->nd_of(e); ++r) {
         double v = sfx[((size_t)c->dof_off_h[e] + r) * 3 + d];
@@ -370,11 +427,9 @@ int build_sf_lists(pic_ctx* c, const pic_mesh_t* m, const std::vector<double>& d
     for (int e = 0; e < ne; ++e)
       for (int d = 0; d < 3; ++d) {
         if (!kdir[d]) continue;
-        double lo = 1e300, hi = -1e300;
-        for (int q = 0; q < 8; ++q) {
-          const double v = m->xcl_ngeo[((size_t)e * 8 + q) * 3 + d] - dofc[(size_t)e * 3 + d];
-          lo = std::min(lo, v); hi = std::max(hi, v);
-        }
+        double blo[3], bhi[3];
+        elem_bbox(m, e, blo, bhi);
+        const double lo = blo[d] - dofc[(size_t)e * 3 + d], hi = bhi[d] - dofc[(size_t)e * 3 + d];
         const double pad = 0.05 * (hi - lo);
         ebox[(size_t)e * 8 + d] = (float)(lo - pad);
         ebox[(size_t)e * 8 + 4 + d] = (float)(hi + pad);
@@ -578,8 +633,17 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     return bail(fail(PIC_ERR_CUDA, "cudaEventCreate failed"));
 
   // ---- element geometry -------------------------------------------------------------------
-  std::vector<double> xcl(m->xcl_ngeo, m->xcl_ngeo + (size_t)ne * 24);
-  std::vector<double> dxcl(m->dxcl_ngeo, m->dxcl_ngeo + (size_t)ne * 72);
+  // each element's corners and their dXCL_NGeo (XCL_NGeo1, dXCL_NGeo1 of GetPositionInRefElem; XCL_NGeo itself at
+  // NGeo = 1), tensor order i + 2 j + 4 k
+  const int ng = m->n_geo, g1 = ng + 1;
+  const size_t g3 = (size_t)g1 * g1 * g1;
+  std::vector<double> xcl((size_t)ne * 24), dxcl((size_t)ne * 72);
+  for (int e = 0; e < ne; ++e)
+    for (int t = 0; t < 8; ++t) {
+      const size_t q = (size_t)e * g3 + (size_t)((t >> 2) * ng * g1 + ((t >> 1) & 1) * ng) * g1 + (t & 1) * ng;
+      for (int c = 0; c < 3; ++c) xcl[((size_t)e * 8 + t) * 3 + c] = m->xcl_ngeo[q * 3 + c];
+      for (int c = 0; c < 9; ++c) dxcl[((size_t)e * 8 + t) * 9 + c] = m->dxcl_ngeo[q * 9 + c];
+    }
   std::vector<double> bary(m->elem_bary, m->elem_bary + (size_t)ne * 3);
   std::vector<double> xez(m->xez_basis, m->xez_basis + (size_t)ne * 18);
   std::vector<double> slen(m->slen_basis, m->slen_basis + (size_t)ne * 6);
@@ -727,6 +791,16 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   c->M = DevMesh{ne, d_xcl, d_dxcl, d_bary, d_xez, d_slen, d_rad, d_eps1, d_snb, d_sinfo, d_ecan, d_nvol, d_exgp,
                  d_fn, d_fo, d_fe, d_xclr};
   c->M.sf_xgp = d_exgp;
+  if (ng > 1) {
+    std::vector<double> xng(m->xcl_ngeo, m->xcl_ngeo + (size_t)ne * g3 * 3), dng(m->dxcl_ngeo, m->dxcl_ngeo + (size_t)ne * g3 * 9);
+    std::vector<int> crv(ne, 1);
+    if (m->elem_curved)
+      for (int e = 0; e < ne; ++e) crv[e] = m->elem_curved[e] ? 1 : 0;
+    double *d_xng = nullptr, *d_dng = nullptr;
+    int* d_crv = nullptr;
+    if ((rc = upload(c, &d_xng, xng)) || (rc = upload(c, &d_dng, dng)) || (rc = upload(c, &d_crv, crv))) return bail(rc);
+    c->M.xcl_ng = d_xng; c->M.dxcl_ng = d_dng; c->M.curved = d_crv;
+  }
   if (c->var_n) {
     int *d_doff = nullptr, *d_en = nullptr;
     if ((rc = upload(c, &d_doff, c->dof_off_h)) || (rc = upload(c, &d_en, c->elem_n_h))) return bail(rc);
@@ -790,8 +864,15 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       k.xgp_nf[kd][i] = (float)xg[i]; k.wbary_nf[kd][i] = (float)wb[i];
     }
   }
-  k.xi_cl[0] = m->xi_cl_ngeo[0]; k.xi_cl[1] = m->xi_cl_ngeo[1];
-  k.wbary_cl[0] = m->wbary_cl_ngeo[0]; k.wbary_cl[1] = m->wbary_cl_ngeo[1];
+  k.ngeo = ng;
+  for (int i = 0; i <= ng; ++i) { k.xi_cl_ng[i] = m->xi_cl_ngeo[i]; k.wbary_cl_ng[i] = m->wbary_cl_ngeo[i]; }
+  if (ng == 1) {
+    k.xi_cl[0] = m->xi_cl_ngeo[0]; k.xi_cl[1] = m->xi_cl_ngeo[1];
+    k.wbary_cl[0] = m->wbary_cl_ngeo[0]; k.wbary_cl[1] = m->wbary_cl_ngeo[1];
+  } else {   // XiCL_NGeo1 = ChebyGaussLobNodes(1), wBaryCL_NGeo1 = its barycentric weights
+    k.xi_cl[0] = -1.0; k.xi_cl[1] = 1.0;
+    k.wbary_cl[0] = -0.5; k.wbary_cl[1] = 0.5;
+  }
   k.n_pv = m->n_periodic_vectors;
   for (int q = 0; q < 9; ++q) k.pv[q] = m->periodic_vectors[q];
   for (int d = 0; d < 3; ++d) {

@@ -11,6 +11,7 @@
 namespace pic {
 
 constexpr int kMaxN = 5;                 // highest DG degree instantiated
+constexpr int kMaxNGeo = 4;              // highest geometry degree (curved elements)
 constexpr int kMaxTrackLoops = 10000;    // hop cap of the tracking walks (status bit on overflow)
 constexpr double kEpsMach = 2.220446049250313080847e-16;
 
@@ -46,6 +47,8 @@ struct Consts {
   int sf_keep[3];                              // 1D/2D shape function: 1 in the kernel directions
   int periodic_tracing;                        // RefTracking: periodic sides traced as BC sides (CartesianPeriodic = F)
   int ref_guess;                               // RefMappingGuess 1..4
+  int ngeo;                                    // NGeo (curved elements when > 1)
+  double xi_cl_ng[kMaxNGeo + 1], wbary_cl_ng[kMaxNGeo + 1];   // XiCL_NGeo, wBaryCL_NGeo (xi_cl: of NGeo = 1)
   // N_Inter(k)%xGP, %wBary and CellVolWeight(k)%Fac for every degree k (row k; rows up to NMax are set), FP64
   // and FP32: the kernels of degree k read row k, so elements of different degrees (p-adaption) share them
   double xgp_n[kMaxN + 1][kMaxN + 1], wbary_n[kMaxN + 1][kMaxN + 1], fac_n[kMaxN + 1][kMaxN + 1];
@@ -83,6 +86,11 @@ struct DevMesh {
   // N_DG_Mapping(2,:) [ne]; both null when every element has degree N (DOF offset e (N+1)^3)
   const int* dof_off;
   const int* elem_n;
+  // curved elements (NGeo > 1): XCL_NGeo [ne][(NGeo+1)^3][3] and dXCL_NGeo [ne][(NGeo+1)^3][9] ([k][j][i] order),
+  // ElemCurved [ne] (null: all curved); xcl/dxcl above then hold each element's corners (XCL_NGeo1, dXCL_NGeo1)
+  const double* xcl_ng;
+  const double* dxcl_ng;
+  const int* curved;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
@@ -187,14 +195,17 @@ static __device__ __noinline__ void newton_start_closest(const DevMesh& M, int e
         }
     return;
   }
-  const double* X = M.xcl + (size_t)e * 24;      // corner (i, j, k) at tensor index i + 2 j + 4 k
+  // XCL_NGeo: corner (i, j, k) at tensor index i + 2 j + 4 k (NGeo = 1), CL point (i, j, k) of XCL_NGeo else
+  const int g1 = kc.ngeo + 1;
+  const double* X = M.xcl_ng ? M.xcl_ng + (size_t)e * g1 * g1 * g1 * 3 : M.xcl + (size_t)e * 24;
+  const double* xcl = M.xcl_ng ? kc.xi_cl_ng : kc.xi_cl;
   const double d0 = x[0] - __ldg(X), d1 = x[1] - __ldg(X + 1), d2 = x[2] - __ldg(X + 2);
   double winner = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-  xi[0] = xi[1] = xi[2] = kc.xi_cl[0];
-  for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j)
-      for (int k = 0; k < 2; ++k) {
-        const double* Q = X + (i + 2 * j + 4 * k) * 3;
+  xi[0] = xi[1] = xi[2] = xcl[0];
+  for (int i = 0; i < g1; ++i)
+    for (int j = 0; j < g1; ++j)
+      for (int k = 0; k < g1; ++k) {
+        const double* Q = X + (i + g1 * (j + g1 * k)) * 3;
         const double dX = fabs(x[0] - __ldg(Q));
         if (dX > winner) continue;
         const double dY = fabs(x[1] - __ldg(Q + 1));
@@ -202,7 +213,7 @@ static __device__ __noinline__ void newton_start_closest(const DevMesh& M, int e
         const double dZ = fabs(x[2] - __ldg(Q + 2));
         if (dZ > winner) continue;
         const double dist = sqrt(dX * dX + dY * dY + dZ * dZ);
-        if (dist < winner) { winner = dist; xi[0] = kc.xi_cl[i]; xi[1] = kc.xi_cl[j]; xi[2] = kc.xi_cl[k]; }
+        if (dist < winner) { winner = dist; xi[0] = xcl[i]; xi[1] = xcl[j]; xi[2] = xcl[k]; }
       }
 }
 
@@ -402,14 +413,112 @@ static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e
   return success;
 }
 
+__device__ __forceinline__ void lagrange_rt(double x, int np, const double* xgp, const double* wb, double* L) {
+  bool hit = false;
+  for (int i = 0; i < np; ++i) {
+    L[i] = 0.0;
+    if (almost_equal_unity(x, xgp[i])) { L[i] = 1.0; hit = true; }
+  }
+  if (hit) return;
+  double s = 0.0;
+  for (int i = 0; i < np; ++i) { L[i] = wb[i] / (x - xgp[i]); s = s + L[i]; }
+  for (int i = 0; i < np; ++i) L[i] = L[i] / s;
+}
+
+// RefElemNewton (eval_xyz.f90:298-445) on the NGeo map of a curved element, in the reference's order
+static __device__ __noinline__ bool ref_elem_newton_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
+  const int n1 = kc.ngeo + 1;
+  const size_t n3 = (size_t)n1 * n1 * n1;
+  const double* X = M.xcl_ng + (size_t)e * n3 * 3;
+  const double* DX = M.dxcl_ng + (size_t)e * n3 * 9;
+  double L[3][kMaxNGeo + 1];
+  for (int d = 0; d < 3; ++d) lagrange_rt(xi[d], n1, kc.xi_cl_ng, kc.wbary_cl_ng, L[d]);
+  double F[3] = {-x[0], -x[1], -x[2]};
+  for (int k = 0; k < n1; ++k)
+    for (int j = 0; j < n1; ++j) {
+      const double buff = L[1][j] * L[2][k];
+      for (int i = 0; i < n1; ++i) {
+        const double* P = X + ((size_t)(k * n1 + j) * n1 + i) * 3;
+        for (int c = 0; c < 3; ++c) F[c] = F[c] + __ldg(P + c) * L[0][i] * buff;
+      }
+    }
+  double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
+  double normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+  int iter = 0;
+  bool success = true;
+  while (deltaXi2 > kc.refmapping_eps && iter < 100) {
+    iter = iter + 1;
+    double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    for (int k = 0; k < n1; ++k)
+      for (int j = 0; j < n1; ++j) {
+        const double buff = L[1][j] * L[2][k];
+        for (int i = 0; i < n1; ++i) {
+          const double buff2 = L[0][i] * buff;
+          const double* D = DX + ((size_t)(k * n1 + j) * n1 + i) * 9;
+#pragma unroll
+          for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd) J[nn][dd] = J[nn][dd] + __ldg(D + 3 * nn + dd) * buff2;
+        }
+      }
+    double sdet = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * J[2][2] + (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * J[2][0] +
+                  (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * J[2][1];
+    if (sdet > 0.0) sdet = 1.0 / sdet;
+    double sJ[3][3];
+    sJ[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * sdet;
+    sJ[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * sdet;
+    sJ[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * sdet;
+    sJ[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * sdet;
+    sJ[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * sdet;
+    sJ[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * sdet;
+    sJ[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * sdet;
+    sJ[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * sdet;
+    sJ[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * sdet;
+    double dxi[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) dxi[r] = ((0.0 + sJ[r][0] * F[0]) + sJ[r][1] * F[1]) + sJ[r][2] * F[2];
+    deltaXi2 = dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2];
+    const double xo[3] = {xi[0], xi[1], xi[2]};
+    const double normFold = normF;
+    normF = normF * 2.0;
+    double lambda = 1.0;
+    for (int iArmijo = 1; normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
+      for (int d = 0; d < 3; ++d) xi[d] = xo[d] - lambda * dxi[d];
+      for (int d = 0; d < 3; ++d) lagrange_rt(xi[d], n1, kc.xi_cl_ng, kc.wbary_cl_ng, L[d]);
+      F[0] = -x[0]; F[1] = -x[1]; F[2] = -x[2];
+      for (int k = 0; k < n1; ++k)
+        for (int j = 0; j < n1; ++j) {
+          const double buff = L[1][j] * L[2][k];
+          for (int i = 0; i < n1; ++i) {
+            const double buff2 = L[0][i] * buff;
+            const double* P = X + ((size_t)(k * n1 + j) * n1 + i) * 3;
+            for (int c = 0; c < 3; ++c) F[c] = F[c] + __ldg(P + c) * buff2;
+          }
+        }
+      lambda = 0.2 * lambda;
+      normF = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+    }
+    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = false; break; }
+  }
+  return success;
+}
+
+// GetPositionInRefElem (eval_xyz.f90:87-117): the NGeo Newton for a curved element of an NGeo > 1 mesh, the
+// NGeo = 1 Newton on the corners otherwise
+__device__ __forceinline__ bool elem_curved(const DevMesh& M, int e) {
+  return M.xcl_ng && (!M.curved || __ldg(M.curved + e) != 0);
+}
+
 __device__ __forceinline__ bool position_in_ref_elem(const DevMesh& M, int e, const double x[3], double xi[3]) {
   newton_start(M, e, x, xi);
-  return ref_elem_newton(M, e, x, xi);
+  return elem_curved(M, e) ? ref_elem_newton_ng(M, e, x, xi) : ref_elem_newton(M, e, x, xi);
 }
 
 template <bool FAST>
 __device__ __forceinline__ bool position_in_ref_elem_t(const DevMesh& M, int e, const double x[3], double xi[3]) {
   newton_start(M, e, x, xi);
+  if (elem_curved(M, e)) return ref_elem_newton_ng(M, e, x, xi);
   return FAST ? ref_elem_newton_fast(M, e, x, xi) : ref_elem_newton(M, e, x, xi);
 }
 

@@ -158,8 +158,8 @@ class BoxMesh:
     xgp: np.ndarray
     wgp: np.ndarray
     wbary_gp: np.ndarray
-    xcl_ngeo: np.ndarray                  # (3,0:1,0:1,0:1,nElems) -> C [e][c][b][a][3]
-    dxcl_ngeo: np.ndarray                 # (3,3,0:1,0:1,0:1,nElems) -> C [e][c][b][a][nn][dd]
+    xcl_ngeo: np.ndarray                  # (3,0:NGeo,0:NGeo,0:NGeo,nElems) -> C [e][c][b][a][3]
+    dxcl_ngeo: np.ndarray                 # (3,3,0:NGeo,0:NGeo,0:NGeo,nElems) -> C [e][c][b][a][nn][dd]
     elem_bary: np.ndarray                 # (3,nElems)
     xez_basis: np.ndarray                 # (3,6,nElems)
     slen_basis: np.ndarray                # (6,nElems)
@@ -191,6 +191,7 @@ class BoxMesh:
     sf_elem_radius: np.ndarray = field(default=None)  # SFElemr2_Shared(1,:) for shape_function_adaptive
     # RefTracking with walls: BuildBCElemDistance output (see build_bc_elem_distance)
     n_loc: np.ndarray = field(default=None)          # per-element degree Nloc (p-adaption); None: N everywhere
+    elem_curved: np.ndarray = field(default=None)    # ElemCurved (0/1) of an NGeo > 1 mesh; None at NGeo = 1
     dof_offset: np.ndarray = field(default=None)     # N_DG_Mapping(1,:): 0-based DOF offset of each element (nElems+1)
     elem_to_bc_sides: np.ndarray = field(default=None)
     bc_side_elem_loc: np.ndarray = field(default=None)
@@ -254,11 +255,15 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                    perturb: float = 0.0, refmapping_eps: float = 1.0e-4,
                    bc=("periodic", "periodic", "periodic"), bc_halo_eps: float | None = None,
                    wall_bulge: float = 0.0, wall_shear: float = 0.0, periodic_tracing: bool = False,
-                   n_loc=None) -> BoxMesh:
+                   n_loc=None, n_geo: int = 1) -> BoxMesh:
     """Build a box of nx*ny*nz NGeo=1 hexahedra with DG degree N.
 
     ``n_loc`` (p-adaption): the degree Nloc of every element (1..N, N is then NMax); the DOF arrays are then
     packed element by element (N_DG_Mapping offsets), and NodeVolume and ElemEpsOneCell use each element's Nloc.
+    ``n_geo`` > 1: curved elements of geometry degree NGeo -- XCL_NGeo at the Chebyshev-Gauss-Lobatto points of
+    each element, displaced by the same smooth ``perturb`` field as the grid nodes (so the faces are curved,
+    conforming and periodic), with dXCL_NGeo from the CL derivative matrix, ElemCurved, ElemRadiusNGeo from the
+    sides' Bezier control points and the FIBGM from the elements' Bezier bounding boxes (periodic boxes only).
 
     ``perturb`` displaces every interior node by ``perturb*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)``
     along each axis (h per axis); boundary nodes stay put so the periodic faces match.
@@ -274,6 +279,10 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     The face edges stay put.
     """
     bc = tuple(bc)
+    if n_geo < 1 or n_geo > 4:
+        raise ValueError("n_geo must be 1..4")
+    if n_geo > 1 and (any(b != "periodic" for b in bc) or wall_bulge or wall_shear or periodic_tracing):
+        raise ValueError("curved elements (n_geo > 1) are built for fully periodic boxes with CartesianPeriodic")
     if len(bc) != 3 or any(b not in ("periodic", "open", "reflective") for b in bc):
         raise ValueError(f"bc must hold 'periodic', 'open' or 'reflective' per axis, got {bc}")
     periodic = [b == "periodic" for b in bc]
@@ -339,19 +348,51 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     node_coords = np.ascontiguousarray(xcl.reshape(ne, 8, 3))   # NodeCoords_Shared(1:3, 8e+t+1)
 
     # ---- reference-element data ------------------------------------------------------
-    xi_cl = cheby_gauss_lobatto_nodes(1)
+    ng1 = n_geo + 1
+    xi_cl = cheby_gauss_lobatto_nodes(n_geo)
     wb_cl = barycentric_weights(xi_cl)
     xgp, wgp = legendre_gauss_nodes(N)
     wb_gp = barycentric_weights(xgp)
+    if n_geo > 1:
+        # XCL_NGeo: the unperturbed position of every CL point of the element, moved by the perturbation field
+        # (points on the domain boundary stay put); the corner points coincide with the grid nodes above
+        t = 0.5 * (np.asarray(xi_cl) + 1.0)
+        xcl = np.empty((ne, ng1, ng1, ng1, 3))
+        idx = np.stack([ei, ej, ek], axis=1).astype(np.float64)
+        dims_f = np.array([nx, ny, nz], dtype=np.float64)
+        for c in range(ng1):
+            for b in range(ng1):
+                for a in range(ng1):
+                    g = idx + np.array([t[a], t[b], t[c]])          # grid-index coordinates
+                    p0 = lo + g * hvec
+                    p0 = np.where(g >= dims_f, hi, p0)
+                    if perturb != 0.0:
+                        inner = np.all((g > 0.0) & (g < dims_f), axis=1)
+                        sv = (np.sin(2.0 * np.pi * (p0[:, 0] - lo[0]) / L[0]) * np.sin(2.0 * np.pi * (p0[:, 1] - lo[1]) / L[1])
+                              * np.sin(2.0 * np.pi * (p0[:, 2] - lo[2]) / L[2]))
+                        p0 = np.where(inner[:, None], p0 + perturb * hvec[None, :] * sv[:, None], p0)
+                    xcl[:, c, b, a, :] = p0
+        for c in range(2):
+            for b in range(2):
+                for a in range(2):
+                    if not np.array_equal(xcl[:, c * n_geo, b * n_geo, a * n_geo, :], node_coords[:, a + 2 * b + 4 * c, :]):
+                        raise RuntimeError("curved element corners differ from the grid nodes")
 
-    # dXCL_NGeo(dd,nn,i,j,k) = sum_l D(i,l) X(nn,l,j,k) ... (metrics.f90:309-318), D = +-0.5
-    D = np.array([[-0.5, 0.5], [-0.5, 0.5]])
-    dxcl = np.zeros((ne, 2, 2, 2, 3, 3), dtype=np.float64)  # [e][c][b][a][nn][dd]
-    for c in range(2):
-        for b in range(2):
-            for a in range(2):
+    # dXCL_NGeo(dd,nn,i,j,k) = sum_l D(i,l) X(nn,l,j,k) ... (metrics.f90:309-318), D the derivative matrix of the
+    # Lagrange basis on the CL points (PolynomialDerivativeMatrix: D(i,j) = w_j/w_i/(x_i-x_j), D(i,i) = -sum);
+    # at NGeo = 1 D = +-0.5
+    D = np.zeros((ng1, ng1))
+    for i in range(ng1):
+        for j in range(ng1):
+            if i != j:
+                D[i, j] = wb_cl[j] / wb_cl[i] / (xi_cl[i] - xi_cl[j])
+        D[i, i] = -sum(D[i, j] for j in range(ng1) if j != i)
+    dxcl = np.zeros((ne, ng1, ng1, ng1, 3, 3), dtype=np.float64)  # [e][c][b][a][nn][dd]
+    for c in range(ng1):
+        for b in range(ng1):
+            for a in range(ng1):
                 acc = np.zeros((ne, 3, 3))
-                for l in range(2):
+                for l in range(ng1):
                     acc[:, :, 0] = acc[:, :, 0] + D[a, l] * xcl[:, c, b, l, :]
                     acc[:, :, 1] = acc[:, :, 1] + D[b, l] * xcl[:, c, l, a, :]
                     acc[:, :, 2] = acc[:, :, 2] + D[c, l] * xcl[:, l, b, a, :]
@@ -360,10 +401,10 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     # ElemBaryNGeo: evaluate at xi = 0 (particle_mesh_build.f90:1446-1466)
     L0 = lagrange_polys(0.0, xi_cl, wb_cl)
     bary = np.zeros((ne, 3))
-    for c in range(2):
-        for b in range(2):
+    for c in range(ng1):
+        for b in range(ng1):
             buf = L0[b] * L0[c]
-            for a in range(2):
+            for a in range(ng1):
                 bary = bary + xcl[:, c, b, a, :] * L0[a] * buf
 
     # XiEtaZetaBasis, slenXiEtaZetaBasis, ElemRadiusNGeo (particle_mesh_build.f90:1625-1678)
@@ -375,14 +416,43 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         Lb = lagrange_polys(xi[1], xi_cl, wb_cl)
         Lc = lagrange_polys(xi[2], xi_cl, wb_cl)
         xp = np.zeros((ne, 3))
-        for c in range(2):
-            for b in range(2):
-                for a in range(2):
+        for c in range(ng1):
+            for b in range(ng1):
+                for a in range(ng1):
                     xp = xp + xcl[:, c, b, a, :] * La[a] * Lb[b] * Lc[c]
         v = xp - bary
         xez[:, d, :] = v
         slen[:, d] = 1.0 / np.einsum("ij,ij->i", v, v)
-    radius = np.sqrt(np.max(np.sum((node_coords - bary[:, None, :]) ** 2, axis=2), axis=1))
+    if n_geo == 1:
+        radius = np.sqrt(np.max(np.sum((node_coords - bary[:, None, :]) ** 2, axis=2), axis=1))
+        elem_curved = None
+        bez = None
+    else:
+        # Bezier control points of the element (Bernstein coefficients of the map: solve V c = X along each axis,
+        # V(i,j) = B_j(t_i) on the CL points), the sides' control points bound ElemRadiusNGeo (:1662-1672) and the
+        # element's control points its bounding box (convex hull property)
+        tt = 0.5 * (np.asarray(xi_cl) + 1.0)
+        V = np.array([[math.comb(n_geo, j) * tt[i] ** j * (1.0 - tt[i]) ** (n_geo - j) for j in range(ng1)]
+                      for i in range(ng1)])
+        Vi = np.linalg.inv(V)
+        bez = np.einsum("ai,ebcij->ebcaj", Vi, xcl)
+        bez = np.einsum("bi,ecijk->ecbjk", Vi, bez)
+        bez = np.einsum("ci,eijkl->ecjkl", Vi, bez)
+        side_pts = np.concatenate([bez[:, 0].reshape(ne, -1, 3), bez[:, -1].reshape(ne, -1, 3),
+                                   bez[:, :, 0].reshape(ne, -1, 3), bez[:, :, -1].reshape(ne, -1, 3),
+                                   bez[:, :, :, 0].reshape(ne, -1, 3), bez[:, :, :, -1].reshape(ne, -1, 3)], axis=1)
+        radius = np.sqrt(np.max(np.sum((side_pts - bary[:, None, :]) ** 2, axis=2), axis=1))
+        # ElemCurved: XCL_NGeo differs by more than 1e-14 from the trilinear interpolation of its corners
+        # (IdentifyElemAndSideType with PointsEqual, particle_mesh_tools.f90:953-967,1238-1268)
+        lin = np.zeros_like(xcl)
+        for c in range(ng1):
+            for b in range(ng1):
+                for a in range(ng1):
+                    w = [(1.0 - tt[a], tt[a]), (1.0 - tt[b], tt[b]), (1.0 - tt[c], tt[c])]
+                    for q in range(8):
+                        qa, qb, qc = q & 1, (q >> 1) & 1, q >> 2
+                        lin[:, c, b, a, :] += w[0][qa] * w[1][qb] * w[2][qc] * node_coords[:, q, :]
+        elem_curved = np.any(np.abs(lin - xcl) > 1e-14, axis=(1, 2, 3, 4)).astype(np.int32)
 
     # ---- Gauss points, Jacobian (trilinear map) -------------------------------------
     def dof_geometry(sel, Nd):
@@ -398,9 +468,9 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                 for i in range(nd):
                     xp = np.zeros((m, 3))
                     J = np.zeros((m, 3, 3))
-                    for c in range(2):
-                        for b in range(2):
-                            for a in range(2):
+                    for c in range(ng1):
+                        for b in range(ng1):
+                            for a in range(ng1):
                                 w = lg[i][a] * lg[j][b] * lg[k][c]
                                 xp = xp + xcl[sel, c, b, a, :] * w
                                 J = J + dxcl[sel, c, b, a, :, :] * w      # [nn][dd]
@@ -569,8 +639,8 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     # ---- FIBGM: one background cell per unperturbed element cell ----------------------
     fib_imax = (nx, ny, nz)
     fib_d = hvec.copy()
-    bmin = node_coords.min(axis=1)
-    bmax = node_coords.max(axis=1)
+    bmin = node_coords.min(axis=1) if bez is None else bez.reshape(ne, -1, 3).min(axis=1)
+    bmax = node_coords.max(axis=1) if bez is None else bez.reshape(ne, -1, 3).max(axis=1)
     cells = [[] for _ in range(nx * ny * nz)]
     for e in range(ne):
         imn = [max(int(math.floor((bmin[e, d] - lo[d]) / fib_d[d])) + 1, 1) for d in range(3)]
@@ -589,7 +659,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         pv[d, q - 1] = L[d]
 
     mesh = BoxMesh(
-        nx=nx, ny=ny, nz=nz, N=N, lo=lo, hi=hi, n_elems=ne, n_nodes=n_unique, n_geo=1,
+        nx=nx, ny=ny, nz=nz, N=N, lo=lo, hi=hi, n_elems=ne, n_nodes=n_unique, n_geo=n_geo,
         periodic_vectors=pv,
         xi_cl_ngeo=np.asarray(xi_cl), wbary_cl_ngeo=np.asarray(wb_cl),
         xgp=np.asarray(xgp), wgp=np.asarray(wgp), wbary_gp=np.asarray(wb_gp),
@@ -605,6 +675,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         fibgm_imax=fib_imax, fibgm_deltas=fib_d, fibgm_n_elems=fib_n, fibgm_offset=fib_off,
         fibgm_element=fib_el, canonical_node=canon,
         side_bc=side_bc if side_bc.any() else None, bc=bc, n_loc=n_loc, dof_offset=dof_offset,
+        elem_curved=elem_curved,
     )
     if (side_bc.any() and not any(periodic)) or (periodic_tracing and any(periodic)):
         halo = float(hvec.max()) if bc_halo_eps is None else float(bc_halo_eps)
@@ -837,13 +908,14 @@ def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float, include_periodic: 
 
 
 def elem_map(mesh: BoxMesh, e: int, xi) -> np.ndarray:
-    """x(xi) of element e (0-based) through the trilinear CL interpolation."""
+    """x(xi) of element e (0-based) through the Lagrange interpolation of XCL_NGeo on the CL points."""
     La = lagrange_polys(float(xi[0]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
     Lb = lagrange_polys(float(xi[1]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
     Lc = lagrange_polys(float(xi[2]), mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo)
     x = np.zeros(3)
-    for c in range(2):
-        for b in range(2):
-            for a in range(2):
+    ng1 = mesh.n_geo + 1
+    for c in range(ng1):
+        for b in range(ng1):
+            for a in range(ng1):
                 x = x + mesh.xcl_ngeo[e, c, b, a] * La[a] * Lb[b] * Lc[c]
     return x

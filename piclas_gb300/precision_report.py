@@ -37,7 +37,7 @@ def mixed_vs_fp64_per_step(w, nsteps: int, sort_interval: int = 0) -> list[dict]
         for k in range(nsteps):
             res = {}
             for prec, loop in loops.items():
-                PS = np.zeros((w.mesh.n_elems, w.mesh.n_dof, 4))
+                PS = np.zeros(w.mesh.dof_shape(4))
                 loop.time_step(w.dt, 1, PS)
                 loop.interpolate_field_to_particle()
                 F = loop.field_at_particles()

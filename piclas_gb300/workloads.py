@@ -144,6 +144,31 @@ def _trilinear(mesh: BoxMesh, e0: np.ndarray, xi: np.ndarray):
     return x, det
 
 
+def _lagrange_vec(x: np.ndarray, nodes, wbary) -> np.ndarray:
+    """Lagrange basis on the nodes at every x (barycentric form; Kronecker at a node), shape (len(x), len(nodes))."""
+    nodes = np.asarray(nodes, dtype=np.float64)
+    d = x[:, None] - nodes[None, :]
+    hit = d == 0.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t = np.asarray(wbary)[None, :] / d
+        L = t / t.sum(axis=1, keepdims=True)
+    rows = hit.any(axis=1)
+    L[rows] = hit[rows].astype(np.float64)
+    return L
+
+
+def _curved_map(mesh: BoxMesh, e0: np.ndarray, xi: np.ndarray):
+    """x(xi) and det J of the NGeo map (Lagrange on the CL points) for elements e0 (0-based), vectorised."""
+    ng1 = mesh.n_geo + 1
+    L = [_lagrange_vec(xi[:, d], mesh.xi_cl_ngeo, mesh.wbary_cl_ngeo) for d in range(3)]
+    X = mesh.xcl_ngeo.reshape(mesh.n_elems, ng1, ng1, ng1, 3)[e0]
+    DX = mesh.dxcl_ngeo.reshape(mesh.n_elems, ng1, ng1, ng1, 3, 3)[e0]
+    w = np.einsum("na,nb,nc->ncba", L[0], L[1], L[2])
+    x = np.einsum("ncba,ncbad->nd", w, X)
+    J = np.einsum("ncba,ncbaij->nij", w, DX)              # [nn][dd] = d x_nn / d xi_dd
+    return x, np.linalg.det(J)
+
+
 def _uniform_in_mesh(mesh: BoxMesh, n: int, rng, chunk: int = 1 << 20) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Positions uniform in space, with their element and reference coordinates (chunked)."""
     x = np.empty((n, 3))
@@ -157,7 +182,7 @@ def _uniform_in_mesh(mesh: BoxMesh, n: int, rng, chunk: int = 1 << 20) -> tuple[
         m = min(chunk, int((n - got) * 1.4) + 1024)
         e0 = rng.integers(0, mesh.n_elems, size=m)
         xr = rng.random((m, 3)) * 2.0 - 1.0
-        xc, det = _trilinear(mesh, e0, xr)
+        xc, det = _trilinear(mesh, e0, xr) if mesh.n_geo == 1 else _curved_map(mesh, e0, xr)
         if det.max() >= dmax or det.min() <= 0.0:
             raise RuntimeError("element Jacobian outside the sampling bound")
         keep = np.nonzero(rng.random(m) * dmax < det)[0][: n - got]

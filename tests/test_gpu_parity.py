@@ -1288,3 +1288,64 @@ def test_ref_mapping_guess_against_oracle(gpu_lib, oracle_lib, guess, kind):
     gm = lm.download_particles()
     lm.close()
     assert (gm["elem"] != st.elem).sum() <= 2
+
+
+# ---- curved elements (NGeo > 1) --------------------------------------------------------------------------------
+def _curved_ngeo(ng, deposition, seed, n=6000, tracking=capi.PIC_TRACK_REFMAPPING):
+    mesh = build_box_mesh(5, 5, 5, 3, perturb=0.08, n_geo=ng)
+    w = workloads.curved_two_species(mesh=mesh, n_per_species=n // 2, seed=seed, Te_eV=1000.0, nsteps=5)
+    w.dt *= 10.0
+    w.deposition = deposition
+    w.tracking = tracking
+    return w
+
+
+@pytest.mark.parametrize("ng,dep", [(2, capi.PIC_DEPO_SHAPE_FUNCTION), (3, capi.PIC_DEPO_SHAPE_FUNCTION),
+                                    (2, capi.PIC_DEPO_CVWM), (2, capi.PIC_DEPO_SHAPE_FUNCTION_CC)])
+def test_curved_ngeo_against_oracle(gpu_lib, oracle_lib, ng, dep):
+    """Curved elements (NGeo 2, 3): the Newton on XCL_NGeo (RefTracking, the FIBGM candidate search, the deposition
+    and the interpolation) against the oracle -- elements exact, states within 1e-13, PartPosRef within 1e-10,
+    PartSource within 1e-12 of its maximum; mixed: elements within two, rho within 1e-6 of max sum_s |rho_s|."""
+    w = _curved_ngeo(ng, dep, seed=41)
+    g = _run_gpu(w, w.nsteps)
+    st, PS = _run_oracle(oracle_lib, w, w.nsteps)
+    assert np.array_equal(g["elem"], st.elem) and np.array_equal(g["inside"], st.inside)
+    assert _rel(g["part_state"][:, :3], st.part_state[:, :3]) <= 1e-13
+    assert _rel(g["part_state"][:, 3:], st.part_state[:, 3:]) <= 1e-13
+    assert np.max(np.abs(g["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0 and (st.elem != w.elem).sum() > 20
+    gm = _run_gpu(w, w.nsteps, precision=capi.PIC_PREC_MIXED)
+    assert (gm["elem"] != st.elem).sum() <= 2
+    assert _rho_err_species(oracle_lib, w, st, gm["PS"], PS) <= 1e-6
+
+
+def test_curved_ngeo_triatracking_against_oracle(gpu_lib, oracle_lib):
+    """TriaTracking + cell_volweight_mean on an NGeo = 2 box: the tracking walks the triangulated corner faces,
+    the deposition and the interpolation map x -> xi with the curved Newton; against the oracle with exact
+    elements, including which particles the triangulated faces lose (curved faces bulge beyond them), and states
+    within 1e-13 (B_z: CUDA's tan against libm's)."""
+    w = _curved_ngeo(2, capi.PIC_DEPO_CVWM, seed=43, tracking=capi.PIC_TRACK_TRIA)
+    g = _run_gpu(w, w.nsteps)
+    st, PS = _run_oracle(oracle_lib, w, w.nsteps)
+    assert np.array_equal(g["elem"], st.elem) and np.array_equal(g["inside"], st.inside)
+    assert _rel(g["part_state"], st.part_state) <= 1e-13
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["n_lost"] == st.counters.n_lost
+
+
+def test_curved_ngeo_uncurved_elements_use_corner_newton(gpu_lib, oracle_lib):
+    """An NGeo = 2 box without perturbation has no curved element: GetPositionInRefElem then runs the NGeo = 1
+    Newton on the corners with their dXCL_NGeo; GPU and oracle agree bit-for-bit, and both agree with the
+    NGeo = 1 box to rounding."""
+    res = []
+    for ng in (2, 1):
+        mesh = build_box_mesh(5, 5, 5, 3, n_geo=ng)
+        w = workloads.curved_two_species(mesh=mesh, n_per_species=3000, seed=44, Te_eV=1000.0, nsteps=4)
+        g = _run_gpu(w, 4)
+        st, PS = _run_oracle(oracle_lib, w, 4)
+        assert np.array_equal(g["elem"], st.elem)
+        assert _rel(g["part_state"], st.part_state) <= 1e-13
+        res.append(g)
+    assert np.array_equal(res[0]["elem"], res[1]["elem"])
+    assert _rel(res[0]["part_state"], res[1]["part_state"]) <= 1e-12
