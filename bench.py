@@ -415,7 +415,8 @@ def run_gpu(args, rank, world, local_rank):
     except Exception:
         fma_peak = None
     dom = prof["deposit_main"]
-    avg_ms = dom["ms"] / max(dom["launches"], 1)
+    # a p-adapted mesh gathers with one launch per degree: the gather of a step is all of them
+    avg_ms = dom["ms"] / max(dom["launches"] if w.mesh.n_loc is None else args.steps, 1)
     peak, peak_kind = hbm_peak()
     achieved = kbytes / (avg_ms / 1e3) / 1e9
     default_size = args.cells is None and args.particles is None
@@ -531,7 +532,7 @@ def mixed_arm(args, w):
         fp32_peak = None
     loop.close()
     dom = prof["deposit_main"]
-    avg_ms = dom["ms"] / max(dom["launches"], 1)
+    avg_ms = dom["ms"] / max(dom["launches"] if w.mesh.n_loc is None else args.steps, 1)
     kname, kbytes = dominant_kernel_bytes(w, True)
     out = {"value": w.n * args.steps / (ms / 1e3), "unit": "particle-steps/s", "ms_per_step": ms / args.steps,
            "phases_ms": {k: round(v["ms"] / args.steps, 4) for k, v in prof.items() if v["launches"]},
