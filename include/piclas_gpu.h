@@ -218,10 +218,17 @@ typedef struct pic_mesh_t {
    * runs on XCL_NGeo/dXCL_NGeo at NGeo for a curved element and on its eight corners (with dXCL_NGeo of the
    * corners) otherwise (GetPositionInRefElem, eval_xyz.f90:87-117); NULL: every element curved.  node_coords
    * holds the corners; elem_bary, xez_basis, slen_basis, elem_radius, elem_xgp, elem_sj and the FIBGM are
-   * those of the curved map.  NGeo > 1 is built for meshes without open/reflective walls and with
-   * CartesianPeriodic (periodic_tracing = 0): curved side intersections (ComputeCurvedIntersection,
-   * particle_intersection.f90) are not built; the differentiable loop needs NGeo = 1. */
+   * those of the curved map; BC sides need side_bezier and side_type below.  The differentiable loop needs
+   * NGeo = 1. */
   const int32_t* elem_curved;
+  /* BC sides of curved elements (NGeo > 1 with BC-element lists): BezierControlPoints3D(1:3,0:NGeo,0:NGeo) of
+   * every local side (1:6) of every element in the element's own orientation (its master orientation;
+   * RotateMasterToSlave, particle_surfaces.f90:1171-1202, of the master's points for a slave side), and SideType
+   * of those sides (PLANAR_RECT 0, PLANAR_NONRECT 1, BILINEAR 2, PLANAR_CURVED 3, CURVED 4; IdentifyElemAndSideType,
+   * particle_mesh_tools.f90:848-1235).  PLANAR_CURVED sides are traced by ComputePlanarCurvedIntersection, CURVED
+   * ones by ComputeCurvedIntersection (Bezier clipping); NULL at NGeo = 1 (the corners give the side geometry). */
+  const double* side_bezier;
+  const int32_t* side_type;
 } pic_mesh_t;
 
 typedef struct pic_status_t {

@@ -14,6 +14,7 @@
  * deposition, TriaTracking, and RefTracking with CartesianPeriodic = FastPeriodic = T.
  */
 #include "pic_oracle.h"
+#include "pic_oracle_bezier.h"
 
 #include <float.h>
 #include <math.h>
@@ -665,12 +666,16 @@ static int almost_equal(double x, double y) { return fabs(x - y) <= fmax(fabs(x)
  * SideNormVec / SideDistance oriented away from the element (particle_mesh_tools.f90:1011-1048). */
 typedef struct {
   double bv0[3], bv1[3], bv2[3], bv3[3], n[3], dist, P[4][3];
-  int bc, type;                     /* type: SideType PLANAR_RECT (0), PLANAR_NONRECT (1), BILINEAR (2) */
+  int bc, type;                     /* type: SideType PLANAR_RECT (0), PLANAR_NONRECT (1), BILINEAR (2),
+                                       PLANAR_CURVED (3), CURVED (4) */
   int pvid, nb;                     /* bc = 3 (periodic): BoundaryType(BC_ALPHA) and SIDE_NBELEMID (1-based) */
+  orc_bz_side_t bz;                 /* curved sides (NGeo > 1): Bezier points, slab normals and intervals */
 } orc_bc_side_t;
-enum { ORC_PLANAR_RECT = 0, ORC_PLANAR_NONRECT = 1, ORC_BILINEAR = 2 };
+enum { ORC_PLANAR_RECT = 0, ORC_PLANAR_NONRECT = 1, ORC_BILINEAR = 2, ORC_PLANAR_CURVED = 3, ORC_CURVED = 4 };
 
+/* corner (p,q) in {0,1} of local side s of element e (0-based): XCL_NGeo at the volume index of CGNS_SideToVol2 */
 static void side_corner(const pic_mesh_t* m, int e, int s, int p, int q, double out[3]) {
+  const int ng = m->n_geo;
   int a, b, c;
   switch (s) {
     case 0: a = q; b = p; c = 0; break;
@@ -680,8 +685,7 @@ static void side_corner(const pic_mesh_t* m, int e, int s, int p, int q, double 
     case 4: a = 0; b = q; c = p; break;
     default: a = p; b = q; c = 1; break;
   }
-  const double* X = m->xcl_ngeo + ((((size_t)e * 2 + c) * 2 + b) * 2 + a) * 3;
-  out[0] = X[0]; out[1] = X[1]; out[2] = X[2];
+  for (int k = 0; k < 3; ++k) out[k] = XCL(m, k, a * ng, b * ng, c * ng, e + 1);
 }
 
 static void unit3(const double v[3], double u[3]) {
@@ -697,6 +701,13 @@ static void unit3(const double v[3], double u[3]) {
  * angles (:1026-1041), PLANAR_NONRECT otherwise; a non-planar side is BILINEAR with the non-oriented
  * averaged normal.  Returns the type. */
 static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t* g) {
+  memset(g, 0, sizeof(*g));
+  if (m->n_geo > 1) {
+    /* curved mesh: the side's Bezier points and the reference's SideType; SideNormVec/SideDistance of a planar
+     * side from its corners as below (IdentifyElemAndSideType, particle_mesh_tools.f90:991-1012) */
+    const size_t n2 = (size_t)(m->n_geo + 1) * (m->n_geo + 1);
+    orc_bz_side_init(&g->bz, m->n_geo, &m->side_bezier[((size_t)e * 6 + s) * n2 * 3]);
+  }
   double P00[3], P10[3], P01[3], P11[3];
   side_corner(m, e, s, 0, 0, P00); side_corner(m, e, s, 1, 0, P10);
   side_corner(m, e, s, 0, 1, P01); side_corner(m, e, s, 1, 1, P11);
@@ -728,10 +739,11 @@ static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t
   const double l1 = 0.5 * sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
   const double l2 = 0.5 * sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
   const double h = hmax - hmin, dmax = fmax(h, fmax(l1, l2));
-  if (!(h < 1.0e-6 * dmax)) {
+  const int given = m->n_geo > 1 ? m->side_type[(size_t)e * 6 + s] : -1;
+  if (given == ORC_BILINEAR || given == ORC_CURVED || (given < 0 && !(h < 1.0e-6 * dmax))) {
     for (int c = 0; c < 3; ++c) g->n[c] = n[c];
     g->dist = 0.0;
-    g->type = ORC_BILINEAR;
+    g->type = given == ORC_CURVED ? ORC_CURVED : ORC_BILINEAR;
     return g->type;
   }
   const double* bary = &m->elem_bary[(size_t)e * 3];
@@ -746,7 +758,7 @@ static int orc_bc_side_geometry(const pic_mesh_t* m, int e, int s, orc_bc_side_t
   int rect = fabs(DOT3(u1, u2)) <= 2.22e-16 && fabs(DOT3(u1, u3)) <= 2.22e-16;
   if (rect) rect = fabs(DOT3(u4, u2)) <= 2.22e-16 && fabs(DOT3(u4, u3)) <= 2.22e-16;
 #undef DOT3
-  g->type = rect ? ORC_PLANAR_RECT : ORC_PLANAR_NONRECT;
+  g->type = given >= 0 ? given : (rect ? ORC_PLANAR_RECT : ORC_PLANAR_NONRECT);
   return g->type;
 }
 
@@ -918,6 +930,12 @@ static int bc_tracking(const pic_mesh_t* m, const orc_bc_side_t* geo, int* elem,
         sxi[nc] = 0.0; seta[nc] = 0.0;
         if (g->type == ORC_PLANAR_RECT) {
           alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+        } else if (g->type == ORC_PLANAR_CURVED || g->type == ORC_CURVED) {
+          int bad = 0;
+          alpha[nc] = g->type == ORC_CURVED
+                          ? orc_bz_curved(&g->bz, g->n, xl, x, traj, len, &sxi[nc], &seta[nc], &bad)
+                          : orc_bz_planar_curved(&g->bz, g->n, g->dist, xl, traj, len, &sxi[nc], &seta[nc], &bad);
+          if (bad) (*ncap)++;
         } else {
           int bad = 0;
           alpha[nc] = bilinear_alpha(g, xl, traj, len, doubleCheck ? alphaOld : -1.0, &sxi[nc], &seta[nc], &bad);
@@ -946,6 +964,7 @@ static int bc_tracking(const pic_mesh_t* m, const orc_bc_side_t* geo, int* elem,
          * planar sides, CalcNormAndTangBilinear at the hit of bilinear ones */
         double nl[3] = {g->n[0], g->n[1], g->n[2]};
         if (g->type == ORC_BILINEAR) bilinear_normal(g, sxi[slot[k]], seta[slot[k]], nl);
+        if (g->type == ORC_PLANAR_CURVED || g->type == ORC_CURVED) orc_bz_normal(&g->bz, sxi[slot[k]], seta[slot[k]], nl);
         if (nl[0] * traj[0] + nl[1] * traj[1] + nl[2] * traj[2] <= 0.0) { reflected = 0; continue; }
         reflected = 1;
         if (g->bc == 1) { *inside = 0; break; }                  /* RemoveParticle */

@@ -68,7 +68,7 @@ class PicMesh(C.Structure):
         ("fibgm_offset", _ip), ("fibgm_element", _ip), ("fibgm_n_total", C.c_int32),
         ("side_bc", _ip), ("sf_elem_radius", _dp),
         ("n_bc_entries", C.c_int32), ("elem_to_bc_sides", _ip), ("bc_side_elem_loc", _ip), ("bc_side_distance", _dp),
-        ("n_dg_mapping", _ip), ("n_inter", _dp), ("elem_curved", _ip),
+        ("n_dg_mapping", _ip), ("n_inter", _dp), ("elem_curved", _ip), ("side_bezier", _dp), ("side_type", _ip),
     ]
 
 
@@ -230,6 +230,10 @@ class MeshStruct:
             s.n_inter = C.POINTER(C.c_double)()
         ec = getattr(mesh, "elem_curved", None)
         s.elem_curved = i("ecurv", ec) if ec is not None else C.POINTER(C.c_int32)()
+        sbz = getattr(mesh, "side_bezier", None)
+        s.side_bezier = d("sbez", sbz) if sbz is not None else C.POINTER(C.c_double)()
+        sty = getattr(mesh, "side_type", None)
+        s.side_type = i("stype", sty) if sty is not None else C.POINTER(C.c_int32)()
         self.struct = s
         self._keep = keep
 

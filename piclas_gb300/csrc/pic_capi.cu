@@ -829,6 +829,44 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     double* d_tc = nullptr;
     if ((rc = upload(c, &d_tc, tc))) return bail(rc);
     c->M.tcoef = d_tc;
+    if (ng > 1) {
+      // the NGeo map in power form: along each axis C_a = sum_i T(a,i) X_i with T = V^-1, V(i,a) = XiCL_i^a
+      double V[5][10];
+      for (int i = 0; i < g1; ++i)
+        for (int a = 0; a < g1; ++a) {
+          V[i][a] = std::pow(m->xi_cl_ngeo[i], a);
+          V[i][g1 + a] = i == a ? 1.0 : 0.0;
+        }
+      for (int col = 0; col < g1; ++col) {
+        int p = col;
+        for (int r = col + 1; r < g1; ++r) if (std::fabs(V[r][col]) > std::fabs(V[p][col])) p = r;
+        for (int q = 0; q < 2 * g1; ++q) std::swap(V[col][q], V[p][q]);
+        const double piv = V[col][col];
+        for (int q = 0; q < 2 * g1; ++q) V[col][q] /= piv;
+        for (int r = 0; r < g1; ++r)
+          if (r != col) { const double fct = V[r][col]; for (int q = 0; q < 2 * g1; ++q) V[r][q] -= fct * V[col][q]; }
+      }
+      std::vector<double> pc((size_t)ne * g3 * 3);
+      for (int e = 0; e < ne; ++e)
+        for (int k = 0; k < 3; ++k) {
+          double A[125], B[125];
+          for (size_t q = 0; q < g3; ++q) A[q] = m->xcl_ngeo[((size_t)e * g3 + q) * 3 + k];
+          for (int ax = 0; ax < 3; ++ax) {
+            const int st = ax == 0 ? 1 : ax == 1 ? g1 : g1 * g1;
+            for (int q = 0; q < (int)g3; ++q) {
+              const int aa = (q / st) % g1, base = q - aa * st;
+              double v = 0.0;
+              for (int l = 0; l < g1; ++l) v += V[aa][g1 + l] * A[base + l * st];
+              B[q] = v;
+            }
+            for (size_t q = 0; q < g3; ++q) A[q] = B[q];
+          }
+          for (size_t q = 0; q < g3; ++q) pc[((size_t)e * g3 + q) * 3 + k] = A[q];
+        }
+      double* d_pc = nullptr;
+      if ((rc = upload(c, &d_pc, pc))) return bail(rc);
+      c->M.tcoef_ng = d_pc;
+    }
   }
 
   // ---- constants -------------------------------------------------------------------------------

@@ -91,6 +91,9 @@ struct DevMesh {
   const double* xcl_ng;
   const double* dxcl_ng;
   const int* curved;
+  // mixed variant on curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c,
+  // [ne][(NGeo+1)^3][3] in that index order
+  const double* tcoef_ng;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
@@ -245,7 +248,7 @@ __device__ __forceinline__ void newton_start(const DevMesh& M, int e, const doub
 }
 
 // Returns isSuccessful (false when the iterate left |xi| <= 1.5).
-static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, const double x[3], double xi[3]) {
+__device__ __forceinline__ bool ref_elem_newton_lin(const DevMesh& M, int e, const double x[3], double xi[3]) {
   const Consts& kc = M.k;
   const double* X = M.xcl + (size_t)e * 24;
   const double* DX = M.dxcl + (size_t)e * 72;
@@ -349,7 +352,7 @@ static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, con
 // monomial form (DevMesh::tcoef): the residual in 18 and the Jacobian in 30 fused multiply-adds instead of
 // the tensor-product sums over 8 corners (about half the FP64 work per iteration), and one reciprocal of
 // det(J) per iteration.  The same map, so it converges to the same xi up to rounding.
-static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
+__device__ __forceinline__ bool ref_elem_newton_fast_lin(const DevMesh& M, int e, const double x[3], double xi[3]) {
   const Consts& kc = M.k;
   const double* Cg = M.tcoef + (size_t)e * 24;
   double c[8][3];
@@ -413,7 +416,7 @@ static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e
   return success;
 }
 
-__device__ __forceinline__ void lagrange_rt(double x, int np, const double* xgp, const double* wb, double* L) {
+static __device__ __noinline__ void lagrange_rt(double x, int np, const double* xgp, const double* wb, double* L) {
   bool hit = false;
   for (int i = 0; i < np; ++i) {
     L[i] = 0.0;
@@ -426,7 +429,7 @@ __device__ __forceinline__ void lagrange_rt(double x, int np, const double* xgp,
 }
 
 // RefElemNewton (eval_xyz.f90:298-445) on the NGeo map of a curved element, in the reference's order
-static __device__ __noinline__ bool ref_elem_newton_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
+__device__ __forceinline__ bool ref_elem_newton_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
   const Consts& kc = M.k;
   const int n1 = kc.ngeo + 1;
   const size_t n3 = (size_t)n1 * n1 * n1;
@@ -510,15 +513,109 @@ __device__ __forceinline__ bool elem_curved(const DevMesh& M, int e) {
   return M.xcl_ng && (!M.curved || __ldg(M.curved + e) != 0);
 }
 
+// One out-of-line Newton per call site (the curved and the trilinear forms inside): the kernels call it from
+// many places, and a second out-of-line callee per site multiplies the compile time
+static __device__ __noinline__ bool ref_elem_newton(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  return elem_curved(M, e) ? ref_elem_newton_ng(M, e, x, xi) : ref_elem_newton_lin(M, e, x, xi);
+}
+
 __device__ __forceinline__ bool position_in_ref_elem(const DevMesh& M, int e, const double x[3], double xi[3]) {
   newton_start(M, e, x, xi);
-  return elem_curved(M, e) ? ref_elem_newton_ng(M, e, x, xi) : ref_elem_newton(M, e, x, xi);
+  return ref_elem_newton(M, e, x, xi);
+}
+
+// Mixed variant, curved element: the Newton of ref_elem_newton_fast on the NGeo map in power form (nested
+// Horner with fused multiply-adds for x(xi) and its Jacobian, no divisions) instead of the barycentric Lagrange
+// sums over the (NGeo+1)^3 CL points; the same start value, stopping rule, Armijo damping and bound, the same map
+template <int NG>
+static __device__ __noinline__ bool ref_elem_newton_fast_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
+  constexpr int n1 = NG + 1;
+  const double* Cg = M.tcoef_ng + (size_t)e * n1 * n1 * n1 * 3;
+  // x(z) - x and, with J, its derivatives (J[nn][dd] = d x_nn / d xi_dd)
+  auto eval = [&](const double z[3], double F[3], double (*J)[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double q = 0.0, q0 = 0.0, q1 = 0.0, q2 = 0.0;   // Horner in xi3 of the value and the three derivatives
+#pragma unroll 1
+      for (int c = NG; c >= 0; --c) {
+        double r = 0.0, r0 = 0.0, r1 = 0.0;           // Horner in xi2
+#pragma unroll 1
+        for (int b = NG; b >= 0; --b) {
+          const double* C = Cg + ((size_t)(c * n1 + b) * n1) * 3 + k;
+          double p = __ldg(C + 3 * NG), dp = 0.0;     // Horner in xi1 with its derivative
+#pragma unroll
+          for (int a = NG - 1; a >= 0; --a) {
+            if (J) dp = fma(dp, z[0], p);
+            p = fma(p, z[0], __ldg(C + 3 * a));
+          }
+          if (J) { r1 = fma(r1, z[1], r); r0 = fma(r0, z[1], dp); }
+          r = fma(r, z[1], p);
+        }
+        if (J) { q2 = fma(q2, z[2], q); q0 = fma(q0, z[2], r0); q1 = fma(q1, z[2], r1); }
+        q = fma(q, z[2], r);
+      }
+      F[k] = q - x[k];
+      if (J) { J[k][0] = q0; J[k][1] = q1; J[k][2] = q2; }
+    }
+  };
+  double F[3];
+  eval(xi, F, nullptr);
+  double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
+  double normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
+  bool success = true;
+  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
+    double J[3][3], Fd[3];
+    eval(xi, Fd, J);
+    const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
+    const double c01 = fma(J[0][2], J[2][1], -J[0][1] * J[2][2]);
+    const double c02 = fma(J[0][1], J[1][2], -J[0][2] * J[1][1]);
+    const double c10 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
+    const double c11 = fma(J[0][0], J[2][2], -J[0][2] * J[2][0]);
+    const double c12 = fma(J[0][2], J[1][0], -J[0][0] * J[1][2]);
+    const double c20 = fma(J[1][0], J[2][1], -J[1][1] * J[2][0]);
+    const double c21 = fma(J[0][1], J[2][0], -J[0][0] * J[2][1]);
+    const double c22 = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
+    const double det = fma(J[0][0], c00, fma(J[0][1], c10, J[0][2] * c20));
+    const double sd = det > 0.0 ? 1.0 / det : det;
+    double dxi[3];
+    dxi[0] = fma(c00, F[0], fma(c01, F[1], c02 * F[2])) * sd;
+    dxi[1] = fma(c10, F[0], fma(c11, F[1], c12 * F[2])) * sd;
+    dxi[2] = fma(c20, F[0], fma(c21, F[1], c22 * F[2])) * sd;
+    deltaXi2 = fma(dxi[0], dxi[0], fma(dxi[1], dxi[1], dxi[2] * dxi[2]));
+    const double xo[3] = {xi[0], xi[1], xi[2]};
+    const double normFold = normF;
+    normF = normF * 2.0;
+    double lambda = 1.0;
+    for (int iArmijo = 1; normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) xi[dd] = fma(-lambda, dxi[dd], xo[dd]);
+      eval(xi, F, nullptr);
+      lambda = 0.2 * lambda;
+      normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
+    }
+    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = false; break; }
+  }
+  return success;
+}
+
+__device__ __forceinline__ bool ref_elem_newton_fast_curved(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  switch (M.k.ngeo) {
+    case 2: return ref_elem_newton_fast_ng<2>(M, e, x, xi);
+    case 3: return ref_elem_newton_fast_ng<3>(M, e, x, xi);
+    default: return ref_elem_newton_fast_ng<4>(M, e, x, xi);
+  }
+}
+
+// the mixed variant's Newton: power forms (fused multiply-adds) of the trilinear or the curved map
+static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  if (elem_curved(M, e)) return M.tcoef_ng ? ref_elem_newton_fast_curved(M, e, x, xi) : ref_elem_newton_ng(M, e, x, xi);
+  return ref_elem_newton_fast_lin(M, e, x, xi);
 }
 
 template <bool FAST>
 __device__ __forceinline__ bool position_in_ref_elem_t(const DevMesh& M, int e, const double x[3], double xi[3]) {
   newton_start(M, e, x, xi);
-  if (elem_curved(M, e)) return ref_elem_newton_ng(M, e, x, xi);
   return FAST ? ref_elem_newton_fast(M, e, x, xi) : ref_elem_newton(M, e, x, xi);
 }
 

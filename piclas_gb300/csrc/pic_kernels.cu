@@ -23,9 +23,9 @@ namespace pic {
 __device__ __forceinline__ bool position_in_ref_elem_f(const DevMesh& M, const MeshF& F, int e, const double x[3],
                                                        const float p[3], float xi[3]) {
   const Consts& kc = M.k;
-  if (elem_curved(M, e)) {        // NGeo > 1: the FP64 Newton on XCL_NGeo
+  if (elem_curved(M, e)) {        // NGeo > 1: the FP64 Newton on the NGeo map (power form)
     double xd[3];
-    const bool suc = position_in_ref_elem(M, e, x, xd);
+    const bool suc = position_in_ref_elem_t<true>(M, e, x, xd);
     xi[0] = (float)xd[0]; xi[1] = (float)xd[1]; xi[2] = (float)xd[2];
     return suc;
   }

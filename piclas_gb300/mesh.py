@@ -192,6 +192,8 @@ class BoxMesh:
     # RefTracking with walls: BuildBCElemDistance output (see build_bc_elem_distance)
     n_loc: np.ndarray = field(default=None)          # per-element degree Nloc (p-adaption); None: N everywhere
     elem_curved: np.ndarray = field(default=None)    # ElemCurved (0/1) of an NGeo > 1 mesh; None at NGeo = 1
+    side_bezier: np.ndarray = field(default=None)    # NGeo > 1: BezierControlPoints3D per (element, local side) [e][s][q][p][3]
+    side_type: np.ndarray = field(default=None)      # NGeo > 1: SideType per (element, local side) (PLANAR_RECT 0 .. CURVED 4)
     dof_offset: np.ndarray = field(default=None)     # N_DG_Mapping(1,:): 0-based DOF offset of each element (nElems+1)
     elem_to_bc_sides: np.ndarray = field(default=None)
     bc_side_elem_loc: np.ndarray = field(default=None)
@@ -281,8 +283,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     bc = tuple(bc)
     if n_geo < 1 or n_geo > 4:
         raise ValueError("n_geo must be 1..4")
-    if n_geo > 1 and (any(b != "periodic" for b in bc) or wall_bulge or wall_shear or periodic_tracing):
-        raise ValueError("curved elements (n_geo > 1) are built for fully periodic boxes with CartesianPeriodic")
+
     if len(bc) != 3 or any(b not in ("periodic", "open", "reflective") for b in bc):
         raise ValueError(f"bc must hold 'periodic', 'open' or 'reflective' per axis, got {bc}")
     periodic = [b == "periodic" for b in bc]
@@ -371,6 +372,18 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                         sv = (np.sin(2.0 * np.pi * (p0[:, 0] - lo[0]) / L[0]) * np.sin(2.0 * np.pi * (p0[:, 1] - lo[1]) / L[1])
                               * np.sin(2.0 * np.pi * (p0[:, 2] - lo[2]) / L[2]))
                         p0 = np.where(inner[:, None], p0 + perturb * hvec[None, :] * sv[:, None], p0)
+                    if wall_bulge != 0.0 or wall_shear != 0.0:
+                        # the wall faces' bump, as for the grid nodes: along the wall normal and within the plane
+                        U = (p0 - lo) / L
+                        p0 = p0.copy()
+                        for d in range(3):
+                            if periodic[d]:
+                                continue
+                            o1, o2 = [q for q in range(3) if q != d]
+                            bump = np.sin(np.pi * U[:, o1]) * np.sin(np.pi * U[:, o2])
+                            for on_face, sign in ((g[:, d] == 0.0, 1.0), (g[:, d] >= dims_f[d], -1.0)):
+                                p0[:, d] = np.where(on_face, p0[:, d] + sign * wall_bulge * hvec[d] * bump, p0[:, d])
+                                p0[:, o1] = np.where(on_face, p0[:, o1] + wall_shear * hvec[o1] * bump, p0[:, o1])
                     xcl[:, c, b, a, :] = p0
         for c in range(2):
             for b in range(2):
@@ -427,6 +440,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         radius = np.sqrt(np.max(np.sum((node_coords - bary[:, None, :]) ** 2, axis=2), axis=1))
         elem_curved = None
         bez = None
+        side_bezier = side_type = None
     else:
         # Bezier control points of the element (Bernstein coefficients of the map: solve V c = X along each axis,
         # V(i,j) = B_j(t_i) on the CL points), the sides' control points bound ElemRadiusNGeo (:1662-1672) and the
@@ -453,6 +467,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                         qa, qb, qc = q & 1, (q >> 1) & 1, q >> 2
                         lin[:, c, b, a, :] += w[0][qa] * w[1][qb] * w[2][qc] * node_coords[:, q, :]
         elem_curved = np.any(np.abs(lin - xcl) > 1e-14, axis=(1, 2, 3, 4)).astype(np.int32)
+        side_bezier, side_type = _curved_side_data(xcl, lin, elem_curved, bary, xi_cl, n_geo)
 
     # ---- Gauss points, Jacobian (trilinear map) -------------------------------------
     def dof_geometry(sel, Nd):
@@ -675,7 +690,7 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
         fibgm_imax=fib_imax, fibgm_deltas=fib_d, fibgm_n_elems=fib_n, fibgm_offset=fib_off,
         fibgm_element=fib_el, canonical_node=canon,
         side_bc=side_bc if side_bc.any() else None, bc=bc, n_loc=n_loc, dof_offset=dof_offset,
-        elem_curved=elem_curved,
+        elem_curved=elem_curved, side_bezier=side_bezier, side_type=side_type,
     )
     if (side_bc.any() and not any(periodic)) or (periodic_tracing and any(periodic)):
         halo = float(hvec.max()) if bc_halo_eps is None else float(bc_halo_eps)
@@ -702,6 +717,96 @@ def p_adaption_degrees(nx: int, ny: int, nz: int, kind: str, nmin: int, nmax: in
     raise ValueError("kind must be 'random' or 'half-half'")
 
 
+# CGNS_SideToVol2 of a master side at geometry degree n: point (p,q) of local side s -> volume index (a,b,c)
+_SIDE_VOL = {
+    0: lambda p, q, n: (q, p, 0),          # ZETA_MINUS
+    1: lambda p, q, n: (p, 0, q),          # ETA_MINUS
+    2: lambda p, q, n: (n, p, q),          # XI_PLUS
+    3: lambda p, q, n: (n - p, n, q),      # ETA_PLUS
+    4: lambda p, q, n: (0, q, p),          # XI_MINUS
+    5: lambda p, q, n: (p, q, n),          # ZETA_PLUS
+}
+
+
+def _slab_bounding_box_empty(P) -> bool:
+    """BoundingBoxIsEmpty of GetSideSlabNormalsAndIntervals (particle_surfaces.f90:619-816) for the control
+    points P[q][p][3] of one side."""
+    n = P.shape[0] - 1
+
+    def crossnorm(a, b):
+        c = np.cross(a, b)
+        return c / math.sqrt(float(c @ c))
+    s1 = ((P[0, n] - P[0, 0]) + P[n, n]) - P[n, 0]
+    s1 = s1 / math.sqrt(float(s1 @ s1))
+    s2 = crossnorm(s1, ((P[n, 0] - P[0, 0]) + P[n, n]) - P[0, n])
+    s3 = crossnorm(s2, s1)
+    iv = np.zeros(6)
+    for q in range(n + 1):
+        for p in range(n + 1):
+            if p == 0 and q == 0:
+                continue
+            d = P[q, p] - P[0, 0]
+            for i, sn in enumerate((s1, s2, s3)):
+                sk = (d[0] * sn[0] + d[1] * sn[1]) + d[2] * sn[2]
+                if sk < 0.0:
+                    iv[2 * i] = min(iv[2 * i], sk)
+                elif sk > 0.0:
+                    iv[2 * i + 1] = max(iv[2 * i + 1], sk)
+    dx, dy, dz = abs(iv[1] - iv[0]), abs(iv[3] - iv[2]), abs(iv[5] - iv[4])
+    h, w, l = dy, min(dx, dz), max(dx, dz)
+    if h / max(h, l, w) < 1.0e-6:
+        h = 0.0
+    return abs(h / math.sqrt(l * l + w * w + h * h)) <= 2.220446049250313e-16
+
+
+def _curved_side_data(xcl, lin, elem_curved, bary, xi_cl, n):
+    """BezierControlPoints3D and SideType of every (element, local side) of an NGeo mesh, each side in its
+    element's own (master) orientation: the Bernstein coefficients of the side's CL interpolant (sVdm_Bezier of
+    BuildBezierVdm, basis.f90:275-358), and IdentifyElemAndSideType (particle_mesh_tools.f90:953-1233): an
+    element that is not curved has planar (BoundingBoxIsEmpty: PLANAR_RECT if the edges meet at right angles,
+    else PLANAR_NONRECT) or BILINEAR sides; a curved element's side whose CL points differ from the trilinear
+    interpolation of the corners (PointsEqual, 1e-14) is PLANAR_CURVED (empty box) or CURVED, its other sides
+    as for an element that is not curved."""
+    ne = xcl.shape[0]
+    n1 = n + 1
+    xc = np.asarray(xi_cl)
+    V = np.array([[math.comb(n, j) / 2.0 ** n * (1.0 + xc[i]) ** j * (1.0 - xc[i]) ** (n - j) for j in range(n1)]
+                  for i in range(n1)])
+    sV = np.linalg.inv(V)
+    bez = np.zeros((ne, 6, n1, n1, 3))
+    stype = np.zeros((ne, 6), dtype=np.int32)
+    eps = 2.220446049250313e-16
+
+    def unit(v):
+        ln = math.sqrt(float(v @ v))
+        return v / ln if ln > 0.0 else v * 0.0
+    for s in range(6):
+        idx = [[_SIDE_VOL[s](p, q, n) for p in range(n1)] for q in range(n1)]
+        Xs = np.stack([np.stack([xcl[:, c, b, a] for (a, b, c) in row], axis=1) for row in idx], axis=1)  # [e][q][p][3]
+        Ls = np.stack([np.stack([lin[:, c, b, a] for (a, b, c) in row], axis=1) for row in idx], axis=1)
+        B = np.einsum("pi,eqid->eqpd", sV, Xs)
+        B = np.einsum("qj,ejpd->eqpd", sV, B)
+        bez[:, s] = B
+        curved_side = np.any(np.abs(Ls - Xs) > 1e-14, axis=(1, 2, 3))
+        for e in range(ne):
+            P = B[e]
+            empty = _slab_bounding_box_empty(P)
+            if elem_curved[e] and curved_side[e]:
+                stype[e, s] = 3 if empty else 4
+            elif empty:
+                v1 = unit(P[n, 0] - P[0, 0])
+                v2 = unit(P[0, n] - P[0, 0])
+                v3 = unit(P[n, n] - P[n, 0])
+                rect = abs(float(v1 @ v2)) <= eps and abs(float(v1 @ v3)) <= eps
+                if rect:
+                    v1 = unit(P[n, n] - P[0, n])
+                    rect = abs(float(v1 @ v2)) <= eps and abs(float(v1 @ v3)) <= eps
+                stype[e, s] = 0 if rect else 1
+            else:
+                stype[e, s] = 2
+    return np.ascontiguousarray(bez), stype
+
+
 # CGNS_SideToVol2 at NGeo = 1 for a master side: corner (p,q) of local side s -> tensor corner (a,b,c)
 _SIDE_CORNER = {
     0: lambda p, q: (q, p, 0),        # ZETA_MINUS: (p,q) = (j,i)
@@ -714,8 +819,10 @@ _SIDE_CORNER = {
 
 
 def side_control_points(mesh: BoxMesh, e: int, s: int) -> np.ndarray:
-    """BezierControlPoints3D(1:3,0:1,0:1) of local side s of element e (0-based), as [q][p][3]
+    """BezierControlPoints3D(1:3,0:NGeo,0:NGeo) of local side s of element e (0-based), as [q][p][3]
     (particle_mesh_tools.f90:1748-1773 at NGeo = 1, where the Bezier and CL corner points coincide)."""
+    if mesh.side_bezier is not None:
+        return mesh.side_bezier[e, s]
     out = np.zeros((2, 2, 3))
     for q in range(2):
         for p in range(2):
@@ -864,11 +971,18 @@ def build_bc_elem_distance(mesh: BoxMesh, bc_halo_eps: float, include_periodic: 
     radius = np.zeros(nbc)
     for k in range(nbc):
         P = side_control_points(mesh, int(we_arr[k]), int(ws_arr[k]))
-        o = (((0.5 * P[0, 0]) * 0.5 + (0.5 * P[1, 0]) * 0.5) + (0.5 * P[0, 1]) * 0.5) + (0.5 * P[1, 1]) * 0.5
+        n = P.shape[0] - 1
+        R = P.copy()                                      # DeCasteljauInterpolation at xi = (0,0) (basis.f90:429-476)
+        for l in range(n - 1, -1, -1):
+            for q in range(l + 1):
+                for p in range(l + 1):
+                    R[q, p] = (((0.5 * R[q, p]) * 0.5 + (0.5 * R[q + 1, p]) * 0.5) + (0.5 * R[q, p + 1]) * 0.5) \
+                        + (0.5 * R[q + 1, p + 1]) * 0.5
+        o = R[0, 0]
         origin[k] = o
         rmax = 0.0
-        for q in range(2):
-            for p in range(2):
+        for q in range(n + 1):
+            for p in range(n + 1):
                 v = P[q, p] - o
                 rmax = max(rmax, float(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]))
         radius[k] = math.sqrt(rmax)

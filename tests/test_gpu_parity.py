@@ -1349,3 +1349,20 @@ def test_curved_ngeo_uncurved_elements_use_corner_newton(gpu_lib, oracle_lib):
         res.append(g)
     assert np.array_equal(res[0]["elem"], res[1]["elem"])
     assert _rel(res[0]["part_state"], res[1]["part_state"]) <= 1e-12
+
+
+@pytest.mark.parametrize("ng", [2, 3])
+def test_mixed_curved_newton_against_fp64(gpu_lib, oracle_lib, ng):
+    """Mixed RefTracking on curved elements maps x -> xi with the NGeo map in power form (nested Horner, fused
+    multiply-adds): over 30 steps the element ids equal the FP64 run's, and PartPosRef equals, within 1e-10, the
+    reference Newton (oracle, Lagrange form) at the mixed run's own positions."""
+    mesh = build_box_mesh(8, 8, 8, 3, perturb=0.08, n_geo=ng)
+    w = workloads.curved_two_species(mesh=mesh, n_per_species=20_000, seed=82, nsteps=30, Te_eV=1000.0)
+    w.dt *= 5.0
+    g64 = _run_gpu(w, 30)
+    g32 = _run_gpu(w, 30, precision=capi.PIC_PREC_MIXED)
+    assert (g32["elem"] != g64["elem"]).sum() <= 2
+    assert g32["status"]["error_word"] == 0 and (g64["elem"] != w.elem).sum() > 100
+    st = oracle_lib.OracleState(g32["part_state"], g32["elem"], w.part_species)
+    oracle_lib.map_particles(w.config(), capi.MeshStruct(w.mesh), st)
+    assert np.max(np.abs(g32["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
