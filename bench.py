@@ -267,7 +267,8 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------------------------
-def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0, nthreads: int | None = None):
+def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0, nthreads: int | None = None,
+                      mesh_kw: dict | None = None):
     """Time the reference algorithm (oracle, OpenMP) on a bounded sample of the workload: the full mesh
     with as many particles as fit ~target_s seconds per step (at most the full particle count).  The
     per-step cost is a fixed part (zeroing PartSource, per-thread accumulators and their reduction) plus
@@ -277,7 +278,7 @@ def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0
     oracle.build()
     oracle.set_timing_build(True)     # -O3 with FMA contraction, as the reference's release build
     nthreads = nthreads or max(1, os.cpu_count() or 1)
-    w = make_workload(name, seed=0, n_override=20000)
+    w = make_workload(name, seed=0, n_override=20000, **(mesh_kw or {}))
     ms = capi.MeshStruct(w.mesh)
     cfg = w.config()
     n_full = 16_000_000 if name == "curved" else 200_000
@@ -319,15 +320,22 @@ def cpu_reference_run(name: str, steps: int, warmup: int, target_s: float = 15.0
                       f"{per * 1e6:.2f} us/particle)"}
 
 
-def cpu_baselines(name: str, target_s: float):
+def cpu_baselines(name: str, target_s: float, mesh_kw: dict | None = None):
     """All host cores (the reported baseline) and one core (the reference itself runs one rank per core)."""
-    allc = cpu_reference_run(name, steps=1, warmup=0, target_s=target_s)
+    allc = cpu_reference_run(name, steps=1, warmup=0, target_s=target_s, mesh_kw=mesh_kw)
     try:
-        one = cpu_reference_run(name, steps=1, warmup=0, target_s=target_s * 0.6, nthreads=1)
+        one = cpu_reference_run(name, steps=1, warmup=0, target_s=target_s * 0.6, nthreads=1, mesh_kw=mesh_kw)
         allc["one_core"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
     except Exception as ex:
         allc["one_core"] = {"error": repr(ex)}
     return allc
+
+
+def mesh_kwargs(args):
+    """The mesh variant flags of a curved-workload run (periodic BC tracing, NGeo, p-adaption)."""
+    if args.workload != "curved":
+        return {}
+    return {"periodic_tracing": args.periodic_tracing, "n_geo": args.ngeo, "p_adaption": args.p_adaption}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -478,7 +486,7 @@ def run_gpu(args, rank, world, local_rank):
             out["extras"] = {"error": repr(ex)}
     if rank == 0 and not args.no_cpu:
         try:
-            out["cpu_baseline"] = cpu_baselines(args.workload, args.cpu_seconds)
+            out["cpu_baseline"] = cpu_baselines(args.workload, args.cpu_seconds, mesh_kwargs(args))
         except Exception as ex:
             out["cpu_baseline"] = {"error": repr(ex)}
     if dist:
@@ -826,8 +834,12 @@ def reference_config(args):
     """The config of this arm's line for the same flags (the reference computes in FP64 whatever the
     precision flag says)."""
     from types import SimpleNamespace as NS
+    from piclas_gb300.mesh import p_adaption_degrees
     cells, n = {"curved": (32, 16_000_000), "plasma_wave": (8, 200_000)}.get(args.workload, (8, 200_000))
-    stand_in = NS(mesh=NS(n_elems=cells ** 3, N=3), n=n)
+    n_loc = p_adaption_degrees(cells, cells, cells, args.p_adaption, 1, 3, seed=0) if args.p_adaption else None
+    n_dofs = cells ** 3 * 64 if n_loc is None else int(((np.asarray(n_loc) + 1) ** 3).sum())
+    stand_in = NS(mesh=NS(n_elems=cells ** 3, N=3, n_geo=args.ngeo, n_loc=n_loc, n_dofs=n_dofs), n=n,
+                  periodic_tracing=args.periodic_tracing)
     return dict(workload_config(stand_in, args.workload if args.workload == "curved" else "plasma_wave"),
                 precision=args.precision, parallelism=f"replicas x{args.gpus}")
 
@@ -838,7 +850,8 @@ def run_reference(args, rank):
     nsteps = max(args.steps, 1)
     # each step a bounded sample; the whole run (probes, warm-up, steps) stays within about three minutes
     per_step = min(args.cpu_seconds, 150.0 / (nsteps + (1 if args.warmup > 0 else 0)))
-    base = cpu_reference_run(args.workload, steps=nsteps, warmup=args.warmup, target_s=per_step)
+    base = cpu_reference_run(args.workload, steps=nsteps, warmup=args.warmup, target_s=per_step,
+                             mesh_kw=mesh_kwargs(args))
     out = {"metric": METRIC, "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded), frozen field",

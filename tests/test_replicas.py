@@ -59,12 +59,20 @@ def test_reference_arm_reports_the_gpu_arms_config():
     import bench
     from piclas_gb300 import workloads
     from piclas_gb300.mesh import build_box_mesh
-    for name, cells, n in (("curved", 32, 16_000_000), ("plasma_wave", 8, 200_000)):
-        args = argparse.Namespace(workload=name, precision="fp64", gpus=1)
+    from piclas_gb300.mesh import p_adaption_degrees
+    cases = (("curved", 32, 16_000_000, 1, None, False), ("plasma_wave", 8, 200_000, 1, None, False),
+             ("curved", 32, 16_000_000, 2, None, True), ("curved", 32, 16_000_000, 1, "random", False))
+    for name, cells, n, ngeo, padapt, ptrace in cases:
+        args = argparse.Namespace(workload=name, precision="fp64", gpus=1, ngeo=ngeo, p_adaption=padapt,
+                                  periodic_tracing=ptrace)
         ref = bench.reference_config(args)
         mesh = build_box_mesh(2, 2, 2, 3)
         stand_in = workloads.Workload(**{**workloads.plasma_wave(mesh=mesh, n_particles=10).__dict__})
-        stand_in.mesh = type("M", (), {"n_elems": cells ** 3, "N": 3})()
+        n_loc = p_adaption_degrees(cells, cells, cells, padapt, 1, 3, seed=0) if padapt else None
+        n_dofs = cells ** 3 * 64 if n_loc is None else int(((n_loc + 1) ** 3).sum())
+        stand_in.mesh = type("M", (), {"n_elems": cells ** 3, "N": 3, "n_geo": ngeo, "n_loc": n_loc,
+                                       "n_dofs": n_dofs})()
         stand_in.part_state = type("P", (), {"shape": (n, 6)})()
+        stand_in.periodic_tracing = ptrace
         gpu = dict(bench.workload_config(stand_in, name), precision="fp64", parallelism="replicas x1")
         assert ref == gpu
