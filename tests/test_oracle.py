@@ -960,3 +960,163 @@ def test_curved_newton_and_loop(oracle_lib, ng):
     total = sum(w.species[s - 1][0] * w.species[s - 1][2] for s in w.part_species)
     scale = sum(abs(w.species[s - 1][0] * w.species[s - 1][2]) for s in w.part_species)
     assert abs(oracle_lib.integrate_charge(ms, mesh.N, PS) - total) <= 1e-12 * scale
+
+
+# ---- curved wall sides (Bezier clipping) --------------------------------------------------------------------
+def _face_point(mesh, e, s, u, v):
+    """Point and tangents of the wall face of element e (0-based) at the face parameters (u, v): the element's
+    NGeo map with the face's reference coordinate fixed (s: 'ylo' -> xi_2 = -1, u = xi_1, v = xi_3)."""
+    assert s == "ylo"
+    x = elem_map(mesh, e, (u, -1.0, v))
+    d = 1e-5                                            # central differences: exact for the quadratic map
+    tu = (elem_map(mesh, e, (u + d, -1.0, v)) - elem_map(mesh, e, (u - d, -1.0, v))) / (2 * d)
+    tv = (elem_map(mesh, e, (u, -1.0, v + d)) - elem_map(mesh, e, (u, -1.0, v - d))) / (2 * d)
+    return x, tu, tv
+
+
+def _line_face_hit(mesh, e, x0, dx):
+    """(alpha, hit point, unit normal) of the segment x0 + alpha*dx (alpha in [0, 1]) and the lower y wall face of
+    element e, by Newton's method on x(u, v) - x0 - alpha*dx = 0 (independent of the library's Bezier clipping)."""
+    q = np.array([0.0, 0.0, 0.5])
+    for _ in range(50):
+        x, tu, tv = _face_point(mesh, e, "ylo", q[0], q[1])
+        r = x - x0 - q[2] * dx
+        J = np.stack([tu, tv, -dx], axis=1)
+        q = q - np.linalg.solve(J, r)
+        if np.max(np.abs(r)) < 1e-15:
+            break
+    x, tu, tv = _face_point(mesh, e, "ylo", q[0], q[1])
+    n = np.cross(tu, tv)
+    return q, x, n / np.linalg.norm(n)
+
+
+@pytest.mark.parametrize("n_geo", [2, 3])
+def test_curved_wall_reflection_against_an_independent_solve(oracle_lib, n_geo):
+    """Bulged (SideType CURVED) reflective walls: a particle that reaches the lower y wall within one step ends at
+    the mirror image of its path in the wall's tangent plane at the hit point, with the velocity reflected there;
+    hit point and normal from a plain Newton solve on the face of the element map (the Bezier clipping stops at
+    ClipTol = 1e-8 in the face parameters: positions agree to 1e-8 h)."""
+    mesh = build_box_mesh(4, 4, 4, 2, bc=("reflective", "reflective", "reflective"), wall_bulge=0.2, n_geo=n_geo)
+    assert (mesh.side_type[mesh.side_nb_elem == 0] == 4).all()
+    rng = np.random.default_rng(7)
+    n = 40
+    h = 0.25
+    xz = rng.uniform(0.15, 0.85, size=(n, 2))
+    p0 = np.column_stack([xz[:, 0], np.full(n, 0.06), xz[:, 1]])
+    vel = np.column_stack([rng.uniform(-0.3, 0.3, n), -np.ones(n), rng.uniform(-0.3, 0.3, n)]) * 1.0e6
+    dt = 0.035 / 1.0e6
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, seed=3, dt=dt)
+    w.e_dof[:] = 0.0
+    w.part_state[:, :3], w.part_state[:, 3:] = p0, vel
+    ix, iz = np.floor(p0[:, 0] / h).astype(int), np.floor(p0[:, 2] / h).astype(int)
+    w.elem = (ix + 4 * (0 + 4 * iz) + 1).astype(np.int32)
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    cfg, ms = w.config(), capi.MeshStruct(mesh)
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species, is_new=np.zeros(n, np.uint8))
+    oracle_lib.map_particles(cfg, ms, st)
+    assert np.abs(st.part_pos_ref).max() <= 1.0
+    oracle_lib.step(cfg, ms, w.e_dof, st, dt, 1)
+    assert st.inside.all() and st.counters.n_lost == 0
+    checked = 0
+    for i in range(n):
+        dx = vel[i] * dt
+        q, xh, nrm = _line_face_hit(mesh, w.elem[i] - 1, p0[i], dx)
+        if not (-1.0 < q[0] < 1.0 and -1.0 < q[1] < 1.0 and 0.0 < q[2] < 1.0):
+            continue                        # leaves the element's face patch first (hits a neighbour's face)
+        v2 = vel[i] - 2.0 * np.dot(vel[i], nrm) * nrm
+        x2 = xh + v2 * dt * (1.0 - q[2])
+        assert np.max(np.abs(st.part_state[i, :3] - x2)) < 1e-8 * h, i
+        assert np.max(np.abs(st.part_state[i, 3:] - v2)) < 1e-7 * np.linalg.norm(vel[i]), i
+        checked += 1
+    assert checked >= 25
+
+
+def test_planar_curved_walls_fold_straight_paths(oracle_lib):
+    """Sheared wall faces of an NGeo = 2 box stay in the box planes (SideType PLANAR_CURVED, in-plane CL points
+    moved): reflective walls fold every straight path exactly as plane walls do, open walls remove the particles
+    whose unfolded y path leaves (0, 1).  The hit points come from BezierNewton on the projected patch (stopped at
+    a squared update below BezierNewtonTolerance2): the folded positions agree to 1e-9."""
+    mesh = build_box_mesh(4, 4, 4, 2, bc=("reflective", "open", "reflective"), wall_shear=0.3, n_geo=2)
+    assert (mesh.side_type[mesh.side_nb_elem == 0] == 3).all()
+    w = workloads.plasma_wave(mesh=mesh, n_particles=3000, T_eV=2000.0, seed=15, dt=2e-10)
+    w.e_dof[:] = 0.0
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(15))
+    w.part_state[:, :3] = x
+    w.elem = e
+    K = 20
+    ref = _ref_wall_steps(oracle_lib, w, K)
+    assert ref.counters.n_ref_tolerance == 0 and ref.counters.n_lost == 0
+    xs = w.part_state[:, :3] + w.part_state[:, 3:] * (w.dt * K)
+
+    def fold(u):
+        u = np.mod(u, 2.0)
+        return np.where(u > 1.0, 2.0 - u, u)
+
+    y = xs[:, 1]
+    clear = (np.abs(y) > 1e-9) & (np.abs(y - 1.0) > 1e-9)
+    expect = (y > 0.0) & (y < 1.0)
+    assert np.array_equal(ref.inside[clear].astype(bool), expect[clear]) and (~expect).sum() > 100
+    k = ref.inside.astype(bool)
+    assert np.max(np.abs(ref.part_state[k, 0] - fold(xs[k, 0]))) < 1e-9
+    assert np.max(np.abs(ref.part_state[k, 2] - fold(xs[k, 2]))) < 1e-9
+    assert np.max(np.abs(ref.part_state[k, 1] - y[k])) < 1e-12
+    assert np.max(np.abs(ref.part_pos_ref[k])) <= 1.0 + 1e-9
+
+
+def test_curved_open_walls_remove_exactly_the_crossing_particles(oracle_lib):
+    """Bulged open walls in y: particles moving along y (away from the x and z walls) are removed iff their end
+    point lies beyond the wall surface at their (x, z); the survivors move on their straight paths, stay mapped
+    within [-1, 1]^3 and their element map reproduces their position."""
+    mesh = build_box_mesh(4, 4, 4, 2, perturb=0.05, bc=("reflective", "open", "reflective"), wall_bulge=0.2, n_geo=2)
+    rng = np.random.default_rng(16)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=2000, T_eV=2000.0, seed=16, dt=2e-10)
+    w.e_dof[:] = 0.0
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, rng)
+    keep = np.all((x[:, [0, 2]] > 0.1) & (x[:, [0, 2]] < 0.9), axis=1)
+    x, e = x[keep], e[keep]
+    n = len(x)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=2000.0, seed=16, dt=2e-10)
+    w.e_dof[:] = 0.0
+    w.part_state[:, :3] = x
+    w.part_state[:, 3] = 0.0
+    w.part_state[:, 5] = 0.0
+    w.part_state[:, 4] = rng.choice([-1.0, 1.0], n) * rng.uniform(0.2, 0.6, n) / (w.dt * 10)
+    w.elem = e
+    ref = _ref_wall_steps(oracle_lib, w, 10)
+    assert ref.counters.n_lost == 0 and ref.counters.n_ref_tolerance == 0
+    yend = x[:, 1] + w.part_state[:, 4] * w.dt * 10
+    h = 0.25
+
+    def wall_y(px, pz, top):
+        # the wall face above/below (px, pz): solve x(u, +-1, v)[x, z] = (px, pz) on the wall element by Newton's
+        # method (all particles at once, central differences: exact for the quadratic map), then take its y
+        ix, iz = np.minimum((px / h).astype(int), 3), np.minimum((pz / h).astype(int), 3)
+        eidx = ix + 4 * ((3 if top else 0) + 4 * iz)
+        s2 = 1.0 if top else -1.0
+
+        def xmap(q):
+            return workloads._curved_map(mesh, eidx, np.column_stack([q[:, 0], np.full(len(q), s2), q[:, 1]]))[0]
+        q = np.zeros((len(px), 2))
+        d = 1e-5
+        for _ in range(30):
+            r = xmap(q)[:, [0, 2]] - np.column_stack([px, pz])
+            J = np.empty((len(px), 2, 2))
+            for a in range(2):
+                dq = np.zeros(2)
+                dq[a] = d
+                J[:, :, a] = (xmap(q + dq) - xmap(q - dq))[:, [0, 2]] / (2 * d)
+            q = q - np.linalg.solve(J, r[..., None])[..., 0]
+        return xmap(q)[:, 1]
+
+    ylo = wall_y(x[:, 0], x[:, 2], False)
+    yhi = wall_y(x[:, 0], x[:, 2], True)
+    expect = (yend > ylo) & (yend < yhi)
+    clear = (np.abs(yend - ylo) > 1e-7) & (np.abs(yend - yhi) > 1e-7)
+    got = ref.inside.astype(bool)
+    assert np.array_equal(got[clear], expect[clear]) and (~expect).sum() > 50 and expect.sum() > 50
+    k = got
+    assert np.max(np.abs(ref.part_state[k, :3] - np.column_stack([x[:, 0], yend, x[:, 2]])[k])) < 1e-12
+    assert np.max(np.abs(ref.part_pos_ref[k])) <= 1.0 + 1e-9
+    for i in np.nonzero(k)[0][:50]:
+        # PartPosRef from RefElemNewton, stopped by its tolerance (RefMappingEps = 1e-4 on the update)
+        assert np.allclose(elem_map(mesh, ref.elem[i] - 1, ref.part_pos_ref[i]), ref.part_state[i, :3], atol=1e-4 * h)
