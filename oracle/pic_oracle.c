@@ -897,7 +897,7 @@ static double planar_rect_alpha(const orc_bc_side_t* g, const double xl[3], cons
   return alpha;
 }
 
-#define ORC_BC_CAP 32   /* wall sides within reach of one trajectory; more are not traced (same cap on the GPU) */
+#define ORC_BC_CAP 64   /* wall sides within reach of one trajectory; more are not traced (same cap on the GPU) */
 
 /* ParticleBCTracking, particle_reftracking.f90:417-694: trace the trajectory against the BC sides of the
  * element's list (sorted by SideBCMetrics distance, stopping beyond the trajectory length) -- open and

@@ -17,8 +17,10 @@
  * The recursion of BezierClipRecursive <-> CheckXiClip/CheckEtaClip is restated as a loop with an explicit
  * stack: at a split the first half is clipped next, and the second half is pushed together with the state the
  * reference saves around the first recursive call (clip counters, line vectors, ClipMode); when a branch
- * returns, the next pending half continues with that state -- the reference's visiting order.  Floating-point
- * order follows the Fortran (built with -ffp-contract=off).
+ * returns, the next pending half continues with that state -- the reference's visiting order.  The stack holds
+ * 8 nested splits (as the GPU library's); deeper nesting raises the error flag, as more than
+ * BezierClipMaxIntersec hits and a degenerated patch do, where the reference aborts.  Floating-point order
+ * follows the Fortran (built with -ffp-contract=off).
  */
 #include "pic_oracle_bezier.h"
 
@@ -379,7 +381,7 @@ typedef struct {
   double a0, a1;                  /* the interval the pending half clips to (XiArray/EtaArray at nClip) */
   int clipMode, iClipIter, nXi, nEta, eta;
 } bz_pending_t;
-#define BZ_STACK 32
+#define BZ_STACK 8   /* nested splits held (the library holds the same number) */
 
 /* CheckXiClip (dir 0, particle_intersection.f90:2459-2851) / CheckEtaClip (dir 1, :2853-3243) on the patch cp.
  * Returns 1 at a split: the first half is in cp, the second half in *pend (to be clipped after the first). */

@@ -158,10 +158,10 @@ int validate(const pic_config_t* cfg, const pic_mesh_t* m) {
   }
   if (m->n_elems < 1) return fail(PIC_ERR_INVALID_ARGUMENT, "n_elems must be positive");
   if (m->n_geo < 1 || m->n_geo > 4) return fail(PIC_ERR_INVALID_ARGUMENT, "NGeo must be 1..4");
-  if (m->n_geo > 1 && (m->side_bc || cfg->periodic_tracing))
-    return fail(PIC_ERR_INVALID_ARGUMENT, "curved elements (NGeo > 1) need a mesh without open/reflective sides and "
-                                          "CartesianPeriodic (periodic_tracing = 0): curved side intersections are "
-                                          "not built");
+  if (m->n_geo > 1 && cfg->tracking == PIC_TRACK_REFMAPPING && (m->side_bc || cfg->periodic_tracing) &&
+      (!m->side_bezier || !m->side_type))
+    return fail(PIC_ERR_INVALID_ARGUMENT, "RefTracking with BC sides on curved elements (NGeo > 1) needs side_bezier "
+                                          "and side_type");
   if (m->n_periodic_vectors < 0 || m->n_periodic_vectors > 3) return fail(PIC_ERR_INVALID_ARGUMENT, "n_periodic_vectors");
   const void* req[] = {m->xi_cl_ngeo, m->wbary_cl_ngeo, m->xgp, m->wgp, m->wbary_gp, m->xcl_ngeo, m->dxcl_ngeo,
                        m->elem_bary, m->xez_basis, m->slen_basis, m->elem_radius, m->elem_xgp, m->node_coords,
@@ -527,8 +527,11 @@ const char* pic_last_error(void) { return g_last_error.c_str(); }
 // corners in the side's BezierControlPoints3D order (CGNS side order, particle_mesh_tools.f90:1748-1773),
 // planar when they lie within 1e-6 of the side's extent of the
 // averaged plane (then SideNormVec oriented away from the element, SideDistance, PLANAR_RECT or
-// PLANAR_NONRECT), else BILINEAR with the non-oriented averaged normal.  Fills kBcGeo doubles.
-static void wall_side_geometry(const double* xcl, const double* bary, int e, int s, double* g) {
+// PLANAR_NONRECT), else BILINEAR with the non-oriented averaged normal.  Fills kBcGeo doubles.  On curved
+// meshes the side's type is given (the mesh's SideType, GetSideType for NGeo > 1): BILINEAR and CURVED sides
+// keep the non-oriented averaged normal, planar ones (PLANAR_RECT, _NONRECT, _CURVED) get SideNormVec and
+// SideDistance from their corners as above (IdentifyElemAndSideType, particle_mesh_tools.f90:991-1012).
+static void wall_side_geometry(const double* xcl, const double* bary, int e, int s, double* g, int given) {
   auto corner = [&](int p, int q, double out[3]) {
     int a, b, cc;
     switch (s) {
@@ -566,10 +569,10 @@ static void wall_side_geometry(const double* xcl, const double* bary, int e, int
   const double l1 = 0.5 * std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
   const double l2 = 0.5 * std::sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
   const double h = hmax - hmin, dmax = std::max(h, std::max(l1, l2));
-  if (!(h < 1.0e-6 * dmax)) {
+  if (given == 2 || given == 4 || (given < 0 && !(h < 1.0e-6 * dmax))) {
     for (int c = 0; c < 3; ++c) g[9 + c] = n[c];
     g[12] = 0.0;
-    g[15] = 2.0;                                   // BILINEAR
+    g[15] = given == 4 ? 4.0 : 2.0;                // CURVED / BILINEAR
     return;
   }
   const double* b = bary + (size_t)e * 3;
@@ -588,7 +591,76 @@ static void wall_side_geometry(const double* xcl, const double* bary, int e, int
   unit(P01, P00, u1); unit(P10, P00, u2); unit(P11, P01, u3); unit(P11, P10, u4);
   auto dz = [](const double a[3], const double bb[3]) { return std::fabs(a[0] * bb[0] + a[1] * bb[1] + a[2] * bb[2]) <= 2.22e-16; };
   const bool rect = dz(u1, u2) && dz(u1, u3) && dz(u4, u2) && dz(u4, u3);
-  g[15] = rect ? 0.0 : 1.0;                        // PLANAR_RECT / PLANAR_NONRECT
+  g[15] = given >= 0 ? (double)given : (rect ? 0.0 : 1.0);   // PLANAR_RECT / PLANAR_NONRECT (/ PLANAR_CURVED)
+}
+
+// FacNchooseK, Xi_NGeo and D_Bezier of NGeo (BuildBezierVdm, basis.f90:275-358; particle_mesh_tools.f90:
+// 1470-1473; BuildBezierDMat, basis.f90:361-402)
+static void bezier_basis(int ng, pic::BzBasis& B) {
+  std::memset(&B, 0, sizeof(B));
+  B.ng = ng;
+  auto ipow = [](double x, int n) { double r = 1.0; for (int i = 0; i < n; ++i) r = r * x; return r; };
+  for (int i = 0; i <= ng; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double c = 1.0;
+      for (int q = 0; q < j; ++q) c = c * (double)(i - q) / (double)(q + 1);
+      B.fnk[i][j] = (1.0 / ipow(2.0, i)) * c;
+    }
+  for (int i = 0; i <= ng; ++i) B.xi[i] = 2.0 / (double)ng * (double)i - 1.0;
+  for (int i = 0; i <= ng; ++i) B.dbez[i][0] = -B.fnk[ng][0] * (double)ng * ipow(1 - B.xi[i], ng - 1);
+  for (int i = 0; i <= ng; ++i) B.dbez[i][ng] = B.fnk[ng][ng] * (double)ng * ipow(B.xi[i] + 1, ng - 1);
+  for (int j = 1; j <= ng - 1; ++j)
+    for (int i = 0; i <= ng; ++i) {
+      const double XiPlus = B.xi[i] + 1.0, XiMinus = 1.0 - B.xi[i];
+      B.dbez[i][j] = B.fnk[ng][j] * ((double)j * ipow(XiPlus, j - 1) * ipow(XiMinus, ng - j) -
+                                     (double)(ng - j) * ipow(XiPlus, j) * ipow(XiMinus, ng - j - 1));
+    }
+}
+
+// GetSideSlabNormalsAndIntervals (particle_surfaces.f90:619-816, BezierElevation = 0) of a side's Bezier
+// points bcp[(q (NGeo+1) + p) 3 + c]: fills kBzGeo doubles (points, slab normals and intervals,
+// BoundingBoxIsEmpty).  Returns false where the reference aborts (a degenerated side).
+static bool bezier_side_slab(int ng, const double* bcp, double* S) {
+  const int n1 = ng + 1;
+  for (int k = 0; k < n1 * n1 * 3; ++k) S[k] = bcp[k];
+  auto CP = [&](int p, int q, int c) { return bcp[(q * n1 + p) * 3 + c]; };
+  auto crossnorm = [](const double a[3], const double b[3], double n[3]) {
+    n[0] = a[1] * b[2] - a[2] * b[1];
+    n[1] = a[2] * b[0] - a[0] * b[2];
+    n[2] = a[0] * b[1] - a[1] * b[0];
+    const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] = n[0] / l; n[1] = n[1] / l; n[2] = n[2] / l;
+  };
+  double n1v[3], n2v[3], n3v[3], t[3];
+  for (int c = 0; c < 3; ++c) n1v[c] = ((CP(ng, 0, c) - CP(0, 0, c)) + CP(ng, ng, c)) - CP(0, ng, c);
+  if (n1v[0] == 0.0 && n1v[1] == 0.0 && n1v[2] == 0.0) return false;
+  const double l = std::sqrt(n1v[0] * n1v[0] + n1v[1] * n1v[1] + n1v[2] * n1v[2]);
+  for (int c = 0; c < 3; ++c) n1v[c] = n1v[c] / l;
+  for (int c = 0; c < 3; ++c) t[c] = ((CP(0, ng, c) - CP(0, 0, c)) + CP(ng, ng, c)) - CP(ng, 0, c);
+  crossnorm(n1v, t, n2v);
+  crossnorm(n2v, n1v, n3v);
+  double* sn = S + pic::kBzSlabN;
+  double* si = S + pic::kBzSlabI;
+  for (int c = 0; c < 3; ++c) { sn[c] = n1v[c]; sn[3 + c] = n2v[c]; sn[6 + c] = n3v[c]; }
+  for (int k = 0; k < 6; ++k) si[k] = 0.0;
+  for (int q = 0; q <= ng; ++q)
+    for (int p = 0; p <= ng; ++p) {
+      if (p == 0 && q == 0) continue;
+      const double d[3] = {CP(p, q, 0) - CP(0, 0, 0), CP(p, q, 1) - CP(0, 0, 1), CP(p, q, 2) - CP(0, 0, 2)};
+      for (int i = 0; i < 3; ++i) {
+        const double sk = (d[0] * sn[3 * i] + d[1] * sn[3 * i + 1]) + d[2] * sn[3 * i + 2];
+        if (sk < 0.0) si[2 * i] = std::fmin(si[2 * i], sk);
+        else if (sk > 0.0) si[2 * i + 1] = std::fmax(si[2 * i + 1], sk);
+      }
+    }
+  const double dx = std::fabs(si[1] - si[0]), dy = std::fabs(si[3] - si[2]), dz = std::fabs(si[5] - si[4]);
+  double h = dy;
+  const double w = std::fmin(dx, dz), len = std::fmax(dx, dz);
+  const double dMax = std::fmax(h, std::fmax(len, w));
+  if (len / dMax < 1.0e-6 || w / dMax < 1.0e-6) return false;
+  if (h / dMax < 1.0e-6) { si[2] = 0.0; si[3] = 0.0; h = 0.0; }
+  S[pic::kBzEmpty] = std::fabs(h / std::sqrt(len * len + w * w + h * h)) <= pic::kEpsMach ? 1.0 : 0.0;
+  return true;
 }
 
 int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
@@ -695,7 +767,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   }
   // ---- RefTracking wall sides: BC-element lists and planar-side geometry ------------------------
   std::vector<int> bc_e2b;
-  std::vector<double> bc_geo;
+  std::vector<double> bc_geo, bc_bz;
   // BC sides: the open/reflective walls, and with periodic_tracing (CartesianPeriodic = F) the periodic sides
   const bool bc_lists = cfg->tracking == PIC_TRACK_REFMAPPING &&
                         (m->n_periodic_vectors > 0 ? cfg->periodic_tracing != 0 : c->has_walls);
@@ -712,6 +784,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       if (n <= 0) { bc_e2b[2 * e] = -1; bc_e2b[2 * e + 1] = -1; }
     }
     bc_geo.assign((size_t)nent * kBcGeo, 0.0);
+    if (ng > 1) bc_bz.assign((size_t)nent * pic::kBzGeo, 0.0);
     for (int k = 0; k < nent; ++k) {
       const int e = m->bc_side_elem_loc[2 * k] - 1, sd = m->bc_side_elem_loc[2 * k + 1] - 1;
       const bool periodic_side = e >= 0 && e < ne && sd >= 0 && sd <= 5 && cfg->periodic_tracing &&
@@ -719,7 +792,15 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       if (e < 0 || e >= ne || sd < 0 || sd > 5 || (m->side_nb_elem[e * 6 + sd] != 0 && !periodic_side))
         return bail(fail(PIC_ERR_INVALID_ARGUMENT, "bc_side_elem_loc must name open/reflective wall sides, or "
                                                    "periodic sides with periodic_tracing"));
-      wall_side_geometry(xcl.data(), bary.data(), e, sd, &bc_geo[(size_t)k * kBcGeo]);
+      int given = -1;
+      if (ng > 1) {
+        // the side's SideType and Bezier patch (BezierControlPoints3D, slab normals and intervals)
+        given = m->side_type[e * 6 + sd];
+        if (given < 0 || given > 4) return bail(fail(PIC_ERR_INVALID_ARGUMENT, "side_type must be 0..4"));
+        if (!bezier_side_slab(ng, m->side_bezier + ((size_t)e * 6 + sd) * g1 * g1 * 3, &bc_bz[(size_t)k * pic::kBzGeo]))
+          return bail(fail(PIC_ERR_INVALID_ARGUMENT, "degenerated Bezier side (GetSideSlabNormalsAndIntervals)"));
+      }
+      wall_side_geometry(xcl.data(), bary.data(), e, sd, &bc_geo[(size_t)k * kBcGeo], given);
       bc_geo[(size_t)k * kBcGeo + 13] = m->bc_side_distance[k];
       if (periodic_side) {
         // PeriodicBC: the neighbour element (0-based) and BoundaryType(BC_ALPHA) of the side
@@ -813,6 +894,11 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     if ((rc = upload(c, &d_be, bc_e2b)) || (rc = upload(c, &d_bg, bc_geo))) return bail(rc);
     c->M.bc_e2b = d_be;
     c->M.bc_geo = d_bg;
+    if (!bc_bz.empty()) {
+      double* d_bz = nullptr;
+      if ((rc = upload(c, &d_bz, bc_bz))) return bail(rc);
+      c->M.bc_bz = d_bz;
+    }
   }
   c->MF = MeshF{d_xclr, d_dxclf, d_xezf, d_slenf};
   if (c->mixed) {
@@ -903,6 +989,7 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     }
   }
   k.ngeo = ng;
+  if (ng > 1) bezier_basis(ng, k.bz);
   for (int i = 0; i <= ng; ++i) { k.xi_cl_ng[i] = m->xi_cl_ngeo[i]; k.wbary_cl_ng[i] = m->wbary_cl_ngeo[i]; }
   if (ng == 1) {
     k.xi_cl[0] = m->xi_cl_ngeo[0]; k.xi_cl[1] = m->xi_cl_ngeo[1];

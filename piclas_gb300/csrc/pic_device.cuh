@@ -23,6 +23,15 @@ struct DevStatus {
   int n_ref_tolerance;
 };
 
+// the Bernstein tables of the mesh's NGeo for curved wall sides: FacNchooseK(n,k) = C(n,k)/2^n, Xi_NGeo
+// (equidistant nodes on [-1,1]) and D_Bezier (BuildBezierVdm, BuildBezierDMat: basis.f90:275-402)
+struct BzBasis {
+  int ng;
+  double fnk[kMaxNGeo + 1][kMaxNGeo + 1];
+  double xi[kMaxNGeo + 1];
+  double dbez[kMaxNGeo + 1][kMaxNGeo + 1];
+};
+
 // ---- run-time constants (constant memory) -------------------------------------------
 struct Consts {
   int N, n1, ndof, n_species;
@@ -49,6 +58,7 @@ struct Consts {
   int ref_guess;                               // RefMappingGuess 1..4
   int ngeo;                                    // NGeo (curved elements when > 1)
   double xi_cl_ng[kMaxNGeo + 1], wbary_cl_ng[kMaxNGeo + 1];   // XiCL_NGeo, wBaryCL_NGeo (xi_cl: of NGeo = 1)
+  BzBasis bz;                                  // curved wall sides (NGeo > 1)
   // N_Inter(k)%xGP, %wBary and CellVolWeight(k)%Fac for every degree k (row k; rows up to NMax are set), FP64
   // and FP32: the kernels of degree k read row k, so elements of different degrees (p-adaption) share them
   double xgp_n[kMaxN + 1][kMaxN + 1], wbary_n[kMaxN + 1][kMaxN + 1], fac_n[kMaxN + 1][kMaxN + 1];
@@ -77,6 +87,9 @@ struct DevMesh {
   // RefTracking with walls: per element (ELEM_NBR_BCSIDES, first entry) or (-1,-1); per entry kBcGeo doubles
   const int* bc_e2b;
   const double* bc_geo;
+  // curved meshes (NGeo > 1): per BC-side entry kBzGeo doubles -- BezierControlPoints3D [(q (NGeo+1) + p) 3 + c],
+  // SideSlabNormals [75..83], SideSlabIntervals [84..89], BoundingBoxIsEmpty [90]
+  const double* bc_bz;
   // shape-function DOF coordinates: elem_xgp, or for a 1D/2D kernel its directions only (others zero)
   const double* sf_xgp;
   // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
@@ -100,10 +113,10 @@ struct DevMesh {
 };
 // per BC-side entry: BaseVectors0-2 [0..8], SideNormVec (away from the element) [9..11], SideDistance [12],
 // SideBCMetrics(BCSIDE_DISTANCE) [13], boundary [14] (1 open, 2 reflective, 3 periodic), SideType [15]
-// (0 PLANAR_RECT, 1 PLANAR_NONRECT, 2 BILINEAR), BaseVectors3 [16..18], the corners P00, P10, P01, P11
+// (0 PLANAR_RECT, 1 PLANAR_NONRECT, 2 BILINEAR, 3 PLANAR_CURVED, 4 CURVED), BaseVectors3 [16..18], the corners P00, P10, P01, P11
 // [19..30], periodic sides: 16 (neighbour element, 0-based) + (BoundaryType(BC_ALPHA) + 8) [31]
 constexpr int kBcGeo = 32;
-constexpr int kBcCap = 32;   // wall sides traced per trajectory (entries within reach beyond it are not)
+constexpr int kBcCap = 64;   // wall sides traced per trajectory (entries within reach beyond it are not)
 
 // ---- particles (SoA) ---------------------------------------------------------------------
 struct DevParticles {
@@ -1216,6 +1229,10 @@ __device__ __forceinline__ void bilinear_normal(const double* __restrict__ g, do
   for (int c = 0; c < 3; ++c) nv[c] = n[c] / l;
 }
 
+}  // namespace pic
+#include "pic_bezier.cuh"
+namespace pic {
+
 // ParticleBCTracking, particle_reftracking.f90:417-694, for wall sides only (the element never changes).
 // Returns true when the particle is done: it has not moved (PARTHASMOVED) or an open wall removed it.
 static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int& elem, double x[3], double xl[3], double v[3],
@@ -1235,7 +1252,7 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int& elem, dou
     bool doubleCheck = false, moved_elem = false;
     double alphaOld = -1.0;
     for (int loop = 0; loop < 10000; ++loop) {
-      double alpha[kBcCap];
+      double alpha[kBcCap], sxi[kBcCap], seta[kBcCap];
       int list[kBcCap];
       int nc = 0, nInter = 0;
       const double alpha2 = doubleCheck ? alphaOld : -1.0;
@@ -1243,8 +1260,22 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int& elem, dou
         const double* g = M.bc_geo + (size_t)kBcGeo * (first + i);
         if (__ldg(g + 13) > len0) break;
         if (nc == kBcCap) { cap_hit = true; break; }
-        if (__ldg(g + 15) == 0.0) {
+        const double type = __ldg(g + 15);
+        sxi[nc] = 0.0;
+        seta[nc] = 0.0;
+        if (type == 0.0) {
           alpha[nc] = planar_rect_alpha(g, xl, traj, len);
+        } else if (type >= 3.0) {
+          // curved side: ComputeCurvedIntersection / ComputePlanarCurvedIntersection on its Bezier patch
+          const double* S = M.bc_bz + (size_t)kBzGeo * (first + i);
+          bool bad = false;
+          if (type == 4.0) {
+            alpha[nc] = bz_curved(kc.bz, S, xl, x, traj, len, sxi[nc], seta[nc], bad);
+          } else {
+            const double nv[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
+            alpha[nc] = bz_planar_curved(kc.bz, S, nv, __ldg(g + 12), xl, traj, len, sxi[nc], seta[nc], bad);
+          }
+          if (bad) cap_hit = true;
         } else {
           double sxi, seta;
           bool bad = false;
@@ -1257,12 +1288,17 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int& elem, dou
       }
       if (nInter == 0) return false;
       for (int i = 1; i < nc; ++i) {                       // InsertionSort (stable)
-        const double t = alpha[i];
+        const double t = alpha[i], txi = sxi[i], teta = seta[i];
         const int ti = list[i];
         int j = i - 1;
-        while (j >= 0 && !(alpha[j] <= t)) { alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; j--; }
+        while (j >= 0 && !(alpha[j] <= t)) {
+          alpha[j + 1] = alpha[j]; list[j + 1] = list[j]; sxi[j + 1] = sxi[j]; seta[j + 1] = seta[j];
+          j--;
+        }
         alpha[j + 1] = t;
         list[j + 1] = ti;
+        sxi[j + 1] = txi;
+        seta[j + 1] = teta;
       }
       for (int k = 0; k < nc; ++k)
         if (alpha[k] > -1.0) { alphaOld = alpha[k]; break; }
@@ -1271,12 +1307,15 @@ static __device__ __noinline__ bool bc_tracking(const DevMesh& M, int& elem, dou
         if (!(alpha[k] > -1.0)) continue;
         const double* g = M.bc_geo + (size_t)kBcGeo * (first + list[k]);
         double n[3] = {__ldg(g + 9), __ldg(g + 10), __ldg(g + 11)};
-        if (__ldg(g + 15) == 2.0) {
+        const double type = __ldg(g + 15);
+        if (type == 2.0) {
           // the hit's xi/eta: the same call as above (xl, traj, len and alpha2 are unchanged until an interaction)
-          double sxi = 0.0, seta = 0.0;
+          double bxi = 0.0, beta = 0.0;
           bool bad = false;
-          bilinear_alpha(g, xl, traj, len, alpha2, sxi, seta, bad);
-          bilinear_normal(g, sxi, seta, n);
+          bilinear_alpha(g, xl, traj, len, alpha2, bxi, beta, bad);
+          bilinear_normal(g, bxi, beta, n);
+        } else if (type >= 3.0) {
+          bz_normal(kc.bz, M.bc_bz + (size_t)kBzGeo * (first + list[k]), sxi[k], seta[k], n);   // CalcNormAndTangBezier
         }
         // GetBoundaryInteraction, REFMAPPING branch (particle_boundary_condition.f90:35-221)
         if (n[0] * traj[0] + n[1] * traj[1] + n[2] * traj[2] <= 0.0) { reflected = false; continue; }

@@ -1366,3 +1366,69 @@ def test_mixed_curved_newton_against_fp64(gpu_lib, oracle_lib, ng):
     st = oracle_lib.OracleState(g32["part_state"], g32["elem"], w.part_species)
     oracle_lib.map_particles(w.config(), capi.MeshStruct(w.mesh), st)
     assert np.max(np.abs(g32["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
+
+
+# ---- curved wall sides (NGeo > 1: Bezier clipping, BezierNewton) ------------------------------------------------
+def _curved_wall_workload(bc, ng, seed, bulge=0.0, shear=0.0, perturb=0.05, n=3000):
+    mesh = build_box_mesh(4, 4, 4, 2, perturb=perturb, bc=bc, wall_bulge=bulge, wall_shear=shear, n_geo=ng)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=n, T_eV=2000.0, seed=seed, dt=2e-10)
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(seed))
+    w.part_state[:, :3] = x
+    w.elem = e
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    return w
+
+
+@pytest.mark.parametrize("bc,ng,bulge,shear", [(("reflective",) * 3, 2, 0.2, 0.0),
+                                               (("reflective", "open", "reflective"), 2, 0.2, 0.0),
+                                               (("reflective", "open", "reflective"), 2, 0.0, 0.3),
+                                               (("open", "reflective", "reflective"), 3, 0.15, 0.1)])
+def test_reftracking_curved_walls_against_oracle(gpu_lib, oracle_lib, bc, ng, bulge, shear):
+    """Curved wall sides of an NGeo = 2, 3 box: bulged faces (SideType CURVED, Bezier clipping) and sheared planar
+    faces (PLANAR_CURVED, BezierNewton), reflective and open, 12 fused steps against the oracle -- the same
+    particles inside, the same elements, states within 1e-13, PartSource within 1e-12 of its maximum, no status
+    bit; mixed: the same particles inside but three, positions within 1e-6."""
+    w = _curved_wall_workload(bc, ng, seed=51, bulge=bulge, shear=shear)
+    g = _run_gpu(w, 12)
+    st, PS = _run_oracle(oracle_lib, w, 12)
+    assert np.array_equal(g["inside"], st.inside)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["part_state"], st.part_state) <= 1e-13
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0 and st.counters.n_ref_tolerance == 0 and st.counters.n_lost == 0
+    assert (np.sign(st.part_state[:, 3:]) != np.sign(w.part_state[:, 3:])).any(axis=1).sum() > 100
+    if "open" in bc:
+        assert (st.inside == 0).sum() > 100
+    gm = _run_gpu(w, 12, precision=capi.PIC_PREC_MIXED)
+    assert (gm["inside"] != st.inside).sum() <= 3
+    k = (gm["inside"] == 1) & (st.inside == 1)
+    assert np.max(np.abs(gm["part_state"][k, :3] - st.part_state[k, :3])) < 1e-6
+
+
+def test_reftracking_curved_periodic_tracing_against_oracle(gpu_lib, oracle_lib):
+    """CartesianPeriodic = F on a curved NGeo = 2 box: the periodic sides are BC sides of the RefTracking lists
+    (PLANAR_RECT faces of curved elements), together with a bulged reflective wall pair (CURVED); 8 steps against
+    the oracle with the same elements and particles inside, states within 1e-13, no status bit."""
+    mesh = build_box_mesh(6, 6, 6, 2, perturb=0.05, bc=("reflective", "periodic", "periodic"), wall_bulge=0.2,
+                          n_geo=2, periodic_tracing=True)
+    w = workloads.plasma_wave(mesh=mesh, n_particles=4000, T_eV=3000.0, seed=52, dt=1e-10)
+    x, e, _ = workloads._uniform_in_mesh(mesh, w.n, np.random.default_rng(52))
+    w.part_state[:, :3] = x
+    w.elem = e
+    w.tracking = capi.PIC_TRACK_REFMAPPING
+    w.periodic_tracing = True
+    g = _run_gpu(w, 8)
+    st, PS = _run_oracle(oracle_lib, w, 8)
+    assert np.array_equal(g["elem"], st.elem) and np.array_equal(g["inside"], st.inside)
+    assert _rel(g["part_state"], st.part_state) <= 1e-13
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert st.counters.n_hop_limit == 0 and st.counters.n_ref_tolerance == 0
+    assert g["status"]["error_word"] == 0 and (st.elem != w.elem).sum() > 200
+
+
+def test_reftracking_curved_walls_need_the_bezier_sides(gpu_lib):
+    w = _curved_wall_workload(("reflective",) * 3, 2, seed=53, bulge=0.2, n=100)
+    w.mesh.side_bezier = None
+    with pytest.raises(PicError) as e:
+        ParticleLoop(w.config(), w.mesh)
+    assert e.value.code == 1 and "side_bezier" in str(e.value)
