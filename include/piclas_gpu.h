@@ -226,7 +226,10 @@ typedef struct pic_mesh_t {
    * RotateMasterToSlave, particle_surfaces.f90:1171-1202, of the master's points for a slave side), and SideType
    * of those sides (PLANAR_RECT 0, PLANAR_NONRECT 1, BILINEAR 2, PLANAR_CURVED 3, CURVED 4; IdentifyElemAndSideType,
    * particle_mesh_tools.f90:848-1235).  PLANAR_CURVED sides are traced by ComputePlanarCurvedIntersection, CURVED
-   * ones by ComputeCurvedIntersection (Bezier clipping); NULL at NGeo = 1 (the corners give the side geometry). */
+   * ones by ComputeCurvedIntersection (Bezier clipping); NULL at NGeo = 1 (the corners give the side geometry).
+   * Layout: side_bezier[((e * 6 + s) * (NGeo+1) + q) * (NGeo+1) + p][3] (p the first Bezier index), side_type[e * 6 + s].
+   * Only the sides of the BC-element lists are read; pic_create rejects a degenerated one
+   * (GetSideSlabNormalsAndIntervals) and RefTracking with BC sides on a curved mesh without these arrays. */
   const double* side_bezier;
   const int32_t* side_type;
 } pic_mesh_t;
