@@ -1038,6 +1038,12 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(const __grid_constan
 // multiply-adds, at most kSf5Chunk / npar terms, ~30 on average) and adds that partial to its DOF's
 // (hi, lo) pair with TwoSum; the FP64 result is hi + lo.  Against the same accumulation with TwoSum per
 // hit: 15 % less time, rho error vs FP64 1.7e-7 instead of 1.3e-7 (32^3 curved, 16M particles).
+// FP64 with alpha = 2 and one radius: a staged particle whose kernel covers every DOF of the target (the far
+// corner of the DOF box within R (1 - 1e-6), so each reference test r^2 <= R^2 holds) adds
+// S_g^2 = (u.v_g + B_g)^2 to all of them, u = (p', A_p), v_g = (g, 1).  Summed over such particles it is
+// v^T Q_c v + 2 B_g v.L_c + B_g^2 Z_c with the moments Q_c = sum f_c u u^T, L_c = sum f_c u, Z_c = sum f_c
+// (15 per component), accumulated by 60 threads per particle and evaluated per DOF at the end: 2 FP64
+// instructions per thread and particle instead of 64 hits of 9 (about 16 % of the hits at R = 1.5 h, N = 3).
 constexpr int kSf5Chunk = 256;
 constexpr int kSf5Threads = 128;
 constexpr int kSf5Pairs = 160;
@@ -1079,6 +1085,10 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
   // p + npar*(2i+1) of parity p (see the comment at phase A)
   // (mixed uses s_pq only for the final per-DOF sums, so the FP16 copy lives there)
   constexpr bool H2 = MIXED && !ADAPT;
+  constexpr bool MOM = !MIXED && !ADAPT && A2;
+  __shared__ unsigned long long s_hbb[3];              // moments: DOF-box half extents (bits of |g_d| maxima)
+  __shared__ int s_nfull;
+  __shared__ uint8_t s_flist[MOM ? kSf5Chunk : 1];     // slots of the staged particles covering every DOF
   __shared__ int s_cnt, s_max;
   static_assert(sizeof(double) * 4 * npar * (halves * 32) <= sizeof(double2) * 2 * kSf5Chunk, "sums alias s_pq");
   static_assert(sizeof(__half2) * 3 * (kSf5Chunk / 2 + 4) <= sizeof(double2) * 2 * kSf5Chunk, "FP16 set aliases s_pq");
@@ -1104,6 +1114,18 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
     // B_g = 1 - |g|^2/R^2; adaptive: |g|^2 (the particle's own radius enters at each hit)
     gd[3] = ADAPT ? fma(gx, gx, fma(gy, gy, gz * gz)) : fma(-R2inv, fma(gx, gx, fma(gy, gy, gz * gz)), 1.0);
     gf[0] = (float)gx; gf[1] = (float)gy; gf[2] = (float)gz;
+  }
+  // moments: thread (half mh, index mm < 60) accumulates moment mm (component mm / 15; 0..9 Q_ij, 10..13 L_i,
+  // 14 Z) over the covering particles of its half; u[4] stands for 1
+  const int mh = t >> 6, mm = t & 63, mk = mm % 15;
+  const int mi = mk < 10 ? (mk < 4 ? 0 : mk < 7 ? 1 : mk < 9 ? 2 : 3) : (mk < 14 ? mk - 10 : 4);
+  const int mj = mk < 10 ? (mk < 4 ? mk : mk < 7 ? mk - 3 : mk < 9 ? mk - 5 : 3) : 4;
+  double mom = 0.0;
+  if constexpr (MOM) {
+    if (t < 3) s_hbb[t] = 0ull;
+    __syncthreads();
+    if (active)
+      for (int d = 0; d < 3; ++d) atomicMax(&s_hbb[d], (unsigned long long)__double_as_longlong(fabs(gd[d])));
   }
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1144,7 +1166,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
     long long cursor = 0;
     while (cursor < total) {
       __syncthreads();                     // the previous set is evaluated
-      if (t == 0) s_cnt = 0;
+      if (t == 0) { s_cnt = 0; s_nfull = 0; }
       __syncthreads();
       int nst = 0;
       while (cursor < total && nst <= kSf5Chunk - kSf5Threads) {
@@ -1193,8 +1215,29 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
           const double2* fp = reinterpret_cast<const double2*>(K.fac + 4 * j);
           s_fac[2 * slot] = fp[0];
           s_fac[2 * slot + 1] = fp[1];
+          if constexpr (MOM) {
+            const double fx = fabs(px) + __longlong_as_double((long long)s_hbb[0]),
+                         fy = fabs(py) + __longlong_as_double((long long)s_hbb[1]),
+                         fz = fabs(pz) + __longlong_as_double((long long)s_hbb[2]);
+            if (fma(fx, fx, fma(fy, fy, fz * fz)) <= kc.sf_r2 * (1.0 - 1.0e-6)) {
+              s_rel[slot].x = 1.0e30f;                       // the FP32 test of phase A skips it
+              s_flist[atomicAdd(&s_nfull, 1)] = (uint8_t)slot;
+            }
+          }
         }
         __syncthreads();
+        if constexpr (MOM) {
+          const int nf = s_nfull;
+          if (mm < 60) {
+            const int c = mm / 15;
+            for (int f = mh; f < nf; f += 2) {
+              const int q = s_flist[f];
+              const double* u = reinterpret_cast<const double*>(&s_pq[2 * q]);
+              const double ua = mi < 4 ? u[mi & 3] : 1.0, ub = mj < 4 ? u[mj & 3] : 1.0;
+              mom = fma(ua * ub, reinterpret_cast<const double*>(&s_fac[2 * q])[c], mom);
+            }
+          }
+        }
       }
       const int nper = (nst + npar - 1) / npar, np2 = (nper + 1) / 2;   // slots and slot pairs per parity
       if (h2) {
@@ -1293,6 +1336,10 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
 #pragma unroll
     for (int c = 0; c < 4; ++c) s_red[parity][dof][c] = acc[c];
   }
+  // the two halves of the 60 moments, in s_pq behind the per-DOF sums
+  double (*s_mom)[64] = reinterpret_cast<double (*)[64]>(s_pq) + 2 * npar * halves;
+  static_assert(sizeof(double) * (4 * npar * halves * 32 + 2 * 64) <= sizeof(double2) * 2 * kSf5Chunk, "moments alias s_pq");
+  if constexpr (MOM) s_mom[mh][mm] = mom;
   __syncthreads();
   if (t < nd) {
     double o[4];
@@ -1300,6 +1347,21 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
     for (int c = 0; c < 4; ++c) {
       o[c] = s_red[0][t][c];
       for (int k = 1; k < npar; ++k) o[c] = o[c] + s_red[k][t][c];
+    }
+    if constexpr (MOM) {
+      // the covering particles: v^T Q_c v + B (2 v.L_c + B Z_c), v = (g, 1), for the DOF of thread t (dof == t)
+      const double v[4] = {gd[0], gd[1], gd[2], 1.0}, B = gd[3];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        double m[15];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) m[k] = s_mom[0][15 * c + k] + s_mom[1][15 * c + k];
+        const double quad = v[0] * (v[0] * m[0] + 2.0 * (v[1] * m[1] + v[2] * m[2] + v[3] * m[3])) +
+                            v[1] * (v[1] * m[4] + 2.0 * (v[2] * m[5] + v[3] * m[6])) +
+                            v[2] * (v[2] * m[7] + 2.0 * v[3] * m[8]) + v[3] * v[3] * m[9];
+        const double lin = v[0] * m[10] + v[1] * m[11] + v[2] * m[12] + v[3] * m[13];
+        o[c] = o[c] + (quad + B * (2.0 * lin + B * m[14]));
+      }
     }
     double2* out = reinterpret_cast<double2*>(PS + (dof_base<N>(M, e) + t) * 4);
     out[0] = make_double2(o[0], o[1]);
