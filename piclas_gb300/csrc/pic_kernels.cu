@@ -1038,12 +1038,14 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(const __grid_constan
 // multiply-adds, at most kSf5Chunk / npar terms, ~30 on average) and adds that partial to its DOF's
 // (hi, lo) pair with TwoSum; the FP64 result is hi + lo.  Against the same accumulation with TwoSum per
 // hit: 15 % less time, rho error vs FP64 1.7e-7 instead of 1.3e-7 (32^3 curved, 16M particles).
-// FP64 with alpha = 2 and one radius: a staged particle whose kernel covers every DOF of the target (the far
-// corner of the DOF box within R (1 - 1e-6), so each reference test r^2 <= R^2 holds) adds
-// S_g^2 = (u.v_g + B_g)^2 to all of them, u = (p', A_p), v_g = (g, 1).  Summed over such particles it is
-// v^T Q_c v + 2 B_g v.L_c + B_g^2 Z_c with the moments Q_c = sum f_c u u^T, L_c = sum f_c u, Z_c = sum f_c
-// (15 per component), accumulated by 60 threads per particle and evaluated per DOF at the end: 2 FP64
-// instructions per thread and particle instead of 64 hits of 9 (about 16 % of the hits at R = 1.5 h, N = 3).
+// FP64 with alpha = 2 and one radius: a staged particle whose kernel covers every DOF of a DOF group -- the
+// target element, or (N = 3) one of its two DOF halves -- adds S_g^2 = (u.v_g + B_g)^2 to each of them,
+// u = (p', A_p), v_g = (g, 1).  Summed over such particles that is v^T Q_c v + 2 B_g v.L_c + B_g^2 Z_c with
+// the moments Q_c = sum f_c u u^T, L_c = sum f_c u, Z_c = sum f_c (15 per component), accumulated by 60
+// threads per particle and evaluated per DOF at the end: 2 FP64 instructions per thread and particle instead
+// of 9 per hit (at R = 1.5 h and N = 3 about 16 % of the hits are covered by the element test, 27 % with the
+// halves).  Covered means the group's DOF box lies within R (1 - 1e-4) of the particle in an FP32 test with
+// the box rounded outwards, so every reference test r^2 <= R^2 of the group holds.
 constexpr int kSf5Chunk = 256;
 constexpr int kSf5Threads = 128;
 constexpr int kSf5Pairs = 160;
@@ -1086,9 +1088,11 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
   // (mixed uses s_pq only for the final per-DOF sums, so the FP16 copy lives there)
   constexpr bool H2 = MIXED && !ADAPT;
   constexpr bool MOM = !MIXED && !ADAPT && A2;
-  __shared__ unsigned long long s_hbb[3];              // moments: DOF-box half extents (bits of |g_d| maxima)
+  // moments: DOF boxes (FP32, rounded outwards) of the halves and of the element, [group][lo, hi][axis]; the
+  // slots of the staged particles covering the element or one half (which: the bits in s_rel[slot].w)
+  __shared__ float s_box[3][2][3];
   __shared__ int s_nfull;
-  __shared__ uint8_t s_flist[MOM ? kSf5Chunk : 1];     // slots of the staged particles covering every DOF
+  __shared__ uint8_t s_flist[MOM ? kSf5Chunk : 1];
   __shared__ int s_cnt, s_max;
   static_assert(sizeof(double) * 4 * npar * (halves * 32) <= sizeof(double2) * 2 * kSf5Chunk, "sums alias s_pq");
   static_assert(sizeof(__half2) * 3 * (kSf5Chunk / 2 + 4) <= sizeof(double2) * 2 * kSf5Chunk, "FP16 set aliases s_pq");
@@ -1120,13 +1124,30 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
   const int mh = t >> 6, mm = t & 63, mk = mm % 15;
   const int mi = mk < 10 ? (mk < 4 ? 0 : mk < 7 ? 1 : mk < 9 ? 2 : 3) : (mk < 14 ? mk - 10 : 4);
   const int mj = mk < 10 ? (mk < 4 ? mk : mk < 7 ? mk - 3 : mk < 9 ? mk - 5 : 3) : 4;
-  double mom = 0.0;
+  double mom = 0.0, momh = 0.0;            // the element's moment (two copies) and half mh's
   if constexpr (MOM) {
-    if (t < 3) s_hbb[t] = 0ull;
+    // per-warp DOF boxes (a warp holds DOFs of one half); the parity-0 warps write their half's box
+    float lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = active ? __double2float_rd(gd[d]) : 3.0e38f;
+      hi[d] = active ? __double2float_ru(gd[d]) : -3.0e38f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+        hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+      }
+    }
+    if (parity == 0 && lane == 0)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) { s_box[w][0][d] = lo[d]; s_box[w][1][d] = hi[d]; }
     __syncthreads();
-    if (active)
-      for (int d = 0; d < 3; ++d) atomicMax(&s_hbb[d], (unsigned long long)__double_as_longlong(fabs(gd[d])));
+    if (t < 3) {
+      s_box[2][0][t] = halves == 2 ? fminf(s_box[0][0][t], s_box[1][0][t]) : s_box[0][0][t];
+      s_box[2][1][t] = halves == 2 ? fmaxf(s_box[0][1][t], s_box[1][1][t]) : s_box[0][1][t];
+    }
   }
+  const float cover2 = (float)(kc.sf_r2 * (1.0 - 1.0e-4));
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
   const double t2 = 2.0 * R2inv;
@@ -1181,7 +1202,23 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
             const float rx = r.x + s_o[pr][0], ry = r.y + s_o[pr][1], rz = r.z + s_o[pr][2];
             if (fmaf(rx, rx, fmaf(ry, ry, rz * rz)) <= cull2) {
               const int slot = atomicAdd(&s_cnt, 1);
-              s_rel[slot] = make_float4(rx, ry, rz, ADAPT ? s_r2f[pr] : 0.0f);
+              unsigned cov = 0;       // moments: bit h = the particle covers DOF half h (both: the element)
+              if constexpr (MOM) {
+                const float rr[3] = {rx, ry, rz};
+                auto far2 = [&](int b) {
+                  float sum = 0.f;
+#pragma unroll
+                  for (int d = 0; d < 3; ++d) {
+                    const float a = fmaxf(fabsf(rr[d] - s_box[b][0][d]), fabsf(rr[d] - s_box[b][1][d]));
+                    sum = fmaf(a, a, sum);
+                  }
+                  return sum;
+                };
+                if (far2(2) <= cover2) cov = halves == 2 ? 3u : 1u;
+                else if (halves == 2) cov = far2(0) <= cover2 ? 1u : far2(1) <= cover2 ? 2u : 0u;
+                if (cov) s_flist[atomicAdd(&s_nfull, 1)] = (uint8_t)slot;
+              }
+              s_rel[slot] = make_float4(rx, ry, rz, ADAPT ? s_r2f[pr] : __uint_as_float(cov));
               if constexpr (MIXED) {
                 s_facf[slot] = reinterpret_cast<const float4*>(K.facf)[j];
                 if constexpr (ADAPT) s_rp[slot] = s_rpf[pr];
@@ -1215,26 +1252,25 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
           const double2* fp = reinterpret_cast<const double2*>(K.fac + 4 * j);
           s_fac[2 * slot] = fp[0];
           s_fac[2 * slot + 1] = fp[1];
-          if constexpr (MOM) {
-            const double fx = fabs(px) + __longlong_as_double((long long)s_hbb[0]),
-                         fy = fabs(py) + __longlong_as_double((long long)s_hbb[1]),
-                         fz = fabs(pz) + __longlong_as_double((long long)s_hbb[2]);
-            if (fma(fx, fx, fma(fy, fy, fz * fz)) <= kc.sf_r2 * (1.0 - 1.0e-6)) {
-              s_rel[slot].x = 1.0e30f;                       // the FP32 test of phase A skips it
-              s_flist[atomicAdd(&s_nfull, 1)] = (uint8_t)slot;
-            }
-          }
         }
         __syncthreads();
         if constexpr (MOM) {
-          const int nf = s_nfull;
+          // thread group mh (two warps): the element-covering entries of its parity into mom, the entries
+          // covering half mh into momh (the branches are uniform per warp)
           if (mm < 60) {
             const int c = mm / 15;
-            for (int f = mh; f < nf; f += 2) {
+            const unsigned all = halves == 2 ? 3u : 1u;
+            const int nf = s_nfull;
+            for (int f = 0; f < nf; ++f) {
               const int q = s_flist[f];
+              const unsigned cov = __float_as_uint(s_rel[q].w);
+              const bool el = cov == all;
+              if (el ? (f & 1) != mh : cov != (1u << mh)) continue;
               const double* u = reinterpret_cast<const double*>(&s_pq[2 * q]);
               const double ua = mi < 4 ? u[mi & 3] : 1.0, ub = mj < 4 ? u[mj & 3] : 1.0;
-              mom = fma(ua * ub, reinterpret_cast<const double*>(&s_fac[2 * q])[c], mom);
+              const double fc = reinterpret_cast<const double*>(&s_fac[2 * q])[c];
+              if (el) mom = fma(ua * ub, fc, mom);
+              else momh = fma(ua * ub, fc, momh);
             }
           }
         }
@@ -1274,10 +1310,13 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
           if (msk & 0xFFFF0000u) s_list[w][nh++][lane] = (uint8_t)(2 * k + 1);
         }
       } else {
+        // moments: a particle covering this lane's DOF half is in the moments instead
+        const unsigned hbit = 1u << (w % halves);
         for (int m = 0; parity + npar * m < nst; ++m) {
           const float4 r = s_rel[parity + npar * m];
           const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
-          if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f)) s_list[w][nh++][lane] = (uint8_t)m;
+          const bool in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f);
+          if (MOM ? (in && !(__float_as_uint(r.w) & hbit)) : in) s_list[w][nh++][lane] = (uint8_t)m;
         }
       }
       // phase B: this lane's hits
@@ -1336,10 +1375,10 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
 #pragma unroll
     for (int c = 0; c < 4; ++c) s_red[parity][dof][c] = acc[c];
   }
-  // the two halves of the 60 moments, in s_pq behind the per-DOF sums
+  // the moments (element: two copies, then half 0 and half 1), in s_pq behind the per-DOF sums
   double (*s_mom)[64] = reinterpret_cast<double (*)[64]>(s_pq) + 2 * npar * halves;
-  static_assert(sizeof(double) * (4 * npar * halves * 32 + 2 * 64) <= sizeof(double2) * 2 * kSf5Chunk, "moments alias s_pq");
-  if constexpr (MOM) s_mom[mh][mm] = mom;
+  static_assert(sizeof(double) * (4 * npar * halves * 32 + 4 * 64) <= sizeof(double2) * 2 * kSf5Chunk, "moments alias s_pq");
+  if constexpr (MOM) { s_mom[mh][mm] = mom; s_mom[2 + mh][mm] = momh; }
   __syncthreads();
   if (t < nd) {
     double o[4];
@@ -1349,13 +1388,16 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
       for (int k = 1; k < npar; ++k) o[c] = o[c] + s_red[k][t][c];
     }
     if constexpr (MOM) {
-      // the covering particles: v^T Q_c v + B (2 v.L_c + B Z_c), v = (g, 1), for the DOF of thread t (dof == t)
+      // the covering particles: v^T Q_c v + B (2 v.L_c + B Z_c), v = (g, 1), for the DOF of thread t (dof == t,
+      // in half t / 32)
       const double v[4] = {gd[0], gd[1], gd[2], 1.0}, B = gd[3];
+      const int hrow = 2 + (halves == 2 ? t / 32 : 0);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         double m[15];
 #pragma unroll
-        for (int k = 0; k < 15; ++k) m[k] = s_mom[0][15 * c + k] + s_mom[1][15 * c + k];
+        for (int k = 0; k < 15; ++k)
+          m[k] = (s_mom[0][15 * c + k] + s_mom[1][15 * c + k]) + (halves == 2 ? s_mom[hrow][15 * c + k] : 0.0);
         const double quad = v[0] * (v[0] * m[0] + 2.0 * (v[1] * m[1] + v[2] * m[2] + v[3] * m[3])) +
                             v[1] * (v[1] * m[4] + 2.0 * (v[2] * m[5] + v[3] * m[6])) +
                             v[2] * (v[2] * m[7] + 2.0 * v[3] * m[8]) + v[3] * v[3] * m[9];
