@@ -1048,7 +1048,7 @@ __global__ void __launch_bounds__(kSf2Threads) k_sf_gather2(const __grid_constan
 // the box rounded outwards, so every reference test r^2 <= R^2 of the group holds.
 constexpr int kSf5Chunk = 256;
 constexpr int kSf5Threads = 128;
-constexpr int kSf5Pairs = 160;
+constexpr int kSf5Pairs = 152;
 
 // (1 - r^2/R^2)^alpha from Sv = 1 - r^2/R^2: S*S, then alpha - 2 more factors (runtime alpha unless A2)
 template <bool A2, typename T>
@@ -1072,6 +1072,7 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
   __shared__ __align__(16) double2 s_pq[2 * kSf5Chunk];  // FP64: (p'x, p'y), (p'z, A_p); per-DOF sums at the end
   __shared__ double2 s_fac[MIXED ? 1 : 2 * kSf5Chunk];
   __shared__ uint8_t s_list[kSf5Threads / 32][cap][32];
+  __shared__ uint8_t s_nh[kSf5Threads / 32][32];         // hit-list lengths (pooled phase B)
   __shared__ int s_j[kSf5Chunk];
   __shared__ uint8_t s_pr[kSf5Chunk];
   __shared__ int s_b0[kSf5Pairs], s_n[kSf5Pairs];
@@ -1290,39 +1291,54 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
         }
         __syncthreads();
       }
-      if (!active) continue;
-      // phase A: test of this lane's DOF against its parity's particles, into the lane's hit list (slot
-      // index / npar, ascending).  FP32 with (1+1e-4) R^2; mixed with one radius and a DOF box within 2R:
-      // packed FP16 in units of R against 1.05 (error of r^2/R^2 below 1.5e-2 near the threshold), two
-      // particles per instruction.  Either way phase B repeats the exact test, so only the work changes.
       int nh = 0;
-      if (h2) {
-        const float ir = kc.sf_r_inv;
-        const __half2 gx = __float2half2_rn(gf[0] * ir), gy = __float2half2_rn(gf[1] * ir),
-                      gz = __float2half2_rn(gf[2] * ir);
-        const __half2 thr = __float2half2_rn(1.05f);
-        for (int k = 0; k < np2; ++k) {
-          const __half2* e = s_h[k * npar + parity];
-          const __half2 dx = __hsub2(e[0], gx), dy = __hsub2(e[1], gy), dz = __hsub2(e[2], gz);
-          const __half2 r2 = __hfma2(dx, dx, __hfma2(dy, dy, __hmul2(dz, dz)));
-          const unsigned msk = __hle2_mask(r2, thr);
-          if (msk & 0xFFFFu) s_list[w][nh++][lane] = (uint8_t)(2 * k);
-          if (msk & 0xFFFF0000u) s_list[w][nh++][lane] = (uint8_t)(2 * k + 1);
-        }
-      } else {
-        // moments: a particle covering this lane's DOF half is in the moments instead
-        const unsigned hbit = 1u << (w % halves);
-        for (int m = 0; parity + npar * m < nst; ++m) {
-          const float4 r = s_rel[parity + npar * m];
-          const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
-          const bool in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f);
-          if (MOM ? (in && !(__float_as_uint(r.w) & hbit)) : in) s_list[w][nh++][lane] = (uint8_t)m;
+      if (active) {
+        // phase A: test of this lane's DOF against its parity's particles, into the lane's hit list (slot
+        // index / npar, ascending).  FP32 with (1+1e-4) R^2; mixed with one radius and a DOF box within 2R:
+        // packed FP16 in units of R against 1.05 (error of r^2/R^2 below 1.5e-2 near the threshold), two
+        // particles per instruction.  Either way phase B repeats the exact test, so only the work changes.
+        if (h2) {
+          const float ir = kc.sf_r_inv;
+          const __half2 gx = __float2half2_rn(gf[0] * ir), gy = __float2half2_rn(gf[1] * ir),
+                        gz = __float2half2_rn(gf[2] * ir);
+          const __half2 thr = __float2half2_rn(1.05f);
+          for (int k = 0; k < np2; ++k) {
+            const __half2* e = s_h[k * npar + parity];
+            const __half2 dx = __hsub2(e[0], gx), dy = __hsub2(e[1], gy), dz = __hsub2(e[2], gz);
+            const __half2 r2 = __hfma2(dx, dx, __hfma2(dy, dy, __hmul2(dz, dz)));
+            const unsigned msk = __hle2_mask(r2, thr);
+            if (msk & 0xFFFFu) s_list[w][nh++][lane] = (uint8_t)(2 * k);
+            if (msk & 0xFFFF0000u) s_list[w][nh++][lane] = (uint8_t)(2 * k + 1);
+          }
+        } else {
+          // moments: a particle covering this lane's DOF half is in the moments instead
+          const unsigned hbit = 1u << (w % halves);
+          for (int m = 0; parity + npar * m < nst; ++m) {
+            const float4 r = s_rel[parity + npar * m];
+            const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
+            const bool in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= (ADAPT ? r.w : R2f);
+            if (MOM ? (in && !(__float_as_uint(r.w) & hbit)) : in) s_list[w][nh++][lane] = (uint8_t)m;
+          }
         }
       }
-      // phase B: this lane's hits
+      // the npar warps holding a DOF (one per particle parity) pool its hit lists and take equal shares: the
+      // longest share of a warp is closer to the mean than the longest own list
+      s_nh[w][lane] = (uint8_t)nh;
+      __syncthreads();
+      if (!active) continue;
+      // phase B: this lane's share of its DOF's pooled hits (the lists of parities 0..npar-1 in turn)
+      int pre[npar + 1];
+      pre[0] = 0;
+#pragma unroll
+      for (int k = 0; k < npar; ++k) pre[k + 1] = pre[k] + s_nh[w % halves + halves * k][lane];
+      const int plo = (parity * pre[npar]) / npar, phi = ((parity + 1) * pre[npar]) / npar;
       float part[4] = {0.f, 0.f, 0.f, 0.f};      // mixed: this staged set's FP32 partial sums
-      for (int k = 0; k < nh; ++k) {
-        const int q = parity + npar * (int)s_list[w][k][lane];
+      for (int pos = plo; pos < phi; ++pos) {
+        int kp = 0;
+#pragma unroll
+        for (int k = 1; k < npar; ++k) kp += pos >= pre[k] ? 1 : 0;
+        const int base = kp == 0 ? 0 : kp == 1 ? pre[1] : kp == 2 ? pre[2] : pre[npar - 1];
+        const int q = kp + npar * (int)s_list[w % halves + halves * kp][pos - base][lane];
         if constexpr (MIXED) {
           const float4 r = s_rel[q];
           const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
