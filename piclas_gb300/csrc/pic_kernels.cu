@@ -1321,24 +1321,29 @@ __global__ void __launch_bounds__(kSf5Threads) k_sf_gather5(const __grid_constan
           }
         }
       }
-      // the npar warps holding a DOF (one per particle parity) pool its hit lists and take equal shares: the
-      // longest share of a warp is closer to the mean than the longest own list
-      s_nh[w][lane] = (uint8_t)nh;
-      __syncthreads();
+      // FP64: the npar warps holding a DOF (one per particle parity) pool its hit lists and take equal shares:
+      // the longest share of a warp is closer to the mean than the longest own list (mixed: the FP32 hits are
+      // too cheap for the extra barrier and bookkeeping, each lane takes its own list)
+      if constexpr (!MIXED) {
+        s_nh[w][lane] = (uint8_t)nh;
+        __syncthreads();
+      }
       if (!active) continue;
       // phase B: this lane's share of its DOF's pooled hits (the lists of parities 0..npar-1 in turn)
       int pre[npar + 1];
       pre[0] = 0;
 #pragma unroll
-      for (int k = 0; k < npar; ++k) pre[k + 1] = pre[k] + s_nh[w % halves + halves * k][lane];
-      const int plo = (parity * pre[npar]) / npar, phi = ((parity + 1) * pre[npar]) / npar;
+      for (int k = 0; k < npar; ++k)
+        pre[k + 1] = pre[k] + (MIXED ? (k == parity ? nh : 0) : (int)s_nh[w % halves + halves * k][lane]);
+      const int plo = MIXED ? 0 : (parity * pre[npar]) / npar, phi = MIXED ? nh : ((parity + 1) * pre[npar]) / npar;
       float part[4] = {0.f, 0.f, 0.f, 0.f};      // mixed: this staged set's FP32 partial sums
       for (int pos = plo; pos < phi; ++pos) {
         int kp = 0;
 #pragma unroll
         for (int k = 1; k < npar; ++k) kp += pos >= pre[k] ? 1 : 0;
         const int base = kp == 0 ? 0 : kp == 1 ? pre[1] : kp == 2 ? pre[2] : pre[npar - 1];
-        const int q = kp + npar * (int)s_list[w % halves + halves * kp][pos - base][lane];
+        const int q = MIXED ? parity + npar * (int)s_list[w][pos][lane]
+                            : kp + npar * (int)s_list[w % halves + halves * kp][pos - base][lane];
         if constexpr (MIXED) {
           const float4 r = s_rel[q];
           const float dx = r.x - gf[0], dy = r.y - gf[1], dz = r.z - gf[2];
