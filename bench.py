@@ -41,22 +41,27 @@ def log(*a):
 
 # ----------------------------------------------------------------------------------------------
 def make_workload(name: str, seed: int, n_override: int | None = None, cells: int | None = None,
-                  periodic_tracing: bool = False, n_geo: int = 1, p_adaption: str | None = None):
+                  periodic_tracing: bool = False, n_geo: int = 1, p_adaption: str | None = None,
+                  walls: str | None = None, wall_bulge: float = 0.0):
     from piclas_gb300 import workloads
     from piclas_gb300.mesh import build_box_mesh, p_adaption_degrees
     kw = {} if cells is None else {"n_cells": cells}
     if name == "curved":
         if n_override is not None:
             kw["n_per_species"] = n_override // 2
-        if periodic_tracing or n_geo > 1 or p_adaption:
+        if periodic_tracing or n_geo > 1 or p_adaption or walls:
             # periodic_tracing: the reference's default periodic RefTracking (CartesianPeriodic = F), BC lists with
-            # the periodic sides; n_geo: curved elements of that geometry degree; p_adaption: degrees 1..3 per element
+            # the periodic sides; n_geo: curved elements of that geometry degree; p_adaption: degrees 1..3 per
+            # element; walls: a closed box with reflective walls (wall_bulge: bulged wall faces, bilinear sides at
+            # NGeo = 1 and curved Bezier sides at NGeo > 1)
             nc = kw.pop("n_cells", 32)
             n_loc = p_adaption_degrees(nc, nc, nc, p_adaption, 1, 3, seed=seed) if p_adaption else None
+            bc = (walls,) * 3 if walls else ("periodic",) * 3
             kw["mesh"] = build_box_mesh(nc, nc, nc, 3, perturb=0.05, periodic_tracing=periodic_tracing, n_geo=n_geo,
-                                        n_loc=n_loc)
+                                        n_loc=n_loc, bc=bc, wall_bulge=wall_bulge if walls else 0.0)
         w = workloads.curved_two_species(seed=seed, **kw)
         w.periodic_tracing = periodic_tracing
+        w.walls, w.wall_bulge = walls, (wall_bulge if walls else 0.0)
         return w
     if name == "plasma_wave":
         if n_override is not None:
@@ -72,6 +77,11 @@ def workload_config(w, name):
         tag = "plain FP64 at scale: " if (cells == 32 and w.n == 16_000_000) else "profiling case of plain FP64 at scale: "
         trk = ("RefTracking (CartesianPeriodic = F: periodic sides traced as BC sides)"
                if getattr(w, "periodic_tracing", False) else "RefTracking (CartesianPeriodic/FastPeriodic)")
+        walls = getattr(w, "walls", None)
+        if walls:
+            bulge = getattr(w, "wall_bulge", 0.0)
+            side = ("planar" if bulge == 0.0 else "bilinear" if m.n_geo == 1 else "curved Bezier (clipping)")
+            trk = f"RefTracking, {walls} walls all round ({side} wall sides, ParticleBCTracking)"
         geo = "curved hex" if m.n_geo == 1 else f"curved NGeo={m.n_geo} hex"
         deg = f"N={m.N}" if m.n_loc is None else f"N_loc random 1..{m.N} ({m.n_dofs} DOFs)"
         out = {"workload": f"{tag}{cells}^3 {geo}, {deg}, {w.n // 2} e- + {w.n - w.n // 2} ions, "
@@ -82,6 +92,9 @@ def workload_config(w, name):
             out["n_geo"] = m.n_geo
         if m.n_loc is not None:
             out["p_adaption"] = "random 1..3"
+        if walls:
+            out["walls"] = walls
+            out["wall_bulge"] = getattr(w, "wall_bulge", 0.0)
         return out
     cells = round(m.n_elems ** (1.0 / 3.0))
     return {"workload": f"plasma wave: {cells}^3 hex, N={m.N}, {w.n} e-, CVWM, TriaTracking, dt=1e-11",
@@ -335,7 +348,8 @@ def mesh_kwargs(args):
     """The mesh variant flags of a curved-workload run (periodic BC tracing, NGeo, p-adaption)."""
     if args.workload != "curved":
         return {}
-    return {"periodic_tracing": args.periodic_tracing, "n_geo": args.ngeo, "p_adaption": args.p_adaption}
+    return {"periodic_tracing": args.periodic_tracing, "n_geo": args.ngeo, "p_adaption": args.p_adaption,
+            "walls": args.walls, "wall_bulge": args.wall_bulge}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -353,7 +367,7 @@ def run_gpu(args, rank, world, local_rank):
     prec = capi.PIC_PREC_MIXED if mixed else capi.PIC_PREC_FP64
     t0 = time.time()
     w = make_workload(args.workload, seed=rank, n_override=args.particles, cells=args.cells,
-                      periodic_tracing=args.periodic_tracing, n_geo=args.ngeo, p_adaption=args.p_adaption)
+                      **mesh_kwargs(args))
     log(f"[rank {rank}] workload {w.name} built in {time.time() - t0:.1f}s")
     cfg = w.config(precision=prec, sort_interval=args.sort_interval)
     loop = ParticleLoop(cfg, w.mesh)
@@ -838,8 +852,9 @@ def reference_config(args):
     cells, n = {"curved": (32, 16_000_000), "plasma_wave": (8, 200_000)}.get(args.workload, (8, 200_000))
     n_loc = p_adaption_degrees(cells, cells, cells, args.p_adaption, 1, 3, seed=0) if args.p_adaption else None
     n_dofs = cells ** 3 * 64 if n_loc is None else int(((np.asarray(n_loc) + 1) ** 3).sum())
+    walls = args.walls if args.workload == "curved" else None
     stand_in = NS(mesh=NS(n_elems=cells ** 3, N=3, n_geo=args.ngeo, n_loc=n_loc, n_dofs=n_dofs), n=n,
-                  periodic_tracing=args.periodic_tracing)
+                  periodic_tracing=args.periodic_tracing, walls=walls, wall_bulge=args.wall_bulge if walls else 0.0)
     return dict(workload_config(stand_in, args.workload if args.workload == "curved" else "plasma_wave"),
                 precision=args.precision, parallelism=f"replicas x{args.gpus}")
 
@@ -881,6 +896,10 @@ def main():
                     help="curved workload with per-element degrees 1..3 (N_DG_Mapping)")
     ap.add_argument("--periodic-tracing", action="store_true",
                     help="RefTracking traces the periodic sides as BC sides (the reference's default CartesianPeriodic = F)")
+    ap.add_argument("--walls", default=None, choices=["reflective"],
+                    help="curved workload in a closed box with these walls all round (ParticleBCTracking)")
+    ap.add_argument("--wall-bulge", type=float, default=0.0,
+                    help="with --walls: bulge the wall faces inwards by this fraction of h (curved sides at NGeo > 1)")
     ap.add_argument("--hdg-cg-kernel", type=int, default=0, choices=[0, 1, 2],
                     help="HDG CG launch form: 0 auto, 1 kernel per phase (graph), 2 cooperative")
     args = ap.parse_args()

@@ -177,13 +177,13 @@ def _uniform_in_mesh(mesh: BoxMesh, n: int, rng, chunk: int = 1 << 20) -> tuple[
     # rejection bound on det J: the displacement field is smooth, det J stays within a few
     # percent of h^3/8; the bound is checked on every sample
     dmax = float(np.prod(mesh.h)) / 8.0 * 1.25
-    if mesh.n_geo > 1:
-        # curved walls (bulged or sheared faces) vary det J by more: bound it from a probe sample
-        pr = np.random.default_rng(12345)
-        m = min(65536, 64 * mesh.n_elems)
-        _, det = _curved_map(mesh, pr.integers(0, mesh.n_elems, size=m), pr.random((m, 3)) * 2.0 - 1.0)
-        if det.max() >= dmax:
-            dmax = 1.3 * float(det.max())
+    # bulged or sheared wall faces vary det J by more: then the bound comes from a probe sample
+    pr = np.random.default_rng(12345)
+    m = min(65536, 64 * mesh.n_elems)
+    e_pr, xi_pr = pr.integers(0, mesh.n_elems, size=m), pr.random((m, 3)) * 2.0 - 1.0
+    _, det = _trilinear(mesh, e_pr, xi_pr) if mesh.n_geo == 1 else _curved_map(mesh, e_pr, xi_pr)
+    if det.max() >= dmax:
+        dmax = 1.3 * float(det.max())
     got = 0
     while got < n:
         m = min(chunk, int((n - got) * 1.4) + 1024)

@@ -64,7 +64,7 @@ def test_reference_arm_reports_the_gpu_arms_config():
              ("curved", 32, 16_000_000, 2, None, True), ("curved", 32, 16_000_000, 1, "random", False))
     for name, cells, n, ngeo, padapt, ptrace in cases:
         args = argparse.Namespace(workload=name, precision="fp64", gpus=1, ngeo=ngeo, p_adaption=padapt,
-                                  periodic_tracing=ptrace)
+                                  periodic_tracing=ptrace, walls=None, wall_bulge=0.0)
         ref = bench.reference_config(args)
         mesh = build_box_mesh(2, 2, 2, 3)
         stand_in = workloads.Workload(**{**workloads.plasma_wave(mesh=mesh, n_particles=10).__dict__})
