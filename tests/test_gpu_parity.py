@@ -1432,3 +1432,31 @@ def test_reftracking_curved_walls_need_the_bezier_sides(gpu_lib):
     with pytest.raises(PicError) as e:
         ParticleLoop(w.config(), w.mesh)
     assert e.value.code == 1 and "side_bezier" in str(e.value)
+
+
+# ---- FP64 shape-function gather: particles covering the target's DOFs enter through moments ----------------------
+@pytest.mark.parametrize("N,radius_cells", [(3, 1.5), (3, 3.0), (2, 3.0), (1, 2.0)])
+def test_sf_gather_moments_against_oracle(gpu_lib, oracle_lib, N, radius_cells):
+    """The FP64 gather sums the particles whose kernel covers every DOF of the target element (or, at N = 3, of
+    one DOF half) as moments of (A_p + B_g + p'.g)^2 instead of per (particle, DOF) hit: at R = 3 h most of the
+    hits go that way, at R = 1.5 h about a quarter.  PartSource within 1e-12 of the oracle's per-hit sum, the
+    same for the deposition of a single step (no tracking between) and for 4 fused steps."""
+    mesh = build_box_mesh(6, 6, 6, N, perturb=0.05)
+    w = workloads.curved_two_species(mesh=mesh, n_per_species=3000, seed=61, Te_eV=1000.0, nsteps=4,
+                                     sf_radius_cells=radius_cells)
+    cfg, ms = w.config(), capi.MeshStruct(mesh)
+    loop = ParticleLoop(cfg, mesh)
+    loop.set_field(w.e_dof)
+    loop.upload_particles(w.part_state, w.elem, w.part_species)
+    PSg = loop.deposition()
+    loop.close()
+    st = oracle_lib.OracleState(w.part_state, w.elem, w.part_species)
+    oracle_lib.map_particles(cfg, ms, st)
+    PSo = np.zeros(mesh.dof_shape(4))
+    oracle_lib.deposit(cfg, ms, st, PSo)
+    assert _rel(PSg, PSo) <= 1e-12
+    g = _run_gpu(w, 4, dt=2e-11)
+    st, PS = _run_oracle(oracle_lib, w, 4, dt=2e-11)
+    assert np.array_equal(g["elem"], st.elem)
+    assert _rel(g["PS"], PS) <= 1e-12
+    assert g["status"]["error_word"] == 0
