@@ -1382,7 +1382,8 @@ def _curved_wall_workload(bc, ng, seed, bulge=0.0, shear=0.0, perturb=0.05, n=30
 @pytest.mark.parametrize("bc,ng,bulge,shear", [(("reflective",) * 3, 2, 0.2, 0.0),
                                                (("reflective", "open", "reflective"), 2, 0.2, 0.0),
                                                (("reflective", "open", "reflective"), 2, 0.0, 0.3),
-                                               (("open", "reflective", "reflective"), 3, 0.15, 0.1)])
+                                               (("open", "reflective", "reflective"), 3, 0.15, 0.1),
+                                               (("reflective", "reflective", "open"), 4, 0.2, 0.0)])
 def test_reftracking_curved_walls_against_oracle(gpu_lib, oracle_lib, bc, ng, bulge, shear):
     """Curved wall sides of an NGeo = 2, 3 box: bulged faces (SideType CURVED, Bezier clipping) and sheared planar
     faces (PLANAR_CURVED, BezierNewton), reflective and open, 12 fused steps against the oracle -- the same

@@ -968,7 +968,7 @@ def _face_point(mesh, e, s, u, v):
     NGeo map with the face's reference coordinate fixed (s: 'ylo' -> xi_2 = -1, u = xi_1, v = xi_3)."""
     assert s == "ylo"
     x = elem_map(mesh, e, (u, -1.0, v))
-    d = 1e-5                                            # central differences: exact for the quadratic map
+    d = 1e-5                                            # central differences (O(d^2) for the polynomial map)
     tu = (elem_map(mesh, e, (u + d, -1.0, v)) - elem_map(mesh, e, (u - d, -1.0, v))) / (2 * d)
     tv = (elem_map(mesh, e, (u, -1.0, v + d)) - elem_map(mesh, e, (u, -1.0, v - d))) / (2 * d)
     return x, tu, tv
@@ -990,7 +990,7 @@ def _line_face_hit(mesh, e, x0, dx):
     return q, x, n / np.linalg.norm(n)
 
 
-@pytest.mark.parametrize("n_geo", [2, 3])
+@pytest.mark.parametrize("n_geo", [2, 3, 4])
 def test_curved_wall_reflection_against_an_independent_solve(oracle_lib, n_geo):
     """Bulged (SideType CURVED) reflective walls: a particle that reaches the lower y wall within one step ends at
     the mirror image of its path in the wall's tangent plane at the hit point, with the velocity reflected there;
