@@ -276,9 +276,10 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
     (CartesianPeriodic = F) they include the periodic sides, and walls may be combined with periodic axes.
     ``wall_bulge`` moves the nodes of each open/reflective face inwards along its normal by
     ``wall_bulge*h*sin(pi u)sin(pi v)`` (u, v in [0,1] across the face): the wall sides become bilinear
-    (SideType BILINEAR).  ``wall_shear`` moves them within the face plane by ``wall_shear*h`` times the
-    same bump along the first in-plane axis: planar sides that are no longer rectangles (PLANAR_NONRECT).
-    The face edges stay put.
+    (SideType BILINEAR; at NGeo > 1 curved, CURVED, with the CL points inside the wall elements moved by the
+    same bump fading linearly across the element layer).  ``wall_shear`` moves them within the face plane by
+    ``wall_shear*h`` times the same bump along the first in-plane axis: planar sides that are no longer
+    rectangles (PLANAR_NONRECT; at NGeo > 1 PLANAR_CURVED).  The face edges stay put.
     """
     bc = tuple(bc)
     if n_geo < 1 or n_geo > 4:
@@ -373,7 +374,9 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                               * np.sin(2.0 * np.pi * (p0[:, 2] - lo[2]) / L[2]))
                         p0 = np.where(inner[:, None], p0 + perturb * hvec[None, :] * sv[:, None], p0)
                     if wall_bulge != 0.0 or wall_shear != 0.0:
-                        # the wall faces' bump, as for the grid nodes: along the wall normal and within the plane
+                        # the wall faces' bump, as for the grid nodes: along the wall normal and within the plane,
+                        # fading linearly to zero across the wall element layer (grid index distance 1), so that the
+                        # CL points inside a wall element follow the face and no element folds over
                         U = (p0 - lo) / L
                         p0 = p0.copy()
                         for d in range(3):
@@ -381,9 +384,11 @@ def build_box_mesh(nx: int, ny: int, nz: int, N: int, lo=(0.0, 0.0, 0.0), hi=(1.
                                 continue
                             o1, o2 = [q for q in range(3) if q != d]
                             bump = np.sin(np.pi * U[:, o1]) * np.sin(np.pi * U[:, o2])
-                            for on_face, sign in ((g[:, d] == 0.0, 1.0), (g[:, d] >= dims_f[d], -1.0)):
-                                p0[:, d] = np.where(on_face, p0[:, d] + sign * wall_bulge * hvec[d] * bump, p0[:, d])
-                                p0[:, o1] = np.where(on_face, p0[:, o1] + wall_shear * hvec[o1] * bump, p0[:, o1])
+                            wlo = np.clip(1.0 - g[:, d], 0.0, 1.0)
+                            whi = np.clip(1.0 - (dims_f[d] - g[:, d]), 0.0, 1.0)
+                            for wgt, sign in ((wlo, 1.0), (whi, -1.0)):
+                                p0[:, d] = p0[:, d] + sign * wall_bulge * hvec[d] * bump * wgt
+                                p0[:, o1] = p0[:, o1] + wall_shear * hvec[o1] * bump * wgt
                     xcl[:, c, b, a, :] = p0
         for c in range(2):
             for b in range(2):

@@ -1080,7 +1080,7 @@ def test_curved_open_walls_remove_exactly_the_crossing_particles(oracle_lib):
     w.part_state[:, :3] = x
     w.part_state[:, 3] = 0.0
     w.part_state[:, 5] = 0.0
-    w.part_state[:, 4] = rng.choice([-1.0, 1.0], n) * rng.uniform(0.2, 0.6, n) / (w.dt * 10)
+    w.part_state[:, 4] = rng.choice([-1.0, 1.0], n) * rng.uniform(0.1, 0.45, n) / (w.dt * 10)   # |v| < 0.76 c
     w.elem = e
     ref = _ref_wall_steps(oracle_lib, w, 10)
     assert ref.counters.n_lost == 0 and ref.counters.n_ref_tolerance == 0
