@@ -915,6 +915,23 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
     double* d_tc = nullptr;
     if ((rc = upload(c, &d_tc, tc))) return bail(rc);
     c->M.tcoef = d_tc;
+    // the same coefficients over s_e = 2^round(log2 max|c1..c3|) as double-FP32 pairs, then (s_e, 1/s_e)
+    std::vector<float2> tdf((size_t)ne * 25);
+    for (int e = 0; e < ne; ++e) {
+      double mx = 0.0;
+      for (int q = 1; q <= 3; ++q)
+        for (int k = 0; k < 3; ++k) mx = std::max(mx, std::fabs(tc[(size_t)e * 24 + 3 * q + k]));
+      const double sc = mx > 0.0 ? std::ldexp(1.0, (int)std::lround(std::log2(mx))) : 1.0;
+      for (int j = 0; j < 24; ++j) {
+        const double v = tc[(size_t)e * 24 + j] / sc;
+        const float hi = (float)v;
+        tdf[(size_t)e * 25 + j] = make_float2(hi, (float)(v - (double)hi));
+      }
+      tdf[(size_t)e * 25 + 24] = make_float2((float)sc, (float)(1.0 / sc));
+    }
+    float2* d_tdf = nullptr;
+    if ((rc = upload(c, &d_tdf, tdf))) return bail(rc);
+    c->M.tcoef_df = d_tdf;
     if (ng > 1) {
       // the NGeo map in power form: along each axis C_a = sum_i T(a,i) X_i with T = V^-1, V(i,a) = XiCL_i^a
       double V[5][10];

@@ -107,6 +107,10 @@ struct DevMesh {
   // mixed variant on curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c,
   // [ne][(NGeo+1)^3][3] in that index order
   const double* tcoef_ng;
+  // mixed variant: tcoef / s_e as double-FP32 pairs (hi, lo) for the Newton in double-FP32 arithmetic, [ne][25]:
+  // 24 coefficients, then (s_e, 1/s_e) with s_e the power of two nearest the element's size (the scaled map is
+  // O(1), far from the FP32 range limits)
+  const float2* tcoef_df;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
@@ -429,6 +433,126 @@ __device__ __forceinline__ bool ref_elem_newton_fast_lin(const DevMesh& M, int e
   return success;
 }
 
+// ---- double-FP32 ("double-float") arithmetic: a value is the unevaluated sum hi + lo of two floats, |lo| <= ulp(hi)/2,
+// about 48 significant bits.  Error-free transforms after Dekker (1971, "A floating-point technique for extending
+// the available precision") and Knuth (TwoSum, TAOCP vol. 2, 4.2.2), the product error from one fused multiply-add,
+// and the accurate addition of Hida, Li and Bailey (QD library, 2001).  GB300 runs FP32 at about 70x its FP64 rate.
+struct DF { float hi, lo; };
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {      // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  const DF s = df_two_sum(x.hi, y.hi), t = df_two_sum(x.lo, y.lo);
+  const DF u = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return df_fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF df_div(DF a, DF b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const DF r = df_add(a, df_neg(df_mul(DF{q1, 0.f}, b)));
+  return df_fast_two_sum(q1, __fdiv_rn(r.hi, b.hi));
+}
+__device__ __forceinline__ DF df_of(double d) {
+  const float h = __double2float_rn(d);
+  return DF{h, __double2float_rn(d - (double)h)};
+}
+__device__ __forceinline__ double df_val(DF a) { return (double)a.hi + (double)a.lo; }
+
+// The Newton of ref_elem_newton_fast_lin in double-FP32 arithmetic: the same start value, monomial map, stopping
+// rule (||dxi||^2 <= RefMappingEps, taken in FP64 from the double-FP32 value), Armijo damping and plausibility
+// bound, each FP64 operation replaced by its double-FP32 counterpart (relative error ~1e-14 instead of ~1e-16), so
+// the iterates follow the FP64 ones to ~1e-13 in xi.  The map is scaled by the element's power-of-two size s_e
+// (exact): dxi and the Armijo ratios do not change, the initial |F| < epsMach test compares |F/s_e| s_e.
+__device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
+  const float2* Cg = M.tcoef_df + (size_t)e * 25;
+  DF c[8][3];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float2 v = __ldg(Cg + 3 * q + k);
+      c[q][k] = DF{v.x, v.y};
+    }
+  const float2 sc = __ldg(Cg + 24);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c[0][k] = df_add(c[0][k], df_neg(df_of(x[k] * (double)sc.y)));
+  auto residual = [&](const DF z[3], DF F[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const DF t = df_add(df_mul(z[1], df_fma(z[2], c[7][k], c[4][k])), df_fma(z[2], c[5][k], c[1][k]));
+      const DF u = df_fma(z[2], c[6][k], c[2][k]);
+      F[k] = df_fma(z[0], t, df_fma(z[1], u, df_fma(z[2], c[3][k], c[0][k])));
+    }
+  };
+  auto norm2 = [&](const DF v[3]) { return df_fma(v[0], v[0], df_fma(v[1], v[1], df_mul(v[2], v[2]))); };
+  DF z[3] = {df_of(xi[0]), df_of(xi[1]), df_of(xi[2])};
+  DF F[3];
+  residual(z, F);
+  const float eps = (float)kEpsMach;
+  double deltaXi2 = (fabsf(F[0].hi) * sc.x < eps && fabsf(F[1].hi) * sc.x < eps && fabsf(F[2].hi) * sc.x < eps) ? 0.0 : 1.0;
+  bool moved = false;
+  DF normF = norm2(F);
+  bool success = true;
+  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
+    const DF z12 = df_mul(z[0], z[1]), z13 = df_mul(z[0], z[2]), z23 = df_mul(z[1], z[2]);
+    DF J[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      J[k][0] = df_fma(z23, c[7][k], df_fma(z[2], c[5][k], df_fma(z[1], c[4][k], c[1][k])));
+      J[k][1] = df_fma(z13, c[7][k], df_fma(z[2], c[6][k], df_fma(z[0], c[4][k], c[2][k])));
+      J[k][2] = df_fma(z12, c[7][k], df_fma(z[1], c[6][k], df_fma(z[0], c[5][k], c[3][k])));
+    }
+    auto cof = [&](const DF& a, const DF& b, const DF& cc, const DF& d) { return df_add(df_mul(a, b), df_neg(df_mul(cc, d))); };
+    const DF c00 = cof(J[1][1], J[2][2], J[1][2], J[2][1]);
+    const DF c01 = cof(J[0][2], J[2][1], J[0][1], J[2][2]);
+    const DF c02 = cof(J[0][1], J[1][2], J[0][2], J[1][1]);
+    const DF c10 = cof(J[1][2], J[2][0], J[1][0], J[2][2]);
+    const DF c11 = cof(J[0][0], J[2][2], J[0][2], J[2][0]);
+    const DF c12 = cof(J[0][2], J[1][0], J[0][0], J[1][2]);
+    const DF c20 = cof(J[1][0], J[2][1], J[1][1], J[2][0]);
+    const DF c21 = cof(J[0][1], J[2][0], J[0][0], J[2][1]);
+    const DF c22 = cof(J[0][0], J[1][1], J[0][1], J[1][0]);
+    const DF det = df_fma(J[0][0], c00, df_fma(J[0][1], c10, df_mul(J[0][2], c20)));
+    const DF sd = det.hi > 0.f ? df_div(DF{1.f, 0.f}, det) : det;
+    DF dxi[3];
+    dxi[0] = df_mul(df_fma(c00, F[0], df_fma(c01, F[1], df_mul(c02, F[2]))), sd);
+    dxi[1] = df_mul(df_fma(c10, F[0], df_fma(c11, F[1], df_mul(c12, F[2]))), sd);
+    dxi[2] = df_mul(df_fma(c20, F[0], df_fma(c21, F[1], df_mul(c22, F[2]))), sd);
+    deltaXi2 = df_val(norm2(dxi));
+    const DF zo[3] = {z[0], z[1], z[2]};
+    const double normFold = df_val(normF);
+    double nF = normFold * 2.0;
+    double lambda = 1.0;
+    for (int iArmijo = 1; nF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
+      const DF lam = df_of(-lambda);
+      moved = true;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) z[dd] = df_fma(lam, dxi[dd], zo[dd]);
+      residual(z, F);
+      lambda = 0.2 * lambda;
+      normF = norm2(F);
+      nF = df_val(normF);
+    }
+    if (fabsf(z[0].hi) > 1.5f || fabsf(z[1].hi) > 1.5f || fabsf(z[2].hi) > 1.5f) { success = false; break; }
+  }
+  if (moved) { xi[0] = df_val(z[0]); xi[1] = df_val(z[1]); xi[2] = df_val(z[2]); }
+  return success;
+}
+
 static __device__ __noinline__ void lagrange_rt(double x, int np, const double* xgp, const double* wb, double* L) {
   bool hit = false;
   for (int i = 0; i < np; ++i) {
@@ -623,7 +747,7 @@ __device__ __forceinline__ bool ref_elem_newton_fast_curved(const DevMesh& M, in
 // the mixed variant's Newton: power forms (fused multiply-adds) of the trilinear or the curved map
 static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
   if (elem_curved(M, e)) return M.tcoef_ng ? ref_elem_newton_fast_curved(M, e, x, xi) : ref_elem_newton_ng(M, e, x, xi);
-  return ref_elem_newton_fast_lin(M, e, x, xi);
+  return M.tcoef_df ? ref_elem_newton_df_lin(M, e, x, xi) : ref_elem_newton_fast_lin(M, e, x, xi);
 }
 
 template <bool FAST>
