@@ -912,9 +912,6 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
         for (int q = 0; q < 8; ++q)
           for (int k = 0; k < 3; ++k) tc[(size_t)e * 24 + 3 * q + k] += 0.125 * w[q] * xcl[(size_t)e * 24 + 3 * t + k];
       }
-    double* d_tc = nullptr;
-    if ((rc = upload(c, &d_tc, tc))) return bail(rc);
-    c->M.tcoef = d_tc;
     // the same coefficients over s_e = 2^round(log2 max|c1..c3|) as double-FP32 pairs, then (s_e, 1/s_e)
     std::vector<float2> tdf((size_t)ne * 25);
     for (int e = 0; e < ne; ++e) {
@@ -966,9 +963,24 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
           }
           for (size_t q = 0; q < g3; ++q) pc[((size_t)e * g3 + q) * 3 + k] = A[q];
         }
-      double* d_pc = nullptr;
-      if ((rc = upload(c, &d_pc, pc))) return bail(rc);
-      c->M.tcoef_ng = d_pc;
+      // the same over s_e = 2^round(log2 max |first-order coefficient|) as double-FP32 pairs, then (s_e, 1/s_e)
+      std::vector<float2> pdf((size_t)ne * (g3 * 3 + 1));
+      for (int e = 0; e < ne; ++e) {
+        double mx = 0.0;
+        const size_t first[3] = {1, (size_t)g1, (size_t)g1 * g1};     // the xi1, xi2, xi3 terms
+        for (int a = 0; a < 3; ++a)
+          for (int k = 0; k < 3; ++k) mx = std::max(mx, std::fabs(pc[((size_t)e * g3 + first[a]) * 3 + k]));
+        const double sc = mx > 0.0 ? std::ldexp(1.0, (int)std::lround(std::log2(mx))) : 1.0;
+        for (size_t j = 0; j < g3 * 3; ++j) {
+          const double v = pc[(size_t)e * g3 * 3 + j] / sc;
+          const float hi = (float)v;
+          pdf[(size_t)e * (g3 * 3 + 1) + j] = make_float2(hi, (float)(v - (double)hi));
+        }
+        pdf[(size_t)e * (g3 * 3 + 1) + g3 * 3] = make_float2((float)sc, (float)(1.0 / sc));
+      }
+      float2* d_pdf = nullptr;
+      if ((rc = upload(c, &d_pdf, pdf))) return bail(rc);
+      c->M.tcoef_ng_df = d_pdf;
     }
   }
 

@@ -92,9 +92,7 @@ struct DevMesh {
   const double* bc_bz;
   // shape-function DOF coordinates: elem_xgp, or for a 1D/2D kernel its directions only (others zero)
   const double* sf_xgp;
-  // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
-  // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3, [ne][8][3] in that order (from the corners at pic_create)
-  const double* tcoef;
+
   // per-element polynomial degree (p-adaption): N_DG_Mapping(1,:) as 0-based DOF offsets [ne+1] and
   // N_DG_Mapping(2,:) [ne]; both null when every element has degree N (DOF offset e (N+1)^3)
   const int* dof_off;
@@ -104,13 +102,14 @@ struct DevMesh {
   const double* xcl_ng;
   const double* dxcl_ng;
   const int* curved;
-  // mixed variant on curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c,
-  // [ne][(NGeo+1)^3][3] in that index order
-  const double* tcoef_ng;
-  // mixed variant: tcoef / s_e as double-FP32 pairs (hi, lo) for the Newton in double-FP32 arithmetic, [ne][25]:
-  // 24 coefficients, then (s_e, 1/s_e) with s_e the power of two nearest the element's size (the scaled map is
-  // O(1), far from the FP32 range limits)
+  // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
+  // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3 (from the corners at pic_create), divided by s_e, the power of
+  // two nearest the element's size (exact; the scaled map is O(1), far from the FP32 range limits), as double-FP32
+  // pairs (hi, lo) for the Newton in double-FP32 arithmetic: [ne][25], 24 coefficients then (s_e, 1/s_e)
   const float2* tcoef_df;
+  // curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c, over s_e the same way,
+  // [ne][(NGeo+1)^3 3 + 1] in that index order, the last entry (s_e, 1/s_e)
+  const float2* tcoef_ng_df;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
   Consts k;
@@ -364,75 +363,6 @@ __device__ __forceinline__ bool ref_elem_newton_lin(const DevMesh& M, int e, con
   return success;
 }
 
-// FP64 Newton of the mixed variant: same start value, stopping rule (||dxi||^2 <= RefMappingEps,
-// 100 iterations), Armijo damping and plausibility bound as RefElemNewton, but with the NGeo = 1 map in
-// monomial form (DevMesh::tcoef): the residual in 18 and the Jacobian in 30 fused multiply-adds instead of
-// the tensor-product sums over 8 corners (about half the FP64 work per iteration), and one reciprocal of
-// det(J) per iteration.  The same map, so it converges to the same xi up to rounding.
-__device__ __forceinline__ bool ref_elem_newton_fast_lin(const DevMesh& M, int e, const double x[3], double xi[3]) {
-  const Consts& kc = M.k;
-  const double* Cg = M.tcoef + (size_t)e * 24;
-  double c[8][3];
-#pragma unroll
-  for (int q = 0; q < 8; ++q)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) c[q][k] = __ldg(Cg + 3 * q + k);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) c[0][k] = c[0][k] - x[k];     // the residual x(xi) - x is the polynomial itself
-  auto residual = [&](const double z[3], double F[3]) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double t = fma(z[1], fma(z[2], c[7][k], c[4][k]), fma(z[2], c[5][k], c[1][k]));
-      const double u = fma(z[2], c[6][k], c[2][k]);
-      F[k] = fma(z[0], t, fma(z[1], u, fma(z[2], c[3][k], c[0][k])));
-    }
-  };
-  double F[3];
-  residual(xi, F);
-  double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
-  double normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
-  bool success = true;
-  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
-    const double z12 = xi[0] * xi[1], z13 = xi[0] * xi[2], z23 = xi[1] * xi[2];
-    double J[3][3];                                      // J[nn][dd] = d x_nn / d xi_dd
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      J[k][0] = fma(z23, c[7][k], fma(xi[2], c[5][k], fma(xi[1], c[4][k], c[1][k])));
-      J[k][1] = fma(z13, c[7][k], fma(xi[2], c[6][k], fma(xi[0], c[4][k], c[2][k])));
-      J[k][2] = fma(z12, c[7][k], fma(xi[1], c[6][k], fma(xi[0], c[5][k], c[3][k])));
-    }
-    const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
-    const double c01 = fma(J[0][2], J[2][1], -J[0][1] * J[2][2]);
-    const double c02 = fma(J[0][1], J[1][2], -J[0][2] * J[1][1]);
-    const double c10 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
-    const double c11 = fma(J[0][0], J[2][2], -J[0][2] * J[2][0]);
-    const double c12 = fma(J[0][2], J[1][0], -J[0][0] * J[1][2]);
-    const double c20 = fma(J[1][0], J[2][1], -J[1][1] * J[2][0]);
-    const double c21 = fma(J[0][1], J[2][0], -J[0][0] * J[2][1]);
-    const double c22 = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
-    double det = fma(J[0][0], c00, fma(J[0][1], c10, J[0][2] * c20));
-    const double sd = det > 0.0 ? 1.0 / det : det;
-    double dxi[3];
-    dxi[0] = fma(c00, F[0], fma(c01, F[1], c02 * F[2])) * sd;
-    dxi[1] = fma(c10, F[0], fma(c11, F[1], c12 * F[2])) * sd;
-    dxi[2] = fma(c20, F[0], fma(c21, F[1], c22 * F[2])) * sd;
-    deltaXi2 = fma(dxi[0], dxi[0], fma(dxi[1], dxi[1], dxi[2] * dxi[2]));
-    const double xo[3] = {xi[0], xi[1], xi[2]};
-    const double normFold = normF;
-    normF = normF * 2.0;
-    double lambda = 1.0;
-    for (int iArmijo = 1; normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
-#pragma unroll
-      for (int dd = 0; dd < 3; ++dd) xi[dd] = fma(-lambda, dxi[dd], xo[dd]);
-      residual(xi, F);
-      lambda = 0.2 * lambda;
-      normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
-    }
-    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = false; break; }
-  }
-  return success;
-}
-
 // ---- double-FP32 ("double-float") arithmetic: a value is the unevaluated sum hi + lo of two floats, |lo| <= ulp(hi)/2,
 // about 48 significant bits.  Error-free transforms after Dekker (1971, "A floating-point technique for extending
 // the available precision") and Knuth (TwoSum, TAOCP vol. 2, 4.2.2), the product error from one fused multiply-add,
@@ -471,10 +401,11 @@ __device__ __forceinline__ DF df_of(double d) {
 }
 __device__ __forceinline__ double df_val(DF a) { return (double)a.hi + (double)a.lo; }
 
-// The Newton of ref_elem_newton_fast_lin in double-FP32 arithmetic: the same start value, monomial map, stopping
-// rule (||dxi||^2 <= RefMappingEps, taken in FP64 from the double-FP32 value), Armijo damping and plausibility
-// bound, each FP64 operation replaced by its double-FP32 counterpart (relative error ~1e-14 instead of ~1e-16), so
-// the iterates follow the FP64 ones to ~1e-13 in xi.  The map is scaled by the element's power-of-two size s_e
+// Newton of the mixed variant: the same start value, stopping rule (||dxi||^2 <= RefMappingEps, 100 iterations,
+// taken in FP64 from the double-FP32 value), Armijo damping and plausibility bound as RefElemNewton, but on the
+// NGeo = 1 map in monomial form (DevMesh::tcoef_df: the residual in 18 and the Jacobian in 30 multiply-adds instead
+// of the tensor-product sums over 8 corners, one reciprocal of det(J) per iteration) and in double-FP32 arithmetic
+// (relative error ~1e-14 instead of ~1e-16): the same map, so the iterates follow the FP64 ones to ~1e-13 in xi.  The map is scaled by the element's power-of-two size s_e
 // (exact): dxi and the Armijo ratios do not change, the initial |F| < epsMach test compares |F/s_e| s_e.
 __device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, const double x[3], double xi[3]) {
   const Consts& kc = M.k;
@@ -661,93 +592,110 @@ __device__ __forceinline__ bool position_in_ref_elem(const DevMesh& M, int e, co
   return ref_elem_newton(M, e, x, xi);
 }
 
-// Mixed variant, curved element: the Newton of ref_elem_newton_fast on the NGeo map in power form (nested
-// Horner with fused multiply-adds for x(xi) and its Jacobian, no divisions) instead of the barycentric Lagrange
-// sums over the (NGeo+1)^3 CL points; the same start value, stopping rule, Armijo damping and bound, the same map
-template <int NG>
-static __device__ __noinline__ bool ref_elem_newton_fast_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
-  const Consts& kc = M.k;
+// Mixed variant, curved element: the Newton of ref_elem_newton_df_lin on the NGeo map in power form (nested Horner
+// for x(xi) and its Jacobian, no divisions) instead of the barycentric Lagrange sums over the (NGeo+1)^3 CL points,
+// in double-FP32 arithmetic with the map scaled by the element's power-of-two size; the same start value, stopping
+// rule, Armijo damping and bound as RefElemNewton on the same map
+// x(z) - x (scaled) of the power form and, with WJ, its Jacobian J[nn][dd] = d x_nn / d xi_dd (nested Horner)
+template <int NG, bool WJ>
+static __device__ __noinline__ void df_eval_ng(const float2* __restrict__ Cg, const DF xs[3], const DF z[3], DF F[3],
+                                               DF (*J)[3]) {
   constexpr int n1 = NG + 1;
-  const double* Cg = M.tcoef_ng + (size_t)e * n1 * n1 * n1 * 3;
-  // x(z) - x and, with J, its derivatives (J[nn][dd] = d x_nn / d xi_dd)
-  auto eval = [&](const double z[3], double F[3], double (*J)[3]) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      double q = 0.0, q0 = 0.0, q1 = 0.0, q2 = 0.0;   // Horner in xi3 of the value and the three derivatives
+  auto ld = [&](int i) { const float2 v = __ldg(Cg + i); return DF{v.x, v.y}; };
 #pragma unroll 1
-      for (int c = NG; c >= 0; --c) {
-        double r = 0.0, r0 = 0.0, r1 = 0.0;           // Horner in xi2
+  for (int k = 0; k < 3; ++k) {
+    const DF zero{0.f, 0.f};
+    DF q = zero, q0 = zero, q1 = zero, q2 = zero;
 #pragma unroll 1
-        for (int b = NG; b >= 0; --b) {
-          const double* C = Cg + ((size_t)(c * n1 + b) * n1) * 3 + k;
-          double p = __ldg(C + 3 * NG), dp = 0.0;     // Horner in xi1 with its derivative
+    for (int c = NG; c >= 0; --c) {
+      DF r = zero, r0 = zero, r1 = zero;
+#pragma unroll 1
+      for (int b = NG; b >= 0; --b) {
+        const int base = ((c * n1 + b) * n1) * 3 + k;
+        DF p = ld(base + 3 * NG), dp = zero;
 #pragma unroll
-          for (int a = NG - 1; a >= 0; --a) {
-            if (J) dp = fma(dp, z[0], p);
-            p = fma(p, z[0], __ldg(C + 3 * a));
-          }
-          if (J) { r1 = fma(r1, z[1], r); r0 = fma(r0, z[1], dp); }
-          r = fma(r, z[1], p);
+        for (int a = NG - 1; a >= 0; --a) {
+          if (WJ) dp = df_fma(dp, z[0], p);
+          p = df_fma(p, z[0], ld(base + 3 * a));
         }
-        if (J) { q2 = fma(q2, z[2], q); q0 = fma(q0, z[2], r0); q1 = fma(q1, z[2], r1); }
-        q = fma(q, z[2], r);
+        if (WJ) { r1 = df_fma(r1, z[1], r); r0 = df_fma(r0, z[1], dp); }
+        r = df_fma(r, z[1], p);
       }
-      F[k] = q - x[k];
-      if (J) { J[k][0] = q0; J[k][1] = q1; J[k][2] = q2; }
+      if (WJ) { q2 = df_fma(q2, z[2], q); q0 = df_fma(q0, z[2], r0); q1 = df_fma(q1, z[2], r1); }
+      q = df_fma(q, z[2], r);
     }
-  };
-  double F[3];
-  eval(xi, F, nullptr);
-  double deltaXi2 = (fabs(F[0]) < kEpsMach && fabs(F[1]) < kEpsMach && fabs(F[2]) < kEpsMach) ? 0.0 : 1.0;
-  double normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
-  bool success = true;
-  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
-    double J[3][3], Fd[3];
-    eval(xi, Fd, J);
-    const double c00 = fma(J[1][1], J[2][2], -J[1][2] * J[2][1]);
-    const double c01 = fma(J[0][2], J[2][1], -J[0][1] * J[2][2]);
-    const double c02 = fma(J[0][1], J[1][2], -J[0][2] * J[1][1]);
-    const double c10 = fma(J[1][2], J[2][0], -J[1][0] * J[2][2]);
-    const double c11 = fma(J[0][0], J[2][2], -J[0][2] * J[2][0]);
-    const double c12 = fma(J[0][2], J[1][0], -J[0][0] * J[1][2]);
-    const double c20 = fma(J[1][0], J[2][1], -J[1][1] * J[2][0]);
-    const double c21 = fma(J[0][1], J[2][0], -J[0][0] * J[2][1]);
-    const double c22 = fma(J[0][0], J[1][1], -J[0][1] * J[1][0]);
-    const double det = fma(J[0][0], c00, fma(J[0][1], c10, J[0][2] * c20));
-    const double sd = det > 0.0 ? 1.0 / det : det;
-    double dxi[3];
-    dxi[0] = fma(c00, F[0], fma(c01, F[1], c02 * F[2])) * sd;
-    dxi[1] = fma(c10, F[0], fma(c11, F[1], c12 * F[2])) * sd;
-    dxi[2] = fma(c20, F[0], fma(c21, F[1], c22 * F[2])) * sd;
-    deltaXi2 = fma(dxi[0], dxi[0], fma(dxi[1], dxi[1], dxi[2] * dxi[2]));
-    const double xo[3] = {xi[0], xi[1], xi[2]};
-    const double normFold = normF;
-    normF = normF * 2.0;
-    double lambda = 1.0;
-    for (int iArmijo = 1; normF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
-#pragma unroll
-      for (int dd = 0; dd < 3; ++dd) xi[dd] = fma(-lambda, dxi[dd], xo[dd]);
-      eval(xi, F, nullptr);
-      lambda = 0.2 * lambda;
-      normF = fma(F[0], F[0], fma(F[1], F[1], F[2] * F[2]));
-    }
-    if (fabs(xi[0]) > 1.5 || fabs(xi[1]) > 1.5 || fabs(xi[2]) > 1.5) { success = false; break; }
+    F[k] = df_add(q, df_neg(xs[k]));
+    if (WJ) { J[k][0] = q0; J[k][1] = q1; J[k][2] = q2; }
   }
+}
+
+template <int NG>
+static __device__ __noinline__ bool ref_elem_newton_df_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  const Consts& kc = M.k;
+  constexpr int n1 = NG + 1, n3 = n1 * n1 * n1;
+  const float2* Cg = M.tcoef_ng_df + (size_t)e * (n3 * 3 + 1);
+  const float2 sc = __ldg(Cg + n3 * 3);
+  const DF xs[3] = {df_of(x[0] * (double)sc.y), df_of(x[1] * (double)sc.y), df_of(x[2] * (double)sc.y)};
+  auto norm2 = [&](const DF v[3]) { return df_fma(v[0], v[0], df_fma(v[1], v[1], df_mul(v[2], v[2]))); };
+  DF z[3] = {df_of(xi[0]), df_of(xi[1]), df_of(xi[2])};
+  DF F[3];
+  df_eval_ng<NG, false>(Cg, xs, z, F, nullptr);
+  const float eps = (float)kEpsMach;
+  double deltaXi2 = (fabsf(F[0].hi) * sc.x < eps && fabsf(F[1].hi) * sc.x < eps && fabsf(F[2].hi) * sc.x < eps) ? 0.0 : 1.0;
+  DF normF = norm2(F);
+  bool success = true, moved = false;
+  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
+    DF J[3][3], Fd[3];
+    df_eval_ng<NG, true>(Cg, xs, z, Fd, J);
+    auto cof = [&](const DF& a, const DF& b, const DF& cc, const DF& d) { return df_add(df_mul(a, b), df_neg(df_mul(cc, d))); };
+    const DF c00 = cof(J[1][1], J[2][2], J[1][2], J[2][1]);
+    const DF c01 = cof(J[0][2], J[2][1], J[0][1], J[2][2]);
+    const DF c02 = cof(J[0][1], J[1][2], J[0][2], J[1][1]);
+    const DF c10 = cof(J[1][2], J[2][0], J[1][0], J[2][2]);
+    const DF c11 = cof(J[0][0], J[2][2], J[0][2], J[2][0]);
+    const DF c12 = cof(J[0][2], J[1][0], J[0][0], J[1][2]);
+    const DF c20 = cof(J[1][0], J[2][1], J[1][1], J[2][0]);
+    const DF c21 = cof(J[0][1], J[2][0], J[0][0], J[2][1]);
+    const DF c22 = cof(J[0][0], J[1][1], J[0][1], J[1][0]);
+    const DF det = df_fma(J[0][0], c00, df_fma(J[0][1], c10, df_mul(J[0][2], c20)));
+    const DF sd = det.hi > 0.f ? df_div(DF{1.f, 0.f}, det) : det;
+    DF dxi[3];
+    dxi[0] = df_mul(df_fma(c00, F[0], df_fma(c01, F[1], df_mul(c02, F[2]))), sd);
+    dxi[1] = df_mul(df_fma(c10, F[0], df_fma(c11, F[1], df_mul(c12, F[2]))), sd);
+    dxi[2] = df_mul(df_fma(c20, F[0], df_fma(c21, F[1], df_mul(c22, F[2]))), sd);
+    deltaXi2 = df_val(norm2(dxi));
+    const DF zo[3] = {z[0], z[1], z[2]};
+    const double normFold = df_val(normF);
+    double nF = normFold * 2.0;
+    double lambda = 1.0;
+    for (int iArmijo = 1; nF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
+      const DF lam = df_of(-lambda);
+      moved = true;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) z[dd] = df_fma(lam, dxi[dd], zo[dd]);
+      df_eval_ng<NG, false>(Cg, xs, z, F, nullptr);
+      lambda = 0.2 * lambda;
+      normF = norm2(F);
+      nF = df_val(normF);
+    }
+    if (fabsf(z[0].hi) > 1.5f || fabsf(z[1].hi) > 1.5f || fabsf(z[2].hi) > 1.5f) { success = false; break; }
+  }
+  if (moved) { xi[0] = df_val(z[0]); xi[1] = df_val(z[1]); xi[2] = df_val(z[2]); }
   return success;
 }
 
 __device__ __forceinline__ bool ref_elem_newton_fast_curved(const DevMesh& M, int e, const double x[3], double xi[3]) {
   switch (M.k.ngeo) {
-    case 2: return ref_elem_newton_fast_ng<2>(M, e, x, xi);
-    case 3: return ref_elem_newton_fast_ng<3>(M, e, x, xi);
-    default: return ref_elem_newton_fast_ng<4>(M, e, x, xi);
+    case 2: return ref_elem_newton_df_ng<2>(M, e, x, xi);
+    case 3: return ref_elem_newton_df_ng<3>(M, e, x, xi);
+    default: return ref_elem_newton_df_ng<4>(M, e, x, xi);
   }
 }
 
 // the mixed variant's Newton: power forms (fused multiply-adds) of the trilinear or the curved map
 static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
-  if (elem_curved(M, e)) return M.tcoef_ng ? ref_elem_newton_fast_curved(M, e, x, xi) : ref_elem_newton_ng(M, e, x, xi);
-  return M.tcoef_df ? ref_elem_newton_df_lin(M, e, x, xi) : ref_elem_newton_fast_lin(M, e, x, xi);
+  if (elem_curved(M, e)) return M.tcoef_ng_df ? ref_elem_newton_fast_curved(M, e, x, xi) : ref_elem_newton_ng(M, e, x, xi);
+  return M.tcoef_df ? ref_elem_newton_df_lin(M, e, x, xi) : ref_elem_newton_lin(M, e, x, xi);
 }
 
 template <bool FAST>
