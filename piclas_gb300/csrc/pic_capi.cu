@@ -912,19 +912,23 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
         for (int q = 0; q < 8; ++q)
           for (int k = 0; k < 3; ++k) tc[(size_t)e * 24 + 3 * q + k] += 0.125 * w[q] * xcl[(size_t)e * 24 + 3 * t + k];
       }
-    // the same coefficients over s_e = 2^round(log2 max|c1..c3|) as double-FP32 pairs, then (s_e, 1/s_e)
-    std::vector<float2> tdf((size_t)ne * 25);
+    // the same coefficients over s_e = 2^round(log2 max|c1..c3|) as double-FP32 pairs, then (s_e, 1/s_e) and the
+    // start-value data of RefMappingGuess 1 in the same units (bary / s_e, XiEtaZetaBasis, slen s_e)
+    auto pair = [](double v) { const float hi = (float)v; return make_float2(hi, (float)(v - (double)hi)); };
+    auto start_data = [&](int e, double sc, float2* out) {
+      for (int d = 0; d < 3; ++d) out[d] = pair(bary[(size_t)e * 3 + d] / sc);
+      for (int d = 0; d < 18; ++d) out[3 + d] = pair(xez[(size_t)e * 18 + d]);
+      for (int d = 0; d < 6; ++d) out[21 + d] = pair(slen[(size_t)e * 6 + d] * sc);
+    };
+    std::vector<float2> tdf((size_t)ne * pic::kDfLin);
     for (int e = 0; e < ne; ++e) {
       double mx = 0.0;
       for (int q = 1; q <= 3; ++q)
         for (int k = 0; k < 3; ++k) mx = std::max(mx, std::fabs(tc[(size_t)e * 24 + 3 * q + k]));
       const double sc = mx > 0.0 ? std::ldexp(1.0, (int)std::lround(std::log2(mx))) : 1.0;
-      for (int j = 0; j < 24; ++j) {
-        const double v = tc[(size_t)e * 24 + j] / sc;
-        const float hi = (float)v;
-        tdf[(size_t)e * 25 + j] = make_float2(hi, (float)(v - (double)hi));
-      }
-      tdf[(size_t)e * 25 + 24] = make_float2((float)sc, (float)(1.0 / sc));
+      for (int j = 0; j < 24; ++j) tdf[(size_t)e * pic::kDfLin + j] = pair(tc[(size_t)e * 24 + j] / sc);
+      tdf[(size_t)e * pic::kDfLin + 24] = make_float2((float)sc, (float)(1.0 / sc));
+      start_data(e, sc, &tdf[(size_t)e * pic::kDfLin + 25]);
     }
     float2* d_tdf = nullptr;
     if ((rc = upload(c, &d_tdf, tdf))) return bail(rc);
@@ -964,19 +968,17 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
           for (size_t q = 0; q < g3; ++q) pc[((size_t)e * g3 + q) * 3 + k] = A[q];
         }
       // the same over s_e = 2^round(log2 max |first-order coefficient|) as double-FP32 pairs, then (s_e, 1/s_e)
-      std::vector<float2> pdf((size_t)ne * (g3 * 3 + 1));
+      const size_t nb = g3 * 3 + 1 + pic::kDfStart;
+      std::vector<float2> pdf((size_t)ne * nb);
       for (int e = 0; e < ne; ++e) {
         double mx = 0.0;
         const size_t first[3] = {1, (size_t)g1, (size_t)g1 * g1};     // the xi1, xi2, xi3 terms
         for (int a = 0; a < 3; ++a)
           for (int k = 0; k < 3; ++k) mx = std::max(mx, std::fabs(pc[((size_t)e * g3 + first[a]) * 3 + k]));
         const double sc = mx > 0.0 ? std::ldexp(1.0, (int)std::lround(std::log2(mx))) : 1.0;
-        for (size_t j = 0; j < g3 * 3; ++j) {
-          const double v = pc[(size_t)e * g3 * 3 + j] / sc;
-          const float hi = (float)v;
-          pdf[(size_t)e * (g3 * 3 + 1) + j] = make_float2(hi, (float)(v - (double)hi));
-        }
-        pdf[(size_t)e * (g3 * 3 + 1) + g3 * 3] = make_float2((float)sc, (float)(1.0 / sc));
+        for (size_t j = 0; j < g3 * 3; ++j) pdf[(size_t)e * nb + j] = pair(pc[(size_t)e * g3 * 3 + j] / sc);
+        pdf[(size_t)e * nb + g3 * 3] = make_float2((float)sc, (float)(1.0 / sc));
+        start_data(e, sc, &pdf[(size_t)e * nb + g3 * 3 + 1]);
       }
       float2* d_pdf = nullptr;
       if ((rc = upload(c, &d_pdf, pdf))) return bail(rc);
@@ -1019,6 +1021,18 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
   }
   k.ngeo = ng;
   if (ng > 1) bezier_basis(ng, k.bz);
+  {
+    // the mixed Newton's constants in double-FP32: RefMappingEps, 1 + RefMappingEps, -lambda_k and 1 - 1e-4 lambda_k
+    auto pair = [](double v) { const float hi = (float)v; return make_float2(hi, (float)(v - (double)hi)); };
+    k.df_eps = pair(k.refmapping_eps);
+    k.df_one_eps = pair(1.0 + k.refmapping_eps);
+    double lambda = 1.0;
+    for (int j = 0; j < 9; ++j) {
+      k.df_lam[j] = pair(-lambda);
+      k.df_arm[j] = pair(1.0 - 0.0001 * lambda);
+      lambda = 0.2 * lambda;
+    }
+  }
   for (int i = 0; i <= ng; ++i) { k.xi_cl_ng[i] = m->xi_cl_ngeo[i]; k.wbary_cl_ng[i] = m->wbary_cl_ngeo[i]; }
   if (ng == 1) {
     k.xi_cl[0] = m->xi_cl_ngeo[0]; k.xi_cl[1] = m->xi_cl_ngeo[1];

@@ -59,6 +59,9 @@ struct Consts {
   int ngeo;                                    // NGeo (curved elements when > 1)
   double xi_cl_ng[kMaxNGeo + 1], wbary_cl_ng[kMaxNGeo + 1];   // XiCL_NGeo, wBaryCL_NGeo (xi_cl: of NGeo = 1)
   BzBasis bz;                                  // curved wall sides (NGeo > 1)
+  // mixed Newton in double-FP32 arithmetic: RefMappingEps, 1 + RefMappingEps, and per Armijo step k (lambda_k =
+  // 0.2^k in FP64) -lambda_k and 1 - 1e-4 lambda_k, each as a (hi, lo) pair
+  float2 df_eps, df_one_eps, df_lam[9], df_arm[9];
   // N_Inter(k)%xGP, %wBary and CellVolWeight(k)%Fac for every degree k (row k; rows up to NMax are set), FP64
   // and FP32: the kernels of degree k read row k, so elements of different degrees (p-adaption) share them
   double xgp_n[kMaxN + 1][kMaxN + 1], wbary_n[kMaxN + 1][kMaxN + 1], fac_n[kMaxN + 1][kMaxN + 1];
@@ -105,10 +108,12 @@ struct DevMesh {
   // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
   // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3 (from the corners at pic_create), divided by s_e, the power of
   // two nearest the element's size (exact; the scaled map is O(1), far from the FP32 range limits), as double-FP32
-  // pairs (hi, lo) for the Newton in double-FP32 arithmetic: [ne][25], 24 coefficients then (s_e, 1/s_e)
+  // pairs (hi, lo) for the Newton in double-FP32 arithmetic: [ne][kDfLin], 24 coefficients, (s_e, 1/s_e), then the
+  // start-value data of RefMappingGuess 1 in the same units: ElemBaryNGeo / s_e (3), XiEtaZetaBasis (18),
+  // slenXiEtaZetaBasis s_e (6)
   const float2* tcoef_df;
   // curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c, over s_e the same way,
-  // [ne][(NGeo+1)^3 3 + 1] in that index order, the last entry (s_e, 1/s_e)
+  // [ne][(NGeo+1)^3 3 + 1 + 27] in that index order, then (s_e, 1/s_e) and the start-value data
   const float2* tcoef_ng_df;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
@@ -119,6 +124,7 @@ struct DevMesh {
 // (0 PLANAR_RECT, 1 PLANAR_NONRECT, 2 BILINEAR, 3 PLANAR_CURVED, 4 CURVED), BaseVectors3 [16..18], the corners P00, P10, P01, P11
 // [19..30], periodic sides: 16 (neighbour element, 0-based) + (BoundaryType(BC_ALPHA) + 8) [31]
 constexpr int kBcGeo = 32;
+constexpr int kDfStart = 27, kDfLin = 25 + kDfStart;   // double-FP32 start-value data; trilinear block size
 constexpr int kBcCap = 64;   // wall sides traced per trajectory (entries within reach beyond it are not)
 
 // ---- particles (SoA) ---------------------------------------------------------------------
@@ -400,6 +406,34 @@ __device__ __forceinline__ DF df_of(double d) {
   return DF{h, __double2float_rn(d - (double)h)};
 }
 __device__ __forceinline__ double df_val(DF a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ DF df_ld(const float2* __restrict__ p) { const float2 v = __ldg(p); return DF{v.x, v.y}; }
+__device__ __forceinline__ DF df_c(float2 v) { return DF{v.x, v.y}; }
+// a > b for normalised pairs
+__device__ __forceinline__ bool df_gt(DF a, DF b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+__device__ __forceinline__ DF df_abs(DF a) { return a.hi < 0.f ? df_neg(a) : a; }
+
+// GetRefNewtonStartValue, RefMappingGuess 1 (eval_xyz.f90:498-535) in double-FP32 arithmetic on the scaled
+// data S (bary / s_e, XiEtaZetaBasis, slen s_e) and the scaled position xs
+__device__ __forceinline__ void df_start(const Consts& kc, const float2* __restrict__ S, const DF xs[3], DF z[3]) {
+  const DF P[3] = {df_add(xs[0], df_neg(df_ld(S))), df_add(xs[1], df_neg(df_ld(S + 1))), df_add(xs[2], df_neg(df_ld(S + 2)))};
+  DF xil[6];
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    const DF dp = df_add(df_add(df_mul(P[0], df_ld(S + 3 + 3 * d)), df_mul(P[1], df_ld(S + 4 + 3 * d))),
+                         df_mul(P[2], df_ld(S + 5 + 3 * d)));
+    xil[d] = df_mul(dp, df_ld(S + 21 + d));
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) z[d] = df_mul(DF{0.5f, 0.f}, df_add(xil[d], df_neg(xil[d + 3])));
+  const DF one_eps = df_c(kc.df_one_eps);
+  if (df_gt(df_abs(z[0]), one_eps) || df_gt(df_abs(z[1]), one_eps) || df_gt(df_abs(z[2]), one_eps)) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (df_gt(z[d], DF{1.f, 0.f})) z[d] = DF{1.f, 0.f};
+      if (df_gt(DF{-1.f, 0.f}, z[d])) z[d] = DF{-1.f, 0.f};
+    }
+  }
+}
 
 // Newton of the mixed variant: the same start value, stopping rule (||dxi||^2 <= RefMappingEps, 100 iterations,
 // taken in FP64 from the double-FP32 value), Armijo damping and plausibility bound as RefElemNewton, but on the
@@ -407,20 +441,65 @@ __device__ __forceinline__ double df_val(DF a) { return (double)a.hi + (double)a
 // of the tensor-product sums over 8 corners, one reciprocal of det(J) per iteration) and in double-FP32 arithmetic
 // (relative error ~1e-14 instead of ~1e-16): the same map, so the iterates follow the FP64 ones to ~1e-13 in xi.  The map is scaled by the element's power-of-two size s_e
 // (exact): dxi and the Armijo ratios do not change, the initial |F| < epsMach test compares |F/s_e| s_e.
-__device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, const double x[3], double xi[3]) {
+// one Newton iteration's common tail in double-FP32 arithmetic: dxi = J^-1 F from the cofactors, ||dxi||^2, and
+// the Armijo line search on F; EVAL(z, F) evaluates the residual.  Returns false when |xi| left 1.5.
+template <class EVAL>
+__device__ __forceinline__ bool df_newton_step(const Consts& kc, const DF (*J)[3], DF z[3], DF F[3], DF& normF,
+                                               DF& deltaXi2, bool& moved, EVAL&& eval) {
+  auto norm2 = [&](const DF v[3]) { return df_fma(v[0], v[0], df_fma(v[1], v[1], df_mul(v[2], v[2]))); };
+  auto cof = [&](const DF& a, const DF& b, const DF& cc, const DF& d) { return df_add(df_mul(a, b), df_neg(df_mul(cc, d))); };
+  const DF c00 = cof(J[1][1], J[2][2], J[1][2], J[2][1]);
+  const DF c01 = cof(J[0][2], J[2][1], J[0][1], J[2][2]);
+  const DF c02 = cof(J[0][1], J[1][2], J[0][2], J[1][1]);
+  const DF c10 = cof(J[1][2], J[2][0], J[1][0], J[2][2]);
+  const DF c11 = cof(J[0][0], J[2][2], J[0][2], J[2][0]);
+  const DF c12 = cof(J[0][2], J[1][0], J[0][0], J[1][2]);
+  const DF c20 = cof(J[1][0], J[2][1], J[1][1], J[2][0]);
+  const DF c21 = cof(J[0][1], J[2][0], J[0][0], J[2][1]);
+  const DF c22 = cof(J[0][0], J[1][1], J[0][1], J[1][0]);
+  const DF det = df_fma(J[0][0], c00, df_fma(J[0][1], c10, df_mul(J[0][2], c20)));
+  const DF sd = det.hi > 0.f ? df_div(DF{1.f, 0.f}, det) : det;
+  DF dxi[3];
+  dxi[0] = df_mul(df_fma(c00, F[0], df_fma(c01, F[1], df_mul(c02, F[2]))), sd);
+  dxi[1] = df_mul(df_fma(c10, F[0], df_fma(c11, F[1], df_mul(c12, F[2]))), sd);
+  dxi[2] = df_mul(df_fma(c20, F[0], df_fma(c21, F[1], df_mul(c22, F[2]))), sd);
+  deltaXi2 = norm2(dxi);
+  const DF zo[3] = {z[0], z[1], z[2]};
+  const DF normFold = normF;
+  // Armijo: the first trial always runs unless ||F||^2 = 0 (2 ||F||^2 > (1 - 1e-4) ||F||^2); lambda_k = 0.2^k
+  bool go = normFold.hi > 0.f;
+  for (int k = 0; go && k < 8; ++k) {
+    moved = true;
+    const DF lam = df_c(kc.df_lam[k]);
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) z[dd] = df_fma(lam, dxi[dd], zo[dd]);
+    eval(z, F);
+    normF = norm2(F);
+    go = df_gt(normF, df_mul(normFold, df_c(kc.df_arm[k + 1])));
+  }
+  return !(fabsf(z[0].hi) > 1.5f || fabsf(z[1].hi) > 1.5f || fabsf(z[2].hi) > 1.5f);
+}
+
+// Newton of the mixed variant: the same start value, stopping rule (||dxi||^2 <= RefMappingEps, 100 iterations),
+// Armijo damping and plausibility bound as RefElemNewton, but on the NGeo = 1 map in monomial form
+// (DevMesh::tcoef_df: the residual in 18 and the Jacobian in 30 multiply-adds instead of the tensor-product sums
+// over 8 corners, one reciprocal of det(J) per iteration) and in double-FP32 arithmetic (relative error ~1e-14
+// instead of ~1e-16), the start value of RefMappingGuess 1 too (start): the same map, so the iterates follow the
+// FP64 ones to ~1e-13 in xi.  The map is scaled by the element's power-of-two size s_e (exact): dxi and the
+// Armijo ratios do not change, the initial |F| < epsMach test compares |F/s_e| s_e.
+__device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, const double x[3], double xi[3],
+                                                       bool start) {
   const Consts& kc = M.k;
-  const float2* Cg = M.tcoef_df + (size_t)e * 25;
+  const float2* Cg = M.tcoef_df + (size_t)e * kDfLin;
   DF c[8][3];
 #pragma unroll
   for (int q = 0; q < 8; ++q)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float2 v = __ldg(Cg + 3 * q + k);
-      c[q][k] = DF{v.x, v.y};
-    }
+    for (int k = 0; k < 3; ++k) c[q][k] = df_ld(Cg + 3 * q + k);
   const float2 sc = __ldg(Cg + 24);
+  const DF xs[3] = {df_of(x[0] * (double)sc.y), df_of(x[1] * (double)sc.y), df_of(x[2] * (double)sc.y)};
 #pragma unroll
-  for (int k = 0; k < 3; ++k) c[0][k] = df_add(c[0][k], df_neg(df_of(x[k] * (double)sc.y)));
+  for (int k = 0; k < 3; ++k) c[0][k] = df_add(c[0][k], df_neg(xs[k]));
   auto residual = [&](const DF z[3], DF F[3]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -429,16 +508,18 @@ __device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, 
       F[k] = df_fma(z[0], t, df_fma(z[1], u, df_fma(z[2], c[3][k], c[0][k])));
     }
   };
-  auto norm2 = [&](const DF v[3]) { return df_fma(v[0], v[0], df_fma(v[1], v[1], df_mul(v[2], v[2]))); };
-  DF z[3] = {df_of(xi[0]), df_of(xi[1]), df_of(xi[2])};
+  DF z[3];
+  if (start) df_start(kc, Cg + 25, xs, z);
+  else { z[0] = df_of(xi[0]); z[1] = df_of(xi[1]); z[2] = df_of(xi[2]); }
   DF F[3];
   residual(z, F);
   const float eps = (float)kEpsMach;
-  double deltaXi2 = (fabsf(F[0].hi) * sc.x < eps && fabsf(F[1].hi) * sc.x < eps && fabsf(F[2].hi) * sc.x < eps) ? 0.0 : 1.0;
-  bool moved = false;
-  DF normF = norm2(F);
+  bool moved = start;
+  bool more = !(fabsf(F[0].hi) * sc.x < eps && fabsf(F[1].hi) * sc.x < eps && fabsf(F[2].hi) * sc.x < eps);
+  DF normF = df_fma(F[0], F[0], df_fma(F[1], F[1], df_mul(F[2], F[2])));
   bool success = true;
-  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
+  const DF eps_map = df_c(kc.df_eps);
+  for (int iter = 0; iter < 100 && more; ++iter) {
     const DF z12 = df_mul(z[0], z[1]), z13 = df_mul(z[0], z[2]), z23 = df_mul(z[1], z[2]);
     DF J[3][3];
 #pragma unroll
@@ -447,38 +528,9 @@ __device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, 
       J[k][1] = df_fma(z13, c[7][k], df_fma(z[2], c[6][k], df_fma(z[0], c[4][k], c[2][k])));
       J[k][2] = df_fma(z12, c[7][k], df_fma(z[1], c[6][k], df_fma(z[0], c[5][k], c[3][k])));
     }
-    auto cof = [&](const DF& a, const DF& b, const DF& cc, const DF& d) { return df_add(df_mul(a, b), df_neg(df_mul(cc, d))); };
-    const DF c00 = cof(J[1][1], J[2][2], J[1][2], J[2][1]);
-    const DF c01 = cof(J[0][2], J[2][1], J[0][1], J[2][2]);
-    const DF c02 = cof(J[0][1], J[1][2], J[0][2], J[1][1]);
-    const DF c10 = cof(J[1][2], J[2][0], J[1][0], J[2][2]);
-    const DF c11 = cof(J[0][0], J[2][2], J[0][2], J[2][0]);
-    const DF c12 = cof(J[0][2], J[1][0], J[0][0], J[1][2]);
-    const DF c20 = cof(J[1][0], J[2][1], J[1][1], J[2][0]);
-    const DF c21 = cof(J[0][1], J[2][0], J[0][0], J[2][1]);
-    const DF c22 = cof(J[0][0], J[1][1], J[0][1], J[1][0]);
-    const DF det = df_fma(J[0][0], c00, df_fma(J[0][1], c10, df_mul(J[0][2], c20)));
-    const DF sd = det.hi > 0.f ? df_div(DF{1.f, 0.f}, det) : det;
-    DF dxi[3];
-    dxi[0] = df_mul(df_fma(c00, F[0], df_fma(c01, F[1], df_mul(c02, F[2]))), sd);
-    dxi[1] = df_mul(df_fma(c10, F[0], df_fma(c11, F[1], df_mul(c12, F[2]))), sd);
-    dxi[2] = df_mul(df_fma(c20, F[0], df_fma(c21, F[1], df_mul(c22, F[2]))), sd);
-    deltaXi2 = df_val(norm2(dxi));
-    const DF zo[3] = {z[0], z[1], z[2]};
-    const double normFold = df_val(normF);
-    double nF = normFold * 2.0;
-    double lambda = 1.0;
-    for (int iArmijo = 1; nF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
-      const DF lam = df_of(-lambda);
-      moved = true;
-#pragma unroll
-      for (int dd = 0; dd < 3; ++dd) z[dd] = df_fma(lam, dxi[dd], zo[dd]);
-      residual(z, F);
-      lambda = 0.2 * lambda;
-      normF = norm2(F);
-      nF = df_val(normF);
-    }
-    if (fabsf(z[0].hi) > 1.5f || fabsf(z[1].hi) > 1.5f || fabsf(z[2].hi) > 1.5f) { success = false; break; }
+    DF d2;
+    if (!df_newton_step(kc, J, z, F, normF, d2, moved, residual)) { success = false; break; }
+    more = df_gt(d2, eps_map);
   }
   if (moved) { xi[0] = df_val(z[0]); xi[1] = df_val(z[1]); xi[2] = df_val(z[2]); }
   return success;
@@ -630,78 +682,64 @@ static __device__ __noinline__ void df_eval_ng(const float2* __restrict__ Cg, co
 }
 
 template <int NG>
-static __device__ __noinline__ bool ref_elem_newton_df_ng(const DevMesh& M, int e, const double x[3], double xi[3]) {
+static __device__ __noinline__ bool ref_elem_newton_df_ng(const DevMesh& M, int e, const double x[3], double xi[3],
+                                                          bool start) {
   const Consts& kc = M.k;
   constexpr int n1 = NG + 1, n3 = n1 * n1 * n1;
-  const float2* Cg = M.tcoef_ng_df + (size_t)e * (n3 * 3 + 1);
+  const float2* Cg = M.tcoef_ng_df + (size_t)e * (n3 * 3 + 1 + kDfStart);
   const float2 sc = __ldg(Cg + n3 * 3);
   const DF xs[3] = {df_of(x[0] * (double)sc.y), df_of(x[1] * (double)sc.y), df_of(x[2] * (double)sc.y)};
-  auto norm2 = [&](const DF v[3]) { return df_fma(v[0], v[0], df_fma(v[1], v[1], df_mul(v[2], v[2]))); };
-  DF z[3] = {df_of(xi[0]), df_of(xi[1]), df_of(xi[2])};
+  DF z[3];
+  if (start) df_start(kc, Cg + n3 * 3 + 1, xs, z);
+  else { z[0] = df_of(xi[0]); z[1] = df_of(xi[1]); z[2] = df_of(xi[2]); }
+  auto residual = [&](const DF zz[3], DF F[3]) { df_eval_ng<NG, false>(Cg, xs, zz, F, nullptr); };
   DF F[3];
-  df_eval_ng<NG, false>(Cg, xs, z, F, nullptr);
+  residual(z, F);
   const float eps = (float)kEpsMach;
-  double deltaXi2 = (fabsf(F[0].hi) * sc.x < eps && fabsf(F[1].hi) * sc.x < eps && fabsf(F[2].hi) * sc.x < eps) ? 0.0 : 1.0;
-  DF normF = norm2(F);
-  bool success = true, moved = false;
-  for (int iter = 0; iter < 100 && deltaXi2 > kc.refmapping_eps; ++iter) {
+  bool moved = start;
+  bool more = !(fabsf(F[0].hi) * sc.x < eps && fabsf(F[1].hi) * sc.x < eps && fabsf(F[2].hi) * sc.x < eps);
+  DF normF = df_fma(F[0], F[0], df_fma(F[1], F[1], df_mul(F[2], F[2])));
+  bool success = true;
+  const DF eps_map = df_c(kc.df_eps);
+  for (int iter = 0; iter < 100 && more; ++iter) {
     DF J[3][3], Fd[3];
     df_eval_ng<NG, true>(Cg, xs, z, Fd, J);
-    auto cof = [&](const DF& a, const DF& b, const DF& cc, const DF& d) { return df_add(df_mul(a, b), df_neg(df_mul(cc, d))); };
-    const DF c00 = cof(J[1][1], J[2][2], J[1][2], J[2][1]);
-    const DF c01 = cof(J[0][2], J[2][1], J[0][1], J[2][2]);
-    const DF c02 = cof(J[0][1], J[1][2], J[0][2], J[1][1]);
-    const DF c10 = cof(J[1][2], J[2][0], J[1][0], J[2][2]);
-    const DF c11 = cof(J[0][0], J[2][2], J[0][2], J[2][0]);
-    const DF c12 = cof(J[0][2], J[1][0], J[0][0], J[1][2]);
-    const DF c20 = cof(J[1][0], J[2][1], J[1][1], J[2][0]);
-    const DF c21 = cof(J[0][1], J[2][0], J[0][0], J[2][1]);
-    const DF c22 = cof(J[0][0], J[1][1], J[0][1], J[1][0]);
-    const DF det = df_fma(J[0][0], c00, df_fma(J[0][1], c10, df_mul(J[0][2], c20)));
-    const DF sd = det.hi > 0.f ? df_div(DF{1.f, 0.f}, det) : det;
-    DF dxi[3];
-    dxi[0] = df_mul(df_fma(c00, F[0], df_fma(c01, F[1], df_mul(c02, F[2]))), sd);
-    dxi[1] = df_mul(df_fma(c10, F[0], df_fma(c11, F[1], df_mul(c12, F[2]))), sd);
-    dxi[2] = df_mul(df_fma(c20, F[0], df_fma(c21, F[1], df_mul(c22, F[2]))), sd);
-    deltaXi2 = df_val(norm2(dxi));
-    const DF zo[3] = {z[0], z[1], z[2]};
-    const double normFold = df_val(normF);
-    double nF = normFold * 2.0;
-    double lambda = 1.0;
-    for (int iArmijo = 1; nF > normFold * (1.0 - 0.0001 * lambda) && iArmijo <= 8; ++iArmijo) {
-      const DF lam = df_of(-lambda);
-      moved = true;
-#pragma unroll
-      for (int dd = 0; dd < 3; ++dd) z[dd] = df_fma(lam, dxi[dd], zo[dd]);
-      df_eval_ng<NG, false>(Cg, xs, z, F, nullptr);
-      lambda = 0.2 * lambda;
-      normF = norm2(F);
-      nF = df_val(normF);
-    }
-    if (fabsf(z[0].hi) > 1.5f || fabsf(z[1].hi) > 1.5f || fabsf(z[2].hi) > 1.5f) { success = false; break; }
+    DF d2;
+    if (!df_newton_step(kc, J, z, F, normF, d2, moved, residual)) { success = false; break; }
+    more = df_gt(d2, eps_map);
   }
   if (moved) { xi[0] = df_val(z[0]); xi[1] = df_val(z[1]); xi[2] = df_val(z[2]); }
   return success;
 }
 
-__device__ __forceinline__ bool ref_elem_newton_fast_curved(const DevMesh& M, int e, const double x[3], double xi[3]) {
+__device__ __forceinline__ bool ref_elem_newton_fast_curved(const DevMesh& M, int e, const double x[3], double xi[3],
+                                                            bool start) {
   switch (M.k.ngeo) {
-    case 2: return ref_elem_newton_df_ng<2>(M, e, x, xi);
-    case 3: return ref_elem_newton_df_ng<3>(M, e, x, xi);
-    default: return ref_elem_newton_df_ng<4>(M, e, x, xi);
+    case 2: return ref_elem_newton_df_ng<2>(M, e, x, xi, start);
+    case 3: return ref_elem_newton_df_ng<3>(M, e, x, xi, start);
+    default: return ref_elem_newton_df_ng<4>(M, e, x, xi, start);
   }
 }
 
-// the mixed variant's Newton: power forms (fused multiply-adds) of the trilinear or the curved map
-static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3]) {
-  if (elem_curved(M, e)) return M.tcoef_ng_df ? ref_elem_newton_fast_curved(M, e, x, xi) : ref_elem_newton_ng(M, e, x, xi);
-  return M.tcoef_df ? ref_elem_newton_df_lin(M, e, x, xi) : ref_elem_newton_lin(M, e, x, xi);
+// the mixed variant's Newton: power forms of the trilinear or the curved map in double-FP32 arithmetic; with start
+// it takes RefMappingGuess 1 itself (in double-FP32), else xi holds the start value
+static __device__ __noinline__ bool ref_elem_newton_fast(const DevMesh& M, int e, const double x[3], double xi[3],
+                                                        bool start) {
+  if (elem_curved(M, e)) {
+    if (M.tcoef_ng_df) return ref_elem_newton_fast_curved(M, e, x, xi, start);
+    if (start) newton_start(M, e, x, xi);
+    return ref_elem_newton_ng(M, e, x, xi);
+  }
+  if (M.tcoef_df) return ref_elem_newton_df_lin(M, e, x, xi, start);
+  if (start) newton_start(M, e, x, xi);
+  return ref_elem_newton_lin(M, e, x, xi);
 }
 
 template <bool FAST>
 __device__ __forceinline__ bool position_in_ref_elem_t(const DevMesh& M, int e, const double x[3], double xi[3]) {
+  if (FAST && M.k.ref_guess == 1) return ref_elem_newton_fast(M, e, x, xi, true);
   newton_start(M, e, x, xi);
-  return FAST ? ref_elem_newton_fast(M, e, x, xi) : ref_elem_newton(M, e, x, xi);
+  return FAST ? ref_elem_newton_fast(M, e, x, xi, false) : ref_elem_newton(M, e, x, xi);
 }
 
 // ==========================================================================================
