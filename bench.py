@@ -474,6 +474,9 @@ def run_gpu(args, rank, world, local_rank):
         roof = {"kernel": kname, "bound": comp["bound"], "achieved": comp["achieved"], "peak": comp["peak"],
                 "unit": comp["unit"], "frac": comp["frac"], "traffic": traffic, "peak_kind": comp["peak_kind"],
                 "avg_launch_ms": avg_ms, "share": share, "hbm": hbm}
+        for extra in ("ncu_16cube", "note"):
+            if extra in comp:
+                roof[extra] = comp[extra]
     else:
         roof = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind, "avg_launch_ms": avg_ms,
