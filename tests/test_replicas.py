@@ -60,11 +60,12 @@ def test_reference_arm_reports_the_gpu_arms_config():
     from piclas_gb300 import workloads
     from piclas_gb300.mesh import build_box_mesh
     from piclas_gb300.mesh import p_adaption_degrees
-    cases = (("curved", 32, 16_000_000, 1, None, False), ("plasma_wave", 8, 200_000, 1, None, False),
-             ("curved", 32, 16_000_000, 2, None, True), ("curved", 32, 16_000_000, 1, "random", False))
-    for name, cells, n, ngeo, padapt, ptrace in cases:
+    cases = (("curved", 32, 16_000_000, 1, None, False, None, 0.0), ("plasma_wave", 8, 200_000, 1, None, False, None, 0.0),
+             ("curved", 32, 16_000_000, 2, None, True, None, 0.0), ("curved", 32, 16_000_000, 1, "random", False, None, 0.0),
+             ("curved", 32, 16_000_000, 2, None, False, "reflective", 0.2))
+    for name, cells, n, ngeo, padapt, ptrace, walls, bulge in cases:
         args = argparse.Namespace(workload=name, precision="fp64", gpus=1, ngeo=ngeo, p_adaption=padapt,
-                                  periodic_tracing=ptrace, walls=None, wall_bulge=0.0)
+                                  periodic_tracing=ptrace, walls=walls, wall_bulge=bulge)
         ref = bench.reference_config(args)
         mesh = build_box_mesh(2, 2, 2, 3)
         stand_in = workloads.Workload(**{**workloads.plasma_wave(mesh=mesh, n_particles=10).__dict__})
@@ -74,5 +75,6 @@ def test_reference_arm_reports_the_gpu_arms_config():
                                        "n_dofs": n_dofs})()
         stand_in.part_state = type("P", (), {"shape": (n, 6)})()
         stand_in.periodic_tracing = ptrace
+        stand_in.walls, stand_in.wall_bulge = walls, bulge
         gpu = dict(bench.workload_config(stand_in, name), precision="fp64", parallelism="replicas x1")
         assert ref == gpu
