@@ -912,11 +912,12 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
         for (int q = 0; q < 8; ++q)
           for (int k = 0; k < 3; ++k) tc[(size_t)e * 24 + 3 * q + k] += 0.125 * w[q] * xcl[(size_t)e * 24 + 3 * t + k];
       }
-    // the same coefficients over s_e = 2^round(log2 max|c1..c3|) as double-FP32 pairs, then (s_e, 1/s_e) and the
-    // start-value data of RefMappingGuess 1 in the same units (bary / s_e, XiEtaZetaBasis, slen s_e)
+    // the same coefficients relative to the element's barycentre (c0 - bary) over s_e = 2^round(log2 max|c1..c3|)
+    // as double-FP32 pairs, then (s_e, 1/s_e) and the start-value data of RefMappingGuess 1 in the same frame and
+    // units (bary - bary = 0, XiEtaZetaBasis, slen s_e): every value O(1) wherever the element lies
     auto pair = [](double v) { const float hi = (float)v; return make_float2(hi, (float)(v - (double)hi)); };
     auto start_data = [&](int e, double sc, float2* out) {
-      for (int d = 0; d < 3; ++d) out[d] = pair(bary[(size_t)e * 3 + d] / sc);
+      for (int d = 0; d < 3; ++d) out[d] = make_float2(0.f, 0.f);
       for (int d = 0; d < 18; ++d) out[3 + d] = pair(xez[(size_t)e * 18 + d]);
       for (int d = 0; d < 6; ++d) out[21 + d] = pair(slen[(size_t)e * 6 + d] * sc);
     };
@@ -926,7 +927,8 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
       for (int q = 1; q <= 3; ++q)
         for (int k = 0; k < 3; ++k) mx = std::max(mx, std::fabs(tc[(size_t)e * 24 + 3 * q + k]));
       const double sc = mx > 0.0 ? std::ldexp(1.0, (int)std::lround(std::log2(mx))) : 1.0;
-      for (int j = 0; j < 24; ++j) tdf[(size_t)e * pic::kDfLin + j] = pair(tc[(size_t)e * 24 + j] / sc);
+      for (int j = 0; j < 24; ++j)
+        tdf[(size_t)e * pic::kDfLin + j] = pair((j < 3 ? tc[(size_t)e * 24 + j] - bary[(size_t)e * 3 + j] : tc[(size_t)e * 24 + j]) / sc);
       tdf[(size_t)e * pic::kDfLin + 24] = make_float2((float)sc, (float)(1.0 / sc));
       start_data(e, sc, &tdf[(size_t)e * pic::kDfLin + 25]);
     }
@@ -976,7 +978,8 @@ int pic_create(const pic_config_t* cfg, const pic_mesh_t* m, pic_ctx_t** out) {
         for (int a = 0; a < 3; ++a)
           for (int k = 0; k < 3; ++k) mx = std::max(mx, std::fabs(pc[((size_t)e * g3 + first[a]) * 3 + k]));
         const double sc = mx > 0.0 ? std::ldexp(1.0, (int)std::lround(std::log2(mx))) : 1.0;
-        for (size_t j = 0; j < g3 * 3; ++j) pdf[(size_t)e * nb + j] = pair(pc[(size_t)e * g3 * 3 + j] / sc);
+        for (size_t j = 0; j < g3 * 3; ++j)   // j < 3: the constant term, relative to the barycentre
+          pdf[(size_t)e * nb + j] = pair((j < 3 ? pc[(size_t)e * g3 * 3 + j] - bary[(size_t)e * 3 + j] : pc[(size_t)e * g3 * 3 + j]) / sc);
         pdf[(size_t)e * nb + g3 * 3] = make_float2((float)sc, (float)(1.0 / sc));
         start_data(e, sc, &pdf[(size_t)e * nb + g3 * 3 + 1]);
       }

@@ -106,14 +106,16 @@ struct DevMesh {
   const double* dxcl_ng;
   const int* curved;
   // mixed variant: the NGeo = 1 map in monomial form, x(xi) = c0 + c1 xi1 + c2 xi2 + c3 xi3 + c12 xi1 xi2
-  // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3 (from the corners at pic_create), divided by s_e, the power of
-  // two nearest the element's size (exact; the scaled map is O(1), far from the FP32 range limits), as double-FP32
-  // pairs (hi, lo) for the Newton in double-FP32 arithmetic: [ne][kDfLin], 24 coefficients, (s_e, 1/s_e), then the
-  // start-value data of RefMappingGuess 1 in the same units: ElemBaryNGeo / s_e (3), XiEtaZetaBasis (18),
+  // + c13 xi1 xi3 + c23 xi2 xi3 + c123 xi1 xi2 xi3 (from the corners at pic_create), relative to the element's
+  // barycentre (c0 - bary) and divided by s_e, the power of two nearest the element's size (exact; the map is O(1)
+  // wherever the element lies, far from the FP32 range limits), as double-FP32 pairs (hi, lo) for the Newton in
+  // double-FP32 arithmetic: [ne][kDfLin], 24 coefficients, (s_e, 1/s_e), then the start-value data of
+  // RefMappingGuess 1 in the same frame and units: the barycentre (0, 0, 0), XiEtaZetaBasis (18),
   // slenXiEtaZetaBasis s_e (6)
   const float2* tcoef_df;
-  // curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c, over s_e the same way,
-  // [ne][(NGeo+1)^3 3 + 1 + 27] in that index order, then (s_e, 1/s_e) and the start-value data
+  // curved elements: the NGeo map in power form, x(xi) = sum C[c][b][a] xi1^a xi2^b xi3^c, the same way (constant
+  // term relative to the barycentre, over s_e), [ne][(NGeo+1)^3 3 + 1 + 27] in that index order, then (s_e, 1/s_e)
+  // and the start-value data
   const float2* tcoef_ng_df;
   // run-time constants of the context; kernels take DevMesh as a __grid_constant__ parameter, so these are
   // read from the launch's parameter bank (each launch carries its own context's copy)
@@ -497,7 +499,9 @@ __device__ __forceinline__ bool ref_elem_newton_df_lin(const DevMesh& M, int e, 
 #pragma unroll
     for (int k = 0; k < 3; ++k) c[q][k] = df_ld(Cg + 3 * q + k);
   const float2 sc = __ldg(Cg + 24);
-  const DF xs[3] = {df_of(x[0] * (double)sc.y), df_of(x[1] * (double)sc.y), df_of(x[2] * (double)sc.y)};
+  const double* by = M.bary + (size_t)e * 3;       // the map is stored relative to the barycentre
+  const DF xs[3] = {df_of((x[0] - __ldg(by)) * (double)sc.y), df_of((x[1] - __ldg(by + 1)) * (double)sc.y),
+                    df_of((x[2] - __ldg(by + 2)) * (double)sc.y)};
 #pragma unroll
   for (int k = 0; k < 3; ++k) c[0][k] = df_add(c[0][k], df_neg(xs[k]));
   auto residual = [&](const DF z[3], DF F[3]) {
@@ -688,7 +692,9 @@ static __device__ __noinline__ bool ref_elem_newton_df_ng(const DevMesh& M, int 
   constexpr int n1 = NG + 1, n3 = n1 * n1 * n1;
   const float2* Cg = M.tcoef_ng_df + (size_t)e * (n3 * 3 + 1 + kDfStart);
   const float2 sc = __ldg(Cg + n3 * 3);
-  const DF xs[3] = {df_of(x[0] * (double)sc.y), df_of(x[1] * (double)sc.y), df_of(x[2] * (double)sc.y)};
+  const double* by = M.bary + (size_t)e * 3;       // the map is stored relative to the barycentre
+  const DF xs[3] = {df_of((x[0] - __ldg(by)) * (double)sc.y), df_of((x[1] - __ldg(by + 1)) * (double)sc.y),
+                    df_of((x[2] - __ldg(by + 2)) * (double)sc.y)};
   DF z[3];
   if (start) df_start(kc, Cg + n3 * 3 + 1, xs, z);
   else { z[0] = df_of(xi[0]); z[1] = df_of(xi[1]); z[2] = df_of(xi[2]); }

@@ -1461,3 +1461,19 @@ def test_sf_gather_moments_against_oracle(gpu_lib, oracle_lib, N, radius_cells):
     assert np.array_equal(g["elem"], st.elem)
     assert _rel(g["PS"], PS) <= 1e-12
     assert g["status"]["error_word"] == 0
+
+
+def test_mixed_newton_far_from_origin(gpu_lib, oracle_lib):
+    """The mixed Newton works in double-FP32 on each element's map relative to its barycentre: on a box 1000 m from
+    the origin (h = 1/8 m) 20 mixed steps keep the FP64 run's element ids but two, and PartPosRef equals the
+    reference Newton (oracle) at the mixed run's own positions within 1e-10."""
+    mesh = build_box_mesh(8, 8, 8, 3, lo=(1000.0, -500.0, 250.0), hi=(1001.0, -499.0, 251.0), perturb=0.08)
+    w = workloads.curved_two_species(mesh=mesh, n_per_species=20_000, seed=83, nsteps=20, Te_eV=1000.0)
+    w.dt *= 5.0
+    g64 = _run_gpu(w, 20)
+    g32 = _run_gpu(w, 20, precision=capi.PIC_PREC_MIXED)
+    assert (g32["elem"] != g64["elem"]).sum() <= 2
+    assert g32["status"]["error_word"] == 0 and (g64["elem"] != w.elem).sum() > 100
+    st = oracle_lib.OracleState(g32["part_state"], g32["elem"], w.part_species)
+    oracle_lib.map_particles(w.config(), capi.MeshStruct(w.mesh), st)
+    assert np.max(np.abs(g32["part_pos_ref"] - st.part_pos_ref)) <= 1e-10
