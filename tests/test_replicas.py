@@ -78,3 +78,14 @@ def test_reference_arm_reports_the_gpu_arms_config():
         stand_in.walls, stand_in.wall_bulge = walls, bulge
         gpu = dict(bench.workload_config(stand_in, name), precision="fp64", parallelism="replicas x1")
         assert ref == gpu
+
+
+def test_bench_reads_the_committed_ncu_figures():
+    """The bench line's roofline takes DRAM traffic, issue and FP64-pipe figures from the committed ncu summary:
+    the keys it builds must be present there (a renamed kernel or row would silently drop them)."""
+    import bench
+    assert bench.read_traffic("k_sf_gather5<3,0,0,1> @ curved") > 1e9
+    assert bench.read_traffic("k_sf_gather7<1> @ curved") > 1e8
+    assert bench.read_ncu_summary("k_sf_gather7<1> @ 16^3 curved, 2M particles")["inst_per_hit"] > 0
+    fp64 = bench.read_ncu_fp64("k_sf_gather5<3,0,0,1> @ 16^3 curved, 2M particles")
+    assert 0 < fp64["fp64_pipe_busy_pct"] <= 100 and 0 < fp64["lanes_active_of_32"] <= 32
